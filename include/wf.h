@@ -1,0 +1,192 @@
+/*
+ * wf.h — C ABI of the GB300 wavefront path tracer.
+ *
+ * The entry points replace the reference renderer's front end for its hot
+ * path (source/renderer/renderer.h:13-55, renderer.cpp:632-1049) and its two
+ * acceleration-structure builders (source/renderer/bvh/bvh_builder.h:32-33,
+ * tlas_builder.h:17-18).  Data crosses the boundary in the reference's own
+ * layouts (wf_shared.h).  Conventions:
+ *   - every call returns an int status: WF_OK (0) or a negative WF_ERR_*;
+ *     nothing aborts the process (the reference aborts through ASSERT_MSG /
+ *     FATAL_ERROR, source/core/assertion.h:51-67);
+ *   - a wf_ctx owns one CUDA device, one stream and all device memory; one
+ *     context must not be used from two threads at once, separate contexts may;
+ *   - host pointers are plain host memory unless the name says "device";
+ *   - wf_last_error() returns a message for the calling thread's last failure.
+ */
+#ifndef WF_H
+#define WF_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "wf_shared.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WF_ABI_VERSION 1
+
+enum wf_status {
+    WF_OK = 0,
+    WF_ERR_INVALID = -1,   /* bad argument: null pointer, size, unknown handle */
+    WF_ERR_OOM = -2,       /* a device or pinned-host allocation failed */
+    WF_ERR_CAPACITY = -3,  /* a fixed capacity was exceeded (instances, output size) */
+    WF_ERR_TIMEOUT = -4,   /* a bounded device wait gave up */
+    WF_ERR_STACK = -5,     /* a traversal stack overflowed (the ray was abandoned) */
+    WF_ERR_CUDA = -6,      /* a CUDA runtime call failed */
+    WF_ERR_STATE = -7      /* call out of order (e.g. render before scene_end) */
+};
+
+typedef struct wf_ctx wf_ctx;
+
+/* renderer::init_params_t (renderer.h:15-21) plus device-side options. */
+typedef struct wf_init_params {
+    uint32_t render_width;
+    uint32_t render_height;
+    uint32_t backbuffer_count;  /* accepted for source compatibility; unused (headless) */
+    uint32_t vsync;             /* accepted for source compatibility; unused */
+    int32_t  device;            /* CUDA device ordinal */
+    uint32_t wave_capacity;     /* max paths per wave; 0 = render_width*render_height */
+    uint32_t reserved[2];
+} wf_init_params;
+
+/* bvh_builder_t::build_options_t (bvh_builder.h:13-17) plus max_leaf_prims:
+ * 0 keeps the reference's rule (stop when the best split is not cheaper);
+ * k > 0 also forces a split of any node holding more than k triangles. */
+typedef struct wf_bvh_options {
+    uint32_t interval_count;        /* SAH bins per axis (reference renderer: 8) */
+    uint32_t subdivide_single_prim; /* split down to one triangle per leaf */
+    uint32_t max_leaf_prims;
+} wf_bvh_options;
+
+/* Scattering models.  The reference shades Lambert only (shade.hlsl:107-137);
+ * metal and dielectric are additions. */
+enum wf_bsdf_type {
+    WF_BSDF_LAMBERT = 0,
+    WF_BSDF_METAL = 1,       /* GGX conductor, alpha = roughness^2, F0 = base colour */
+    WF_BSDF_DIELECTRIC = 2   /* smooth glass, exact Fresnel, index of refraction ior */
+};
+
+typedef struct wf_material_ext {
+    material_t base;
+    uint32_t   bsdf;   /* enum wf_bsdf_type */
+    float      ior;    /* dielectric only */
+} wf_material_ext;
+
+/* Constant environment radiance seen by rays that miss (the reference's
+ * default environment is a 1x1 white texture, renderer.cpp:608-611). */
+typedef struct wf_env {
+    float color[3];
+} wf_env;
+
+/* Options of one wf_render call beyond render_settings_t. */
+typedef struct wf_render_options {
+    uint32_t spp;            /* samples per pixel rendered by this call (>= 1) */
+    uint32_t nee;            /* 1 = next-event estimation with shadow rays (connect stage) */
+    uint32_t rr_start_depth; /* Russian roulette from this depth; 0xFFFFFFFF = off */
+    uint32_t wave_paths;     /* paths per wave, <= context capacity; 0 = capacity */
+    uint32_t profile;        /* 1 = time every stage with CUDA events (wf_get_stats) */
+    uint32_t count_traffic;  /* 1 = count node/instance/triangle fetches (slower) */
+    uint32_t reserved[2];
+} wf_render_options;
+
+enum wf_trace_flags {
+    WF_TRACE_ANY_HIT = 1u,   /* stop at the first accepted hit (shadow-ray query) */
+    WF_TRACE_NO_CULL = 2u    /* accept back-facing triangles (|det| test) */
+};
+
+/* Counters and timings of the most recent wf_render / wf_trace call. */
+typedef struct wf_stats {
+    double   ms_total;       /* GPU time of the whole call (CUDA events) */
+    double   ms_generate, ms_extend, ms_shade, ms_connect, ms_post, ms_tlas_build;
+    uint64_t launches;       /* kernels this library launched */
+    uint64_t launches_extend, launches_connect;
+    uint64_t rays_extend;    /* closest-hit rays traced */
+    uint64_t rays_connect;   /* shadow rays traced */
+    uint64_t paths;          /* camera paths started */
+    /* count_traffic = 1 only: fetches made by the traversal kernels */
+    uint64_t tlas_node_loads, instance_loads, blas_node_loads, triangle_tests;
+    uint64_t shadow_tlas_node_loads, shadow_instance_loads, shadow_blas_node_loads, shadow_triangle_tests;
+} wf_stats;
+
+/* ---- lifetime (renderer::init / exit, renderer.h:23-24) ------------------ */
+int wf_create(const wf_init_params* params, wf_ctx** out_ctx);
+int wf_destroy(wf_ctx* ctx);
+const char* wf_status_string(int status);
+const char* wf_last_error(void);
+int wf_abi_version(void);
+/* The context's cudaStream_t, for callers that time or order work around it. */
+int wf_get_stream(wf_ctx* ctx, void** out_stream);
+/* Waits for the context's stream; reports a device-side error flag if set. */
+int wf_synchronize(wf_ctx* ctx);
+
+/* ---- meshes (renderer::create_render_mesh, renderer.cpp:1246-1281) ------- */
+/* De-indexes (vertices, indices) into triangle_t, uploads it and builds the
+ * mesh's BLAS on the GPU with `opts` (NULL = reference defaults: 8 bins). */
+int wf_mesh_create(wf_ctx* ctx, const vertex_t* vertices, uint32_t vertex_count,
+                   const uint32_t* indices, uint32_t index_count,
+                   const wf_bvh_options* opts, uint32_t* out_mesh);
+/* Same, but uploads a BLAS blob built elsewhere ([bvh_header_t | extract()],
+ * the buffer renderer.cpp:113-155 uploads) instead of building one. */
+int wf_mesh_create_prebuilt(wf_ctx* ctx, const triangle_t* triangles, uint32_t triangle_count,
+                            const void* blas_blob, uint64_t blob_size, uint32_t* out_mesh);
+/* Copies the mesh's BLAS blob ([bvh_header_t | nodes | bvh_triangle_t | uint32 index]). */
+int wf_mesh_get_blas(wf_ctx* ctx, uint32_t mesh, void* out_blob, uint64_t* inout_size);
+
+/* ---- scene (renderer::begin_scene / submit_render_mesh / end_scene) ------ */
+/* begin_scene (renderer.cpp:599-630): sets the view, clears the instance list,
+ * and resets accumulation when the view changed. env may be NULL (white). */
+int wf_scene_begin(wf_ctx* ctx, const view_t* view, const wf_env* env);
+/* submit_render_mesh (renderer.cpp:1283-1350): local_to_world is a glm
+ * column-major mat4; world_to_local is its inverse. Lambert BSDF. */
+int wf_instance_submit(wf_ctx* ctx, uint32_t mesh, const float local_to_world[16],
+                       const material_t* material);
+/* Same with a chosen scattering model (metal, dielectric). */
+int wf_instance_submit_ex(wf_ctx* ctx, uint32_t mesh, const float local_to_world[16],
+                          const wf_material_ext* material);
+/* Uploads instances, builds the TLAS on the GPU (renderer.cpp:637-669 builds
+ * it on the CPU every frame) and the emitter table used by next-event estimation. */
+int wf_scene_end(wf_ctx* ctx);
+/* The scene's bvh_instance_t array (world_to_local, world AABB, mesh id). */
+int wf_scene_get_instances(wf_ctx* ctx, bvh_instance_t* out, uint32_t capacity, uint32_t* out_count);
+/* The scene's TLAS blob ([tlas_header_t | nodes | bvh_instance_t]). */
+int wf_scene_get_tlas(wf_ctx* ctx, void* out_blob, uint64_t* inout_size);
+
+/* ---- rendering (renderer::render, renderer.cpp:742-939 + post_process) --- */
+/* Renders opts->spp samples per pixel through generate -> extend -> shade ->
+ * connect for depth 0..settings->max_bounces, adding them to the accumulator
+ * (or replacing it when settings->accumulate == 0).  Asynchronous: errors
+ * detected on the device are reported by the next synchronizing call. */
+int wf_render(wf_ctx* ctx, const render_settings_t* settings,
+              const wf_render_options* opts, uint32_t frame_seed);
+/* Average radiance per pixel, RGBA float32 (alpha = samples), row-major, row 0 = top. */
+int wf_read_image(wf_ctx* ctx, float* out_rgba, uint64_t float_count);
+/* post_process.hlsl:25-72: NaN/Inf flag, Reinhard, linear->sRGB, RGBA8. */
+int wf_read_image_ldr(wf_ctx* ctx, uint8_t* out_rgba8, uint64_t byte_count);
+int wf_get_stats(wf_ctx* ctx, wf_stats* out);
+
+/* ---- ray queries (extend.hlsl / accelstruct.hlsl:151-218) ---------------- */
+/* Traces host rays against the current scene; copies in, traces, copies out. */
+int wf_trace(wf_ctx* ctx, const RayDesc2* rays, uint32_t count, hit_result_t* hits, uint32_t flags);
+/* Same on device buffers already resident on the context's device; enqueued
+ * on the context stream (no synchronization). */
+int wf_trace_device(wf_ctx* ctx, const RayDesc2* device_rays, uint32_t count,
+                    hit_result_t* device_hits, uint32_t flags);
+
+/* ---- stand-alone builders (bvh_builder_t / tlas_builder_t) --------------- */
+/* Builds a BLAS on the GPU; writes [bvh_header_t | extract()] byte-identical to
+ * the reference builder's output at equal options.  *inout_size: capacity in,
+ * bytes written out (WF_ERR_CAPACITY with the needed size if too small). */
+int wf_bvh_build(wf_ctx* ctx, const triangle_t* triangles, uint32_t triangle_count,
+                 const wf_bvh_options* opts, void* out_blob, uint64_t* inout_size);
+/* Builds a TLAS on the GPU; writes [tlas_header_t | extract()] byte-identical
+ * to tlas_builder_t.  Up to 32768 instances (16-bit child indices). */
+int wf_tlas_build(wf_ctx* ctx, const bvh_instance_t* instances, uint32_t instance_count,
+                  void* out_blob, uint64_t* inout_size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WF_H */

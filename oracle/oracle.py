@@ -1,0 +1,231 @@
+"""ctypes wrapper of the CPU oracle (oracle/_build/liborc.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, bench.py's CPU-baseline leg and
+__graft_entry__.smoke() as the checker.  The product (the GPU library) never
+imports it.  The optional reference library oracle/_ref/libref_bvh.so (the
+reference's own builders, built by oracle/build_ref.sh where the reference
+checkout exists) pins the builder restatement.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from wavefrontpathtracing_gb300.abi import (INVALID, bvh_instance_dtype, hit_dtype, material_dtype, ptr, ray_dtype,
+                                            triangle_dtype, View)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref_bvh.so")
+
+instance_dtype = np.dtype([("local_to_world", "<f4", 16), ("world_to_local", "<f4", 16),
+                           ("material", material_dtype), ("mesh", "<u4"), ("bsdf", "<u4"), ("ior", "<f4")])
+assert instance_dtype.itemsize == 192
+
+ANY_HIT, NO_CULL = 1, 2
+
+
+class _Mesh(ctypes.Structure):
+    _fields_ = [("tris", ctypes.c_void_p), ("tri_count", ctypes.c_uint32), ("blas", ctypes.c_void_p)]
+
+
+class _Scene(ctypes.Structure):
+    _fields_ = [("meshes", ctypes.POINTER(_Mesh)), ("mesh_count", ctypes.c_uint32), ("tlas", ctypes.c_void_p),
+                ("inst", ctypes.c_void_p), ("inst_count", ctypes.c_uint32)]
+
+
+class Counters(ctypes.Structure):
+    _fields_ = [("tlas_node_loads", ctypes.c_uint64), ("instance_loads", ctypes.c_uint64),
+                ("blas_node_loads", ctypes.c_uint64), ("triangle_tests", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class RenderParams(ctypes.Structure):
+    _fields_ = [("max_bounces", ctypes.c_uint32), ("cosine_weighted_diffuse", ctypes.c_uint32),
+                ("hdr_env_strength", ctypes.c_float), ("env_color", ctypes.c_float * 3),
+                ("spp", ctypes.c_uint32), ("sample_offset", ctypes.c_uint32), ("nee", ctypes.c_uint32),
+                ("rr_start_depth", ctypes.c_uint32), ("frame_seed", ctypes.c_uint32),
+                ("pixel_begin", ctypes.c_uint32), ("pixel_end", ctypes.c_uint32)]
+
+
+class RenderStats(ctypes.Structure):
+    _fields_ = [("extend_rays", ctypes.c_uint64 * 16), ("shadow_rays", ctypes.c_uint64 * 16),
+                ("stack_overflows", ctypes.c_uint64), ("extend_traffic", Counters), ("shadow_traffic", Counters)]
+
+
+_lib = None
+_ref = None
+
+
+def build():
+    """Compiles liborc.so with the oracle's Makefile (gcc -O2 -ffp-contract=off)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
+        L.orc_bvh_build.argtypes = [vp, u32, u32, u32, u32, ctypes.POINTER(ctypes.c_void_p),
+                                    ctypes.POINTER(ctypes.c_uint64)]
+        L.orc_tlas_build.argtypes = [vp, u32, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)]
+        L.orc_free.argtypes = [vp]
+        L.orc_trace.argtypes = [ctypes.POINTER(_Scene), vp, u32, vp, u32, ctypes.POINTER(Counters), i32]
+        L.orc_trace.restype = u32
+        L.orc_trace_f64.argtypes = [ctypes.POINTER(_Scene), vp, u32, vp, u32, i32]
+        L.orc_trace_f64.restype = u32
+        L.orc_render.argtypes = [ctypes.POINTER(_Scene), ctypes.POINTER(View), ctypes.POINTER(RenderParams), vp,
+                                 ctypes.POINTER(RenderStats), i32]
+        L.orc_render_f64.argtypes = [ctypes.POINTER(_Scene), ctypes.POINTER(View), ctypes.POINTER(RenderParams),
+                                     vp, i32]
+        L.orc_wang_hash.argtypes = [u32]
+        L.orc_wang_hash.restype = u32
+        L.orc_rand_float.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+        L.orc_rand_float.restype = ctypes.c_float
+        L.orc_path_seed.argtypes = [u32, u32, u32, u32]
+        L.orc_path_seed.restype = u32
+        L.orc_sincos_2pi.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+        L.orc_intersect_triangle.argtypes = [vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_float), vp, i32]
+        L.orc_intersect_aabb.argtypes = [vp, vp, vp, vp, ctypes.c_float]
+        L.orc_intersect_aabb.restype = ctypes.c_float
+        L.orc_primary_ray.argtypes = [ctypes.POINTER(View), u32, u32, vp]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own builders, or None where they were not compiled."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        R = ctypes.CDLL(REF_PATH)
+        vp, u32 = ctypes.c_void_p, ctypes.c_uint32
+        R.ref_bvh_build.argtypes = [vp, u32, u32, u32, vp, ctypes.POINTER(ctypes.c_uint64)]
+        R.ref_tlas_build.argtypes = [vp, u32, vp, ctypes.POINTER(ctypes.c_uint64)]
+        _ref = R
+    return _ref
+
+
+def _blob(fn, *args):
+    p = ctypes.c_void_p()
+    n = ctypes.c_uint64()
+    rc = fn(*args, ctypes.byref(p), ctypes.byref(n))
+    if rc != 0:
+        raise ValueError(f"oracle builder failed ({rc})")
+    out = np.frombuffer(ctypes.string_at(p, n.value), dtype=np.uint8).copy()
+    lib().orc_free(p)
+    return out
+
+
+def bvh_build(tris, interval_count=8, subdivide_single_prim=False, max_leaf_prims=0):
+    tris = np.ascontiguousarray(tris, dtype=triangle_dtype)
+    return _blob(lib().orc_bvh_build, ptr(tris), len(tris), interval_count, int(subdivide_single_prim),
+                 max_leaf_prims)
+
+
+def tlas_build(instances):
+    instances = np.ascontiguousarray(instances, dtype=bvh_instance_dtype)
+    return _blob(lib().orc_tlas_build, ptr(instances), len(instances))
+
+
+def ref_bvh_build(tris, interval_count=8, subdivide_single_prim=False):
+    R = ref_lib()
+    tris = np.ascontiguousarray(tris, dtype=triangle_dtype)
+    n = ctypes.c_uint64(0)
+    R.ref_bvh_build(ptr(tris), len(tris), interval_count, int(subdivide_single_prim), None, ctypes.byref(n))
+    out = np.zeros(n.value, dtype=np.uint8)
+    rc = R.ref_bvh_build(ptr(tris), len(tris), interval_count, int(subdivide_single_prim), ptr(out),
+                         ctypes.byref(n))
+    assert rc == 0
+    return out
+
+
+def ref_tlas_build(instances):
+    R = ref_lib()
+    instances = np.ascontiguousarray(instances, dtype=bvh_instance_dtype)
+    n = ctypes.c_uint64(0)
+    R.ref_tlas_build(ptr(instances), len(instances), None, ctypes.byref(n))
+    out = np.zeros(n.value, dtype=np.uint8)
+    rc = R.ref_tlas_build(ptr(instances), len(instances), ptr(out), ctypes.byref(n))
+    assert rc == 0
+    return out
+
+
+class Scene:
+    """An oracle scene: meshes (triangles + BLAS blobs), a TLAS blob and the
+    per-instance shading data.  Keeps every array alive for the C side."""
+
+    def __init__(self, meshes, tlas, instances):
+        # meshes: list of (triangles ndarray[triangle_dtype], blas blob uint8)
+        self._tris = [np.ascontiguousarray(t, dtype=triangle_dtype) for t, _ in meshes]
+        self._blas = [np.ascontiguousarray(b, dtype=np.uint8) for _, b in meshes]
+        self._tlas = np.ascontiguousarray(tlas, dtype=np.uint8)
+        self._inst = np.ascontiguousarray(instances, dtype=instance_dtype)
+        arr = (_Mesh * max(1, len(meshes)))()
+        for i, (t, b) in enumerate(zip(self._tris, self._blas)):
+            arr[i].tris = t.ctypes.data
+            arr[i].tri_count = len(t)
+            arr[i].blas = b.ctypes.data
+        self._meshes = arr
+        self.c = _Scene(arr, len(meshes), self._tlas.ctypes.data, self._inst.ctypes.data if len(self._inst) else None,
+                        len(self._inst))
+
+    def trace(self, rays, flags=0, threads=1, f64=False):
+        rays = np.ascontiguousarray(rays, dtype=ray_dtype)
+        hits = np.zeros(len(rays), dtype=hit_dtype)
+        cnt = Counters()
+        if f64:
+            ovf = lib().orc_trace_f64(ctypes.byref(self.c), ptr(rays), len(rays), ptr(hits), flags, threads)
+        else:
+            ovf = lib().orc_trace(ctypes.byref(self.c), ptr(rays), len(rays), ptr(hits), flags, ctypes.byref(cnt),
+                                  threads)
+        return hits, cnt.as_dict(), int(ovf)
+
+    def render(self, view, width, height, max_bounces=4, spp=1, frame_seed=1, nee=0, rr_start_depth=0xFFFFFFFF,
+               env_color=(0.0, 0.0, 0.0), env_strength=1.0, cosine=1, sample_offset=0, threads=1, f64=False,
+               pixel_range=None, accum=None):
+        p = RenderParams()
+        p.max_bounces, p.cosine_weighted_diffuse, p.hdr_env_strength = max_bounces, cosine, env_strength
+        p.env_color[:] = env_color
+        p.spp, p.sample_offset, p.nee, p.rr_start_depth, p.frame_seed = spp, sample_offset, nee, rr_start_depth, \
+            frame_seed
+        if pixel_range:
+            p.pixel_begin, p.pixel_end = pixel_range
+        if accum is None:
+            accum = np.zeros((height, width, 4), dtype=np.float64 if f64 else np.float32)
+        st = RenderStats()
+        if f64:
+            rc = lib().orc_render_f64(ctypes.byref(self.c), ctypes.byref(view), ctypes.byref(p), ptr(accum), threads)
+        else:
+            rc = lib().orc_render(ctypes.byref(self.c), ctypes.byref(view), ctypes.byref(p), ptr(accum),
+                                  ctypes.byref(st), threads)
+        if rc != 0:
+            raise ValueError("oracle render failed")
+        stats = {"extend_rays": list(st.extend_rays), "shadow_rays": list(st.shadow_rays),
+                 "stack_overflows": st.stack_overflows, "extend_traffic": st.extend_traffic.as_dict(),
+                 "shadow_traffic": st.shadow_traffic.as_dict()}
+        return accum, stats
+
+
+def primary_rays(view, width, height):
+    """All primary rays of an image, row-major (orc_primary_ray per pixel)."""
+    L = lib()
+    out = np.zeros(width * height, dtype=ray_dtype)
+    one = np.zeros(1, dtype=ray_dtype)
+    for y in range(height):
+        for x in range(width):
+            L.orc_primary_ray(ctypes.byref(view), x, y, ptr(one))
+            out[y * width + x] = one[0]
+    return out
+
+
+def miss_hit():
+    h = np.zeros(1, dtype=hit_dtype)
+    h["instance"] = INVALID
+    h["primitive"] = INVALID
+    return h

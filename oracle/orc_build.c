@@ -1,0 +1,304 @@
+/*
+ * orc_build.c — oracle restatement of the reference's CPU acceleration-
+ * structure builders.  TEST INFRASTRUCTURE ONLY (see wf_oracle.h).
+ *
+ * BLAS: binned-SAH builder, bvh_builder.cpp:6-264 with as_util.h:7-23.
+ * TLAS: agglomerative builder, tlas_builder.cpp:6-110.
+ *
+ * min/max follow glm 1.0.0 (extern/glm/detail/func_common.inl:17-35):
+ * min(x, y) = (y < x) ? y : x and max(x, y) = (x < y) ? y : x, folded in the
+ * same order as the reference so that even the sign of a zero bound matches.
+ */
+#include <float.h>
+#include <stdlib.h>
+#include <string.h>
+#include "wf_oracle.h"
+
+static inline float gmin(float x, float y) { return (y < x) ? y : x; }
+static inline float gmax(float x, float y) { return (x < y) ? y : x; }
+
+typedef struct { float v[3]; } f3;
+
+/* as_util::get_aabb_volume (as_util.h:7-11): the half surface area. */
+static inline float half_area(const float* mn, const float* mx) {
+    float ex = mx[0] - mn[0], ey = mx[1] - mn[1], ez = mx[2] - mn[2];
+    return ex * ey + ey * ez + ez * ex;
+}
+
+typedef struct {
+    uint32_t interval_count, subdivide_single_prim, max_leaf_prims;
+    uint32_t n;
+    bvh_triangle_t* tris;
+    uint32_t* idx;
+    f3* centroid;
+    bvh_node_t* nodes;
+    uint32_t node_at;
+    /* per-call bin scratch */
+    float* bmin; float* bmax; uint32_t* bcnt; float* larea; float* rarea;
+} builder;
+
+/* get_triangle_centroid (bvh_builder.cpp:252-255): (p0 + p1 + p2) * 0.3333f. */
+static f3 centroid_of(const bvh_triangle_t* t) {
+    f3 c;
+    for (int a = 0; a < 3; ++a) c.v[a] = ((t->p0[a] + t->p1[a]) + t->p2[a]) * 0.3333f;
+    return c;
+}
+
+/* calc_node_min_max (bvh_builder.cpp:71-93). */
+static void node_bounds(builder* b, bvh_node_t* node, float* cmin, float* cmax) {
+    for (int a = 0; a < 3; ++a) {
+        node->aabb_min[a] = FLT_MAX; node->aabb_max[a] = -FLT_MAX;
+        cmin[a] = FLT_MAX; cmax[a] = -FLT_MAX;
+    }
+    for (uint32_t i = node->left_first; i < node->left_first + node->prim_count; ++i) {
+        const bvh_triangle_t* t = &b->tris[b->idx[i]];
+        const f3* c = &b->centroid[b->idx[i]];
+        for (int a = 0; a < 3; ++a) {
+            float tmn = gmin(gmin(t->p0[a], t->p1[a]), t->p2[a]);
+            float tmx = gmax(gmax(t->p0[a], t->p1[a]), t->p2[a]);
+            node->aabb_min[a] = gmin(node->aabb_min[a], tmn);
+            node->aabb_max[a] = gmax(node->aabb_max[a], tmx);
+            cmin[a] = gmin(cmin[a], c->v[a]);
+            cmax[a] = gmax(cmax[a], c->v[a]);
+        }
+    }
+}
+
+/* find_best_split_plane (bvh_builder.cpp:170-250). */
+static float best_split(builder* b, const bvh_node_t* node, const float* cmin, const float* cmax,
+                        uint32_t* out_axis, uint32_t* out_pos) {
+    float cheapest = FLT_MAX;
+    const uint32_t nb = b->interval_count;
+    for (uint32_t axis = 0; axis < 3; ++axis) {
+        float lo = cmin[axis], hi = cmax[axis];
+        if (lo == hi) continue;
+        for (uint32_t i = 0; i < nb; ++i) {
+            b->bcnt[i] = 0;
+            for (int a = 0; a < 3; ++a) { b->bmin[i * 3 + a] = FLT_MAX; b->bmax[i * 3 + a] = -FLT_MAX; }
+        }
+        float scale = (float)nb / (hi - lo);
+        for (uint32_t i = node->left_first; i < node->left_first + node->prim_count; ++i) {
+            const bvh_triangle_t* t = &b->tris[b->idx[i]];
+            int32_t bin = (int32_t)((b->centroid[b->idx[i]].v[axis] - lo) * scale);
+            if ((int32_t)nb - 1 < bin) bin = (int32_t)nb - 1;
+            b->bcnt[bin]++;
+            const float* p[3] = {t->p0, t->p1, t->p2};
+            for (int k = 0; k < 3; ++k)
+                for (int a = 0; a < 3; ++a) {
+                    b->bmin[bin * 3 + a] = gmin(b->bmin[bin * 3 + a], p[k][a]);
+                    b->bmax[bin * 3 + a] = gmax(b->bmax[bin * 3 + a], p[k][a]);
+                }
+        }
+        float lmn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lmx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        float rmn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rmx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        uint32_t lsum = 0, rsum = 0;
+        for (uint32_t i = 0; i < nb - 1; ++i) {
+            lsum += b->bcnt[i];
+            for (int a = 0; a < 3; ++a) {
+                lmn[a] = gmin(lmn[a], b->bmin[i * 3 + a]);
+                lmx[a] = gmax(lmx[a], b->bmax[i * 3 + a]);
+            }
+            b->larea[i] = (float)lsum * half_area(lmn, lmx);
+            uint32_t r = nb - 1 - i;
+            rsum += b->bcnt[r];
+            for (int a = 0; a < 3; ++a) {
+                rmn[a] = gmin(rmn[a], b->bmin[r * 3 + a]);
+                rmx[a] = gmax(rmx[a], b->bmax[r * 3 + a]);
+            }
+            b->rarea[nb - 2 - i] = (float)rsum * half_area(rmn, rmx);
+        }
+        for (uint32_t i = 0; i < nb - 1; ++i) {
+            float cost = b->larea[i] + b->rarea[i];
+            if (cost < cheapest) { *out_axis = axis; *out_pos = i + 1; cheapest = cost; }
+        }
+    }
+    return cheapest;
+}
+
+/* subdivide_node (bvh_builder.cpp:100-168), with the recursion unrolled onto an
+ * explicit stack that still visits left before right (pre-order), so child
+ * pairs are numbered exactly as the recursive version numbers them. */
+static void subdivide(builder* b) {
+    typedef struct { uint32_t node; float cmin[3], cmax[3]; } item;
+    uint32_t cap = 128, top = 0;
+    item* st = (item*)malloc(sizeof(item) * cap);
+    st[top].node = 0;
+    node_bounds(b, &b->nodes[0], st[top].cmin, st[top].cmax);
+    top++;
+    while (top > 0) {
+        item it = st[--top];
+        bvh_node_t* node = &b->nodes[it.node];
+        uint32_t axis = 0, pos = 0;
+        float cost = best_split(b, node, it.cmin, it.cmax, &axis, &pos);
+        if (b->subdivide_single_prim) {
+            if (node->prim_count == 1) continue;
+        } else {
+            int force = b->max_leaf_prims > 0 && node->prim_count > b->max_leaf_prims;
+            float parent = (float)node->prim_count * half_area(node->aabb_min, node->aabb_max);
+            if (!force && cost >= parent) continue;
+        }
+        /* Two-pointer partition (bvh_builder.cpp:121-137).  With pos == 0
+         * (no plane found: every centroid axis degenerate) the comparison
+         * "bin < 0u" is false for every triangle, so the loop still runs and
+         * rotates the index range left by one before the node stays a leaf;
+         * the bin itself (0 * inf = NaN cast to int) is never needed then. */
+        int32_t i = (int32_t)node->left_first;
+        int32_t j = i + (int32_t)node->prim_count - 1;
+        float scale = pos > 0 ? (float)b->interval_count / (it.cmax[axis] - it.cmin[axis]) : 0.0f;
+        while (i <= j) {
+            int left = 0;
+            if (pos > 0) {
+                float c = b->centroid[b->idx[i]].v[axis];
+                int32_t bin = (int32_t)((c - it.cmin[axis]) * scale);
+                if ((int32_t)b->interval_count - 1 < bin) bin = (int32_t)b->interval_count - 1;
+                left = (uint32_t)bin < pos;
+            }
+            if (left) i++;
+            else { uint32_t tmp = b->idx[i]; b->idx[i] = b->idx[j]; b->idx[j] = tmp; j--; }
+        }
+        uint32_t nleft = (uint32_t)i - node->left_first;
+        if (nleft == 0 || nleft == node->prim_count) continue;
+        uint32_t l = b->node_at++, r = b->node_at++;
+        b->nodes[l].left_first = node->left_first;
+        b->nodes[l].prim_count = nleft;
+        b->nodes[r].left_first = (uint32_t)i;
+        b->nodes[r].prim_count = node->prim_count - nleft;
+        node->left_first = l;
+        node->prim_count = 0;
+        if (top + 2 > cap) { cap *= 2; st = (item*)realloc(st, sizeof(item) * cap); }
+        st[top].node = r; node_bounds(b, &b->nodes[r], st[top].cmin, st[top].cmax); top++;
+        st[top].node = l; node_bounds(b, &b->nodes[l], st[top].cmin, st[top].cmax); top++;
+    }
+    free(st);
+}
+
+int orc_bvh_build(const triangle_t* tris, uint32_t n, uint32_t interval_count,
+                  uint32_t subdivide_single_prim, uint32_t max_leaf_prims,
+                  uint8_t** out_blob, uint64_t* out_size) {
+    if (!out_blob || !out_size || (n > 0 && !tris) || interval_count < 2) return -1;
+    builder b;
+    memset(&b, 0, sizeof(b));
+    b.interval_count = interval_count;
+    b.subdivide_single_prim = subdivide_single_prim;
+    b.max_leaf_prims = max_leaf_prims;
+    b.n = n;
+    uint32_t ncap = n * 2 < 2 ? 2 : n * 2;
+    b.tris = (bvh_triangle_t*)calloc(n ? n : 1, sizeof(bvh_triangle_t));
+    b.idx = (uint32_t*)calloc(n ? n : 1, sizeof(uint32_t));
+    b.centroid = (f3*)calloc(n ? n : 1, sizeof(f3));
+    b.nodes = (bvh_node_t*)calloc(ncap, sizeof(bvh_node_t));
+    b.bmin = (float*)malloc(sizeof(float) * 3 * interval_count);
+    b.bmax = (float*)malloc(sizeof(float) * 3 * interval_count);
+    b.bcnt = (uint32_t*)malloc(sizeof(uint32_t) * interval_count);
+    b.larea = (float*)malloc(sizeof(float) * interval_count);
+    b.rarea = (float*)malloc(sizeof(float) * interval_count);
+    for (uint32_t i = 0; i < n; ++i) {
+        memcpy(b.tris[i].p0, tris[i].v0.position, 12);
+        memcpy(b.tris[i].p1, tris[i].v1.position, 12);
+        memcpy(b.tris[i].p2, tris[i].v2.position, 12);
+        b.idx[i] = i;
+        b.centroid[i] = centroid_of(&b.tris[i]);
+    }
+    b.nodes[0].left_first = 0;
+    b.nodes[0].prim_count = n;
+    b.node_at = 2;  /* node 1 stays unused so sibling pairs share a 64-byte line */
+    subdivide(&b);
+
+    /* extract (bvh_builder.cpp:52-69) behind the 12-byte header the renderer
+     * uploads in front of it (renderer.cpp:113-155). */
+    uint64_t nodes_bytes = 32ull * b.node_at, tri_bytes = 36ull * n, idx_bytes = 4ull * n;
+    uint64_t size = 12 + nodes_bytes + tri_bytes + idx_bytes;
+    uint8_t* blob = (uint8_t*)malloc(size);
+    bvh_header_t h;
+    h.nodes_offset = 12;
+    h.triangles_offset = (uint32_t)(12 + nodes_bytes);
+    h.indices_offset = (uint32_t)(12 + nodes_bytes + tri_bytes);
+    memcpy(blob, &h, 12);
+    memcpy(blob + 12, b.nodes, nodes_bytes);
+    if (n) {
+        memcpy(blob + h.triangles_offset, b.tris, tri_bytes);
+        memcpy(blob + h.indices_offset, b.idx, idx_bytes);
+    }
+    free(b.tris); free(b.idx); free(b.centroid); free(b.nodes);
+    free(b.bmin); free(b.bmax); free(b.bcnt); free(b.larea); free(b.rarea);
+    *out_blob = blob;
+    *out_size = size;
+    return 0;
+}
+
+/* find_best_match (tlas_builder.cpp:86-110), including the reference's
+ * argument order: the "max" corner is max(A.min, B.min) and the "min" corner
+ * is max(A.max, B.max); the metric is half_area of that box. */
+static uint32_t best_match(const tlas_node_t* nodes, uint32_t A, const uint32_t* idx, uint32_t count) {
+    float smallest = FLT_MAX;
+    uint32_t best = 0xFFFFFFFFu;
+    const tlas_node_t* na = &nodes[idx[A]];
+    for (uint32_t B = 0; B < count; ++B) {
+        if (B == A) continue;
+        const tlas_node_t* nb = &nodes[idx[B]];
+        float bmx[3], bmn[3];
+        for (int a = 0; a < 3; ++a) {
+            bmx[a] = gmax(na->aabb_min[a], nb->aabb_min[a]);
+            bmn[a] = gmax(na->aabb_max[a], nb->aabb_max[a]);
+        }
+        float area = half_area(bmn, bmx);
+        if (area < smallest) { smallest = area; best = B; }
+    }
+    return best;
+}
+
+/* tlas_builder_t::build + extract (tlas_builder.cpp:6-84).  The reference's
+ * working list is a 256-entry stack array (:14); this one is sized to n. */
+int orc_tlas_build(const bvh_instance_t* inst, uint32_t n, uint8_t** out_blob, uint64_t* out_size) {
+    if (!out_blob || !out_size || (n > 0 && !inst) || n > 32768) return -1;
+    uint32_t ncount = n * 2;
+    tlas_node_t* nodes = (tlas_node_t*)calloc(ncount ? ncount : 1, sizeof(tlas_node_t));
+    uint32_t* idx = (uint32_t*)calloc(n ? n : 1, sizeof(uint32_t));
+    uint32_t remaining = n, at = 1;
+    for (uint32_t i = 0; i < n; ++i) {
+        idx[i] = at;
+        memcpy(nodes[at].aabb_min, inst[i].aabb_min, 12);
+        memcpy(nodes[at].aabb_max, inst[i].aabb_max, 12);
+        nodes[at].instance_idx = i;
+        nodes[at].left_right = 0;
+        at++;
+    }
+    if (n > 0) {
+        uint32_t A = 0;
+        uint32_t B = best_match(nodes, A, idx, remaining);
+        while (remaining > 1) {
+            uint32_t C = best_match(nodes, B, idx, remaining);
+            if (A == C) {
+                uint32_t ia = idx[A], ib = idx[B];
+                tlas_node_t* nn = &nodes[at];
+                nn->left_right = ia + (ib << 16);
+                for (int a = 0; a < 3; ++a) {
+                    nn->aabb_min[a] = gmin(nodes[ia].aabb_min[a], nodes[ib].aabb_min[a]);
+                    nn->aabb_max[a] = gmax(nodes[ia].aabb_max[a], nodes[ib].aabb_max[a]);
+                }
+                idx[A] = at++;
+                idx[B] = idx[remaining - 1];
+                B = best_match(nodes, A, idx, --remaining);
+            } else {
+                A = B;
+                B = C;
+            }
+        }
+        nodes[0] = nodes[idx[A]];
+    }
+    uint64_t nodes_bytes = 32ull * at, inst_bytes = 92ull * n;
+    uint64_t size = 8 + nodes_bytes + inst_bytes;
+    uint8_t* blob = (uint8_t*)malloc(size);
+    tlas_header_t h;
+    h.nodes_offset = 8;
+    h.instances_offset = (uint32_t)(8 + nodes_bytes);
+    memcpy(blob, &h, 8);
+    memcpy(blob + 8, nodes, nodes_bytes);
+    if (n) memcpy(blob + h.instances_offset, inst, inst_bytes);
+    free(nodes); free(idx);
+    *out_blob = blob;
+    *out_size = size;
+    return 0;
+}
+
+void orc_free(void* p) { free(p); }

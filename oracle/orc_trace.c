@@ -1,0 +1,329 @@
+/*
+ * orc_trace.c — oracle traversal, shading and rendering entry points.
+ * TEST INFRASTRUCTURE ONLY (see wf_oracle.h).  Instantiates orc_impl.h for
+ * float (the GPU's bit-exact contract) and double (the image oracle).
+ */
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include "wf_oracle.h"
+
+/* ---- random numbers (common.hlsl:79-97, core/random.h:7-24) ----------- */
+uint32_t orc_wang_hash(uint32_t seed) {
+    seed = (seed ^ 61u) ^ (seed >> 16);
+    seed *= 9u;
+    seed = seed ^ (seed >> 4);
+    seed *= 0x27d4eb2du;
+    seed = seed ^ (seed >> 15);
+    return seed;
+}
+
+/* rand_float: float(wang_hash(seed)) * 2.3283064365387e-10f; the result can
+ * round up to exactly 1.0f. */
+float orc_rand_float(uint32_t* seed) {
+    *seed = orc_wang_hash(*seed);
+    return (float)(*seed) * 2.3283064365387e-10f;
+}
+
+/* Per-path seed.  The reference seeds by frame_seed + compacted queue index
+ * (shade.hlsl:80), which changes with the order in which an atomic hands out
+ * slots; this build keys the stream by (pixel, sample, depth) so that a path
+ * can be replayed and the GPU and CPU draw the same numbers. */
+uint32_t orc_path_seed(uint32_t frame_seed, uint32_t pixel, uint32_t sample, uint32_t depth) {
+    uint32_t s = frame_seed + pixel;
+    s = orc_wang_hash(s) ^ (sample * 0x9E3779B9u);
+    s = orc_wang_hash(s) ^ (depth * 0x85EBCA6Bu);
+    return s;
+}
+
+/* sin(2*pi*r), cos(2*pi*r) for r in [0, 1].  Range reduction is exact in r:
+ * t = 4r, k = rint(t), f = t - k in [-1/2, 1/2], x = f * (pi/2) in
+ * [-pi/4, pi/4]; then truncated Taylor series (sin to x^9, cos to x^10,
+ * truncation error below 2e-9) in Horner form, and a quarter-turn rotation by
+ * k mod 4.  Written out operation by operation so the CUDA kernels can
+ * evaluate the identical sequence. */
+void orc_sincos_2pi(float r, float* s_out, float* c_out) {
+    float t = r * 4.0f;
+    float k = rintf(t);
+    float f = t - k;
+    float x = f * 1.57079637f;
+    float x2 = x * x;
+    float sp = -1.98412698e-4f + x2 * 2.75573192e-6f;
+    sp = 8.33333377e-3f + x2 * sp;
+    sp = -1.66666672e-1f + x2 * sp;
+    float sn = x + (x * x2) * sp;
+    float cp = 2.48015876e-5f + x2 * -2.75573188e-7f;
+    cp = -1.38888892e-3f + x2 * cp;
+    cp = 4.16666679e-2f + x2 * cp;
+    cp = -0.5f + x2 * cp;
+    float cs = 1.0f + x2 * cp;
+    int q = ((int)k) & 3;
+    float s, c;
+    if (q == 0) { s = sn; c = cs; }
+    else if (q == 1) { s = cs; c = -sn; }
+    else if (q == 2) { s = -sn; c = -cs; }
+    else { s = -cs; c = sn; }
+    *s_out = s;
+    *c_out = c;
+}
+
+static void sincos_2pi_f64(double r, double* s, double* c) {
+    double a = 6.283185307179586 * r;
+    *s = sin(a);
+    *c = cos(a);
+}
+
+/* ---- instantiations ------------------------------------------------------ */
+#define R float
+#define FN(x) x##_f32
+#define K(x) x##f
+#define SQRT sqrtf
+#define FABS fabsf
+#define FMIN fminf
+#define FMAX fmaxf
+#define SINCOS2PI(r, s, c) orc_sincos_2pi((r), (s), (c))
+#define MAXT FLT_MAX
+#include "orc_impl.h"
+#undef R
+#undef FN
+#undef K
+#undef SQRT
+#undef FABS
+#undef FMIN
+#undef FMAX
+#undef SINCOS2PI
+#undef MAXT
+
+#define R double
+#define FN(x) x##_f64
+#define K(x) x
+#define SQRT sqrt
+#define FABS fabs
+#define FMIN fmin
+#define FMAX fmax
+#define SINCOS2PI(r, s, c) sincos_2pi_f64((r), (s), (c))
+#define MAXT ((double)FLT_MAX)
+#include "orc_impl.h"
+
+/* ---- exported known-answer helpers ---------------------------------------- */
+int orc_intersect_triangle(const float v0[3], const float v1[3], const float v2[3], const float org[3],
+                           const float dir[3], float* t_inout, float bary[2], int no_cull) {
+    return tri_f32(ld_f32(v0), ld_f32(v1), ld_f32(v2), ld_f32(org), ld_f32(dir), t_inout, &bary[0], &bary[1],
+                   no_cull);
+}
+
+float orc_intersect_aabb(const float bmin[3], const float bmax[3], const float org[3], const float inv_dir[3],
+                         float t) {
+    return slab_f32(bmin, bmax, ld_f32(org), ld_f32(inv_dir), t);
+}
+
+/* make_primary_ray (hardware-ray variant, common.hlsl:182-195): no origin
+ * nudge, TMin = 1e-8, TMax = FLT_MAX. */
+void orc_primary_ray(const view_t* view, uint32_t px, uint32_t py, RayDesc2* out) {
+    float uvx = ((float)px + 0.5f) / view->render_dim[0];
+    float uvy = ((float)py + 0.5f) / view->render_dim[1];
+    uvy = 1.0f - uvy;
+    float cx = 2.0f * uvx - 1.0f, cy = 2.0f * uvy - 1.0f;
+    v3_f32 pv = xform_f32(mk_f32(cx, cy, 1.0f), 1.0f, view->clip_to_view);
+    v3_f32 dv = normalize_f32(pv);
+    v3_f32 dw = xform_f32(dv, 0.0f, view->view_to_world);
+    v3_f32 ow = xform_f32(mk_f32(0.0f, 0.0f, 0.0f), 1.0f, view->view_to_world);
+    out->Origin[0] = ow.x; out->Origin[1] = ow.y; out->Origin[2] = ow.z;
+    out->TMin = 1e-8f;
+    out->Direction[0] = dw.x; out->Direction[1] = dw.y; out->Direction[2] = dw.z;
+    out->TMax = FLT_MAX;
+}
+
+/* ---- multithreaded ray queries -------------------------------------------- */
+typedef struct {
+    const orc_scene* s;
+    const RayDesc2* rays;
+    hit_result_t* hits;
+    uint32_t n, flags;
+    int f64;
+    volatile uint32_t next;
+    pthread_mutex_t mu;
+    orc_counters total;
+    uint32_t overflows;
+} trace_job;
+
+static void* trace_worker(void* arg) {
+    trace_job* J = (trace_job*)arg;
+    orc_counters c = {0, 0, 0, 0};
+    uint32_t ovf = 0;
+    for (;;) {
+        uint32_t begin = __atomic_fetch_add(&J->next, 4096u, __ATOMIC_RELAXED);
+        if (begin >= J->n) break;
+        uint32_t end = begin + 4096u < J->n ? begin + 4096u : J->n;
+        for (uint32_t i = begin; i < end; ++i) {
+            const RayDesc2* r = &J->rays[i];
+            hit_result_t* o = &J->hits[i];
+            if (!J->f64) {
+                hit_f32 h;
+                int rc = trace_one_f32(J->s, ld_f32(r->Origin), ld_f32(r->Direction), r->TMax, J->flags, &h, &c);
+                if (rc < 0) ovf++;
+                o->instance_idx = h.inst; o->primitive_idx = h.prim; o->t = h.t;
+                o->bary[0] = h.u; o->bary[1] = h.v;
+            } else {
+                hit_f64 h;
+                int rc = trace_one_f64(J->s, ld_f64(r->Origin), ld_f64(r->Direction), (double)r->TMax, J->flags,
+                                       &h, &c);
+                if (rc < 0) ovf++;
+                o->instance_idx = h.inst; o->primitive_idx = h.prim; o->t = (float)h.t;
+                o->bary[0] = (float)h.u; o->bary[1] = (float)h.v;
+            }
+        }
+    }
+    pthread_mutex_lock(&J->mu);
+    J->total.tlas_node_loads += c.tlas_node_loads;
+    J->total.instance_loads += c.instance_loads;
+    J->total.blas_node_loads += c.blas_node_loads;
+    J->total.triangle_tests += c.triangle_tests;
+    J->overflows += ovf;
+    pthread_mutex_unlock(&J->mu);
+    return NULL;
+}
+
+static uint32_t run_trace(const orc_scene* s, const RayDesc2* rays, uint32_t n, hit_result_t* hits, uint32_t flags,
+                          orc_counters* counters, int threads, int f64) {
+    trace_job J;
+    memset(&J, 0, sizeof(J));
+    J.s = s; J.rays = rays; J.hits = hits; J.n = n; J.flags = flags; J.f64 = f64;
+    pthread_mutex_init(&J.mu, NULL);
+    if (threads <= 1) {
+        trace_worker(&J);
+    } else {
+        pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
+        for (int i = 0; i < threads; ++i) pthread_create(&th[i], NULL, trace_worker, &J);
+        for (int i = 0; i < threads; ++i) pthread_join(th[i], NULL);
+        free(th);
+    }
+    pthread_mutex_destroy(&J.mu);
+    if (counters) *counters = J.total;
+    return J.overflows;
+}
+
+uint32_t orc_trace(const orc_scene* s, const RayDesc2* rays, uint32_t n, hit_result_t* hits, uint32_t flags,
+                   orc_counters* counters, int threads) {
+    return run_trace(s, rays, n, hits, flags, counters, threads, 0);
+}
+
+uint32_t orc_trace_f64(const orc_scene* s, const RayDesc2* rays, uint32_t n, hit_result_t* hits, uint32_t flags,
+                       int threads) {
+    return run_trace(s, rays, n, hits, flags, NULL, threads, 1);
+}
+
+/* ---- rendering ----------------------------------------------------------- */
+typedef struct {
+    const orc_scene* s;
+    const view_t* view;
+    const orc_render_params* p;
+    lights_f32 l32;
+    lights_f64 l64;
+    int f64;
+    uint32_t width, pix0, pix1;
+    float* acc32;
+    double* acc64;
+    volatile uint32_t next;
+    pthread_mutex_t mu;
+    orc_render_stats total;
+} render_job;
+
+static void merge_counters(orc_counters* a, const orc_counters* b) {
+    a->tlas_node_loads += b->tlas_node_loads;
+    a->instance_loads += b->instance_loads;
+    a->blas_node_loads += b->blas_node_loads;
+    a->triangle_tests += b->triangle_tests;
+}
+
+static void* render_worker(void* arg) {
+    render_job* J = (render_job*)arg;
+    orc_render_stats st;
+    memset(&st, 0, sizeof(st));
+    job_f32 j32;
+    job_f64 j64;
+    memset(&j32, 0, sizeof(j32));
+    memset(&j64, 0, sizeof(j64));
+    j32.s = J->s; j32.view = J->view; j32.p = J->p; j32.lights = J->l32; j32.width = J->width;
+    j64.s = J->s; j64.view = J->view; j64.p = J->p; j64.lights = J->l64; j64.width = J->width;
+    const uint32_t chunk = 256;
+    for (;;) {
+        uint32_t begin = __atomic_fetch_add(&J->next, chunk, __ATOMIC_RELAXED);
+        uint32_t b = J->pix0 + begin;
+        if (b >= J->pix1) break;
+        uint32_t e = b + chunk < J->pix1 ? b + chunk : J->pix1;
+        for (uint32_t px = b; px < e; ++px) {
+            for (uint32_t sidx = 0; sidx < J->p->spp; ++sidx) {
+                uint32_t sample = J->p->sample_offset + sidx;
+                if (!J->f64) {
+                    float acc[3] = {J->acc32[4ull * px], J->acc32[4ull * px + 1], J->acc32[4ull * px + 2]};
+                    path_f32(&j32, px, sample, acc, &st);
+                    J->acc32[4ull * px] = acc[0];
+                    J->acc32[4ull * px + 1] = acc[1];
+                    J->acc32[4ull * px + 2] = acc[2];
+                    J->acc32[4ull * px + 3] += 1.0f;
+                } else {
+                    double acc[3] = {J->acc64[4ull * px], J->acc64[4ull * px + 1], J->acc64[4ull * px + 2]};
+                    path_f64(&j64, px, sample, acc, &st);
+                    J->acc64[4ull * px] = acc[0];
+                    J->acc64[4ull * px + 1] = acc[1];
+                    J->acc64[4ull * px + 2] = acc[2];
+                    J->acc64[4ull * px + 3] += 1.0;
+                }
+            }
+        }
+    }
+    pthread_mutex_lock(&J->mu);
+    for (int d = 0; d < 16; ++d) {
+        J->total.extend_rays[d] += st.extend_rays[d];
+        J->total.shadow_rays[d] += st.shadow_rays[d];
+    }
+    J->total.stack_overflows += st.stack_overflows;
+    merge_counters(&J->total.extend_traffic, &st.extend_traffic);
+    merge_counters(&J->total.shadow_traffic, &st.shadow_traffic);
+    pthread_mutex_unlock(&J->mu);
+    return NULL;
+}
+
+static int run_render(const orc_scene* s, const view_t* view, const orc_render_params* p, float* acc32,
+                      double* acc64, orc_render_stats* stats, int threads) {
+    if (!s || !view || !p || p->max_bounces > 15) return -1;
+    render_job J;
+    memset(&J, 0, sizeof(J));
+    J.s = s; J.view = view; J.p = p; J.acc32 = acc32; J.acc64 = acc64; J.f64 = acc64 != NULL;
+    J.width = (uint32_t)view->render_dim[0];
+    uint32_t npix = J.width * (uint32_t)view->render_dim[1];
+    J.pix0 = p->pixel_begin;
+    J.pix1 = p->pixel_end ? p->pixel_end : npix;
+    if (J.pix1 > npix || J.pix0 > J.pix1) return -1;
+    if (J.f64) build_lights_f64(s, &J.l64);
+    else build_lights_f32(s, &J.l32);
+    pthread_mutex_init(&J.mu, NULL);
+    if (threads <= 1) {
+        render_worker(&J);
+    } else {
+        pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
+        for (int i = 0; i < threads; ++i) pthread_create(&th[i], NULL, render_worker, &J);
+        for (int i = 0; i < threads; ++i) pthread_join(th[i], NULL);
+        free(th);
+    }
+    pthread_mutex_destroy(&J.mu);
+    if (J.f64) { free(J.l64.tri); free(J.l64.cdf); }
+    else { free(J.l32.tri); free(J.l32.cdf); }
+    if (stats) *stats = J.total;
+    return 0;
+}
+
+int orc_render(const orc_scene* s, const view_t* view, const orc_render_params* p, float* accum,
+               orc_render_stats* stats, int threads) {
+    if (!accum) return -1;
+    return run_render(s, view, p, accum, NULL, stats, threads);
+}
+
+int orc_render_f64(const orc_scene* s, const view_t* view, const orc_render_params* p, double* accum,
+                   int threads) {
+    if (!accum) return -1;
+    return run_render(s, view, p, NULL, accum, NULL, threads);
+}

@@ -1,0 +1,129 @@
+/*
+ * wf_oracle.h — CPU oracle for the wavefront path-tracing hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a scalar C restatement of the reference
+ * renderer's software acceleration-structure builders, traversal and shading
+ * (Contingencyy/WavefrontPathtracing, source/renderer/bvh/ builders and
+ * source/renderer/shaders/ HLSL), plus the same restatement of the scattering
+ * models this project adds (metal, dielectric, next-event estimation, Russian
+ * roulette).  It is the checker the GPU library is compared against and the
+ * timed CPU baseline; the product never links, loads or calls it.
+ *
+ * Build: oracle/Makefile, gcc -O2 -ffp-contract=off (no fused multiply-add, so
+ * every float operation rounds exactly as written — on aarch64 gcc would
+ * otherwise contract a*b+c into fma).
+ *
+ * Pinning: the builders are pinned byte-for-byte against the reference's own
+ * bvh_builder.cpp / tlas_builder.cpp compiled from the reference sources
+ * (oracle/build_ref.sh -> oracle/_ref/libref_bvh.so) and against golden blobs
+ * in tests/golden/.  The reference has no test, golden image or known-answer
+ * vector for traversal or shading, and its HLSL cannot run here (no D3D12), so
+ * those parts follow the HLSL line by line with the operation order written
+ * down in each function ("parity unpinned" by reference outputs for them).
+ */
+#ifndef WF_ORACLE_H
+#define WF_ORACLE_H
+
+#include <stdint.h>
+#include "../include/wf_shared.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* --- builders (bvh_builder.cpp:6-264, tlas_builder.cpp:6-110) ----------- */
+/* Writes a malloc'ed blob [bvh_header_t | nodes | bvh_triangle_t | uint32]. */
+int orc_bvh_build(const triangle_t* tris, uint32_t n, uint32_t interval_count,
+                  uint32_t subdivide_single_prim, uint32_t max_leaf_prims,
+                  uint8_t** out_blob, uint64_t* out_size);
+/* Writes a malloc'ed blob [tlas_header_t | nodes | bvh_instance_t]. */
+int orc_tlas_build(const bvh_instance_t* inst, uint32_t n, uint8_t** out_blob, uint64_t* out_size);
+void orc_free(void* p);
+
+/* --- scene ----------------------------------------------------------------- */
+typedef struct orc_mesh {
+    const triangle_t* tris;   /* original triangle order (primitive ids) */
+    uint32_t tri_count;
+    const uint8_t* blas;      /* [bvh_header_t | nodes | bvh_triangle_t | uint32] */
+} orc_mesh;
+
+typedef struct orc_instance {
+    float local_to_world[16];
+    float world_to_local[16];
+    material_t material;
+    uint32_t mesh;            /* index into orc_scene.meshes */
+    uint32_t bsdf;            /* 0 lambert, 1 metal, 2 dielectric */
+    float ior;
+} orc_instance;
+
+typedef struct orc_scene {
+    const orc_mesh* meshes;
+    uint32_t mesh_count;
+    const uint8_t* tlas;      /* [tlas_header_t | nodes | bvh_instance_t]; bvh_index = mesh */
+    const orc_instance* inst;
+    uint32_t inst_count;
+} orc_scene;
+
+typedef struct orc_counters {
+    uint64_t tlas_node_loads, instance_loads, blas_node_loads, triangle_tests;
+} orc_counters;
+
+enum { ORC_ANY_HIT = 1, ORC_NO_CULL = 2 };
+
+/* Software closest-hit / any-hit query (accelstruct.hlsl:58-218,
+ * intersect.hlsl:7-76).  Returns the number of rays whose 64-entry stack
+ * overflowed (those report a miss).  threads <= 1 runs single-threaded. */
+uint32_t orc_trace(const orc_scene* s, const RayDesc2* rays, uint32_t n, hit_result_t* hits,
+                   uint32_t flags, orc_counters* counters, int threads);
+/* The same query evaluated in double precision (intersection and slab math). */
+uint32_t orc_trace_f64(const orc_scene* s, const RayDesc2* rays, uint32_t n, hit_result_t* hits,
+                       uint32_t flags, int threads);
+
+/* --- rendering -------------------------------------------------------------- */
+typedef struct orc_render_params {
+    uint32_t max_bounces;
+    uint32_t cosine_weighted_diffuse;
+    float hdr_env_strength;
+    float env_color[3];
+    uint32_t spp;
+    uint32_t sample_offset;   /* first sample index (accumulated renders) */
+    uint32_t nee;
+    uint32_t rr_start_depth;
+    uint32_t frame_seed;
+    uint32_t pixel_begin, pixel_end;   /* render only this pixel range (end 0 = all) */
+} orc_render_params;
+
+typedef struct orc_render_stats {
+    uint64_t extend_rays[16];   /* rays traced at each depth */
+    uint64_t shadow_rays[16];   /* shadow rays traced at each depth */
+    uint64_t stack_overflows;
+    orc_counters extend_traffic, shadow_traffic;
+} orc_render_stats;
+
+/* FP32 restatement of generate/extend/shade/connect: adds each path's
+ * contributions to accum (RGBA float, width*height*4; alpha counts samples) in
+ * the same per-pixel order as the GPU kernels. */
+int orc_render(const orc_scene* s, const view_t* view, const orc_render_params* p,
+               float* accum, orc_render_stats* stats, int threads);
+/* Same paths in double precision (libm sin/cos, double geometry math, the same
+ * uniform random numbers); accum is double RGBA. */
+int orc_render_f64(const orc_scene* s, const view_t* view, const orc_render_params* p,
+                   double* accum, int threads);
+
+/* --- small helpers exported for known-answer tests --------------------------- */
+uint32_t orc_wang_hash(uint32_t seed);
+float orc_rand_float(uint32_t* seed);
+uint32_t orc_path_seed(uint32_t frame_seed, uint32_t pixel, uint32_t sample, uint32_t depth);
+void orc_sincos_2pi(float r, float* s, float* c);
+int orc_intersect_triangle(const float v0[3], const float v1[3], const float v2[3],
+                           const float org[3], const float dir[3], float* t_inout,
+                           float bary[2], int no_cull);
+float orc_intersect_aabb(const float bmin[3], const float bmax[3], const float org[3],
+                         const float inv_dir[3], float t);
+void orc_primary_ray(const view_t* view, uint32_t px, uint32_t py, RayDesc2* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,141 @@
+"""CPU: known answers for the oracle's scalar helpers (RNG, sin/cos,
+intersection edge cases) and basic traversal/render sanity."""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+from wavefrontpathtracing_gb300.abi import ptr
+
+
+def wang_ref(s):
+    # common.hlsl:79-88 written out in Python integers
+    s = ((s ^ 61) ^ (s >> 16)) & 0xFFFFFFFF
+    s = (s * 9) & 0xFFFFFFFF
+    s = s ^ (s >> 4)
+    s = (s * 0x27D4EB2D) & 0xFFFFFFFF
+    s = s ^ (s >> 15)
+    return s
+
+
+def test_wang_hash_known_answers(orc):
+    L = orc.lib()
+    for s in [0, 1, 61, 0xC977E154, 0xFFFFFFFF, 123456789]:
+        assert L.orc_wang_hash(s) == wang_ref(s)
+
+
+def test_rand_float_range_and_rounding(orc):
+    L = orc.lib()
+    seed = ctypes.c_uint32(1)
+    vals = [L.orc_rand_float(ctypes.byref(seed)) for _ in range(10000)]
+    assert min(vals) >= 0.0 and max(vals) <= 1.0
+    # float(0xFFFFFFFF) * 2.3283064365387e-10f rounds to exactly 1.0f
+    assert np.float32(np.float32(4294967295.0) * np.float32(2.3283064365387e-10)) == np.float32(1.0)
+
+
+def test_sincos_2pi_accuracy(orc):
+    L = orc.lib()
+    s, c = ctypes.c_float(), ctypes.c_float()
+    worst = 0.0
+    for r in np.linspace(0.0, 1.0, 4097, dtype=np.float32):
+        L.orc_sincos_2pi(float(r), ctypes.byref(s), ctypes.byref(c))
+        a = 2.0 * math.pi * float(r)
+        worst = max(worst, abs(s.value - math.sin(a)), abs(c.value - math.cos(a)))
+    assert worst < 4e-7
+
+
+def _tri(orc, v0, v1, v2, o, d, t=3.4e38, no_cull=0):
+    arr = [np.asarray(x, dtype=np.float32) for x in (v0, v1, v2, o, d)]
+    tt = ctypes.c_float(t)
+    bary = np.zeros(2, dtype=np.float32)
+    hit = orc.lib().orc_intersect_triangle(*[ptr(a) for a in arr], ctypes.byref(tt), ptr(bary), no_cull)
+    return hit, tt.value, bary
+
+
+def test_triangle_front_back_and_ties(orc):
+    v0, v1, v2 = (0, 0, 0), (1, 0, 0), (0, 1, 0)   # (v1-v0)x(v2-v0) = +z: front side is +z
+    hit, t, bary = _tri(orc, v0, v1, v2, (0.25, 0.25, 1.0), (0, 0, -1))
+    assert hit and t == np.float32(1.0) and np.allclose(bary, [0.25, 0.25])
+    hit, _, _ = _tri(orc, v0, v1, v2, (0.25, 0.25, -1.0), (0, 0, 1))
+    assert not hit                                          # back face culled (det < 1e-8)
+    hit, _, _ = _tri(orc, v0, v1, v2, (0.25, 0.25, -1.0), (0, 0, 1), no_cull=1)
+    assert hit
+    hit, _, _ = _tri(orc, v0, v1, v2, (0.25, 0.25, 1.0), (0, 0, -1), t=1.0)
+    assert not hit                                          # t >= ray.t is rejected: first found wins ties
+    hit, _, _ = _tri(orc, v0, v1, v2, (0.25, 0.25, 1.0), (1, 0, 0))
+    assert not hit                                          # parallel ray: det = 0
+    hit, t, bary = _tri(orc, v0, v1, v2, (0.0, 0.0, 1.0), (0, 0, -1))
+    assert hit and bary[0] == 0 and bary[1] == 0            # vertex hit: v = w = 0 accepted
+
+
+def test_aabb_slab_edge_cases(orc):
+    L = orc.lib()
+    bmin = np.zeros(3, np.float32)
+    bmax = np.ones(3, np.float32)
+
+    def slab(o, d, t=3.4e38):
+        d = np.asarray(d, np.float32)
+        with np.errstate(divide="ignore"):
+            inv = (np.float32(1.0) / d).astype(np.float32)
+        return L.orc_intersect_aabb(ptr(bmin), ptr(bmax), ptr(np.asarray(o, np.float32)), ptr(inv), t)
+
+    big = np.float32(3.4028235e38)
+    assert slab((-1, 0.5, 0.5), (1, 0, 0)) == np.float32(1.0)
+    assert slab((0.5, 0.5, 0.5), (1, 0, 0)) == np.float32(-0.5)   # origin inside: negative tmin
+    assert slab((2, 0.5, 0.5), (1, 0, 0)) == big                  # box behind the ray
+    assert slab((-1, 0.5, 0.5), (1, 0, 0), t=0.5) == big          # beyond ray.t
+    # axis-parallel ray in the plane of a face: (0 - 0) * inf = NaN, and
+    # minNum/maxNum then keep the other slab value (+inf), so tmin = +inf: a miss
+    assert slab((-1, 0.0, 0.5), (1, 0, 0)) == big
+    # strictly inside the slab of the parallel axis: hit
+    assert slab((-1, 1e-3, 0.5), (1, 0, 0)) == np.float32(1.0)
+
+
+def test_primary_ray_points_forward(orc):
+    from wavefrontpathtracing_gb300 import scenes
+    view = scenes.make_view((0.0, 0.0, -5.0), (0.0, 0.0, 0.0), 60.0, 65, 33)
+    rays = orc.primary_rays(view, 65, 33)
+    centre = rays[16 * 65 + 32]
+    assert np.allclose(centre["origin"], (0, 0, -5), atol=1e-5)
+    assert np.allclose(centre["dir"], (0, 0, 1), atol=1e-3)
+    assert rays[0]["dir"][1] > 0 and rays[0]["dir"][0] < 0           # row 0 is the top, x grows right
+    assert np.allclose(np.linalg.norm(rays["dir"], axis=1), 1.0, atol=1e-5)
+
+
+def test_trace_single_instance_against_brute_force(orc):
+    """Closest hits through the BVH equal a brute-force minimum over all triangles
+    (ties excepted), for a small random soup."""
+    from wavefrontpathtracing_gb300 import scenes
+    from tests.helpers import single_instance_scene
+    tris = scenes.triangle_soup(400, seed=3, mu=-2.5)
+    sc = single_instance_scene(orc, [tris])
+    rays = scenes.soup_rays(24, kind="incoherent")
+    hits, cnt, ovf = sc.trace(rays)
+    assert ovf == 0 and cnt["triangle_tests"] > 0
+    bt = np.full(len(rays), np.inf)
+    for i in range(len(tris)):
+        for j in range(len(rays)):
+            ok, t, _ = _tri(orc, tris["v0"]["position"][i], tris["v1"]["position"][i], tris["v2"]["position"][i],
+                            rays["origin"][j], rays["dir"][j])
+            if ok and t < bt[j]:
+                bt[j] = t
+    got = np.where(hits["instance"] == 0xFFFFFFFF, np.inf, hits["t"])
+    assert np.array_equal(np.isinf(got), np.isinf(bt))
+    fin = np.isfinite(bt)
+    assert np.array_equal(got[fin].astype(np.float32), bt[fin].astype(np.float32))
+
+
+def test_render_f32_and_f64_agree_on_box(orc):
+    from wavefrontpathtracing_gb300 import scenes
+    from tests.helpers import oracle_scene_from_desc
+    desc = scenes.box_scene(width=24, height=24, subdivision=2)
+    sc = oracle_scene_from_desc(orc, desc)
+    a32, st = sc.render(desc.view, 24, 24, max_bounces=4, spp=8, frame_seed=7)
+    a64, _ = sc.render(desc.view, 24, 24, max_bounces=4, spp=8, frame_seed=7, f64=True)
+    assert st["extend_rays"][0] == 24 * 24 * 8 and st["stack_overflows"] == 0
+    img32 = a32[..., :3] / a32[..., 3:]
+    img64 = a64[..., :3] / a64[..., 3:]
+    assert img32.mean() > 0.01
+    # the same random numbers drive both; rare paths diverge at triangle edges
+    assert np.sqrt(np.mean((img32 - img64) ** 2)) < 2e-2

@@ -1,0 +1,263 @@
+"""GB300 wavefront path tracer: Python binding of the C ABI (include/wf.h).
+
+The compute path is libwf.so (hand-written CUDA for sm_103a plus the C++ host
+orchestration).  This module only loads it with ctypes and mirrors the
+reference renderer's front end (source/renderer/renderer.h:13-55):
+
+    r = Renderer(width, height)
+    mesh = r.create_render_mesh(vertices, indices)      # create_render_mesh
+    r.begin_scene(view)                                  # begin_scene
+    r.submit_render_mesh(mesh, transform, material)      # submit_render_mesh
+    r.end_scene()                                        # TLAS build
+    r.render(settings, spp=16)                           # render
+    img = r.read_image()
+
+There is no CPU fallback: if libwf.so is missing or no CUDA device exists the
+calls raise WFError.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import (BvhOptions, Env, InitParams, RenderOptions, RenderSettings, Stats, View, bvh_instance_dtype,
+                  hit_dtype, material_dtype, material_ext_dtype, ptr, ray_dtype, triangle_dtype, vertex_dtype)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libwf.so")
+
+STATUS = {0: "WF_OK", -1: "WF_ERR_INVALID", -2: "WF_ERR_OOM", -3: "WF_ERR_CAPACITY", -4: "WF_ERR_TIMEOUT",
+          -5: "WF_ERR_STACK", -6: "WF_ERR_CUDA", -7: "WF_ERR_STATE"}
+
+# Every entry point declared in include/wf.h, with its ctypes signature.
+_vp, _u32, _u64, _i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32
+_pu64, _pu32 = ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32)
+SIGNATURES = {
+    "wf_create": [_vp, ctypes.POINTER(_vp)],
+    "wf_destroy": [_vp],
+    "wf_status_string": [ctypes.c_int],
+    "wf_last_error": [],
+    "wf_abi_version": [],
+    "wf_get_stream": [_vp, ctypes.POINTER(_vp)],
+    "wf_synchronize": [_vp],
+    "wf_mesh_create": [_vp, _vp, _u32, _vp, _u32, _vp, _pu32],
+    "wf_mesh_create_prebuilt": [_vp, _vp, _u32, _vp, _u64, _pu32],
+    "wf_mesh_get_blas": [_vp, _u32, _vp, _pu64],
+    "wf_scene_begin": [_vp, _vp, _vp],
+    "wf_instance_submit": [_vp, _u32, _vp, _vp],
+    "wf_instance_submit_ex": [_vp, _u32, _vp, _vp],
+    "wf_scene_end": [_vp],
+    "wf_scene_get_instances": [_vp, _vp, _u32, _pu32],
+    "wf_scene_get_tlas": [_vp, _vp, _pu64],
+    "wf_render": [_vp, _vp, _vp, _u32],
+    "wf_read_image": [_vp, _vp, _u64],
+    "wf_read_image_ldr": [_vp, _vp, _u64],
+    "wf_get_stats": [_vp, _vp],
+    "wf_trace": [_vp, _vp, _u32, _vp, _u32],
+    "wf_trace_device": [_vp, _vp, _u32, _vp, _u32],
+    "wf_bvh_build": [_vp, _vp, _u32, _vp, _vp, _pu64],
+    "wf_tlas_build": [_vp, _vp, _u32, _vp, _pu64],
+}
+_RESTYPES = {"wf_status_string": ctypes.c_char_p, "wf_last_error": ctypes.c_char_p}
+
+
+class WFError(RuntimeError):
+    def __init__(self, status, message):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+
+
+_lib = None
+
+
+def load(path=None):
+    """Loads libwf.so (building it first when only the sources are present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        from . import build as _build
+        _build.build()
+    L = ctypes.CDLL(path)
+    for name, args in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = _RESTYPES.get(name, ctypes.c_int)
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != 0:
+        msg = load().wf_last_error()
+        raise WFError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def _f16(m):
+    a = np.ascontiguousarray(m, dtype=np.float32)
+    if a.shape == (4, 4):
+        a = abi.mat_f32(a)
+    assert a.shape == (16,)
+    return a
+
+
+class Renderer:
+    """One wf_ctx: a CUDA device, its stream and all device memory."""
+
+    def __init__(self, width, height, device=0, wave_capacity=0):
+        L = load()
+        p = InitParams(width, height, 1, 0, device, wave_capacity)
+        h = ctypes.c_void_p()
+        check(L.wf_create(ctypes.byref(p), ctypes.byref(h)))
+        self.h, self.L, self.width, self.height = h, L, width, height
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.wf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- meshes
+    def create_render_mesh(self, vertices, indices, interval_count=8, subdivide_single_prim=False,
+                           max_leaf_prims=0):
+        v = np.ascontiguousarray(vertices, dtype=vertex_dtype)
+        i = np.ascontiguousarray(indices, dtype=np.uint32)
+        o = BvhOptions(interval_count, int(subdivide_single_prim), max_leaf_prims)
+        out = ctypes.c_uint32()
+        check(self.L.wf_mesh_create(self.h, ptr(v), len(v), ptr(i), len(i), ctypes.byref(o), ctypes.byref(out)))
+        return out.value
+
+    def create_mesh_from_triangles(self, tris, **opts):
+        """De-indexed triangle_t input: vertices = the 3n corners, indices = 0..3n-1."""
+        tris = np.ascontiguousarray(tris, dtype=triangle_dtype)
+        verts = tris.view(vertex_dtype).reshape(-1)
+        return self.create_render_mesh(verts, np.arange(len(verts), dtype=np.uint32), **opts)
+
+    def create_mesh_prebuilt(self, tris, blob):
+        tris = np.ascontiguousarray(tris, dtype=triangle_dtype)
+        blob = np.ascontiguousarray(blob, dtype=np.uint8)
+        out = ctypes.c_uint32()
+        check(self.L.wf_mesh_create_prebuilt(self.h, ptr(tris), len(tris), ptr(blob), blob.nbytes,
+                                             ctypes.byref(out)))
+        return out.value
+
+    def mesh_blas(self, mesh):
+        n = ctypes.c_uint64(0)
+        self.L.wf_mesh_get_blas(self.h, mesh, None, ctypes.byref(n))
+        out = np.zeros(n.value, dtype=np.uint8)
+        check(self.L.wf_mesh_get_blas(self.h, mesh, ptr(out), ctypes.byref(n)))
+        return out
+
+    # ---- scene
+    def begin_scene(self, view, env=None):
+        e = None
+        if env is not None:
+            e = Env()
+            e.color[:] = list(env)
+        check(self.L.wf_scene_begin(self.h, ctypes.byref(view), ctypes.byref(e) if e is not None else None))
+
+    def submit_render_mesh(self, mesh, transform, material=None):
+        """material: material_ext_dtype record (bsdf + ior) or material_dtype record (Lambert)."""
+        m = _f16(transform)
+        if material is None:
+            material = np.zeros(1, dtype=material_ext_dtype)[0]
+            material["base"]["base_color_factor"] = (0.8, 0.8, 0.8)
+        if material.dtype == material_dtype:
+            rec = np.array([material], dtype=material_dtype)
+            check(self.L.wf_instance_submit(self.h, mesh, ptr(m), ptr(rec)))
+        else:
+            rec = np.array([material], dtype=material_ext_dtype)
+            check(self.L.wf_instance_submit_ex(self.h, mesh, ptr(m), ptr(rec)))
+
+    def end_scene(self):
+        check(self.L.wf_scene_end(self.h))
+
+    def scene_instances(self):
+        n = ctypes.c_uint32(0)
+        self.L.wf_scene_get_instances(self.h, None, 0, ctypes.byref(n))
+        out = np.zeros(n.value, dtype=bvh_instance_dtype)
+        check(self.L.wf_scene_get_instances(self.h, ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def scene_tlas(self):
+        n = ctypes.c_uint64(0)
+        self.L.wf_scene_get_tlas(self.h, None, ctypes.byref(n))
+        out = np.zeros(n.value, dtype=np.uint8)
+        check(self.L.wf_scene_get_tlas(self.h, ptr(out), ctypes.byref(n)))
+        return out
+
+    # ---- rendering
+    def render(self, max_bounces=3, spp=1, frame_seed=1, nee=0, rr_start_depth=0xFFFFFFFF, accumulate=True,
+               cosine=1, env_strength=1.0, wave_paths=0, profile=False, count_traffic=False, view_mode=0):
+        s = RenderSettings(1, 1, view_mode, max_bounces, cosine, int(accumulate), env_strength)
+        o = RenderOptions(spp, nee, rr_start_depth, wave_paths, int(profile), int(count_traffic))
+        check(self.L.wf_render(self.h, ctypes.byref(s), ctypes.byref(o), frame_seed))
+
+    def read_image(self):
+        out = np.zeros((self.height, self.width, 4), dtype=np.float32)
+        check(self.L.wf_read_image(self.h, ptr(out), out.size))
+        return out
+
+    def read_image_ldr(self):
+        out = np.zeros((self.height, self.width, 4), dtype=np.uint8)
+        check(self.L.wf_read_image_ldr(self.h, ptr(out), out.size))
+        return out
+
+    def stats(self):
+        s = Stats()
+        check(self.L.wf_get_stats(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def synchronize(self):
+        check(self.L.wf_synchronize(self.h))
+
+    def stream(self):
+        p = ctypes.c_void_p()
+        check(self.L.wf_get_stream(self.h, ctypes.byref(p)))
+        return p.value
+
+    # ---- queries and builders
+    def trace(self, rays, any_hit=False, no_cull=False):
+        rays = np.ascontiguousarray(rays, dtype=ray_dtype)
+        hits = np.zeros(len(rays), dtype=hit_dtype)
+        flags = (abi.TRACE_ANY_HIT if any_hit else 0) | (abi.TRACE_NO_CULL if no_cull else 0)
+        check(self.L.wf_trace(self.h, ptr(rays), len(rays), ptr(hits), flags))
+        return hits
+
+    def trace_device(self, d_rays, n, d_hits, any_hit=False, no_cull=False):
+        flags = (abi.TRACE_ANY_HIT if any_hit else 0) | (abi.TRACE_NO_CULL if no_cull else 0)
+        check(self.L.wf_trace_device(self.h, ctypes.c_void_p(d_rays), n, ctypes.c_void_p(d_hits), flags))
+
+    def bvh_build(self, tris, interval_count=8, subdivide_single_prim=False, max_leaf_prims=0):
+        tris = np.ascontiguousarray(tris, dtype=triangle_dtype)
+        o = BvhOptions(interval_count, int(subdivide_single_prim), max_leaf_prims)
+        n = ctypes.c_uint64(0)
+        self.L.wf_bvh_build(self.h, ptr(tris), len(tris), ctypes.byref(o), None, ctypes.byref(n))
+        out = np.zeros(n.value, dtype=np.uint8)
+        check(self.L.wf_bvh_build(self.h, ptr(tris), len(tris), ctypes.byref(o), ptr(out), ctypes.byref(n)))
+        return out
+
+    def tlas_build(self, instances):
+        inst = np.ascontiguousarray(instances, dtype=bvh_instance_dtype)
+        n = ctypes.c_uint64(0)
+        self.L.wf_tlas_build(self.h, ptr(inst), len(inst), None, ctypes.byref(n))
+        out = np.zeros(n.value, dtype=np.uint8)
+        check(self.L.wf_tlas_build(self.h, ptr(inst), len(inst), ptr(out), ctypes.byref(n)))
+        return out
+
+
+__all__ = ["Renderer", "WFError", "load", "check", "abi", "SIGNATURES", "View", "LIB_PATH"]

@@ -1,0 +1,1014 @@
+// wf_api.cu — the C ABI (include/wf.h): context, meshes, scene, wavefront
+// orchestration, ray queries and the stand-alone builders.
+//
+// The orchestration mirrors renderer::render (renderer.cpp:742-939): per
+// wave, generate once, then for depth 0..max_bounces extend -> shade ->
+// connect.  The reference sizes its indirect dispatches on the GPU
+// (init_args.hlsl:15-22); here every stage reads its queue length from device
+// memory and runs a grid-stride loop, so the host never reads a count back.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/wf.h"
+#include "wf_bvh.h"
+#include "wf_kernels.h"
+
+using namespace wf;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+    g_error = msg;
+    return code;
+}
+
+#define WF_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) {                                                               \
+            return fail(e_ == cudaErrorMemoryAllocation ? WF_ERR_OOM : WF_ERR_CUDA,            \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+        }                                                                                      \
+    } while (0)
+
+template <typename T>
+int dev_alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(WF_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    return WF_OK;
+}
+
+template <typename T>
+void dev_free(T*& p) {
+    if (p) cudaFree(const_cast<void*>(reinterpret_cast<const void*>(p)));
+    p = nullptr;
+}
+
+// Grow-only device buffer.
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    int reserve(size_t n) {
+        if (n <= cap && p) return WF_OK;
+        dev_free(p);
+        cap = 0;
+        int rc = dev_alloc(&p, n);
+        if (rc == WF_OK) cap = n ? n : 1;
+        return rc;
+    }
+    void release() { dev_free(p); cap = 0; }
+};
+
+struct Mesh {
+    uint32_t tri_count = 0, node_count = 0;
+    std::vector<triangle_t> tris;     // original order (create_render_mesh keeps them too)
+    std::vector<uint8_t> blob;        // [bvh_header_t | nodes | bvh_triangle_t | uint32]
+    float root_min[3], root_max[3];
+    float4* d_nodes = nullptr;
+    float4* d_tris = nullptr;         // traversal triangles, leaf order
+    float4* d_stri = nullptr;         // shading triangles, original order
+};
+
+struct Instance {
+    uint32_t mesh;
+    float l2w[16], w2l[16];
+    material_t mat;
+    uint32_t bsdf;
+    float ior;
+    bvh_instance_t bi;
+};
+
+struct EventPair {
+    cudaEvent_t a, b;
+    int stage;
+};
+
+enum Stage { ST_GENERATE = 0, ST_EXTEND, ST_SHADE, ST_CONNECT, ST_POST, ST_TLAS, ST_COUNT };
+
+}  // namespace
+
+struct wf_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t width = 0, height = 0, capacity = 0;
+    std::vector<Mesh> meshes;
+    std::vector<Instance> instances;
+    view_t view{};
+    bool view_valid = false, in_scene = false, scene_ready = false, view_changed = true;
+    float env[3] = {1.0f, 1.0f, 1.0f};
+
+    // device scene
+    DevBuf<float4> tnodes, tinst, sinst;
+    DevBuf<BlasRef> blas;
+    DevBuf<const float4*> stri;
+    DevBuf<LightTri> lights;
+    DevBuf<float> aabbs;
+    DevBuf<uint32_t> tlas_scratch;
+    uint32_t light_count = 0;
+    float light_total = 0.0f;
+    std::vector<bvh_instance_t> scene_bi;
+
+    // wavefront buffers
+    bool buffers_ready = false;
+    RenderBuffers B{};
+    float4* accum = nullptr;
+    uint32_t accum_samples = 0;
+    unsigned long long* totals = nullptr;   // [0] extension rays, [1] shadow rays
+    DevBuf<float4> image;
+    DevBuf<uchar4> image_ldr;
+    DevBuf<uint8_t> trace_io;
+    uint32_t* status = nullptr;
+    Counters* counters = nullptr;
+
+    // timing
+    std::vector<EventPair> events;
+    size_t events_used = 0;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    bool timing_pending = false;
+    wf_stats stats{};
+    uint64_t launches = 0, launches_extend = 0, launches_connect = 0;
+    bool count_traffic = false;
+};
+
+namespace {
+
+int use_device(wf_ctx* c) {
+    WF_CUDA(cudaSetDevice(c->device));
+    return WF_OK;
+}
+
+// Records an event pair around a stage when profiling.
+struct StageTimer {
+    wf_ctx* c;
+    EventPair* ev = nullptr;
+    StageTimer(wf_ctx* ctx, bool on, int stage) : c(ctx) {
+        if (!on) return;
+        if (c->events_used == c->events.size()) {
+            EventPair p{};
+            cudaEventCreate(&p.a);
+            cudaEventCreate(&p.b);
+            c->events.push_back(p);
+        }
+        ev = &c->events[c->events_used++];
+        ev->stage = stage;
+        cudaEventRecord(ev->a, c->stream);
+    }
+    ~StageTimer() {
+        if (ev) cudaEventRecord(ev->b, c->stream);
+    }
+};
+
+// 4x4 inverse by cofactor expansion in double precision, rounded to float.
+// Input and output are glm column-major (m[4*col + row]).
+bool invert4(const float* m, float* out) {
+    double a[4][4];
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) a[r][c] = m[4 * c + r];
+    double inv[4][4];
+    double det = 0.0;
+    auto minor3 = [&](int rr, int cc) {
+        double s[3][3];
+        for (int r = 0, i = 0; r < 4; ++r) {
+            if (r == rr) continue;
+            for (int c2 = 0, j = 0; c2 < 4; ++c2) {
+                if (c2 == cc) continue;
+                s[i][j++] = a[r][c2];
+            }
+            ++i;
+        }
+        return s[0][0] * (s[1][1] * s[2][2] - s[1][2] * s[2][1]) - s[0][1] * (s[1][0] * s[2][2] - s[1][2] * s[2][0]) +
+               s[0][2] * (s[1][0] * s[2][1] - s[1][1] * s[2][0]);
+    };
+    double cof[4][4];
+    for (int r = 0; r < 4; ++r)
+        for (int c2 = 0; c2 < 4; ++c2) cof[r][c2] = (((r + c2) & 1) ? -1.0 : 1.0) * minor3(r, c2);
+    for (int c2 = 0; c2 < 4; ++c2) det += a[0][c2] * cof[0][c2];
+    if (!(std::fabs(det) > 0.0) || !std::isfinite(det)) return false;
+    for (int r = 0; r < 4; ++r)
+        for (int c2 = 0; c2 < 4; ++c2) inv[r][c2] = cof[c2][r] / det;
+    for (int c2 = 0; c2 < 4; ++c2)
+        for (int r = 0; r < 4; ++r) out[4 * c2 + r] = (float)inv[r][c2];
+    return true;
+}
+
+// glm mat4 * vec4 (type_mat4x4.inl): (m0*v0 + m1*v1) + (m2*v2 + m3*v3).
+void glm_mul_point(const float* m, const float v[3], float out[3]) {
+    for (int j = 0; j < 3; ++j) {
+        float a0 = m[j] * v[0];
+        float a1 = m[4 + j] * v[1];
+        float a2 = m[8 + j] * v[2];
+        float a3 = m[12 + j] * 1.0f;
+        out[j] = (a0 + a1) + (a2 + a3);
+    }
+}
+
+// HLSL mul(float4(v, w), M) order, as the kernels and the oracle evaluate it.
+void hlsl_xform(const float* m, const float v[3], float w, float out[3]) {
+    for (int j = 0; j < 3; ++j) out[j] = v[0] * m[j] + v[1] * m[4 + j] + v[2] * m[8 + j] + w * m[12 + j];
+}
+
+int check_blob(const void* blob, uint64_t size, uint32_t n, uint32_t* out_nodes) {
+    if (size < 12) return fail(WF_ERR_INVALID, "BLAS blob shorter than its header");
+    bvh_header_t h;
+    std::memcpy(&h, blob, 12);
+    if (h.nodes_offset != 12 || h.triangles_offset < 12 || ((h.triangles_offset - 12) % 32) != 0)
+        return fail(WF_ERR_INVALID, "BLAS blob header offsets are not [header | nodes | ...]");
+    uint64_t nc = (h.triangles_offset - 12) / 32;
+    if (nc < 2) return fail(WF_ERR_INVALID, "BLAS blob has fewer than 2 nodes");
+    if ((uint64_t)h.indices_offset != (uint64_t)h.triangles_offset + 36ull * n ||
+        size != (uint64_t)h.indices_offset + 4ull * n)
+        return fail(WF_ERR_INVALID, "BLAS blob size does not match the triangle count");
+    const uint8_t* b = static_cast<const uint8_t*>(blob);
+    for (uint64_t i = 0; i < nc; ++i) {
+        if (i == 1) continue;
+        bvh_node_t node;
+        std::memcpy(&node, b + 12 + 32 * i, 32);
+        if (node.prim_count > 0) {
+            if ((uint64_t)node.left_first + node.prim_count > n) return fail(WF_ERR_INVALID, "BLAS leaf range out of bounds");
+        } else if (!(node.left_first > i && (uint64_t)node.left_first + 1 < nc)) {
+            // children are allocated after their parent, which also rules out cycles
+            return fail(WF_ERR_INVALID, "BLAS child index out of range or not after its parent");
+        }
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t t;
+        std::memcpy(&t, b + h.indices_offset + 4ull * i, 4);
+        if (t >= n) return fail(WF_ERR_INVALID, "BLAS index list entry out of range");
+    }
+    *out_nodes = (uint32_t)nc;
+    return WF_OK;
+}
+
+void free_mesh(Mesh& m) {
+    dev_free(m.d_nodes);
+    dev_free(m.d_tris);
+    dev_free(m.d_stri);
+}
+
+int upload_shading_tris(wf_ctx* c, Mesh& m) {
+    std::vector<float4> st(6ull * m.tri_count);
+    for (uint32_t i = 0; i < m.tri_count; ++i) {
+        const triangle_t& t = m.tris[i];
+        const vertex_t* v[3] = {&t.v0, &t.v1, &t.v2};
+        for (int k = 0; k < 3; ++k) {
+            st[6ull * i + k] = make_float4(v[k]->position[0], v[k]->position[1], v[k]->position[2], 0.0f);
+            st[6ull * i + 3 + k] = make_float4(v[k]->normal[0], v[k]->normal[1], v[k]->normal[2], 0.0f);
+        }
+    }
+    int rc = dev_alloc(&m.d_stri, st.size());
+    if (rc) return rc;
+    WF_CUDA(cudaMemcpyAsync(m.d_stri, st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    return WF_OK;
+}
+
+// Device copies of a BLAS given as a blob (host).
+int upload_blob(wf_ctx* c, Mesh& m) {
+    bvh_header_t h;
+    std::memcpy(&h, m.blob.data(), 12);
+    std::vector<float4> nodes(2ull * m.node_count);
+    std::memcpy(nodes.data(), m.blob.data() + 12, 32ull * m.node_count);
+    std::vector<float4> tt(3ull * m.tri_count);
+    const uint8_t* tb = m.blob.data() + h.triangles_offset;
+    const uint8_t* ib = m.blob.data() + h.indices_offset;
+    for (uint32_t i = 0; i < m.tri_count; ++i) {
+        uint32_t t;
+        std::memcpy(&t, ib + 4ull * i, 4);
+        bvh_triangle_t tri;
+        std::memcpy(&tri, tb + 36ull * t, 36);
+        float e1[3], e2[3];
+        for (int a = 0; a < 3; ++a) { e1[a] = tri.p1[a] - tri.p0[a]; e2[a] = tri.p2[a] - tri.p0[a]; }
+        float w;
+        std::memcpy(&w, &t, 4);
+        tt[3ull * i] = make_float4(tri.p0[0], tri.p0[1], tri.p0[2], w);
+        tt[3ull * i + 1] = make_float4(e1[0], e1[1], e1[2], 0.0f);
+        tt[3ull * i + 2] = make_float4(e2[0], e2[1], e2[2], 0.0f);
+    }
+    bvh_node_t root;
+    std::memcpy(&root, m.blob.data() + 12, 32);
+    std::memcpy(m.root_min, root.aabb_min, 12);
+    std::memcpy(m.root_max, root.aabb_max, 12);
+    int rc = dev_alloc(&m.d_nodes, nodes.size());
+    if (rc) return rc;
+    rc = dev_alloc(&m.d_tris, tt.size());
+    if (rc) return rc;
+    WF_CUDA(cudaMemcpyAsync(m.d_nodes, nodes.data(), nodes.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    WF_CUDA(cudaMemcpyAsync(m.d_tris, tt.data(), tt.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    return WF_OK;
+}
+
+int ensure_buffers(wf_ctx* c) {
+    if (c->buffers_ready) return WF_OK;
+    const size_t C = c->capacity, npix = (size_t)c->width * c->height;
+    RenderBuffers& B = c->B;
+    int rc = 0;
+    for (int k = 0; k < 2; ++k) {
+        if ((rc = dev_alloc(&B.q_o[k], C)) || (rc = dev_alloc(&B.q_d[k], C)) || (rc = dev_alloc(&B.q_path[k], C)))
+            return rc;
+    }
+    if ((rc = dev_alloc(&B.h_tuvp, C)) || (rc = dev_alloc(&B.h_inst, C)) || (rc = dev_alloc(&B.ps_T, C)) ||
+        (rc = dev_alloc(&B.ps_flags, C)) || (rc = dev_alloc(&B.s_o, C)) || (rc = dev_alloc(&B.s_d, C)) ||
+        (rc = dev_alloc(&B.s_c, C)) || (rc = dev_alloc(&B.counts, 2 * kMaxDepth)) || (rc = dev_alloc(&c->accum, npix)))
+        return rc;
+    B.accum = c->accum;
+    B.status = c->status;
+    B.counters = c->counters;
+    WF_CUDA(cudaMemsetAsync(c->accum, 0, npix * sizeof(float4), c->stream));
+    c->accum_samples = 0;
+    c->buffers_ready = true;
+    return WF_OK;
+}
+
+void release_buffers(wf_ctx* c) {
+    RenderBuffers& B = c->B;
+    for (int k = 0; k < 2; ++k) { dev_free(B.q_o[k]); dev_free(B.q_d[k]); dev_free(B.q_path[k]); }
+    dev_free(B.h_tuvp); dev_free(B.h_inst); dev_free(B.ps_T); dev_free(B.ps_flags);
+    dev_free(B.s_o); dev_free(B.s_d); dev_free(B.s_c); dev_free(B.counts);
+    dev_free(c->accum);
+    c->buffers_ready = false;
+}
+
+SceneRefs scene_refs(wf_ctx* c) {
+    SceneRefs S;
+    S.tnodes = c->tnodes.p;
+    S.tinst = c->tinst.p;
+    S.blas = c->blas.p;
+    S.inst_count = (uint32_t)c->scene_bi.size();
+    return S;
+}
+
+// Reads and clears the device status word (after a synchronization).
+int take_status(wf_ctx* c) {
+    uint32_t s = 0;
+    WF_CUDA(cudaMemcpy(&s, c->status, 4, cudaMemcpyDeviceToHost));
+    if (s) WF_CUDA(cudaMemset(c->status, 0, 4));
+    if (s & ERRF_STACK) return fail(WF_ERR_STACK, "a traversal stack overflowed; affected rays report a miss");
+    if (s & ERRF_TIMEOUT) return fail(WF_ERR_TIMEOUT, "a bounded device wait gave up");
+    if (s & ERRF_CAPACITY) return fail(WF_ERR_CAPACITY, "a device queue overflowed");
+    return WF_OK;
+}
+
+int finish_timing(wf_ctx* c) {
+    if (!c->timing_pending) return WF_OK;
+    WF_CUDA(cudaEventSynchronize(c->t1));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, c->t0, c->t1);
+    c->stats.ms_total = ms;
+    double st[ST_COUNT] = {0, 0, 0, 0, 0, 0};
+    for (size_t i = 0; i < c->events_used; ++i) {
+        float e = 0.0f;
+        cudaEventElapsedTime(&e, c->events[i].a, c->events[i].b);
+        st[c->events[i].stage] += e;
+    }
+    c->stats.ms_generate = st[ST_GENERATE];
+    c->stats.ms_extend = st[ST_EXTEND];
+    c->stats.ms_shade = st[ST_SHADE];
+    c->stats.ms_connect = st[ST_CONNECT];
+    c->stats.ms_post = st[ST_POST];
+    c->stats.ms_tlas_build = st[ST_TLAS];
+    unsigned long long tot[2] = {0, 0};
+    WF_CUDA(cudaMemcpy(tot, c->totals, sizeof(tot), cudaMemcpyDeviceToHost));
+    c->stats.rays_extend = tot[0];
+    c->stats.rays_connect = tot[1];
+    if (c->count_traffic) {
+        Counters k[2];
+        WF_CUDA(cudaMemcpy(k, c->counters, sizeof(k), cudaMemcpyDeviceToHost));
+        c->stats.tlas_node_loads = k[0].tlas_node_loads;
+        c->stats.instance_loads = k[0].instance_loads;
+        c->stats.blas_node_loads = k[0].blas_node_loads;
+        c->stats.triangle_tests = k[0].triangle_tests;
+        c->stats.shadow_tlas_node_loads = k[1].tlas_node_loads;
+        c->stats.shadow_instance_loads = k[1].instance_loads;
+        c->stats.shadow_blas_node_loads = k[1].blas_node_loads;
+        c->stats.shadow_triangle_tests = k[1].triangle_tests;
+    }
+    c->timing_pending = false;
+    return WF_OK;
+}
+
+int begin_call(wf_ctx* c, bool count_traffic) {
+    int rc = finish_timing(c);
+    if (rc) return rc;
+    std::memset(&c->stats, 0, sizeof(c->stats));
+    c->events_used = 0;
+    c->launches = c->launches_extend = c->launches_connect = 0;
+    c->count_traffic = count_traffic;
+    WF_CUDA(cudaMemsetAsync(c->totals, 0, 2 * sizeof(unsigned long long), c->stream));
+    WF_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(Counters), c->stream));
+    WF_CUDA(cudaEventRecord(c->t0, c->stream));
+    return WF_OK;
+}
+
+int end_call(wf_ctx* c) {
+    WF_CUDA(cudaEventRecord(c->t1, c->stream));
+    c->timing_pending = true;
+    c->stats.launches = c->launches;
+    c->stats.launches_extend = c->launches_extend;
+    c->stats.launches_connect = c->launches_connect;
+    return WF_OK;
+}
+
+}  // namespace
+
+// ============================================================================ C ABI
+
+extern "C" {
+
+const char* wf_status_string(int s) {
+    switch (s) {
+        case WF_OK: return "ok";
+        case WF_ERR_INVALID: return "invalid argument";
+        case WF_ERR_OOM: return "out of memory";
+        case WF_ERR_CAPACITY: return "capacity exceeded";
+        case WF_ERR_TIMEOUT: return "device wait timed out";
+        case WF_ERR_STACK: return "traversal stack overflow";
+        case WF_ERR_CUDA: return "CUDA error";
+        case WF_ERR_STATE: return "call out of order";
+        default: return "unknown status";
+    }
+}
+
+const char* wf_last_error(void) { return g_error.c_str(); }
+
+int wf_abi_version(void) { return WF_ABI_VERSION; }
+
+int wf_create(const wf_init_params* p, wf_ctx** out) {
+    if (!p || !out) return fail(WF_ERR_INVALID, "wf_create: null argument");
+    *out = nullptr;
+    if (p->render_width == 0 || p->render_height == 0 || p->render_width > 16384 || p->render_height > 16384)
+        return fail(WF_ERR_INVALID, "wf_create: render size must be 1..16384 per side");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(WF_ERR_CUDA, std::string("wf_create: no CUDA device: ") + cudaGetErrorString(e));
+    }
+    if (p->device < 0 || p->device >= ndev) return fail(WF_ERR_INVALID, "wf_create: device ordinal out of range");
+    wf_ctx* c = new wf_ctx();
+    c->device = p->device;
+    c->width = p->render_width;
+    c->height = p->render_height;
+    const uint64_t npix = (uint64_t)c->width * c->height;
+    c->capacity = p->wave_capacity ? (uint32_t)std::min<uint64_t>(p->wave_capacity, npix) : (uint32_t)npix;
+    int rc = use_device(c);
+    if (rc == WF_OK) {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreate(&c->t0) != cudaSuccess || cudaEventCreate(&c->t1) != cudaSuccess) {
+            rc = fail(WF_ERR_CUDA, "wf_create: stream/event creation failed");
+        }
+    }
+    if (rc == WF_OK) rc = dev_alloc(&c->status, 1);
+    if (rc == WF_OK) rc = dev_alloc(&c->counters, 2);
+    if (rc == WF_OK) rc = dev_alloc(&c->totals, 2);
+    if (rc == WF_OK) {
+        cudaMemset(c->status, 0, 4);
+        cudaMemset(c->counters, 0, 2 * sizeof(Counters));
+        cudaMemset(c->totals, 0, 2 * sizeof(unsigned long long));
+        if (cudaDeviceSynchronize() != cudaSuccess) rc = fail(WF_ERR_CUDA, "wf_create: device initialization failed");
+    }
+    if (rc != WF_OK) {
+        wf_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return WF_OK;
+}
+
+int wf_destroy(wf_ctx* c) {
+    if (!c) return WF_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (Mesh& m : c->meshes) free_mesh(m);
+    release_buffers(c);
+    c->tnodes.release(); c->tinst.release(); c->sinst.release(); c->blas.release(); c->stri.release();
+    c->lights.release(); c->aabbs.release(); c->tlas_scratch.release();
+    c->image.release(); c->image_ldr.release(); c->trace_io.release();
+    dev_free(c->status); dev_free(c->counters); dev_free(c->totals);
+    for (EventPair& p : c->events) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    if (c->t0) cudaEventDestroy(c->t0);
+    if (c->t1) cudaEventDestroy(c->t1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return WF_OK;
+}
+
+int wf_get_stream(wf_ctx* c, void** out) {
+    if (!c || !out) return fail(WF_ERR_INVALID, "wf_get_stream: null argument");
+    *out = (void*)c->stream;
+    return WF_OK;
+}
+
+int wf_synchronize(wf_ctx* c) {
+    if (!c) return fail(WF_ERR_INVALID, "wf_synchronize: null context");
+    int rc = use_device(c);
+    if (rc) return rc;
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    return take_status(c);
+}
+
+// ---------------------------------------------------------------------------- meshes
+
+static int add_mesh(wf_ctx* c, Mesh&& m, uint32_t* out_mesh) {
+    c->meshes.push_back(std::move(m));
+    *out_mesh = (uint32_t)(c->meshes.size() - 1);
+    c->scene_ready = false;
+    return WF_OK;
+}
+
+int wf_mesh_create_prebuilt(wf_ctx* c, const triangle_t* tris, uint32_t n, const void* blob, uint64_t size,
+                            uint32_t* out_mesh) {
+    if (!c || !tris || !blob || !out_mesh || n == 0) return fail(WF_ERR_INVALID, "wf_mesh_create_prebuilt: bad argument");
+    int rc = use_device(c);
+    if (rc) return rc;
+    Mesh m;
+    if ((rc = check_blob(blob, size, n, &m.node_count))) return rc;
+    m.tri_count = n;
+    m.tris.assign(tris, tris + n);
+    m.blob.assign(static_cast<const uint8_t*>(blob), static_cast<const uint8_t*>(blob) + size);
+    if ((rc = upload_blob(c, m)) || (rc = upload_shading_tris(c, m))) {
+        free_mesh(m);
+        return rc;
+    }
+    return add_mesh(c, std::move(m), out_mesh);
+}
+
+int wf_mesh_create(wf_ctx* c, const vertex_t* vertices, uint32_t nv, const uint32_t* indices, uint32_t ni,
+                   const wf_bvh_options* opts, uint32_t* out_mesh) {
+    if (!c || !vertices || !indices || !out_mesh || ni < 3 || ni % 3 != 0)
+        return fail(WF_ERR_INVALID, "wf_mesh_create: bad argument");
+    const uint32_t n = ni / 3;
+    std::vector<triangle_t> tris(n);
+    for (uint32_t t = 0; t < n; ++t) {
+        uint32_t a = indices[3 * t], b = indices[3 * t + 1], d = indices[3 * t + 2];
+        if (a >= nv || b >= nv || d >= nv) return fail(WF_ERR_INVALID, "wf_mesh_create: index out of range");
+        tris[t].v0 = vertices[a];
+        tris[t].v1 = vertices[b];
+        tris[t].v2 = vertices[d];
+    }
+    wf_bvh_options o = opts ? *opts : wf_bvh_options{8, 0, 0};
+    int rc = use_device(c);
+    if (rc) return rc;
+    Mesh m;
+    m.tri_count = n;
+    m.tris = std::move(tris);
+    BvhBuildOut bo;
+    if ((rc = gpu_bvh_build(m.tris.data(), n, o, c->stream, &bo))) return fail(rc, bvh_last_error());
+    m.node_count = bo.node_count;
+    m.d_nodes = bo.d_nodes;
+    m.d_tris = bo.d_tris;
+    m.blob = std::move(bo.blob);
+    std::memcpy(m.root_min, bo.root_min, 12);
+    std::memcpy(m.root_max, bo.root_max, 12);
+    if ((rc = upload_shading_tris(c, m))) {
+        free_mesh(m);
+        return rc;
+    }
+    return add_mesh(c, std::move(m), out_mesh);
+}
+
+int wf_mesh_get_blas(wf_ctx* c, uint32_t mesh, void* out, uint64_t* inout_size) {
+    if (!c || !inout_size || mesh >= c->meshes.size()) return fail(WF_ERR_INVALID, "wf_mesh_get_blas: bad argument");
+    const std::vector<uint8_t>& b = c->meshes[mesh].blob;
+    if (!out || *inout_size < b.size()) {
+        *inout_size = b.size();
+        return fail(WF_ERR_CAPACITY, "wf_mesh_get_blas: output buffer too small");
+    }
+    std::memcpy(out, b.data(), b.size());
+    *inout_size = b.size();
+    return WF_OK;
+}
+
+// ---------------------------------------------------------------------------- scene
+
+int wf_scene_begin(wf_ctx* c, const view_t* view, const wf_env* env) {
+    if (!c || !view) return fail(WF_ERR_INVALID, "wf_scene_begin: null argument");
+    // begin_scene resets accumulation when the view changes (renderer.cpp:601-604)
+    c->view_changed = !c->view_valid || std::memcmp(&c->view.world_to_view, view->world_to_view, 64) != 0;
+    c->view = *view;
+    c->view_valid = true;
+    if (env) std::memcpy(c->env, env->color, 12);
+    else c->env[0] = c->env[1] = c->env[2] = 1.0f;
+    c->instances.clear();
+    c->in_scene = true;
+    c->scene_ready = false;
+    return WF_OK;
+}
+
+static int submit(wf_ctx* c, uint32_t mesh, const float* l2w, const material_t* mat, uint32_t bsdf, float ior) {
+    if (!c || !l2w || !mat) return fail(WF_ERR_INVALID, "wf_instance_submit: null argument");
+    if (!c->in_scene) return fail(WF_ERR_STATE, "wf_instance_submit: outside wf_scene_begin/wf_scene_end");
+    if (mesh >= c->meshes.size()) return fail(WF_ERR_INVALID, "wf_instance_submit: unknown mesh");
+    if (bsdf > WF_BSDF_DIELECTRIC) return fail(WF_ERR_INVALID, "wf_instance_submit: unknown BSDF");
+    if (c->instances.size() >= 32768) return fail(WF_ERR_CAPACITY, "wf_instance_submit: more than 32768 instances");
+    Instance in{};
+    in.mesh = mesh;
+    std::memcpy(in.l2w, l2w, 64);
+    if (!invert4(l2w, in.w2l)) return fail(WF_ERR_INVALID, "wf_instance_submit: transform is not invertible");
+    in.mat = *mat;
+    in.bsdf = bsdf;
+    in.ior = ior;
+    std::memcpy(in.bi.world_to_local, in.w2l, 64);
+    in.bi.bvh_index = mesh;
+    // world AABB of the BLAS root box (renderer.cpp:1324-1336), grown from
+    // +/-FLT_MAX; the reference grows it from a zeroed box, so its box also
+    // always contains the origin.
+    const Mesh& m = c->meshes[mesh];
+    for (int a = 0; a < 3; ++a) { in.bi.aabb_min[a] = FLT_MAX; in.bi.aabb_max[a] = -FLT_MAX; }
+    for (uint32_t i = 0; i < 8; ++i) {
+        float corner[3] = {(i & 1) ? m.root_max[0] : m.root_min[0], (i & 2) ? m.root_max[1] : m.root_min[1],
+                           (i & 4) ? m.root_max[2] : m.root_min[2]};
+        float w[3];
+        glm_mul_point(l2w, corner, w);
+        for (int a = 0; a < 3; ++a) {
+            in.bi.aabb_min[a] = (w[a] < in.bi.aabb_min[a]) ? w[a] : in.bi.aabb_min[a];
+            in.bi.aabb_max[a] = (in.bi.aabb_max[a] < w[a]) ? w[a] : in.bi.aabb_max[a];
+        }
+    }
+    c->instances.push_back(in);
+    return WF_OK;
+}
+
+int wf_instance_submit(wf_ctx* c, uint32_t mesh, const float l2w[16], const material_t* mat) {
+    return submit(c, mesh, l2w, mat, WF_BSDF_LAMBERT, 1.5f);
+}
+
+int wf_instance_submit_ex(wf_ctx* c, uint32_t mesh, const float l2w[16], const wf_material_ext* mat) {
+    if (!mat) return fail(WF_ERR_INVALID, "wf_instance_submit_ex: null material");
+    return submit(c, mesh, l2w, &mat->base, mat->bsdf, mat->ior);
+}
+
+int wf_scene_end(wf_ctx* c) {
+    if (!c) return fail(WF_ERR_INVALID, "wf_scene_end: null context");
+    if (!c->in_scene) return fail(WF_ERR_STATE, "wf_scene_end: no wf_scene_begin");
+    int rc = use_device(c);
+    if (rc) return rc;
+    const uint32_t n = (uint32_t)c->instances.size();
+    const uint32_t nm = (uint32_t)c->meshes.size();
+    // per-mesh device tables
+    {
+        std::vector<BlasRef> br(nm ? nm : 1);
+        std::vector<const float4*> sp(nm ? nm : 1);
+        for (uint32_t i = 0; i < nm; ++i) {
+            br[i].nodes = c->meshes[i].d_nodes;
+            br[i].tris = c->meshes[i].d_tris;
+            sp[i] = c->meshes[i].d_stri;
+        }
+        if ((rc = c->blas.reserve(br.size())) || (rc = c->stri.reserve(sp.size()))) return rc;
+        WF_CUDA(cudaMemcpyAsync(c->blas.p, br.data(), br.size() * sizeof(BlasRef), cudaMemcpyHostToDevice, c->stream));
+        WF_CUDA(cudaMemcpyAsync(c->stri.p, sp.data(), sp.size() * sizeof(void*), cudaMemcpyHostToDevice, c->stream));
+    }
+    // per-instance data
+    std::vector<float> aabbs(6ull * n);
+    std::vector<float4> ti(4ull * n), si(6ull * n);
+    c->scene_bi.resize(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const Instance& in = c->instances[i];
+        c->scene_bi[i] = in.bi;
+        std::memcpy(&aabbs[6ull * i], in.bi.aabb_min, 12);
+        std::memcpy(&aabbs[6ull * i + 3], in.bi.aabb_max, 12);
+        float meshf, bsdff;
+        std::memcpy(&meshf, &in.mesh, 4);
+        std::memcpy(&bsdff, &in.bsdf, 4);
+        const float* w = in.w2l;
+        ti[4ull * i] = make_float4(w[0], w[1], w[2], meshf);
+        ti[4ull * i + 1] = make_float4(w[4], w[5], w[6], 0.0f);
+        ti[4ull * i + 2] = make_float4(w[8], w[9], w[10], 0.0f);
+        ti[4ull * i + 3] = make_float4(w[12], w[13], w[14], 0.0f);
+        const float* l = in.l2w;
+        const material_t& mt = in.mat;
+        si[6ull * i] = make_float4(l[0], l[1], l[2], meshf);
+        si[6ull * i + 1] = make_float4(l[4], l[5], l[6], bsdff);
+        si[6ull * i + 2] = make_float4(l[8], l[9], l[10], in.ior);
+        si[6ull * i + 3] = make_float4(l[12], l[13], l[14], mt.roughness_factor);
+        si[6ull * i + 4] = make_float4(mt.base_color_factor[0], mt.base_color_factor[1], mt.base_color_factor[2],
+                                       mt.metallic_factor);
+        si[6ull * i + 5] = make_float4(mt.emissive_strength * mt.emissive_factor[0],
+                                       mt.emissive_strength * mt.emissive_factor[1],
+                                       mt.emissive_strength * mt.emissive_factor[2], 0.0f);
+    }
+    if ((rc = c->tnodes.reserve(2ull * std::max<uint32_t>(2 * n, 1))) || (rc = c->tinst.reserve(ti.size())) ||
+        (rc = c->sinst.reserve(si.size())) || (rc = c->aabbs.reserve(aabbs.size())) ||
+        (rc = c->tlas_scratch.reserve(7ull * n + 1)))
+        return rc;
+    WF_CUDA(cudaMemsetAsync(c->tnodes.p, 0, 32, c->stream));
+    if (n) {
+        WF_CUDA(cudaMemcpyAsync(c->aabbs.p, aabbs.data(), aabbs.size() * 4, cudaMemcpyHostToDevice, c->stream));
+        WF_CUDA(cudaMemcpyAsync(c->tinst.p, ti.data(), ti.size() * 16, cudaMemcpyHostToDevice, c->stream));
+        WF_CUDA(cudaMemcpyAsync(c->sinst.p, si.data(), si.size() * 16, cudaMemcpyHostToDevice, c->stream));
+        StageTimer st(c, true, ST_TLAS);
+        WF_CUDA(launch_tlas_build(c->aabbs.p, n, c->tnodes.p, c->tlas_scratch.p, c->stream));
+        c->launches++;
+    }
+    // emitter table (every triangle of every emissive instance, world space)
+    std::vector<LightTri> lt;
+    float run = 0.0f;
+    for (uint32_t i = 0; i < n; ++i) {
+        const Instance& in = c->instances[i];
+        float le[3] = {in.mat.emissive_strength * in.mat.emissive_factor[0],
+                       in.mat.emissive_strength * in.mat.emissive_factor[1],
+                       in.mat.emissive_strength * in.mat.emissive_factor[2]};
+        if (!(le[0] != 0.0f || le[1] != 0.0f || le[2] != 0.0f)) continue;
+        const Mesh& m = c->meshes[in.mesh];
+        for (uint32_t t = 0; t < m.tri_count; ++t) {
+            float p0[3], p1[3], p2[3];
+            hlsl_xform(in.l2w, m.tris[t].v0.position, 1.0f, p0);
+            hlsl_xform(in.l2w, m.tris[t].v1.position, 1.0f, p1);
+            hlsl_xform(in.l2w, m.tris[t].v2.position, 1.0f, p2);
+            float e1[3], e2[3];
+            for (int a = 0; a < 3; ++a) { e1[a] = p1[a] - p0[a]; e2[a] = p2[a] - p0[a]; }
+            float cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            float len = sqrtf(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+            float area = 0.5f * len;
+            float il = 1.0f / len;
+            run = run + area;
+            LightTri L;
+            L.p0 = make_float4(p0[0], p0[1], p0[2], area);
+            L.e1 = make_float4(e1[0], e1[1], e1[2], run);
+            L.e2 = make_float4(e2[0], e2[1], e2[2], 0.0f);
+            L.n = make_float4(cr[0] * il, cr[1] * il, cr[2] * il, 0.0f);
+            L.le = make_float4(le[0], le[1], le[2], 0.0f);
+            lt.push_back(L);
+        }
+    }
+    c->light_count = (uint32_t)lt.size();
+    c->light_total = run;
+    if ((rc = c->lights.reserve(lt.size()))) return rc;
+    if (!lt.empty())
+        WF_CUDA(cudaMemcpyAsync(c->lights.p, lt.data(), lt.size() * sizeof(LightTri), cudaMemcpyHostToDevice, c->stream));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    c->in_scene = false;
+    c->scene_ready = true;
+    return WF_OK;
+}
+
+int wf_scene_get_instances(wf_ctx* c, bvh_instance_t* out, uint32_t cap, uint32_t* count) {
+    if (!c || !count) return fail(WF_ERR_INVALID, "wf_scene_get_instances: null argument");
+    if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_scene_get_instances: no finished scene");
+    *count = (uint32_t)c->scene_bi.size();
+    if (!out || cap < *count) return fail(WF_ERR_CAPACITY, "wf_scene_get_instances: output too small");
+    std::memcpy(out, c->scene_bi.data(), c->scene_bi.size() * sizeof(bvh_instance_t));
+    return WF_OK;
+}
+
+int wf_scene_get_tlas(wf_ctx* c, void* out, uint64_t* inout_size) {
+    if (!c || !inout_size) return fail(WF_ERR_INVALID, "wf_scene_get_tlas: null argument");
+    if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_scene_get_tlas: no finished scene");
+    int rc = use_device(c);
+    if (rc) return rc;
+    const uint32_t n = (uint32_t)c->scene_bi.size();
+    const uint64_t nodes = n ? 2ull * n : 1ull;
+    const uint64_t size = 8 + 32 * nodes + 92ull * n;
+    if (!out || *inout_size < size) {
+        *inout_size = size;
+        return fail(WF_ERR_CAPACITY, "wf_scene_get_tlas: output buffer too small");
+    }
+    uint8_t* o = static_cast<uint8_t*>(out);
+    tlas_header_t h{8u, (uint32_t)(8 + 32 * nodes)};
+    std::memcpy(o, &h, 8);
+    WF_CUDA(cudaMemcpyAsync(o + 8, c->tnodes.p, 32 * nodes, cudaMemcpyDeviceToHost, c->stream));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    if (n) std::memcpy(o + h.instances_offset, c->scene_bi.data(), 92ull * n);
+    *inout_size = size;
+    return WF_OK;
+}
+
+// ---------------------------------------------------------------------------- rendering
+
+int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o, uint32_t frame_seed) {
+    if (!c || !s || !o) return fail(WF_ERR_INVALID, "wf_render: null argument");
+    if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_render: call wf_scene_end first");
+    if (s->max_bounces >= kMaxDepth - 1) return fail(WF_ERR_INVALID, "wf_render: max_bounces must be < 15");
+    if (o->spp == 0) return fail(WF_ERR_INVALID, "wf_render: spp must be >= 1");
+    if (s->render_view_mode != RENDER_VIEW_MODE_NONE)
+        return fail(WF_ERR_INVALID, "wf_render: only RENDER_VIEW_MODE_NONE is implemented");
+    int rc = use_device(c);
+    if (rc) return rc;
+    if ((rc = ensure_buffers(c))) return rc;
+    if ((rc = begin_call(c, o->count_traffic != 0))) return rc;
+    const uint32_t npix = c->width * c->height;
+    if (!s->accumulate || c->view_changed) {
+        WF_CUDA(cudaMemsetAsync(c->accum, 0, (size_t)npix * sizeof(float4), c->stream));
+        c->accum_samples = 0;
+        c->view_changed = false;
+    }
+    const uint32_t wave = o->wave_paths ? std::min(o->wave_paths, c->capacity) : c->capacity;
+    WaveParams W{};
+    for (int k = 0; k < 4; ++k) {
+        const float* m1 = c->view.clip_to_view + 4 * k;
+        const float* m2 = c->view.view_to_world + 4 * k;
+        W.clip_to_view[k] = make_float4(m1[0], m1[1], m1[2], m1[3]);
+        W.view_to_world[k] = make_float4(m2[0], m2[1], m2[2], m2[3]);
+    }
+    W.width = c->width;
+    W.height = c->height;
+    W.dim_x = c->view.render_dim[0];
+    W.dim_y = c->view.render_dim[1];
+    W.frame_seed = frame_seed;
+    W.max_bounces = s->max_bounces;
+    W.nee = o->nee ? 1u : 0u;
+    W.rr_start = o->rr_start_depth;
+    W.cosine = s->cosine_weighted_diffuse ? 1u : 0u;
+    W.env_strength = s->hdr_env_strength;
+    std::memcpy(W.env, c->env, 12);
+    const bool prof = o->profile != 0, cnt = o->count_traffic != 0;
+    const SceneRefs S = scene_refs(c);
+    ShadeRefs SH;
+    SH.sinst = c->sinst.p;
+    SH.stri = c->stri.p;
+    SH.lights = c->lights.p;
+    SH.light_count = c->light_count;
+    SH.light_total = c->light_total;
+    RenderBuffers B = c->B;
+    B.status = c->status;
+    B.counters = c->counters;
+    const bool nee = W.nee && c->light_count > 0;
+    for (uint32_t si = 0; si < o->spp; ++si) {
+        W.sample = c->accum_samples + si;
+        for (uint32_t p0 = 0; p0 < npix; p0 += wave) {
+            W.pix0 = p0;
+            W.npaths = std::min(wave, npix - p0);
+            WF_CUDA(cudaMemsetAsync(B.counts, 0, 2 * kMaxDepth * sizeof(uint32_t), c->stream));
+            {
+                StageTimer t(c, prof, ST_GENERATE);
+                WF_CUDA(launch_generate(B, W, c->stream));
+            }
+            c->launches++;
+            for (uint32_t d = 0; d <= s->max_bounces; ++d) {
+                {
+                    StageTimer t(c, prof, ST_EXTEND);
+                    WF_CUDA(launch_extend(S, B, d, W.npaths, cnt, c->totals, c->stream));
+                }
+                {
+                    StageTimer t(c, prof, ST_SHADE);
+                    WF_CUDA(launch_shade(SH, B, W, d, W.npaths, c->stream));
+                }
+                c->launches += 2;
+                c->launches_extend++;
+                if (nee && d < s->max_bounces) {
+                    StageTimer t(c, prof, ST_CONNECT);
+                    WF_CUDA(launch_connect(S, B, d, W.npaths, cnt, c->totals + 1, c->stream));
+                    c->launches++;
+                    c->launches_connect++;
+                }
+            }
+        }
+    }
+    c->accum_samples += o->spp;
+    c->stats.paths = (uint64_t)npix * o->spp;
+    uint64_t paths = c->stats.paths;
+    rc = end_call(c);
+    c->stats.paths = paths;
+    return rc;
+}
+
+int wf_read_image(wf_ctx* c, float* out, uint64_t nfloat) {
+    if (!c || !out) return fail(WF_ERR_INVALID, "wf_read_image: null argument");
+    const uint64_t npix = (uint64_t)c->width * c->height;
+    if (nfloat < 4 * npix) return fail(WF_ERR_CAPACITY, "wf_read_image: output smaller than width*height*4 floats");
+    if (!c->buffers_ready) return fail(WF_ERR_STATE, "wf_read_image: nothing rendered");
+    int rc = use_device(c);
+    if (rc) return rc;
+    if ((rc = c->image.reserve(npix))) return rc;
+    WF_CUDA(launch_resolve(c->accum, (uint32_t)npix, c->image.p, c->stream));
+    WF_CUDA(cudaMemcpyAsync(out, c->image.p, npix * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    return take_status(c);
+}
+
+int wf_read_image_ldr(wf_ctx* c, uint8_t* out, uint64_t nbytes) {
+    if (!c || !out) return fail(WF_ERR_INVALID, "wf_read_image_ldr: null argument");
+    const uint64_t npix = (uint64_t)c->width * c->height;
+    if (nbytes < 4 * npix) return fail(WF_ERR_CAPACITY, "wf_read_image_ldr: output smaller than width*height*4 bytes");
+    if (!c->buffers_ready) return fail(WF_ERR_STATE, "wf_read_image_ldr: nothing rendered");
+    int rc = use_device(c);
+    if (rc) return rc;
+    if ((rc = c->image_ldr.reserve(npix))) return rc;
+    WF_CUDA(launch_post(c->accum, (uint32_t)npix, 1u, c->image_ldr.p, c->stream));
+    WF_CUDA(cudaMemcpyAsync(out, c->image_ldr.p, npix * 4, cudaMemcpyDeviceToHost, c->stream));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    return take_status(c);
+}
+
+int wf_get_stats(wf_ctx* c, wf_stats* out) {
+    if (!c || !out) return fail(WF_ERR_INVALID, "wf_get_stats: null argument");
+    int rc = use_device(c);
+    if (rc) return rc;
+    if ((rc = finish_timing(c))) return rc;
+    *out = c->stats;
+    return WF_OK;
+}
+
+// ---------------------------------------------------------------------------- ray queries
+
+int wf_trace_device(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* hits, uint32_t flags) {
+    if (!c || (n && (!rays || !hits))) return fail(WF_ERR_INVALID, "wf_trace_device: null argument");
+    if ((reinterpret_cast<uintptr_t>(rays) & 15u) != 0 || (reinterpret_cast<uintptr_t>(hits) & 3u) != 0)
+        return fail(WF_ERR_INVALID, "wf_trace_device: rays must be 16-byte and hits 4-byte aligned");
+    if (flags & ~3u) return fail(WF_ERR_INVALID, "wf_trace_device: unknown flags");
+    if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_trace_device: call wf_scene_end first");
+    int rc = use_device(c);
+    if (rc) return rc;
+    if ((rc = begin_call(c, false))) return rc;
+    {
+        StageTimer t(c, true, ST_EXTEND);
+        WF_CUDA(launch_trace_aos(scene_refs(c), rays, n, hits, flags, false, c->status, c->counters, c->stream));
+    }
+    c->launches++;
+    c->launches_extend++;
+    c->stats.rays_extend = n;
+    rc = end_call(c);
+    return rc;
+}
+
+int wf_trace(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* hits, uint32_t flags) {
+    if (!c || (n && (!rays || !hits))) return fail(WF_ERR_INVALID, "wf_trace: null argument");
+    if (flags & ~3u) return fail(WF_ERR_INVALID, "wf_trace: unknown flags");
+    if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_trace: call wf_scene_end first");
+    if (n == 0) return WF_OK;
+    int rc = use_device(c);
+    if (rc) return rc;
+    const size_t rb = 32ull * n, hb = 20ull * n;
+    if ((rc = c->trace_io.reserve(rb + ((hb + 15) & ~size_t(15))))) return rc;
+    RayDesc2* dr = reinterpret_cast<RayDesc2*>(c->trace_io.p);
+    hit_result_t* dh = reinterpret_cast<hit_result_t*>(c->trace_io.p + rb);
+    WF_CUDA(cudaMemcpyAsync(dr, rays, rb, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = wf_trace_device(c, dr, n, dh, flags))) return rc;
+    WF_CUDA(cudaMemcpyAsync(hits, dh, hb, cudaMemcpyDeviceToHost, c->stream));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    return take_status(c);
+}
+
+// ---------------------------------------------------------------------------- builders
+
+int wf_bvh_build(wf_ctx* c, const triangle_t* tris, uint32_t n, const wf_bvh_options* opts, void* out,
+                 uint64_t* inout_size) {
+    if (!c || !tris || !inout_size || n == 0) return fail(WF_ERR_INVALID, "wf_bvh_build: bad argument");
+    int rc = use_device(c);
+    if (rc) return rc;
+    wf_bvh_options o = opts ? *opts : wf_bvh_options{8, 0, 0};
+    BvhBuildOut bo;
+    if ((rc = gpu_bvh_build(tris, n, o, c->stream, &bo))) return fail(rc, bvh_last_error());
+    dev_free(bo.d_nodes);
+    dev_free(bo.d_tris);
+    if (!out || *inout_size < bo.blob.size()) {
+        *inout_size = bo.blob.size();
+        return fail(WF_ERR_CAPACITY, "wf_bvh_build: output buffer too small");
+    }
+    std::memcpy(out, bo.blob.data(), bo.blob.size());
+    *inout_size = bo.blob.size();
+    return WF_OK;
+}
+
+int wf_tlas_build(wf_ctx* c, const bvh_instance_t* inst, uint32_t n, void* out, uint64_t* inout_size) {
+    if (!c || !inout_size || (n && !inst)) return fail(WF_ERR_INVALID, "wf_tlas_build: bad argument");
+    if (n > 32768) return fail(WF_ERR_CAPACITY, "wf_tlas_build: more than 32768 instances");
+    const uint64_t nodes = n ? 2ull * n : 1ull;
+    const uint64_t size = 8 + 32 * nodes + 92ull * n;
+    if (!out || *inout_size < size) {
+        *inout_size = size;
+        return fail(WF_ERR_CAPACITY, "wf_tlas_build: output buffer too small");
+    }
+    int rc = use_device(c);
+    if (rc) return rc;
+    std::vector<float> aabbs(6ull * n);
+    for (uint32_t i = 0; i < n; ++i) {
+        std::memcpy(&aabbs[6ull * i], inst[i].aabb_min, 12);
+        std::memcpy(&aabbs[6ull * i + 3], inst[i].aabb_max, 12);
+    }
+    float* d_aabbs = nullptr;
+    float4* d_nodes = nullptr;
+    uint32_t* d_scratch = nullptr;
+    if ((rc = dev_alloc(&d_aabbs, aabbs.size())) || (rc = dev_alloc(&d_nodes, 2 * nodes)) ||
+        (rc = dev_alloc(&d_scratch, 7ull * n + 1))) {
+        dev_free(d_aabbs); dev_free(d_nodes); dev_free(d_scratch);
+        return rc;
+    }
+    cudaError_t e = cudaMemsetAsync(d_nodes, 0, 32 * nodes, c->stream);
+    if (e == cudaSuccess && n)
+        e = cudaMemcpyAsync(d_aabbs, aabbs.data(), aabbs.size() * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = launch_tlas_build(d_aabbs, n, d_nodes, d_scratch, c->stream);
+    uint8_t* o = static_cast<uint8_t*>(out);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(o + 8, d_nodes, 32 * nodes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    dev_free(d_aabbs); dev_free(d_nodes); dev_free(d_scratch);
+    if (e != cudaSuccess) return fail(WF_ERR_CUDA, std::string("wf_tlas_build: ") + cudaGetErrorString(e));
+    tlas_header_t h{8u, (uint32_t)(8 + 32 * nodes)};
+    std::memcpy(o, &h, 8);
+    if (n) std::memcpy(o + h.instances_offset, inst, 92ull * n);
+    *inout_size = size;
+    return WF_OK;
+}
+
+}  // extern "C"

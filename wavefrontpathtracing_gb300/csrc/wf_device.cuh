@@ -1,0 +1,183 @@
+// wf_device.cuh — device-side layouts and exact-order float helpers.
+//
+// Every kernel is compiled with --fmad=false, -prec-div=true and
+// -prec-sqrt=true, so a*b+c rounds twice, x/y and sqrtf are correctly
+// rounded, and expressions evaluate in the order written.  The helpers below
+// fix that order (dot = (ax*bx + ay*by) + az*bz, and so on); the CPU oracle
+// performs the same operations, which is what makes hit ids, t values and
+// per-path radiance bit-identical between the two.
+#pragma once
+#include <cstdint>
+#include <cfloat>
+#include <cuda_runtime.h>
+
+namespace wf {
+
+// ---------------------------------------------------------------- layouts in HBM
+//
+// BLAS (one per mesh), traversal side:
+//   nodes : 2 x float4 per node, the reference's 32-byte bvh_node_t verbatim
+//           {min.xyz, left_first} {max.xyz, prim_count}; node 1 is unused so a
+//           child pair (2k, 2k+1) is one 64-byte aligned line.
+//   tris  : 3 x float4 per triangle in leaf order (position i of the index
+//           list): {v0.xyz, original index} {e1 = v1-v0} {e2 = v2-v0}; e1 and
+//           e2 are the exact differences Moeller-Trumbore forms first, so
+//           storing them changes no result and removes the index indirection.
+// TLAS:
+//   tnodes: the reference's 32-byte tlas_node_t verbatim.
+//   tinst : 4 x float4 per instance: world_to_local columns m[0..2], m[4..6],
+//           m[8..10], m[12..14] (the only entries the transform reads), with
+//           the mesh id in the first .w.
+// Shading side, per mesh: stri = 6 x float4 per triangle in original order
+//   {p0, -} {p1, -} {p2, -} {n0, -} {n1, -} {n2, -}.
+// Shading side, per instance: sinst = 6 x float4
+//   {l2w m[0..2], mesh} {m[4..6], bsdf} {m[8..10], ior} {m[12..14], roughness}
+//   {base rgb, metallic} {emissive rgb (strength*factor), flags}
+
+struct BlasRef {
+    const float4* nodes;
+    const float4* tris;
+};
+
+struct SceneRefs {
+    const float4* tnodes;      // TLAS nodes
+    const float4* tinst;       // TLAS instances
+    const BlasRef* blas;       // indexed by mesh id
+    uint32_t inst_count;
+};
+
+struct LightTri {
+    float4 p0;   // .w = area
+    float4 e1;   // .w = running area sum (cdf)
+    float4 e2;
+    float4 n;    // unit geometric normal
+    float4 le;   // emitted radiance
+};
+
+struct Counters {
+    unsigned long long tlas_node_loads, instance_loads, blas_node_loads, triangle_tests;
+};
+
+// Device error flags (bit set in the context's status word).
+enum : uint32_t { ERRF_STACK = 1u, ERRF_CAPACITY = 2u, ERRF_TIMEOUT = 4u };
+
+constexpr int kStack = 64;                 // per level, as the reference (accelstruct.hlsl:64,160)
+constexpr float kEps = 1e-8f;              // SMALL_FLOAT (common.hlsl:8)
+constexpr float kPi = 3.14159265f;         // PI (common.hlsl:20)
+constexpr float kInvPi = 0.31830988f;      // INV_PI
+constexpr float kInvTwoPi = 0.15915494f;   // INV_TWO_PI
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+
+// ---------------------------------------------------------------- vector helpers
+struct V3 { float x, y, z; };
+
+__host__ __device__ __forceinline__ V3 mk(float x, float y, float z) { V3 r; r.x = x; r.y = y; r.z = z; return r; }
+__host__ __device__ __forceinline__ V3 xyz(float4 a) { return mk(a.x, a.y, a.z); }
+__host__ __device__ __forceinline__ V3 add(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ V3 sub(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ V3 mul(V3 a, V3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+__host__ __device__ __forceinline__ V3 scl(V3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ V3 neg(V3 a) { return mk(-a.x, -a.y, -a.z); }
+__host__ __device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ V3 cross(V3 a, V3 b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__host__ __device__ __forceinline__ V3 normalize(V3 v) { float s = 1.0f / sqrtf(dot(v, v)); return scl(v, s); }
+__host__ __device__ __forceinline__ V3 rcp(V3 v) { return mk(1.0f / v.x, 1.0f / v.y, 1.0f / v.z); }
+
+// HLSL mul(float4(v, w), M) with row-major packing (= glm M*v):
+// out_j = ((v.x*m[j] + v.y*m[4+j]) + v.z*m[8+j]) + w*m[12+j]; the matrix is
+// given as its four column-triples c0 = m[0..2], c1 = m[4..6], ...
+__host__ __device__ __forceinline__ V3 xform(V3 v, float w, float4 c0, float4 c1, float4 c2, float4 c3) {
+    return mk(v.x * c0.x + v.y * c1.x + v.z * c2.x + w * c3.x,
+              v.x * c0.y + v.y * c1.y + v.z * c2.y + w * c3.y,
+              v.x * c0.z + v.y * c1.z + v.z * c2.z + w * c3.z);
+}
+
+// ---------------------------------------------------------------- random numbers
+// wang_hash / rand_float (common.hlsl:79-97).
+__host__ __device__ __forceinline__ uint32_t wang_hash(uint32_t s) {
+    s = (s ^ 61u) ^ (s >> 16);
+    s *= 9u;
+    s = s ^ (s >> 4);
+    s *= 0x27d4eb2du;
+    s = s ^ (s >> 15);
+    return s;
+}
+__host__ __device__ __forceinline__ float rand_float(uint32_t& s) {
+    s = wang_hash(s);
+    return (float)s * 2.3283064365387e-10f;
+}
+// Per-path stream keyed by (pixel, sample, depth) instead of the reference's
+// frame_seed + compacted queue index (shade.hlsl:80), so paths replay exactly.
+__host__ __device__ __forceinline__ uint32_t path_seed(uint32_t frame_seed, uint32_t pixel, uint32_t sample,
+                                                       uint32_t depth) {
+    uint32_t s = frame_seed + pixel;
+    s = wang_hash(s) ^ (sample * 0x9E3779B9u);
+    s = wang_hash(s) ^ (depth * 0x85EBCA6Bu);
+    return s;
+}
+
+// sin(2*pi*r), cos(2*pi*r): exact reduction in r (t = 4r, k = rint(t),
+// f = t - k), x = f*(pi/2), truncated Taylor series in Horner form (sin to
+// x^9, cos to x^10; truncation error < 2e-9 on [-pi/4, pi/4]), then a
+// quarter-turn rotation by k mod 4.
+__host__ __device__ __forceinline__ void sincos_2pi(float r, float& s_out, float& c_out) {
+    float t = r * 4.0f;
+    float k = rintf(t);
+    float f = t - k;
+    float x = f * 1.57079637f;
+    float x2 = x * x;
+    float sp = -1.98412698e-4f + x2 * 2.75573192e-6f;
+    sp = 8.33333377e-3f + x2 * sp;
+    sp = -1.66666672e-1f + x2 * sp;
+    float sn = x + (x * x2) * sp;
+    float cp = 2.48015876e-5f + x2 * -2.75573188e-7f;
+    cp = -1.38888892e-3f + x2 * cp;
+    cp = 4.16666679e-2f + x2 * cp;
+    cp = -0.5f + x2 * cp;
+    float cs = 1.0f + x2 * cp;
+    int q = ((int)k) & 3;
+    if (q == 0) { s_out = sn; c_out = cs; }
+    else if (q == 1) { s_out = cs; c_out = -sn; }
+    else if (q == 2) { s_out = -sn; c_out = -cs; }
+    else { s_out = -cs; c_out = sn; }
+}
+
+// ---------------------------------------------------------------- intersection
+// intersect_ray_aabb (intersect.hlsl:53-76): fminf/fmaxf are IEEE
+// minNum/maxNum, as HLSL min/max.
+__device__ __forceinline__ float slab(V3 bmn, V3 bmx, V3 o, V3 inv, float t) {
+    float tx1 = (bmn.x - o.x) * inv.x, tx2 = (bmx.x - o.x) * inv.x;
+    float tmin = fminf(tx1, tx2), tmax = fmaxf(tx1, tx2);
+    float ty1 = (bmn.y - o.y) * inv.y, ty2 = (bmx.y - o.y) * inv.y;
+    tmin = fmaxf(tmin, fminf(ty1, ty2));
+    tmax = fminf(tmax, fmaxf(ty1, ty2));
+    float tz1 = (bmn.z - o.z) * inv.z, tz2 = (bmx.z - o.z) * inv.z;
+    tmin = fmaxf(tmin, fminf(tz1, tz2));
+    tmax = fminf(tmax, fmaxf(tz1, tz2));
+    return (tmax >= tmin && tmin < t && tmax > 0.0f) ? tmin : FLT_MAX;
+}
+
+// intersect_ray_triangle (intersect.hlsl:7-51) on a pre-differenced triangle.
+__device__ __forceinline__ bool tri_hit(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& t_io, float& bu, float& bv,
+                                        bool no_cull) {
+    V3 pvec = cross(d, e2);
+    float det = dot(e1, pvec);
+    if (no_cull ? (fabsf(det) < kEps) : (det < kEps)) return false;
+    float inv_det = 1.0f / det;
+    V3 tvec = sub(o, v0);
+    float v = dot(tvec, pvec) * inv_det;
+    if (v < 0.0f || v > 1.0f) return false;
+    V3 qvec = cross(tvec, e1);
+    float w = dot(d, qvec) * inv_det;
+    if (w < 0.0f || v + w > 1.0f) return false;
+    float t = dot(e2, qvec) * inv_det;
+    if (t < 0.0f || t >= t_io) return false;
+    t_io = t; bu = v; bv = w;
+    return true;
+}
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+}  // namespace wf

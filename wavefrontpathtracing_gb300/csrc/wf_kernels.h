@@ -1,0 +1,76 @@
+// wf_kernels.h — launch wrappers shared by the host orchestration (wf_api.cu)
+// and the kernel translation units.  Every wrapper enqueues on `stream` and
+// returns the launch error (cudaGetLastError) without synchronizing.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "wf_device.cuh"
+
+namespace wf {
+
+// Shading-side scene (see the layout comment in wf_device.cuh).
+struct ShadeRefs {
+    const float4* sinst;          // 6 x float4 per instance
+    const float4* const* stri;    // per mesh: 6 x float4 per triangle, original order
+    const LightTri* lights;
+    uint32_t light_count;
+    float light_total;
+};
+
+// Wavefront buffers: double-buffered ray queues (the reference reads and
+// appends to one ray buffer inside a single shade dispatch, shade.hlsl:52,167),
+// hits, per-path state, the shadow-ray queue and the per-pixel accumulator.
+struct RenderBuffers {
+    float4* q_o[2];       // {origin, ray flags}
+    float4* q_d[2];       // {direction, tmax}
+    uint32_t* q_path[2];  // path id within the wave
+    float4* h_tuvp;       // {t, bary u, bary v, primitive}
+    uint32_t* h_inst;     // instance id
+    float4* ps_T;         // {throughput rgb, pdf of the last BSDF sample}
+    uint32_t* ps_flags;   // path flags
+    float4* s_o;          // shadow {origin, tmax}
+    float4* s_d;          // shadow {direction, pixel}
+    float4* s_c;          // shadow {contribution rgb, -}
+    uint32_t* counts;     // [d] extension rays at depth d, [kMaxDepth + d] shadow rays
+    float4* accum;        // per pixel {radiance sum rgb, samples}
+    uint32_t* status;     // device error flags (ERRF_*)
+    Counters* counters;   // [0] extension traffic, [1] shadow traffic
+};
+
+constexpr uint32_t kMaxDepth = 16;
+constexpr uint32_t kFlagInside = 1u;    // ray travels inside a dielectric: no back-face culling
+constexpr uint32_t kFlagSpecular = 2u;  // last scattering event was a delta lobe
+
+struct WaveParams {
+    float4 clip_to_view[4];   // matrix columns (x,y,z of m[4c..4c+2]), see xform()
+    float4 view_to_world[4];
+    uint32_t width, height;     // image size (pixel index -> x, y)
+    float dim_x, dim_y;         // view_t.render_dim (uv of the primary ray)
+    uint32_t pix0, npaths;    // pixels [pix0, pix0 + npaths) of sample `sample`
+    uint32_t sample, frame_seed;
+    uint32_t max_bounces, nee, rr_start, cosine;
+    float env_strength;
+    float env[3];
+};
+
+cudaError_t launch_trace_aos(const SceneRefs& S, const void* rays, uint32_t n, void* hits, uint32_t flags,
+                             bool count, uint32_t* status, Counters* counters, cudaStream_t stream);
+cudaError_t launch_generate(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream);
+// total (device) accumulates the number of rays each launch traced.
+cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
+                          bool count, unsigned long long* total, cudaStream_t stream);
+cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W, uint32_t depth,
+                         uint32_t max_rays, cudaStream_t stream);
+cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
+                           bool count, unsigned long long* total, cudaStream_t stream);
+cudaError_t launch_post(const float4* accum, uint32_t npix, uint32_t view_mode_none, uchar4* out,
+                        cudaStream_t stream);
+cudaError_t launch_resolve(const float4* accum, uint32_t npix, float4* out, cudaStream_t stream);
+
+// TLAS: builds nodes [0, 2n) from per-instance world AABBs (tlas_builder.cpp).
+cudaError_t launch_tlas_build(const float* aabbs /* 6 floats per instance */, uint32_t n, float4* nodes,
+                              uint32_t* scratch, cudaStream_t stream);
+
+int sm_count();
+
+}  // namespace wf
