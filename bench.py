@@ -1,0 +1,357 @@
+"""Benchmark: path-traced Mrays/s and spp/s at 1080p on the instanced scene.
+
+Workload (one step = one frame): the instanced configuration — 8 noise-
+displaced icospheres (1.70M unique triangles), 1,024 random instances
+(217.6M instanced triangles) plus one area light, 60/25/15 % Lambert / GGX
+metal / dielectric, 1920x1080, 16 samples per pixel, max depth 8, Russian
+roulette from depth 3, next-event estimation through the connect stage.
+
+Our arm (default): value = (extension + shadow rays) / GPU time of the K
+timed frames (CUDA events recorded by the library on its own stream around
+each frame); e2e = the same metric through the C ABI with host buffers — per
+frame the scene is re-submitted (1,025 instances, TLAS rebuilt on the GPU, as
+the reference rebuilds its TLAS every frame, renderer.cpp:637-669) and the
+1080p RGBA float image is read back to the host.
+
+Reference arm (--impl reference): the reference's algorithm on the host CPU
+cores: the oracle's restatement of its builders, traversal and shading
+(reference TLAS metric), all threads, each step a bounded sample of pixels of
+the same frame.
+
+Prints one JSON line (rank 0).  Multi-GPU (torchrun): each rank renders its
+own frame (different seeds), weak scaling, max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s & spp/s @1080p vs plain wavefront; adjoint grad-spp/s; % HBM peak"
+WORKLOAD = "instanced scene 1920x1080, 16 spp, max depth 8, RR from 3, NEE"
+W, H, SPP, DEPTH, RR = 1920, 1080, 16, 8, 3
+L2_BYTES = 256 << 20
+# algorithmic bytes per extend ray, reference layouts: ray 32 + hit 20, and per
+# fetch: TLAS node 32, bvh_instance_t 92, BLAS node 32, triangle 36 + index 4
+B_RAY, B_HIT, B_TNODE, B_INST, B_BNODE, B_TRI = 32, 20, 32, 92, 32, 40
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_pg(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.p, self.path = device, None, None
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+            self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the extend kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "extend_instanced_1080p.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("dram_bytes_per_launch")
+    return None
+
+
+def build_scene(r, desc):
+    from tests.helpers import load_scene_into
+    return load_scene_into(r, desc)
+
+
+def oracle_scene(desc, tlas_metric):
+    """Oracle scene for the CPU legs, from the oracle's own builders (untimed)."""
+    from oracle import oracle as orc
+    from tests.helpers import oracle_scene_from_desc
+    sc = oracle_scene_from_desc(orc, desc)
+    if tlas_metric:
+        # rebuild the TLAS of the same instances with the merged-box metric
+        from wavefrontpathtracing_gb300.abi import bvh_instance_dtype
+        h = sc._tlas[:8].view(np.uint32)
+        inst = sc._tlas[h[1]:].view(bvh_instance_dtype).copy()
+        sc = orc.Scene(list(zip(sc._tris, sc._blas)), orc.tlas_build(inst, metric=1), sc._inst)
+    return sc
+
+
+def cpu_sample(sc, desc, seconds, threads, seed):
+    """Renders consecutive pixel rows of the frame on the host until ~seconds of
+    work, calibrated by a short first pass.  Returns (Mrays/s, description)."""
+    npix = W * H
+    n = 2048
+    t0 = time.perf_counter()
+    _, st = sc.render(desc.view, W, H, max_bounces=DEPTH, spp=SPP, frame_seed=seed, nee=1, rr_start_depth=RR,
+                      threads=threads, pixel_range=(npix // 2, npix // 2 + n))
+    dt = time.perf_counter() - t0
+    n = int(min(npix, max(n, n * seconds / max(dt, 1e-3))))
+    p0 = max(0, npix // 2 - n // 2)
+    t0 = time.perf_counter()
+    _, st = sc.render(desc.view, W, H, max_bounces=DEPTH, spp=SPP, frame_seed=seed, nee=1, rr_start_depth=RR,
+                      threads=threads, pixel_range=(p0, p0 + n))
+    dt = time.perf_counter() - t0
+    rays = sum(st["extend_rays"]) + sum(st["shadow_rays"])
+    return rays / dt / 1e6, f"{n} pixels x {SPP} spp of the 1920x1080 frame ({rays} rays, {dt:.1f} s)", rays, dt
+
+
+def run_reference(args, rank, world):
+    dist = init_pg(world)
+    if rank != 0:
+        return
+    from wavefrontpathtracing_gb300 import scenes
+    desc = scenes.instanced_scene(width=W, height=H, spp=SPP, max_bounces=DEPTH)
+    sc = oracle_scene(desc, tlas_metric=0)
+    threads = os.cpu_count() or 1
+    per_step = max(3.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
+    for i in range(args.warmup):
+        cpu_sample(sc, desc, per_step, threads, seed=100 + i)
+    rays_total, t_total, desc_s = 0, 0.0, ""
+    for i in range(args.steps):
+        _, desc_s, rays, dt = cpu_sample(sc, desc, per_step, threads, seed=1 + i)
+        rays_total += rays
+        t_total += dt
+    v = rays_total / t_total / 1e6
+    line = {"metric": METRIC, "value": round(v, 3), "unit": "Mrays/s", "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t_total / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": WORKLOAD, "tlas_metric": "reference", "sample": desc_s},
+            "cpu_baseline": {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": desc_s},
+            "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def flush_l2(torch, buf):
+    if buf is not None:
+        buf.add_(1)
+
+
+def run_ours(args, rank, world, local):
+    dist = init_pg(world)
+    import wavefrontpathtracing_gb300 as wf
+    from wavefrontpathtracing_gb300 import scenes
+    try:
+        import torch
+        torch.cuda.set_device(local)
+        l2buf = torch.zeros(L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+    except Exception:
+        torch, l2buf = None, None
+    desc = scenes.instanced_scene(width=W, height=H, spp=SPP, max_bounces=DEPTH)
+    r = wf.Renderer(W, H, device=local, tlas_metric=args.tlas_metric)
+    ids = build_scene(r, desc)
+
+    def frame(seed, profile):
+        r.render(max_bounces=DEPTH, spp=SPP, frame_seed=seed, nee=1, rr_start_depth=RR, accumulate=False,
+                 profile=profile)
+        return r.stats()
+
+    for i in range(args.warmup):
+        frame(1000 + i + 97 * rank, True)
+    r.synchronize()
+    # --- device-resident timing
+    barrier(dist)
+    gpu_ms, rays, launches, ext_ms, ext_launches = 0.0, 0, 0, 0.0, 0
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush_l2(torch, l2buf)
+            if torch is not None:
+                torch.cuda.synchronize()
+            s = frame(1 + i + 7919 * rank, True)
+            gpu_ms += s["ms_total"]
+            rays += s["rays_extend"] + s["rays_connect"]
+            launches += s["launches"]
+            ext_ms += s["ms_extend"]
+            ext_launches += s["launches_extend"]
+        r.synchronize()
+    barrier(dist)
+    t_max = max_over_ranks(dist, gpu_ms)
+    rays_all = sum_over_ranks(dist, rays)
+    value = rays_all / (t_max / 1e3) / 1e6
+    spp_per_s = world * SPP * args.steps / (t_max / 1e3)
+    # --- algorithmic bytes of the extend kernel (counted pass, same seeds, untimed)
+    r.render(max_bounces=DEPTH, spp=SPP, frame_seed=1, nee=1, rr_start_depth=RR, accumulate=False,
+             count_traffic=True)
+    c = r.stats()
+    alg_bytes = (c["rays_extend"] * (B_RAY + B_HIT) + c["tlas_node_loads"] * B_TNODE + c["instance_loads"] * B_INST
+                 + c["blas_node_loads"] * B_BNODE + c["triangle_tests"] * B_TRI)
+    bytes_per_launch = alg_bytes / max(1, c["launches_extend"])
+    ms_per_launch = ext_ms / max(1, ext_launches)
+    achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    # --- end to end through the C ABI with host buffers
+    img = np.zeros((H, W, 4), dtype=np.float32)
+    s0 = r.stats()
+    barrier(dist)
+    t0 = time.perf_counter()
+    e2e_rays = 0
+    for i in range(args.steps):
+        r.begin_scene(desc.view, desc.settings["env"])
+        for mesh, l2w, mat in desc.instances:
+            r.submit_render_mesh(ids[mesh], l2w, mat)
+        r.end_scene()
+        r.render(max_bounces=DEPTH, spp=SPP, frame_seed=1 + i + 7919 * rank, nee=1, rr_start_depth=RR,
+                 accumulate=False)
+        wf.check(r.L.wf_read_image(r.h, wf.abi.ptr(img), img.size))
+        s = r.stats()
+        e2e_rays += s["rays_extend"] + s["rays_connect"]
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    s1 = r.stats()
+    e2e_value = sum_over_ranks(dist, e2e_rays) / e2e_s / 1e6
+    h2d = (s1["h2d_bytes"] - s0["h2d_bytes"]) // args.steps
+    d2h = (s1["d2h_bytes"] - s0["d2h_bytes"]) // args.steps
+    # --- CPU baseline (rank 0 only, N = 1 only): the oracle on a bounded sample
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sc = oracle_scene(desc, tlas_metric=0)
+        threads = os.cpu_count() or 1
+        v, sdesc, _, _ = cpu_sample(sc, desc, args.cpu_seconds, threads, seed=1)
+        cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": sdesc + "; reference TLAS metric"}
+    r.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(t_max / args.steps, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded procedural scene, no assets)",
+                "config": {"workload": WORKLOAD, "triangles": desc.triangle_count,
+                           "instanced_triangles": desc.instanced_triangle_count, "instances": len(desc.instances),
+                           "tlas_metric": "merged-box" if args.tlas_metric else "reference",
+                           "l2": "256 MiB buffer written between timed frames; working set > L2"},
+                "spp_per_s": round(spp_per_s, 3),
+                "rays_per_step": rays // args.steps,
+                "gpu_launches": launches,
+                "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h)},
+                "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": round(achieved, 1),
+                             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                             "frac": round(achieved / peak, 4), "traffic": ncu_traffic(),
+                             "alg_bytes_per_launch": int(bytes_per_launch),
+                             "ms_per_launch": round(ms_per_launch, 4)},
+                "clocks": clk.summary()}
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--tlas-metric", type=int, default=1, help="0 = reference pairing metric, 1 = merged box")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

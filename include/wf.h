@@ -47,8 +47,10 @@ typedef struct wf_init_params {
     uint32_t backbuffer_count;  /* accepted for source compatibility; unused (headless) */
     uint32_t vsync;             /* accepted for source compatibility; unused */
     int32_t  device;            /* CUDA device ordinal */
-    uint32_t wave_capacity;     /* max paths per wave; 0 = render_width*render_height */
-    uint32_t reserved[2];
+    uint32_t wave_capacity;     /* max paths in flight per wave; 0 = min(16 * width * height, 2^25) */
+    uint32_t tlas_metric;       /* TLAS pairing metric: 0 = the reference's (tlas_builder.cpp:96-97,
+                                   bit-exact), 1 = half area of the merged box (better trees) */
+    uint32_t reserved[1];
 } wf_init_params;
 
 /* bvh_builder_t::build_options_t (bvh_builder.h:13-17) plus max_leaf_prims:
@@ -108,6 +110,8 @@ typedef struct wf_stats {
     /* count_traffic = 1 only: fetches made by the traversal kernels */
     uint64_t tlas_node_loads, instance_loads, blas_node_loads, triangle_tests;
     uint64_t shadow_tlas_node_loads, shadow_instance_loads, shadow_blas_node_loads, shadow_triangle_tests;
+    /* host<->device bytes copied by this context since wf_create (cumulative) */
+    uint64_t h2d_bytes, d2h_bytes;
 } wf_stats;
 
 /* ---- lifetime (renderer::init / exit, renderer.h:23-24) ------------------ */
@@ -180,8 +184,9 @@ int wf_trace_device(wf_ctx* ctx, const RayDesc2* device_rays, uint32_t count,
  * bytes written out (WF_ERR_CAPACITY with the needed size if too small). */
 int wf_bvh_build(wf_ctx* ctx, const triangle_t* triangles, uint32_t triangle_count,
                  const wf_bvh_options* opts, void* out_blob, uint64_t* inout_size);
-/* Builds a TLAS on the GPU; writes [tlas_header_t | extract()] byte-identical
- * to tlas_builder_t.  Up to 32768 instances (16-bit child indices). */
+/* Builds a TLAS on the GPU with the context's tlas_metric; with metric 0 it
+ * writes [tlas_header_t | extract()] byte-identical to tlas_builder_t.  Up to
+ * 32768 instances (16-bit child indices). */
 int wf_tlas_build(wf_ctx* ctx, const bvh_instance_t* instances, uint32_t instance_count,
                   void* out_blob, uint64_t* inout_size);
 

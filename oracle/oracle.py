@@ -75,6 +75,8 @@ def lib():
         L.orc_bvh_build.argtypes = [vp, u32, u32, u32, u32, ctypes.POINTER(ctypes.c_void_p),
                                     ctypes.POINTER(ctypes.c_uint64)]
         L.orc_tlas_build.argtypes = [vp, u32, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)]
+        L.orc_tlas_build_metric.argtypes = [vp, u32, u32, ctypes.POINTER(ctypes.c_void_p),
+                                            ctypes.POINTER(ctypes.c_uint64)]
         L.orc_free.argtypes = [vp]
         L.orc_trace.argtypes = [ctypes.POINTER(_Scene), vp, u32, vp, u32, ctypes.POINTER(Counters), i32]
         L.orc_trace.restype = u32
@@ -128,9 +130,9 @@ def bvh_build(tris, interval_count=8, subdivide_single_prim=False, max_leaf_prim
                  max_leaf_prims)
 
 
-def tlas_build(instances):
+def tlas_build(instances, metric=0):
     instances = np.ascontiguousarray(instances, dtype=bvh_instance_dtype)
-    return _blob(lib().orc_tlas_build, ptr(instances), len(instances))
+    return _blob(lib().orc_tlas_build_metric, ptr(instances), len(instances), metric)
 
 
 def ref_bvh_build(tris, interval_count=8, subdivide_single_prim=False):

@@ -229,7 +229,8 @@ int orc_bvh_build(const triangle_t* tris, uint32_t n, uint32_t interval_count,
 /* find_best_match (tlas_builder.cpp:86-110), including the reference's
  * argument order: the "max" corner is max(A.min, B.min) and the "min" corner
  * is max(A.max, B.max); the metric is half_area of that box. */
-static uint32_t best_match(const tlas_node_t* nodes, uint32_t A, const uint32_t* idx, uint32_t count) {
+static uint32_t best_match(const tlas_node_t* nodes, uint32_t A, const uint32_t* idx, uint32_t count,
+                           uint32_t metric) {
     float smallest = FLT_MAX;
     uint32_t best = 0xFFFFFFFFu;
     const tlas_node_t* na = &nodes[idx[A]];
@@ -238,8 +239,14 @@ static uint32_t best_match(const tlas_node_t* nodes, uint32_t A, const uint32_t*
         const tlas_node_t* nb = &nodes[idx[B]];
         float bmx[3], bmn[3];
         for (int a = 0; a < 3; ++a) {
-            bmx[a] = gmax(na->aabb_min[a], nb->aabb_min[a]);
-            bmn[a] = gmax(na->aabb_max[a], nb->aabb_max[a]);
+            if (metric == 0) {
+                bmx[a] = gmax(na->aabb_min[a], nb->aabb_min[a]);
+                bmn[a] = gmax(na->aabb_max[a], nb->aabb_max[a]);
+            } else {
+                /* merged box: the metric the reference's comment describes */
+                bmn[a] = gmin(na->aabb_min[a], nb->aabb_min[a]);
+                bmx[a] = gmax(na->aabb_max[a], nb->aabb_max[a]);
+            }
         }
         float area = half_area(bmn, bmx);
         if (area < smallest) { smallest = area; best = B; }
@@ -248,8 +255,11 @@ static uint32_t best_match(const tlas_node_t* nodes, uint32_t A, const uint32_t*
 }
 
 /* tlas_builder_t::build + extract (tlas_builder.cpp:6-84).  The reference's
- * working list is a 256-entry stack array (:14); this one is sized to n. */
-int orc_tlas_build(const bvh_instance_t* inst, uint32_t n, uint8_t** out_blob, uint64_t* out_size) {
+ * working list is a 256-entry stack array (:14); this one is sized to n.
+ * metric 0 is the reference's pairing metric; metric 1 replaces it by the
+ * half area of the merged box (same walk, same tie rule). */
+int orc_tlas_build_metric(const bvh_instance_t* inst, uint32_t n, uint32_t metric, uint8_t** out_blob,
+                          uint64_t* out_size) {
     if (!out_blob || !out_size || (n > 0 && !inst) || n > 32768) return -1;
     uint32_t ncount = n * 2;
     tlas_node_t* nodes = (tlas_node_t*)calloc(ncount ? ncount : 1, sizeof(tlas_node_t));
@@ -265,9 +275,9 @@ int orc_tlas_build(const bvh_instance_t* inst, uint32_t n, uint8_t** out_blob, u
     }
     if (n > 0) {
         uint32_t A = 0;
-        uint32_t B = best_match(nodes, A, idx, remaining);
+        uint32_t B = best_match(nodes, A, idx, remaining, metric);
         while (remaining > 1) {
-            uint32_t C = best_match(nodes, B, idx, remaining);
+            uint32_t C = best_match(nodes, B, idx, remaining, metric);
             if (A == C) {
                 uint32_t ia = idx[A], ib = idx[B];
                 tlas_node_t* nn = &nodes[at];
@@ -278,7 +288,7 @@ int orc_tlas_build(const bvh_instance_t* inst, uint32_t n, uint8_t** out_blob, u
                 }
                 idx[A] = at++;
                 idx[B] = idx[remaining - 1];
-                B = best_match(nodes, A, idx, --remaining);
+                B = best_match(nodes, A, idx, --remaining, metric);
             } else {
                 A = B;
                 B = C;
@@ -299,6 +309,10 @@ int orc_tlas_build(const bvh_instance_t* inst, uint32_t n, uint8_t** out_blob, u
     *out_blob = blob;
     *out_size = size;
     return 0;
+}
+
+int orc_tlas_build(const bvh_instance_t* inst, uint32_t n, uint8_t** out_blob, uint64_t* out_size) {
+    return orc_tlas_build_metric(inst, n, 0, out_blob, out_size);
 }
 
 void orc_free(void* p) { free(p); }

@@ -329,8 +329,9 @@ typedef struct {
 } FN(tstate);
 
 /* One camera path of the wavefront loop (generate.hlsl, extend.hlsl,
- * shade.hlsl:42-174 and the added connect stage), contributions added to the
- * pixel in the order the GPU stages add them. */
+ * shade.hlsl:42-174 and the added connect stage).  acc is the path's own
+ * radiance, which receives the contributions in the order the GPU stages add
+ * them (shade at depth d, then connect at depth d, then depth d+1). */
 static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_render_stats* st) {
     const orc_scene* s = J->s;
     const orc_render_params* P = J->p;
@@ -383,8 +384,9 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
                 if (cos_l > K(0.0)) {
                     R d2 = (h.t * h.t) * FN(dot)(rd, rd);
                     R pdf_l = d2 / (cos_l * J->lights.total);
-                    R b2 = last_pdf * last_pdf;
-                    w = b2 / (b2 + pdf_l * pdf_l);
+                    /* power heuristic in ratio form: 1 / (1 + (pdf_l / pdf_bsdf)^2) */
+                    R q = pdf_l / last_pdf;
+                    w = (q == q) ? K(1.0) / (K(1.0) + q * q) : K(0.0);
                 }
             }
             acc[0] = acc[0] + (T.x * le.x) * w;
@@ -438,7 +440,7 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
             R voh = FN(dot)(V, H);
             L = FN(sub)(FN(scl)(H, K(2.0) * voh), V);
             R nol = FN(dot)(N, L), nov = FN(dot)(N, V), noh = FN(dot)(N, H);
-            if (nol <= K(0.0) || nov <= K(0.0) || voh <= K(0.0)) {
+            if (nol <= K(0.0) || nov <= K(0.0) || voh <= K(0.0) || noh <= K(0.0)) {
                 valid = 0;
             } else {
                 FN(v3) F = FN(schlick)(base, voh);
@@ -517,11 +519,12 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
                         FN(v3) F = FN(schlick)(base, voh);
                         f = FN(scl)(F, (D * G) / ((K(4.0) * cos_x) * nov));
                         pdf_b = (D * noh) / (K(4.0) * voh);
+                        if (!(D <= MAXT)) ok = 0;
                     }
                 }
                 if (ok) {
-                    R l2 = pdf_l * pdf_l;
-                    R w = l2 / (l2 + pdf_b * pdf_b);
+                    R q = pdf_b / pdf_l;
+                    R w = (q == q) ? K(1.0) / (K(1.0) + q * q) : K(0.0);
                     R sc = (cos_x * w) / pdf_l;
                     FN(v3) contrib = FN(mk)(((T.x * f.x) * sc) * lt->le.x, ((T.y * f.y) * sc) * lt->le.y,
                                             ((T.z * f.z) * sc) * lt->le.z);

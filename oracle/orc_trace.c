@@ -257,19 +257,21 @@ static void* render_worker(void* arg) {
         for (uint32_t px = b; px < e; ++px) {
             for (uint32_t sidx = 0; sidx < J->p->spp; ++sidx) {
                 uint32_t sample = J->p->sample_offset + sidx;
+                /* a path sums its own contributions from zero; the pixel then
+                 * adds whole paths in sample order */
                 if (!J->f64) {
-                    float acc[3] = {J->acc32[4ull * px], J->acc32[4ull * px + 1], J->acc32[4ull * px + 2]};
-                    path_f32(&j32, px, sample, acc, &st);
-                    J->acc32[4ull * px] = acc[0];
-                    J->acc32[4ull * px + 1] = acc[1];
-                    J->acc32[4ull * px + 2] = acc[2];
+                    float L[3] = {0.0f, 0.0f, 0.0f};
+                    path_f32(&j32, px, sample, L, &st);
+                    J->acc32[4ull * px] = J->acc32[4ull * px] + L[0];
+                    J->acc32[4ull * px + 1] = J->acc32[4ull * px + 1] + L[1];
+                    J->acc32[4ull * px + 2] = J->acc32[4ull * px + 2] + L[2];
                     J->acc32[4ull * px + 3] += 1.0f;
                 } else {
-                    double acc[3] = {J->acc64[4ull * px], J->acc64[4ull * px + 1], J->acc64[4ull * px + 2]};
-                    path_f64(&j64, px, sample, acc, &st);
-                    J->acc64[4ull * px] = acc[0];
-                    J->acc64[4ull * px + 1] = acc[1];
-                    J->acc64[4ull * px + 2] = acc[2];
+                    double L[3] = {0.0, 0.0, 0.0};
+                    path_f64(&j64, px, sample, L, &st);
+                    J->acc64[4ull * px] = J->acc64[4ull * px] + L[0];
+                    J->acc64[4ull * px + 1] = J->acc64[4ull * px + 1] + L[1];
+                    J->acc64[4ull * px + 2] = J->acc64[4ull * px + 2] + L[2];
                     J->acc64[4ull * px + 3] += 1.0;
                 }
             }

@@ -107,9 +107,9 @@ def _f16(m):
 class Renderer:
     """One wf_ctx: a CUDA device, its stream and all device memory."""
 
-    def __init__(self, width, height, device=0, wave_capacity=0):
+    def __init__(self, width, height, device=0, wave_capacity=0, tlas_metric=0):
         L = load()
-        p = InitParams(width, height, 1, 0, device, wave_capacity)
+        p = InitParams(width, height, 1, 0, device, wave_capacity, tlas_metric)
         h = ctypes.c_void_p()
         check(L.wf_create(ctypes.byref(p), ctypes.byref(h)))
         self.h, self.L, self.width, self.height = h, L, width, height

@@ -55,7 +55,7 @@ class InitParams(ctypes.Structure):
     _fields_ = [("render_width", ctypes.c_uint32), ("render_height", ctypes.c_uint32),
                 ("backbuffer_count", ctypes.c_uint32), ("vsync", ctypes.c_uint32),
                 ("device", ctypes.c_int32), ("wave_capacity", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 2)]
+                ("tlas_metric", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 1)]
 
 
 class BvhOptions(ctypes.Structure):
@@ -83,7 +83,8 @@ class Stats(ctypes.Structure):
                 ("tlas_node_loads", ctypes.c_uint64), ("instance_loads", ctypes.c_uint64),
                 ("blas_node_loads", ctypes.c_uint64), ("triangle_tests", ctypes.c_uint64),
                 ("shadow_tlas_node_loads", ctypes.c_uint64), ("shadow_instance_loads", ctypes.c_uint64),
-                ("shadow_blas_node_loads", ctypes.c_uint64), ("shadow_triangle_tests", ctypes.c_uint64)]
+                ("shadow_blas_node_loads", ctypes.c_uint64), ("shadow_triangle_tests", ctypes.c_uint64),
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

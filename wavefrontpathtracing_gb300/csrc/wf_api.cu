@@ -102,7 +102,7 @@ enum Stage { ST_GENERATE = 0, ST_EXTEND, ST_SHADE, ST_CONNECT, ST_POST, ST_TLAS,
 struct wf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
-    uint32_t width = 0, height = 0, capacity = 0;
+    uint32_t width = 0, height = 0, capacity = 0, tlas_metric = 0;
     std::vector<Mesh> meshes;
     std::vector<Instance> instances;
     view_t view{};
@@ -140,6 +140,7 @@ struct wf_ctx {
     wf_stats stats{};
     uint64_t launches = 0, launches_extend = 0, launches_connect = 0;
     bool count_traffic = false;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;   // cumulative over the context's life
 };
 
 namespace {
@@ -147,6 +148,16 @@ namespace {
 int use_device(wf_ctx* c) {
     WF_CUDA(cudaSetDevice(c->device));
     return WF_OK;
+}
+
+// Host<->device copies on the context stream, counted for wf_stats.
+cudaError_t h2d(wf_ctx* c, void* dst, const void* src, size_t bytes) {
+    c->h2d_bytes += bytes;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+}
+cudaError_t d2h(wf_ctx* c, void* dst, const void* src, size_t bytes) {
+    c->d2h_bytes += bytes;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
 }
 
 // Records an event pair around a stage when profiling.
@@ -269,7 +280,7 @@ int upload_shading_tris(wf_ctx* c, Mesh& m) {
     }
     int rc = dev_alloc(&m.d_stri, st.size());
     if (rc) return rc;
-    WF_CUDA(cudaMemcpyAsync(m.d_stri, st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    WF_CUDA(h2d(c, m.d_stri, st.data(), st.size() * sizeof(float4)));
     return WF_OK;
 }
 
@@ -303,8 +314,8 @@ int upload_blob(wf_ctx* c, Mesh& m) {
     if (rc) return rc;
     rc = dev_alloc(&m.d_tris, tt.size());
     if (rc) return rc;
-    WF_CUDA(cudaMemcpyAsync(m.d_nodes, nodes.data(), nodes.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
-    WF_CUDA(cudaMemcpyAsync(m.d_tris, tt.data(), tt.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    WF_CUDA(h2d(c, m.d_nodes, nodes.data(), nodes.size() * sizeof(float4)));
+    WF_CUDA(h2d(c, m.d_tris, tt.data(), tt.size() * sizeof(float4)));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     return WF_OK;
 }
@@ -319,7 +330,8 @@ int ensure_buffers(wf_ctx* c) {
             return rc;
     }
     if ((rc = dev_alloc(&B.h_tuvp, C)) || (rc = dev_alloc(&B.h_inst, C)) || (rc = dev_alloc(&B.ps_T, C)) ||
-        (rc = dev_alloc(&B.ps_flags, C)) || (rc = dev_alloc(&B.s_o, C)) || (rc = dev_alloc(&B.s_d, C)) ||
+        (rc = dev_alloc(&B.ps_flags, C)) || (rc = dev_alloc(&B.ps_L, C)) || (rc = dev_alloc(&B.s_o, C)) ||
+        (rc = dev_alloc(&B.s_d, C)) ||
         (rc = dev_alloc(&B.s_c, C)) || (rc = dev_alloc(&B.counts, 2 * kMaxDepth)) || (rc = dev_alloc(&c->accum, npix)))
         return rc;
     B.accum = c->accum;
@@ -334,7 +346,7 @@ int ensure_buffers(wf_ctx* c) {
 void release_buffers(wf_ctx* c) {
     RenderBuffers& B = c->B;
     for (int k = 0; k < 2; ++k) { dev_free(B.q_o[k]); dev_free(B.q_d[k]); dev_free(B.q_path[k]); }
-    dev_free(B.h_tuvp); dev_free(B.h_inst); dev_free(B.ps_T); dev_free(B.ps_flags);
+    dev_free(B.h_tuvp); dev_free(B.h_inst); dev_free(B.ps_T); dev_free(B.ps_flags); dev_free(B.ps_L);
     dev_free(B.s_o); dev_free(B.s_d); dev_free(B.s_c); dev_free(B.counts);
     dev_free(c->accum);
     c->buffers_ready = false;
@@ -352,8 +364,12 @@ SceneRefs scene_refs(wf_ctx* c) {
 // Reads and clears the device status word (after a synchronization).
 int take_status(wf_ctx* c) {
     uint32_t s = 0;
-    WF_CUDA(cudaMemcpy(&s, c->status, 4, cudaMemcpyDeviceToHost));
-    if (s) WF_CUDA(cudaMemset(c->status, 0, 4));
+    WF_CUDA(d2h(c, &s, c->status, 4));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    if (s) {
+        WF_CUDA(cudaMemsetAsync(c->status, 0, 4, c->stream));
+        WF_CUDA(cudaStreamSynchronize(c->stream));
+    }
     if (s & ERRF_STACK) return fail(WF_ERR_STACK, "a traversal stack overflowed; affected rays report a miss");
     if (s & ERRF_TIMEOUT) return fail(WF_ERR_TIMEOUT, "a bounded device wait gave up");
     if (s & ERRF_CAPACITY) return fail(WF_ERR_CAPACITY, "a device queue overflowed");
@@ -379,12 +395,14 @@ int finish_timing(wf_ctx* c) {
     c->stats.ms_post = st[ST_POST];
     c->stats.ms_tlas_build = st[ST_TLAS];
     unsigned long long tot[2] = {0, 0};
-    WF_CUDA(cudaMemcpy(tot, c->totals, sizeof(tot), cudaMemcpyDeviceToHost));
+    WF_CUDA(d2h(c, tot, c->totals, sizeof(tot)));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
     c->stats.rays_extend = tot[0];
     c->stats.rays_connect = tot[1];
     if (c->count_traffic) {
         Counters k[2];
-        WF_CUDA(cudaMemcpy(k, c->counters, sizeof(k), cudaMemcpyDeviceToHost));
+        WF_CUDA(d2h(c, k, c->counters, sizeof(k)));
+        WF_CUDA(cudaStreamSynchronize(c->stream));
         c->stats.tlas_node_loads = k[0].tlas_node_loads;
         c->stats.instance_loads = k[0].instance_loads;
         c->stats.blas_node_loads = k[0].blas_node_loads;
@@ -460,8 +478,15 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
     c->device = p->device;
     c->width = p->render_width;
     c->height = p->render_height;
+    if (p->tlas_metric > 1) {
+        delete c;
+        return fail(WF_ERR_INVALID, "wf_create: tlas_metric must be 0 or 1");
+    }
+    c->tlas_metric = p->tlas_metric;
     const uint64_t npix = (uint64_t)c->width * c->height;
-    c->capacity = p->wave_capacity ? (uint32_t)std::min<uint64_t>(p->wave_capacity, npix) : (uint32_t)npix;
+    // default: up to 16 samples of every pixel in flight, at most 2^25 paths
+    const uint64_t cap = p->wave_capacity ? p->wave_capacity : std::min<uint64_t>(npix * 16, 1ull << 25);
+    c->capacity = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(cap, 1ull << 30));
     int rc = use_device(c);
     if (rc == WF_OK) {
         if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -666,8 +691,8 @@ int wf_scene_end(wf_ctx* c) {
             sp[i] = c->meshes[i].d_stri;
         }
         if ((rc = c->blas.reserve(br.size())) || (rc = c->stri.reserve(sp.size()))) return rc;
-        WF_CUDA(cudaMemcpyAsync(c->blas.p, br.data(), br.size() * sizeof(BlasRef), cudaMemcpyHostToDevice, c->stream));
-        WF_CUDA(cudaMemcpyAsync(c->stri.p, sp.data(), sp.size() * sizeof(void*), cudaMemcpyHostToDevice, c->stream));
+        WF_CUDA(h2d(c, c->blas.p, br.data(), br.size() * sizeof(BlasRef)));
+        WF_CUDA(h2d(c, c->stri.p, sp.data(), sp.size() * sizeof(void*)));
     }
     // per-instance data
     std::vector<float> aabbs(6ull * n);
@@ -704,11 +729,11 @@ int wf_scene_end(wf_ctx* c) {
         return rc;
     WF_CUDA(cudaMemsetAsync(c->tnodes.p, 0, 32, c->stream));
     if (n) {
-        WF_CUDA(cudaMemcpyAsync(c->aabbs.p, aabbs.data(), aabbs.size() * 4, cudaMemcpyHostToDevice, c->stream));
-        WF_CUDA(cudaMemcpyAsync(c->tinst.p, ti.data(), ti.size() * 16, cudaMemcpyHostToDevice, c->stream));
-        WF_CUDA(cudaMemcpyAsync(c->sinst.p, si.data(), si.size() * 16, cudaMemcpyHostToDevice, c->stream));
+        WF_CUDA(h2d(c, c->aabbs.p, aabbs.data(), aabbs.size() * 4));
+        WF_CUDA(h2d(c, c->tinst.p, ti.data(), ti.size() * 16));
+        WF_CUDA(h2d(c, c->sinst.p, si.data(), si.size() * 16));
         StageTimer st(c, true, ST_TLAS);
-        WF_CUDA(launch_tlas_build(c->aabbs.p, n, c->tnodes.p, c->tlas_scratch.p, c->stream));
+        WF_CUDA(launch_tlas_build(c->aabbs.p, n, c->tnodes.p, c->tlas_scratch.p, c->tlas_metric, c->stream));
         c->launches++;
     }
     // emitter table (every triangle of every emissive instance, world space)
@@ -746,7 +771,7 @@ int wf_scene_end(wf_ctx* c) {
     c->light_total = run;
     if ((rc = c->lights.reserve(lt.size()))) return rc;
     if (!lt.empty())
-        WF_CUDA(cudaMemcpyAsync(c->lights.p, lt.data(), lt.size() * sizeof(LightTri), cudaMemcpyHostToDevice, c->stream));
+        WF_CUDA(h2d(c, c->lights.p, lt.data(), lt.size() * sizeof(LightTri)));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     c->in_scene = false;
     c->scene_ready = true;
@@ -777,7 +802,7 @@ int wf_scene_get_tlas(wf_ctx* c, void* out, uint64_t* inout_size) {
     uint8_t* o = static_cast<uint8_t*>(out);
     tlas_header_t h{8u, (uint32_t)(8 + 32 * nodes)};
     std::memcpy(o, &h, 8);
-    WF_CUDA(cudaMemcpyAsync(o + 8, c->tnodes.p, 32 * nodes, cudaMemcpyDeviceToHost, c->stream));
+    WF_CUDA(d2h(c, o + 8, c->tnodes.p, 32 * nodes));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     if (n) std::memcpy(o + h.instances_offset, c->scene_bi.data(), 92ull * n);
     *inout_size = size;
@@ -834,11 +859,26 @@ int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o,
     B.status = c->status;
     B.counters = c->counters;
     const bool nee = W.nee && c->light_count > 0;
-    for (uint32_t si = 0; si < o->spp; ++si) {
-        W.sample = c->accum_samples + si;
-        for (uint32_t p0 = 0; p0 < npix; p0 += wave) {
-            W.pix0 = p0;
-            W.npaths = std::min(wave, npix - p0);
+    // Waves: whole images of k samples when a wave holds at least one image,
+    // else pixel ranges of one sample.  Results do not depend on the split:
+    // every path's random numbers are keyed by (pixel, sample, depth) and the
+    // resolve adds paths to a pixel in sample order.
+    struct Wave { uint32_t s0, k, p0, np; };
+    std::vector<Wave> waves;
+    if (wave >= npix) {
+        const uint32_t k = wave / npix;
+        for (uint32_t si = 0; si < o->spp; si += k) waves.push_back({si, std::min(k, o->spp - si), 0u, npix});
+    } else {
+        for (uint32_t si = 0; si < o->spp; ++si)
+            for (uint32_t p0 = 0; p0 < npix; p0 += wave) waves.push_back({si, 1u, p0, std::min(wave, npix - p0)});
+    }
+    for (const Wave& wv : waves) {
+        {
+            W.s0 = c->accum_samples + wv.s0;
+            W.nsamples = wv.k;
+            W.pix0 = wv.p0;
+            W.np = wv.np;
+            W.npaths = wv.k * wv.np;
             WF_CUDA(cudaMemsetAsync(B.counts, 0, 2 * kMaxDepth * sizeof(uint32_t), c->stream));
             {
                 StageTimer t(c, prof, ST_GENERATE);
@@ -863,6 +903,11 @@ int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o,
                     c->launches_connect++;
                 }
             }
+            {
+                StageTimer t(c, prof, ST_POST);
+                WF_CUDA(launch_wave_resolve(B, W, c->stream));
+            }
+            c->launches++;
         }
     }
     c->accum_samples += o->spp;
@@ -882,7 +927,7 @@ int wf_read_image(wf_ctx* c, float* out, uint64_t nfloat) {
     if (rc) return rc;
     if ((rc = c->image.reserve(npix))) return rc;
     WF_CUDA(launch_resolve(c->accum, (uint32_t)npix, c->image.p, c->stream));
-    WF_CUDA(cudaMemcpyAsync(out, c->image.p, npix * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    WF_CUDA(d2h(c, out, c->image.p, npix * sizeof(float4)));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     return take_status(c);
 }
@@ -896,7 +941,7 @@ int wf_read_image_ldr(wf_ctx* c, uint8_t* out, uint64_t nbytes) {
     if (rc) return rc;
     if ((rc = c->image_ldr.reserve(npix))) return rc;
     WF_CUDA(launch_post(c->accum, (uint32_t)npix, 1u, c->image_ldr.p, c->stream));
-    WF_CUDA(cudaMemcpyAsync(out, c->image_ldr.p, npix * 4, cudaMemcpyDeviceToHost, c->stream));
+    WF_CUDA(d2h(c, out, c->image_ldr.p, npix * 4));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     return take_status(c);
 }
@@ -907,6 +952,8 @@ int wf_get_stats(wf_ctx* c, wf_stats* out) {
     if (rc) return rc;
     if ((rc = finish_timing(c))) return rc;
     *out = c->stats;
+    out->h2d_bytes = c->h2d_bytes;
+    out->d2h_bytes = c->d2h_bytes;
     return WF_OK;
 }
 
@@ -943,9 +990,9 @@ int wf_trace(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* hits, ui
     if ((rc = c->trace_io.reserve(rb + ((hb + 15) & ~size_t(15))))) return rc;
     RayDesc2* dr = reinterpret_cast<RayDesc2*>(c->trace_io.p);
     hit_result_t* dh = reinterpret_cast<hit_result_t*>(c->trace_io.p + rb);
-    WF_CUDA(cudaMemcpyAsync(dr, rays, rb, cudaMemcpyHostToDevice, c->stream));
+    WF_CUDA(h2d(c, dr, rays, rb));
     if ((rc = wf_trace_device(c, dr, n, dh, flags))) return rc;
-    WF_CUDA(cudaMemcpyAsync(hits, dh, hb, cudaMemcpyDeviceToHost, c->stream));
+    WF_CUDA(d2h(c, hits, dh, hb));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     return take_status(c);
 }
@@ -997,10 +1044,10 @@ int wf_tlas_build(wf_ctx* c, const bvh_instance_t* inst, uint32_t n, void* out, 
     }
     cudaError_t e = cudaMemsetAsync(d_nodes, 0, 32 * nodes, c->stream);
     if (e == cudaSuccess && n)
-        e = cudaMemcpyAsync(d_aabbs, aabbs.data(), aabbs.size() * 4, cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = launch_tlas_build(d_aabbs, n, d_nodes, d_scratch, c->stream);
+        e = h2d(c, d_aabbs, aabbs.data(), aabbs.size() * 4);
+    if (e == cudaSuccess) e = launch_tlas_build(d_aabbs, n, d_nodes, d_scratch, c->tlas_metric, c->stream);
     uint8_t* o = static_cast<uint8_t*>(out);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(o + 8, d_nodes, 32 * nodes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = d2h(c, o + 8, d_nodes, 32 * nodes);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     dev_free(d_aabbs); dev_free(d_nodes); dev_free(d_scratch);
     if (e != cudaSuccess) return fail(WF_ERR_CUDA, std::string("wf_tlas_build: ") + cudaGetErrorString(e));

@@ -28,8 +28,9 @@ struct RenderBuffers {
     uint32_t* h_inst;     // instance id
     float4* ps_T;         // {throughput rgb, pdf of the last BSDF sample}
     uint32_t* ps_flags;   // path flags
+    float4* ps_L;         // path radiance (rgb), summed from zero
     float4* s_o;          // shadow {origin, tmax}
-    float4* s_d;          // shadow {direction, pixel}
+    float4* s_d;          // shadow {direction, path id}
     float4* s_c;          // shadow {contribution rgb, -}
     uint32_t* counts;     // [d] extension rays at depth d, [kMaxDepth + d] shadow rays
     float4* accum;        // per pixel {radiance sum rgb, samples}
@@ -46,8 +47,10 @@ struct WaveParams {
     float4 view_to_world[4];
     uint32_t width, height;     // image size (pixel index -> x, y)
     float dim_x, dim_y;         // view_t.render_dim (uv of the primary ray)
-    uint32_t pix0, npaths;    // pixels [pix0, pix0 + npaths) of sample `sample`
-    uint32_t sample, frame_seed;
+    // A wave holds samples [s0, s0 + nsamples) of pixels [pix0, pix0 + np):
+    // path p is sample s0 + p / np of pixel pix0 + p % np; npaths = nsamples * np.
+    uint32_t pix0, np, s0, nsamples, npaths;
+    uint32_t frame_seed;
     uint32_t max_bounces, nee, rr_start, cosine;
     float env_strength;
     float env[3];
@@ -63,13 +66,16 @@ cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const Wave
                          uint32_t max_rays, cudaStream_t stream);
 cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
                            bool count, unsigned long long* total, cudaStream_t stream);
+// Adds each pixel's paths of the wave to the accumulator in sample order.
+cudaError_t launch_wave_resolve(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream);
 cudaError_t launch_post(const float4* accum, uint32_t npix, uint32_t view_mode_none, uchar4* out,
                         cudaStream_t stream);
 cudaError_t launch_resolve(const float4* accum, uint32_t npix, float4* out, cudaStream_t stream);
 
 // TLAS: builds nodes [0, 2n) from per-instance world AABBs (tlas_builder.cpp).
+// metric 0 = the reference's pairing metric, 1 = merged-box half area.
 cudaError_t launch_tlas_build(const float* aabbs /* 6 floats per instance */, uint32_t n, float4* nodes,
-                              uint32_t* scratch, cudaStream_t stream);
+                              uint32_t* scratch, uint32_t metric, cudaStream_t stream);
 
 int sm_count();
 

@@ -49,7 +49,7 @@ __device__ __forceinline__ void primary_ray(const WaveParams& W, uint32_t px, ui
 __global__ void __launch_bounds__(kBlock) k_generate(RenderBuffers B, WaveParams W) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W.npaths; p += stride) {
-        const uint32_t pixel = W.pix0 + p;
+        const uint32_t pixel = W.pix0 + p % W.np;
         V3 o, d;
         primary_ray(W, pixel % W.width, pixel / W.width, o, d);
         B.q_o[0][p] = make_float4(o.x, o.y, o.z, __uint_as_float(0u));
@@ -57,9 +57,7 @@ __global__ void __launch_bounds__(kBlock) k_generate(RenderBuffers B, WaveParams
         B.q_path[0][p] = p;
         B.ps_T[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         B.ps_flags[p] = kFlagSpecular;
-        float4 acc = B.accum[pixel];
-        acc.w = acc.w + 1.0f;
-        B.accum[pixel] = acc;
+        B.ps_L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) B.counts[0] = W.npaths;
 }
@@ -116,7 +114,8 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
         if (i < n) {
             const float4 d4 = B.q_d[cur][i];
             path = B.q_path[cur][i];
-            pixel = W.pix0 + path;
+            pixel = W.pix0 + path % W.np;
+            const uint32_t sample = W.s0 + path / W.np;
             const float4 tuvp = B.h_tuvp[i];
             const uint32_t inst = B.h_inst[i];
             const float4 T4 = B.ps_T[path];
@@ -126,11 +125,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
             const V3 rd = xyz(d4);
             if (inst == kInvalid) {
                 // miss: energy += throughput * strength * env (shade.hlsl:60-65)
-                float4 acc = B.accum[pixel];
+                float4 acc = B.ps_L[path];
                 acc.x = acc.x + (T.x * W.env_strength) * W.env[0];
                 acc.y = acc.y + (T.y * W.env_strength) * W.env[1];
                 acc.z = acc.z + (T.z * W.env_strength) * W.env[2];
-                B.accum[pixel] = acc;
+                B.ps_L[path] = acc;
             } else {
                 const float4* ip = SH.sinst + 6ull * inst;
                 const float4 c0 = ip[0], c1 = ip[1], c2 = ip[2], c3 = ip[3], mb = ip[4], me = ip[5];
@@ -155,17 +154,18 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
                         if (cos_l > 0.0f) {
                             float d2 = (tuvp.x * tuvp.x) * dot(rd, rd);
                             float pdf_l = d2 / (cos_l * SH.light_total);
-                            float b2 = last_pdf * last_pdf;
-                            w = b2 / (b2 + pdf_l * pdf_l);
+                            // power heuristic in ratio form: 1 / (1 + (pdf_l / pdf_bsdf)^2)
+                            float q = pdf_l / last_pdf;
+                            w = (q == q) ? 1.0f / (1.0f + q * q) : 0.0f;
                         }
                     }
-                    float4 acc = B.accum[pixel];
+                    float4 acc = B.ps_L[path];
                     acc.x = acc.x + (T.x * le.x) * w;
                     acc.y = acc.y + (T.y * le.y) * w;
                     acc.z = acc.z + (T.z * le.z) * w;
-                    B.accum[pixel] = acc;
+                    B.ps_L[path] = acc;
                 } else {
-                    uint32_t seed = path_seed(W.frame_seed, pixel, W.sample, depth);
+                    uint32_t seed = path_seed(W.frame_seed, pixel, sample, depth);
                     (void)rand_float(seed);  // r_path (shade.hlsl:81), drawn and unused
                     const float r1 = rand_float(seed);
                     const float r2 = rand_float(seed);
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
                         const float voh = dot(V, H);
                         L = sub(scl(H, 2.0f * voh), V);
                         const float nol = dot(N, L), nov = dot(N, V), noh = dot(N, H);
-                        if (nol <= 0.0f || nov <= 0.0f || voh <= 0.0f) {
+                        if (nol <= 0.0f || nov <= 0.0f || voh <= 0.0f || noh <= 0.0f) {
                             valid = false;
                         } else {
                             const V3 F = schlick(base_c, voh);
@@ -288,11 +288,12 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
                                     const V3 F = schlick(base_c, voh);
                                     f = scl(F, (D * G) / ((4.0f * cos_x) * nov));
                                     pdf_b = (D * noh) / (4.0f * voh);
+                                    if (!(D <= FLT_MAX)) ok = false;
                                 }
                             }
                             if (ok) {
-                                const float l2 = pdf_l * pdf_l;
-                                const float w = l2 / (l2 + pdf_b * pdf_b);
+                                const float q = pdf_b / pdf_l;
+                                const float w = (q == q) ? 1.0f / (1.0f + q * q) : 0.0f;
                                 const float sc = (cos_x * w) / pdf_l;
                                 const V3 ltle = xyz(lt.le);
                                 contrib = mk(((T.x * f.x) * sc) * ltle.x, ((T.y * f.y) * sc) * ltle.y,
@@ -339,7 +340,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
         const uint32_t sslot = warp_append(&B.counts[kMaxDepth + depth], shadow);
         if (shadow) {
             B.s_o[sslot] = make_float4(spos.x, spos.y, spos.z, stmax);
-            B.s_d[sslot] = make_float4(sdir.x, sdir.y, sdir.z, __uint_as_float(pixel));
+            B.s_d[sslot] = make_float4(sdir.x, sdir.y, sdir.z, __uint_as_float(path));
             B.s_c[sslot] = make_float4(contrib.x, contrib.y, contrib.z, 0.0f);
         }
     }
@@ -368,6 +369,21 @@ __global__ void k_post(const float4* __restrict__ accum, uint32_t npix, uint32_t
     }
 }
 
+__global__ void k_wave_resolve(RenderBuffers B, WaveParams W) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W.np; p += stride) {
+        float4 acc = B.accum[W.pix0 + p];
+        for (uint32_t s = 0; s < W.nsamples; ++s) {
+            const float4 L = B.ps_L[(size_t)s * W.np + p];
+            acc.x = acc.x + L.x;
+            acc.y = acc.y + L.y;
+            acc.z = acc.z + L.z;
+            acc.w = acc.w + 1.0f;
+        }
+        B.accum[W.pix0 + p] = acc;
+    }
+}
+
 __global__ void k_resolve(const float4* __restrict__ accum, uint32_t npix, float4* __restrict__ out) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += stride) {
@@ -386,6 +402,11 @@ cudaError_t launch_generate(const RenderBuffers& B, const WaveParams& W, cudaStr
 cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W, uint32_t depth,
                          uint32_t max_rays, cudaStream_t stream) {
     k_shade<<<grid_for(max_rays), kBlock, 0, stream>>>(SH, B, W, depth);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wave_resolve(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream) {
+    k_wave_resolve<<<grid_for(W.np), kBlock, 0, stream>>>(B, W);
     return cudaGetLastError();
 }
 

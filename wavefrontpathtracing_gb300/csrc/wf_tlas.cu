@@ -27,7 +27,7 @@ struct List {
 };
 
 // find_best_match: partner of list position X among positions [0, count).
-__device__ uint32_t best_match(const List& L, uint32_t X, uint32_t count) {
+__device__ uint32_t best_match(const List& L, uint32_t X, uint32_t count, uint32_t metric) {
     const uint32_t lane = threadIdx.x;
     const float ax0 = L.bmn[3 * X], ax1 = L.bmn[3 * X + 1], ax2 = L.bmn[3 * X + 2];
     const float bx0 = L.bmx[3 * X], bx1 = L.bmx[3 * X + 1], bx2 = L.bmx[3 * X + 2];
@@ -35,9 +35,16 @@ __device__ uint32_t best_match(const List& L, uint32_t X, uint32_t count) {
     uint32_t bi = 0xFFFFFFFFu;
     for (uint32_t j = lane; j < count; j += 32u) {
         if (j == X) continue;
-        // the reference's corners: "max" = max(A.min, B.min), "min" = max(A.max, B.max)
-        float hx = gmax(ax0, L.bmn[3 * j]), hy = gmax(ax1, L.bmn[3 * j + 1]), hz = gmax(ax2, L.bmn[3 * j + 2]);
-        float lx = gmax(bx0, L.bmx[3 * j]), ly = gmax(bx1, L.bmx[3 * j + 1]), lz = gmax(bx2, L.bmx[3 * j + 2]);
+        float hx, hy, hz, lx, ly, lz;
+        if (metric == 0) {
+            // the reference's corners: "max" = max(A.min, B.min), "min" = max(A.max, B.max)
+            hx = gmax(ax0, L.bmn[3 * j]); hy = gmax(ax1, L.bmn[3 * j + 1]); hz = gmax(ax2, L.bmn[3 * j + 2]);
+            lx = gmax(bx0, L.bmx[3 * j]); ly = gmax(bx1, L.bmx[3 * j + 1]); lz = gmax(bx2, L.bmx[3 * j + 2]);
+        } else {
+            // the merged box
+            lx = gmin(ax0, L.bmn[3 * j]); ly = gmin(ax1, L.bmn[3 * j + 1]); lz = gmin(ax2, L.bmn[3 * j + 2]);
+            hx = gmax(bx0, L.bmx[3 * j]); hy = gmax(bx1, L.bmx[3 * j + 1]); hz = gmax(bx2, L.bmx[3 * j + 2]);
+        }
         float ex = hx - lx, ey = hy - ly, ez = hz - lz;
         float area = ex * ey + ey * ez + ez * ex;
         if (area < best) { best = area; bi = j; }
@@ -58,7 +65,7 @@ __device__ __forceinline__ void store_node(float4* nodes, uint32_t k, const floa
 
 // One warp.  aabbs: 6 floats per instance (min xyz, max xyz); nodes: 2n nodes.
 __global__ void __launch_bounds__(32) k_tlas_build(const float* __restrict__ aabbs, uint32_t n, float4* nodes,
-                                                   uint32_t* gscratch) {
+                                                   uint32_t* gscratch, uint32_t metric) {
     extern __shared__ uint32_t smem[];
     uint32_t* base = (n <= kSmemInstances) ? smem : gscratch;
     List L;
@@ -76,9 +83,9 @@ __global__ void __launch_bounds__(32) k_tlas_build(const float* __restrict__ aab
     __syncwarp();
     uint32_t remaining = n, at = n + 1;
     uint32_t A = 0;
-    uint32_t B = best_match(L, A, remaining);
+    uint32_t B = best_match(L, A, remaining, metric);
     while (remaining > 1) {
-        const uint32_t C = best_match(L, B, remaining);
+        const uint32_t C = best_match(L, B, remaining, metric);
         if (A == C) {
             if (lane == 0) {
                 const uint32_t ia = L.idx[A], ib = L.idx[B];
@@ -97,7 +104,7 @@ __global__ void __launch_bounds__(32) k_tlas_build(const float* __restrict__ aab
             __syncwarp();
             at++;
             remaining--;
-            B = best_match(L, A, remaining);
+            B = best_match(L, A, remaining, metric);
         } else {
             A = B;
             B = C;
@@ -114,14 +121,15 @@ __global__ void __launch_bounds__(32) k_tlas_build(const float* __restrict__ aab
 
 }  // namespace
 
-cudaError_t launch_tlas_build(const float* aabbs, uint32_t n, float4* nodes, uint32_t* scratch, cudaStream_t stream) {
+cudaError_t launch_tlas_build(const float* aabbs, uint32_t n, float4* nodes, uint32_t* scratch, uint32_t metric,
+                              cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
     size_t smem = (n <= kSmemInstances) ? (size_t)n * 7u * 4u : 0u;
     if (smem > 48u * 1024u) {
         cudaError_t e = cudaFuncSetAttribute(k_tlas_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_tlas_build<<<1, 32, smem, stream>>>(aabbs, n, nodes, scratch);
+    k_tlas_build<<<1, 32, smem, stream>>>(aabbs, n, nodes, scratch, metric);
     return cudaGetLastError();
 }
 

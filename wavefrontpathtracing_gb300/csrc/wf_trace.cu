@@ -67,8 +67,8 @@ __global__ void __launch_bounds__(kBlock) k_extend(SceneRefs S, RenderBuffers B,
 }
 
 // Connect: any-hit query per shadow ray; unoccluded rays add their
-// contribution to the pixel (one shadow ray per pixel per wave and depth, so
-// the read-modify-write needs no atomic).
+// contribution to their path's radiance (a path has at most one shadow ray
+// per depth, so the read-modify-write needs no atomic).
 template <bool COUNT>
 __global__ void __launch_bounds__(kBlock) k_connect(SceneRefs S, RenderBuffers B, uint32_t depth,
                                                     unsigned long long* total) {
@@ -84,12 +84,12 @@ __global__ void __launch_bounds__(kBlock) k_connect(SceneRefs S, RenderBuffers B
         if (!ok) overflow = true;
         if (ok && h.inst == kInvalid) {
             float4 k = B.s_c[i];
-            uint32_t pixel = __float_as_uint(b.w);
-            float4 acc = B.accum[pixel];
+            uint32_t path = __float_as_uint(b.w);
+            float4 acc = B.ps_L[path];
             acc.x = acc.x + k.x;
             acc.y = acc.y + k.y;
             acc.z = acc.z + k.z;
-            B.accum[pixel] = acc;
+            B.ps_L[path] = acc;
         }
     }
     if (overflow) atomicOr(B.status, ERRF_STACK);
