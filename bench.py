@@ -283,7 +283,7 @@ def run_ours(args, rank, world, local):
     barrier(dist)
     t0 = time.perf_counter()
     e2e_rays = 0
-    for i in range(args.steps):
+    for i in range(0 if args.no_e2e else args.steps):
         r.begin_scene(desc.view, desc.settings["env"])
         for mesh, l2w, mat in desc.instances:
             r.submit_render_mesh(ids[mesh], l2w, mat)
@@ -295,7 +295,7 @@ def run_ours(args, rank, world, local):
         e2e_rays += s["rays_extend"] + s["rays_connect"]
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
     s1 = r.stats()
-    e2e_value = sum_over_ranks(dist, e2e_rays) / e2e_s / 1e6
+    e2e_value = sum_over_ranks(dist, e2e_rays) / e2e_s / 1e6 if not args.no_e2e else None
     h2d = (s1["h2d_bytes"] - s0["h2d_bytes"]) // args.steps
     d2h = (s1["d2h_bytes"] - s0["d2h_bytes"]) // args.steps
     # --- CPU baseline (rank 0 only, N = 1 only): the oracle on a bounded sample
@@ -312,15 +312,16 @@ def run_ours(args, rank, world, local):
                 "warmup": args.warmup, "ms_per_step": round(t_max / args.steps, 3), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded procedural scene, no assets)",
-                "config": {"workload": WORKLOAD, "triangles": desc.triangle_count,
+                "config": {"workload": WORKLOAD if (W, H) == (1920, 1080) else f"{WORKLOAD} at {W}x{H}",
+                           "triangles": desc.triangle_count,
                            "instanced_triangles": desc.instanced_triangle_count, "instances": len(desc.instances),
                            "tlas_metric": "merged-box" if args.tlas_metric else "reference",
                            "l2": "256 MiB buffer written between timed frames; working set > L2"},
                 "spp_per_s": round(spp_per_s, 3),
                 "rays_per_step": rays // args.steps,
                 "gpu_launches": launches,
-                "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
-                        "d2h_bytes_per_step": int(d2h)},
+                "e2e": {"value": round(e2e_value, 3) if e2e_value else None, "unit": "Mrays/s",
+                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": round(achieved, 1),
                              "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                              "frac": round(achieved / peak, 4), "traffic": ncu_traffic(),
@@ -343,9 +344,14 @@ def main():
     ap.add_argument("--tlas-metric", type=int, default=1, help="0 = reference pairing metric, 1 = merged box")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--res", default="1920x1080", help="image size WxH (the workload is 1920x1080; smaller sizes "
+                                                       "are for profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    global W, H
+    W, H = (int(x) for x in args.res.lower().split("x"))
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
