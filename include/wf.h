@@ -190,6 +190,25 @@ int wf_bvh_build(wf_ctx* ctx, const triangle_t* triangles, uint32_t triangle_cou
 int wf_tlas_build(wf_ctx* ctx, const bvh_instance_t* instances, uint32_t instance_count,
                   void* out_blob, uint64_t* inout_size);
 
+/* ---- allocation-free TLAS build (no counterpart in the reference) --------
+ * For callers that cannot allocate device memory: code running while a CUDA
+ * stream is being captured into a graph (cudaMalloc / cudaFree are not allowed
+ * during capture) and per-frame render threads that must not pay an
+ * allocation's implicit device synchronisation.  The caller owns both device
+ * buffers: device_aabbs = instance_count x {min xyz, max xyz} floats,
+ * device_nodes = 2 * instance_count tlas_node_t (one when instance_count is 0);
+ * the result equals the nodes wf_tlas_build writes with the same tlas_metric.
+ * The build's working list lives in a static 224 KiB device array, so:
+ *   - at most 8192 instances (larger counts return WF_ERR_CAPACITY);
+ *   - every call on a device shares that array: calls that overlap on the GPU
+ *     (other streams, other threads) race and must be serialised by the caller;
+ *   - the first call on a device (with that device current) loads the module and
+ *     looks up the array's device address; make it before any stream capture.
+ * Enqueued on `stream` (a cudaStream_t; NULL = default stream), not synchronised;
+ * allocates nothing. */
+int wf_tlas_build_noalloc(const float* device_aabbs, uint32_t instance_count, void* device_nodes,
+                          uint32_t tlas_metric, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,7 @@ SIGNATURES = {
     "wf_trace_device": [_vp, _vp, _u32, _vp, _u32],
     "wf_bvh_build": [_vp, _vp, _u32, _vp, _vp, _pu64],
     "wf_tlas_build": [_vp, _vp, _u32, _vp, _pu64],
+    "wf_tlas_build_noalloc": [_vp, _u32, _vp, _u32, _vp],
 }
 _RESTYPES = {"wf_status_string": ctypes.c_char_p, "wf_last_error": ctypes.c_char_p}
 

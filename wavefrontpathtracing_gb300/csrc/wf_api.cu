@@ -440,6 +440,11 @@ int end_call(wf_ctx* c) {
 
 }  // namespace
 
+namespace wf {
+// Lets entry points defined in other translation units set wf_last_error().
+int report_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace wf
+
 // ============================================================================ C ABI
 
 extern "C" {

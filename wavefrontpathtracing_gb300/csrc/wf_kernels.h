@@ -78,5 +78,7 @@ cudaError_t launch_tlas_build(const float* aabbs /* 6 floats per instance */, ui
                               uint32_t* scratch, uint32_t metric, cudaStream_t stream);
 
 int sm_count();
+// Sets the calling thread's wf_last_error() message; returns code.
+int report_error(int code, const char* msg);
 
 }  // namespace wf

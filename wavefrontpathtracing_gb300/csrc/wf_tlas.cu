@@ -9,6 +9,9 @@
 // smallest value and, on equal values, the smallest list position — exactly
 // the element the reference's sequential "area < smallest" loop keeps).  The
 // remaining list and its boxes live in shared memory when they fit.
+#include <mutex>
+
+#include "../../include/wf.h"
 #include "wf_kernels.h"
 
 namespace wf {
@@ -133,4 +136,128 @@ cudaError_t launch_tlas_build(const float* aabbs, uint32_t n, float4* nodes, uin
     return cudaGetLastError();
 }
 
+// ============================================================================
+// Allocation-free TLAS build (wf_tlas_build_noalloc).
+//
+// Some callers cannot allocate device memory: code that runs while a stream is
+// being captured into a CUDA graph (cudaMalloc/cudaFree are not permitted during
+// capture), or a per-frame render thread where an allocation's implicit
+// device-wide synchronisation would stall the frame.  They pass their own
+// device buffers for the instance boxes and the output nodes; the build's
+// working list (7 words per instance) lives in one fixed-size static device
+// array that every call on a device shares.
+
+namespace {
+
+constexpr uint32_t kNoAllocMaxInstances = 8192;
+constexpr int kNoAllocMaxDevices = 64;
+
+// 7 x 8192 words = 224 KiB, resident on every GPU that loads the library.
+static __device__ __align__(256) uint32_t g_tlas_noalloc_list[7u * kNoAllocMaxInstances];
+
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_list_addr[kNoAllocMaxDevices] = {};
+
+// The walk of k_tlas_build with the list always in `list` (global memory).
+__global__ void __launch_bounds__(32) k_tlas_build_noalloc(const float* __restrict__ aabbs, uint32_t n,
+                                                           float4* nodes, uint32_t* list, uint32_t metric) {
+    List L;
+    L.idx = list;
+    L.bmn = reinterpret_cast<float*>(list + n);
+    L.bmx = reinterpret_cast<float*>(list + 4 * n);
+    const uint32_t lane = threadIdx.x;
+    for (uint32_t i = lane; i < n; i += 32u) {
+        float mn[3] = {aabbs[6 * i], aabbs[6 * i + 1], aabbs[6 * i + 2]};
+        float mx[3] = {aabbs[6 * i + 3], aabbs[6 * i + 4], aabbs[6 * i + 5]};
+        store_node(nodes, 1 + i, mn, 0u, mx, i);
+        L.idx[i] = 1 + i;
+        for (int a = 0; a < 3; ++a) { L.bmn[3 * i + a] = mn[a]; L.bmx[3 * i + a] = mx[a]; }
+    }
+    __syncwarp();
+    uint32_t remaining = n, at = n + 1;
+    uint32_t A = 0;
+    uint32_t B = best_match(L, A, remaining, metric);
+    while (remaining > 1) {
+        const uint32_t C = best_match(L, B, remaining, metric);
+        if (A == C) {
+            if (lane == 0) {
+                const uint32_t ia = L.idx[A], ib = L.idx[B];
+                float mn[3], mx[3];
+                for (int a = 0; a < 3; ++a) {
+                    mn[a] = gmin(L.bmn[3 * A + a], L.bmn[3 * B + a]);
+                    mx[a] = gmax(L.bmx[3 * A + a], L.bmx[3 * B + a]);
+                }
+                store_node(nodes, at, mn, ia + (ib << 16), mx, 0u);
+                L.idx[A] = at;
+                for (int a = 0; a < 3; ++a) { L.bmn[3 * A + a] = mn[a]; L.bmx[3 * A + a] = mx[a]; }
+                const uint32_t last = remaining - 1;
+                L.idx[B] = L.idx[last];
+                for (int a = 0; a < 3; ++a) { L.bmn[3 * B + a] = L.bmn[3 * last + a]; L.bmx[3 * B + a] = L.bmx[3 * last + a]; }
+            }
+            __syncwarp();
+            at++;
+            remaining--;
+            B = best_match(L, A, remaining, metric);
+        } else {
+            A = B;
+            B = C;
+        }
+    }
+    __syncwarp();
+    if (lane == 0) {
+        const uint32_t r = L.idx[A];
+        const float4 a = nodes[2 * r], b = nodes[2 * r + 1];
+        nodes[0] = a;
+        nodes[1] = b;
+    }
+}
+
+}  // namespace
+
 }  // namespace wf
+
+extern "C" int wf_tlas_build_noalloc(const float* device_aabbs, uint32_t instance_count, void* device_nodes,
+                                     uint32_t tlas_metric, void* stream) {
+    using namespace wf;
+    if (instance_count > kNoAllocMaxInstances)
+        return report_error(WF_ERR_CAPACITY, "wf_tlas_build_noalloc: at most 8192 instances (static working list)");
+    if (!device_nodes || (instance_count > 0 && !device_aabbs))
+        return report_error(WF_ERR_INVALID, "wf_tlas_build_noalloc: null device pointer");
+    if (tlas_metric > 1) return report_error(WF_ERR_INVALID, "wf_tlas_build_noalloc: tlas_metric must be 0 or 1");
+    if ((reinterpret_cast<uintptr_t>(device_aabbs) & 3u) || (reinterpret_cast<uintptr_t>(device_nodes) & 15u))
+        return report_error(WF_ERR_INVALID, "wf_tlas_build_noalloc: boxes must be 4-byte, nodes 16-byte aligned");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+        cudaGetLastError();
+        return report_error(WF_ERR_CUDA, "wf_tlas_build_noalloc: no usable current CUDA device");
+    }
+    uint32_t* list = nullptr;
+    {
+        // Set-up, once per device, with that device current: the host-side name
+        // g_tlas_noalloc_list is only a stand-in, so the kernel gets the
+        // array's device address.
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_list_addr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_tlas_noalloc_list);
+            if (e != cudaSuccess || !p) {
+                cudaGetLastError();
+                return report_error(WF_ERR_CUDA, "wf_tlas_build_noalloc: cudaGetSymbolAddress failed");
+            }
+            g_noalloc_list_addr[dev] = static_cast<uint32_t*>(p);
+        }
+        list = g_noalloc_list_addr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e;
+    if (instance_count == 0) {
+        e = cudaMemsetAsync(device_nodes, 0, 32, st);   // one zero node, as tlas_builder_t leaves it
+    } else {
+        k_tlas_build_noalloc<<<1, 32, 0, st>>>(device_aabbs, instance_count, static_cast<float4*>(device_nodes),
+                                                list, tlas_metric);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return report_error(WF_ERR_CUDA, cudaGetErrorString(e));
+    return WF_OK;
+}
+
