@@ -130,6 +130,7 @@ struct wf_ctx {
     DevBuf<uchar4> image_ldr;
     DevBuf<uint8_t> trace_io;
     uint32_t* status = nullptr;
+    uint32_t* trace_fetch = nullptr;        // fetch counter of wf_trace / wf_trace_device
     Counters* counters = nullptr;
 
     // timing
@@ -332,7 +333,7 @@ int ensure_buffers(wf_ctx* c) {
     if ((rc = dev_alloc(&B.h_tuvp, C)) || (rc = dev_alloc(&B.h_inst, C)) || (rc = dev_alloc(&B.ps_T, C)) ||
         (rc = dev_alloc(&B.ps_flags, C)) || (rc = dev_alloc(&B.ps_L, C)) || (rc = dev_alloc(&B.s_o, C)) ||
         (rc = dev_alloc(&B.s_d, C)) ||
-        (rc = dev_alloc(&B.s_c, C)) || (rc = dev_alloc(&B.counts, 2 * kMaxDepth)) || (rc = dev_alloc(&c->accum, npix)))
+        (rc = dev_alloc(&B.s_c, C)) || (rc = dev_alloc(&B.counts, 4 * kMaxDepth)) || (rc = dev_alloc(&c->accum, npix)))
         return rc;
     B.accum = c->accum;
     B.status = c->status;
@@ -501,6 +502,7 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
     }
     if (rc == WF_OK) rc = dev_alloc(&c->status, 1);
     if (rc == WF_OK) rc = dev_alloc(&c->counters, 2);
+    if (rc == WF_OK) rc = dev_alloc(&c->trace_fetch, 1);
     if (rc == WF_OK) rc = dev_alloc(&c->totals, 2);
     if (rc == WF_OK) {
         cudaMemset(c->status, 0, 4);
@@ -525,7 +527,7 @@ int wf_destroy(wf_ctx* c) {
     c->tnodes.release(); c->tinst.release(); c->sinst.release(); c->blas.release(); c->stri.release();
     c->lights.release(); c->aabbs.release(); c->tlas_scratch.release();
     c->image.release(); c->image_ldr.release(); c->trace_io.release();
-    dev_free(c->status); dev_free(c->counters); dev_free(c->totals);
+    dev_free(c->status); dev_free(c->counters); dev_free(c->totals); dev_free(c->trace_fetch);
     for (EventPair& p : c->events) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
@@ -884,7 +886,7 @@ int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o,
             W.pix0 = wv.p0;
             W.np = wv.np;
             W.npaths = wv.k * wv.np;
-            WF_CUDA(cudaMemsetAsync(B.counts, 0, 2 * kMaxDepth * sizeof(uint32_t), c->stream));
+            WF_CUDA(cudaMemsetAsync(B.counts, 0, 4 * kMaxDepth * sizeof(uint32_t), c->stream));
             {
                 StageTimer t(c, prof, ST_GENERATE);
                 WF_CUDA(launch_generate(B, W, c->stream));
@@ -973,9 +975,11 @@ int wf_trace_device(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* h
     int rc = use_device(c);
     if (rc) return rc;
     if ((rc = begin_call(c, false))) return rc;
+    WF_CUDA(cudaMemsetAsync(c->trace_fetch, 0, 4, c->stream));
     {
         StageTimer t(c, true, ST_EXTEND);
-        WF_CUDA(launch_trace_aos(scene_refs(c), rays, n, hits, flags, false, c->status, c->counters, c->stream));
+        WF_CUDA(launch_trace_aos(scene_refs(c), rays, n, hits, flags, false, c->trace_fetch, c->status, c->counters,
+                                 c->stream));
     }
     c->launches++;
     c->launches_extend++;

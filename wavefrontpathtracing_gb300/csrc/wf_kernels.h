@@ -32,7 +32,8 @@ struct RenderBuffers {
     float4* s_o;          // shadow {origin, tmax}
     float4* s_d;          // shadow {direction, path id}
     float4* s_c;          // shadow {contribution rgb, -}
-    uint32_t* counts;     // [d] extension rays at depth d, [kMaxDepth + d] shadow rays
+    uint32_t* counts;     // [d] extension rays at depth d, [kMaxDepth + d] shadow rays,
+                          // [2 kMaxDepth + d], [3 kMaxDepth + d] the traversal kernels' fetch counters
     float4* accum;        // per pixel {radiance sum rgb, samples}
     uint32_t* status;     // device error flags (ERRF_*)
     Counters* counters;   // [0] extension traffic, [1] shadow traffic
@@ -56,8 +57,9 @@ struct WaveParams {
     float env[3];
 };
 
+// fetch: a zeroed device counter the persistent kernel hands rays out from.
 cudaError_t launch_trace_aos(const SceneRefs& S, const void* rays, uint32_t n, void* hits, uint32_t flags,
-                             bool count, uint32_t* status, Counters* counters, cudaStream_t stream);
+                             bool count, uint32_t* fetch, uint32_t* status, Counters* counters, cudaStream_t stream);
 cudaError_t launch_generate(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream);
 // total (device) accumulates the number of rays each launch traced.
 cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,

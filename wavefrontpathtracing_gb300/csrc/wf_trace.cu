@@ -12,88 +12,77 @@ constexpr int kBlock = 128;
 
 int g_sms = 0;
 
-unsigned grid_for(uint32_t n) {
-    unsigned blocks = (n + kBlock - 1) / kBlock;
-    unsigned cap = (unsigned)sm_count() * 16u;
-    if (blocks > cap) blocks = cap;
-    return blocks ? blocks : 1u;
-}
+// Extension rays: queue[depth & 1] -> hits.  Ray flags in origin.w select culling.
+struct ExtendIO {
+    const float4* qo;
+    const float4* qd;
+    float4* tuvp;
+    uint32_t* inst;
+    __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
+        const float4 a = qo[i], b = qd[i];
+        o = xyz(a); d = xyz(b); tmax = b.w;
+        nc = (__float_as_uint(a.w) & kFlagInside) != 0u;
+    }
+    __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool) const {
+        tuvp[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+        inst[i] = h.inst;
+    }
+};
 
-// RayDesc2 in, hit_result_t out (wf_trace / wf_trace_device).
-template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_trace_aos(SceneRefs S, const float4* __restrict__ rays, uint32_t n,
-                                                      uint32_t* __restrict__ hits, bool no_cull,
-                                                      uint32_t* status, Counters* counters) {
+// Shadow rays: an unoccluded ray adds its contribution to its path's radiance
+// (a path has at most one shadow ray per depth, so the read-modify-write
+// needs no atomic).
+struct ConnectIO {
+    const float4* so;
+    const float4* sd;
+    const float4* sc;
+    float4* L;
+    __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
+        const float4 a = so[i], b = sd[i];
+        o = xyz(a); d = xyz(b); tmax = a.w; nc = false;
+    }
+    __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool ok) const {
+        if (!ok || h.inst != kInvalid) return;
+        const float4 k = sc[i];
+        const uint32_t path = __float_as_uint(sd[i].w);
+        float4 acc = L[path];
+        acc.x = acc.x + k.x;
+        acc.y = acc.y + k.y;
+        acc.z = acc.z + k.z;
+        L[path] = acc;
+    }
+};
+
+template <bool ANY, bool COUNT, class IO>
+__global__ void __launch_bounds__(kBlock) k_trace(SceneRefs S, IO io, const uint32_t* count_ptr, uint32_t count,
+                                                  uint32_t* fetch, uint32_t* status, Counters* counters,
+                                                  unsigned long long* total) {
+    const uint32_t n = count_ptr ? *count_ptr : count;
+    if (total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(total, (unsigned long long)n);
     LocalCounters c = {0, 0, 0, 0};
     bool overflow = false;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        float4 a = ldg4(rays + 2ull * i), b = ldg4(rays + 2ull * i + 1);
-        Hit h;
-        if (!trace_ray<ANY, COUNT>(S, xyz(a), xyz(b), b.w, no_cull, h, c)) overflow = true;
-        uint32_t* o = hits + 5ull * i;
-        o[0] = h.inst;
-        o[1] = h.prim;
-        o[2] = __float_as_uint(h.t);
-        o[3] = __float_as_uint(h.u);
-        o[4] = __float_as_uint(h.v);
-    }
+    trace_persistent<ANY, COUNT>(S, io, n, fetch, c, overflow);
     if (overflow) atomicOr(status, ERRF_STACK);
     if (COUNT) flush_counters(c, counters);
 }
 
-// Extend: queue[depth & 1] -> hits.  Ray flags in origin.w select culling.
-template <bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_extend(SceneRefs S, RenderBuffers B, uint32_t depth,
-                                                   unsigned long long* total) {
-    const uint32_t n = B.counts[depth];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(total, (unsigned long long)n);
-    const int cur = depth & 1;
-    const float4* __restrict__ qo = B.q_o[cur];
-    const float4* __restrict__ qd = B.q_d[cur];
-    LocalCounters c = {0, 0, 0, 0};
-    bool overflow = false;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        float4 a = qo[i], b = qd[i];
-        Hit h;
-        bool no_cull = (__float_as_uint(a.w) & kFlagInside) != 0u;
-        if (!trace_ray<false, COUNT>(S, xyz(a), xyz(b), b.w, no_cull, h, c)) overflow = true;
-        B.h_tuvp[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
-        B.h_inst[i] = h.inst;
+// Resident blocks per SM for a kernel, queried once per instantiation.
+template <class K>
+unsigned persistent_grid(K kernel) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+        if (per_sm <= 0) per_sm = 1;
     }
-    if (overflow) atomicOr(B.status, ERRF_STACK);
-    if (COUNT) flush_counters(c, B.counters);
+    return (unsigned)(sm_count() * per_sm);
 }
 
-// Connect: any-hit query per shadow ray; unoccluded rays add their
-// contribution to their path's radiance (a path has at most one shadow ray
-// per depth, so the read-modify-write needs no atomic).
-template <bool COUNT>
-__global__ void __launch_bounds__(kBlock) k_connect(SceneRefs S, RenderBuffers B, uint32_t depth,
-                                                    unsigned long long* total) {
-    const uint32_t n = B.counts[kMaxDepth + depth];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(total, (unsigned long long)n);
-    LocalCounters c = {0, 0, 0, 0};
-    bool overflow = false;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        float4 a = B.s_o[i], b = B.s_d[i];
-        Hit h;
-        bool ok = trace_ray<true, COUNT>(S, xyz(a), xyz(b), a.w, false, h, c);
-        if (!ok) overflow = true;
-        if (ok && h.inst == kInvalid) {
-            float4 k = B.s_c[i];
-            uint32_t path = __float_as_uint(b.w);
-            float4 acc = B.ps_L[path];
-            acc.x = acc.x + k.x;
-            acc.y = acc.y + k.y;
-            acc.z = acc.z + k.z;
-            B.ps_L[path] = acc;
-        }
-    }
-    if (overflow) atomicOr(B.status, ERRF_STACK);
-    if (COUNT) flush_counters(c, B.counters + 1);
+template <bool ANY, bool COUNT, class IO>
+cudaError_t launch(const SceneRefs& S, const IO& io, const uint32_t* count_ptr, uint32_t count, uint32_t* fetch,
+                   uint32_t* status, Counters* counters, unsigned long long* total, cudaStream_t stream) {
+    auto k = k_trace<ANY, COUNT, IO>;
+    k<<<persistent_grid(k), kBlock, 0, stream>>>(S, io, count_ptr, count, fetch, status, counters, total);
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -109,36 +98,38 @@ int sm_count() {
 }
 
 cudaError_t launch_trace_aos(const SceneRefs& S, const void* rays, uint32_t n, void* hits, uint32_t flags,
-                             bool count, uint32_t* status, Counters* counters, cudaStream_t stream) {
+                             bool count, uint32_t* fetch, uint32_t* status, Counters* counters, cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
-    const bool any = (flags & 1u) != 0, no_cull = (flags & 2u) != 0;
-    const float4* r = static_cast<const float4*>(rays);
-    uint32_t* h = static_cast<uint32_t*>(hits);
-    unsigned g = grid_for(n);
-    if (any) {
-        if (count) k_trace_aos<true, true><<<g, kBlock, 0, stream>>>(S, r, n, h, no_cull, status, counters);
-        else k_trace_aos<true, false><<<g, kBlock, 0, stream>>>(S, r, n, h, no_cull, status, counters);
-    } else {
-        if (count) k_trace_aos<false, true><<<g, kBlock, 0, stream>>>(S, r, n, h, no_cull, status, counters);
-        else k_trace_aos<false, false><<<g, kBlock, 0, stream>>>(S, r, n, h, no_cull, status, counters);
-    }
-    return cudaGetLastError();
+    AosIO io;
+    io.rays = static_cast<const float4*>(rays);
+    io.hits = static_cast<uint32_t*>(hits);
+    io.no_cull = (flags & 2u) != 0;
+    const bool any = (flags & 1u) != 0;
+    if (any) return count ? launch<true, true>(S, io, nullptr, n, fetch, status, counters, nullptr, stream)
+                          : launch<true, false>(S, io, nullptr, n, fetch, status, counters, nullptr, stream);
+    return count ? launch<false, true>(S, io, nullptr, n, fetch, status, counters, nullptr, stream)
+                 : launch<false, false>(S, io, nullptr, n, fetch, status, counters, nullptr, stream);
 }
 
-cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays, bool count,
+cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t, bool count,
                           unsigned long long* total, cudaStream_t stream) {
-    unsigned g = grid_for(max_rays);
-    if (count) k_extend<true><<<g, kBlock, 0, stream>>>(S, B, depth, total);
-    else k_extend<false><<<g, kBlock, 0, stream>>>(S, B, depth, total);
-    return cudaGetLastError();
+    ExtendIO io;
+    const int cur = depth & 1;
+    io.qo = B.q_o[cur]; io.qd = B.q_d[cur]; io.tuvp = B.h_tuvp; io.inst = B.h_inst;
+    uint32_t* fetch = B.counts + 2 * kMaxDepth + depth;
+    return count ? launch<false, true>(S, io, B.counts + depth, 0, fetch, B.status, B.counters, total, stream)
+                 : launch<false, false>(S, io, B.counts + depth, 0, fetch, B.status, B.counters, total, stream);
 }
 
-cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays, bool count,
+cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t, bool count,
                            unsigned long long* total, cudaStream_t stream) {
-    unsigned g = grid_for(max_rays);
-    if (count) k_connect<true><<<g, kBlock, 0, stream>>>(S, B, depth, total);
-    else k_connect<false><<<g, kBlock, 0, stream>>>(S, B, depth, total);
-    return cudaGetLastError();
+    ConnectIO io;
+    io.so = B.s_o; io.sd = B.s_d; io.sc = B.s_c; io.L = B.ps_L;
+    uint32_t* fetch = B.counts + 3 * kMaxDepth + depth;
+    return count ? launch<true, true>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, B.counters + 1, total,
+                                      stream)
+                 : launch<true, false>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, B.counters + 1, total,
+                                       stream);
 }
 
 }  // namespace wf

@@ -1,16 +1,24 @@
 // wf_traverse.cuh — software TLAS -> BLAS traversal (closest hit / any hit).
 //
-// Follows trace_ray_tlas / trace_ray_bvh_instance / trace_ray_bvh_local
-// (accelstruct.hlsl:58-218) step for step: TLAS root box test, near-child-first
-// descent with ties to the left, far child pushed only when it was hit, leaf
-// triangles tested in index-list order with strict "t < ray.t" acceptance (the
-// first triangle found wins an exact tie), instance rays transformed by
-// world_to_local without renormalising.  The reference pushes whole node
-// copies; this pushes the 8 bytes a popped node needs ({left_first,
-// prim_count} or {left_right, instance_idx}), which visits the same nodes in
-// the same order.  Each level keeps its own 64-entry stack, as the reference;
-// an overflow abandons the ray (reported as a miss) and raises ERRF_STACK
-// where the reference would write past its array.
+// Per ray it follows trace_ray_tlas / trace_ray_bvh_instance /
+// trace_ray_bvh_local (accelstruct.hlsl:58-218) step for step: TLAS root box
+// test, near-child-first descent with ties to the left, far child pushed only
+// when it was hit, leaf triangles tested in index-list order with strict
+// "t < ray.t" acceptance (the first triangle found wins an exact tie),
+// instance rays transformed by world_to_local without renormalising.  The
+// reference pushes whole node copies; this pushes the 8 bytes a popped node
+// needs ({left_first, prim_count} or {left_right, instance_idx}), which visits
+// the same nodes in the same order.  Each level keeps its own 64-entry stack,
+// as the reference; an overflow abandons the ray (reported as a miss) and
+// raises ERRF_STACK where the reference would write past its array.
+//
+// GPU organisation: a persistent grid; every warp runs one warp-uniform loop
+// whose iterations perform one traversal step per lane — an interior visit
+// (the same code for TLAS and BLAS nodes: two child boxes, one slab test
+// each), an instance entry, or a leaf's triangles — so lanes stay converged on
+// the common interior step instead of drifting apart in nested per-lane loops.
+// Lanes whose ray finished take new rays in groups through one atomic per warp
+// (kRefill idle lanes, or all of them) from a per-launch counter.
 #pragma once
 #include "wf_device.cuh"
 
@@ -25,121 +33,184 @@ struct LocalCounters {
     uint32_t tlas_nodes, instances, blas_nodes, tris;
 };
 
-// Returns false when a stack overflowed (h then reports a miss).
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool trace_ray(const SceneRefs& S, V3 o, V3 d, float tmax, bool no_cull, Hit& h,
-                                          LocalCounters& cnt) {
+constexpr uint32_t kNoRay = 0xFFFFFFFFu;
+constexpr int kRefill = 12;
+
+// Ray sources / sinks.  load(i, o, d, tmax, no_cull); store(i, hit, ok) where
+// ok is false when a traversal stack overflowed.
+struct AosIO {
+    const float4* rays;   // RayDesc2
+    uint32_t* hits;       // hit_result_t
+    bool no_cull;
+    __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
+        const float4 a = ldg4(rays + 2ull * i), b = ldg4(rays + 2ull * i + 1);
+        o = xyz(a); d = xyz(b); tmax = b.w; nc = no_cull;
+    }
+    __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool) const {
+        uint32_t* o = hits + 5ull * i;
+        o[0] = h.inst; o[1] = h.prim; o[2] = __float_as_uint(h.t); o[3] = __float_as_uint(h.u);
+        o[4] = __float_as_uint(h.v);
+    }
+};
+
+template <bool ANY, bool COUNT, class IO>
+__device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& io, uint32_t n, uint32_t* fetch,
+                                                 LocalCounters& cnt, bool& overflow) {
+    const unsigned FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t ri = kNoRay;
+    bool exhausted = false;
+    V3 wo = mk(0, 0, 0), wd = mk(0, 0, 0);   // world ray
+    float wt = 0.0f;                          // world ray.t (closest hit so far)
+    V3 co = mk(0, 0, 0), cd = mk(0, 0, 0), ci = mk(0, 0, 0);  // current-space ray and 1/dir
+    float ct = 0.0f;                          // current-space ray.t
+    bool no_cull = false, hit_here = false;
+    uint32_t level = 0, w0 = 0, w1 = 0, ii = 0;
+    BlasRef B;
+    B.nodes = nullptr; B.tris = nullptr;
+    Hit h;
     h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
-    if (S.inst_count == 0) return true;
-    const V3 inv = rcp(d);
-    float t = tmax;
-    float4 n0 = ldg4(S.tnodes), n1 = ldg4(S.tnodes + 1);
-    if (COUNT) cnt.tlas_nodes++;
-    if (slab(xyz(n0), xyz(n1), o, inv, t) == FLT_MAX) return true;
-    uint32_t lr = __float_as_uint(n0.w), ii = __float_as_uint(n1.w);
+    int tsp = 0, bsp = 0;
     uint2 tstack[kStack];
     uint2 bstack[kStack];
-    int tsp = 0;
+
     for (;;) {
-        if (lr == 0u) {
-            // instance leaf: trace_ray_bvh_instance
-            const float4* ip = S.tinst + 4ull * ii;
-            float4 c0 = ldg4(ip), c1 = ldg4(ip + 1), c2 = ldg4(ip + 2), c3 = ldg4(ip + 3);
-            if (COUNT) cnt.instances++;
-            const V3 lo = xform(o, 1.0f, c0, c1, c2, c3);
-            const V3 ld = xform(d, 0.0f, c0, c1, c2, c3);
-            const V3 linv = rcp(ld);
-            const BlasRef B = S.blas[__float_as_uint(c0.w)];
-            float lt = t;
-            bool hit_here = false;
-            float4 r0 = ldg4(B.nodes), r1 = ldg4(B.nodes + 1);
-            if (COUNT) cnt.blas_nodes++;
-            uint32_t first = __float_as_uint(r0.w), count = __float_as_uint(r1.w);
-            int bsp = 0;
-            for (;;) {
-                if (count > 0u) {
-                    for (uint32_t i = first; i < first + count; ++i) {
-                        const float4* tp = B.tris + 3ull * i;
-                        float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
-                        if (COUNT) cnt.tris++;
-                        float bu, bv;
-                        if (tri_hit(xyz(a), xyz(b), xyz(c), lo, ld, lt, bu, bv, no_cull)) {
-                            h.prim = __float_as_uint(a.w);
-                            h.u = bu; h.v = bv;
-                            hit_here = true;
-                            if (ANY) {
-                                h.inst = ii;
-                                h.t = lt;
-                                return true;
-                            }
+        // ---- refill idle lanes (one atomic per warp)
+        const bool idle = ri == kNoRay;
+        const unsigned want = __ballot_sync(FULL, idle && !exhausted);
+        if (want) {
+            const unsigned busy = __ballot_sync(FULL, !idle);
+            if (busy == 0u || __popc(want) >= kRefill) {
+                const int leader = __ffs(want) - 1;
+                uint32_t base = 0;
+                if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(want));
+                base = __shfl_sync(FULL, base, leader);
+                if (idle && !exhausted) {
+                    const uint32_t k = base + (uint32_t)__popc(want & ((1u << lane) - 1u));
+                    if (k < n) {
+                        ri = k;
+                        io.load(k, wo, wd, wt, no_cull);
+                        h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
+                        co = wo; cd = wd; ci = rcp(wd); ct = wt;
+                        bool miss = S.inst_count == 0;
+                        if (!miss) {
+                            const float4 n0 = ldg4(S.tnodes), n1 = ldg4(S.tnodes + 1);
+                            if (COUNT) cnt.tlas_nodes++;
+                            miss = slab(xyz(n0), xyz(n1), co, ci, ct) == FLT_MAX;
+                            level = 0; w0 = __float_as_uint(n0.w); w1 = __float_as_uint(n1.w); tsp = 0;
                         }
-                    }
-                    if (bsp == 0) break;
-                    uint2 e = bstack[--bsp];
-                    first = e.x; count = e.y;
-                    continue;
-                }
-                const float4* np = B.nodes + 2ull * first;
-                float4 l0 = ldg4(np), l1 = ldg4(np + 1), q0 = ldg4(np + 2), q1 = ldg4(np + 3);
-                if (COUNT) cnt.blas_nodes += 2;
-                float dl = slab(xyz(l0), xyz(l1), lo, linv, lt);
-                float dr = slab(xyz(q0), xyz(q1), lo, linv, lt);
-                uint2 L = make_uint2(__float_as_uint(l0.w), __float_as_uint(l1.w));
-                uint2 R = make_uint2(__float_as_uint(q0.w), __float_as_uint(q1.w));
-                if (dl > dr) {
-                    float td = dl; dl = dr; dr = td;
-                    uint2 tn = L; L = R; R = tn;
-                }
-                if (dl == FLT_MAX) {
-                    if (bsp == 0) break;
-                    uint2 e = bstack[--bsp];
-                    first = e.x; count = e.y;
-                } else {
-                    first = L.x; count = L.y;
-                    if (dr != FLT_MAX) {
-                        if (bsp == kStack) {
-                            h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
-                            return false;
-                        }
-                        bstack[bsp++] = R;
+                        if (miss) { io.store(k, h, true); ri = kNoRay; }
+                    } else {
+                        exhausted = true;
                     }
                 }
             }
-            t = lt;
-            if (hit_here) { h.inst = ii; h.t = t; }
-            if (tsp == 0) break;
-            uint2 e = tstack[--tsp];
-            lr = e.x; ii = e.y;
+        }
+        const unsigned active = __ballot_sync(FULL, ri != kNoRay);
+        if (active == 0u) {
+            if (__all_sync(FULL, exhausted)) break;
             continue;
         }
-        const float4* ap = S.tnodes + 2ull * (lr >> 16);
-        const float4* bp = S.tnodes + 2ull * (lr & 0xFFFFu);
-        float4 a0 = ldg4(ap), a1 = ldg4(ap + 1), b0 = ldg4(bp), b1 = ldg4(bp + 1);
-        if (COUNT) cnt.tlas_nodes += 2;
-        float dl = slab(xyz(a0), xyz(a1), o, inv, t);
-        float dr = slab(xyz(b0), xyz(b1), o, inv, t);
-        uint2 L = make_uint2(__float_as_uint(a0.w), __float_as_uint(a1.w));
-        uint2 R = make_uint2(__float_as_uint(b0.w), __float_as_uint(b1.w));
-        if (dl > dr) {
-            float td = dl; dl = dr; dr = td;
-            uint2 tn = L; L = R; R = tn;
-        }
-        if (dl == FLT_MAX) {
-            if (tsp == 0) break;
-            uint2 e = tstack[--tsp];
-            lr = e.x; ii = e.y;
-        } else {
-            lr = L.x; ii = L.y;
-            if (dr != FLT_MAX) {
-                if (tsp == kStack) {
-                    h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
-                    return false;
+        if (ri == kNoRay) continue;
+
+        // ---- one traversal step
+        bool finish = false, ok = true;
+        bool pop = false;
+        if (level == 0u && w0 == 0u) {
+            // TLAS leaf: enter the instance (trace_ray_bvh_instance)
+            ii = w1;
+            const float4* ip = S.tinst + 4ull * ii;
+            const float4 c0 = ldg4(ip), c1 = ldg4(ip + 1), c2 = ldg4(ip + 2), c3 = ldg4(ip + 3);
+            if (COUNT) cnt.instances++;
+            co = xform(wo, 1.0f, c0, c1, c2, c3);
+            cd = xform(wd, 0.0f, c0, c1, c2, c3);
+            ci = rcp(cd);
+            ct = wt;
+            B = S.blas[__float_as_uint(c0.w)];
+            const float4 r0 = ldg4(B.nodes), r1 = ldg4(B.nodes + 1);
+            if (COUNT) cnt.blas_nodes++;
+            w0 = __float_as_uint(r0.w);
+            w1 = __float_as_uint(r1.w);
+            level = 1; bsp = 0; hit_here = false;
+        } else if (level == 1u && w1 > 0u) {
+            // BLAS leaf: its triangles in index-list order
+            for (uint32_t i = w0; i < w0 + w1; ++i) {
+                const float4* tp = B.tris + 3ull * i;
+                const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+                if (COUNT) cnt.tris++;
+                float bu, bv;
+                if (tri_hit(xyz(a), xyz(b), xyz(c), co, cd, ct, bu, bv, no_cull)) {
+                    h.prim = __float_as_uint(a.w);
+                    h.u = bu; h.v = bv;
+                    hit_here = true;
+                    if (ANY) { h.inst = ii; h.t = ct; finish = true; break; }
                 }
-                tstack[tsp++] = R;
+            }
+            pop = !finish;
+        } else {
+            // interior node, TLAS or BLAS: the two children, nearer first
+            const float4* pa;
+            const float4* pb;
+            if (level == 0u) {
+                pa = S.tnodes + 2ull * (w0 >> 16);
+                pb = S.tnodes + 2ull * (w0 & 0xFFFFu);
+            } else {
+                pa = B.nodes + 2ull * w0;
+                pb = pa + 2;
+            }
+            const float4 a0 = ldg4(pa), a1 = ldg4(pa + 1), b0 = ldg4(pb), b1 = ldg4(pb + 1);
+            if (COUNT) { if (level == 0u) cnt.tlas_nodes += 2; else cnt.blas_nodes += 2; }
+            float dl = slab(xyz(a0), xyz(a1), co, ci, ct);
+            float dr = slab(xyz(b0), xyz(b1), co, ci, ct);
+            uint2 L = make_uint2(__float_as_uint(a0.w), __float_as_uint(a1.w));
+            uint2 R = make_uint2(__float_as_uint(b0.w), __float_as_uint(b1.w));
+            if (dl > dr) {
+                float td = dl; dl = dr; dr = td;
+                uint2 tn = L; L = R; R = tn;
+            }
+            if (dl == FLT_MAX) {
+                pop = true;
+            } else {
+                w0 = L.x; w1 = L.y;
+                if (dr != FLT_MAX) {
+                    int& sp = level == 0u ? tsp : bsp;
+                    if (sp == kStack) {
+                        h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
+                        finish = true; ok = false; overflow = true;
+                    } else {
+                        if (level == 0u) tstack[tsp++] = R; else bstack[bsp++] = R;
+                    }
+                }
             }
         }
+        if (pop) {
+            if (level == 1u) {
+                if (bsp > 0) {
+                    const uint2 e = bstack[--bsp];
+                    w0 = e.x; w1 = e.y;
+                    pop = false;
+                } else {
+                    // leave the instance: ray.t = ray_local.t (accelstruct.hlsl:146, 170-174)
+                    wt = ct;
+                    if (hit_here) { h.inst = ii; h.t = wt; }
+                    level = 0;
+                    co = wo; cd = wd; ci = rcp(wd); ct = wt;
+                }
+            }
+            if (pop) {
+                if (tsp > 0) {
+                    const uint2 e = tstack[--tsp];
+                    w0 = e.x; w1 = e.y;
+                } else {
+                    finish = true;
+                }
+            }
+        }
+        if (finish) {
+            io.store(ri, h, ok);
+            ri = kNoRay;
+        }
     }
-    return true;
 }
 
 // Adds a thread's fetch counts to the global counters (one atomic per warp).
