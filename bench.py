@@ -220,6 +220,39 @@ def run_reference(args, rank, world):
         dist.destroy_process_group()
 
 
+def adjoint_leg(device, tlas_metric):
+    """Differentiable configuration: box scene (20,506 triangles) at 512x512,
+    64 spp, depth 6; per-triangle albedo 0.5, emitter strength 10, L2 loss to a
+    target rendered with albedo U[0.1, 0.9] (seed 2).  Returns forward and
+    adjoint samples per pixel per second (GPU time, CUDA events)."""
+    import wavefrontpathtracing_gb300 as wf
+    from wavefrontpathtracing_gb300 import scenes
+    from tests.helpers import load_scene_into
+    w = h = 512
+    spp, depth, seed = 64, 6, 5
+    desc = scenes.box_scene(width=w, height=h, max_bounces=depth)
+    with wf.Renderer(w, h, device=device, tlas_metric=tlas_metric) as r:
+        load_scene_into(r, desc)
+        n = r.scene_triangle_count()
+        rng = np.random.default_rng(2)
+        r.set_albedo(rng.uniform(0.1, 0.9, (n, 3)).astype(np.float32))
+        r.render(max_bounces=depth, spp=spp, frame_seed=seed, accumulate=False)
+        target = r.read_image()[..., :3]
+        r.set_albedo(np.full((n, 3), 0.5, np.float32))
+        r.set_emission(2, 10.0)
+        fwd, adj = [], []
+        for it in range(3):
+            r.render(max_bounces=depth, spp=spp, frame_seed=seed, accumulate=False, profile=False)
+            img = r.read_image()[..., :3]
+            fwd.append(r.stats()["ms_total"])
+            r.adjoint(2.0 * (img - target), max_bounces=depth, spp=spp, frame_seed=seed)
+            adj.append(r.stats()["ms_total"])
+        f_ms, a_ms = min(fwd[1:]), min(adj[1:])
+        return {"config": "box scene 512x512, 64 spp, depth 6, 20,506 per-triangle albedos + emitter strength",
+                "forward_spp_per_s": round(spp / (f_ms / 1e3), 2), "grad_spp_per_s": round(spp / (a_ms / 1e3), 2),
+                "ratio": round(f_ms / a_ms, 3), "forward_ms": round(f_ms, 3), "adjoint_ms": round(a_ms, 3)}
+
+
 def flush_l2(torch, buf):
     if buf is not None:
         buf.add_(1)
@@ -307,6 +340,9 @@ def run_ours(args, rank, world, local):
         cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                "sample": sdesc + "; reference TLAS metric"}
     r.close()
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = adjoint_leg(local, args.tlas_metric)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(t_max / args.steps, 3), "higher_is_better": True,
@@ -330,9 +366,84 @@ def run_ours(args, rank, world, local):
                 "clocks": clk.summary()}
         if cpu:
             line["cpu_baseline"] = cpu
+        if adjoint:
+            line["adjoint"] = adjoint
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_traversal(args, rank, world, local):
+    """Traversal micro-benchmark: 8M soup triangles (centroids uniform in the
+    unit cube, log-normal edges mu=-5 sigma=0.5, seed 7), one BLAS (16 bins,
+    <= 4 triangles per leaf) under a 1-instance TLAS; 16.8M coherent pinhole
+    rays (4096^2) and 16.8M incoherent rays (origins in the cube, uniform
+    directions); closest hit and any hit (tmax U[0,1]).  Prints one JSON line
+    per ray set / query kind (the headline line is the default workload)."""
+    import torch
+    import wavefrontpathtracing_gb300 as wf
+    from wavefrontpathtracing_gb300 import scenes
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    n_tris = args.soup_triangles
+    side = args.soup_side
+    tris = scenes.triangle_soup(n_tris, seed=7)
+    peak, peak_kind = measured_peaks()
+    with wf.Renderer(16, 16, device=local) as r:
+        t0 = time.perf_counter()
+        mesh = r.create_mesh_from_triangles(tris, interval_count=16, max_leaf_prims=4)
+        build_s = time.perf_counter() - t0
+        r.begin_scene(scenes.make_view((0.5, 0.5, -1.0), (0.5, 0.5, 0.5), 60.0, 16, 16))
+        r.submit_render_mesh(mesh, np.eye(4))
+        r.end_scene()
+        blas_bytes = len(r.mesh_blas(mesh))
+        for kind in ("coherent", "incoherent"):
+            rays = scenes.soup_rays(side, seed=7, kind=kind)
+            for any_hit in (False, True):
+                if any_hit:
+                    rays["tmax"] = np.random.default_rng(9).uniform(0, 1, len(rays)).astype(np.float32)
+                d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+                d_hits = torch.zeros(len(rays) * 20, dtype=torch.uint8, device="cuda")
+                torch.cuda.synchronize()
+                for _ in range(args.warmup):
+                    r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit)
+                r.synchronize()
+                ms = []
+                l2 = torch.zeros(L2_BYTES // 4, dtype=torch.float32, device="cuda")
+                for _ in range(args.steps):
+                    l2.add_(1)
+                    torch.cuda.synchronize()
+                    r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit)
+                    ms.append(r.stats()["ms_total"])
+                r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit, count_traffic=True)
+                c = r.stats()
+                alg = (len(rays) * (B_RAY + B_HIT) + c["tlas_node_loads"] * B_TNODE + c["instance_loads"] * B_INST
+                       + c["blas_node_loads"] * B_BNODE + c["triangle_tests"] * B_TRI)
+                t = float(np.mean(ms))
+                hits = d_hits.cpu().numpy().view(wf.abi.hit_dtype)
+                # e2e: host rays in, host hits out
+                t1 = time.perf_counter()
+                r.trace(rays, any_hit=any_hit)
+                e2e_s = time.perf_counter() - t1
+                line = {"metric": "traversal Mrays/s", "value": round(len(rays) / (t / 1e3) / 1e6, 2),
+                        "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                        "ms_per_step": round(t, 3), "higher_is_better": True, "dtype": "f32",
+                        "data": "synthetic (seeded triangle soup)",
+                        "config": {"workload": f"traversal micro-benchmark, {n_tris} soup triangles, {len(rays)} "
+                                               f"{kind} rays, {'any' if any_hit else 'closest'} hit",
+                                   "blas_bytes": blas_bytes, "gpu_bvh_build_s": round(build_s, 3),
+                                   "hit_fraction": round(float((hits['instance'] != 0xFFFFFFFF).mean()), 4)},
+                        "e2e": {"value": round(len(rays) / e2e_s / 1e6, 2), "unit": "Mrays/s",
+                                "h2d_bytes_per_step": int(rays.nbytes), "d2h_bytes_per_step": int(len(rays) * 20)},
+                        "roofline": {"bound": "hbm", "kernel": "k_trace (AoS)",
+                                     "achieved": round(alg / (t / 1e3) / 1e9, 1), "peak": peak, "peak_kind": peak_kind,
+                                     "unit": "GB/s", "frac": round(alg / (t / 1e3) / 1e9 / peak, 4),
+                                     "alg_bytes_per_launch": int(alg),
+                                     "fetches_per_ray": round((c["blas_node_loads"] + c["tlas_node_loads"]) / len(rays), 2),
+                                     "triangle_tests_per_ray": round(c["triangle_tests"] / len(rays), 2)}}
+                print(json.dumps(line), flush=True)
+                del d_rays, d_hits
 
 
 def main():
@@ -345,6 +456,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rendering leg")
+    ap.add_argument("--workload", default="instanced", choices=["instanced", "traversal"])
+    ap.add_argument("--soup-triangles", type=int, default=8_000_000)
+    ap.add_argument("--soup-side", type=int, default=4096, help="rays per set = side^2")
     ap.add_argument("--res", default="1920x1080", help="image size WxH (the workload is 1920x1080; smaller sizes "
                                                        "are for profiling captures)")
     args = ap.parse_args()
@@ -353,7 +468,9 @@ def main():
     global W, H
     W, H = (int(x) for x in args.res.lower().split("x"))
     rank, world, local = dist_env()
-    if args.impl == "reference":
+    if args.workload == "traversal":
+        run_traversal(args, rank, world, local)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world, local)

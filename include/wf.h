@@ -94,8 +94,9 @@ typedef struct wf_render_options {
 } wf_render_options;
 
 enum wf_trace_flags {
-    WF_TRACE_ANY_HIT = 1u,   /* stop at the first accepted hit (shadow-ray query) */
-    WF_TRACE_NO_CULL = 2u    /* accept back-facing triangles (|det| test) */
+    WF_TRACE_ANY_HIT = 1u,       /* stop at the first accepted hit (shadow-ray query) */
+    WF_TRACE_NO_CULL = 2u,       /* accept back-facing triangles (|det| test) */
+    WF_TRACE_COUNT_TRAFFIC = 4u  /* count node/instance/triangle fetches into wf_stats (slower) */
 };
 
 /* Counters and timings of the most recent wf_render / wf_trace call. */
@@ -169,6 +170,26 @@ int wf_read_image(wf_ctx* ctx, float* out_rgba, uint64_t float_count);
 /* post_process.hlsl:25-72: NaN/Inf flag, Reinhard, linear->sRGB, RGBA8. */
 int wf_read_image_ldr(wf_ctx* ctx, uint8_t* out_rgba8, uint64_t byte_count);
 int wf_get_stats(wf_ctx* ctx, wf_stats* out);
+
+/* ---- differentiable rendering (no counterpart in the reference) ---------- */
+/* Number of scene triangles: the instances' triangles in submission order,
+ * each instance's in primitive order.  Valid after wf_scene_end. */
+int wf_scene_triangle_count(wf_ctx* ctx, uint64_t* out_count);
+/* Per scene triangle RGB albedo (3 floats each), replacing the instances'
+ * base colours until the next wf_scene_begin; NULL restores them. */
+int wf_scene_set_albedo(wf_ctx* ctx, const float* rgb, uint64_t triangle_count);
+/* Sets an instance's emissive_strength and rebuilds the scene tables. */
+int wf_scene_set_emission(wf_ctx* ctx, uint32_t instance, float strength);
+/* Path-replay adjoint of the image that wf_render(settings, opts, frame_seed)
+ * produces with accumulate = 0: dloss_dimage = d(loss)/d(average radiance),
+ * 3 floats per pixel (row-major); writes d(loss)/d(albedo) (3 floats per scene
+ * triangle) and d(loss)/d(emissive_strength) (1 per instance).  Each wave is
+ * traced once forward (path radiance L) and replayed from the same per-path
+ * seeds, adding w*L/albedo at every Lambert vertex and w.L/strength at the
+ * emitter (w = dloss_dimage / spp) with atomics — memory O(paths), no tape.
+ * Requires wf_scene_set_albedo, nee = 0 and Russian roulette off. */
+int wf_adjoint(wf_ctx* ctx, const render_settings_t* settings, const wf_render_options* opts, uint32_t frame_seed,
+               const float* dloss_dimage, float* d_albedo, float* d_emission);
 
 /* ---- ray queries (extend.hlsl / accelstruct.hlsl:151-218) ---------------- */
 /* Traces host rays against the current scene; copies in, traces, copies out. */

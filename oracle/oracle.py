@@ -32,7 +32,8 @@ class _Mesh(ctypes.Structure):
 
 class _Scene(ctypes.Structure):
     _fields_ = [("meshes", ctypes.POINTER(_Mesh)), ("mesh_count", ctypes.c_uint32), ("tlas", ctypes.c_void_p),
-                ("inst", ctypes.c_void_p), ("inst_count", ctypes.c_uint32)]
+                ("inst", ctypes.c_void_p), ("inst_count", ctypes.c_uint32), ("tri_albedo", ctypes.c_void_p),
+                ("inst_tri_offset", ctypes.c_void_p)]
 
 
 class Counters(ctypes.Structure):
@@ -86,6 +87,8 @@ def lib():
                                  ctypes.POINTER(RenderStats), i32]
         L.orc_render_f64.argtypes = [ctypes.POINTER(_Scene), ctypes.POINTER(View), ctypes.POINTER(RenderParams),
                                      vp, i32]
+        L.orc_adjoint_f64.argtypes = [ctypes.POINTER(_Scene), ctypes.POINTER(View), ctypes.POINTER(RenderParams), vp,
+                                      vp, vp]
         L.orc_wang_hash.argtypes = [u32]
         L.orc_wang_hash.restype = u32
         L.orc_rand_float.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
@@ -175,7 +178,42 @@ class Scene:
             arr[i].blas = b.ctypes.data
         self._meshes = arr
         self.c = _Scene(arr, len(meshes), self._tlas.ctypes.data, self._inst.ctypes.data if len(self._inst) else None,
-                        len(self._inst))
+                        len(self._inst), None, None)
+        self._albedo = None
+        counts = [len(self._tris[m]) for m in self._inst["mesh"]]
+        self.inst_tri_offset = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint32) if counts else \
+            np.zeros(0, np.uint32)
+        self.triangle_count = int(sum(counts))
+
+    def set_albedo(self, rgb):
+        """Per scene triangle albedo (triangle_count x 3), or None for the materials."""
+        if rgb is None:
+            self._albedo = None
+            self.c.tri_albedo = None
+            self.c.inst_tri_offset = None
+            return
+        self._albedo = np.ascontiguousarray(rgb, dtype=np.float64).reshape(-1)
+        assert len(self._albedo) == 3 * self.triangle_count
+        self.c.tri_albedo = self._albedo.ctypes.data
+        self.c.inst_tri_offset = self.inst_tri_offset.ctypes.data
+
+    def set_emission(self, instance, strength):
+        self._inst[instance]["material"]["emissive_strength"] = strength
+
+    def adjoint(self, view, width, height, dloss_dimage, max_bounces=6, spp=1, frame_seed=1, cosine=1,
+                env_color=(0.0, 0.0, 0.0), env_strength=1.0):
+        p = RenderParams()
+        p.max_bounces, p.cosine_weighted_diffuse, p.hdr_env_strength = max_bounces, cosine, env_strength
+        p.env_color[:] = env_color
+        p.spp, p.sample_offset, p.nee, p.rr_start_depth, p.frame_seed = spp, 0, 0, 0xFFFFFFFF, frame_seed
+        d = np.ascontiguousarray(dloss_dimage, dtype=np.float64).reshape(-1)
+        assert len(d) == 3 * width * height
+        ga = np.zeros(3 * self.triangle_count, dtype=np.float64)
+        ge = np.zeros(len(self._inst), dtype=np.float64)
+        rc = lib().orc_adjoint_f64(ctypes.byref(self.c), ctypes.byref(view), ctypes.byref(p), ptr(d), ptr(ga), ptr(ge))
+        if rc != 0:
+            raise ValueError("oracle adjoint failed")
+        return ga.reshape(-1, 3), ge
 
     def trace(self, rays, flags=0, threads=1, f64=False):
         rays = np.ascontiguousarray(rays, dtype=ray_dtype)

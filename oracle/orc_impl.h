@@ -328,11 +328,21 @@ typedef struct {
     orc_render_stats st;
 } FN(tstate);
 
+typedef struct {
+    uint32_t n;
+    uint32_t tri[32];       /* scene triangle of each Lambert vertex */
+    R rho[32][3];           /* its albedo */
+    uint32_t emitter;       /* instance whose emission ended the path, or WF_INVALID_INDEX */
+    R strength;
+} FN(record);
+
 /* One camera path of the wavefront loop (generate.hlsl, extend.hlsl,
  * shade.hlsl:42-174 and the added connect stage).  acc is the path's own
  * radiance, which receives the contributions in the order the GPU stages add
  * them (shade at depth d, then connect at depth d, then depth d+1). */
-static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_render_stats* st) {
+static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_render_stats* st,
+                     FN(record)* rec) {
+    if (rec) { rec->n = 0; rec->emitter = WF_INVALID_INDEX; rec->strength = K(0.0); }
     const orc_scene* s = J->s;
     const orc_render_params* P = J->p;
     uint32_t px = pixel % J->width, py = pixel / J->width;
@@ -372,6 +382,12 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
         const material_t* m = &in->material;
         FN(v3) base = FN(mk)((R)m->base_color_factor[0] * K(1.0), (R)m->base_color_factor[1] * K(1.0),
                              (R)m->base_color_factor[2] * K(1.0));
+        uint32_t stri = 0;
+        if (s->tri_albedo) {
+            stri = s->inst_tri_offset[h.inst] + h.prim;
+            base = FN(mk)((R)s->tri_albedo[3ull * stri], (R)s->tri_albedo[3ull * stri + 1],
+                          (R)s->tri_albedo[3ull * stri + 2]);
+        }
         FN(v3) le = FN(mk)(((R)m->emissive_strength * (R)m->emissive_factor[0]) * K(1.0),
                            ((R)m->emissive_strength * (R)m->emissive_factor[1]) * K(1.0),
                            ((R)m->emissive_strength * (R)m->emissive_factor[2]) * K(1.0));
@@ -392,6 +408,7 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
             acc[0] = acc[0] + (T.x * le.x) * w;
             acc[1] = acc[1] + (T.y * le.y) * w;
             acc[2] = acc[2] + (T.z * le.z) * w;
+            if (rec) { rec->emitter = h.inst; rec->strength = (R)m->emissive_strength; }
             return;
         }
         uint32_t seed = orc_path_seed(P->frame_seed, pixel, sample, d);
@@ -410,6 +427,11 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
         if ((flags & ORC_F_INSIDE) && bsdf != 2 && FN(dot)(N, V) < K(0.0)) N = FN(neg)(N);
         FN(v3) tg, bt;
         FN(basis)(N, &tg, &bt);
+        if (bsdf == 0 && rec && s->tri_albedo && rec->n < 32) {
+            rec->tri[rec->n] = stri;
+            rec->rho[rec->n][0] = base.x; rec->rho[rec->n][1] = base.y; rec->rho[rec->n][2] = base.z;
+            rec->n++;
+        }
         if (bsdf == 0) {
             /* shade.hlsl:107-135 */
             FN(v3) loc;

@@ -261,14 +261,14 @@ static void* render_worker(void* arg) {
                  * adds whole paths in sample order */
                 if (!J->f64) {
                     float L[3] = {0.0f, 0.0f, 0.0f};
-                    path_f32(&j32, px, sample, L, &st);
+                    path_f32(&j32, px, sample, L, &st, NULL);
                     J->acc32[4ull * px] = J->acc32[4ull * px] + L[0];
                     J->acc32[4ull * px + 1] = J->acc32[4ull * px + 1] + L[1];
                     J->acc32[4ull * px + 2] = J->acc32[4ull * px + 2] + L[2];
                     J->acc32[4ull * px + 3] += 1.0f;
                 } else {
                     double L[3] = {0.0, 0.0, 0.0};
-                    path_f64(&j64, px, sample, L, &st);
+                    path_f64(&j64, px, sample, L, &st, NULL);
                     J->acc64[4ull * px] = J->acc64[4ull * px] + L[0];
                     J->acc64[4ull * px + 1] = J->acc64[4ull * px + 1] + L[1];
                     J->acc64[4ull * px + 2] = J->acc64[4ull * px + 2] + L[2];
@@ -328,4 +328,35 @@ int orc_render_f64(const orc_scene* s, const view_t* view, const orc_render_para
                    int threads) {
     if (!accum) return -1;
     return run_render(s, view, p, NULL, accum, NULL, threads);
+}
+
+int orc_adjoint_f64(const orc_scene* s, const view_t* view, const orc_render_params* p, const double* dimg,
+                    double* g_albedo, double* g_emission) {
+    if (!s || !view || !p || !dimg || !g_albedo || !g_emission || !s->tri_albedo || p->nee ||
+        p->rr_start_depth <= p->max_bounces || p->max_bounces > 15)
+        return -1;
+    job_f64 J;
+    memset(&J, 0, sizeof(J));
+    J.s = s; J.view = view; J.p = p; J.width = (uint32_t)view->render_dim[0];
+    build_lights_f64(s, &J.lights);
+    const uint32_t npix = J.width * (uint32_t)view->render_dim[1];
+    const double inv_spp = 1.0 / (double)p->spp;
+    orc_render_stats st;
+    memset(&st, 0, sizeof(st));
+    record_f64 rec;
+    for (uint32_t px = 0; px < npix; ++px) {
+        for (uint32_t si = 0; si < p->spp; ++si) {
+            double L[3] = {0.0, 0.0, 0.0};
+            path_f64(&J, px, p->sample_offset + si, L, &st, &rec);
+            const double w[3] = {dimg[3ull * px] * inv_spp, dimg[3ull * px + 1] * inv_spp, dimg[3ull * px + 2] * inv_spp};
+            for (uint32_t v = 0; v < rec.n; ++v)
+                for (int c = 0; c < 3; ++c)
+                    if (rec.rho[v][c] != 0.0) g_albedo[3ull * rec.tri[v] + c] += w[c] * L[c] / rec.rho[v][c];
+            if (rec.emitter != WF_INVALID_INDEX && rec.strength != 0.0)
+                g_emission[rec.emitter] += (w[0] * L[0] + w[1] * L[1] + w[2] * L[2]) / rec.strength;
+        }
+    }
+    free(J.lights.tri);
+    free(J.lights.cdf);
+    return 0;
 }

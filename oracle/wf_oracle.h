@@ -65,6 +65,10 @@ typedef struct orc_scene {
     const uint8_t* tlas;      /* [tlas_header_t | nodes | bvh_instance_t]; bvh_index = mesh */
     const orc_instance* inst;
     uint32_t inst_count;
+    /* optional per-triangle albedo (3 per scene triangle; NULL = material base
+     * colour); scene triangle of (instance i, primitive p) = inst_tri_offset[i] + p */
+    const double* tri_albedo;
+    const uint32_t* inst_tri_offset;
 } orc_scene;
 
 typedef struct orc_counters {
@@ -112,6 +116,16 @@ int orc_render(const orc_scene* s, const view_t* view, const orc_render_params* 
  * uniform random numbers); accum is double RGBA. */
 int orc_render_f64(const orc_scene* s, const view_t* view, const orc_render_params* p,
                    double* accum, int threads);
+
+/* Path-replay adjoint reference (double precision, single thread): for the
+ * paths orc_render_f64 would trace, accumulates d(loss)/d(albedo) per scene
+ * triangle (3 per triangle) and d(loss)/d(emissive_strength) per instance,
+ * given dloss_dimage = d(loss)/d(average radiance), 3 per pixel.  Every path
+ * contribution is a product of Lambert albedos along the path times the
+ * emitter's strength, so each contributes L/albedo per vertex and L/strength
+ * for its emitter.  Requires nee = 0 and Russian roulette off. */
+int orc_adjoint_f64(const orc_scene* s, const view_t* view, const orc_render_params* p, const double* dloss_dimage,
+                    double* d_albedo, double* d_emission);
 
 /* --- small helpers exported for known-answer tests --------------------------- */
 uint32_t orc_wang_hash(uint32_t seed);

@@ -1,0 +1,102 @@
+"""GPU: the path-replay adjoint (wf_adjoint) for per-triangle albedo and the
+emitter strength, checked against (a) the CPU reference gradient (the
+oracle's FP64 replay of the same paths) and (b) FP64 central finite
+differences of the oracle's image loss (h = 1e-3) on 32 random parameters,
+through the torch.autograd.Function harness."""
+import numpy as np
+import pytest
+
+from wavefrontpathtracing_gb300 import Renderer, scenes
+from tests.helpers import load_scene_into, oracle_scene_from_renderer
+
+pytestmark = pytest.mark.gpu
+
+W = H = 48
+SETTINGS = dict(max_bounces=6, spp=16, frame_seed=3)
+LIGHT = 2   # the emissive ceiling quad is the box scene's third instance
+
+
+@pytest.fixture(scope="module")
+def setup(orc):
+    desc = scenes.box_scene(width=W, height=H, subdivision=2, max_bounces=6)
+    o = desc.bvh_options
+    blobs = [orc.bvh_build(t, o["interval_count"], False, o["max_leaf_prims"]) for t in desc.meshes]
+    r = Renderer(W, H)
+    ids = load_scene_into(r, desc, prebuilt_blobs=blobs)
+    sc, _ = oracle_scene_from_renderer(orc, desc, r, ids)
+    n = r.scene_triangle_count()
+    assert n == sc.triangle_count == 24 + 320 + 2
+    rng = np.random.default_rng(2)
+    truth = rng.uniform(0.1, 0.9, (n, 3)).astype(np.float32)
+    r.set_albedo(truth)
+    r.render(accumulate=False, **SETTINGS)
+    target = r.read_image()[..., :3].astype(np.float64)
+    yield desc, r, sc, n, target
+    r.close()
+
+
+def oracle_loss(sc, desc, albedo, strength, target):
+    sc.set_albedo(albedo)
+    sc.set_emission(LIGHT, strength)
+    acc, _ = sc.render(desc.view, W, H, max_bounces=SETTINGS["max_bounces"], spp=SETTINGS["spp"],
+                       frame_seed=SETTINGS["frame_seed"], f64=True, threads=8)
+    img = acc[..., :3] / acc[..., 3:]
+    return float(np.sum((img - target) ** 2)), img
+
+
+def test_adjoint_matches_cpu_reference_and_finite_differences(orc, setup):
+    torch = pytest.importorskip("torch")
+    from tests.gradcheck_harness import RenderImage
+    desc, r, sc, n, target = setup
+    albedo = torch.full((n, 3), 0.5, dtype=torch.float64, requires_grad=True)
+    strength = torch.tensor(10.0, dtype=torch.float64, requires_grad=True)
+    img = RenderImage.apply(albedo, strength, r, LIGHT, SETTINGS)
+    loss = ((img - torch.from_numpy(target)) ** 2).sum()
+    loss.backward()
+    g_alb = albedo.grad.numpy()
+    g_em = float(strength.grad)
+    assert np.abs(g_alb).max() > 0 and g_em != 0
+
+    # (a) CPU reference gradient: FP64 replay of the same paths
+    base = np.full((n, 3), 0.5)
+    l0, img64 = oracle_loss(sc, desc, base, 10.0, target)
+    assert abs(float(loss.detach()) - l0) <= 1e-3 * max(1.0, l0)
+    ref_a, ref_e = sc.adjoint(desc.view, W, H, 2.0 * (img64 - target), **SETTINGS)
+    scale = np.abs(ref_a).max()
+    # FP32 paths and float atomics against an FP64 replay: relative L2 error and
+    # a per-entry bound (the few paths that take a different triangle in FP64
+    # near an edge move single entries, hence the 99.5 % quantile)
+    rel = np.linalg.norm(g_alb - ref_a) / np.linalg.norm(ref_a)
+    assert rel <= 2e-3, rel
+    err = np.abs(g_alb - ref_a) / (np.abs(ref_a) + 1e-3 * scale)
+    assert np.quantile(err, 0.995) <= 1e-2, np.quantile(err, 0.995)
+    assert abs(g_em - ref_e[LIGHT]) <= 2e-3 * abs(ref_e[LIGHT])
+
+    # (b) FP64 central finite differences on 32 random parameters
+    h = 1e-3
+    rng = np.random.default_rng(7)
+    picks = rng.choice(3 * n, size=31, replace=False)
+    for k in picks:
+        t, c = divmod(int(k), 3)
+        ap, am = base.copy(), base.copy()
+        ap[t, c] += h
+        am[t, c] -= h
+        fd = (oracle_loss(sc, desc, ap, 10.0, target)[0] - oracle_loss(sc, desc, am, 10.0, target)[0]) / (2 * h)
+        assert abs(g_alb[t, c] - fd) <= 1e-2 * max(abs(fd), 0.01 * scale), (t, c, g_alb[t, c], fd)
+    sp, sm = float(np.float32(10.0 + h)), float(np.float32(10.0 - h))   # strengths are stored as float32
+    fd = (oracle_loss(sc, desc, base, sp, target)[0] - oracle_loss(sc, desc, base, sm, target)[0]) / (sp - sm)
+    assert abs(g_em - fd) <= 2e-3 * abs(fd), (g_em, fd)
+
+
+def test_adjoint_rejects_nee_and_roulette(setup):
+    from wavefrontpathtracing_gb300 import WFError
+    from wavefrontpathtracing_gb300.abi import RenderOptions, RenderSettings
+    import ctypes
+    desc, r, sc, n, target = setup
+    s = RenderSettings(1, 1, 0, 6, 1, 0, 1.0)
+    d = np.zeros(3 * W * H, np.float32)
+    ga = np.zeros(3 * n, np.float32)
+    ge = np.zeros(3, np.float32)
+    for o in (RenderOptions(4, 1, 0xFFFFFFFF, 0, 0, 0), RenderOptions(4, 0, 2, 0, 0, 0)):
+        rc = r.L.wf_adjoint(r.h, ctypes.byref(s), ctypes.byref(o), 3, d.ctypes.data, ga.ctypes.data, ge.ctypes.data)
+        assert rc == -1

@@ -59,6 +59,10 @@ SIGNATURES = {
     "wf_bvh_build": [_vp, _vp, _u32, _vp, _vp, _pu64],
     "wf_tlas_build": [_vp, _vp, _u32, _vp, _pu64],
     "wf_tlas_build_noalloc": [_vp, _u32, _vp, _u32, _vp],
+    "wf_scene_triangle_count": [_vp, _pu64],
+    "wf_scene_set_albedo": [_vp, _vp, _u64],
+    "wf_scene_set_emission": [_vp, _u32, ctypes.c_float],
+    "wf_adjoint": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
 }
 _RESTYPES = {"wf_status_string": ctypes.c_char_p, "wf_last_error": ctypes.c_char_p}
 
@@ -208,6 +212,35 @@ class Renderer:
         o = RenderOptions(spp, nee, rr_start_depth, wave_paths, int(profile), int(count_traffic))
         check(self.L.wf_render(self.h, ctypes.byref(s), ctypes.byref(o), frame_seed))
 
+    # ---- differentiable rendering
+    def scene_triangle_count(self):
+        n = ctypes.c_uint64()
+        check(self.L.wf_scene_triangle_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def set_albedo(self, rgb):
+        """Per scene triangle albedo, shape (triangle_count, 3); None restores the materials."""
+        if rgb is None:
+            check(self.L.wf_scene_set_albedo(self.h, None, 0))
+            return
+        a = np.ascontiguousarray(rgb, dtype=np.float32).reshape(-1)
+        check(self.L.wf_scene_set_albedo(self.h, ptr(a), len(a) // 3))
+
+    def set_emission(self, instance, strength):
+        check(self.L.wf_scene_set_emission(self.h, instance, strength))
+
+    def adjoint(self, dloss_dimage, max_bounces=6, spp=1, frame_seed=1, cosine=1, env_strength=1.0, wave_paths=0,
+                profile=False):
+        """Returns (d_albedo (triangles x 3), d_emission (instances,))."""
+        s = RenderSettings(1, 1, 0, max_bounces, cosine, 0, env_strength)
+        o = RenderOptions(spp, 0, 0xFFFFFFFF, wave_paths, int(profile), 0)
+        d = np.ascontiguousarray(dloss_dimage, dtype=np.float32).reshape(-1)
+        assert len(d) == 3 * self.width * self.height
+        ga = np.zeros(3 * self.scene_triangle_count(), dtype=np.float32)
+        ge = np.zeros(len(self.scene_instances()), dtype=np.float32)
+        check(self.L.wf_adjoint(self.h, ctypes.byref(s), ctypes.byref(o), frame_seed, ptr(d), ptr(ga), ptr(ge)))
+        return ga.reshape(-1, 3), ge
+
     def read_image(self):
         out = np.zeros((self.height, self.width, 4), dtype=np.float32)
         check(self.L.wf_read_image(self.h, ptr(out), out.size))
@@ -239,8 +272,9 @@ class Renderer:
         check(self.L.wf_trace(self.h, ptr(rays), len(rays), ptr(hits), flags))
         return hits
 
-    def trace_device(self, d_rays, n, d_hits, any_hit=False, no_cull=False):
-        flags = (abi.TRACE_ANY_HIT if any_hit else 0) | (abi.TRACE_NO_CULL if no_cull else 0)
+    def trace_device(self, d_rays, n, d_hits, any_hit=False, no_cull=False, count_traffic=False):
+        flags = (abi.TRACE_ANY_HIT if any_hit else 0) | (abi.TRACE_NO_CULL if no_cull else 0) | \
+            (abi.TRACE_COUNT_TRAFFIC if count_traffic else 0)
         check(self.L.wf_trace_device(self.h, ctypes.c_void_p(d_rays), n, ctypes.c_void_p(d_hits), flags))
 
     def bvh_build(self, tris, interval_count=8, subdivide_single_prim=False, max_leaf_prims=0):

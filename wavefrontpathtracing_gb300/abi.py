@@ -32,7 +32,7 @@ for _dt, _size in ((vertex_dtype, 48), (triangle_dtype, 144), (material_dtype, 5
 
 INVALID = 0xFFFFFFFF
 BSDF_LAMBERT, BSDF_METAL, BSDF_DIELECTRIC = 0, 1, 2
-TRACE_ANY_HIT, TRACE_NO_CULL = 1, 2
+TRACE_ANY_HIT, TRACE_NO_CULL, TRACE_COUNT_TRAFFIC = 1, 2, 4
 
 
 class RenderSettings(ctypes.Structure):

@@ -119,6 +119,12 @@ struct wf_ctx {
     uint32_t light_count = 0;
     float light_total = 0.0f;
     std::vector<bvh_instance_t> scene_bi;
+    uint64_t scene_triangles = 0;           // sum of the instances' triangle counts
+    bool albedo_set = false;
+    DevBuf<float4> tri_albedo;              // per scene triangle (wf_scene_set_albedo)
+    DevBuf<uint32_t> inst_tri_offset;
+    DevBuf<float4> L_final, dimage, g_albedo;   // adjoint buffers
+    DevBuf<float> g_emission;
 
     // wavefront buffers
     bool buffers_ready = false;
@@ -526,6 +532,8 @@ int wf_destroy(wf_ctx* c) {
     release_buffers(c);
     c->tnodes.release(); c->tinst.release(); c->sinst.release(); c->blas.release(); c->stri.release();
     c->lights.release(); c->aabbs.release(); c->tlas_scratch.release();
+    c->tri_albedo.release(); c->inst_tri_offset.release(); c->L_final.release(); c->dimage.release();
+    c->g_albedo.release(); c->g_emission.release();
     c->image.release(); c->image_ldr.release(); c->trace_io.release();
     dev_free(c->status); dev_free(c->counters); dev_free(c->totals); dev_free(c->trace_fetch);
     for (EventPair& p : c->events) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
@@ -635,6 +643,7 @@ int wf_scene_begin(wf_ctx* c, const view_t* view, const wf_env* env) {
     c->instances.clear();
     c->in_scene = true;
     c->scene_ready = false;
+    c->albedo_set = false;
     return WF_OK;
 }
 
@@ -705,6 +714,8 @@ int wf_scene_end(wf_ctx* c) {
     std::vector<float> aabbs(6ull * n);
     std::vector<float4> ti(4ull * n), si(6ull * n);
     c->scene_bi.resize(n);
+    c->scene_triangles = 0;
+    for (uint32_t i = 0; i < n; ++i) c->scene_triangles += c->meshes[c->instances[i].mesh].tri_count;
     for (uint32_t i = 0; i < n; ++i) {
         const Instance& in = c->instances[i];
         c->scene_bi[i] = in.bi;
@@ -728,7 +739,7 @@ int wf_scene_end(wf_ctx* c) {
                                        mt.metallic_factor);
         si[6ull * i + 5] = make_float4(mt.emissive_strength * mt.emissive_factor[0],
                                        mt.emissive_strength * mt.emissive_factor[1],
-                                       mt.emissive_strength * mt.emissive_factor[2], 0.0f);
+                                       mt.emissive_strength * mt.emissive_factor[2], mt.emissive_strength);
     }
     if ((rc = c->tnodes.reserve(2ull * std::max<uint32_t>(2 * n, 1))) || (rc = c->tinst.reserve(ti.size())) ||
         (rc = c->sinst.reserve(si.size())) || (rc = c->aabbs.reserve(aabbs.size())) ||
@@ -818,25 +829,51 @@ int wf_scene_get_tlas(wf_ctx* c, void* out, uint64_t* inout_size) {
 
 // ---------------------------------------------------------------------------- rendering
 
-int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o, uint32_t frame_seed) {
-    if (!c || !s || !o) return fail(WF_ERR_INVALID, "wf_render: null argument");
-    if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_render: call wf_scene_end first");
-    if (s->max_bounces >= kMaxDepth - 1) return fail(WF_ERR_INVALID, "wf_render: max_bounces must be < 15");
-    if (o->spp == 0) return fail(WF_ERR_INVALID, "wf_render: spp must be >= 1");
-    if (s->render_view_mode != RENDER_VIEW_MODE_NONE)
-        return fail(WF_ERR_INVALID, "wf_render: only RENDER_VIEW_MODE_NONE is implemented");
-    int rc = use_device(c);
-    if (rc) return rc;
-    if ((rc = ensure_buffers(c))) return rc;
-    if ((rc = begin_call(c, o->count_traffic != 0))) return rc;
-    const uint32_t npix = c->width * c->height;
-    if (!s->accumulate || c->view_changed) {
-        WF_CUDA(cudaMemsetAsync(c->accum, 0, (size_t)npix * sizeof(float4), c->stream));
-        c->accum_samples = 0;
-        c->view_changed = false;
+}  // extern "C"
+
+namespace {
+
+struct Wave {
+    uint32_t s0, k, p0, np;
+};
+
+// Waves: whole images of k samples when a wave holds at least one image, else
+// pixel ranges of one sample.  Results do not depend on the split: every
+// path's random numbers are keyed by (pixel, sample, depth) and the resolve
+// adds paths to a pixel in sample order.
+std::vector<Wave> plan_waves(uint32_t spp, uint32_t npix, uint32_t wave) {
+    std::vector<Wave> waves;
+    if (wave >= npix) {
+        const uint32_t k = wave / npix;
+        for (uint32_t si = 0; si < spp; si += k) waves.push_back({si, std::min(k, spp - si), 0u, npix});
+    } else {
+        for (uint32_t si = 0; si < spp; ++si)
+            for (uint32_t p0 = 0; p0 < npix; p0 += wave) waves.push_back({si, 1u, p0, std::min(wave, npix - p0)});
     }
-    const uint32_t wave = o->wave_paths ? std::min(o->wave_paths, c->capacity) : c->capacity;
-    WaveParams W{};
+    return waves;
+}
+
+struct Pass {
+    WaveParams W;
+    SceneRefs S;
+    ShadeRefs SH;
+    RenderBuffers B;
+    bool nee, prof, cnt;
+};
+
+int validate_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o, const char* who) {
+    if (!c || !s || !o) return fail(WF_ERR_INVALID, std::string(who) + ": null argument");
+    if (!c->scene_ready) return fail(WF_ERR_STATE, std::string(who) + ": call wf_scene_end first");
+    if (s->max_bounces >= kMaxDepth - 1) return fail(WF_ERR_INVALID, std::string(who) + ": max_bounces must be < 15");
+    if (o->spp == 0) return fail(WF_ERR_INVALID, std::string(who) + ": spp must be >= 1");
+    if (s->render_view_mode != RENDER_VIEW_MODE_NONE)
+        return fail(WF_ERR_INVALID, std::string(who) + ": only RENDER_VIEW_MODE_NONE is implemented");
+    return WF_OK;
+}
+
+Pass make_pass(wf_ctx* c, const render_settings_t* s, const wf_render_options* o, uint32_t frame_seed) {
+    Pass P{};
+    WaveParams& W = P.W;
     for (int k = 0; k < 4; ++k) {
         const float* m1 = c->view.clip_to_view + 4 * k;
         const float* m2 = c->view.view_to_world + 4 * k;
@@ -854,75 +891,198 @@ int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o,
     W.cosine = s->cosine_weighted_diffuse ? 1u : 0u;
     W.env_strength = s->hdr_env_strength;
     std::memcpy(W.env, c->env, 12);
-    const bool prof = o->profile != 0, cnt = o->count_traffic != 0;
-    const SceneRefs S = scene_refs(c);
-    ShadeRefs SH;
-    SH.sinst = c->sinst.p;
-    SH.stri = c->stri.p;
-    SH.lights = c->lights.p;
-    SH.light_count = c->light_count;
-    SH.light_total = c->light_total;
-    RenderBuffers B = c->B;
-    B.status = c->status;
-    B.counters = c->counters;
-    const bool nee = W.nee && c->light_count > 0;
-    // Waves: whole images of k samples when a wave holds at least one image,
-    // else pixel ranges of one sample.  Results do not depend on the split:
-    // every path's random numbers are keyed by (pixel, sample, depth) and the
-    // resolve adds paths to a pixel in sample order.
-    struct Wave { uint32_t s0, k, p0, np; };
-    std::vector<Wave> waves;
-    if (wave >= npix) {
-        const uint32_t k = wave / npix;
-        for (uint32_t si = 0; si < o->spp; si += k) waves.push_back({si, std::min(k, o->spp - si), 0u, npix});
-    } else {
-        for (uint32_t si = 0; si < o->spp; ++si)
-            for (uint32_t p0 = 0; p0 < npix; p0 += wave) waves.push_back({si, 1u, p0, std::min(wave, npix - p0)});
+    P.S = scene_refs(c);
+    P.SH.sinst = c->sinst.p;
+    P.SH.stri = c->stri.p;
+    P.SH.lights = c->lights.p;
+    P.SH.light_count = c->light_count;
+    P.SH.light_total = c->light_total;
+    P.SH.tri_albedo = c->albedo_set ? c->tri_albedo.p : nullptr;
+    P.SH.inst_tri_offset = c->albedo_set ? c->inst_tri_offset.p : nullptr;
+    P.B = c->B;
+    P.B.status = c->status;
+    P.B.counters = c->counters;
+    P.nee = W.nee && c->light_count > 0;
+    P.prof = o->profile != 0;
+    P.cnt = o->count_traffic != 0;
+    return P;
+}
+
+// One wave through generate -> (extend -> shade -> connect) x depth [-> resolve].
+int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const AdjointRefs& A, bool resolve) {
+    WaveParams& W = P.W;
+    RenderBuffers& B = P.B;
+    W.s0 = sample_base + wv.s0;
+    W.nsamples = wv.k;
+    W.pix0 = wv.p0;
+    W.np = wv.np;
+    W.npaths = wv.k * wv.np;
+    WF_CUDA(cudaMemsetAsync(B.counts, 0, 4 * kMaxDepth * sizeof(uint32_t), c->stream));
+    {
+        StageTimer t(c, P.prof, ST_GENERATE);
+        WF_CUDA(launch_generate(B, W, c->stream));
     }
-    for (const Wave& wv : waves) {
+    c->launches++;
+    for (uint32_t d = 0; d <= W.max_bounces; ++d) {
         {
-            W.s0 = c->accum_samples + wv.s0;
-            W.nsamples = wv.k;
-            W.pix0 = wv.p0;
-            W.np = wv.np;
-            W.npaths = wv.k * wv.np;
-            WF_CUDA(cudaMemsetAsync(B.counts, 0, 4 * kMaxDepth * sizeof(uint32_t), c->stream));
-            {
-                StageTimer t(c, prof, ST_GENERATE);
-                WF_CUDA(launch_generate(B, W, c->stream));
-            }
+            StageTimer t(c, P.prof, ST_EXTEND);
+            WF_CUDA(launch_extend(P.S, B, d, W.npaths, P.cnt, c->totals, c->stream));
+        }
+        {
+            StageTimer t(c, P.prof, ST_SHADE);
+            WF_CUDA(launch_shade(P.SH, B, W, d, W.npaths, A, c->stream));
+        }
+        c->launches += 2;
+        c->launches_extend++;
+        if (P.nee && d < W.max_bounces) {
+            StageTimer t(c, P.prof, ST_CONNECT);
+            WF_CUDA(launch_connect(P.S, B, d, W.npaths, P.cnt, c->totals + 1, c->stream));
             c->launches++;
-            for (uint32_t d = 0; d <= s->max_bounces; ++d) {
-                {
-                    StageTimer t(c, prof, ST_EXTEND);
-                    WF_CUDA(launch_extend(S, B, d, W.npaths, cnt, c->totals, c->stream));
-                }
-                {
-                    StageTimer t(c, prof, ST_SHADE);
-                    WF_CUDA(launch_shade(SH, B, W, d, W.npaths, c->stream));
-                }
-                c->launches += 2;
-                c->launches_extend++;
-                if (nee && d < s->max_bounces) {
-                    StageTimer t(c, prof, ST_CONNECT);
-                    WF_CUDA(launch_connect(S, B, d, W.npaths, cnt, c->totals + 1, c->stream));
-                    c->launches++;
-                    c->launches_connect++;
-                }
-            }
-            {
-                StageTimer t(c, prof, ST_POST);
-                WF_CUDA(launch_wave_resolve(B, W, c->stream));
-            }
-            c->launches++;
+            c->launches_connect++;
         }
     }
+    if (resolve) {
+        {
+            StageTimer t(c, P.prof, ST_POST);
+            WF_CUDA(launch_wave_resolve(B, W, c->stream));
+        }
+        c->launches++;
+    }
+    return WF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o, uint32_t frame_seed) {
+    int rc = validate_render(c, s, o, "wf_render");
+    if (rc) return rc;
+    if ((rc = use_device(c))) return rc;
+    if ((rc = ensure_buffers(c))) return rc;
+    if ((rc = begin_call(c, o->count_traffic != 0))) return rc;
+    const uint32_t npix = c->width * c->height;
+    if (!s->accumulate || c->view_changed) {
+        WF_CUDA(cudaMemsetAsync(c->accum, 0, (size_t)npix * sizeof(float4), c->stream));
+        c->accum_samples = 0;
+        c->view_changed = false;
+    }
+    const uint32_t wave = o->wave_paths ? std::min(o->wave_paths, c->capacity) : c->capacity;
+    Pass P = make_pass(c, s, o, frame_seed);
+    const AdjointRefs none{};
+    for (const Wave& wv : plan_waves(o->spp, npix, wave))
+        if ((rc = run_wave(c, P, wv, c->accum_samples, none, true))) return rc;
     c->accum_samples += o->spp;
     c->stats.paths = (uint64_t)npix * o->spp;
     uint64_t paths = c->stats.paths;
     rc = end_call(c);
     c->stats.paths = paths;
     return rc;
+}
+
+int wf_adjoint(wf_ctx* c, const render_settings_t* s, const wf_render_options* o, uint32_t frame_seed,
+               const float* dloss_dimage, float* d_albedo, float* d_emission) {
+    int rc = validate_render(c, s, o, "wf_adjoint");
+    if (rc) return rc;
+    if (!dloss_dimage || !d_albedo || !d_emission) return fail(WF_ERR_INVALID, "wf_adjoint: null argument");
+    if (!c->albedo_set) return fail(WF_ERR_STATE, "wf_adjoint: set the per-triangle albedo first (wf_scene_set_albedo)");
+    if (o->nee || o->rr_start_depth <= s->max_bounces)
+        return fail(WF_ERR_INVALID, "wf_adjoint: path replay needs nee = 0 and Russian roulette off");
+    if ((rc = use_device(c))) return rc;
+    if ((rc = ensure_buffers(c))) return rc;
+    const uint32_t npix = c->width * c->height;
+    const uint64_t ntri = c->scene_triangles, ninst = c->scene_bi.size();
+    // gradient replicas spread the atomics of heavily hit triangles; at most 256 MiB
+    uint32_t replicas = 32;
+    while (replicas > 1 && (uint64_t)replicas * ntri * sizeof(float4) > (256ull << 20)) replicas >>= 1;
+    if ((rc = c->L_final.reserve(c->capacity)) || (rc = c->dimage.reserve(npix)) ||
+        (rc = c->g_albedo.reserve((uint64_t)replicas * ntri)) || (rc = c->g_emission.reserve(ninst)))
+        return rc;
+    std::vector<float4> dimg(npix);
+    for (uint32_t p = 0; p < npix; ++p)
+        dimg[p] = make_float4(dloss_dimage[3ull * p], dloss_dimage[3ull * p + 1], dloss_dimage[3ull * p + 2], 0.0f);
+    if ((rc = begin_call(c, false))) return rc;
+    WF_CUDA(h2d(c, c->dimage.p, dimg.data(), dimg.size() * sizeof(float4)));
+    WF_CUDA(cudaMemsetAsync(c->g_albedo.p, 0, (uint64_t)replicas * ntri * sizeof(float4), c->stream));
+    WF_CUDA(cudaMemsetAsync(c->g_emission.p, 0, std::max<uint64_t>(ninst, 1) * sizeof(float), c->stream));
+    const uint32_t wave = o->wave_paths ? std::min(o->wave_paths, c->capacity) : c->capacity;
+    Pass P = make_pass(c, s, o, frame_seed);
+    AdjointRefs A{};
+    A.L_final = c->L_final.p;
+    A.dimage = c->dimage.p;
+    A.g_albedo = c->g_albedo.p;
+    A.g_emission = c->g_emission.p;
+    A.inv_spp = 1.0f / (float)o->spp;
+    A.replicas = replicas;
+    A.triangles = (uint32_t)ntri;
+    const AdjointRefs none{};
+    for (const Wave& wv : plan_waves(o->spp, npix, wave)) {
+        // forward pass: each path's radiance, kept for the replay
+        if ((rc = run_wave(c, P, wv, 0, none, false))) return rc;
+        WF_CUDA(cudaMemcpyAsync(c->L_final.p, c->B.ps_L, (size_t)wv.k * wv.np * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, c->stream));
+        // replay: the same paths from the same seeds, accumulating gradients
+        if ((rc = run_wave(c, P, wv, 0, A, false))) return rc;
+    }
+    WF_CUDA(launch_reduce_replicas(c->g_albedo.p, (uint32_t)ntri, replicas, c->stream));
+    c->launches++;
+    std::vector<float4> ga(ntri);
+    std::vector<float> ge(ninst);
+    WF_CUDA(d2h(c, ga.data(), c->g_albedo.p, ntri * sizeof(float4)));
+    if (ninst) WF_CUDA(d2h(c, ge.data(), c->g_emission.p, ninst * sizeof(float)));
+    if ((rc = end_call(c))) return rc;
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    for (uint64_t t = 0; t < ntri; ++t) {
+        d_albedo[3 * t] = ga[t].x;
+        d_albedo[3 * t + 1] = ga[t].y;
+        d_albedo[3 * t + 2] = ga[t].z;
+    }
+    for (uint64_t i = 0; i < ninst; ++i) d_emission[i] = ge[i];
+    c->stats.paths = (uint64_t)npix * o->spp;
+    return take_status(c);
+}
+
+int wf_scene_triangle_count(wf_ctx* c, uint64_t* out) {
+    if (!c || !out) return fail(WF_ERR_INVALID, "wf_scene_triangle_count: null argument");
+    if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_scene_triangle_count: no finished scene");
+    *out = c->scene_triangles;
+    return WF_OK;
+}
+
+int wf_scene_set_albedo(wf_ctx* c, const float* rgb, uint64_t count) {
+    if (!c) return fail(WF_ERR_INVALID, "wf_scene_set_albedo: null context");
+    if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_scene_set_albedo: call wf_scene_end first");
+    if (!rgb) {
+        c->albedo_set = false;
+        return WF_OK;
+    }
+    if (count != c->scene_triangles) return fail(WF_ERR_INVALID, "wf_scene_set_albedo: count != scene triangle count");
+    int rc = use_device(c);
+    if (rc) return rc;
+    std::vector<float4> a(count);
+    for (uint64_t t = 0; t < count; ++t) a[t] = make_float4(rgb[3 * t], rgb[3 * t + 1], rgb[3 * t + 2], 0.0f);
+    std::vector<uint32_t> off(c->scene_bi.size());
+    uint64_t run = 0;
+    for (size_t i = 0; i < off.size(); ++i) {
+        off[i] = (uint32_t)run;
+        run += c->meshes[c->instances[i].mesh].tri_count;
+    }
+    if ((rc = c->tri_albedo.reserve(count)) || (rc = c->inst_tri_offset.reserve(off.size()))) return rc;
+    WF_CUDA(h2d(c, c->tri_albedo.p, a.data(), count * sizeof(float4)));
+    if (!off.empty()) WF_CUDA(h2d(c, c->inst_tri_offset.p, off.data(), off.size() * 4));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    c->albedo_set = true;
+    return WF_OK;
+}
+
+int wf_scene_set_emission(wf_ctx* c, uint32_t instance, float strength) {
+    if (!c) return fail(WF_ERR_INVALID, "wf_scene_set_emission: null context");
+    if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_scene_set_emission: call wf_scene_end first");
+    if (instance >= c->instances.size()) return fail(WF_ERR_INVALID, "wf_scene_set_emission: unknown instance");
+    c->instances[instance].mat.emissive_strength = strength;
+    // rebuild the scene's device tables (instance data, TLAS, emitter table)
+    c->in_scene = true;
+    return wf_scene_end(c);
 }
 
 int wf_read_image(wf_ctx* c, float* out, uint64_t nfloat) {
@@ -970,16 +1130,17 @@ int wf_trace_device(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* h
     if (!c || (n && (!rays || !hits))) return fail(WF_ERR_INVALID, "wf_trace_device: null argument");
     if ((reinterpret_cast<uintptr_t>(rays) & 15u) != 0 || (reinterpret_cast<uintptr_t>(hits) & 3u) != 0)
         return fail(WF_ERR_INVALID, "wf_trace_device: rays must be 16-byte and hits 4-byte aligned");
-    if (flags & ~3u) return fail(WF_ERR_INVALID, "wf_trace_device: unknown flags");
+    if (flags & ~7u) return fail(WF_ERR_INVALID, "wf_trace_device: unknown flags");
     if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_trace_device: call wf_scene_end first");
     int rc = use_device(c);
     if (rc) return rc;
-    if ((rc = begin_call(c, false))) return rc;
+    const bool count = (flags & WF_TRACE_COUNT_TRAFFIC) != 0;
+    if ((rc = begin_call(c, count))) return rc;
     WF_CUDA(cudaMemsetAsync(c->trace_fetch, 0, 4, c->stream));
     {
         StageTimer t(c, true, ST_EXTEND);
-        WF_CUDA(launch_trace_aos(scene_refs(c), rays, n, hits, flags, false, c->trace_fetch, c->status, c->counters,
-                                 c->stream));
+        WF_CUDA(launch_trace_aos(scene_refs(c), rays, n, hits, flags & 3u, count, c->trace_fetch, c->status,
+                                 c->counters, c->stream));
     }
     c->launches++;
     c->launches_extend++;
@@ -990,7 +1151,7 @@ int wf_trace_device(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* h
 
 int wf_trace(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* hits, uint32_t flags) {
     if (!c || (n && (!rays || !hits))) return fail(WF_ERR_INVALID, "wf_trace: null argument");
-    if (flags & ~3u) return fail(WF_ERR_INVALID, "wf_trace: unknown flags");
+    if (flags & ~7u) return fail(WF_ERR_INVALID, "wf_trace: unknown flags");
     if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_trace: call wf_scene_end first");
     if (n == 0) return WF_OK;
     int rc = use_device(c);

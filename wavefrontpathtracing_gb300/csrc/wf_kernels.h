@@ -15,7 +15,27 @@ struct ShadeRefs {
     const LightTri* lights;
     uint32_t light_count;
     float light_total;
+    const float4* tri_albedo;     // optional per scene triangle albedo (replaces the base colour)
+    const uint32_t* inst_tri_offset;  // scene triangle of (instance i, primitive p) = offset[i] + p
 };
+
+// Path-replay adjoint (null pointers in a forward pass).  The replay traces
+// the same paths as the forward pass; every path contribution is the product
+// of the Lambert albedos along the path and the emitter strength, so a vertex
+// on scene triangle t adds w * L / albedo(t) and the emitter adds w . L / strength,
+// with L the path's radiance from the forward pass and w = dloss/dimage / spp.
+struct AdjointRefs {
+    const float4* L_final;        // per path: radiance of the forward pass
+    const float4* dimage;         // per pixel: dloss/d(average radiance)
+    float4* g_albedo;             // replicas x scene triangles (atomic adds to x, y, z)
+    float* g_emission;            // per instance
+    float inv_spp;
+    uint32_t replicas;            // power of two; a warp adds into replica (block ^ warp) % replicas
+    uint32_t triangles;
+};
+
+// Sums the gradient replicas into replica 0.
+cudaError_t launch_reduce_replicas(float4* g, uint32_t triangles, uint32_t replicas, cudaStream_t stream);
 
 // Wavefront buffers: double-buffered ray queues (the reference reads and
 // appends to one ray buffer inside a single shade dispatch, shade.hlsl:52,167),
@@ -65,7 +85,7 @@ cudaError_t launch_generate(const RenderBuffers& B, const WaveParams& W, cudaStr
 cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
                           bool count, unsigned long long* total, cudaStream_t stream);
 cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W, uint32_t depth,
-                         uint32_t max_rays, cudaStream_t stream);
+                         uint32_t max_rays, const AdjointRefs& A, cudaStream_t stream);
 cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
                            bool count, unsigned long long* total, cudaStream_t stream);
 // Adds each pixel's paths of the wave to the accumulator in sample order.

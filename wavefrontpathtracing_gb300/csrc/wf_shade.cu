@@ -100,7 +100,8 @@ __device__ __forceinline__ uint32_t pick_light(const LightTri* L, uint32_t count
     return lo;
 }
 
-__global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B, WaveParams W, uint32_t depth) {
+__global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B, WaveParams W, uint32_t depth,
+                                                  AdjointRefs A) {
     const uint32_t n = B.counts[depth];
     const int cur = depth & 1, nxt = cur ^ 1;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -111,6 +112,8 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
         V3 T = mk(0, 0, 0), norg = mk(0, 0, 0), ndir = mk(0, 0, 0), sdir = mk(0, 0, 0), contrib = mk(0, 0, 0);
         float npdf = 0.0f, stmax = 0.0f;
         V3 spos = mk(0, 0, 0);
+        uint32_t em_key = kInvalid;   // adjoint: emitter instance reached by this path
+        float em_val = 0.0f;
         if (i < n) {
             const float4 d4 = B.q_d[cur][i];
             path = B.q_path[cur][i];
@@ -144,7 +147,12 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
                 const V3 pos = xform(pl, 1.0f, c0, c1, c2, c3);
                 const V3 nl = add(add(n0, scl(sub(n1, n0), hu)), scl(sub(n2, n0), hv));
                 V3 N = normalize(xform(nl, 0.0f, c0, c1, c2, c3));
-                const V3 base_c = mk(mb.x * 1.0f, mb.y * 1.0f, mb.z * 1.0f);
+                V3 base_c = mk(mb.x * 1.0f, mb.y * 1.0f, mb.z * 1.0f);
+                uint32_t stri = 0;
+                if (SH.tri_albedo) {
+                    stri = SH.inst_tri_offset[inst] + prim;
+                    base_c = xyz(SH.tri_albedo[stri]);
+                }
                 const V3 le = mk(me.x * 1.0f, me.y * 1.0f, me.z * 1.0f);
                 if (le.x != 0.0f || le.y != 0.0f || le.z != 0.0f) {
                     float w = 1.0f;
@@ -164,6 +172,12 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
                     acc.y = acc.y + (T.y * le.y) * w;
                     acc.z = acc.z + (T.z * le.z) * w;
                     B.ps_L[path] = acc;
+                    if (A.g_emission && me.w != 0.0f) {
+                        const float4 L = A.L_final[path], g = A.dimage[pixel];
+                        const float gl = (g.x * A.inv_spp) * L.x + (g.y * A.inv_spp) * L.y + (g.z * A.inv_spp) * L.z;
+                        em_key = inst;
+                        em_val = gl / me.w;
+                    }
                 } else {
                     uint32_t seed = path_seed(W.frame_seed, pixel, sample, depth);
                     (void)rand_float(seed);  // r_path (shade.hlsl:81), drawn and unused
@@ -180,6 +194,14 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
                     if ((flags & kFlagInside) && bsdf != 2u && dot(N, V) < 0.0f) N = neg(N);
                     V3 tg, bt;
                     basis(N, tg, bt);
+                    if (bsdf == 0u && A.g_albedo && SH.tri_albedo) {
+                        const float4 L = A.L_final[path], g = A.dimage[pixel];
+                        const uint32_t rep = (blockIdx.x ^ (threadIdx.x >> 5)) & (A.replicas - 1u);
+                        float* ga = reinterpret_cast<float*>(A.g_albedo + (size_t)rep * A.triangles + stri);
+                        if (base_c.x != 0.0f) atomicAdd(ga, ((g.x * A.inv_spp) * L.x) / base_c.x);
+                        if (base_c.y != 0.0f) atomicAdd(ga + 1, ((g.y * A.inv_spp) * L.y) / base_c.y);
+                        if (base_c.z != 0.0f) atomicAdd(ga + 2, ((g.z * A.inv_spp) * L.z) / base_c.z);
+                    }
                     if (bsdf == 0u) {
                         V3 loc;
                         float sn, cs;
@@ -329,6 +351,21 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
                 }
             }
         }
+        if (A.g_emission) {
+            // one atomic per distinct emitter in the warp (usually one)
+            bool pending = em_key != kInvalid;
+            for (;;) {
+                const unsigned rem = __ballot_sync(0xffffffffu, pending);
+                if (!rem) break;
+                const int leader = __ffs(rem) - 1;
+                const uint32_t k = __shfl_sync(0xffffffffu, em_key, leader);
+                const bool mine = pending && em_key == k;
+                float v = mine ? em_val : 0.0f;
+                for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+                if ((int)(threadIdx.x & 31) == leader) atomicAdd(&A.g_emission[k], v);
+                if (mine) pending = false;
+            }
+        }
         const uint32_t slot = warp_append(&B.counts[depth + 1], enqueue);
         if (enqueue) {
             B.q_o[nxt][slot] = make_float4(norg.x, norg.y, norg.z, __uint_as_float(nflags & kFlagInside));
@@ -392,6 +429,18 @@ __global__ void k_resolve(const float4* __restrict__ accum, uint32_t npix, float
     }
 }
 
+__global__ void k_reduce_replicas(float4* g, uint32_t triangles, uint32_t replicas) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < triangles; t += stride) {
+        float4 a = g[t];
+        for (uint32_t r = 1; r < replicas; ++r) {
+            const float4 b = g[(size_t)r * triangles + t];
+            a.x += b.x; a.y += b.y; a.z += b.z;
+        }
+        g[t] = a;
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_generate(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream) {
@@ -400,8 +449,13 @@ cudaError_t launch_generate(const RenderBuffers& B, const WaveParams& W, cudaStr
 }
 
 cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W, uint32_t depth,
-                         uint32_t max_rays, cudaStream_t stream) {
-    k_shade<<<grid_for(max_rays), kBlock, 0, stream>>>(SH, B, W, depth);
+                         uint32_t max_rays, const AdjointRefs& A, cudaStream_t stream) {
+    k_shade<<<grid_for(max_rays), kBlock, 0, stream>>>(SH, B, W, depth, A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_replicas(float4* g, uint32_t triangles, uint32_t replicas, cudaStream_t stream) {
+    k_reduce_replicas<<<grid_for(triangles), kBlock, 0, stream>>>(g, triangles, replicas);
     return cudaGetLastError();
 }
 
