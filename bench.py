@@ -253,6 +253,89 @@ def adjoint_leg(device, tlas_metric):
                 "ratio": round(f_ms / a_ms, 3), "forward_ms": round(f_ms, 3), "adjoint_ms": round(a_ms, 3)}
 
 
+def batched_leg(device, tlas_metric, steps=3, count=64):
+    """Batched configuration: 64 scenes (displaced icosphere soups, triangles
+    log-uniform in [1k, 2M]; square images of side 64..1024; spp 1, 4 or 16;
+    depth 6, NEE, RR from 3) rendered as one batch (one CUDA-graph launch, pool
+    parameters from the autotuner) against the same 64 scenes rendered one
+    after another with wf_render (the plain single-scene wavefront loop).  Both
+    sides are timed on the device with CUDA events; the plain side is the sum
+    of the 64 renders' GPU times.  Camera paths per second over all scenes."""
+    import wavefrontpathtracing_gb300 as wf
+    from wavefrontpathtracing_gb300 import scenes
+    depth, rr, seed = 6, 3, 11
+    t_gen = time.perf_counter()
+    meshes, descs = scenes.batch_scenes(count=count)
+    gen_s = time.perf_counter() - t_gen
+    paths = sum(d.paths for d in descs)
+    kw = dict(max_bounces=depth, nee=1, rr_start_depth=rr)
+    out = {"config": f"{count} scenes, {sum(len(m) for m in meshes[2:])} soup triangles "
+                     f"(per scene {min(d.sphere_triangles for d in descs)}..{max(d.sphere_triangles for d in descs)}), "
+                     f"{paths} camera paths, depth {depth}, NEE, RR from {rr}",
+           "scene_generation_s": round(gen_s, 1)}
+    # --- batched
+    with wf.Renderer(8, 8, device=device, tlas_metric=tlas_metric) as r:
+        ids = [r.create_mesh_from_triangles(t, interval_count=16, max_leaf_prims=4) for t in meshes]
+        b = wf.Batch(r)
+        for d in descs:
+            b.begin_scene(d.width, d.height, d.spp, d.view, d.env)
+            for mesh, l2w, mat in d.instances:
+                b.submit(ids[mesh], l2w, mat)
+            b.end_scene()
+        t_tune = time.perf_counter()
+        cfg = b.autotune(frame_seed=seed, **kw)
+        tune_s = time.perf_counter() - t_tune
+        bms, bst = [], None
+        for i in range(steps):
+            b.render(frame_seed=seed, **kw)
+            bst = b.stats()
+            bms.append(bst["ms_total"])
+        sample = [b.read_image(k) for k in (0, count // 2, count - 1)]
+        b.close()
+    # --- plain: one wf_render per scene, one context per image size
+    pms = [0.0] * steps
+    plain_rays = 0
+    plain_launches = 0
+    equal = True
+    for side in sorted({d.width for d in descs}):
+        group = [(k, d) for k, d in enumerate(descs) if d.width == side]
+        with wf.Renderer(side, side, device=device, tlas_metric=tlas_metric) as r:
+            mid = {}
+            for k, d in group:
+                for mesh, _, _ in d.instances:
+                    if mesh not in mid:
+                        mid[mesh] = r.create_mesh_from_triangles(meshes[mesh], interval_count=16, max_leaf_prims=4)
+            for k, d in group:
+                r.begin_scene(d.view, d.env)
+                for mesh, l2w, mat in d.instances:
+                    r.submit_render_mesh(mid[mesh], l2w, mat)
+                r.end_scene()
+                r.render(spp=d.spp, frame_seed=seed, accumulate=False, **kw)   # warm-up
+                for i in range(steps):
+                    r.render(spp=d.spp, frame_seed=seed, accumulate=False, **kw)
+                    st = r.stats()
+                    pms[i] += st["ms_total"]
+                    if i == 0:
+                        plain_rays += st["rays_extend"] + st["rays_connect"]
+                        plain_launches += st["launches"]
+                if k in (0, count // 2, count - 1):
+                    img = r.read_image()
+                    equal = equal and bool(np.array_equal(img.view(np.uint32),
+                                                          sample[(0, count // 2, count - 1).index(k)].view(np.uint32)))
+    b_ms, p_ms = min(bms), min(pms)
+    rays = bst["rays_extend"] + bst["rays_connect"]
+    out.update({"autotuned": cfg, "autotune_s": round(tune_s, 1),
+                "batched_ms": round(b_ms, 3), "plain_ms": round(p_ms, 3),
+                "speedup_vs_plain": round(p_ms / b_ms, 3),
+                "batched_spp_per_s": round(paths / (b_ms / 1e3), 1), "plain_spp_per_s": round(paths / (p_ms / 1e3), 1),
+                "batched_mrays_per_s": round(rays / (b_ms / 1e3) / 1e6, 1),
+                "plain_mrays_per_s": round(plain_rays / (p_ms / 1e3) / 1e6, 1),
+                "rays_equal": rays == plain_rays, "images_equal_sampled": equal,
+                "iterations": bst["iterations"], "graph_launches": bst["graph_launches"],
+                "device_kernels": bst["kernel_launches"], "plain_launches": plain_launches})
+    return out
+
+
 def flush_l2(torch, buf):
     if buf is not None:
         buf.add_(1)
@@ -343,6 +426,9 @@ def run_ours(args, rank, world, local):
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = adjoint_leg(local, args.tlas_metric)
+    batched = None
+    if rank == 0 and not args.no_batched:
+        batched = batched_leg(local, args.tlas_metric)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(t_max / args.steps, 3), "higher_is_better": True,
@@ -368,6 +454,8 @@ def run_ours(args, rank, world, local):
             line["cpu_baseline"] = cpu
         if adjoint:
             line["adjoint"] = adjoint
+        if batched:
+            line["batched"] = batched
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -457,7 +545,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rendering leg")
-    ap.add_argument("--workload", default="instanced", choices=["instanced", "traversal"])
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes leg")
+    ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--workload", default="instanced", choices=["instanced", "traversal", "batched"])
     ap.add_argument("--soup-triangles", type=int, default=8_000_000)
     ap.add_argument("--soup-side", type=int, default=4096, help="rays per set = side^2")
     ap.add_argument("--res", default="1920x1080", help="image size WxH (the workload is 1920x1080; smaller sizes "
@@ -470,6 +560,14 @@ def main():
     rank, world, local = dist_env()
     if args.workload == "traversal":
         run_traversal(args, rank, world, local)
+    elif args.workload == "batched":
+        if rank == 0:
+            res = batched_leg(local, args.tlas_metric, steps=args.steps, count=args.batch_scenes)
+            print(json.dumps({"metric": "batched camera paths/s vs plain wavefront", "value": res["batched_spp_per_s"],
+                              "unit": "paths/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": res["batched_ms"], "higher_is_better": True, "dtype": "f32",
+                              "data": "synthetic (seeded procedural scenes)", "config": {"workload": res["config"]},
+                              "batched": res}), flush=True)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

@@ -191,6 +191,66 @@ int wf_scene_set_emission(wf_ctx* ctx, uint32_t instance, float strength);
 int wf_adjoint(wf_ctx* ctx, const render_settings_t* settings, const wf_render_options* opts, uint32_t frame_seed,
                const float* dloss_dimage, float* d_albedo, float* d_emission);
 
+/* ---- batched rendering (no counterpart in the reference) ----------------
+ * Many independent scenes, each with its own camera, resolution, spp and
+ * instances of the context's meshes, rendered together.  All scenes share one
+ * pool of paths in flight that is refilled with the scenes' camera paths
+ * whenever the live count falls below a threshold (path regeneration); every
+ * stage reads its sizes from the device, so the whole render is one CUDA-graph
+ * launch whose device-side loop runs until every path has finished.  A scene's
+ * image equals the image wf_render produces for the same scene, settings and
+ * frame_seed with accumulate = 0, bit for bit. */
+typedef struct wf_batch wf_batch;
+
+typedef struct wf_batch_config {
+    uint32_t capacity;        /* paths in flight (pool entries), 1024 .. 2^27; 0 = 2^21 */
+    float    regen_threshold; /* admit new camera paths when fewer than threshold * capacity
+                                 are live, (0, 1]; 0 = 1 (refill every iteration) */
+    uint32_t block;           /* threads per block of regeneration and shading: 128, 256 or 512; 0 = 256 */
+    uint32_t use_graph;       /* 1 = one CUDA-graph launch with a device-side loop (default);
+                                 0 = host-driven loop that polls for completion */
+    uint32_t reserved[4];
+} wf_batch_config;
+
+typedef struct wf_batch_stats {
+    double   ms_total;        /* GPU time of the last wf_batch_render (CUDA events) */
+    uint64_t paths;           /* camera paths: sum over scenes of width * height * spp */
+    uint64_t rays_extend;     /* closest-hit rays traced */
+    uint64_t rays_connect;    /* shadow rays traced */
+    uint64_t kernel_launches; /* kernels the device executed for the last render */
+    uint32_t iterations;      /* pipeline iterations (regenerate, extend, shade, connect) */
+    uint32_t graph_launches;  /* CUDA-graph launches of the last render (0 with the host loop) */
+    uint32_t scenes;
+    uint32_t reserved[3];
+} wf_batch_stats;
+
+/* A batch renders instances of ctx's meshes on ctx's device and stream; it
+ * must be destroyed before ctx. */
+int wf_batch_create(wf_ctx* ctx, wf_batch** out_batch);
+int wf_batch_destroy(wf_batch* batch);
+/* Opens scene *out_scene (numbered from 0): image width x height, spp camera
+ * paths per pixel, view as wf_scene_begin, env NULL = white. */
+int wf_batch_scene_begin(wf_batch* batch, uint32_t width, uint32_t height, uint32_t spp,
+                         const view_t* view, const wf_env* env, uint32_t* out_scene);
+/* wf_instance_submit_ex into the open scene. */
+int wf_batch_instance_submit(wf_batch* batch, uint32_t mesh, const float local_to_world[16],
+                             const wf_material_ext* material);
+int wf_batch_scene_end(wf_batch* batch);
+int wf_batch_set_config(wf_batch* batch, const wf_batch_config* config);
+int wf_batch_get_config(wf_batch* batch, wf_batch_config* out_config);
+/* Renders every scene (opts->spp is ignored: each scene has its own), then
+ * synchronizes.  The first render after a scene change builds the scene tables
+ * (one GPU TLAS per scene) and the CUDA graph. */
+int wf_batch_render(wf_batch* batch, const render_settings_t* settings,
+                    const wf_render_options* opts, uint32_t frame_seed);
+/* Picks capacity, regeneration threshold and block size by timing renders of
+ * this batch (coordinate descent); leaves the best configuration set. */
+int wf_batch_autotune(wf_batch* batch, const render_settings_t* settings,
+                      const wf_render_options* opts, uint32_t frame_seed, wf_batch_config* out_config);
+/* Average radiance of one scene, RGBA float32 (alpha = samples), as wf_read_image. */
+int wf_batch_read_image(wf_batch* batch, uint32_t scene, float* out_rgba, uint64_t float_count);
+int wf_batch_get_stats(wf_batch* batch, wf_batch_stats* out);
+
 /* ---- ray queries (extend.hlsl / accelstruct.hlsl:151-218) ---------------- */
 /* Traces host rays against the current scene; copies in, traces, copies out. */
 int wf_trace(wf_ctx* ctx, const RayDesc2* rays, uint32_t count, hit_result_t* hits, uint32_t flags);

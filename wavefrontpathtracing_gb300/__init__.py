@@ -17,11 +17,13 @@ calls raise WFError.
 """
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
 from . import abi
-from .abi import (BvhOptions, Env, InitParams, RenderOptions, RenderSettings, Stats, View, bvh_instance_dtype,
+from .abi import (BatchConfig, BatchStats, BvhOptions, Env, InitParams, RenderOptions, RenderSettings, Stats, View,
+                  bvh_instance_dtype,
                   hit_dtype, material_dtype, material_ext_dtype, ptr, ray_dtype, triangle_dtype, vertex_dtype)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -63,6 +65,17 @@ SIGNATURES = {
     "wf_scene_set_albedo": [_vp, _vp, _u64],
     "wf_scene_set_emission": [_vp, _u32, ctypes.c_float],
     "wf_adjoint": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
+    "wf_batch_create": [_vp, ctypes.POINTER(_vp)],
+    "wf_batch_destroy": [_vp],
+    "wf_batch_scene_begin": [_vp, _u32, _u32, _u32, _vp, _vp, _pu32],
+    "wf_batch_instance_submit": [_vp, _u32, _vp, _vp],
+    "wf_batch_scene_end": [_vp],
+    "wf_batch_set_config": [_vp, _vp],
+    "wf_batch_get_config": [_vp, _vp],
+    "wf_batch_render": [_vp, _vp, _vp, _u32],
+    "wf_batch_autotune": [_vp, _vp, _vp, _u32, _vp],
+    "wf_batch_read_image": [_vp, _u32, _vp, _u64],
+    "wf_batch_get_stats": [_vp, _vp],
 }
 _RESTYPES = {"wf_status_string": ctypes.c_char_p, "wf_last_error": ctypes.c_char_p}
 
@@ -118,9 +131,12 @@ class Renderer:
         h = ctypes.c_void_p()
         check(L.wf_create(ctypes.byref(p), ctypes.byref(h)))
         self.h, self.L, self.width, self.height = h, L, width, height
+        self._batches = weakref.WeakSet()
 
     def close(self):
         if getattr(self, "h", None):
+            for b in list(self._batches):   # a batch must not outlive its context
+                b.close()
             self.L.wf_destroy(self.h)
             self.h = None
 
@@ -295,4 +311,101 @@ class Renderer:
         return out
 
 
-__all__ = ["Renderer", "WFError", "load", "check", "abi", "SIGNATURES", "View", "LIB_PATH"]
+class Batch:
+    """Many scenes of one Renderer's meshes rendered together (wf_batch_*).
+
+    Each scene has its own camera, resolution, spp and instances; a scene's
+    image equals Renderer.render's image of the same scene (accumulate off)."""
+
+    def __init__(self, renderer):
+        self.r = renderer
+        self.L = renderer.L
+        h = ctypes.c_void_p()
+        check(self.L.wf_batch_create(renderer.h, ctypes.byref(h)))
+        self.h = h
+        self.sizes = []
+        renderer._batches.add(self)
+
+    def close(self):
+        if self.h:
+            self.L.wf_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def begin_scene(self, width, height, spp, view, env=None):
+        e = None
+        if env is not None:
+            e = Env()
+            e.color[:] = list(env)
+        idx = ctypes.c_uint32(0)
+        check(self.L.wf_batch_scene_begin(self.h, width, height, spp, ctypes.byref(view),
+                                          ctypes.byref(e) if e is not None else None, ctypes.byref(idx)))
+        self.sizes.append((width, height))
+        return idx.value
+
+    def submit(self, mesh, transform, material=None):
+        m = _f16(transform)
+        if material is None:
+            material = np.zeros(1, dtype=material_ext_dtype)[0]
+            material["base"]["base_color_factor"] = (0.8, 0.8, 0.8)
+        if material.dtype == material_dtype:
+            ext = np.zeros(1, dtype=material_ext_dtype)
+            ext[0]["base"] = material
+            ext[0]["ior"] = 1.5
+            rec = ext
+        else:
+            rec = np.array([material], dtype=material_ext_dtype)
+        check(self.L.wf_batch_instance_submit(self.h, mesh, ptr(m), ptr(rec)))
+
+    def end_scene(self):
+        check(self.L.wf_batch_scene_end(self.h))
+
+    def config(self):
+        c = BatchConfig()
+        check(self.L.wf_batch_get_config(self.h, ctypes.byref(c)))
+        return c.as_dict()
+
+    def set_config(self, capacity=0, regen_threshold=0.0, block=0, use_graph=1):
+        c = BatchConfig(capacity, regen_threshold, block, use_graph)
+        check(self.L.wf_batch_set_config(self.h, ctypes.byref(c)))
+
+    @staticmethod
+    def _settings(max_bounces, nee, rr_start_depth, cosine, env_strength):
+        s = RenderSettings(1, 1, 0, max_bounces, cosine, 0, env_strength)
+        o = RenderOptions(0, nee, rr_start_depth, 0, 0, 0)
+        return s, o
+
+    def render(self, max_bounces=3, frame_seed=1, nee=0, rr_start_depth=0xFFFFFFFF, cosine=1, env_strength=1.0):
+        s, o = self._settings(max_bounces, nee, rr_start_depth, cosine, env_strength)
+        check(self.L.wf_batch_render(self.h, ctypes.byref(s), ctypes.byref(o), frame_seed))
+
+    def autotune(self, max_bounces=3, frame_seed=1, nee=0, rr_start_depth=0xFFFFFFFF, cosine=1, env_strength=1.0):
+        s, o = self._settings(max_bounces, nee, rr_start_depth, cosine, env_strength)
+        c = BatchConfig()
+        check(self.L.wf_batch_autotune(self.h, ctypes.byref(s), ctypes.byref(o), frame_seed, ctypes.byref(c)))
+        return c.as_dict()
+
+    def read_image(self, scene):
+        w, h = self.sizes[scene]
+        out = np.zeros((h, w, 4), dtype=np.float32)
+        check(self.L.wf_batch_read_image(self.h, scene, ptr(out), out.size))
+        return out
+
+    def stats(self):
+        s = BatchStats()
+        check(self.L.wf_batch_get_stats(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+
+__all__ = ["Renderer", "Batch", "WFError", "load", "check", "abi", "SIGNATURES", "View", "LIB_PATH"]

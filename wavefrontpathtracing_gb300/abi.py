@@ -90,7 +90,27 @@ class Stats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("capacity", ctypes.c_uint32), ("regen_threshold", ctypes.c_float), ("block", ctypes.c_uint32),
+                ("use_graph", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
+
+    def as_dict(self):
+        return {"capacity": self.capacity, "regen_threshold": self.regen_threshold, "block": self.block,
+                "use_graph": self.use_graph}
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("ms_total", ctypes.c_double), ("paths", ctypes.c_uint64), ("rays_extend", ctypes.c_uint64),
+                ("rays_connect", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
+                ("iterations", ctypes.c_uint32), ("graph_launches", ctypes.c_uint32), ("scenes", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 3)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+
+
 assert ctypes.sizeof(RenderSettings) == 28 and ctypes.sizeof(View) == 272
+assert ctypes.sizeof(BatchConfig) == 32 and ctypes.sizeof(BatchStats) == 64
 
 
 def ptr(a):

@@ -14,6 +14,7 @@
 
 #include "../../include/wf.h"
 #include "wf_bvh.h"
+#include "wf_ctx.h"
 #include "wf_kernels.h"
 
 using namespace wf;
@@ -79,15 +80,6 @@ struct Mesh {
     float4* d_nodes = nullptr;
     float4* d_tris = nullptr;         // traversal triangles, leaf order
     float4* d_stri = nullptr;         // shading triangles, original order
-};
-
-struct Instance {
-    uint32_t mesh;
-    float l2w[16], w2l[16];
-    material_t mat;
-    uint32_t bsdf;
-    float ior;
-    bvh_instance_t bi;
 };
 
 struct EventPair {
@@ -450,6 +442,112 @@ int end_call(wf_ctx* c) {
 namespace wf {
 // Lets entry points defined in other translation units set wf_last_error().
 int report_error(int code, const char* msg) { return fail(code, msg); }
+
+int fail_code(int code, const std::string& msg) { return fail(code, msg); }
+int ctx_use_device(wf_ctx* c) { return use_device(c); }
+cudaStream_t ctx_stream(wf_ctx* c) { return c->stream; }
+uint32_t* ctx_status(wf_ctx* c) { return c->status; }
+uint32_t ctx_mesh_count(wf_ctx* c) { return (uint32_t)c->meshes.size(); }
+uint32_t ctx_tlas_metric(wf_ctx* c) { return c->tlas_metric; }
+int ctx_take_status(wf_ctx* c) { return take_status(c); }
+cudaError_t ctx_h2d(wf_ctx* c, void* dst, const void* src, size_t bytes) { return h2d(c, dst, src, bytes); }
+cudaError_t ctx_d2h(wf_ctx* c, void* dst, const void* src, size_t bytes) { return d2h(c, dst, src, bytes); }
+
+bool ctx_mesh(wf_ctx* c, uint32_t mesh, MeshView* out) {
+    if (mesh >= c->meshes.size()) return false;
+    const Mesh& m = c->meshes[mesh];
+    out->tri_count = m.tri_count;
+    out->tris = m.tris.data();
+    out->root_min = m.root_min;
+    out->root_max = m.root_max;
+    out->d_nodes = m.d_nodes;
+    out->d_tris = m.d_tris;
+    out->d_stri = m.d_stri;
+    return true;
+}
+
+int make_instance(wf_ctx* c, uint32_t mesh, const float* l2w, const material_t* mat, uint32_t bsdf, float ior,
+                  const char* who, Instance* out) {
+    const std::string w(who);
+    if (!l2w || !mat) return fail(WF_ERR_INVALID, w + ": null argument");
+    if (mesh >= c->meshes.size()) return fail(WF_ERR_INVALID, w + ": unknown mesh");
+    if (bsdf > WF_BSDF_DIELECTRIC) return fail(WF_ERR_INVALID, w + ": unknown BSDF");
+    Instance& in = *out;
+    in = Instance{};
+    in.mesh = mesh;
+    std::memcpy(in.l2w, l2w, 64);
+    if (!invert4(l2w, in.w2l)) return fail(WF_ERR_INVALID, w + ": transform is not invertible");
+    in.mat = *mat;
+    in.bsdf = bsdf;
+    in.ior = ior;
+    std::memcpy(in.bi.world_to_local, in.w2l, 64);
+    in.bi.bvh_index = mesh;
+    // world AABB of the BLAS root box (renderer.cpp:1324-1336), grown from
+    // +/-FLT_MAX; the reference grows it from a zeroed box, so its box also
+    // always contains the origin.
+    const Mesh& m = c->meshes[mesh];
+    for (int a = 0; a < 3; ++a) { in.bi.aabb_min[a] = FLT_MAX; in.bi.aabb_max[a] = -FLT_MAX; }
+    for (uint32_t i = 0; i < 8; ++i) {
+        float corner[3] = {(i & 1) ? m.root_max[0] : m.root_min[0], (i & 2) ? m.root_max[1] : m.root_min[1],
+                           (i & 4) ? m.root_max[2] : m.root_min[2]};
+        float wc[3];
+        glm_mul_point(l2w, corner, wc);
+        for (int a = 0; a < 3; ++a) {
+            in.bi.aabb_min[a] = (wc[a] < in.bi.aabb_min[a]) ? wc[a] : in.bi.aabb_min[a];
+            in.bi.aabb_max[a] = (in.bi.aabb_max[a] < wc[a]) ? wc[a] : in.bi.aabb_max[a];
+        }
+    }
+    return WF_OK;
+}
+
+void instance_rows(const Instance& in, float4 ti[4], float4 si[6], float aabb[6]) {
+    std::memcpy(aabb, in.bi.aabb_min, 12);
+    std::memcpy(aabb + 3, in.bi.aabb_max, 12);
+    float meshf, bsdff;
+    std::memcpy(&meshf, &in.mesh, 4);
+    std::memcpy(&bsdff, &in.bsdf, 4);
+    const float* w = in.w2l;
+    ti[0] = make_float4(w[0], w[1], w[2], meshf);
+    ti[1] = make_float4(w[4], w[5], w[6], 0.0f);
+    ti[2] = make_float4(w[8], w[9], w[10], 0.0f);
+    ti[3] = make_float4(w[12], w[13], w[14], 0.0f);
+    const float* l = in.l2w;
+    const material_t& mt = in.mat;
+    si[0] = make_float4(l[0], l[1], l[2], meshf);
+    si[1] = make_float4(l[4], l[5], l[6], bsdff);
+    si[2] = make_float4(l[8], l[9], l[10], in.ior);
+    si[3] = make_float4(l[12], l[13], l[14], mt.roughness_factor);
+    si[4] = make_float4(mt.base_color_factor[0], mt.base_color_factor[1], mt.base_color_factor[2], mt.metallic_factor);
+    si[5] = make_float4(mt.emissive_strength * mt.emissive_factor[0], mt.emissive_strength * mt.emissive_factor[1],
+                        mt.emissive_strength * mt.emissive_factor[2], mt.emissive_strength);
+}
+
+void append_emitters(const Instance& in, const MeshView& m, std::vector<LightTri>& out, float& run) {
+    float le[3] = {in.mat.emissive_strength * in.mat.emissive_factor[0],
+                   in.mat.emissive_strength * in.mat.emissive_factor[1],
+                   in.mat.emissive_strength * in.mat.emissive_factor[2]};
+    if (!(le[0] != 0.0f || le[1] != 0.0f || le[2] != 0.0f)) return;
+    for (uint32_t t = 0; t < m.tri_count; ++t) {
+        float p0[3], p1[3], p2[3];
+        hlsl_xform(in.l2w, m.tris[t].v0.position, 1.0f, p0);
+        hlsl_xform(in.l2w, m.tris[t].v1.position, 1.0f, p1);
+        hlsl_xform(in.l2w, m.tris[t].v2.position, 1.0f, p2);
+        float e1[3], e2[3];
+        for (int a = 0; a < 3; ++a) { e1[a] = p1[a] - p0[a]; e2[a] = p2[a] - p0[a]; }
+        float cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        float len = sqrtf(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+        float area = 0.5f * len;
+        float il = 1.0f / len;
+        run = run + area;
+        LightTri L;
+        L.p0 = make_float4(p0[0], p0[1], p0[2], area);
+        L.e1 = make_float4(e1[0], e1[1], e1[2], run);
+        L.e2 = make_float4(e2[0], e2[1], e2[2], 0.0f);
+        L.n = make_float4(cr[0] * il, cr[1] * il, cr[2] * il, 0.0f);
+        L.le = make_float4(le[0], le[1], le[2], 0.0f);
+        out.push_back(L);
+    }
+}
 }  // namespace wf
 
 // ============================================================================ C ABI
@@ -648,35 +746,12 @@ int wf_scene_begin(wf_ctx* c, const view_t* view, const wf_env* env) {
 }
 
 static int submit(wf_ctx* c, uint32_t mesh, const float* l2w, const material_t* mat, uint32_t bsdf, float ior) {
-    if (!c || !l2w || !mat) return fail(WF_ERR_INVALID, "wf_instance_submit: null argument");
+    if (!c) return fail(WF_ERR_INVALID, "wf_instance_submit: null argument");
     if (!c->in_scene) return fail(WF_ERR_STATE, "wf_instance_submit: outside wf_scene_begin/wf_scene_end");
-    if (mesh >= c->meshes.size()) return fail(WF_ERR_INVALID, "wf_instance_submit: unknown mesh");
-    if (bsdf > WF_BSDF_DIELECTRIC) return fail(WF_ERR_INVALID, "wf_instance_submit: unknown BSDF");
     if (c->instances.size() >= 32768) return fail(WF_ERR_CAPACITY, "wf_instance_submit: more than 32768 instances");
     Instance in{};
-    in.mesh = mesh;
-    std::memcpy(in.l2w, l2w, 64);
-    if (!invert4(l2w, in.w2l)) return fail(WF_ERR_INVALID, "wf_instance_submit: transform is not invertible");
-    in.mat = *mat;
-    in.bsdf = bsdf;
-    in.ior = ior;
-    std::memcpy(in.bi.world_to_local, in.w2l, 64);
-    in.bi.bvh_index = mesh;
-    // world AABB of the BLAS root box (renderer.cpp:1324-1336), grown from
-    // +/-FLT_MAX; the reference grows it from a zeroed box, so its box also
-    // always contains the origin.
-    const Mesh& m = c->meshes[mesh];
-    for (int a = 0; a < 3; ++a) { in.bi.aabb_min[a] = FLT_MAX; in.bi.aabb_max[a] = -FLT_MAX; }
-    for (uint32_t i = 0; i < 8; ++i) {
-        float corner[3] = {(i & 1) ? m.root_max[0] : m.root_min[0], (i & 2) ? m.root_max[1] : m.root_min[1],
-                           (i & 4) ? m.root_max[2] : m.root_min[2]};
-        float w[3];
-        glm_mul_point(l2w, corner, w);
-        for (int a = 0; a < 3; ++a) {
-            in.bi.aabb_min[a] = (w[a] < in.bi.aabb_min[a]) ? w[a] : in.bi.aabb_min[a];
-            in.bi.aabb_max[a] = (in.bi.aabb_max[a] < w[a]) ? w[a] : in.bi.aabb_max[a];
-        }
-    }
+    int rc = make_instance(c, mesh, l2w, mat, bsdf, ior, "wf_instance_submit", &in);
+    if (rc) return rc;
     c->instances.push_back(in);
     return WF_OK;
 }
@@ -719,27 +794,7 @@ int wf_scene_end(wf_ctx* c) {
     for (uint32_t i = 0; i < n; ++i) {
         const Instance& in = c->instances[i];
         c->scene_bi[i] = in.bi;
-        std::memcpy(&aabbs[6ull * i], in.bi.aabb_min, 12);
-        std::memcpy(&aabbs[6ull * i + 3], in.bi.aabb_max, 12);
-        float meshf, bsdff;
-        std::memcpy(&meshf, &in.mesh, 4);
-        std::memcpy(&bsdff, &in.bsdf, 4);
-        const float* w = in.w2l;
-        ti[4ull * i] = make_float4(w[0], w[1], w[2], meshf);
-        ti[4ull * i + 1] = make_float4(w[4], w[5], w[6], 0.0f);
-        ti[4ull * i + 2] = make_float4(w[8], w[9], w[10], 0.0f);
-        ti[4ull * i + 3] = make_float4(w[12], w[13], w[14], 0.0f);
-        const float* l = in.l2w;
-        const material_t& mt = in.mat;
-        si[6ull * i] = make_float4(l[0], l[1], l[2], meshf);
-        si[6ull * i + 1] = make_float4(l[4], l[5], l[6], bsdff);
-        si[6ull * i + 2] = make_float4(l[8], l[9], l[10], in.ior);
-        si[6ull * i + 3] = make_float4(l[12], l[13], l[14], mt.roughness_factor);
-        si[6ull * i + 4] = make_float4(mt.base_color_factor[0], mt.base_color_factor[1], mt.base_color_factor[2],
-                                       mt.metallic_factor);
-        si[6ull * i + 5] = make_float4(mt.emissive_strength * mt.emissive_factor[0],
-                                       mt.emissive_strength * mt.emissive_factor[1],
-                                       mt.emissive_strength * mt.emissive_factor[2], mt.emissive_strength);
+        instance_rows(in, &ti[4ull * i], &si[6ull * i], &aabbs[6ull * i]);
     }
     if ((rc = c->tnodes.reserve(2ull * std::max<uint32_t>(2 * n, 1))) || (rc = c->tinst.reserve(ti.size())) ||
         (rc = c->sinst.reserve(si.size())) || (rc = c->aabbs.reserve(aabbs.size())) ||
@@ -758,32 +813,9 @@ int wf_scene_end(wf_ctx* c) {
     std::vector<LightTri> lt;
     float run = 0.0f;
     for (uint32_t i = 0; i < n; ++i) {
-        const Instance& in = c->instances[i];
-        float le[3] = {in.mat.emissive_strength * in.mat.emissive_factor[0],
-                       in.mat.emissive_strength * in.mat.emissive_factor[1],
-                       in.mat.emissive_strength * in.mat.emissive_factor[2]};
-        if (!(le[0] != 0.0f || le[1] != 0.0f || le[2] != 0.0f)) continue;
-        const Mesh& m = c->meshes[in.mesh];
-        for (uint32_t t = 0; t < m.tri_count; ++t) {
-            float p0[3], p1[3], p2[3];
-            hlsl_xform(in.l2w, m.tris[t].v0.position, 1.0f, p0);
-            hlsl_xform(in.l2w, m.tris[t].v1.position, 1.0f, p1);
-            hlsl_xform(in.l2w, m.tris[t].v2.position, 1.0f, p2);
-            float e1[3], e2[3];
-            for (int a = 0; a < 3; ++a) { e1[a] = p1[a] - p0[a]; e2[a] = p2[a] - p0[a]; }
-            float cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-            float len = sqrtf(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
-            float area = 0.5f * len;
-            float il = 1.0f / len;
-            run = run + area;
-            LightTri L;
-            L.p0 = make_float4(p0[0], p0[1], p0[2], area);
-            L.e1 = make_float4(e1[0], e1[1], e1[2], run);
-            L.e2 = make_float4(e2[0], e2[1], e2[2], 0.0f);
-            L.n = make_float4(cr[0] * il, cr[1] * il, cr[2] * il, 0.0f);
-            L.le = make_float4(le[0], le[1], le[2], 0.0f);
-            lt.push_back(L);
-        }
+        MeshView mv;
+        ctx_mesh(c, c->instances[i].mesh, &mv);
+        append_emitters(c->instances[i], mv, lt, run);
     }
     c->light_count = (uint32_t)lt.size();
     c->light_total = run;

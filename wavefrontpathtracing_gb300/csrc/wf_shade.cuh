@@ -1,0 +1,361 @@
+// wf_shade.cuh — per-path shading arithmetic shared by the single-scene
+// wavefront (wf_shade.cu) and the batched multi-scene pipeline (wf_batch.cu),
+// so both perform the same operations in the same order as the CPU oracle
+// (oracle/orc_impl.h); every translation unit is compiled without fused
+// multiply-add.
+#pragma once
+#include "wf_kernels.h"
+
+namespace wf {
+
+// Slot allocation for a warp: one atomicAdd per warp on the queue tail (the
+// reference issues one InterlockedAdd per surviving ray, shade.hlsl:164).
+__device__ __forceinline__ uint32_t warp_append(uint32_t* tail, bool want) {
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    if (mask == 0u) return 0u;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(tail, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+// make_primary_ray (common.hlsl:182-195).
+template <class Cam>
+__device__ __forceinline__ void primary_ray(const Cam& W, uint32_t px, uint32_t py, V3& o, V3& d) {
+    float uvx = ((float)px + 0.5f) / W.dim_x;
+    float uvy = ((float)py + 0.5f) / W.dim_y;
+    uvy = 1.0f - uvy;
+    float cx = 2.0f * uvx - 1.0f, cy = 2.0f * uvy - 1.0f;
+    V3 pv = xform(mk(cx, cy, 1.0f), 1.0f, W.clip_to_view[0], W.clip_to_view[1], W.clip_to_view[2],
+                  W.clip_to_view[3]);
+    V3 dv = normalize(pv);
+    d = xform(dv, 0.0f, W.view_to_world[0], W.view_to_world[1], W.view_to_world[2], W.view_to_world[3]);
+    o = xform(mk(0.0f, 0.0f, 0.0f), 1.0f, W.view_to_world[0], W.view_to_world[1], W.view_to_world[2],
+              W.view_to_world[3]);
+}
+
+// create_orthonormal_basis (sample.hlsl:13-27).
+__device__ __forceinline__ void basis(V3 n, V3& tg, V3& bt) {
+    if (fabsf(n.x) > fabsf(n.z)) tg = normalize(mk(-n.y, n.x, 0.0f));
+    else tg = normalize(mk(0.0f, -n.z, n.y));
+    bt = cross(n, tg);
+}
+__device__ __forceinline__ V3 to_world(V3 v, V3 tg, V3 n, V3 bt) {
+    return mk(v.x * tg.x + v.y * n.x + v.z * bt.x, v.x * tg.y + v.y * n.y + v.z * bt.y,
+              v.x * tg.z + v.y * n.z + v.z * bt.z);
+}
+__device__ __forceinline__ V3 schlick(V3 f0, float c) {
+    float m = 1.0f - c;
+    float m2 = m * m;
+    float m5 = (m2 * m2) * m;
+    return mk(f0.x + (1.0f - f0.x) * m5, f0.y + (1.0f - f0.y) * m5, f0.z + (1.0f - f0.z) * m5);
+}
+__device__ __forceinline__ float g1(float x, float a2) { return (2.0f * x) / (x + sqrtf(a2 + (1.0f - a2) * (x * x))); }
+__device__ __forceinline__ float ggx_d(float noh, float a2) {
+    float q = (noh * noh) * (a2 - 1.0f) + 1.0f;
+    return a2 / (kPi * (q * q));
+}
+__device__ __forceinline__ float offset_eps(V3 p) {
+    return 1e-5f * (1.0f + fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
+}
+
+constexpr float kMetalDeltaAlpha = 1e-4f;
+constexpr float kShadowTmaxScale = 0.999f;
+
+__device__ __forceinline__ uint32_t pick_light(const LightTri* L, uint32_t count, float total, float r) {
+    float x = r * total;
+    uint32_t lo = 0, hi = count - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (x < L[mid].e1.w) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+// Everything one shading event needs (one queue entry).
+struct ShadeIn {
+    V3 rd;             // ray direction
+    float4 tuvp;       // hit {t, bary u, bary v, primitive}
+    uint32_t inst;     // instance index into ShadeRefs.sinst, kInvalid for a miss
+    V3 T;              // throughput
+    float last_pdf;    // pdf of the BSDF sample that produced the ray
+    uint32_t flags;    // path flags
+    uint32_t pixel, sample, depth;   // keys of the path's random numbers
+};
+
+// Per-wave (or per-scene) constants of shading.
+struct ShadeCtl {
+    uint32_t frame_seed, max_bounces, nee, rr_start, cosine;
+    float env_strength, env0, env1, env2;
+    const LightTri* lights;
+    uint32_t light_count;
+    float light_total;
+};
+
+struct ShadeOut {
+    V3 add;            // radiance this event adds to the path
+    bool has_add;
+    bool enqueue;      // continue the path with (org, dir), throughput T, pdf, flags
+    V3 org, dir, T;
+    float pdf;
+    uint32_t flags;
+    bool shadow;       // a next-event shadow ray (spos, sdir, stmax) carrying contrib
+    V3 spos, sdir, contrib;
+    float stmax;
+    uint32_t em_key;   // adjoint: emitter reached (kInvalid if none) and its gradient
+    float em_val;
+};
+
+// One shading event: shade.hlsl:42-174 (miss -> environment, emission ->
+// terminate, Lambert bounce) plus GGX metal, smooth dielectric, next-event
+// estimation with power-heuristic MIS, and Russian roulette.  The same
+// operations, in the same order, as the oracle (oracle/orc_impl.h path()).
+// adj_path / adj_pixel index the adjoint buffers when A is active.
+__device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K, const ShadeIn& in,
+                                          const AdjointRefs& A, uint32_t adj_path, uint32_t adj_pixel,
+                                          ShadeOut& o) {
+    o.has_add = false; o.enqueue = false; o.shadow = false; o.em_key = kInvalid; o.em_val = 0.0f;
+    V3 T = in.T;
+    const V3 rd = in.rd;
+    uint32_t flags = in.flags;
+    if (in.inst == kInvalid) {
+        // miss: energy += throughput * strength * env (shade.hlsl:60-65)
+        o.add = mk((T.x * K.env_strength) * K.env0, (T.y * K.env_strength) * K.env1, (T.z * K.env_strength) * K.env2);
+        o.has_add = true;
+        return;
+    }
+    const uint32_t inst = in.inst;
+    const float4* ip = SH.sinst + 6ull * inst;
+    const float4 c0 = ip[0], c1 = ip[1], c2 = ip[2], c3 = ip[3], mb = ip[4], me = ip[5];
+    const uint32_t mesh = __float_as_uint(c0.w);
+    const uint32_t prim = __float_as_uint(in.tuvp.w);
+    const float4* tp = SH.stri[mesh] + 6ull * prim;
+    const V3 p0 = xyz(tp[0]), p1 = xyz(tp[1]), p2 = xyz(tp[2]);
+    const V3 n0 = xyz(tp[3]), n1 = xyz(tp[4]), n2 = xyz(tp[5]);
+    const float hu = in.tuvp.y, hv = in.tuvp.z;
+    // get_hit_surface (common.hlsl:228-245)
+    const V3 pl = add(add(p0, scl(sub(p1, p0), hu)), scl(sub(p2, p0), hv));
+    const V3 pos = xform(pl, 1.0f, c0, c1, c2, c3);
+    const V3 nl = add(add(n0, scl(sub(n1, n0), hu)), scl(sub(n2, n0), hv));
+    V3 N = normalize(xform(nl, 0.0f, c0, c1, c2, c3));
+    V3 base_c = mk(mb.x * 1.0f, mb.y * 1.0f, mb.z * 1.0f);
+    uint32_t stri = 0;
+    if (SH.tri_albedo) {
+        stri = SH.inst_tri_offset[inst] + prim;
+        base_c = xyz(SH.tri_albedo[stri]);
+    }
+    const V3 le = mk(me.x * 1.0f, me.y * 1.0f, me.z * 1.0f);
+    if (le.x != 0.0f || le.y != 0.0f || le.z != 0.0f) {
+        float w = 1.0f;
+        if (K.nee && !(flags & kFlagSpecular) && K.light_count > 0) {
+            V3 ng = normalize(xform(cross(sub(p1, p0), sub(p2, p0)), 0.0f, c0, c1, c2, c3));
+            float cos_l = -dot(ng, rd);
+            if (cos_l > 0.0f) {
+                float d2 = (in.tuvp.x * in.tuvp.x) * dot(rd, rd);
+                float pdf_l = d2 / (cos_l * K.light_total);
+                // power heuristic in ratio form: 1 / (1 + (pdf_l / pdf_bsdf)^2)
+                float q = pdf_l / in.last_pdf;
+                w = (q == q) ? 1.0f / (1.0f + q * q) : 0.0f;
+            }
+        }
+        o.add = mk((T.x * le.x) * w, (T.y * le.y) * w, (T.z * le.z) * w);
+        o.has_add = true;
+        if (A.g_emission && me.w != 0.0f) {
+            const float4 L = A.L_final[adj_path], g = A.dimage[adj_pixel];
+            const float gl = (g.x * A.inv_spp) * L.x + (g.y * A.inv_spp) * L.y + (g.z * A.inv_spp) * L.z;
+            o.em_key = inst;
+            o.em_val = gl / me.w;
+        }
+        return;
+    }
+    const uint32_t depth = in.depth;
+    uint32_t seed = path_seed(K.frame_seed, in.pixel, in.sample, depth);
+    (void)rand_float(seed);  // r_path (shade.hlsl:81), drawn and unused
+    const float r1 = rand_float(seed);
+    const float r2 = rand_float(seed);
+    const V3 V = neg(rd);
+    V3 L = mk(0, 0, 0), wgt = mk(0, 0, 0);
+    float pdf = 0.0f;
+    bool delta = false, valid = true, toggle_inside = false;
+    V3 org = pos;
+    const float alpha = c3.w * c3.w;
+    uint32_t bsdf = __float_as_uint(c1.w);
+    if (bsdf == 1u && alpha < kMetalDeltaAlpha) bsdf = 3u;
+    if ((flags & kFlagInside) && bsdf != 2u && dot(N, V) < 0.0f) N = neg(N);
+    V3 tg, bt;
+    basis(N, tg, bt);
+    if (bsdf == 0u && A.g_albedo && SH.tri_albedo) {
+        const float4 Lf = A.L_final[adj_path], g = A.dimage[adj_pixel];
+        const uint32_t rep = (blockIdx.x ^ (threadIdx.x >> 5)) & (A.replicas - 1u);
+        float* ga = reinterpret_cast<float*>(A.g_albedo + (size_t)rep * A.triangles + stri);
+        if (base_c.x != 0.0f) atomicAdd(ga, ((g.x * A.inv_spp) * Lf.x) / base_c.x);
+        if (base_c.y != 0.0f) atomicAdd(ga + 1, ((g.y * A.inv_spp) * Lf.y) / base_c.y);
+        if (base_c.z != 0.0f) atomicAdd(ga + 2, ((g.z * A.inv_spp) * Lf.z) / base_c.z);
+    }
+    if (bsdf == 0u) {
+        V3 loc;
+        float sn, cs;
+        if (K.cosine) {
+            float st = sqrtf(r1);
+            sincos_2pi(r2, sn, cs);
+            loc = mk(st * cs, sqrtf(1.0f - r1), st * sn);
+        } else {
+            float st = sqrtf(1.0f - r1 * r1);
+            sincos_2pi(r2, sn, cs);
+            loc = mk(st * cs, r1, st * sn);
+        }
+        L = to_world(normalize(loc), tg, N, bt);
+        const float nol = fmaxf(0.0f, dot(N, L));
+        pdf = K.cosine ? nol * kInvPi : kInvTwoPi;
+        const float ipdf = 1.0f / pdf;
+        wgt = mk((nol * (base_c.x * kInvPi)) * ipdf, (nol * (base_c.y * kInvPi)) * ipdf,
+                 (nol * (base_c.z * kInvPi)) * ipdf);
+    } else if (bsdf == 1u) {
+        const float a2 = alpha * alpha;
+        const float cth = sqrtf((1.0f - r1) / (1.0f + (a2 - 1.0f) * r1));
+        const float sth = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
+        float sn, cs;
+        sincos_2pi(r2, sn, cs);
+        const V3 H = to_world(mk(sth * cs, cth, sth * sn), tg, N, bt);
+        const float voh = dot(V, H);
+        L = sub(scl(H, 2.0f * voh), V);
+        const float nol = dot(N, L), nov = dot(N, V), noh = dot(N, H);
+        if (nol <= 0.0f || nov <= 0.0f || voh <= 0.0f || noh <= 0.0f) {
+            valid = false;
+        } else {
+            const V3 F = schlick(base_c, voh);
+            const float G = g1(nol, a2) * g1(nov, a2);
+            const float gw = (G * voh) / (nov * noh);
+            wgt = scl(F, gw);
+            pdf = (ggx_d(noh, a2) * noh) / (4.0f * voh);
+        }
+    } else if (bsdf == 3u) {
+        const float nov = dot(N, V);
+        delta = true;
+        if (nov <= 0.0f) {
+            valid = false;
+        } else {
+            L = sub(scl(N, 2.0f * nov), V);
+            wgt = schlick(base_c, nov);
+        }
+    } else {
+        float ci = dot(V, N);
+        const bool entering = ci > 0.0f;
+        const float ior = c2.w;
+        const float n1 = entering ? 1.0f : ior, n2 = entering ? ior : 1.0f;
+        const V3 nn = entering ? N : neg(N);
+        ci = fabsf(ci);
+        const float eta = n1 / n2;
+        const float s2t = (eta * eta) * (1.0f - ci * ci);
+        float F = 1.0f, ct = 0.0f;
+        if (s2t < 1.0f) {
+            ct = sqrtf(1.0f - s2t);
+            const float rs = (n1 * ci - n2 * ct) / (n1 * ci + n2 * ct);
+            const float rp = (n1 * ct - n2 * ci) / (n1 * ct + n2 * ci);
+            F = 0.5f * (rs * rs + rp * rp);
+        }
+        if (r1 < F) {
+            L = add(rd, scl(nn, 2.0f * ci));
+        } else {
+            L = normalize(add(scl(rd, eta), scl(nn, eta * ci - ct)));
+            toggle_inside = true;
+        }
+        wgt = mk(1.0f, 1.0f, 1.0f);
+        delta = true;
+        org = add(pos, scl(L, offset_eps(pos)));
+    }
+
+    // next-event estimation: the shadow ray for the connect stage
+    if (K.nee && !delta && depth < K.max_bounces && K.light_count > 0) {
+        const float rl0 = rand_float(seed);
+        const float rl1 = rand_float(seed);
+        const float rl2 = rand_float(seed);
+        const LightTri lt = K.lights[pick_light(K.lights, K.light_count, K.light_total, rl0)];
+        const float su = sqrtf(rl1);
+        const float b1 = su * (1.0f - rl2), b2 = su * rl2;
+        const V3 y = add(add(xyz(lt.p0), scl(xyz(lt.e1), b1)), scl(xyz(lt.e2), b2));
+        const V3 wv = sub(y, pos);
+        const float dd2 = dot(wv, wv);
+        const float dist = sqrtf(dd2);
+        const V3 wl = scl(wv, 1.0f / dist);
+        const float cos_l = -dot(xyz(lt.n), wl);
+        const float cos_x = dot(N, wl);
+        if (cos_l > 0.0f && cos_x > 0.0f) {
+            const float pdf_l = dd2 / (cos_l * K.light_total);
+            V3 f = mk(0, 0, 0);
+            float pdf_b = 0.0f;
+            bool ok = true;
+            if (bsdf == 0u) {
+                f = scl(base_c, kInvPi);
+                pdf_b = K.cosine ? cos_x * kInvPi : kInvTwoPi;
+            } else {
+                const V3 H = normalize(add(V, wl));
+                const float nov = dot(N, V), noh = dot(N, H), voh = dot(V, H);
+                if (nov <= 0.0f || voh <= 0.0f) {
+                    ok = false;
+                } else {
+                    const float a2 = alpha * alpha;
+                    const float D = ggx_d(noh, a2);
+                    const float G = g1(cos_x, a2) * g1(nov, a2);
+                    const V3 F = schlick(base_c, voh);
+                    f = scl(F, (D * G) / ((4.0f * cos_x) * nov));
+                    pdf_b = (D * noh) / (4.0f * voh);
+                    if (!(D <= FLT_MAX)) ok = false;
+                }
+            }
+            if (ok) {
+                const float q = pdf_b / pdf_l;
+                const float w = (q == q) ? 1.0f / (1.0f + q * q) : 0.0f;
+                const float sc = (cos_x * w) / pdf_l;
+                const V3 ltle = xyz(lt.le);
+                o.contrib = mk(((T.x * f.x) * sc) * ltle.x, ((T.y * f.y) * sc) * ltle.y, ((T.z * f.z) * sc) * ltle.z);
+                o.spos = pos;
+                o.sdir = wl;
+                o.stmax = dist * kShadowTmaxScale;
+                o.shadow = true;
+            }
+        }
+    }
+    if (valid) {
+        T = mul(T, wgt);
+        if (depth < K.max_bounces) {
+            bool survive = true;
+            if (depth >= K.rr_start) {
+                const float rr = rand_float(seed);
+                const float q = fminf(fmaxf(fmaxf(T.x, T.y), T.z), 1.0f);
+                if (rr >= q) survive = false;
+                else T = mk(T.x / q, T.y / q, T.z / q);
+            }
+            if (survive) {
+                if (toggle_inside) flags ^= kFlagInside;
+                flags = delta ? (flags | kFlagSpecular) : (flags & ~kFlagSpecular);
+                o.flags = flags;
+                o.pdf = pdf;
+                o.org = org;
+                o.dir = L;
+                o.T = T;
+                o.enqueue = true;
+            }
+        }
+    }
+}
+
+// Warp-aggregated atomic add of v to g[key] (one atomic per distinct key in the warp).
+__device__ __forceinline__ void warp_add_by_key(float* g, uint32_t key, float v) {
+    bool pending = key != kInvalid;
+    for (;;) {
+        const unsigned rem = __ballot_sync(0xffffffffu, pending);
+        if (!rem) break;
+        const int leader = __ffs(rem) - 1;
+        const uint32_t k = __shfl_sync(0xffffffffu, key, leader);
+        const bool mine = pending && key == k;
+        float s = mine ? v : 0.0f;
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if ((int)(threadIdx.x & 31) == leader) atomicAdd(&g[k], s);
+        if (mine) pending = false;
+    }
+}
+
+}  // namespace wf

@@ -8,8 +8,6 @@ namespace wf {
 
 namespace {
 
-constexpr int kBlock = 128;
-
 int g_sms = 0;
 
 // Extension rays: queue[depth & 1] -> hits.  Ray flags in origin.w select culling.
@@ -23,6 +21,7 @@ struct ExtendIO {
         o = xyz(a); d = xyz(b); tmax = b.w;
         nc = (__float_as_uint(a.w) & kFlagInside) != 0u;
     }
+    __device__ __forceinline__ uint32_t root(uint32_t, const SceneRefs& S) const { return S.inst_count ? 0u : kInvalid; }
     __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool) const {
         tuvp[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
         inst[i] = h.inst;
@@ -41,6 +40,7 @@ struct ConnectIO {
         const float4 a = so[i], b = sd[i];
         o = xyz(a); d = xyz(b); tmax = a.w; nc = false;
     }
+    __device__ __forceinline__ uint32_t root(uint32_t, const SceneRefs& S) const { return S.inst_count ? 0u : kInvalid; }
     __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool ok) const {
         if (!ok || h.inst != kInvalid) return;
         const float4 k = sc[i];
@@ -54,34 +54,10 @@ struct ConnectIO {
 };
 
 template <bool ANY, bool COUNT, class IO>
-__global__ void __launch_bounds__(kBlock) k_trace(SceneRefs S, IO io, const uint32_t* count_ptr, uint32_t count,
-                                                  uint32_t* fetch, uint32_t* status, Counters* counters,
-                                                  unsigned long long* total) {
-    const uint32_t n = count_ptr ? *count_ptr : count;
-    if (total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(total, (unsigned long long)n);
-    LocalCounters c = {0, 0, 0, 0};
-    bool overflow = false;
-    trace_persistent<ANY, COUNT>(S, io, n, fetch, c, overflow);
-    if (overflow) atomicOr(status, ERRF_STACK);
-    if (COUNT) flush_counters(c, counters);
-}
-
-// Resident blocks per SM for a kernel, queried once per instantiation.
-template <class K>
-unsigned persistent_grid(K kernel) {
-    static int per_sm = 0;
-    if (per_sm == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
-        if (per_sm <= 0) per_sm = 1;
-    }
-    return (unsigned)(sm_count() * per_sm);
-}
-
-template <bool ANY, bool COUNT, class IO>
 cudaError_t launch(const SceneRefs& S, const IO& io, const uint32_t* count_ptr, uint32_t count, uint32_t* fetch,
                    uint32_t* status, Counters* counters, unsigned long long* total, cudaStream_t stream) {
     auto k = k_trace<ANY, COUNT, IO>;
-    k<<<persistent_grid(k), kBlock, 0, stream>>>(S, io, count_ptr, count, fetch, status, counters, total);
+    k<<<persistent_grid(k), kTraceBlock, 0, stream>>>(S, io, count_ptr, count, fetch, status, counters, total);
     return cudaGetLastError();
 }
 

@@ -36,8 +36,9 @@ struct LocalCounters {
 constexpr uint32_t kNoRay = 0xFFFFFFFFu;
 constexpr int kRefill = 12;
 
-// Ray sources / sinks.  load(i, o, d, tmax, no_cull); store(i, hit, ok) where
-// ok is false when a traversal stack overflowed.
+// Ray sources / sinks.  load(i, o, d, tmax, no_cull); root(i, S) = the TLAS
+// root node of the ray's scene, kInvalid for an empty scene; store(i, hit, ok)
+// where ok is false when a traversal stack overflowed.
 struct AosIO {
     const float4* rays;   // RayDesc2
     uint32_t* hits;       // hit_result_t
@@ -46,6 +47,7 @@ struct AosIO {
         const float4 a = ldg4(rays + 2ull * i), b = ldg4(rays + 2ull * i + 1);
         o = xyz(a); d = xyz(b); tmax = b.w; nc = no_cull;
     }
+    __device__ __forceinline__ uint32_t root(uint32_t, const SceneRefs& S) const { return S.inst_count ? 0u : kInvalid; }
     __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool) const {
         uint32_t* o = hits + 5ull * i;
         o[0] = h.inst; o[1] = h.prim; o[2] = __float_as_uint(h.t); o[3] = __float_as_uint(h.u);
@@ -92,9 +94,10 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                         io.load(k, wo, wd, wt, no_cull);
                         h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
                         co = wo; cd = wd; ci = rcp(wd); ct = wt;
-                        bool miss = S.inst_count == 0;
+                        const uint32_t root = io.root(k, S);
+                        bool miss = root == kInvalid;
                         if (!miss) {
-                            const float4 n0 = ldg4(S.tnodes), n1 = ldg4(S.tnodes + 1);
+                            const float4 n0 = ldg4(S.tnodes + 2ull * root), n1 = ldg4(S.tnodes + 2ull * root + 1);
                             if (COUNT) cnt.tlas_nodes++;
                             miss = slab(xyz(n0), xyz(n1), co, ci, ct) == FLT_MAX;
                             level = 0; w0 = __float_as_uint(n0.w); w1 = __float_as_uint(n1.w); tsp = 0;
@@ -228,6 +231,36 @@ __device__ __forceinline__ void flush_counters(const LocalCounters& c, Counters*
         atomicAdd(&g->blas_node_loads, x);
         atomicAdd(&g->triangle_tests, y);
     }
+}
+
+constexpr int kTraceBlock = 128;
+int sm_count();
+
+// The traversal kernel: a persistent grid over count rays (read from
+// count_ptr on the device when it is non-null), rays handed out from *fetch.
+// total (optional) accumulates the number of rays of each launch.
+template <bool ANY, bool COUNT, class IO>
+__global__ void __launch_bounds__(kTraceBlock) k_trace(SceneRefs S, IO io, const uint32_t* count_ptr, uint32_t count,
+                                                  uint32_t* fetch, uint32_t* status, Counters* counters,
+                                                  unsigned long long* total) {
+    const uint32_t n = count_ptr ? *count_ptr : count;
+    if (total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(total, (unsigned long long)n);
+    LocalCounters c = {0, 0, 0, 0};
+    bool overflow = false;
+    trace_persistent<ANY, COUNT>(S, io, n, fetch, c, overflow);
+    if (overflow) atomicOr(status, ERRF_STACK);
+    if (COUNT) flush_counters(c, counters);
+}
+
+// Resident blocks per SM for a kernel, queried once per instantiation.
+template <class K>
+inline unsigned persistent_grid(K kernel) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceBlock, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
+    return (unsigned)(sm_count() * per_sm);
 }
 
 }  // namespace wf

@@ -77,32 +77,44 @@ def icosahedron():
     return v, f
 
 
-def unit_icosphere(freq):
-    """Geodesic sphere: every icosahedron face split into freq^2 triangles,
-    vertices projected to the unit sphere (20*freq^2 triangles; freq = 2^k is
-    subdivision level k).  Returns float64 (p0, p1, p2) arrays, wound so that
-    (p1-p0)x(p2-p0) points outward (front faces under back-face culling)."""
+def unit_icosphere_indexed(freq):
+    """Geodesic sphere as (vertices, triangles): every icosahedron face carries
+    a grid of (freq+1)(freq+2)/2 points A + (B-A) i/freq + (C-A) j/freq
+    projected to the unit sphere (points on shared edges repeat per face), and
+    freq^2 triangles over it (20*freq^2 in all; freq = 2^k is subdivision level
+    k), wound so that (p1-p0)x(p2-p0) points outward (front faces under
+    back-face culling)."""
     v, faces = icosahedron()
-    P0, P1, P2 = [], [], []
+    grid = [(i, j) for i in range(freq + 1) for j in range(freq + 1 - i)]
+    gidx = {ij: k for k, ij in enumerate(grid)}
+    st = np.array(grid, dtype=np.float64) / freq
     ii, jj = [], []
     for i in range(freq):
         for j in range(freq - i):
-            ii.append((i, j, i + 1, j, i, j + 1))
+            ii.append((gidx[(i, j)], gidx[(i + 1, j)], gidx[(i, j + 1)]))
             if i + j < freq - 1:
-                jj.append((i + 1, j, i + 1, j + 1, i, j + 1))
-    idx = np.array(ii + jj, dtype=np.float64) / freq
-    for a, b, c in faces:
+                jj.append((gidx[(i + 1, j)], gidx[(i + 1, j + 1)], gidx[(i, j + 1)]))
+    local = np.array(ii + jj, dtype=np.int64)
+    ng = len(grid)
+    V, F = [], []
+    for f, (a, b, c) in enumerate(faces):
         A, B, C = v[a], v[b], v[c]
-        for k in range(3):
-            s, t = idx[:, 2 * k:2 * k + 1], idx[:, 2 * k + 1:2 * k + 2]
-            pts = A + (B - A) * s + (C - A) * t
-            (P0, P1, P2)[k].append(pts)
-    p0, p1, p2 = (np.concatenate(x) for x in (P0, P1, P2))
-    p0, p1, p2 = (x / np.linalg.norm(x, axis=1, keepdims=True) for x in (p0, p1, p2))
+        V.append(A + (B - A) * st[:, 0:1] + (C - A) * st[:, 1:2])
+        F.append(local + f * ng)
+    V = np.concatenate(V)
+    F = np.concatenate(F)
+    V = V / np.linalg.norm(V, axis=1, keepdims=True)
+    p0, p1, p2 = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
     fn = np.cross(p1 - p0, p2 - p0)
     flip = np.einsum("ij,ij->i", fn, p0 + p1 + p2) < 0
-    p1[flip], p2[flip] = p2[flip].copy(), p1[flip].copy()
-    return p0, p1, p2
+    F[flip, 1], F[flip, 2] = F[flip, 2].copy(), F[flip, 1].copy()
+    return V, F
+
+
+def unit_icosphere(freq):
+    """unit_icosphere_indexed as float64 (p0, p1, p2) triangle corner arrays."""
+    V, F = unit_icosphere_indexed(freq)
+    return V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
 
 
 def icosphere(freq, center=(0.0, 0.0, 0.0), radius=1.0):
@@ -137,12 +149,9 @@ def _value_noise(p, seed, cells=4.0):
 
 def displaced_icosphere(freq, seed, amplitude=0.1):
     """Unit icosphere whose radius is 1 + amplitude * value_noise(direction)."""
-    p0, p1, p2 = unit_icosphere(freq)
-    out = []
-    for p in (p0, p1, p2):
-        r = 1.0 + amplitude * _value_noise(p, seed)
-        out.append(p * r[:, None])
-    return _tris_from_arrays(out[0], out[1], out[2], p0, p1, p2)
+    V, F = unit_icosphere_indexed(freq)
+    P = V * (1.0 + amplitude * _value_noise(V, seed))[:, None]
+    return _tris_from_arrays(P[F[:, 0]], P[F[:, 1]], P[F[:, 2]], V[F[:, 0]], V[F[:, 1]], V[F[:, 2]])
 
 
 def quad(origin, e1, e2):
@@ -319,6 +328,61 @@ def instanced_scene(width=1920, height=1080, instances=1024, freqs=INSTANCED_FRE
                     env_strength=1.0, cosine=1)
     return SceneDesc("instanced", meshes, inst, view, width, height, settings,
                      dict(interval_count=16, subdivide_single_prim=0, max_leaf_prims=4))
+
+
+class BatchSceneDesc:
+    """One scene of a batch: instances = list of (mesh index into the batch's
+    mesh list, local_to_world 4x4, material_ext)."""
+
+    def __init__(self, width, height, spp, view, instances, env, sphere_triangles):
+        self.width, self.height, self.spp, self.view = width, height, spp, view
+        self.instances, self.env, self.sphere_triangles = instances, env, sphere_triangles
+
+    @property
+    def paths(self):
+        return self.width * self.height * self.spp
+
+
+def batch_scenes(count=64, seed=5, tri_range=(1_000, 2_000_000), resolutions=(64, 128, 256, 512, 1024),
+                 spps=(1, 4, 16)):
+    """The batched configuration: `count` scenes, each a seeded displaced
+    icosphere soup whose triangle count is log-uniform in tri_range (geodesic
+    frequency round(sqrt(n / 20)), so 20 * freq^2 triangles), a square image
+    with its side drawn from `resolutions`, spp drawn from `spps`, and a
+    material from the 60/25/15 Lambert / metal / dielectric mix.  Every scene
+    also holds a ground quad and an emissive quad light (two meshes shared by
+    all scenes).  Returns (meshes, scenes): meshes[0] ground, meshes[1] light,
+    meshes[2 + k] scene k's soup."""
+    rng = PCG32(seed)
+    ground = quad((-6.0, -1.25, 6.0), (12.0, 0.0, 0.0), (0.0, 0.0, -12.0))   # faces +y
+    light = quad((-0.75, 3.0, -0.75), (1.5, 0.0, 0.0), (0.0, 0.0, 1.5))     # faces -y
+    meshes = [ground, light]
+    scenes = []
+    lo, hi = math.log(tri_range[0]), math.log(tri_range[1])
+    for k in range(count):
+        n = math.exp(rng.uniform(lo, hi))
+        freq = max(1, int(round(math.sqrt(n / 20.0))))
+        meshes.append(displaced_icosphere(freq, seed=1000 + k, amplitude=0.1))
+        side = resolutions[rng.next_u32() % len(resolutions)]
+        spp = spps[rng.next_u32() % len(spps)]
+        u = rng.uniform()
+        base = (rng.uniform(0.2, 0.9), rng.uniform(0.2, 0.9), rng.uniform(0.2, 0.9))
+        rough = rng.uniform(0.0, 0.5)
+        if u < 0.60:
+            m = material(base=base)
+        elif u < 0.85:
+            m = material(base=base, bsdf=BSDF_METAL, roughness=rough, metallic=1.0)
+        else:
+            m = material(base=(1.0, 1.0, 1.0), bsdf=BSDF_DIELECTRIC, ior=1.5)
+        az = rng.uniform(0.0, 2.0 * math.pi)
+        el = rng.uniform(0.15, 0.6)
+        eye = (3.6 * math.cos(el) * math.sin(az), 3.6 * math.sin(el), -3.6 * math.cos(el) * math.cos(az))
+        view = make_view(eye, (0.0, 0.0, 0.0), 45.0, side, side)
+        inst = [(2 + k, np.eye(4), m),
+                (0, np.eye(4), material(base=(0.6, 0.6, 0.6))),
+                (1, np.eye(4), material(base=(0.8, 0.8, 0.8), emissive=(1.0, 0.95, 0.9), strength=25.0))]
+        scenes.append(BatchSceneDesc(side, side, spp, view, inst, (0.05, 0.06, 0.08), len(meshes[-1])))
+    return meshes, scenes
 
 
 def triangle_soup(n, seed=7, mu=-5.0, sigma=0.5):
