@@ -28,7 +28,9 @@ def nvcc():
 
 
 def _flags():
-    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
+    # WF_NVCC_DEFINES: extra -D tuning macros (for example -DWF_TRACE_MIN_BLOCKS=10); rebuild with force=True
+    extra = os.environ.get("WF_NVCC_DEFINES", "").split()
+    return ARCH + extra + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
                    "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-Xptxas", "-warn-spills",
                    "-I", os.path.join(HERE, "..", "include")]
 

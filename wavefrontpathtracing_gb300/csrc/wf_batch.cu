@@ -194,7 +194,7 @@ struct BatchConnectIO {
 };
 
 template <bool ANY, class IO>
-__global__ void __launch_bounds__(kTraceBlock) k_btrace(SceneRefs S, IO io, const uint32_t* count, uint32_t* fetch,
+__global__ void __launch_bounds__(kTraceBlock, WF_TRACE_MIN_BLOCKS) k_btrace(SceneRefs S, IO io, const uint32_t* count, uint32_t* fetch,
                                                         uint32_t* status) {
     const uint32_t n = *count;
     if (n == 0) return;

@@ -34,7 +34,11 @@ struct LocalCounters {
 };
 
 constexpr uint32_t kNoRay = 0xFFFFFFFFu;
-constexpr int kRefill = 12;
+// A warp takes new rays once this many of its lanes are idle (or all are).
+#ifndef WF_TRACE_REFILL
+#define WF_TRACE_REFILL 12
+#endif
+constexpr int kRefill = WF_TRACE_REFILL;
 
 // Ray sources / sinks.  load(i, o, d, tmax, no_cull); root(i, S) = the TLAS
 // root node of the ray's scene, kInvalid for an empty scene; store(i, hit, ok)
@@ -233,14 +237,22 @@ __device__ __forceinline__ void flush_counters(const LocalCounters& c, Counters*
     }
 }
 
-constexpr int kTraceBlock = 128;
+#ifndef WF_TRACE_BLOCK
+#define WF_TRACE_BLOCK 128
+#endif
+constexpr int kTraceBlock = WF_TRACE_BLOCK;
+// Minimum resident blocks per SM asked of the compiler for the traversal
+// kernels (it caps their registers at 65536 / (128 * blocks)).
+#ifndef WF_TRACE_MIN_BLOCKS
+#define WF_TRACE_MIN_BLOCKS 1
+#endif
 int sm_count();
 
 // The traversal kernel: a persistent grid over count rays (read from
 // count_ptr on the device when it is non-null), rays handed out from *fetch.
 // total (optional) accumulates the number of rays of each launch.
 template <bool ANY, bool COUNT, class IO>
-__global__ void __launch_bounds__(kTraceBlock) k_trace(SceneRefs S, IO io, const uint32_t* count_ptr, uint32_t count,
+__global__ void __launch_bounds__(kTraceBlock, WF_TRACE_MIN_BLOCKS) k_trace(SceneRefs S, IO io, const uint32_t* count_ptr, uint32_t count,
                                                   uint32_t* fetch, uint32_t* status, Counters* counters,
                                                   unsigned long long* total) {
     const uint32_t n = count_ptr ? *count_ptr : count;
