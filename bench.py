@@ -82,6 +82,20 @@ def sum_over_ranks(dist, x):
     return float(t.item())
 
 
+def aggregate_weak(dist, gpu_ms, rays):
+    """Weak scaling: every rank traced its own frames; the job took the slowest
+    rank's time and processed every rank's rays.  Returns (max ms, total rays,
+    Mrays/s of the whole job)."""
+    t_max = max_over_ranks(dist, gpu_ms)
+    rays_all = sum_over_ranks(dist, rays)
+    return t_max, rays_all, rays_all / (t_max / 1e3) / 1e6
+
+
+def frame_seed(step, rank):
+    """Distinct frame seeds per rank, so ranks render different samples."""
+    return 1 + step + 7919 * rank
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -371,7 +385,7 @@ def run_ours(args, rank, world, local):
             flush_l2(torch, l2buf)
             if torch is not None:
                 torch.cuda.synchronize()
-            s = frame(1 + i + 7919 * rank, True)
+            s = frame(frame_seed(i, rank), True)
             gpu_ms += s["ms_total"]
             rays += s["rays_extend"] + s["rays_connect"]
             launches += s["launches"]
@@ -379,9 +393,7 @@ def run_ours(args, rank, world, local):
             ext_launches += s["launches_extend"]
         r.synchronize()
     barrier(dist)
-    t_max = max_over_ranks(dist, gpu_ms)
-    rays_all = sum_over_ranks(dist, rays)
-    value = rays_all / (t_max / 1e3) / 1e6
+    t_max, rays_all, value = aggregate_weak(dist, gpu_ms, rays)
     spp_per_s = world * SPP * args.steps / (t_max / 1e3)
     # --- algorithmic bytes of the extend kernel (counted pass, same seeds, untimed)
     r.render(max_bounces=DEPTH, spp=SPP, frame_seed=1, nee=1, rr_start_depth=RR, accumulate=False,
@@ -404,7 +416,7 @@ def run_ours(args, rank, world, local):
         for mesh, l2w, mat in desc.instances:
             r.submit_render_mesh(ids[mesh], l2w, mat)
         r.end_scene()
-        r.render(max_bounces=DEPTH, spp=SPP, frame_seed=1 + i + 7919 * rank, nee=1, rr_start_depth=RR,
+        r.render(max_bounces=DEPTH, spp=SPP, frame_seed=frame_seed(i, rank), nee=1, rr_start_depth=RR,
                  accumulate=False)
         wf.check(r.L.wf_read_image(r.h, wf.abi.ptr(img), img.size))
         s = r.stats()
