@@ -76,11 +76,24 @@ typedef struct wf_material_ext {
     float      ior;    /* dielectric only */
 } wf_material_ext;
 
-/* Constant environment radiance seen by rays that miss (the reference's
- * default environment is a 1x1 white texture, renderer.cpp:608-611). */
+/* Environment seen by rays that miss: an equirectangular HDR texture
+ * (begin_scene's env texture handle, renderer.cpp:599-611; sampled as
+ * shade.hlsl:36-40) or, with texture 0, a constant colour (the reference's
+ * default environment is a 1x1 white texture). */
 typedef struct wf_env {
-    float color[3];
+    float    color[3];
+    uint32_t texture;   /* 0 = constant colour; else a wf_texture_create id */
 } wf_env;
+
+/* Texel formats of wf_texture_create (renderer::create_render_texture,
+ * render_texture_params_t.format).  Texels are converted once to RGBA float:
+ * 8-bit UNORM c -> c / 255, sRGB -> linear, RG8 -> (r, g, 0, 1). */
+enum wf_texture_format {
+    WF_TEXTURE_RGBA8 = 0,
+    WF_TEXTURE_RGBA8_SRGB = 1,
+    WF_TEXTURE_RG8 = 2,
+    WF_TEXTURE_RGBA32F = 3
+};
 
 /* Options of one wf_render call beyond render_settings_t. */
 typedef struct wf_render_options {
@@ -139,6 +152,17 @@ int wf_mesh_create_prebuilt(wf_ctx* ctx, const triangle_t* triangles, uint32_t t
 /* Copies the mesh's BLAS blob ([bvh_header_t | nodes | bvh_triangle_t | uint32 index]). */
 int wf_mesh_get_blas(wf_ctx* ctx, uint32_t mesh, void* out_blob, uint64_t* inout_size);
 
+/* ---- textures (renderer::create_render_texture) ------------------------- */
+/* Uploads a width x height texture (row 0 first); *out_texture is its id
+ * (>= 1).  material_t's base_color_index / normal_index /
+ * metallic_roughness_index / emissive_index and wf_env.texture take these
+ * ids; 0 selects the reference's default texture for the slot (white base
+ * colour and emission, normal (127, 127, 255)/255, metallic-roughness
+ * (1, 1, 0)).  Materials sample with bilinear filtering and wrap addressing;
+ * the metal BSDF's roughness is roughness_factor x the texture's green. */
+int wf_texture_create(wf_ctx* ctx, uint32_t width, uint32_t height, uint32_t format, const void* texels,
+                      uint32_t* out_texture);
+
 /* ---- scene (renderer::begin_scene / submit_render_mesh / end_scene) ------ */
 /* begin_scene (renderer.cpp:599-630): sets the view, clears the instance list,
  * and resets accumulation when the view changed. env may be NULL (white). */
@@ -158,7 +182,12 @@ int wf_scene_get_instances(wf_ctx* ctx, bvh_instance_t* out, uint32_t capacity, 
 /* The scene's TLAS blob ([tlas_header_t | nodes | bvh_instance_t]). */
 int wf_scene_get_tlas(wf_ctx* ctx, void* out_blob, uint64_t* inout_size);
 
-/* ---- rendering (renderer::render, renderer.cpp:742-939 + post_process) --- */
+/* ---- rendering (renderer::render, renderer.cpp:742-939 + post_process) ---
+ * settings->render_view_mode selects the reference's debug views
+ * (shade.hlsl:140-153): the primary hit's instance / primitive colour,
+ * barycentrics, vertex normal, uv, material base colour / normal map /
+ * metallic-roughness / emission, world normal or depth / far_plane; as in the
+ * reference a view mode never accumulates over calls. */
 /* Renders opts->spp samples per pixel through generate -> extend -> shade ->
  * connect for depth 0..settings->max_bounces, adding them to the accumulator
  * (or replacing it when settings->accumulate == 0).  Asynchronous: errors

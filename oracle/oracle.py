@@ -30,10 +30,15 @@ class _Mesh(ctypes.Structure):
     _fields_ = [("tris", ctypes.c_void_p), ("tri_count", ctypes.c_uint32), ("blas", ctypes.c_void_p)]
 
 
+class _Texture(ctypes.Structure):
+    _fields_ = [("texels", ctypes.c_void_p), ("w", ctypes.c_uint32), ("h", ctypes.c_uint32)]
+
+
 class _Scene(ctypes.Structure):
     _fields_ = [("meshes", ctypes.POINTER(_Mesh)), ("mesh_count", ctypes.c_uint32), ("tlas", ctypes.c_void_p),
                 ("inst", ctypes.c_void_p), ("inst_count", ctypes.c_uint32), ("tri_albedo", ctypes.c_void_p),
-                ("inst_tri_offset", ctypes.c_void_p)]
+                ("inst_tri_offset", ctypes.c_void_p), ("textures", ctypes.POINTER(_Texture)),
+                ("texture_count", ctypes.c_uint32), ("env_texture", ctypes.c_uint32)]
 
 
 class Counters(ctypes.Structure):
@@ -49,7 +54,7 @@ class RenderParams(ctypes.Structure):
                 ("hdr_env_strength", ctypes.c_float), ("env_color", ctypes.c_float * 3),
                 ("spp", ctypes.c_uint32), ("sample_offset", ctypes.c_uint32), ("nee", ctypes.c_uint32),
                 ("rr_start_depth", ctypes.c_uint32), ("frame_seed", ctypes.c_uint32),
-                ("pixel_begin", ctypes.c_uint32), ("pixel_end", ctypes.c_uint32)]
+                ("pixel_begin", ctypes.c_uint32), ("pixel_end", ctypes.c_uint32), ("view_mode", ctypes.c_uint32)]
 
 
 class RenderStats(ctypes.Structure):
@@ -100,6 +105,13 @@ def lib():
         L.orc_intersect_aabb.argtypes = [vp, vp, vp, vp, ctypes.c_float]
         L.orc_intersect_aabb.restype = ctypes.c_float
         L.orc_primary_ray.argtypes = [ctypes.POINTER(View), u32, u32, vp]
+        L.orc_atan2.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.orc_atan2.restype = ctypes.c_float
+        L.orc_asin.argtypes = [ctypes.c_float]
+        L.orc_asin.restype = ctypes.c_float
+        L.orc_int_to_color.argtypes = [u32, vp]
+        L.orc_tex_sample.argtypes = [ctypes.POINTER(_Texture), ctypes.c_float, ctypes.c_float, vp]
+        L.orc_env_texel.argtypes = [ctypes.POINTER(_Texture), vp, vp]
         _lib = L
     return _lib
 
@@ -178,7 +190,8 @@ class Scene:
             arr[i].blas = b.ctypes.data
         self._meshes = arr
         self.c = _Scene(arr, len(meshes), self._tlas.ctypes.data, self._inst.ctypes.data if len(self._inst) else None,
-                        len(self._inst), None, None)
+                        len(self._inst), None, None, None, 0, 0)
+        self._textures = []
         self._albedo = None
         counts = [len(self._tris[m]) for m in self._inst["mesh"]]
         self.inst_tri_offset = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint32) if counts else \
@@ -196,6 +209,19 @@ class Scene:
         assert len(self._albedo) == 3 * self.triangle_count
         self.c.tri_albedo = self._albedo.ctypes.data
         self.c.inst_tri_offset = self.inst_tri_offset.ctypes.data
+
+    def set_textures(self, textures, env_texture=0):
+        """textures: list of RGBA float32 arrays (h x w x 4), ids 1..n in list
+        order; env_texture: 0 = the constant env colour, else a texture id."""
+        self._textures = [np.ascontiguousarray(t, dtype=np.float32) for t in textures]
+        arr = (_Texture * max(1, len(self._textures)))()
+        for i, t in enumerate(self._textures):
+            arr[i].texels = t.ctypes.data
+            arr[i].h, arr[i].w = t.shape[0], t.shape[1]
+        self._tex_arr = arr
+        self.c.textures = arr
+        self.c.texture_count = len(self._textures)
+        self.c.env_texture = env_texture
 
     def set_emission(self, instance, strength):
         self._inst[instance]["material"]["emissive_strength"] = strength
@@ -228,8 +254,9 @@ class Scene:
 
     def render(self, view, width, height, max_bounces=4, spp=1, frame_seed=1, nee=0, rr_start_depth=0xFFFFFFFF,
                env_color=(0.0, 0.0, 0.0), env_strength=1.0, cosine=1, sample_offset=0, threads=1, f64=False,
-               pixel_range=None, accum=None):
+               pixel_range=None, accum=None, view_mode=0):
         p = RenderParams()
+        p.view_mode = view_mode
         p.max_bounces, p.cosine_weighted_diffuse, p.hdr_env_strength = max_bounces, cosine, env_strength
         p.env_color[:] = env_color
         p.spp, p.sample_offset, p.nee, p.rr_start_depth, p.frame_seed = spp, sample_offset, nee, rr_start_depth, \
@@ -250,6 +277,35 @@ class Scene:
                  "stack_overflows": st.stack_overflows, "extend_traffic": st.extend_traffic.as_dict(),
                  "shadow_traffic": st.shadow_traffic.as_dict()}
         return accum, stats
+
+
+def texture_struct(texels):
+    """A _Texture over an RGBA float32 array (h x w x 4); keep texels alive."""
+    t = _Texture()
+    t.texels = texels.ctypes.data
+    t.h, t.w = texels.shape[0], texels.shape[1]
+    return t
+
+
+def tex_sample(texels, u, v):
+    texels = np.ascontiguousarray(texels, dtype=np.float32)
+    out = np.zeros(4, np.float32)
+    lib().orc_tex_sample(ctypes.byref(texture_struct(texels)), u, v, ptr(out))
+    return out
+
+
+def env_texel(texels, d):
+    texels = np.ascontiguousarray(texels, dtype=np.float32)
+    dd = np.asarray(d, dtype=np.float32)
+    out = np.zeros(3, np.float32)
+    lib().orc_env_texel(ctypes.byref(texture_struct(texels)), ptr(dd), ptr(out))
+    return out
+
+
+def int_to_color(v):
+    out = np.zeros(3, np.float32)
+    lib().orc_int_to_color(v, ptr(out))
+    return out
 
 
 def primary_rays(view, width, height):

@@ -202,6 +202,61 @@ static int FN(trace_one)(const orc_scene* s, FN(v3) o, FN(v3) d, R tmax, uint32_
 }
 
 /* ---------------------------------------------------------------------------
+ * Textures (material.hlsl:15-39 sampling, shade.hlsl:36-40 environment)
+ * ------------------------------------------------------------------------- */
+
+/* Bilinear, wrap addressing, texel centres at (i + 0.5) / w; weights in R. */
+static void FN(tex_sample)(const orc_texture* t, R u, R v, R out[4]) {
+    R x = u * (R)t->w - K(0.5), y = v * (R)t->h - K(0.5);
+    R x0 = FLOOR(x), y0 = FLOOR(y);
+    R ax = x - x0, ay = y - y0;
+    uint32_t i0 = wrap_texel((double)x0, t->w), i1 = wrap_texel((double)(x0 + K(1.0)), t->w);
+    uint32_t j0 = wrap_texel((double)y0, t->h), j1 = wrap_texel((double)(y0 + K(1.0)), t->h);
+    const float* a = t->texels + 4 * ((size_t)j0 * t->w + i0);
+    const float* b = t->texels + 4 * ((size_t)j0 * t->w + i1);
+    const float* c = t->texels + 4 * ((size_t)j1 * t->w + i0);
+    const float* d = t->texels + 4 * ((size_t)j1 * t->w + i1);
+    for (int k = 0; k < 4; ++k) {
+        R top = (R)a[k] + ((R)b[k] - (R)a[k]) * ax;
+        R bot = (R)c[k] + ((R)d[k] - (R)c[k]) * ax;
+        out[k] = top + (bot - top) * ay;
+    }
+}
+
+/* The texture of a material slot; id 0 = the reference's default texture
+ * (renderer.cpp:244-272): white base colour / emission, normal
+ * (127, 127, 255)/255, metallic-roughness RG8 (255, 255) = (1, 1, 0, 1). */
+static void FN(mat_tex)(const orc_scene* s, uint32_t id, int slot, R u, R v, R out[4]) {
+    if (id == 0) {
+        out[0] = out[1] = out[2] = out[3] = K(1.0);
+        if (slot == 1) { out[0] = K(127.0) / K(255.0); out[1] = K(127.0) / K(255.0); }
+        if (slot == 2) out[2] = K(0.0);
+        return;
+    }
+    FN(tex_sample)(&s->textures[id - 1], u, v, out);
+}
+
+/* sample_hdr_env: direction_to_equirect_uv (sample.hlsl:4-11, INV_ATAN =
+ * (0.1591, 0.3183)) times the texture size, truncated; out of range = 0. */
+static FN(v3) FN(env_texel)(const orc_texture* e, FN(v3) d) {
+    R u = ATAN2(d.z, d.x) * K(0.1591) + K(0.5);
+    R v = ASIN(-d.y) * K(0.3183) + K(0.5);
+    R fx = u * (R)e->w, fy = v * (R)e->h;
+    if (!(fx >= K(0.0) && fx < (R)e->w && fy >= K(0.0) && fy < (R)e->h)) return FN(mk)(0, 0, 0);
+    const float* p = e->texels + 4 * ((size_t)(uint32_t)fy * e->w + (uint32_t)fx);
+    return FN(mk)((R)p[0], (R)p[1], (R)p[2]);
+}
+
+/* int_to_color (common.hlsl:276-295). */
+static FN(v3) FN(int_to_color)(uint32_t v) {
+    uint32_t h = murmur_mix(v);
+    R k = K(1.0) / K(255.0);
+    return FN(mk)((R)(h & 255u) * k, (R)((h >> 8) & 255u) * k, (R)((h >> 16) & 255u) * k);
+}
+
+static inline FN(v3) FN(abs3)(FN(v3) a) { return FN(mk)(FABS(a.x), FABS(a.y), FABS(a.z)); }
+
+/* ---------------------------------------------------------------------------
  * Shading
  * ------------------------------------------------------------------------- */
 
@@ -225,6 +280,8 @@ static inline FN(v3) FN(to_world)(FN(v3) v, FN(v3) tg, FN(v3) n, FN(v3) bt) {
 typedef struct {
     FN(v3) p0, e1, e2, n, le;
     R area;
+    R uv[6];                  /* vertex uv (u0, v0, u1, v1, u2, v2) */
+    uint32_t tex;             /* emissive texture id (0 = none) */
 } FN(light);
 
 typedef struct {
@@ -274,6 +331,10 @@ static void FN(build_lights)(const orc_scene* s, FN(lights)* L) {
             lt->area = K(0.5) * len;
             lt->n = FN(scl)(c, K(1.0) / len);
             lt->le = le;
+            lt->uv[0] = (R)me->tris[t].v0.uv[0]; lt->uv[1] = (R)me->tris[t].v0.uv[1];
+            lt->uv[2] = (R)me->tris[t].v1.uv[0]; lt->uv[3] = (R)me->tris[t].v1.uv[1];
+            lt->uv[4] = (R)me->tris[t].v2.uv[0]; lt->uv[5] = (R)me->tris[t].v2.uv[1];
+            lt->tex = m->emissive_index;
             run = run + lt->area;
             L->cdf[k] = run;
             k++;
@@ -363,6 +424,17 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
                                &st->extend_traffic);
         if (tr < 0) { st->stack_overflows++; }
         if (h.inst == WF_INVALID_INDEX) {
+            if (P->view_mode != 0) {
+                /* debug views of a miss: the hit record's ids, barycentrics and
+                 * t; views of the surface read zero */
+                FN(v3) val = FN(mk)(0, 0, 0);
+                if (P->view_mode == 1 || P->view_mode == 2) val = FN(int_to_color)(WF_INVALID_INDEX);
+                else if (P->view_mode == 3) val = FN(mk)(h.u, h.v, K(0.0));
+                else if (P->view_mode == 11) { R q = h.t / (R)J->view->far_plane; val = FN(mk)(q, q, q); }
+                acc[0] = acc[0] + val.x; acc[1] = acc[1] + val.y; acc[2] = acc[2] + val.z;
+                return;
+            }
+            if (s->env_texture) env = FN(env_texel)(&s->textures[s->env_texture - 1], rd);
             /* miss: energy += throughput * strength * env (shade.hlsl:60-65) */
             acc[0] = acc[0] + (T.x * env_strength) * env.x;
             acc[1] = acc[1] + (T.y * env_strength) * env.y;
@@ -378,19 +450,49 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
         FN(v3) n0 = FN(ld)(tri->v0.normal), n1 = FN(ld)(tri->v1.normal), n2 = FN(ld)(tri->v2.normal);
         FN(v3) nl = FN(add)(FN(add)(n0, FN(scl)(FN(sub)(n1, n0), h.u)), FN(scl)(FN(sub)(n2, n0), h.v));
         FN(v3) N = FN(normalize)(FN(xform)(nl, K(0.0), in->local_to_world));
-        /* sample_material (material.hlsl:15-39) with 1x1 white textures */
+        /* sample_material (material.hlsl:15-39): factors x textures at the uv */
         const material_t* m = &in->material;
-        FN(v3) base = FN(mk)((R)m->base_color_factor[0] * K(1.0), (R)m->base_color_factor[1] * K(1.0),
-                             (R)m->base_color_factor[2] * K(1.0));
+        R tu = K(0.0), tv = K(0.0);
+        if ((m->base_color_index | m->normal_index | m->metallic_roughness_index | m->emissive_index) != 0u ||
+            P->view_mode == 5) {
+            tu = ((R)tri->v0.uv[0] + h.u * ((R)tri->v1.uv[0] - (R)tri->v0.uv[0])) +
+                 h.v * ((R)tri->v2.uv[0] - (R)tri->v0.uv[0]);
+            tv = ((R)tri->v0.uv[1] + h.u * ((R)tri->v1.uv[1] - (R)tri->v0.uv[1])) +
+                 h.v * ((R)tri->v2.uv[1] - (R)tri->v0.uv[1]);
+        }
+        R tb[4], tmr[4], tem[4];
+        FN(mat_tex)(s, m->base_color_index, 0, tu, tv, tb);
+        FN(mat_tex)(s, m->metallic_roughness_index, 2, tu, tv, tmr);
+        FN(mat_tex)(s, m->emissive_index, 3, tu, tv, tem);
+        FN(v3) base = FN(mk)((R)m->base_color_factor[0] * tb[0], (R)m->base_color_factor[1] * tb[1],
+                             (R)m->base_color_factor[2] * tb[2]);
         uint32_t stri = 0;
         if (s->tri_albedo) {
             stri = s->inst_tri_offset[h.inst] + h.prim;
             base = FN(mk)((R)s->tri_albedo[3ull * stri], (R)s->tri_albedo[3ull * stri + 1],
                           (R)s->tri_albedo[3ull * stri + 2]);
         }
-        FN(v3) le = FN(mk)(((R)m->emissive_strength * (R)m->emissive_factor[0]) * K(1.0),
-                           ((R)m->emissive_strength * (R)m->emissive_factor[1]) * K(1.0),
-                           ((R)m->emissive_strength * (R)m->emissive_factor[2]) * K(1.0));
+        FN(v3) le = FN(mk)(((R)m->emissive_strength * (R)m->emissive_factor[0]) * tem[0],
+                           ((R)m->emissive_strength * (R)m->emissive_factor[1]) * tem[1],
+                           ((R)m->emissive_strength * (R)m->emissive_factor[2]) * tem[2]);
+        if (P->view_mode != 0) {
+            /* debug views (shade.hlsl:140-153) */
+            FN(v3) val = FN(mk)(0, 0, 0);
+            uint32_t vm = P->view_mode;
+            if (vm == 1) val = FN(int_to_color)(h.inst);
+            else if (vm == 2) val = FN(int_to_color)(h.prim);
+            else if (vm == 3) val = FN(mk)(h.u, h.v, K(0.0));
+            else if (vm == 4) val = FN(abs3)(nl);
+            else if (vm == 5) val = FN(mk)(tu, tv, K(0.0));
+            else if (vm == 6) val = base;
+            else if (vm == 7) { R tn[4]; FN(mat_tex)(s, m->normal_index, 1, tu, tv, tn); val = FN(abs3)(FN(mk)(tn[0], tn[1], tn[2])); }
+            else if (vm == 8) val = FN(mk)(K(0.0), tmr[1], tmr[2]);
+            else if (vm == 9) val = le;
+            else if (vm == 10) val = FN(abs3)(N);
+            else if (vm == 11) { R q = h.t / (R)J->view->far_plane; val = FN(mk)(q, q, q); }
+            acc[0] = acc[0] + val.x; acc[1] = acc[1] + val.y; acc[2] = acc[2] + val.z;
+            return;
+        }
         if (le.x != K(0.0) || le.y != K(0.0) || le.z != K(0.0)) {
             R w = K(1.0);
             if (P->nee && !(flags & ORC_F_SPECULAR) && J->lights.count > 0) {
@@ -420,7 +522,8 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
         R pdf = K(0.0);
         int delta = 0, valid = 1, toggle_inside = 0;
         FN(v3) org = pos;
-        R alpha = (R)m->roughness_factor * (R)m->roughness_factor;
+        R rough = (R)m->roughness_factor * tmr[1];   /* roughness factor x texture green */
+        R alpha = rough * rough;
         uint32_t bsdf = in->bsdf;
         if (bsdf == 1 && alpha < ORC_METAL_DELTA_ALPHA) bsdf = 3; /* mirror */
         /* a ray travelling inside glass may reach an opaque surface from behind */
@@ -548,8 +651,17 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
                     R q = pdf_b / pdf_l;
                     R w = (q == q) ? K(1.0) / (K(1.0) + q * q) : K(0.0);
                     R sc = (cos_x * w) / pdf_l;
-                    FN(v3) contrib = FN(mk)(((T.x * f.x) * sc) * lt->le.x, ((T.y * f.y) * sc) * lt->le.y,
-                                            ((T.z * f.z) * sc) * lt->le.z);
+                    FN(v3) ltle = lt->le;
+                    if (lt->tex) {
+                        /* textured emitter: its emission texture at the sampled point */
+                        R lu = (lt->uv[0] + b1 * (lt->uv[2] - lt->uv[0])) + b2 * (lt->uv[4] - lt->uv[0]);
+                        R lv = (lt->uv[1] + b1 * (lt->uv[3] - lt->uv[1])) + b2 * (lt->uv[5] - lt->uv[1]);
+                        R te[4];
+                        FN(tex_sample)(&s->textures[lt->tex - 1], lu, lv, te);
+                        ltle = FN(mk)(ltle.x * te[0], ltle.y * te[1], ltle.z * te[2]);
+                    }
+                    FN(v3) contrib = FN(mk)(((T.x * f.x) * sc) * ltle.x, ((T.y * f.y) * sc) * ltle.y,
+                                            ((T.z * f.z) * sc) * ltle.z);
                     st->shadow_rays[d < 16 ? d : 15]++;
                     FN(hit) sh;
                     int r = FN(trace_one)(s, pos, wl, dist * ORC_SHADOW_TMAX_SCALE, ORC_ANY_HIT, &sh,

@@ -76,8 +76,60 @@ static void sincos_2pi_f64(double r, double* s, double* c) {
 }
 
 /* ---- instantiations ------------------------------------------------------ */
+/* ---- FP32 inverse trigonometry (the GPU library's own, same operations) ----
+ * On [0, 1] arguments above tan(pi/8) are reduced by atan z = pi/4 +
+ * atan((z - 1) / (z + 1)); on |z| <= tan(pi/8) the Taylor series of atan
+ * through z^17 in Horner form. */
+static float atan_unit_f(float z) {
+    float off = 0.0f;
+    if (z > 0.41421357f) {
+        z = (z - 1.0f) / (z + 1.0f);
+        off = 0.78539819f;
+    }
+    const float t2 = z * z;
+    float p = 0.05882353f;
+    p = 0.06666667f - t2 * p;
+    p = 0.07692308f - t2 * p;
+    p = 0.09090909f - t2 * p;
+    p = 0.11111111f - t2 * p;
+    p = 0.14285715f - t2 * p;
+    p = 0.2f - t2 * p;
+    p = 0.33333334f - t2 * p;
+    p = 1.0f - t2 * p;
+    return off + z * p;
+}
+float orc_atan2(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    if (ax == 0.0f && ay == 0.0f) return 0.0f;
+    float a = (ay <= ax) ? atan_unit_f(ay / ax) : 1.57079637f - atan_unit_f(ax / ay);
+    if (x < 0.0f) a = 3.14159274f - a;
+    return (y < 0.0f) ? -a : a;
+}
+float orc_asin(float y) { return orc_atan2(y, sqrtf(fmaxf(0.0f, (1.0f - y) * (1.0f + y)))); }
+
+static uint32_t murmur_mix(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+
+/* Wrap addressing of an integral coordinate; out-of-range or non-finite
+ * coordinates read texel 0 (as the GPU library). */
+static uint32_t wrap_texel(double f, uint32_t n) {
+    if (!(f > -16777216.0 && f < 16777216.0)) return 0u;
+    int m = ((int)f) % (int)n;
+    if (m < 0) m += (int)n;
+    return (uint32_t)m;
+}
+
 #define R float
 #define FN(x) x##_f32
+#define ATAN2 orc_atan2
+#define ASIN orc_asin
+#define FLOOR floorf
 #define K(x) x##f
 #define SQRT sqrtf
 #define FABS fabsf
@@ -96,8 +148,24 @@ static void sincos_2pi_f64(double r, double* s, double* c) {
 #undef SINCOS2PI
 #undef MAXT
 
+void orc_int_to_color(uint32_t v, float out[3]) {
+    v3_f32 c = int_to_color_f32(v);
+    out[0] = c.x; out[1] = c.y; out[2] = c.z;
+}
+void orc_tex_sample(const orc_texture* t, float u, float v, float out[4]) { tex_sample_f32(t, u, v, out); }
+void orc_env_texel(const orc_texture* t, const float dir[3], float out[3]) {
+    v3_f32 c = env_texel_f32(t, mk_f32(dir[0], dir[1], dir[2]));
+    out[0] = c.x; out[1] = c.y; out[2] = c.z;
+}
+
+#undef ATAN2
+#undef ASIN
+#undef FLOOR
 #define R double
 #define FN(x) x##_f64
+#define ATAN2 atan2
+#define ASIN asin
+#define FLOOR floor
 #define K(x) x
 #define SQRT sqrt
 #define FABS fabs

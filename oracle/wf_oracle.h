@@ -59,6 +59,12 @@ typedef struct orc_instance {
     float ior;
 } orc_instance;
 
+/* RGBA float texels, row-major, row 0 at v = 0. */
+typedef struct orc_texture {
+    const float* texels;
+    uint32_t w, h;
+} orc_texture;
+
 typedef struct orc_scene {
     const orc_mesh* meshes;
     uint32_t mesh_count;
@@ -69,6 +75,12 @@ typedef struct orc_scene {
      * colour); scene triangle of (instance i, primitive p) = inst_tri_offset[i] + p */
     const double* tri_albedo;
     const uint32_t* inst_tri_offset;
+    /* textures by id (textures[id - 1]; id 0 = the slot's default texture),
+     * named by material_t's four texture indices; env_texture 0 = constant
+     * env_color, else an equirect texture id */
+    const orc_texture* textures;
+    uint32_t texture_count;
+    uint32_t env_texture;
 } orc_scene;
 
 typedef struct orc_counters {
@@ -98,6 +110,7 @@ typedef struct orc_render_params {
     uint32_t rr_start_depth;
     uint32_t frame_seed;
     uint32_t pixel_begin, pixel_end;   /* render only this pixel range (end 0 = all) */
+    uint32_t view_mode;       /* RENDER_VIEW_MODE_* (shade.hlsl:140-153); 0 = path tracing */
 } orc_render_params;
 
 typedef struct orc_render_stats {
@@ -138,6 +151,11 @@ int orc_intersect_triangle(const float v0[3], const float v1[3], const float v2[
 float orc_intersect_aabb(const float bmin[3], const float bmax[3], const float org[3],
                          const float inv_dir[3], float t);
 void orc_primary_ray(const view_t* view, uint32_t px, uint32_t py, RayDesc2* out);
+float orc_atan2(float y, float x);
+float orc_asin(float y);
+void orc_int_to_color(uint32_t v, float out[3]);
+void orc_tex_sample(const orc_texture* t, float u, float v, float out[4]);
+void orc_env_texel(const orc_texture* t, const float dir[3], float out[3]);
 
 #ifdef __cplusplus
 }

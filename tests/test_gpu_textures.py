@@ -1,0 +1,192 @@
+"""GPU: textured materials, the equirect environment and the render view modes
+against the CPU oracle.
+
+The box scene gets random vertex uv (outside [0, 1], so wrap addressing is
+exercised), an RGBA8 base-colour texture on the walls, an RG8
+metallic-roughness texture on a metal sphere, an RGBA32F emission texture on
+the light (sampled both on direct hits and by next-event estimation) and an
+RGBA32F equirect environment.  Texel conversion is exact for these formats
+(c / 255 in float), the bilinear weights, wrap and the environment's own
+atan2 / asin are the same float operations on both sides, so images are
+compared bit for bit, path traced and in every debug view."""
+import numpy as np
+import pytest
+
+from wavefrontpathtracing_gb300 import Batch, Renderer, abi, scenes
+from tests.helpers import load_scene_into, oracle_scene_from_renderer
+
+pytestmark = pytest.mark.gpu
+
+W, H = 64, 48
+
+
+def textures(seed=4):
+    rng = np.random.default_rng(seed)
+    base8 = rng.integers(0, 256, (8, 8, 4), dtype=np.uint8)
+    mr8 = rng.integers(0, 256, (4, 4, 2), dtype=np.uint8)
+    emis = rng.uniform(0.5, 1.5, (4, 4, 4)).astype(np.float32)
+    env = rng.uniform(0.0, 2.0, (8, 16, 4)).astype(np.float32)
+    # the float texels both sides sample (wf_texture_create's conversion)
+    base_f = base8.astype(np.float32) / np.float32(255.0)
+    mr_f = np.zeros((4, 4, 4), np.float32)
+    mr_f[..., :2] = mr8.astype(np.float32) / np.float32(255.0)
+    mr_f[..., 3] = 1.0
+    return [(base8, abi.TEXTURE_RGBA8, base_f), (mr8, abi.TEXTURE_RG8, mr_f), (emis, abi.TEXTURE_RGBA32F, emis),
+            (env, abi.TEXTURE_RGBA32F, env)]
+
+
+def textured_box(seed=4):
+    desc = scenes.box_scene(width=W, height=H, subdivision=3, max_bounces=4)
+    rng = np.random.default_rng(seed)
+    for t in desc.meshes:
+        for v in ("v0", "v1", "v2"):
+            t[v]["uv"] = rng.uniform(-1.0, 2.0, (len(t), 2)).astype(np.float32)
+    (_, _, m0), (_, _, m1), (_, _, m2) = desc.instances
+    m0 = m0.copy()
+    m0["base"]["base_color_index"] = 1
+    m1 = scenes.material(base=(0.9, 0.7, 0.4), bsdf=scenes.BSDF_METAL, roughness=0.6, metallic=1.0)
+    m1["base"]["metallic_roughness_index"] = 2
+    m2 = m2.copy()
+    m2["base"]["emissive_index"] = 3
+    desc.instances = [(0, np.eye(4), m0), (1, np.eye(4), m1), (2, np.eye(4), m2)]
+    desc.settings.update(nee=1, rr_start_depth=2, env=(1.0, 1.0, 1.0))
+    return desc
+
+
+def render_pair(orc, desc, view_mode=0, spp=2, seed=9, env_texture=4):
+    tex = textures()
+    st = desc.settings
+    with Renderer(W, H) as r:
+        ids = [r.create_texture(raw, fmt) for raw, fmt, _ in tex]
+        assert ids == [1, 2, 3, 4]
+        mesh_ids = load_scene_into(r, desc)
+        r.begin_scene(desc.view, st["env"], env_texture=env_texture)   # again, with the environment texture
+        for mesh, l2w, mat in desc.instances:
+            r.submit_render_mesh(mesh_ids[mesh], l2w, mat)
+        r.end_scene()
+        sc, _ = oracle_scene_from_renderer(orc, desc, r, mesh_ids)
+        r.render(max_bounces=st["max_bounces"], spp=spp, frame_seed=seed, nee=st["nee"],
+                 rr_start_depth=st["rr_start_depth"], accumulate=False, view_mode=view_mode)
+        got = r.read_image()
+        ldr = r.read_image_ldr()
+    sc.set_textures([f for _, _, f in tex], env_texture=env_texture)
+    acc, _ = sc.render(desc.view, W, H, max_bounces=st["max_bounces"], spp=spp, frame_seed=seed, nee=st["nee"],
+                       rr_start_depth=st["rr_start_depth"], env_color=st["env"], threads=4, view_mode=view_mode)
+    want = np.zeros_like(acc)
+    want[..., :3] = acc[..., :3] / acc[..., 3:]
+    want[..., 3] = acc[..., 3]
+    return got, want, ldr
+
+
+def assert_same(got, want, what):
+    bad = np.nonzero((got.view(np.uint32) != want.view(np.uint32)).any(axis=-1))
+    assert bad[0].size == 0, f"{what}: {bad[0].size} pixels differ, first at {list(zip(bad[0][:4], bad[1][:4]))}"
+
+
+def test_textured_materials_and_environment_bit_exact(orc):
+    desc = textured_box()
+    got, want, _ = render_pair(orc, desc)
+    assert got[..., :3].mean() > 0.05
+    assert_same(got, want, "path traced")
+
+
+def test_constant_environment_and_textures_bit_exact(orc):
+    got, want, _ = render_pair(orc, textured_box(), env_texture=0)
+    assert_same(got, want, "constant env")
+
+
+@pytest.mark.parametrize("mode", list(range(1, 12)))
+def test_render_view_modes_bit_exact(orc, mode):
+    got, want, ldr = render_pair(orc, textured_box(), view_mode=mode, spp=1)
+    assert_same(got, want, f"view mode {mode}")
+    # post_process.hlsl: no tonemap in a view mode, sRGB only for base colour / emission
+    img = np.nan_to_num(got[..., :3], nan=0.0)
+    bad = ~np.isfinite(got[..., :3]).all(axis=-1)
+    x = np.clip(img, 0.0, 1.0)
+    if mode in (6, 9):
+        x = np.where(x <= 0.0031308, x * 12.92, 1.055 * np.power(x, 1.0 / 2.4) - 0.055)
+    ref = np.floor(np.clip(x, 0, 1) * 255.0 + 0.5).astype(np.int32)
+    ref[bad] = (255, 0, 255)
+    assert np.abs(ldr[..., :3].astype(np.int32) - ref).max() <= 1
+
+
+def test_view_modes_do_not_accumulate(orc):
+    desc = textured_box()
+    with Renderer(W, H) as r:
+        for raw, fmt, _ in textures():
+            r.create_texture(raw, fmt)
+        load_scene_into(r, desc)
+        r.render(max_bounces=2, spp=1, frame_seed=1, view_mode=abi.RENDER_VIEW_MODE_WORLD_NORMAL)
+        a = r.read_image()
+        r.render(max_bounces=2, spp=1, frame_seed=2, view_mode=abi.RENDER_VIEW_MODE_WORLD_NORMAL)
+        b = r.read_image()
+        assert np.array_equal(a, b) and (a[..., 3] == 1.0).all()
+
+
+def test_texture_formats_convert_like_the_reference_defaults(orc):
+    """A 1x1 texture of each format seen through the base-colour view."""
+    quad = scenes.quad((-1.0, -1.0, 0.0), (0.0, 2.0, 0.0), (2.0, 0.0, 0.0))   # faces -z, towards the camera
+    view = scenes.make_view((0.0, 0.0, -2.0), (0.0, 0.0, 0.0), 30.0, 8, 8)
+    cases = [(np.array([[[10, 128, 255, 7]]], np.uint8), abi.TEXTURE_RGBA8),
+             (np.array([[[10, 128, 255, 7]]], np.uint8), abi.TEXTURE_RGBA8_SRGB),
+             (np.array([[[10, 200]]], np.uint8), abi.TEXTURE_RG8),
+             (np.array([[[0.25, 2.5, -1.0, 1.0]]], np.float32), abi.TEXTURE_RGBA32F)]
+
+    def srgb(c):
+        c = c / 255.0
+        return np.where(c <= 0.04045, c / 12.92, ((c + 0.055) / 1.055) ** 2.4)
+
+    want = [np.array([10, 128, 255]) / 255.0, srgb(np.array([10, 128, 255])), np.array([10 / 255.0, 200 / 255.0, 0.0]),
+            np.array([0.25, 2.5, -1.0])]
+    with Renderer(8, 8) as r:
+        mesh = r.create_mesh_from_triangles(quad, interval_count=8)
+        for (raw, fmt), w in zip(cases, want):
+            tid = r.create_texture(raw, fmt)
+            m = scenes.material(base=(1.0, 1.0, 1.0))
+            m["base"]["base_color_index"] = tid
+            r.begin_scene(view)
+            r.submit_render_mesh(mesh, np.eye(4), m)
+            r.end_scene()
+            r.render(max_bounces=1, spp=1, view_mode=abi.RENDER_VIEW_MODE_MATERIAL_BASE_COLOR)
+            px = r.read_image()[4, 4, :3]
+            np.testing.assert_allclose(px, w, rtol=1e-6, atol=1e-7)
+
+
+def test_unknown_texture_ids_are_rejected():
+    import wavefrontpathtracing_gb300 as wf
+    with Renderer(8, 8) as r:
+        mesh = r.create_mesh_from_triangles(scenes.quad((0, 0, 0), (1, 0, 0), (0, 1, 0)))
+        r.begin_scene(scenes.make_view((0.5, 0.5, -1), (0.5, 0.5, 0), 45.0, 8, 8))
+        m = scenes.material()
+        m["base"]["emissive_index"] = 3
+        with pytest.raises(wf.WFError) as e:
+            r.submit_render_mesh(mesh, np.eye(4), m)
+        assert e.value.status == -1
+        with pytest.raises(wf.WFError):
+            r.begin_scene(scenes.make_view((0.5, 0.5, -1), (0.5, 0.5, 0), 45.0, 8, 8), env_texture=1)
+        with pytest.raises(wf.WFError):
+            r.create_texture(np.zeros((0, 4, 4), np.uint8))
+
+
+def test_batch_with_textures_equals_single_render(orc):
+    desc = textured_box()
+    tex = textures()
+    st = desc.settings
+    with Renderer(W, H) as r:
+        [r.create_texture(raw, fmt) for raw, fmt, _ in tex]
+        ids = load_scene_into(r, desc)
+        r.begin_scene(desc.view, st["env"], env_texture=4)
+        for mesh, l2w, mat in desc.instances:
+            r.submit_render_mesh(ids[mesh], l2w, mat)
+        r.end_scene()
+        r.render(max_bounces=st["max_bounces"], spp=2, frame_seed=3, nee=1, rr_start_depth=2, accumulate=False)
+        single = r.read_image()
+        b = Batch(r)
+        b.begin_scene(W, H, 2, desc.view, st["env"], env_texture=4)
+        for mesh, l2w, mat in desc.instances:
+            b.submit(ids[mesh], l2w, mat)
+        b.end_scene()
+        b.set_config(capacity=1024)
+        b.render(max_bounces=st["max_bounces"], frame_seed=3, nee=1, rr_start_depth=2)
+        assert_same(b.read_image(0), single, "batch")
+        b.close()

@@ -139,3 +139,67 @@ def test_render_f32_and_f64_agree_on_box(orc):
     assert img32.mean() > 0.01
     # the same random numbers drive both; rare paths diverge at triangle edges
     assert np.sqrt(np.mean((img32 - img64) ** 2)) < 2e-2
+
+
+def test_own_atan2_and_asin_are_accurate(orc):
+    """The FP32 arctangent both sides evaluate (Taylor series after reduction
+    by tan(pi/8)) against numpy's correctly rounded double results."""
+    L = orc.lib()
+    rng = np.random.default_rng(5)
+    y = rng.normal(size=4000).astype(np.float32)
+    x = rng.normal(size=4000).astype(np.float32)
+    y[:8] = [0, 0, 1, -1, 0, 0, 1e-30, -1e-30]
+    x[:8] = [1, -1, 0, 0, 0, -0.0, 1e-30, -1e-30]
+    got = np.array([L.orc_atan2(float(a), float(b)) for a, b in zip(y, x)])
+    want = np.arctan2(y.astype(np.float64), x.astype(np.float64))
+    want[4:6] = 0.0   # atan2(0, +-0): defined as 0 here
+    assert np.abs(got - want).max() < 6e-7
+    s = np.concatenate([rng.uniform(-1, 1, 2000), [-1.0, 1.0, 0.0, 0.5]]).astype(np.float32)
+    got = np.array([L.orc_asin(float(v)) for v in s])
+    assert np.abs(got - np.arcsin(s.astype(np.float64))).max() < 1e-6
+
+
+def test_int_to_color_known_answers(orc):
+    def murmur(h):
+        h ^= h >> 16
+        h = (h * 0x85EBCA6B) & 0xFFFFFFFF
+        h ^= h >> 13
+        h = (h * 0xC2B2AE35) & 0xFFFFFFFF
+        h ^= h >> 16
+        return h
+    for v in (0, 1, 7, 123456, 0xFFFFFFFF):
+        h = murmur(v)
+        want = np.array([h & 255, (h >> 8) & 255, (h >> 16) & 255], np.float32) * np.float32(1.0 / 255.0)
+        assert np.array_equal(orc.int_to_color(v), want)
+
+
+def test_bilinear_wrap_sampling(orc):
+    rng = np.random.default_rng(3)
+    tex = rng.uniform(0, 1, (5, 7, 4)).astype(np.float32)
+    h, w = tex.shape[:2]
+    for u, v in [(0.0, 0.0), (0.5, 0.5), (1.3, -0.2), (-2.71, 3.14), (0.07, 0.93)]:
+        x, y = u * w - 0.5, v * h - 0.5
+        x0, y0 = np.floor(x), np.floor(y)
+        ax, ay = x - x0, y - y0
+        i0, i1 = int(x0) % w, int(x0 + 1) % w
+        j0, j1 = int(y0) % h, int(y0 + 1) % h
+        t = tex.astype(np.float64)
+        want = (1 - ay) * ((1 - ax) * t[j0, i0] + ax * t[j0, i1]) + ay * ((1 - ax) * t[j1, i0] + ax * t[j1, i1])
+        np.testing.assert_allclose(orc.tex_sample(tex, u, v), want, atol=2e-6)
+    # a 1x1 texture returns its texel exactly
+    one = np.array([[[0.3, 0.6, 0.9, 1.0]]], np.float32)
+    assert np.array_equal(orc.tex_sample(one, 0.37, -5.2), one[0, 0])
+
+
+def test_equirect_environment_lookup(orc):
+    rng = np.random.default_rng(8)
+    env = rng.uniform(0, 1, (8, 16, 4)).astype(np.float32)
+    d = rng.normal(size=(500, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    agree = 0
+    for v in d.astype(np.float32):
+        u = np.arctan2(float(v[2]), float(v[0])) * 0.1591 + 0.5
+        w = np.arcsin(-float(v[1])) * 0.3183 + 0.5
+        want = env[int(w * 8), int(u * 16), :3]
+        agree += np.array_equal(orc.env_texel(env, v), want)
+    assert agree >= 495   # texel boundaries may round either way in float

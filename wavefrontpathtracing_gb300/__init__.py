@@ -65,6 +65,7 @@ SIGNATURES = {
     "wf_scene_set_albedo": [_vp, _vp, _u64],
     "wf_scene_set_emission": [_vp, _u32, ctypes.c_float],
     "wf_adjoint": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
+    "wf_texture_create": [_vp, _u32, _u32, _u32, _vp, _pu32],
     "wf_batch_create": [_vp, ctypes.POINTER(_vp)],
     "wf_batch_destroy": [_vp],
     "wf_batch_scene_begin": [_vp, _u32, _u32, _u32, _vp, _vp, _pu32],
@@ -183,12 +184,30 @@ class Renderer:
         check(self.L.wf_mesh_get_blas(self.h, mesh, ptr(out), ctypes.byref(n)))
         return out
 
+    # ---- textures
+    def create_texture(self, texels, fmt=None):
+        """texels: h x w x 4 uint8 (RGBA8, or RGBA8_SRGB with fmt), h x w x 2
+        uint8 (RG8) or h x w x 4 float32 (RGBA32F).  Returns the texture id."""
+        texels = np.ascontiguousarray(texels)
+        h, w = texels.shape[0], texels.shape[1]
+        if fmt is None:
+            if texels.dtype == np.float32:
+                fmt = abi.TEXTURE_RGBA32F
+            elif texels.shape[2] == 2:
+                fmt = abi.TEXTURE_RG8
+            else:
+                fmt = abi.TEXTURE_RGBA8
+        out = ctypes.c_uint32()
+        check(self.L.wf_texture_create(self.h, w, h, fmt, ptr(texels), ctypes.byref(out)))
+        return out.value
+
     # ---- scene
-    def begin_scene(self, view, env=None):
+    def begin_scene(self, view, env=None, env_texture=0):
         e = None
-        if env is not None:
+        if env is not None or env_texture:
             e = Env()
-            e.color[:] = list(env)
+            e.color[:] = list(env) if env is not None else [1.0, 1.0, 1.0]
+            e.texture = env_texture
         check(self.L.wf_scene_begin(self.h, ctypes.byref(view), ctypes.byref(e) if e is not None else None))
 
     def submit_render_mesh(self, mesh, transform, material=None):
@@ -343,11 +362,12 @@ class Batch:
     def __exit__(self, *a):
         self.close()
 
-    def begin_scene(self, width, height, spp, view, env=None):
+    def begin_scene(self, width, height, spp, view, env=None, env_texture=0):
         e = None
-        if env is not None:
+        if env is not None or env_texture:
             e = Env()
-            e.color[:] = list(env)
+            e.color[:] = list(env) if env is not None else [1.0, 1.0, 1.0]
+            e.texture = env_texture
         idx = ctypes.c_uint32(0)
         check(self.L.wf_batch_scene_begin(self.h, width, height, spp, ctypes.byref(view),
                                           ctypes.byref(e) if e is not None else None, ctypes.byref(idx)))

@@ -32,6 +32,11 @@ for _dt, _size in ((vertex_dtype, 48), (triangle_dtype, 144), (material_dtype, 5
 
 INVALID = 0xFFFFFFFF
 BSDF_LAMBERT, BSDF_METAL, BSDF_DIELECTRIC = 0, 1, 2
+# RENDER_VIEW_MODE (shared.hlsl.h:17-32)
+(RENDER_VIEW_MODE_NONE, RENDER_VIEW_MODE_GEOMETRY_INSTANCE, RENDER_VIEW_MODE_GEOMETRY_PRIMITIVE,
+ RENDER_VIEW_MODE_GEOMETRY_BARYCENTRICS, RENDER_VIEW_MODE_GEOMETRY_NORMAL, RENDER_VIEW_MODE_GEOMETRY_UV,
+ RENDER_VIEW_MODE_MATERIAL_BASE_COLOR, RENDER_VIEW_MODE_MATERIAL_NORMAL, RENDER_VIEW_MODE_MATERIAL_METALLIC_ROUGHNESS,
+ RENDER_VIEW_MODE_MATERIAL_EMISSIVE, RENDER_VIEW_MODE_WORLD_NORMAL, RENDER_VIEW_MODE_RENDER_TARGET_DEPTH) = range(12)
 TRACE_ANY_HIT, TRACE_NO_CULL, TRACE_COUNT_TRAFFIC = 1, 2, 4
 
 
@@ -64,7 +69,10 @@ class BvhOptions(ctypes.Structure):
 
 
 class Env(ctypes.Structure):
-    _fields_ = [("color", ctypes.c_float * 3)]
+    _fields_ = [("color", ctypes.c_float * 3), ("texture", ctypes.c_uint32)]
+
+
+TEXTURE_RGBA8, TEXTURE_RGBA8_SRGB, TEXTURE_RG8, TEXTURE_RGBA32F = 0, 1, 2, 3
 
 
 class RenderOptions(ctypes.Structure):

@@ -72,6 +72,11 @@ struct DevBuf {
     void release() { dev_free(p); cap = 0; }
 };
 
+struct Texture {
+    float4* d = nullptr;
+    uint32_t w = 0, h = 0;
+};
+
 struct Mesh {
     uint32_t tri_count = 0, node_count = 0;
     std::vector<triangle_t> tris;     // original order (create_render_mesh keeps them too)
@@ -100,6 +105,10 @@ struct wf_ctx {
     view_t view{};
     bool view_valid = false, in_scene = false, scene_ready = false, view_changed = true;
     float env[3] = {1.0f, 1.0f, 1.0f};
+    uint32_t env_texture = 0;
+    uint32_t last_view_mode = 0;
+    std::vector<Texture> textures;          // id k + 1
+    DevBuf<TexRef> tex_table;               // entry 0 unused
 
     // device scene
     DevBuf<float4> tnodes, tinst, sinst;
@@ -276,6 +285,11 @@ int upload_shading_tris(wf_ctx* c, Mesh& m) {
             st[6ull * i + k] = make_float4(v[k]->position[0], v[k]->position[1], v[k]->position[2], 0.0f);
             st[6ull * i + 3 + k] = make_float4(v[k]->normal[0], v[k]->normal[1], v[k]->normal[2], 0.0f);
         }
+        // vertex uv in the .w slots: {p0, u0} {p1, v0} {p2, u1} {n0, v1} {n1, u2} {n2, v2}
+        for (int k = 0; k < 3; ++k) {
+            st[6ull * i + 2 * k].w = v[k]->uv[0];
+            st[6ull * i + 2 * k + 1].w = v[k]->uv[1];
+        }
     }
     int rc = dev_alloc(&m.d_stri, st.size());
     if (rc) return rc;
@@ -449,6 +463,13 @@ cudaStream_t ctx_stream(wf_ctx* c) { return c->stream; }
 uint32_t* ctx_status(wf_ctx* c) { return c->status; }
 uint32_t ctx_mesh_count(wf_ctx* c) { return (uint32_t)c->meshes.size(); }
 uint32_t ctx_tlas_metric(wf_ctx* c) { return c->tlas_metric; }
+const TexRef* ctx_texture_table(wf_ctx* c) { return c->tex_table.p; }
+uint32_t ctx_texture_count(wf_ctx* c) { return (uint32_t)c->textures.size(); }
+TexRef ctx_texture(wf_ctx* c, uint32_t id) {
+    if (id == 0 || id > c->textures.size()) return TexRef{nullptr, 0u, 0u};
+    const Texture& t = c->textures[id - 1];
+    return TexRef{t.d, t.w, t.h};
+}
 int ctx_take_status(wf_ctx* c) { return take_status(c); }
 cudaError_t ctx_h2d(wf_ctx* c, void* dst, const void* src, size_t bytes) { return h2d(c, dst, src, bytes); }
 cudaError_t ctx_d2h(wf_ctx* c, void* dst, const void* src, size_t bytes) { return d2h(c, dst, src, bytes); }
@@ -472,6 +493,10 @@ int make_instance(wf_ctx* c, uint32_t mesh, const float* l2w, const material_t* 
     if (!l2w || !mat) return fail(WF_ERR_INVALID, w + ": null argument");
     if (mesh >= c->meshes.size()) return fail(WF_ERR_INVALID, w + ": unknown mesh");
     if (bsdf > WF_BSDF_DIELECTRIC) return fail(WF_ERR_INVALID, w + ": unknown BSDF");
+    const uint32_t ids[4] = {mat->base_color_index, mat->normal_index, mat->metallic_roughness_index,
+                             mat->emissive_index};
+    for (uint32_t id : ids)
+        if (id > c->textures.size()) return fail(WF_ERR_INVALID, w + ": material names an unknown texture");
     Instance& in = *out;
     in = Instance{};
     in.mesh = mesh;
@@ -500,7 +525,7 @@ int make_instance(wf_ctx* c, uint32_t mesh, const float* l2w, const material_t* 
     return WF_OK;
 }
 
-void instance_rows(const Instance& in, float4 ti[4], float4 si[6], float aabb[6]) {
+void instance_rows(const Instance& in, float4 ti[4], float4 si[kInstRows], float aabb[6]) {
     std::memcpy(aabb, in.bi.aabb_min, 12);
     std::memcpy(aabb + 3, in.bi.aabb_max, 12);
     float meshf, bsdff;
@@ -520,6 +545,12 @@ void instance_rows(const Instance& in, float4 ti[4], float4 si[6], float aabb[6]
     si[4] = make_float4(mt.base_color_factor[0], mt.base_color_factor[1], mt.base_color_factor[2], mt.metallic_factor);
     si[5] = make_float4(mt.emissive_strength * mt.emissive_factor[0], mt.emissive_strength * mt.emissive_factor[1],
                         mt.emissive_strength * mt.emissive_factor[2], mt.emissive_strength);
+    float tb, tn, tm, te;
+    std::memcpy(&tb, &mt.base_color_index, 4);
+    std::memcpy(&tn, &mt.normal_index, 4);
+    std::memcpy(&tm, &mt.metallic_roughness_index, 4);
+    std::memcpy(&te, &mt.emissive_index, 4);
+    si[6] = make_float4(tb, tn, tm, te);
 }
 
 void append_emitters(const Instance& in, const MeshView& m, std::vector<LightTri>& out, float& run) {
@@ -544,7 +575,11 @@ void append_emitters(const Instance& in, const MeshView& m, std::vector<LightTri
         L.e1 = make_float4(e1[0], e1[1], e1[2], run);
         L.e2 = make_float4(e2[0], e2[1], e2[2], 0.0f);
         L.n = make_float4(cr[0] * il, cr[1] * il, cr[2] * il, 0.0f);
-        L.le = make_float4(le[0], le[1], le[2], 0.0f);
+        float tex;
+        std::memcpy(&tex, &in.mat.emissive_index, 4);
+        L.le = make_float4(le[0], le[1], le[2], tex);
+        L.uv01 = make_float4(m.tris[t].v0.uv[0], m.tris[t].v0.uv[1], m.tris[t].v1.uv[0], m.tris[t].v1.uv[1]);
+        L.uv2 = make_float4(m.tris[t].v2.uv[0], m.tris[t].v2.uv[1], 0.0f, 0.0f);
         out.push_back(L);
     }
 }
@@ -627,6 +662,8 @@ int wf_destroy(wf_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (Mesh& m : c->meshes) free_mesh(m);
+    for (Texture& t : c->textures) dev_free(t.d);
+    c->tex_table.release();
     release_buffers(c);
     c->tnodes.release(); c->tinst.release(); c->sinst.release(); c->blas.release(); c->stri.release();
     c->lights.release(); c->aabbs.release(); c->tlas_scratch.release();
@@ -728,6 +765,58 @@ int wf_mesh_get_blas(wf_ctx* c, uint32_t mesh, void* out, uint64_t* inout_size) 
     return WF_OK;
 }
 
+// ---------------------------------------------------------------------------- textures
+
+int wf_texture_create(wf_ctx* c, uint32_t w, uint32_t h, uint32_t format, const void* data, uint32_t* out) {
+    if (!c || !data || !out) return fail(WF_ERR_INVALID, "wf_texture_create: null argument");
+    if (w == 0 || h == 0 || w > 16384 || h > 16384)
+        return fail(WF_ERR_INVALID, "wf_texture_create: width and height must be in [1, 16384]");
+    if (format > WF_TEXTURE_RGBA32F) return fail(WF_ERR_INVALID, "wf_texture_create: unknown format");
+    int rc = use_device(c);
+    if (rc) return rc;
+    const size_t n = (size_t)w * h;
+    std::vector<float4> tx(n);
+    const uint8_t* b = static_cast<const uint8_t*>(data);
+    if (format == WF_TEXTURE_RGBA32F) {
+        std::memcpy(tx.data(), data, n * sizeof(float4));
+    } else if (format == WF_TEXTURE_RG8) {
+        for (size_t i = 0; i < n; ++i) tx[i] = make_float4(b[2 * i] / 255.0f, b[2 * i + 1] / 255.0f, 0.0f, 1.0f);
+    } else {
+        float lut[256];
+        for (int k = 0; k < 256; ++k) {
+            if (format == WF_TEXTURE_RGBA8_SRGB) {
+                // sRGB transfer function inverse (IEC 61966-2-1), evaluated in double
+                const double v = k / 255.0;
+                lut[k] = (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
+            } else {
+                lut[k] = k / 255.0f;
+            }
+        }
+        for (size_t i = 0; i < n; ++i)
+            tx[i] = make_float4(lut[b[4 * i]], lut[b[4 * i + 1]], lut[b[4 * i + 2]], b[4 * i + 3] / 255.0f);
+    }
+    Texture t;
+    t.w = w;
+    t.h = h;
+    if ((rc = dev_alloc(&t.d, n))) return rc;
+    cudaError_t e = h2d(c, t.d, tx.data(), n * sizeof(float4));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        dev_free(t.d);
+        return fail(WF_ERR_CUDA, std::string("wf_texture_create: ") + cudaGetErrorString(e));
+    }
+    c->textures.push_back(t);
+    std::vector<TexRef> table(c->textures.size() + 1);
+    table[0] = TexRef{nullptr, 0u, 0u};
+    for (size_t k = 0; k < c->textures.size(); ++k)
+        table[k + 1] = TexRef{c->textures[k].d, c->textures[k].w, c->textures[k].h};
+    if ((rc = c->tex_table.reserve(table.size()))) return rc;
+    WF_CUDA(h2d(c, c->tex_table.p, table.data(), table.size() * sizeof(TexRef)));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    *out = (uint32_t)c->textures.size();
+    return WF_OK;
+}
+
 // ---------------------------------------------------------------------------- scene
 
 int wf_scene_begin(wf_ctx* c, const view_t* view, const wf_env* env) {
@@ -736,8 +825,10 @@ int wf_scene_begin(wf_ctx* c, const view_t* view, const wf_env* env) {
     c->view_changed = !c->view_valid || std::memcmp(&c->view.world_to_view, view->world_to_view, 64) != 0;
     c->view = *view;
     c->view_valid = true;
+    if (env && env->texture > c->textures.size()) return fail(WF_ERR_INVALID, "wf_scene_begin: unknown env texture");
     if (env) std::memcpy(c->env, env->color, 12);
     else c->env[0] = c->env[1] = c->env[2] = 1.0f;
+    c->env_texture = env ? env->texture : 0u;
     c->instances.clear();
     c->in_scene = true;
     c->scene_ready = false;
@@ -787,14 +878,14 @@ int wf_scene_end(wf_ctx* c) {
     }
     // per-instance data
     std::vector<float> aabbs(6ull * n);
-    std::vector<float4> ti(4ull * n), si(6ull * n);
+    std::vector<float4> ti(4ull * n), si((size_t)kInstRows * n);
     c->scene_bi.resize(n);
     c->scene_triangles = 0;
     for (uint32_t i = 0; i < n; ++i) c->scene_triangles += c->meshes[c->instances[i].mesh].tri_count;
     for (uint32_t i = 0; i < n; ++i) {
         const Instance& in = c->instances[i];
         c->scene_bi[i] = in.bi;
-        instance_rows(in, &ti[4ull * i], &si[6ull * i], &aabbs[6ull * i]);
+        instance_rows(in, &ti[4ull * i], &si[(size_t)kInstRows * i], &aabbs[6ull * i]);
     }
     if ((rc = c->tnodes.reserve(2ull * std::max<uint32_t>(2 * n, 1))) || (rc = c->tinst.reserve(ti.size())) ||
         (rc = c->sinst.reserve(si.size())) || (rc = c->aabbs.reserve(aabbs.size())) ||
@@ -898,8 +989,8 @@ int validate_render(wf_ctx* c, const render_settings_t* s, const wf_render_optio
     if (!c->scene_ready) return fail(WF_ERR_STATE, std::string(who) + ": call wf_scene_end first");
     if (s->max_bounces >= kMaxDepth - 1) return fail(WF_ERR_INVALID, std::string(who) + ": max_bounces must be < 15");
     if (o->spp == 0) return fail(WF_ERR_INVALID, std::string(who) + ": spp must be >= 1");
-    if (s->render_view_mode != RENDER_VIEW_MODE_NONE)
-        return fail(WF_ERR_INVALID, std::string(who) + ": only RENDER_VIEW_MODE_NONE is implemented");
+    if (s->render_view_mode >= RENDER_VIEW_MODE_COUNT)
+        return fail(WF_ERR_INVALID, std::string(who) + ": unknown render_view_mode");
     return WF_OK;
 }
 
@@ -923,6 +1014,13 @@ Pass make_pass(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     W.cosine = s->cosine_weighted_diffuse ? 1u : 0u;
     W.env_strength = s->hdr_env_strength;
     std::memcpy(W.env, c->env, 12);
+    W.env_tex = TexRef{nullptr, 0u, 0u};
+    if (c->env_texture) {
+        const Texture& t = c->textures[c->env_texture - 1];
+        W.env_tex = TexRef{t.d, t.w, t.h};
+    }
+    W.view_mode = s->render_view_mode;
+    W.far_plane = c->view.far_plane;
     P.S = scene_refs(c);
     P.SH.sinst = c->sinst.p;
     P.SH.stri = c->stri.p;
@@ -931,6 +1029,7 @@ Pass make_pass(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     P.SH.light_total = c->light_total;
     P.SH.tri_albedo = c->albedo_set ? c->tri_albedo.p : nullptr;
     P.SH.inst_tri_offset = c->albedo_set ? c->inst_tri_offset.p : nullptr;
+    P.SH.textures = c->tex_table.p;
     P.B = c->B;
     P.B.status = c->status;
     P.B.counters = c->counters;
@@ -994,7 +1093,9 @@ int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o,
     if ((rc = ensure_buffers(c))) return rc;
     if ((rc = begin_call(c, o->count_traffic != 0))) return rc;
     const uint32_t npix = c->width * c->height;
-    if (!s->accumulate || c->view_changed) {
+    // a debug view replaces the accumulator every call (post_process.hlsl:44-51)
+    if (!s->accumulate || c->view_changed || s->render_view_mode != RENDER_VIEW_MODE_NONE ||
+        c->last_view_mode != RENDER_VIEW_MODE_NONE) {
         WF_CUDA(cudaMemsetAsync(c->accum, 0, (size_t)npix * sizeof(float4), c->stream));
         c->accum_samples = 0;
         c->view_changed = false;
@@ -1005,6 +1106,7 @@ int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o,
     for (const Wave& wv : plan_waves(o->spp, npix, wave))
         if ((rc = run_wave(c, P, wv, c->accum_samples, none, true))) return rc;
     c->accum_samples += o->spp;
+    c->last_view_mode = s->render_view_mode;
     c->stats.paths = (uint64_t)npix * o->spp;
     uint64_t paths = c->stats.paths;
     rc = end_call(c);
@@ -1017,6 +1119,8 @@ int wf_adjoint(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     int rc = validate_render(c, s, o, "wf_adjoint");
     if (rc) return rc;
     if (!dloss_dimage || !d_albedo || !d_emission) return fail(WF_ERR_INVALID, "wf_adjoint: null argument");
+    if (s->render_view_mode != RENDER_VIEW_MODE_NONE)
+        return fail(WF_ERR_INVALID, "wf_adjoint: differentiates the path-traced image (RENDER_VIEW_MODE_NONE)");
     if (!c->albedo_set) return fail(WF_ERR_STATE, "wf_adjoint: set the per-triangle albedo first (wf_scene_set_albedo)");
     if (o->nee || o->rr_start_depth <= s->max_bounces)
         return fail(WF_ERR_INVALID, "wf_adjoint: path replay needs nee = 0 and Russian roulette off");
@@ -1139,7 +1243,7 @@ int wf_read_image_ldr(wf_ctx* c, uint8_t* out, uint64_t nbytes) {
     int rc = use_device(c);
     if (rc) return rc;
     if ((rc = c->image_ldr.reserve(npix))) return rc;
-    WF_CUDA(launch_post(c->accum, (uint32_t)npix, 1u, c->image_ldr.p, c->stream));
+    WF_CUDA(launch_post(c->accum, (uint32_t)npix, c->last_view_mode, c->image_ldr.p, c->stream));
     WF_CUDA(d2h(c, out, c->image_ldr.p, npix * 4));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     return take_status(c);

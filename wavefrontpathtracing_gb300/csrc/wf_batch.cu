@@ -59,8 +59,9 @@ struct BatchScene {
     float env[3];
     uint32_t frame_seed;
     uint32_t max_bounces, nee, rr_start, cosine;
+    TexRef env_tex;                // texels null: constant env
 };
-static_assert(sizeof(BatchScene) == 208, "BatchScene layout");
+static_assert(sizeof(BatchScene) == 224, "BatchScene layout");
 
 // Pool entry i of queue k: qo {origin, flags word}, qd {direction, pixel},
 // qT {throughput, pdf of the last BSDF sample}, qL {radiance, sample}.
@@ -237,6 +238,7 @@ __global__ void __launch_bounds__(BLOCK) k_bshade(ShadeRefs SH, const BatchScene
             K.cosine = S.cosine; K.env_strength = S.env_strength;
             K.env0 = S.env[0]; K.env1 = S.env[1]; K.env2 = S.env[2];
             K.lights = SH.lights + S.light_off; K.light_count = S.light_count; K.light_total = S.light_total;
+            K.env_tex = S.env_tex; K.view_mode = 0u; K.far_plane = 1.0f;
             ShadeIn in;
             in.rd = xyz(b);
             in.tuvp = Q.h_tuvp[i];
@@ -371,6 +373,7 @@ struct HostScene {
     uint32_t width, height, spp;
     view_t view;
     float env[3];
+    uint32_t env_texture;
     std::vector<Instance> inst;
 };
 
@@ -488,7 +491,7 @@ int build_tables(wf_batch* b) {
     BCUDA(ctx_h2d(c, b->stri.p, sp.data(), sp.size() * sizeof(void*)));
     // instances
     const uint32_t ni = b->total_inst;
-    std::vector<float4> ti(4ull * ni), si(6ull * ni);
+    std::vector<float4> ti(4ull * ni), si((size_t)kInstRows * ni);
     std::vector<float> ab(6ull * ni);
     std::vector<LightTri> lt;
     b->light_off.assign(ns, 0);
@@ -503,7 +506,7 @@ int build_tables(wf_batch* b) {
         b->light_off[s] = (uint32_t)lt.size();
         float run = 0.0f;
         for (const Instance& in : H.inst) {
-            instance_rows(in, &ti[4ull * k], &si[6ull * k], &ab[6ull * k]);
+            instance_rows(in, &ti[4ull * k], &si[(size_t)kInstRows * k], &ab[6ull * k]);
             MeshView mv;
             ctx_mesh(c, in.mesh, &mv);
             append_emitters(in, mv, lt, run);
@@ -627,6 +630,7 @@ int enqueue_iteration(wf_batch* b, int cur, cudaGraphConditionalHandle h, bool s
     SH.light_total = 0.0f;
     SH.tri_albedo = nullptr;
     SH.inst_tri_offset = nullptr;
+    SH.textures = ctx_texture_table(b->ctx);
     k_bbegin<<<1, 1, 0, st>>>(b->ctl, cur);
     BCUDA(cudaGetLastError());
     BCUDA(regen_or_shade(false, b, SH, Q, cur, st));
@@ -703,6 +707,7 @@ int upload_scene_table(wf_batch* b, const render_settings_t* s, const wf_render_
         S.light_total = b->light_total[i];
         S.env_strength = s->hdr_env_strength;
         std::memcpy(S.env, H.env, 12);
+        S.env_tex = ctx_texture(b->ctx, H.env_texture);
         S.frame_seed = frame_seed;
         S.max_bounces = s->max_bounces;
         S.nee = o->nee ? 1u : 0u;
@@ -795,7 +800,7 @@ int validate(wf_batch* b, const render_settings_t* s, const wf_render_options* o
     if (b->scenes.empty()) return fail_code(WF_ERR_STATE, w + ": the batch has no scenes");
     if (s->max_bounces >= kMaxDepth - 1) return fail_code(WF_ERR_INVALID, w + ": max_bounces must be < 15");
     if (s->render_view_mode != RENDER_VIEW_MODE_NONE)
-        return fail_code(WF_ERR_INVALID, w + ": only RENDER_VIEW_MODE_NONE is implemented");
+        return fail_code(WF_ERR_INVALID, w + ": a batch renders RENDER_VIEW_MODE_NONE only");
     return WF_OK;
 }
 
@@ -852,8 +857,11 @@ int wf_batch_scene_begin(wf_batch* b, uint32_t width, uint32_t height, uint32_t 
     H.height = height;
     H.spp = spp;
     H.view = *view;
+    if (env && env->texture > ctx_texture_count(b->ctx))
+        return fail_code(WF_ERR_INVALID, "wf_batch_scene_begin: unknown env texture");
     if (env) std::memcpy(H.env, env->color, 12);
     else H.env[0] = H.env[1] = H.env[2] = 1.0f;
+    H.env_texture = env ? env->texture : 0u;
     b->scenes.push_back(H);
     b->in_scene = true;
     b->tables_ready = false;

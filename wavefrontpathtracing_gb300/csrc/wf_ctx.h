@@ -38,6 +38,10 @@ cudaStream_t ctx_stream(wf_ctx* c);
 uint32_t* ctx_status(wf_ctx* c);
 uint32_t ctx_mesh_count(wf_ctx* c);
 uint32_t ctx_tlas_metric(wf_ctx* c);
+// Device table of the context's textures (indexed by id) and one texture by id.
+const TexRef* ctx_texture_table(wf_ctx* c);
+uint32_t ctx_texture_count(wf_ctx* c);
+TexRef ctx_texture(wf_ctx* c, uint32_t id);
 bool ctx_mesh(wf_ctx* c, uint32_t mesh, MeshView* out);
 // Reads and clears the device status word; maps its flags to a WF_ERR_* code.
 int ctx_take_status(wf_ctx* c);
@@ -49,8 +53,8 @@ cudaError_t ctx_d2h(wf_ctx* c, void* dst, const void* src, size_t bytes);
 int make_instance(wf_ctx* c, uint32_t mesh, const float* l2w, const material_t* mat, uint32_t bsdf, float ior,
                   const char* who, Instance* out);
 // The instance's rows of the traversal table (4 float4), the shading table
-// (6 float4) and its world AABB (min xyz, max xyz).
-void instance_rows(const Instance& in, float4 ti[4], float4 si[6], float aabb[6]);
+// (kInstRows float4) and its world AABB (min xyz, max xyz).
+void instance_rows(const Instance& in, float4 ti[4], float4 si[kInstRows], float aabb[6]);
 // Appends the world-space emitter triangles of an emissive instance, with the
 // running area sum the light sampler searches.
 void append_emitters(const Instance& in, const MeshView& m, std::vector<LightTri>& out, float& running_area);

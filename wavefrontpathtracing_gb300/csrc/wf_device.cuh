@@ -29,10 +29,12 @@ namespace wf {
 //           m[8..10], m[12..14] (the only entries the transform reads), with
 //           the mesh id in the first .w.
 // Shading side, per mesh: stri = 6 x float4 per triangle in original order
-//   {p0, -} {p1, -} {p2, -} {n0, -} {n1, -} {n2, -}.
-// Shading side, per instance: sinst = 6 x float4
+//   {p0, u0} {p1, v0} {p2, u1} {n0, v1} {n1, u2} {n2, v2} (vertex uv in .w).
+// Shading side, per instance: sinst = kInstRows (7) x float4
 //   {l2w m[0..2], mesh} {m[4..6], bsdf} {m[8..10], ior} {m[12..14], roughness}
-//   {base rgb, metallic} {emissive rgb (strength*factor), flags}
+//   {base rgb, metallic} {emissive rgb (strength*factor), strength}
+//   {texture ids: base colour, normal, metallic-roughness, emissive (0 = default)}
+// Textures: RGBA float texels, row-major, row 0 at v = 0.
 
 struct BlasRef {
     const float4* nodes;
@@ -46,12 +48,21 @@ struct SceneRefs {
     uint32_t inst_count;
 };
 
+constexpr int kInstRows = 7;   // float4 rows per instance in the shading table
+
 struct LightTri {
     float4 p0;   // .w = area
     float4 e1;   // .w = running area sum (cdf)
     float4 e2;
     float4 n;    // unit geometric normal
-    float4 le;   // emitted radiance
+    float4 le;   // emitted radiance (strength * factor), .w = emissive texture id (bits)
+    float4 uv01; // vertex uv {u0, v0, u1, v1}
+    float4 uv2;  // {u2, v2, -, -}
+};
+
+struct TexRef {
+    const float4* texels;   // nullptr: no texture
+    uint32_t w, h;
 };
 
 struct Counters {
@@ -179,5 +190,108 @@ __device__ __forceinline__ bool tri_hit(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& 
 }
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// ---------------------------------------------------------------- textures
+// Texture slots of material_t and the values of the reference's default
+// textures (renderer.cpp:244-272): base colour / emissive white, normal
+// RGBA8 (127, 127, 255, 255), metallic-roughness RG8 (255, 255) read as
+// (1, 1, 0, 1).
+enum : uint32_t { TEX_BASE = 0, TEX_NORMAL = 1, TEX_METAL_ROUGH = 2, TEX_EMISSIVE = 3 };
+__host__ __device__ __forceinline__ float4 tex_default(uint32_t slot) {
+    if (slot == TEX_NORMAL) return make_float4(127.0f / 255.0f, 127.0f / 255.0f, 1.0f, 1.0f);
+    if (slot == TEX_METAL_ROUGH) return make_float4(1.0f, 1.0f, 0.0f, 1.0f);
+    return make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+}
+
+// Wrap addressing of an integral float coordinate; out-of-range or
+// non-finite coordinates read texel 0.
+__host__ __device__ __forceinline__ uint32_t wrap_texel(float f, uint32_t n) {
+    if (!(f > -16777216.0f && f < 16777216.0f)) return 0u;
+    int m = ((int)f) % (int)n;
+    if (m < 0) m += (int)n;
+    return (uint32_t)m;
+}
+
+__host__ __device__ __forceinline__ float lerpf(float a, float b, float t) { return a + (b - a) * t; }
+
+// Sample(sampler_linear_wrap, uv) (material.hlsl:20-36) at the top level: texel
+// centres at (i + 0.5) / w, wrap addressing, bilinear weights in FP32 (the
+// hardware filter's weights have 8 fractional bits; these are exact).
+__device__ __forceinline__ float4 tex_bilinear(const TexRef& t, float u, float v) {
+    const float x = u * (float)t.w - 0.5f, y = v * (float)t.h - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float ax = x - x0, ay = y - y0;
+    const uint32_t i0 = wrap_texel(x0, t.w), i1 = wrap_texel(x0 + 1.0f, t.w);
+    const uint32_t j0 = wrap_texel(y0, t.h), j1 = wrap_texel(y0 + 1.0f, t.h);
+    const float4 a = ldg4(t.texels + (size_t)j0 * t.w + i0), b = ldg4(t.texels + (size_t)j0 * t.w + i1);
+    const float4 c = ldg4(t.texels + (size_t)j1 * t.w + i0), d = ldg4(t.texels + (size_t)j1 * t.w + i1);
+    float4 r;
+    r.x = lerpf(lerpf(a.x, b.x, ax), lerpf(c.x, d.x, ax), ay);
+    r.y = lerpf(lerpf(a.y, b.y, ax), lerpf(c.y, d.y, ax), ay);
+    r.z = lerpf(lerpf(a.z, b.z, ax), lerpf(c.z, d.z, ax), ay);
+    r.w = lerpf(lerpf(a.w, b.w, ax), lerpf(c.w, d.w, ax), ay);
+    return r;
+}
+
+// ---------------------------------------------------------------- inverse trigonometry
+// Our own arctangent: on [0, 1], arguments above tan(pi/8) are reduced by
+// atan z = pi/4 + atan((z - 1) / (z + 1)); on |z| <= tan(pi/8) the Taylor series
+// z - z^3/3 + ... - z^15/15 + z^17/17 (truncation error < 3e-9) in Horner form.
+__host__ __device__ __forceinline__ float atan_unit(float z) {
+    float off = 0.0f;
+    if (z > 0.41421357f) {
+        z = (z - 1.0f) / (z + 1.0f);
+        off = 0.78539819f;
+    }
+    const float t2 = z * z;
+    float p = 0.05882353f;             // 1/17
+    p = 0.06666667f - t2 * p;          // 1/15
+    p = 0.07692308f - t2 * p;          // 1/13
+    p = 0.09090909f - t2 * p;          // 1/11
+    p = 0.11111111f - t2 * p;          // 1/9
+    p = 0.14285715f - t2 * p;          // 1/7
+    p = 0.2f - t2 * p;                 // 1/5
+    p = 0.33333334f - t2 * p;          // 1/3
+    p = 1.0f - t2 * p;
+    return off + z * p;
+}
+// atan2 by octant: the smaller of |y|/|x|, |x|/|y| goes to atan_unit.
+__host__ __device__ __forceinline__ float atan2_wf(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    if (ax == 0.0f && ay == 0.0f) return 0.0f;
+    float a = (ay <= ax) ? atan_unit(ay / ax) : 1.57079637f - atan_unit(ax / ay);
+    if (x < 0.0f) a = 3.14159274f - a;
+    return (y < 0.0f) ? -a : a;
+}
+__host__ __device__ __forceinline__ float asin_wf(float y) {
+    return atan2_wf(y, sqrtf(fmaxf(0.0f, (1.0f - y) * (1.0f + y))));
+}
+
+// sample_hdr_env (shade.hlsl:36-40): direction_to_equirect_uv
+// (sample.hlsl:4-11, INV_ATAN = (0.1591, 0.3183)) scaled to texels and
+// truncated; a texel position outside the image reads zero, as an
+// out-of-range Texture2D load does.
+__device__ __forceinline__ V3 env_texel(const TexRef& e, V3 d) {
+    const float u = atan2_wf(d.z, d.x) * 0.1591f + 0.5f;
+    const float v = asin_wf(-d.y) * 0.3183f + 0.5f;
+    const float fx = u * (float)e.w, fy = v * (float)e.h;
+    if (!(fx >= 0.0f && fx < (float)e.w && fy >= 0.0f && fy < (float)e.h)) return mk(0.0f, 0.0f, 0.0f);
+    return xyz(ldg4(e.texels + (size_t)(uint32_t)fy * e.w + (uint32_t)fx));
+}
+
+// int_to_color (common.hlsl:276-295).
+__host__ __device__ __forceinline__ uint32_t murmur_mix(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+__host__ __device__ __forceinline__ V3 int_to_color(uint32_t v) {
+    const uint32_t h = murmur_mix(v);
+    const float k = 1.0f / 255.0f;
+    return mk((float)(h & 255u) * k, (float)((h >> 8) & 255u) * k, (float)((h >> 16) & 255u) * k);
+}
 
 }  // namespace wf

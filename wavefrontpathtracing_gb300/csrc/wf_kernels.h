@@ -5,18 +5,20 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "wf_device.cuh"
+#include "../../include/wf_shared.h"
 
 namespace wf {
 
 // Shading-side scene (see the layout comment in wf_device.cuh).
 struct ShadeRefs {
-    const float4* sinst;          // 6 x float4 per instance
-    const float4* const* stri;    // per mesh: 6 x float4 per triangle, original order
+    const float4* sinst;          // kInstRows x float4 per instance
+    const float4* const* stri;    // per mesh: 6 x float4 per triangle, original order (uv in .w)
     const LightTri* lights;
     uint32_t light_count;
     float light_total;
     const float4* tri_albedo;     // optional per scene triangle albedo (replaces the base colour)
     const uint32_t* inst_tri_offset;  // scene triangle of (instance i, primitive p) = offset[i] + p
+    const TexRef* textures;       // indexed by texture id (entry 0 unused: id 0 = default texture)
 };
 
 // Path-replay adjoint (null pointers in a forward pass).  The replay traces
@@ -75,6 +77,9 @@ struct WaveParams {
     uint32_t max_bounces, nee, rr_start, cosine;
     float env_strength;
     float env[3];
+    TexRef env_tex;             // texels null: constant env
+    uint32_t view_mode;
+    float far_plane;
 };
 
 // fetch: a zeroed device counter the persistent kernel hands rays out from.
@@ -90,8 +95,9 @@ cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t 
                            bool count, unsigned long long* total, cudaStream_t stream);
 // Adds each pixel's paths of the wave to the accumulator in sample order.
 cudaError_t launch_wave_resolve(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream);
-cudaError_t launch_post(const float4* accum, uint32_t npix, uint32_t view_mode_none, uchar4* out,
-                        cudaStream_t stream);
+// post_process.hlsl:25-72 for a render view mode (tonemap only for mode 0,
+// sRGB for modes 0, base colour and emissive).
+cudaError_t launch_post(const float4* accum, uint32_t npix, uint32_t view_mode, uchar4* out, cudaStream_t stream);
 cudaError_t launch_resolve(const float4* accum, uint32_t npix, float4* out, cudaStream_t stream);
 
 // TLAS: builds nodes [0, 2n) from per-instance world AABBs (tlas_builder.cpp).

@@ -43,6 +43,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
     K.frame_seed = W.frame_seed; K.max_bounces = W.max_bounces; K.nee = W.nee; K.rr_start = W.rr_start;
     K.cosine = W.cosine; K.env_strength = W.env_strength; K.env0 = W.env[0]; K.env1 = W.env[1]; K.env2 = W.env[2];
     K.lights = SH.lights; K.light_count = SH.light_count; K.light_total = SH.light_total;
+    K.env_tex = W.env_tex; K.view_mode = W.view_mode; K.far_plane = W.far_plane;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -100,7 +101,10 @@ __device__ __forceinline__ unsigned char unorm8(float c) {
 }
 __device__ __forceinline__ bool bad(float x) { return isnan(x) || isinf(x); }
 
-__global__ void k_post(const float4* __restrict__ accum, uint32_t npix, uint32_t tonemap, uchar4* __restrict__ out) {
+__global__ void k_post(const float4* __restrict__ accum, uint32_t npix, uint32_t view_mode, uchar4* __restrict__ out) {
+    const bool tonemap = view_mode == RENDER_VIEW_MODE_NONE;
+    const bool to_srgb = tonemap || view_mode == RENDER_VIEW_MODE_MATERIAL_BASE_COLOR ||
+                         view_mode == RENDER_VIEW_MODE_MATERIAL_EMISSIVE;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += stride) {
         float4 a = accum[i];
@@ -108,7 +112,8 @@ __global__ void k_post(const float4* __restrict__ accum, uint32_t npix, uint32_t
         float r = a.x * inv, g = a.y * inv, b = a.z * inv;
         if (bad(r) || bad(g) || bad(b)) { r = 1.0f; g = 0.0f; b = 1.0f; }
         if (tonemap) { r = r / (1.0f + r); g = g / (1.0f + g); b = b / (1.0f + b); }
-        out[i] = make_uchar4(unorm8(srgb(r)), unorm8(srgb(g)), unorm8(srgb(b)), 255);
+        if (to_srgb) { r = srgb(r); g = srgb(g); b = srgb(b); }
+        out[i] = make_uchar4(unorm8(r), unorm8(g), unorm8(b), 255);
     }
 }
 
@@ -170,8 +175,8 @@ cudaError_t launch_wave_resolve(const RenderBuffers& B, const WaveParams& W, cud
     return cudaGetLastError();
 }
 
-cudaError_t launch_post(const float4* accum, uint32_t npix, uint32_t tonemap, uchar4* out, cudaStream_t stream) {
-    k_post<<<grid_for(npix), kBlock, 0, stream>>>(accum, npix, tonemap, out);
+cudaError_t launch_post(const float4* accum, uint32_t npix, uint32_t view_mode, uchar4* out, cudaStream_t stream) {
+    k_post<<<grid_for(npix), kBlock, 0, stream>>>(accum, npix, view_mode, out);
     return cudaGetLastError();
 }
 

@@ -92,7 +92,18 @@ struct ShadeCtl {
     const LightTri* lights;
     uint32_t light_count;
     float light_total;
+    TexRef env_tex;         // equirect environment (texels null: constant env0..2)
+    uint32_t view_mode;     // RENDER_VIEW_MODE_* (0 = path tracing)
+    float far_plane;        // view_t.far_plane, for the depth view
 };
+
+__device__ __forceinline__ V3 abs3(V3 a) { return mk(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+
+// Material texture of a slot (id 0: the slot's default texture).
+__device__ __forceinline__ float4 mat_tex(const ShadeRefs& SH, uint32_t id, uint32_t slot, float u, float v) {
+    if (id == 0u) return tex_default(slot);
+    return tex_bilinear(SH.textures[id], u, v);
+}
 
 struct ShadeOut {
     V3 add;            // radiance this event adds to the path
@@ -121,14 +132,29 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
     const V3 rd = in.rd;
     uint32_t flags = in.flags;
     if (in.inst == kInvalid) {
+        if (K.view_mode != 0u) {
+            // debug views of a miss (shade.hlsl:140-153): the hit record's
+            // ids, barycentrics and t; views of the surface read zero (the
+            // reference loads the surface of instance UINT_MAX out of bounds)
+            const uint32_t vm = K.view_mode;
+            V3 val = mk(0.0f, 0.0f, 0.0f);
+            if (vm == 1u) val = int_to_color(kInvalid);
+            else if (vm == 2u) val = int_to_color(__float_as_uint(in.tuvp.w));
+            else if (vm == 3u) val = mk(in.tuvp.y, in.tuvp.z, 0.0f);
+            else if (vm == 11u) { const float q = in.tuvp.x / K.far_plane; val = mk(q, q, q); }
+            o.add = val;
+            o.has_add = true;
+            return;
+        }
         // miss: energy += throughput * strength * env (shade.hlsl:60-65)
-        o.add = mk((T.x * K.env_strength) * K.env0, (T.y * K.env_strength) * K.env1, (T.z * K.env_strength) * K.env2);
+        const V3 env = K.env_tex.texels ? env_texel(K.env_tex, rd) : mk(K.env0, K.env1, K.env2);
+        o.add = mk((T.x * K.env_strength) * env.x, (T.y * K.env_strength) * env.y, (T.z * K.env_strength) * env.z);
         o.has_add = true;
         return;
     }
     const uint32_t inst = in.inst;
-    const float4* ip = SH.sinst + 6ull * inst;
-    const float4 c0 = ip[0], c1 = ip[1], c2 = ip[2], c3 = ip[3], mb = ip[4], me = ip[5];
+    const float4* ip = SH.sinst + (size_t)kInstRows * inst;
+    const float4 c0 = ip[0], c1 = ip[1], c2 = ip[2], c3 = ip[3], mb = ip[4], me = ip[5], tx = ip[6];
     const uint32_t mesh = __float_as_uint(c0.w);
     const uint32_t prim = __float_as_uint(in.tuvp.w);
     const float4* tp = SH.stri[mesh] + 6ull * prim;
@@ -140,13 +166,44 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
     const V3 pos = xform(pl, 1.0f, c0, c1, c2, c3);
     const V3 nl = add(add(n0, scl(sub(n1, n0), hu)), scl(sub(n2, n0), hv));
     V3 N = normalize(xform(nl, 0.0f, c0, c1, c2, c3));
-    V3 base_c = mk(mb.x * 1.0f, mb.y * 1.0f, mb.z * 1.0f);
+    // sample_material (material.hlsl:15-39): factors times textures at the
+    // interpolated uv (default textures when a slot has none)
+    const uint32_t t_base = __float_as_uint(tx.x), t_nrm = __float_as_uint(tx.y);
+    const uint32_t t_mr = __float_as_uint(tx.z), t_em = __float_as_uint(tx.w);
+    float tu = 0.0f, tv = 0.0f;
+    if ((t_base | t_nrm | t_mr | t_em) != 0u || K.view_mode == 5u) {
+        tu = (tp[0].w + hu * (tp[2].w - tp[0].w)) + hv * (tp[4].w - tp[0].w);
+        tv = (tp[1].w + hu * (tp[3].w - tp[1].w)) + hv * (tp[5].w - tp[1].w);
+    }
+    const float4 tbase = mat_tex(SH, t_base, TEX_BASE, tu, tv);
+    const float4 mr = mat_tex(SH, t_mr, TEX_METAL_ROUGH, tu, tv);
+    const float4 et = mat_tex(SH, t_em, TEX_EMISSIVE, tu, tv);
+    V3 base_c = mk(mb.x * tbase.x, mb.y * tbase.y, mb.z * tbase.z);
     uint32_t stri = 0;
     if (SH.tri_albedo) {
         stri = SH.inst_tri_offset[inst] + prim;
         base_c = xyz(SH.tri_albedo[stri]);
     }
-    const V3 le = mk(me.x * 1.0f, me.y * 1.0f, me.z * 1.0f);
+    const V3 le = mk(me.x * et.x, me.y * et.y, me.z * et.z);
+    if (K.view_mode != 0u) {
+        // debug views (shade.hlsl:140-153), written instead of the radiance
+        const uint32_t vm = K.view_mode;
+        V3 val = mk(0.0f, 0.0f, 0.0f);
+        if (vm == 1u) val = int_to_color(inst);
+        else if (vm == 2u) val = int_to_color(prim);
+        else if (vm == 3u) val = mk(hu, hv, 0.0f);
+        else if (vm == 4u) val = abs3(nl);
+        else if (vm == 5u) val = mk(tu, tv, 0.0f);
+        else if (vm == 6u) val = base_c;
+        else if (vm == 7u) val = abs3(xyz(mat_tex(SH, t_nrm, TEX_NORMAL, tu, tv)));
+        else if (vm == 8u) val = mk(0.0f, mr.y, mr.z);
+        else if (vm == 9u) val = le;
+        else if (vm == 10u) val = abs3(N);
+        else if (vm == 11u) { const float q = in.tuvp.x / K.far_plane; val = mk(q, q, q); }
+        o.add = val;
+        o.has_add = true;
+        return;
+    }
     if (le.x != 0.0f || le.y != 0.0f || le.z != 0.0f) {
         float w = 1.0f;
         if (K.nee && !(flags & kFlagSpecular) && K.light_count > 0) {
@@ -180,7 +237,8 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
     float pdf = 0.0f;
     bool delta = false, valid = true, toggle_inside = false;
     V3 org = pos;
-    const float alpha = c3.w * c3.w;
+    const float rough = c3.w * mr.y;   // roughness factor x texture green
+    const float alpha = rough * rough;
     uint32_t bsdf = __float_as_uint(c1.w);
     if (bsdf == 1u && alpha < kMetalDeltaAlpha) bsdf = 3u;
     if ((flags & kFlagInside) && bsdf != 2u && dot(N, V) < 0.0f) N = neg(N);
@@ -309,7 +367,15 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
                 const float q = pdf_b / pdf_l;
                 const float w = (q == q) ? 1.0f / (1.0f + q * q) : 0.0f;
                 const float sc = (cos_x * w) / pdf_l;
-                const V3 ltle = xyz(lt.le);
+                V3 ltle = xyz(lt.le);
+                const uint32_t lt_tex = __float_as_uint(lt.le.w);
+                if (lt_tex != 0u) {
+                    // textured emitter: its emission texture at the sampled point
+                    const float lu = (lt.uv01.x + b1 * (lt.uv01.z - lt.uv01.x)) + b2 * (lt.uv2.x - lt.uv01.x);
+                    const float lv = (lt.uv01.y + b1 * (lt.uv01.w - lt.uv01.y)) + b2 * (lt.uv2.y - lt.uv01.y);
+                    const float4 t = tex_bilinear(SH.textures[lt_tex], lu, lv);
+                    ltle = mk(ltle.x * t.x, ltle.y * t.y, ltle.z * t.z);
+                }
                 o.contrib = mk(((T.x * f.x) * sc) * ltle.x, ((T.y * f.y) * sc) * ltle.y, ((T.z * f.z) * sc) * ltle.z);
                 o.spos = pos;
                 o.sdir = wl;
