@@ -395,6 +395,18 @@ def run_ours(args, rank, world, local):
     barrier(dist)
     t_max, rays_all, value = aggregate_weak(dist, gpu_ms, rays)
     spp_per_s = world * SPP * args.steps / (t_max / 1e3)
+    # --- megakernel A/B (use_wavefront_pathtracing = 0): the same frame, whole paths per thread
+    mega = None
+    if not args.no_megakernel:
+        mms = []
+        for i in range(3):
+            r.render(max_bounces=DEPTH, spp=SPP, frame_seed=frame_seed(i, rank), nee=1, rr_start_depth=RR,
+                     accumulate=False, megakernel=True)
+            mms.append(r.stats()["ms_total"])
+        m_ms = min(mms[1:])
+        mega = {"ms_per_frame": round(m_ms, 3), "spp_per_s": round(SPP / (m_ms / 1e3), 2),
+                "wavefront_ms_per_frame": round(t_max / args.steps, 3),
+                "wavefront_speedup": round(m_ms / (t_max / args.steps), 3)}
     # --- algorithmic bytes of the extend kernel (counted pass, same seeds, untimed)
     r.render(max_bounces=DEPTH, spp=SPP, frame_seed=1, nee=1, rr_start_depth=RR, accumulate=False,
              count_traffic=True)
@@ -468,6 +480,8 @@ def run_ours(args, rank, world, local):
             line["adjoint"] = adjoint
         if batched:
             line["batched"] = batched
+        if mega:
+            line["megakernel"] = mega
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -558,6 +572,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rendering leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes leg")
+    ap.add_argument("--no-megakernel", action="store_true", help="skip the megakernel A/B leg")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--workload", default="instanced", choices=["instanced", "traversal", "batched"])
     ap.add_argument("--soup-triangles", type=int, default=8_000_000)

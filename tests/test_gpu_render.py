@@ -121,3 +121,28 @@ def test_fp64_oracle_rmse(orc):
     tm = lambda x: x / (1.0 + x)
     rmse = float(np.sqrt(np.mean((tm(img[..., :3].astype(np.float64)) - tm(ref)) ** 2)))
     assert rmse <= 1e-3, rmse
+
+
+@pytest.mark.parametrize("name", ["box", "instanced_small"])
+def test_megakernel_equals_wavefront(orc, name):
+    """use_wavefront_pathtracing = 0 (pathtracer.hlsl): whole paths per thread,
+    the same traversal order and shading arithmetic, so the same image bit for
+    bit and the same number of rays."""
+    if name == "box":
+        desc = scenes.box_scene(width=48, height=40, max_bounces=4)
+        kw = dict(max_bounces=4, spp=3, nee=1, rr_start_depth=2)
+    else:
+        desc = scenes.instanced_scene(width=64, height=36, instances=48, freqs=(6, 9), spp=2, max_bounces=6)
+        kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=3)
+    with Renderer(desc.width, desc.height) as r:
+        load_scene_into(r, desc)
+        r.render(frame_seed=21, accumulate=False, **kw)
+        wave = r.read_image()
+        sw = r.stats()
+        r.render(frame_seed=21, accumulate=False, megakernel=True, **kw)
+        mega = r.read_image()
+        sm = r.stats()
+    assert wave[..., :3].mean() > 0.0
+    assert_images_equal(mega, wave)
+    assert sm["rays_extend"] == sw["rays_extend"] and sm["rays_connect"] == sw["rays_connect"]
+    assert sm["launches"] < sw["launches"]

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libwf.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["wf_api.cu", "wf_trace.cu", "wf_shade.cu", "wf_tlas.cu", "wf_bvh.cu", "wf_batch.cu"]
+SOURCES = ["wf_api.cu", "wf_trace.cu", "wf_shade.cu", "wf_tlas.cu", "wf_bvh.cu", "wf_batch.cu", "wf_mega.cu"]
 
 
 def nvcc():

@@ -981,7 +981,7 @@ struct Pass {
     SceneRefs S;
     ShadeRefs SH;
     RenderBuffers B;
-    bool nee, prof, cnt;
+    bool nee, prof, cnt, mega;
 };
 
 int validate_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o, const char* who) {
@@ -1035,6 +1035,7 @@ Pass make_pass(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     P.B.counters = c->counters;
     P.nee = W.nee && c->light_count > 0;
     P.prof = o->profile != 0;
+    P.mega = s->use_wavefront_pathtracing == 0;
     P.cnt = o->count_traffic != 0;
     return P;
 }
@@ -1049,6 +1050,22 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
     W.np = wv.np;
     W.npaths = wv.k * wv.np;
     WF_CUDA(cudaMemsetAsync(B.counts, 0, 4 * kMaxDepth * sizeof(uint32_t), c->stream));
+    if (P.mega) {
+        // pathtracer.hlsl: every bounce of a path in one thread
+        {
+            StageTimer t(c, P.prof, ST_EXTEND);
+            WF_CUDA(launch_megakernel(P.S, P.SH, B, W, B.counts + 2 * kMaxDepth, c->totals, c->stream));
+        }
+        c->launches++;
+        if (resolve) {
+            {
+                StageTimer t(c, P.prof, ST_POST);
+                WF_CUDA(launch_wave_resolve(B, W, c->stream));
+            }
+            c->launches++;
+        }
+        return WF_OK;
+    }
     {
         StageTimer t(c, P.prof, ST_GENERATE);
         WF_CUDA(launch_generate(B, W, c->stream));
@@ -1121,6 +1138,8 @@ int wf_adjoint(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     if (!dloss_dimage || !d_albedo || !d_emission) return fail(WF_ERR_INVALID, "wf_adjoint: null argument");
     if (s->render_view_mode != RENDER_VIEW_MODE_NONE)
         return fail(WF_ERR_INVALID, "wf_adjoint: differentiates the path-traced image (RENDER_VIEW_MODE_NONE)");
+    if (!s->use_wavefront_pathtracing)
+        return fail(WF_ERR_INVALID, "wf_adjoint: replays the wavefront stages (use_wavefront_pathtracing = 1)");
     if (!c->albedo_set) return fail(WF_ERR_STATE, "wf_adjoint: set the per-triangle albedo first (wf_scene_set_albedo)");
     if (o->nee || o->rr_start_depth <= s->max_bounces)
         return fail(WF_ERR_INVALID, "wf_adjoint: path replay needs nee = 0 and Russian roulette off");

@@ -93,6 +93,11 @@ cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const Wave
                          uint32_t max_rays, const AdjointRefs& A, cudaStream_t stream);
 cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
                            bool count, unsigned long long* total, cudaStream_t stream);
+// The megakernel (use_wavefront_pathtracing = 0): whole paths per thread, each
+// path's radiance left in ps_L like the wavefront stages; fetch = a device
+// counter (zeroed here), totals[0..1] += extension / shadow rays.
+cudaError_t launch_megakernel(const SceneRefs& S, const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W,
+                              uint32_t* fetch, unsigned long long* totals, cudaStream_t stream);
 // Adds each pixel's paths of the wave to the accumulator in sample order.
 cudaError_t launch_wave_resolve(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream);
 // post_process.hlsl:25-72 for a render view mode (tonemap only for mode 0,

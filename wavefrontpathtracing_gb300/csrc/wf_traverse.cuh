@@ -220,6 +220,113 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
     }
 }
 
+// One ray traced by one thread in nested TLAS / BLAS loops (the structure of
+// accelstruct.hlsl:58-218 as written), for the megakernel path.  It visits the
+// same nodes and triangles in the same order as trace_persistent and returns
+// the same hit; false when a stack overflowed (the hit is then a miss).
+template <bool ANY>
+__device__ __forceinline__ bool trace_single(const SceneRefs& S, uint32_t root, V3 wo, V3 wd, float tmax,
+                                             bool no_cull, Hit& h) {
+    h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
+    if (root == kInvalid) return true;
+    const V3 wi = rcp(wd);
+    float wt = tmax;
+    float4 n0 = ldg4(S.tnodes + 2ull * root), n1 = ldg4(S.tnodes + 2ull * root + 1);
+    if (slab(xyz(n0), xyz(n1), wo, wi, wt) == FLT_MAX) return true;
+    uint32_t t0 = __float_as_uint(n0.w), t1 = __float_as_uint(n1.w);
+    uint2 tstack[kStack];
+    int tsp = 0;
+    for (;;) {
+        if (t0 == 0u) {
+            // trace_ray_bvh_instance: the ray in object space, t shared
+            const uint32_t ii = t1;
+            const float4* ip = S.tinst + 4ull * ii;
+            const float4 c0 = ldg4(ip), c1 = ldg4(ip + 1), c2 = ldg4(ip + 2), c3 = ldg4(ip + 3);
+            const V3 co = xform(wo, 1.0f, c0, c1, c2, c3);
+            const V3 cd = xform(wd, 0.0f, c0, c1, c2, c3);
+            const V3 ci = rcp(cd);
+            float ct = wt;
+            const BlasRef B = S.blas[__float_as_uint(c0.w)];
+            const float4 r0 = ldg4(B.nodes), r1 = ldg4(B.nodes + 1);
+            uint32_t b0 = __float_as_uint(r0.w), b1 = __float_as_uint(r1.w);
+            uint2 bstack[kStack];
+            int bsp = 0;
+            bool hit_here = false;
+            for (;;) {
+                bool pop = false;
+                if (b1 > 0u) {
+                    for (uint32_t i = b0; i < b0 + b1; ++i) {
+                        const float4* tp = B.tris + 3ull * i;
+                        const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+                        float bu, bv;
+                        if (tri_hit(xyz(a), xyz(b), xyz(c), co, cd, ct, bu, bv, no_cull)) {
+                            h.prim = __float_as_uint(a.w);
+                            h.u = bu; h.v = bv;
+                            hit_here = true;
+                            if (ANY) { h.inst = ii; h.t = ct; return true; }
+                        }
+                    }
+                    pop = true;
+                } else {
+                    const float4* pa = B.nodes + 2ull * b0;
+                    const float4 a0 = ldg4(pa), a1 = ldg4(pa + 1), q0 = ldg4(pa + 2), q1 = ldg4(pa + 3);
+                    float dl = slab(xyz(a0), xyz(a1), co, ci, ct);
+                    float dr = slab(xyz(q0), xyz(q1), co, ci, ct);
+                    uint2 L = make_uint2(__float_as_uint(a0.w), __float_as_uint(a1.w));
+                    uint2 R = make_uint2(__float_as_uint(q0.w), __float_as_uint(q1.w));
+                    if (dl > dr) { float td = dl; dl = dr; dr = td; uint2 tn = L; L = R; R = tn; }
+                    if (dl == FLT_MAX) {
+                        pop = true;
+                    } else {
+                        b0 = L.x; b1 = L.y;
+                        if (dr != FLT_MAX) {
+                            if (bsp == kStack) {
+                                h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
+                                return false;
+                            }
+                            bstack[bsp++] = R;
+                        }
+                    }
+                }
+                if (pop) {
+                    if (bsp == 0) break;
+                    const uint2 e = bstack[--bsp];
+                    b0 = e.x; b1 = e.y;
+                }
+            }
+            wt = ct;
+            if (hit_here) { h.inst = ii; h.t = wt; }
+            if (tsp == 0) break;
+            const uint2 e = tstack[--tsp];
+            t0 = e.x; t1 = e.y;
+            continue;
+        }
+        const float4* pa = S.tnodes + 2ull * (t0 >> 16);
+        const float4* pb = S.tnodes + 2ull * (t0 & 0xFFFFu);
+        const float4 a0 = ldg4(pa), a1 = ldg4(pa + 1), q0 = ldg4(pb), q1 = ldg4(pb + 1);
+        float dl = slab(xyz(a0), xyz(a1), wo, wi, wt);
+        float dr = slab(xyz(q0), xyz(q1), wo, wi, wt);
+        uint2 L = make_uint2(__float_as_uint(a0.w), __float_as_uint(a1.w));
+        uint2 R = make_uint2(__float_as_uint(q0.w), __float_as_uint(q1.w));
+        if (dl > dr) { float td = dl; dl = dr; dr = td; uint2 tn = L; L = R; R = tn; }
+        if (dl == FLT_MAX) {
+            if (tsp == 0) break;
+            const uint2 e = tstack[--tsp];
+            t0 = e.x; t1 = e.y;
+        } else {
+            t0 = L.x; t1 = L.y;
+            if (dr != FLT_MAX) {
+                if (tsp == kStack) {
+                    h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
+                    return false;
+                }
+                tstack[tsp++] = R;
+            }
+        }
+    }
+    return true;
+}
+
 // Adds a thread's fetch counts to the global counters (one atomic per warp).
 __device__ __forceinline__ void flush_counters(const LocalCounters& c, Counters* g) {
     unsigned long long a = c.tlas_nodes, b = c.instances, x = c.blas_nodes, y = c.tris;
