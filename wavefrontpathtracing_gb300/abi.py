@@ -103,7 +103,7 @@ class BatchConfig(ctypes.Structure):
                 ("use_graph", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
 
     def as_dict(self):
-        return {"capacity": self.capacity, "regen_threshold": self.regen_threshold, "block": self.block,
+        return {"capacity": self.capacity, "regen_threshold": round(self.regen_threshold, 6), "block": self.block,
                 "use_graph": self.use_graph}
 
 

@@ -34,6 +34,21 @@ struct LocalCounters {
 };
 
 constexpr uint32_t kNoRay = 0xFFFFFFFFu;
+// Threads per block of the persistent traversal kernels.
+#ifndef WF_TRACE_BLOCK
+#define WF_TRACE_BLOCK 128
+#endif
+constexpr int kTraceBlock = WF_TRACE_BLOCK;
+// Traversal stack: one LIFO for both levels (the TLAS entries below, the
+// current instance's BLAS entries above them), 64 entries per level as the
+// reference.  Its top WF_TRACE_RING entries live in a shared-memory ring (slot
+// index % ring, one column per thread), the older ones in local memory; a
+// push into a full ring moves the ring's oldest entry to local memory, a pop
+// from an empty ring reads local memory.  WF_TRACE_RING 0 keeps the whole
+// stack in local memory.
+#ifndef WF_TRACE_RING
+#define WF_TRACE_RING 8
+#endif
 // A warp takes new rays once this many of its lanes are idle (or all are).
 #ifndef WF_TRACE_REFILL
 #define WF_TRACE_REFILL 12
@@ -64,21 +79,56 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                                                  LocalCounters& cnt, bool& overflow) {
     const unsigned FULL = 0xffffffffu;
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t col = threadIdx.x;
+    // State a step rarely touches lives in shared memory, one column per
+    // thread, to keep the loop's registers (and so the resident warps) up:
+    // the world ray (read back when the ray leaves an instance) and the hit
+    // record (written on a hit, read when the ray finishes).
+    __shared__ float4 s_wo[kTraceBlock], s_wd[kTraceBlock];
+    __shared__ uint32_t s_inst[kTraceBlock], s_prim[kTraceBlock];
+    __shared__ float s_t[kTraceBlock], s_u[kTraceBlock], s_v[kTraceBlock];
     uint32_t ri = kNoRay;
     bool exhausted = false;
-    V3 wo = mk(0, 0, 0), wd = mk(0, 0, 0);   // world ray
-    float wt = 0.0f;                          // world ray.t (closest hit so far)
-    V3 co = mk(0, 0, 0), cd = mk(0, 0, 0), ci = mk(0, 0, 0);  // current-space ray and 1/dir
-    float ct = 0.0f;                          // current-space ray.t
+    // current-space ray and 1/dir; ct = ray.t (the closest hit so far, shared
+    // by world and object space because instance rays are not renormalised)
+    V3 co = mk(0, 0, 0), cd = mk(0, 0, 0), ci = mk(0, 0, 0);
+    float ct = 0.0f;
     bool no_cull = false, hit_here = false;
     uint32_t level = 0, w0 = 0, w1 = 0, ii = 0;
     BlasRef B;
     B.nodes = nullptr; B.tris = nullptr;
-    Hit h;
-    h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
-    int tsp = 0, bsp = 0;
-    uint2 tstack[kStack];
-    uint2 bstack[kStack];
+    // stack: entries [0, sp); the TLAS level's are [0, tb) while inside an
+    // instance; [lo, sp) are in the ring, [0, lo) in local memory
+    int sp = 0, lo = 0, tb = 0;
+    uint2 deep[2 * kStack];
+#if WF_TRACE_RING > 0
+    __shared__ uint2 ring[WF_TRACE_RING][kTraceBlock];
+    auto stack_push = [&](uint2 e) {
+        if (sp - lo == WF_TRACE_RING) {
+            deep[lo] = ring[lo % WF_TRACE_RING][col];
+            lo++;
+        }
+        ring[sp % WF_TRACE_RING][col] = e;
+        sp++;
+    };
+    auto stack_pop = [&]() -> uint2 {
+        sp--;
+        if (sp >= lo) return ring[sp % WF_TRACE_RING][col];
+        lo = sp;
+        return deep[sp];
+    };
+#else
+    auto stack_push = [&](uint2 e) { deep[sp++] = e; };
+    auto stack_pop = [&]() -> uint2 { return deep[--sp]; };
+#endif
+    auto hit_record = [&]() {
+        Hit h;
+        h.inst = s_inst[col]; h.prim = s_prim[col]; h.t = s_t[col]; h.u = s_u[col]; h.v = s_v[col];
+        return h;
+    };
+    auto clear_hit = [&]() {
+        s_inst[col] = kInvalid; s_prim[col] = kInvalid; s_t[col] = FLT_MAX; s_u[col] = 0.0f; s_v[col] = 0.0f;
+    };
 
     for (;;) {
         // ---- refill idle lanes (one atomic per warp)
@@ -95,18 +145,20 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                     const uint32_t k = base + (uint32_t)__popc(want & ((1u << lane) - 1u));
                     if (k < n) {
                         ri = k;
-                        io.load(k, wo, wd, wt, no_cull);
-                        h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
-                        co = wo; cd = wd; ci = rcp(wd); ct = wt;
+                        io.load(k, co, cd, ct, no_cull);
+                        s_wo[col] = make_float4(co.x, co.y, co.z, 0.0f);
+                        s_wd[col] = make_float4(cd.x, cd.y, cd.z, 0.0f);
+                        clear_hit();
+                        ci = rcp(cd);
                         const uint32_t root = io.root(k, S);
                         bool miss = root == kInvalid;
                         if (!miss) {
                             const float4 n0 = ldg4(S.tnodes + 2ull * root), n1 = ldg4(S.tnodes + 2ull * root + 1);
                             if (COUNT) cnt.tlas_nodes++;
                             miss = slab(xyz(n0), xyz(n1), co, ci, ct) == FLT_MAX;
-                            level = 0; w0 = __float_as_uint(n0.w); w1 = __float_as_uint(n1.w); tsp = 0;
+                            level = 0; w0 = __float_as_uint(n0.w); w1 = __float_as_uint(n1.w); sp = 0; lo = 0;
                         }
-                        if (miss) { io.store(k, h, true); ri = kNoRay; }
+                        if (miss) { io.store(k, hit_record(), true); ri = kNoRay; }
                     } else {
                         exhausted = true;
                     }
@@ -124,21 +176,21 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
         bool finish = false, ok = true;
         bool pop = false;
         if (level == 0u && w0 == 0u) {
-            // TLAS leaf: enter the instance (trace_ray_bvh_instance)
+            // TLAS leaf: enter the instance (trace_ray_bvh_instance); at level
+            // 0 the current ray is the world ray
             ii = w1;
             const float4* ip = S.tinst + 4ull * ii;
             const float4 c0 = ldg4(ip), c1 = ldg4(ip + 1), c2 = ldg4(ip + 2), c3 = ldg4(ip + 3);
             if (COUNT) cnt.instances++;
-            co = xform(wo, 1.0f, c0, c1, c2, c3);
-            cd = xform(wd, 0.0f, c0, c1, c2, c3);
+            co = xform(co, 1.0f, c0, c1, c2, c3);
+            cd = xform(cd, 0.0f, c0, c1, c2, c3);
             ci = rcp(cd);
-            ct = wt;
             B = S.blas[__float_as_uint(c0.w)];
             const float4 r0 = ldg4(B.nodes), r1 = ldg4(B.nodes + 1);
             if (COUNT) cnt.blas_nodes++;
             w0 = __float_as_uint(r0.w);
             w1 = __float_as_uint(r1.w);
-            level = 1; bsp = 0; hit_here = false;
+            level = 1; tb = sp; hit_here = false;
         } else if (level == 1u && w1 > 0u) {
             // BLAS leaf: its triangles in index-list order
             for (uint32_t i = w0; i < w0 + w1; ++i) {
@@ -147,10 +199,10 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                 if (COUNT) cnt.tris++;
                 float bu, bv;
                 if (tri_hit(xyz(a), xyz(b), xyz(c), co, cd, ct, bu, bv, no_cull)) {
-                    h.prim = __float_as_uint(a.w);
-                    h.u = bu; h.v = bv;
+                    s_prim[col] = __float_as_uint(a.w);
+                    s_u[col] = bu; s_v[col] = bv;
                     hit_here = true;
-                    if (ANY) { h.inst = ii; h.t = ct; finish = true; break; }
+                    if (ANY) { s_inst[col] = ii; s_t[col] = ct; finish = true; break; }
                 }
             }
             pop = !finish;
@@ -180,33 +232,31 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
             } else {
                 w0 = L.x; w1 = L.y;
                 if (dr != FLT_MAX) {
-                    int& sp = level == 0u ? tsp : bsp;
-                    if (sp == kStack) {
-                        h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
+                    if ((level == 0u ? sp : sp - tb) == kStack) {
+                        clear_hit();
                         finish = true; ok = false; overflow = true;
                     } else {
-                        if (level == 0u) tstack[tsp++] = R; else bstack[bsp++] = R;
+                        stack_push(R);
                     }
                 }
             }
         }
         if (pop) {
             if (level == 1u) {
-                if (bsp > 0) {
-                    const uint2 e = bstack[--bsp];
+                if (sp > tb) {
+                    const uint2 e = stack_pop();
                     w0 = e.x; w1 = e.y;
                     pop = false;
                 } else {
                     // leave the instance: ray.t = ray_local.t (accelstruct.hlsl:146, 170-174)
-                    wt = ct;
-                    if (hit_here) { h.inst = ii; h.t = wt; }
+                    if (hit_here) { s_inst[col] = ii; s_t[col] = ct; }
                     level = 0;
-                    co = wo; cd = wd; ci = rcp(wd); ct = wt;
+                    co = xyz(s_wo[col]); cd = xyz(s_wd[col]); ci = rcp(cd);
                 }
             }
             if (pop) {
-                if (tsp > 0) {
-                    const uint2 e = tstack[--tsp];
+                if (sp > 0) {
+                    const uint2 e = stack_pop();
                     w0 = e.x; w1 = e.y;
                 } else {
                     finish = true;
@@ -214,7 +264,7 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
             }
         }
         if (finish) {
-            io.store(ri, h, ok);
+            io.store(ri, hit_record(), ok);
             ri = kNoRay;
         }
     }
@@ -344,14 +394,13 @@ __device__ __forceinline__ void flush_counters(const LocalCounters& c, Counters*
     }
 }
 
-#ifndef WF_TRACE_BLOCK
-#define WF_TRACE_BLOCK 128
-#endif
-constexpr int kTraceBlock = WF_TRACE_BLOCK;
 // Minimum resident blocks per SM asked of the compiler for the traversal
-// kernels (it caps their registers at 65536 / (128 * blocks)).
+// kernels (it caps their registers at 65536 / (128 * blocks)): 9 blocks = 56
+// registers, 36 warps per SM, for a few bytes of spills in the closest-hit
+// kernel (measured fastest against 7-8 blocks without spills and 10 blocks
+// with 50+ bytes of spills).
 #ifndef WF_TRACE_MIN_BLOCKS
-#define WF_TRACE_MIN_BLOCKS 1
+#define WF_TRACE_MIN_BLOCKS 9
 #endif
 int sm_count();
 
