@@ -48,8 +48,10 @@ typedef struct wf_init_params {
     uint32_t vsync;             /* accepted for source compatibility; unused */
     int32_t  device;            /* CUDA device ordinal */
     uint32_t wave_capacity;     /* max paths in flight per wave; 0 = min(16 * width * height, 2^25) */
-    uint32_t tlas_metric;       /* TLAS pairing metric: 0 = the reference's (tlas_builder.cpp:96-97,
-                                   bit-exact), 1 = half area of the merged box (better trees) */
+    uint32_t tlas_metric;       /* TLAS build: 0 = the reference's agglomerative walk and pairing metric
+                                   (tlas_builder.cpp:96-97, bit-exact), 1 = the same walk pairing by the
+                                   half area of the merged box (better trees), 2 = parallel
+                                   locally-ordered clustering on the merged-box area (fast rebuilds) */
     uint32_t reserved[1];
 } wf_init_params;
 
@@ -174,6 +176,10 @@ int wf_instance_submit(wf_ctx* ctx, uint32_t mesh, const float local_to_world[16
 /* Same with a chosen scattering model (metal, dielectric). */
 int wf_instance_submit_ex(wf_ctx* ctx, uint32_t mesh, const float local_to_world[16],
                           const wf_material_ext* material);
+/* count wf_instance_submit_ex calls in one: meshes[i], local_to_world[16 i ..
+ * 16 i + 15], materials[i]; all are submitted or none (on an error). */
+int wf_instance_submit_many(wf_ctx* ctx, uint32_t count, const uint32_t* meshes, const float* local_to_world,
+                            const wf_material_ext* materials);
 /* Uploads instances, builds the TLAS on the GPU (renderer.cpp:637-669 builds
  * it on the CPU every frame) and the emitter table used by next-event estimation. */
 int wf_scene_end(wf_ctx* ctx);
@@ -307,7 +313,8 @@ int wf_tlas_build(wf_ctx* ctx, const bvh_instance_t* instances, uint32_t instanc
  * allocation's implicit device synchronisation.  The caller owns both device
  * buffers: device_aabbs = instance_count x {min xyz, max xyz} floats,
  * device_nodes = 2 * instance_count tlas_node_t (one when instance_count is 0);
- * the result equals the nodes wf_tlas_build writes with the same tlas_metric.
+ * the result equals the nodes wf_tlas_build writes with the same tlas_metric (0 or 1;
+ * metric 2 needs a larger working set and is not offered here).
  * The build's working list lives in a static 224 KiB device array, so:
  *   - at most 8192 instances (larger counts return WF_ERR_CAPACITY);
  *   - every call on a device shares that array: calls that overlap on the GPU

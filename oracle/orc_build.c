@@ -254,13 +254,131 @@ static uint32_t best_match(const tlas_node_t* nodes, uint32_t A, const uint32_t*
     return best;
 }
 
+/* ---- TLAS metric 2: parallel locally-ordered clustering ---------------------
+ * (Meister and Bittner, "Parallel Locally-Ordered Clustering for Bounding
+ * Volume Hierarchy Construction", 2018), the GPU library's fast TLAS build.
+ * Instances are ordered by the 30-bit Morton code of their box centres (ties
+ * by instance index).  Each round every cluster picks the cluster within
+ * PLOC_RADIUS list positions whose merged box has the smallest half area
+ * (ties to the lower position); mutual pairs merge into a new node (numbered
+ * in list order, left child = the lower position), and the list is compacted
+ * in order.  Leaves are nodes 1..n (instance order), the root is copied to 0. */
+#define PLOC_RADIUS 16
+
+static uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    uint32_t code = 0;
+    for (int b = 0; b < 10; ++b) {
+        code |= ((x >> b) & 1u) << (3 * b + 2);
+        code |= ((y >> b) & 1u) << (3 * b + 1);
+        code |= ((z >> b) & 1u) << (3 * b);
+    }
+    return code;
+}
+
+static uint32_t quantize10(float c, float lo, float ext) {
+    float q = (ext > 0.0f) ? (c - lo) / ext : 0.0f;
+    if (!(q >= 0.0f)) q = 0.0f;
+    if (q > 1.0f) q = 1.0f;
+    return (uint32_t)(q * 1023.0f);
+}
+
+static int cmp_u64(const void* a, const void* b) {
+    uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return (x > y) - (x < y);
+}
+
+static float merged_half_area(const float* amn, const float* amx, const float* bmn, const float* bmx) {
+    float lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) { lo[a] = gmin(amn[a], bmn[a]); hi[a] = gmax(amx[a], bmx[a]); }
+    return half_area(lo, hi);
+}
+
+static void tlas_ploc(const bvh_instance_t* inst, uint32_t n, tlas_node_t* nodes) {
+    for (uint32_t i = 0; i < n; ++i) {
+        memcpy(nodes[1 + i].aabb_min, inst[i].aabb_min, 12);
+        memcpy(nodes[1 + i].aabb_max, inst[i].aabb_max, 12);
+        nodes[1 + i].instance_idx = i;
+        nodes[1 + i].left_right = 0;
+    }
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            float c = (inst[i].aabb_min[a] + inst[i].aabb_max[a]) * 0.5f;
+            lo[a] = gmin(lo[a], c);
+            hi[a] = gmax(hi[a], c);
+        }
+    float ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    uint64_t* key = (uint64_t*)malloc(sizeof(uint64_t) * n);
+    for (uint32_t i = 0; i < n; ++i) {
+        float c[3];
+        for (int a = 0; a < 3; ++a) c[a] = (inst[i].aabb_min[a] + inst[i].aabb_max[a]) * 0.5f;
+        uint32_t code = morton3(quantize10(c[0], lo[0], ext[0]), quantize10(c[1], lo[1], ext[1]),
+                                quantize10(c[2], lo[2], ext[2]));
+        key[i] = ((uint64_t)code << 32) | i;
+    }
+    qsort(key, n, sizeof(uint64_t), cmp_u64);
+    uint32_t* cl = (uint32_t*)malloc(sizeof(uint32_t) * n * 2);
+    uint32_t* nn = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    uint32_t* ncl = cl + n;
+    for (uint32_t k = 0; k < n; ++k) cl[k] = 1 + (uint32_t)(key[k] & 0xFFFFFFFFu);
+    uint32_t count = n, next = n + 1;
+    while (count > 1) {
+        for (uint32_t k = 0; k < count; ++k) {
+            const tlas_node_t* a = &nodes[cl[k]];
+            uint32_t j0 = k > PLOC_RADIUS ? k - PLOC_RADIUS : 0;
+            uint32_t j1 = k + PLOC_RADIUS < count - 1 ? k + PLOC_RADIUS : count - 1;
+            float best = FLT_MAX;
+            uint32_t bj = (k == 0) ? 1 : k - 1;
+            for (uint32_t j = j0; j <= j1; ++j) {
+                if (j == k) continue;
+                const tlas_node_t* b = &nodes[cl[j]];
+                float d = merged_half_area(a->aabb_min, a->aabb_max, b->aabb_min, b->aabb_max);
+                if (d < best) { best = d; bj = j; }
+            }
+            nn[k] = bj;
+        }
+        uint32_t merges = 0, pos = 0;
+        for (uint32_t k = 0; k < count; ++k) merges += (nn[nn[k]] == k && k < nn[k]) ? 1u : 0u;
+        int forced = merges == 0;
+        if (forced) { nn[0] = 1; nn[1] = 0; merges = 1; }
+        uint32_t made = 0;
+        for (uint32_t k = 0; k < count; ++k) {
+            uint32_t m = nn[k];
+            int mutual = nn[m] == k;
+            if (mutual && k > m) continue;   /* merged into the lower position */
+            if (mutual) {
+                uint32_t id = next + made++;
+                tlas_node_t* t = &nodes[id];
+                const tlas_node_t* a = &nodes[cl[k]];
+                const tlas_node_t* b = &nodes[cl[m]];
+                for (int ax = 0; ax < 3; ++ax) {
+                    t->aabb_min[ax] = gmin(a->aabb_min[ax], b->aabb_min[ax]);
+                    t->aabb_max[ax] = gmax(a->aabb_max[ax], b->aabb_max[ax]);
+                }
+                t->left_right = (cl[k] << 16) | cl[m];
+                t->instance_idx = 0;
+                ncl[pos++] = id;
+            } else {
+                ncl[pos++] = cl[k];
+            }
+        }
+        memcpy(cl, ncl, sizeof(uint32_t) * pos);
+        count = pos;
+        next += made;
+    }
+    if (n > 0) nodes[0] = nodes[cl[0]];
+    free(key);
+    free(cl);
+    free(nn);
+}
+
 /* tlas_builder_t::build + extract (tlas_builder.cpp:6-84).  The reference's
  * working list is a 256-entry stack array (:14); this one is sized to n.
  * metric 0 is the reference's pairing metric; metric 1 replaces it by the
  * half area of the merged box (same walk, same tie rule). */
 int orc_tlas_build_metric(const bvh_instance_t* inst, uint32_t n, uint32_t metric, uint8_t** out_blob,
                           uint64_t* out_size) {
-    if (!out_blob || !out_size || (n > 0 && !inst) || n > 32768) return -1;
+    if (!out_blob || !out_size || (n > 0 && !inst) || n > 32768 || metric > 2) return -1;
     uint32_t ncount = n * 2;
     tlas_node_t* nodes = (tlas_node_t*)calloc(ncount ? ncount : 1, sizeof(tlas_node_t));
     uint32_t* idx = (uint32_t*)calloc(n ? n : 1, sizeof(uint32_t));
@@ -273,7 +391,10 @@ int orc_tlas_build_metric(const bvh_instance_t* inst, uint32_t n, uint32_t metri
         nodes[at].left_right = 0;
         at++;
     }
-    if (n > 0) {
+    if (metric == 2) {
+        tlas_ploc(inst, n, nodes);
+        at = n ? 2 * n : 1;
+    } else if (n > 0) {
         uint32_t A = 0;
         uint32_t B = best_match(nodes, A, idx, remaining, metric);
         while (remaining > 1) {

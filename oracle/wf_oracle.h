@@ -38,7 +38,8 @@ int orc_bvh_build(const triangle_t* tris, uint32_t n, uint32_t interval_count,
                   uint8_t** out_blob, uint64_t* out_size);
 /* Writes a malloc'ed blob [tlas_header_t | nodes | bvh_instance_t]. */
 int orc_tlas_build(const bvh_instance_t* inst, uint32_t n, uint8_t** out_blob, uint64_t* out_size);
-/* metric 0: the reference's; 1: half area of the merged box (an added option). */
+/* metric 0: the reference's; 1: half area of the merged box (an added option); 2: parallel
+ * locally-ordered clustering (the GPU library's fast build, an added option). */
 int orc_tlas_build_metric(const bvh_instance_t* inst, uint32_t n, uint32_t metric, uint8_t** out_blob,
                           uint64_t* out_size);
 void orc_free(void* p);

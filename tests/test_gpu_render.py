@@ -146,3 +146,25 @@ def test_megakernel_equals_wavefront(orc, name):
     assert_images_equal(mega, wave)
     assert sm["rays_extend"] == sw["rays_extend"] and sm["rays_connect"] == sw["rays_connect"]
     assert sm["launches"] < sw["launches"]
+
+
+def test_submit_many_equals_one_by_one(orc):
+    desc = scenes.instanced_scene(width=48, height=32, instances=40, freqs=(5, 7), spp=1, max_bounces=4)
+    imgs, insts = [], []
+    for many in (False, True):
+        with Renderer(desc.width, desc.height, tlas_metric=1) as r:
+            ids = [r.create_mesh_from_triangles(t, interval_count=16, max_leaf_prims=4) for t in desc.meshes]
+            r.begin_scene(desc.view, desc.settings["env"])
+            if many:
+                r.submit_render_meshes([ids[m] for m, _, _ in desc.instances],
+                                       np.stack([np.asarray(t, np.float32) for _, t, _ in desc.instances]),
+                                       np.array([m for _, _, m in desc.instances]))
+            else:
+                for m, t, mat in desc.instances:
+                    r.submit_render_mesh(ids[m], t, mat)
+            r.end_scene()
+            insts.append(r.scene_instances())
+            r.render(max_bounces=4, spp=2, frame_seed=3, nee=1, rr_start_depth=2, accumulate=False)
+            imgs.append(r.read_image())
+    assert insts[0].tobytes() == insts[1].tobytes()
+    assert_images_equal(imgs[1], imgs[0])

@@ -107,3 +107,51 @@ def test_tlas_matches_reference_random(orc, n):
         inst["aabb_min"][1] = inst["aabb_min"][0]
         inst["aabb_max"][1] = inst["aabb_max"][0]
     assert np.array_equal(orc.tlas_build(inst), orc.ref_tlas_build(inst))
+
+
+def _tlas_nodes(blob):
+    hdr = blob[:8].view(np.uint32)
+    n_nodes = (int(hdr[1]) - int(hdr[0])) // 32
+    raw = blob[int(hdr[0]):int(hdr[0]) + 32 * n_nodes]
+    f = raw.view(np.float32).reshape(-1, 8)
+    u = raw.view(np.uint32).reshape(-1, 8)
+    return f[:, 0:3], f[:, 4:7], u[:, 3], u[:, 7]
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 1000, 5000])
+def test_tlas_ploc_is_a_valid_tree(orc, n):
+    """tlas_metric 2 (parallel locally-ordered clustering): leaves 1..n in
+    instance order, every instance reached exactly once from the root, every
+    box the union of its children's."""
+    rng = np.random.default_rng(n)
+    inst = np.zeros(n, dtype=bvh_instance_dtype)
+    c = rng.random((n, 3)) * 100
+    inst["aabb_min"] = (c - rng.random((n, 3))).astype(np.float32)
+    inst["aabb_max"] = (c + rng.random((n, 3))).astype(np.float32)
+    if n > 3:
+        inst[3] = inst[2]                      # a duplicate box
+    blob = orc.tlas_build(inst, metric=2)
+    mn, mx, lr, ii = _tlas_nodes(blob)
+    assert len(mn) == 2 * n
+    for i in range(n):
+        assert lr[1 + i] == 0 and ii[1 + i] == i
+    seen = []
+    stack = [0]
+    while stack:
+        k = stack.pop()
+        if lr[k] == 0:
+            seen.append(int(ii[k]))
+            continue
+        a, b = int(lr[k]) >> 16, int(lr[k]) & 0xFFFF
+        assert np.array_equal(mn[k], np.minimum(mn[a], mn[b])) and np.array_equal(mx[k], np.maximum(mx[a], mx[b]))
+        stack += [a, b]
+    assert sorted(seen) == list(range(n))
+
+
+def test_tlas_ploc_all_centres_equal(orc):
+    n = 300
+    inst = np.zeros(n, dtype=bvh_instance_dtype)
+    inst["aabb_min"] = -1.0
+    inst["aabb_max"] = 1.0
+    mn, mx, lr, ii = _tlas_nodes(orc.tlas_build(inst, metric=2))
+    assert len(mn) == 2 * n and lr[0] != 0

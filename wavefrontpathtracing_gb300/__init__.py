@@ -49,6 +49,7 @@ SIGNATURES = {
     "wf_scene_begin": [_vp, _vp, _vp],
     "wf_instance_submit": [_vp, _u32, _vp, _vp],
     "wf_instance_submit_ex": [_vp, _u32, _vp, _vp],
+    "wf_instance_submit_many": [_vp, _u32, _vp, _vp, _vp],
     "wf_scene_end": [_vp],
     "wf_scene_get_instances": [_vp, _vp, _u32, _pu32],
     "wf_scene_get_tlas": [_vp, _vp, _pu64],
@@ -222,6 +223,18 @@ class Renderer:
         else:
             rec = np.array([material], dtype=material_ext_dtype)
             check(self.L.wf_instance_submit_ex(self.h, mesh, ptr(m), ptr(rec)))
+
+    def submit_render_meshes(self, meshes, transforms, materials):
+        """Many instances in one call: meshes (n,), transforms (n, 4, 4) or (n, 16)
+        glm column-major, materials (n,) material_ext_dtype records."""
+        meshes = np.ascontiguousarray(meshes, dtype=np.uint32)
+        t = np.asarray(transforms, dtype=np.float32)
+        if t.ndim == 3:
+            t = np.ascontiguousarray(np.transpose(t, (0, 2, 1))).reshape(len(t), 16)   # column-major
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        mats = np.ascontiguousarray(materials, dtype=material_ext_dtype)
+        assert len(meshes) == len(t) == len(mats)
+        check(self.L.wf_instance_submit_many(self.h, len(meshes), ptr(meshes), ptr(t), ptr(mats)))
 
     def end_scene(self):
         check(self.L.wf_scene_end(self.h))

@@ -623,9 +623,9 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
     c->device = p->device;
     c->width = p->render_width;
     c->height = p->render_height;
-    if (p->tlas_metric > 1) {
+    if (p->tlas_metric > 2) {
         delete c;
-        return fail(WF_ERR_INVALID, "wf_create: tlas_metric must be 0 or 1");
+        return fail(WF_ERR_INVALID, "wf_create: tlas_metric must be 0, 1 or 2");
     }
     c->tlas_metric = p->tlas_metric;
     const uint64_t npix = (uint64_t)c->width * c->height;
@@ -856,6 +856,27 @@ int wf_instance_submit_ex(wf_ctx* c, uint32_t mesh, const float l2w[16], const w
     return submit(c, mesh, l2w, &mat->base, mat->bsdf, mat->ior);
 }
 
+int wf_instance_submit_many(wf_ctx* c, uint32_t count, const uint32_t* meshes, const float* l2w,
+                            const wf_material_ext* mats) {
+    if (!c || (count && (!meshes || !l2w || !mats))) return fail(WF_ERR_INVALID, "wf_instance_submit_many: null argument");
+    if (!c->in_scene) return fail(WF_ERR_STATE, "wf_instance_submit_many: outside wf_scene_begin/wf_scene_end");
+    if (c->instances.size() + count > 32768)
+        return fail(WF_ERR_CAPACITY, "wf_instance_submit_many: more than 32768 instances");
+    const size_t first = c->instances.size();
+    c->instances.reserve(first + count);
+    for (uint32_t i = 0; i < count; ++i) {
+        Instance in{};
+        int rc = make_instance(c, meshes[i], l2w + 16ull * i, &mats[i].base, mats[i].bsdf, mats[i].ior,
+                               "wf_instance_submit_many", &in);
+        if (rc) {
+            c->instances.resize(first);   // all or nothing
+            return rc;
+        }
+        c->instances.push_back(in);
+    }
+    return WF_OK;
+}
+
 int wf_scene_end(wf_ctx* c) {
     if (!c) return fail(WF_ERR_INVALID, "wf_scene_end: null context");
     if (!c->in_scene) return fail(WF_ERR_STATE, "wf_scene_end: no wf_scene_begin");
@@ -889,7 +910,7 @@ int wf_scene_end(wf_ctx* c) {
     }
     if ((rc = c->tnodes.reserve(2ull * std::max<uint32_t>(2 * n, 1))) || (rc = c->tinst.reserve(ti.size())) ||
         (rc = c->sinst.reserve(si.size())) || (rc = c->aabbs.reserve(aabbs.size())) ||
-        (rc = c->tlas_scratch.reserve(7ull * n + 1)))
+        (rc = c->tlas_scratch.reserve(tlas_scratch_words(n, c->tlas_metric))))
         return rc;
     WF_CUDA(cudaMemsetAsync(c->tnodes.p, 0, 32, c->stream));
     if (n) {
@@ -1363,7 +1384,7 @@ int wf_tlas_build(wf_ctx* c, const bvh_instance_t* inst, uint32_t n, void* out, 
     float4* d_nodes = nullptr;
     uint32_t* d_scratch = nullptr;
     if ((rc = dev_alloc(&d_aabbs, aabbs.size())) || (rc = dev_alloc(&d_nodes, 2 * nodes)) ||
-        (rc = dev_alloc(&d_scratch, 7ull * n + 1))) {
+        (rc = dev_alloc(&d_scratch, tlas_scratch_words(n, c->tlas_metric)))) {
         dev_free(d_aabbs); dev_free(d_nodes); dev_free(d_scratch);
         return rc;
     }

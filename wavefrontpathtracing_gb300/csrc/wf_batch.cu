@@ -520,7 +520,7 @@ int build_tables(wf_batch* b) {
     }
     if ((rc = b->tnodes.reserve(4ull * std::max<uint32_t>(ni, 1))) || (rc = b->tinst.reserve(ti.size())) ||
         (rc = b->sinst.reserve(si.size())) || (rc = b->aabbs.reserve(ab.size())) ||
-        (rc = b->tlas_scratch.reserve(7ull * ni + 1)) || (rc = b->lights.reserve(lt.size())) ||
+        (rc = b->tlas_scratch.reserve(tlas_scratch_words(ni, ctx_tlas_metric(c)))) || (rc = b->lights.reserve(lt.size())) ||
         (rc = b->d_roots.reserve(ns)) || (rc = b->d_pbase.reserve(ns + 1)) || (rc = b->d_pixbase.reserve(ns + 1)) ||
         (rc = b->d_scenes.reserve(ns)) || (rc = b->out_L.reserve(b->total_paths)) ||
         (rc = b->image.reserve(b->total_pixels)))

@@ -106,7 +106,10 @@ cudaError_t launch_post(const float4* accum, uint32_t npix, uint32_t view_mode, 
 cudaError_t launch_resolve(const float4* accum, uint32_t npix, float4* out, cudaStream_t stream);
 
 // TLAS: builds nodes [0, 2n) from per-instance world AABBs (tlas_builder.cpp).
-// metric 0 = the reference's pairing metric, 1 = merged-box half area.
+// metric 0 = the reference's pairing metric, 1 = merged-box half area (both the
+// reference's agglomerative walk), 2 = parallel locally-ordered clustering.
+// scratch: tlas_scratch_words(n, metric) words.
+size_t tlas_scratch_words(uint32_t n, uint32_t metric);
 cudaError_t launch_tlas_build(const float* aabbs /* 6 floats per instance */, uint32_t n, float4* nodes,
                               uint32_t* scratch, uint32_t metric, cudaStream_t stream);
 

@@ -124,9 +124,235 @@ __global__ void __launch_bounds__(32) k_tlas_build(const float* __restrict__ aab
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// metric 2: parallel locally-ordered clustering (Meister and Bittner 2018).
+// One block of 1024 threads: Morton order of the box centres by a bitonic sort,
+// then rounds of nearest-neighbour search within kPlocRadius list positions
+// (smallest merged half area, ties to the lower position), merging of mutual
+// pairs (new nodes numbered in list order by a block scan) and in-order
+// compaction.  Identical, node for node, to the oracle's tlas_ploc.
+namespace {
+
+constexpr uint32_t kPlocThreads = 1024;
+constexpr uint32_t kPlocRadius = 16;
+
+__device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    uint32_t code = 0;
+    for (int b = 0; b < 10; ++b) {
+        code |= ((x >> b) & 1u) << (3 * b + 2);
+        code |= ((y >> b) & 1u) << (3 * b + 1);
+        code |= ((z >> b) & 1u) << (3 * b);
+    }
+    return code;
+}
+__device__ __forceinline__ uint32_t quantize10(float c, float lo, float ext) {
+    float q = (ext > 0.0f) ? (c - lo) / ext : 0.0f;
+    if (!(q >= 0.0f)) q = 0.0f;
+    if (q > 1.0f) q = 1.0f;
+    return (uint32_t)(q * 1023.0f);
+}
+
+struct PlocScratch {
+    unsigned long long* key;   // P (power of two >= n)
+    uint32_t* cl[2];           // node id per list position
+    uint32_t* nn;              // nearest neighbour per position
+    uint32_t* flag;            // per position: 1 = creates a node
+    uint32_t* keep;            // per position: 1 = stays in the list
+};
+
+__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xffffffffu, x, off);
+        if ((int)lane >= off) x += o;
+    }
+    return x;
+}
+
+// Exclusive scan of v[0, count) in place by the whole block (each thread a
+// contiguous chunk); returns the total.  s_wt: 33 words of shared memory.
+__device__ uint32_t block_scan(uint32_t* v, uint32_t count, uint32_t* s_wt) {
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    const uint32_t per = (count + kPlocThreads - 1) / kPlocThreads;
+    const uint32_t b = t * per, e = min(count, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; ++i) sum += v[i];
+    const uint32_t incl = warp_inclusive_scan(sum);
+    if (lane == 31u) s_wt[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t y = s_wt[lane];
+        const uint32_t iw = warp_inclusive_scan(y);
+        s_wt[lane] = iw - y;
+        if (lane == 31u) s_wt[32] = iw;
+    }
+    __syncthreads();
+    uint32_t run = (incl - sum) + s_wt[warp];
+    for (uint32_t i = b; i < e; ++i) { const uint32_t x = v[i]; v[i] = run; run += x; }
+    const uint32_t total = s_wt[32];
+    __syncthreads();
+    return total;
+}
+
+__global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restrict__ aabbs, uint32_t n,
+                                                            float4* nodes, PlocScratch S, uint32_t P) {
+    __shared__ uint32_t s_part[33];
+    __shared__ float s_red[6][32];
+    const uint32_t t = threadIdx.x;
+    // leaves and the centre bounds
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t i = t; i < n; i += kPlocThreads) {
+        const float* b = aabbs + 6ull * i;
+        nodes[2 * (1 + i)] = make_float4(b[0], b[1], b[2], __uint_as_float(0u));
+        nodes[2 * (1 + i) + 1] = make_float4(b[3], b[4], b[5], __uint_as_float(i));
+        for (int a = 0; a < 3; ++a) {
+            const float c = (b[a] + b[3 + a]) * 0.5f;
+            lo[a] = gmin(lo[a], c);
+            hi[a] = gmax(hi[a], c);
+        }
+    }
+    // gmin / gmax are order-insensitive for the finite centres here: the
+    // result is the smallest / largest value, whichever order combines them
+    for (int a = 0; a < 3; ++a)
+        for (int off = 16; off > 0; off >>= 1) {
+            lo[a] = gmin(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], off));
+            hi[a] = gmax(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], off));
+        }
+    if ((t & 31u) == 0)
+        for (int a = 0; a < 3; ++a) { s_red[a][t >> 5] = lo[a]; s_red[3 + a][t >> 5] = hi[a]; }
+    __syncthreads();
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = s_red[a][0];
+        hi[a] = s_red[3 + a][0];
+        for (int w = 1; w < 32; ++w) { lo[a] = gmin(lo[a], s_red[a][w]); hi[a] = gmax(hi[a], s_red[3 + a][w]); }
+    }
+    const float ext0 = hi[0] - lo[0], ext1 = hi[1] - lo[1], ext2 = hi[2] - lo[2];
+    for (uint32_t i = t; i < P; i += kPlocThreads) {
+        if (i < n) {
+            const float* b = aabbs + 6ull * i;
+            const uint32_t code = morton3(quantize10((b[0] + b[3]) * 0.5f, lo[0], ext0),
+                                          quantize10((b[1] + b[4]) * 0.5f, lo[1], ext1),
+                                          quantize10((b[2] + b[5]) * 0.5f, lo[2], ext2));
+            S.key[i] = ((unsigned long long)code << 32) | i;
+        } else {
+            S.key[i] = ~0ull;
+        }
+    }
+    __syncthreads();
+    // bitonic sort of the P keys, ascending
+    for (uint32_t size = 2; size <= P; size <<= 1)
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t i = t; i < P; i += kPlocThreads) {
+                const uint32_t j = i ^ stride;
+                if (j > i) {
+                    const unsigned long long x = S.key[i], y = S.key[j];
+                    const bool up = (i & size) == 0;
+                    if (up ? (x > y) : (x < y)) { S.key[i] = y; S.key[j] = x; }
+                }
+            }
+            __syncthreads();
+        }
+    for (uint32_t k = t; k < n; k += kPlocThreads) S.cl[0][k] = 1u + (uint32_t)(S.key[k] & 0xFFFFFFFFull);
+    __syncthreads();
+    uint32_t count = n, next = n + 1, cur = 0;
+    while (count > 1) {
+        const uint32_t* cl = S.cl[cur];
+        uint32_t* ncl = S.cl[cur ^ 1];
+        for (uint32_t k = t; k < count; k += kPlocThreads) {
+            const float4 an = nodes[2 * cl[k]], ax = nodes[2 * cl[k] + 1];
+            const uint32_t j0 = k > kPlocRadius ? k - kPlocRadius : 0u;
+            const uint32_t j1 = k + kPlocRadius < count - 1 ? k + kPlocRadius : count - 1;
+            float best = FLT_MAX;
+            uint32_t bj = (k == 0) ? 1u : k - 1;
+            for (uint32_t j = j0; j <= j1; ++j) {
+                if (j == k) continue;
+                const float4 bn = nodes[2 * cl[j]], bx = nodes[2 * cl[j] + 1];
+                const float ex = gmax(ax.x, bx.x) - gmin(an.x, bn.x);
+                const float ey = gmax(ax.y, bx.y) - gmin(an.y, bn.y);
+                const float ez = gmax(ax.z, bx.z) - gmin(an.z, bn.z);
+                const float d = ex * ey + ey * ez + ez * ex;
+                if (d < best) { best = d; bj = j; }
+            }
+            S.nn[k] = bj;
+        }
+        __syncthreads();
+        // a round without a mutual pair (not seen in practice) merges positions 0 and 1
+        for (uint32_t k = t; k < count; k += kPlocThreads) S.flag[k] = (S.nn[S.nn[k]] == k && k < S.nn[k]) ? 1u : 0u;
+        __syncthreads();
+        uint32_t any = 0;
+        for (uint32_t k = t; k < count; k += kPlocThreads) any |= S.flag[k];
+        any = __syncthreads_or(any);
+        if (!any) {
+            if (t == 0) { S.nn[0] = 1; S.nn[1] = 0; }
+            __syncthreads();
+        }
+        for (uint32_t k = t; k < count; k += kPlocThreads) {
+            const uint32_t m = S.nn[k];
+            const bool mutual = S.nn[m] == k;
+            S.flag[k] = (mutual && k < m) ? 1u : 0u;
+            S.keep[k] = (mutual && k > m) ? 0u : 1u;
+        }
+        __syncthreads();
+        const uint32_t made = block_scan(S.flag, count, s_part);
+        const uint32_t kept = block_scan(S.keep, count, s_part);
+        for (uint32_t k = t; k < count; k += kPlocThreads) {
+            const uint32_t m = S.nn[k];
+            const bool mutual = S.nn[m] == k;
+            if (mutual && k > m) continue;
+            const uint32_t pos = S.keep[k];
+            if (mutual) {
+                const uint32_t id = next + S.flag[k];
+                const float4 an = nodes[2 * cl[k]], ax = nodes[2 * cl[k] + 1];
+                const float4 bn = nodes[2 * cl[m]], bx = nodes[2 * cl[m] + 1];
+                nodes[2 * id] = make_float4(gmin(an.x, bn.x), gmin(an.y, bn.y), gmin(an.z, bn.z),
+                                            __uint_as_float((cl[k] << 16) | cl[m]));
+                nodes[2 * id + 1] = make_float4(gmax(ax.x, bx.x), gmax(ax.y, bx.y), gmax(ax.z, bx.z),
+                                                __uint_as_float(0u));
+                ncl[pos] = id;
+            } else {
+                ncl[pos] = cl[k];
+            }
+        }
+        __syncthreads();
+        count = kept;
+        next += made;
+        cur ^= 1;
+    }
+    if (t == 0 && n > 0) {
+        const uint32_t r = S.cl[cur][0];
+        nodes[0] = nodes[2 * r];
+        nodes[1] = nodes[2 * r + 1];
+    }
+}
+
+uint32_t pow2_at_least(uint32_t n) {
+    uint32_t p = 1;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+}  // namespace
+
+size_t tlas_scratch_words(uint32_t n, uint32_t metric) {
+    if (metric == 2) return 2ull * pow2_at_least(n ? n : 1) + 5ull * n + 8;
+    return 7ull * n + 1;
+}
+
 cudaError_t launch_tlas_build(const float* aabbs, uint32_t n, float4* nodes, uint32_t* scratch, uint32_t metric,
                               cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
+    if (metric == 2) {
+        const uint32_t P = pow2_at_least(n);
+        PlocScratch S;
+        S.key = reinterpret_cast<unsigned long long*>(scratch);   // 8-byte aligned: scratch comes from cudaMalloc
+        S.cl[0] = scratch + 2ull * P;
+        S.cl[1] = S.cl[0] + n;
+        S.nn = S.cl[1] + n;
+        S.flag = S.nn + n;
+        S.keep = S.flag + n;
+        k_tlas_ploc<<<1, kPlocThreads, 0, stream>>>(aabbs, n, nodes, S, P);
+        return cudaGetLastError();
+    }
     size_t smem = (n <= kSmemInstances) ? (size_t)n * 7u * 4u : 0u;
     if (smem > 48u * 1024u) {
         cudaError_t e = cudaFuncSetAttribute(k_tlas_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
