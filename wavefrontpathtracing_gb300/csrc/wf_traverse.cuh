@@ -15,7 +15,7 @@
 // GPU organisation: a persistent grid; every warp runs one warp-uniform loop
 // whose iterations perform one traversal step per lane — an interior visit
 // (the same code for TLAS and BLAS nodes: two child boxes, one slab test
-// each), an instance entry, or a leaf's triangles — so lanes stay converged on
+// each), an instance entry, or one triangle of a leaf — so lanes stay converged on
 // the common interior step instead of drifting apart in nested per-lane loops.
 // Lanes whose ray finished take new rays in groups through one atomic per warp
 // (kRefill idle lanes, or all of them) from a per-launch counter.
@@ -192,20 +192,22 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
             w1 = __float_as_uint(r1.w);
             level = 1; tb = sp; hit_here = false;
         } else if (level == 1u && w1 > 0u) {
-            // BLAS leaf: its triangles in index-list order
-            for (uint32_t i = w0; i < w0 + w1; ++i) {
-                const float4* tp = B.tris + 3ull * i;
-                const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
-                if (COUNT) cnt.tris++;
-                float bu, bv;
-                if (tri_hit(xyz(a), xyz(b), xyz(c), co, cd, ct, bu, bv, no_cull)) {
-                    s_prim[col] = __float_as_uint(a.w);
-                    s_u[col] = bu; s_v[col] = bv;
-                    hit_here = true;
-                    if (ANY) { s_inst[col] = ii; s_t[col] = ct; finish = true; break; }
-                }
+            // BLAS leaf: one triangle per step, in index-list order (w0 = the
+            // next triangle, w1 = triangles left), so lanes on interior nodes
+            // never wait for a whole leaf
+            const float4* tp = B.tris + 3ull * w0;
+            const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+            if (COUNT) cnt.tris++;
+            float bu, bv;
+            if (tri_hit(xyz(a), xyz(b), xyz(c), co, cd, ct, bu, bv, no_cull)) {
+                s_prim[col] = __float_as_uint(a.w);
+                s_u[col] = bu; s_v[col] = bv;
+                hit_here = true;
+                if (ANY) { s_inst[col] = ii; s_t[col] = ct; finish = true; }
             }
-            pop = !finish;
+            w0++;
+            w1--;
+            pop = !finish && w1 == 0u;
         } else {
             // interior node, TLAS or BLAS: the two children, nearer first
             const float4* pa;
