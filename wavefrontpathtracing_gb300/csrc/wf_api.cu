@@ -144,6 +144,10 @@ struct wf_ctx {
     std::vector<EventPair> events;
     size_t events_used = 0;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
+    // connect at depth d runs on `side` while extend at depth d + 1 runs on
+    // `stream`; shade at d + 1 waits for it (both add to the path radiance)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_shade[kMaxDepth] = {}, ev_conn[kMaxDepth] = {};
     bool timing_pending = false;
     wf_stats stats{};
     uint64_t launches = 0, launches_extend = 0, launches_connect = 0;
@@ -171,8 +175,9 @@ cudaError_t d2h(wf_ctx* c, void* dst, const void* src, size_t bytes) {
 // Records an event pair around a stage when profiling.
 struct StageTimer {
     wf_ctx* c;
+    cudaStream_t st;
     EventPair* ev = nullptr;
-    StageTimer(wf_ctx* ctx, bool on, int stage) : c(ctx) {
+    StageTimer(wf_ctx* ctx, bool on, int stage, cudaStream_t stream = nullptr) : c(ctx), st(stream ? stream : ctx->stream) {
         if (!on) return;
         if (c->events_used == c->events.size()) {
             EventPair p{};
@@ -182,10 +187,10 @@ struct StageTimer {
         }
         ev = &c->events[c->events_used++];
         ev->stage = stage;
-        cudaEventRecord(ev->a, c->stream);
+        cudaEventRecord(ev->a, st);
     }
     ~StageTimer() {
-        if (ev) cudaEventRecord(ev->b, c->stream);
+        if (ev) cudaEventRecord(ev->b, st);
     }
 };
 
@@ -343,9 +348,11 @@ int ensure_buffers(wf_ctx* c) {
             return rc;
     }
     if ((rc = dev_alloc(&B.h_tuvp, C)) || (rc = dev_alloc(&B.h_inst, C)) || (rc = dev_alloc(&B.ps_T, C)) ||
-        (rc = dev_alloc(&B.ps_flags, C)) || (rc = dev_alloc(&B.ps_L, C)) || (rc = dev_alloc(&B.s_o, C)) ||
-        (rc = dev_alloc(&B.s_d, C)) ||
-        (rc = dev_alloc(&B.s_c, C)) || (rc = dev_alloc(&B.counts, 4 * kMaxDepth)) || (rc = dev_alloc(&c->accum, npix)))
+        (rc = dev_alloc(&B.ps_flags, C)) || (rc = dev_alloc(&B.ps_L, C)) || (rc = dev_alloc(&B.counts, 4 * kMaxDepth)) ||
+        (rc = dev_alloc(&c->accum, npix)))
+        return rc;
+    for (int k = 0; k < 2; ++k)
+        if ((rc = dev_alloc(&B.s_o[k], C)) || (rc = dev_alloc(&B.s_d[k], C)) || (rc = dev_alloc(&B.s_c[k], C)))
         return rc;
     B.accum = c->accum;
     B.status = c->status;
@@ -360,7 +367,8 @@ void release_buffers(wf_ctx* c) {
     RenderBuffers& B = c->B;
     for (int k = 0; k < 2; ++k) { dev_free(B.q_o[k]); dev_free(B.q_d[k]); dev_free(B.q_path[k]); }
     dev_free(B.h_tuvp); dev_free(B.h_inst); dev_free(B.ps_T); dev_free(B.ps_flags); dev_free(B.ps_L);
-    dev_free(B.s_o); dev_free(B.s_d); dev_free(B.s_c); dev_free(B.counts);
+    for (int k = 0; k < 2; ++k) { dev_free(B.s_o[k]); dev_free(B.s_d[k]); dev_free(B.s_c[k]); }
+    dev_free(B.counts);
     dev_free(c->accum);
     c->buffers_ready = false;
 }
@@ -635,9 +643,14 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
     int rc = use_device(c);
     if (rc == WF_OK) {
         if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreate(&c->t0) != cudaSuccess || cudaEventCreate(&c->t1) != cudaSuccess) {
             rc = fail(WF_ERR_CUDA, "wf_create: stream/event creation failed");
         }
+        for (uint32_t d = 0; rc == WF_OK && d < kMaxDepth; ++d)
+            if (cudaEventCreateWithFlags(&c->ev_shade[d], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&c->ev_conn[d], cudaEventDisableTiming) != cudaSuccess)
+                rc = fail(WF_ERR_CUDA, "wf_create: event creation failed");
     }
     if (rc == WF_OK) rc = dev_alloc(&c->status, 1);
     if (rc == WF_OK) rc = dev_alloc(&c->counters, 2);
@@ -674,6 +687,11 @@ int wf_destroy(wf_ctx* c) {
     for (EventPair& p : c->events) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
+    for (uint32_t d = 0; d < kMaxDepth; ++d) {
+        if (c->ev_shade[d]) cudaEventDestroy(c->ev_shade[d]);
+        if (c->ev_conn[d]) cudaEventDestroy(c->ev_conn[d]);
+    }
+    if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return WF_OK;
@@ -1092,10 +1110,16 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
         WF_CUDA(launch_generate(B, W, c->stream));
     }
     c->launches++;
+    bool pending = false;   // a connect on the side stream not yet joined
     for (uint32_t d = 0; d <= W.max_bounces; ++d) {
         {
             StageTimer t(c, P.prof, ST_EXTEND);
             WF_CUDA(launch_extend(P.S, B, d, W.npaths, P.cnt, c->totals, c->stream));
+        }
+        // connect at depth d - 1 has added its contributions before shade adds more
+        if (pending) {
+            WF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_conn[d - 1], 0));
+            pending = false;
         }
         {
             StageTimer t(c, P.prof, ST_SHADE);
@@ -1104,12 +1128,20 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
         c->launches += 2;
         c->launches_extend++;
         if (P.nee && d < W.max_bounces) {
-            StageTimer t(c, P.prof, ST_CONNECT);
-            WF_CUDA(launch_connect(P.S, B, d, W.npaths, P.cnt, c->totals + 1, c->stream));
+            // the shadow rays of depth d overlap the extension rays of depth d + 1
+            WF_CUDA(cudaEventRecord(c->ev_shade[d], c->stream));
+            WF_CUDA(cudaStreamWaitEvent(c->side, c->ev_shade[d], 0));
+            {
+                StageTimer t(c, P.prof, ST_CONNECT, c->side);
+                WF_CUDA(launch_connect(P.S, B, d, W.npaths, P.cnt, c->totals + 1, c->side));
+            }
+            WF_CUDA(cudaEventRecord(c->ev_conn[d], c->side));
+            pending = true;
             c->launches++;
             c->launches_connect++;
         }
     }
+    if (pending) WF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_conn[W.max_bounces - 1], 0));
     if (resolve) {
         {
             StageTimer t(c, P.prof, ST_POST);

@@ -51,9 +51,9 @@ struct RenderBuffers {
     float4* ps_T;         // {throughput rgb, pdf of the last BSDF sample}
     uint32_t* ps_flags;   // path flags
     float4* ps_L;         // path radiance (rgb), summed from zero
-    float4* s_o;          // shadow {origin, tmax}
-    float4* s_d;          // shadow {direction, path id}
-    float4* s_c;          // shadow {contribution rgb, -}
+    float4* s_o[2];       // shadow {origin, tmax}, by depth parity (connect at depth d
+    float4* s_d[2];       // shadow {direction, path id}   runs while shade at d + 1
+    float4* s_c[2];       // shadow {contribution rgb, -}  fills the other buffer)
     uint32_t* counts;     // [d] extension rays at depth d, [kMaxDepth + d] shadow rays,
                           // [2 kMaxDepth + d], [3 kMaxDepth + d] the traversal kernels' fetch counters
     float4* accum;        // per pixel {radiance sum rgb, samples}

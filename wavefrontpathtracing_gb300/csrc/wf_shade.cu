@@ -44,6 +44,10 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
     K.cosine = W.cosine; K.env_strength = W.env_strength; K.env0 = W.env[0]; K.env1 = W.env[1]; K.env2 = W.env[2];
     K.lights = SH.lights; K.light_count = SH.light_count; K.light_total = SH.light_total;
     K.env_tex = W.env_tex; K.view_mode = W.view_mode; K.far_plane = W.far_plane;
+    // shadow queue of this depth's parity (selects, not a dynamic index into the parameter)
+    float4* const s_o = cur ? B.s_o[1] : B.s_o[0];
+    float4* const s_d = cur ? B.s_d[1] : B.s_d[0];
+    float4* const s_c = cur ? B.s_c[1] : B.s_c[0];
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -83,9 +87,9 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
         }
         const uint32_t sslot = warp_append(&B.counts[kMaxDepth + depth], o.shadow);
         if (o.shadow) {
-            B.s_o[sslot] = make_float4(o.spos.x, o.spos.y, o.spos.z, o.stmax);
-            B.s_d[sslot] = make_float4(o.sdir.x, o.sdir.y, o.sdir.z, __uint_as_float(path));
-            B.s_c[sslot] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, 0.0f);
+            s_o[sslot] = make_float4(o.spos.x, o.spos.y, o.spos.z, o.stmax);
+            s_d[sslot] = make_float4(o.sdir.x, o.sdir.y, o.sdir.z, __uint_as_float(path));
+            s_c[sslot] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, 0.0f);
         }
     }
 }

@@ -100,7 +100,8 @@ cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t d
 cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t, bool count,
                            unsigned long long* total, cudaStream_t stream) {
     ConnectIO io;
-    io.so = B.s_o; io.sd = B.s_d; io.sc = B.s_c; io.L = B.ps_L;
+    const int par = depth & 1;
+    io.so = B.s_o[par]; io.sd = B.s_d[par]; io.sc = B.s_c[par]; io.L = B.ps_L;
     uint32_t* fetch = B.counts + 3 * kMaxDepth + depth;
     return count ? launch<true, true>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, B.counters + 1, total,
                                       stream)
