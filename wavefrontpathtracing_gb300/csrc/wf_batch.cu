@@ -14,9 +14,12 @@
 //     connect                any-hit shadow rays add their contribution
 //     end        (1 thread)  loop bookkeeping and the loop condition
 // Every stage reads its sizes from a control block in device memory, so the
-// host records the iteration once: two iterations (queue A -> B, B -> A) form
-// the body of a CUDA-graph while-loop whose condition the last kernel sets, and
-// one graph launch renders the whole batch.
+// host records the iterations once: four iterations (queues A -> B -> A -> B
+// -> A) form the body of a CUDA-graph while-loop whose condition the last
+// kernel sets, and one graph launch renders the whole batch.  Each connect
+// runs on a second stream beside the next iteration's begin / regenerate /
+// extend (shadow queues, counts and hand-out counters alternate by iteration
+// parity); the next shade waits for it.
 //
 // Camera paths are numbered scene by scene, sample-major inside a scene
 // (path = path_base + sample * pixels + pixel), and admitted in that order.  A
@@ -47,6 +50,7 @@ namespace {
 constexpr uint32_t kSceneShift = 16;       // queue flags word: bits 0-7 path flags, 8-15 depth, 16-31 scene
 constexpr uint32_t kDepthShift = 8;
 constexpr uint32_t kFinishedBit = 0x80000000u;  // shadow target: radiance slot of a finished path
+constexpr int kBodyIterations = 4;              // iterations per graph-loop body (even: queues alternate)
 
 struct BatchScene {
     float4 clip_to_view[4];
@@ -72,22 +76,21 @@ struct BatchQueues {
     float4* qL[2];
     float4* h_tuvp;
     uint32_t* h_inst;
-    float4* s_o;      // {origin, tmax}
-    float4* s_d;      // {direction, target}: pool slot of the continuing path, or kFinishedBit | camera path
-    float4* s_c;      // {contribution, scene}
+    float4* s_o[2];   // by iteration parity: {origin, tmax}
+    float4* s_d[2];   // {direction, target}: pool slot of the continuing path, or kFinishedBit | camera path
+    float4* s_c[2];   // {contribution, scene}
     float4* out_L;    // per camera path: its radiance
 };
 
 struct BatchCtl {
     uint32_t count[2];        // entries in queue k
-    uint32_t shadow;          // shadow rays of this iteration
-    uint32_t fetch[2];        // persistent traversal hand-out counters (extend, connect)
+    uint32_t shadow[2];       // shadow rays of the iteration on queue k
+    uint32_t fetch[3];        // persistent traversal hand-out counters: extend, connect on queue 0 / 1
     uint32_t regen_n, regen_g0, regen_slot0;
     uint32_t next, total;     // next camera path to admit, number of camera paths
     uint32_t capacity, threshold;
     uint32_t iter, stall, stall_limit, done, body_runs;
     uint32_t max_iter;        // hard bound on iterations (a loose upper bound of a correct run)
-    uint32_t pad[2];
     unsigned long long rays_ext, rays_con;
 };
 
@@ -113,9 +116,9 @@ __global__ void k_bbegin(BatchCtl* c, int cur) {
     c->regen_slot0 = n;
     c->next += take;
     c->count[cur ^ 1] = 0;
-    c->shadow = 0;
+    c->shadow[cur] = 0;
     c->fetch[0] = 0;
-    c->fetch[1] = 0;
+    c->fetch[1 + cur] = 0;   // the other parity's connect may still be running
     c->rays_ext += n + take;
 }
 
@@ -219,6 +222,10 @@ __global__ void __launch_bounds__(BLOCK) k_bshade(ShadeRefs SH, const BatchScene
     float4* const nT = cur ? Q.qT[0] : Q.qT[1];
     float4* const nL = cur ? Q.qL[0] : Q.qL[1];
     uint32_t* const ncount = cur ? &c->count[0] : &c->count[1];
+    uint32_t* const shadow_tail = cur ? &c->shadow[1] : &c->shadow[0];
+    float4* const s_o = cur ? Q.s_o[1] : Q.s_o[0];
+    float4* const s_d = cur ? Q.s_d[1] : Q.s_d[0];
+    float4* const s_c = cur ? Q.s_c[1] : Q.s_c[0];
     for (uint32_t base = blockIdx.x * BLOCK; base < n; base += gridDim.x * BLOCK) {
         const uint32_t i = base + threadIdx.x;
         ShadeOut o;
@@ -268,12 +275,12 @@ __global__ void __launch_bounds__(BLOCK) k_bshade(ShadeRefs SH, const BatchScene
             nT[slot] = make_float4(o.T.x, o.T.y, o.T.z, o.pdf);
             nL[slot] = L4;
         }
-        const uint32_t sslot = warp_append(&c->shadow, o.shadow);
+        const uint32_t sslot = warp_append(shadow_tail, o.shadow);
         if (o.shadow) {
             const uint32_t target = o.enqueue ? slot : (kFinishedBit | gidx);
-            Q.s_o[sslot] = make_float4(o.spos.x, o.spos.y, o.spos.z, o.stmax);
-            Q.s_d[sslot] = make_float4(o.sdir.x, o.sdir.y, o.sdir.z, __uint_as_float(target));
-            Q.s_c[sslot] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, __uint_as_float(scene));
+            s_o[sslot] = make_float4(o.spos.x, o.spos.y, o.spos.z, o.stmax);
+            s_d[sslot] = make_float4(o.sdir.x, o.sdir.y, o.sdir.z, __uint_as_float(target));
+            s_c[sslot] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, __uint_as_float(scene));
         }
     }
 }
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(BLOCK) k_bshade(ShadeRefs SH, const BatchScene
 __global__ void k_bend(BatchCtl* c, int cur, uint32_t* status, cudaGraphConditionalHandle h, int set_cond) {
     if (!c->done) {
         c->iter++;
-        c->rays_con += c->shadow;
+        c->rays_con += c->shadow[cur];
         const uint32_t n = c->count[cur], m = c->count[cur ^ 1];
         c->stall = (n > 0u && m >= n) ? c->stall + 1u : 0u;   // m >= n: no path ended
         if (c->stall > c->stall_limit || c->iter >= c->max_iter) {
@@ -408,7 +415,7 @@ struct wf_batch {
     uint32_t pool_cap = 0;
     uint32_t pool_block = 0;
     DBuf<float4> q[8];
-    DBuf<float4> h_tuvp, s_o, s_d, s_c;
+    DBuf<float4> h_tuvp, s_o[2], s_d[2], s_c[2];
     DBuf<uint32_t> h_inst;
     BatchCtl* ctl = nullptr;
     BatchCtl* ctl_host = nullptr;   // pinned
@@ -419,6 +426,8 @@ struct wf_batch {
     bool graph_valid = false;
 
     cudaEvent_t t0 = nullptr, t1 = nullptr;
+    cudaStream_t side = nullptr;                         // the connect stage
+    cudaEvent_t ev_shade[kBodyIterations] = {}, ev_conn[kBodyIterations] = {};
     wf_batch_stats stats{};
     uint64_t host_launches = 0;
     bool rendered = false;
@@ -556,9 +565,9 @@ int ensure_pool(wf_batch* b) {
     int rc;
     for (int k = 0; k < 8; ++k)
         if ((rc = b->q[k].reserve(C))) return rc;
-    if ((rc = b->h_tuvp.reserve(C)) || (rc = b->h_inst.reserve(C)) || (rc = b->s_o.reserve(C)) ||
-        (rc = b->s_d.reserve(C)) || (rc = b->s_c.reserve(C)))
-        return rc;
+    if ((rc = b->h_tuvp.reserve(C)) || (rc = b->h_inst.reserve(C))) return rc;
+    for (int k = 0; k < 2; ++k)
+        if ((rc = b->s_o[k].reserve(C)) || (rc = b->s_d[k].reserve(C)) || (rc = b->s_c[k].reserve(C))) return rc;
     if (!b->ctl) {
         if (cudaMalloc(&b->ctl, sizeof(BatchCtl)) != cudaSuccess) {
             cudaGetLastError();
@@ -585,9 +594,11 @@ BatchQueues queues(wf_batch* b) {
     }
     Q.h_tuvp = b->h_tuvp.p;
     Q.h_inst = b->h_inst.p;
-    Q.s_o = b->s_o.p;
-    Q.s_d = b->s_d.p;
-    Q.s_c = b->s_c.p;
+    for (int k = 0; k < 2; ++k) {
+        Q.s_o[k] = b->s_o[k].p;
+        Q.s_d[k] = b->s_d[k].p;
+        Q.s_c[k] = b->s_c[k].p;
+    }
     Q.out_L = b->out_L.p;
     return Q;
 }
@@ -611,9 +622,14 @@ cudaError_t regen_or_shade(bool shade, wf_batch* b, const ShadeRefs& SH, const B
     }
 }
 
-// One iteration on queue cur (6 kernels).  set_cond: the last kernel sets the
-// graph loop's condition.
-int enqueue_iteration(wf_batch* b, int cur, cudaGraphConditionalHandle h, bool set_cond) {
+// Iteration k of a group (queue cur = k & 1; 6 kernels).  Its connect goes to
+// the side stream; its shade first waits for the previous iteration's connect
+// (join_prev), and the last iteration of a group joins its own connect before
+// its end kernel (join_self).  set_cond: the end kernel sets the graph loop's
+// condition.
+int enqueue_iteration(wf_batch* b, int k, bool join_prev, bool join_self, cudaGraphConditionalHandle h,
+                      bool set_cond) {
+    const int cur = k & 1;
     cudaStream_t st = ctx_stream(b->ctx);
     uint32_t* status = ctx_status(b->ctx);
     const BatchQueues Q = queues(b);
@@ -639,12 +655,19 @@ int enqueue_iteration(wf_batch* b, int cur, cudaGraphConditionalHandle h, bool s
     auto ke = k_btrace<false, BatchExtendIO>;
     ke<<<persistent_grid(ke), kTraceBlock, 0, st>>>(S, ex, &b->ctl->count[cur], &b->ctl->fetch[0], status);
     BCUDA(cudaGetLastError());
+    const int kp = (k + kBodyIterations - 1) % kBodyIterations;
+    if (join_prev) BCUDA(cudaStreamWaitEvent(st, b->ev_conn[kp], 0));   // both add to the path radiance
     BCUDA(regen_or_shade(true, b, SH, Q, cur, st));
+    BCUDA(cudaEventRecord(b->ev_shade[k], st));
+    BCUDA(cudaStreamWaitEvent(b->side, b->ev_shade[k], 0));
     BatchConnectIO cn;
-    cn.so = Q.s_o; cn.sd = Q.s_d; cn.sc = Q.s_c; cn.roots = b->d_roots.p; cn.qL = Q.qL[cur ^ 1]; cn.out_L = Q.out_L;
+    cn.so = Q.s_o[cur]; cn.sd = Q.s_d[cur]; cn.sc = Q.s_c[cur]; cn.roots = b->d_roots.p; cn.qL = Q.qL[cur ^ 1];
+    cn.out_L = Q.out_L;
     auto kc = k_btrace<true, BatchConnectIO>;
-    kc<<<persistent_grid(kc), kTraceBlock, 0, st>>>(S, cn, &b->ctl->shadow, &b->ctl->fetch[1], status);
+    kc<<<persistent_grid(kc), kTraceBlock, 0, b->side>>>(S, cn, &b->ctl->shadow[cur], &b->ctl->fetch[1 + cur], status);
     BCUDA(cudaGetLastError());
+    BCUDA(cudaEventRecord(b->ev_conn[k], b->side));
+    if (join_self) BCUDA(cudaStreamWaitEvent(st, b->ev_conn[k], 0));
     k_bend<<<1, 1, 0, st>>>(b->ctl, cur, status, h, set_cond ? 1 : 0);
     BCUDA(cudaGetLastError());
     return WF_OK;
@@ -670,8 +693,9 @@ int build_graph(wf_batch* b) {
     BCUDA(cudaGraphAddNode(&node, b->graph, nullptr, nullptr, 0, &p));
     cudaGraph_t body = p.conditional.phGraph_out[0];
     BCUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_iteration(b, 0, h, false);
-    if (rc == WF_OK) rc = enqueue_iteration(b, 1, h, true);
+    int rc = WF_OK;
+    for (int k = 0; k < kBodyIterations && rc == WF_OK; ++k)
+        rc = enqueue_iteration(b, k, k > 0, k == kBodyIterations - 1, h, k == kBodyIterations - 1);
     cudaGraph_t captured = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &captured);
     if (rc) return rc;
@@ -753,10 +777,10 @@ int render(wf_batch* b, const render_settings_t* s, const wf_render_options* o, 
         BCUDA(cudaGraphLaunch(b->exec, st));
         graph_launches = 1;
     } else {
-        // host-driven loop: iterations in groups of 8, then a look at `done`
+        // host-driven loop: iterations in groups, then a look at `done`
         for (uint32_t group = 0;; ++group) {
-            for (int k = 0; k < 8; ++k) {
-                if ((rc = enqueue_iteration(b, k & 1, 0, false))) return rc;
+            for (int k = 0; k < kBodyIterations; ++k) {
+                if ((rc = enqueue_iteration(b, k, k > 0, k == kBodyIterations - 1, 0, false))) return rc;
                 b->host_launches += kKernelsPerIteration;
             }
             BCUDA(ctx_d2h(c, b->ctl_host, b->ctl, sizeof(BatchCtl)));
@@ -783,7 +807,8 @@ int render(wf_batch* b, const render_settings_t* s, const wf_render_options* o, 
     S.rays_connect = r.rays_con;
     S.iterations = r.iter;
     S.graph_launches = (uint32_t)graph_launches;
-    S.kernel_launches = (b->cfg.use_graph ? (uint64_t)r.body_runs * 2 * kKernelsPerIteration : b->host_launches) + 1;
+    S.kernel_launches =
+        (b->cfg.use_graph ? (uint64_t)r.body_runs * kBodyIterations * kKernelsPerIteration : b->host_launches) + 1;
     S.scenes = b->nscenes;
     b->rendered = true;
     rc = ctx_take_status(c);
@@ -815,10 +840,15 @@ int wf_batch_create(wf_ctx* ctx, wf_batch** out) {
     wf_batch* b = new wf_batch();
     b->ctx = ctx;
     default_config(&b->cfg);
-    if (cudaEventCreate(&b->t0) != cudaSuccess || cudaEventCreate(&b->t1) != cudaSuccess) {
+    bool ok = cudaEventCreate(&b->t0) == cudaSuccess && cudaEventCreate(&b->t1) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) == cudaSuccess;
+    for (int k = 0; ok && k < kBodyIterations; ++k)
+        ok = cudaEventCreateWithFlags(&b->ev_shade[k], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&b->ev_conn[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
         cudaGetLastError();
-        delete b;
-        return fail_code(WF_ERR_CUDA, "wf_batch_create: event creation failed");
+        wf_batch_destroy(b);
+        return fail_code(WF_ERR_CUDA, "wf_batch_create: stream or event creation failed");
     }
     *out = b;
     return WF_OK;
@@ -834,7 +864,13 @@ int wf_batch_destroy(wf_batch* b) {
     b->lights.release(); b->blas.release(); b->stri.release(); b->d_scenes.release();
     b->out_L.release(); b->image.release();
     for (auto& q : b->q) q.release();
-    b->h_tuvp.release(); b->h_inst.release(); b->s_o.release(); b->s_d.release(); b->s_c.release();
+    b->h_tuvp.release(); b->h_inst.release();
+    for (int k = 0; k < 2; ++k) { b->s_o[k].release(); b->s_d[k].release(); b->s_c[k].release(); }
+    for (int k = 0; k < kBodyIterations; ++k) {
+        if (b->ev_shade[k]) cudaEventDestroy(b->ev_shade[k]);
+        if (b->ev_conn[k]) cudaEventDestroy(b->ev_conn[k]);
+    }
+    if (b->side) cudaStreamDestroy(b->side);
     if (b->ctl) cudaFree(b->ctl);
     if (b->ctl_host) cudaFreeHost(b->ctl_host);
     if (b->t0) cudaEventDestroy(b->t0);
