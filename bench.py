@@ -350,6 +350,37 @@ def batched_leg(device, tlas_metric, steps=3, count=64):
     return out
 
 
+def builders_leg(r, desc):
+    """BLAS build of the largest instanced mesh and TLAS build of the 1,025
+    instance boxes: the GPU builders through the C ABI (host arrays in, blob
+    out) against the oracle's restatement of the reference's single-threaded
+    C++ builders (byte-identical output)."""
+    from oracle import oracle as orc
+    tris = max(desc.meshes, key=len)
+    t0 = time.perf_counter()
+    g = r.bvh_build(tris, interval_count=16, max_leaf_prims=4)
+    gpu_blas = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    c = orc.bvh_build(tris, 16, False, 4)
+    cpu_blas = time.perf_counter() - t0
+    inst = r.scene_instances()
+    out = {"mesh_triangles": len(tris), "gpu_blas_ms": round(1e3 * gpu_blas, 2), "cpu_blas_ms": round(1e3 * cpu_blas, 1),
+           "blas_equal": bool(np.array_equal(g, c)), "tlas_instances": len(inst)}
+    t0 = time.perf_counter()
+    ct = orc.tlas_build(inst, metric=0)
+    out["cpu_tlas_reference_ms"] = round(1e3 * (time.perf_counter() - t0), 2)
+    for metric, name in ((0, "reference"), (2, "clustering")):
+        import wavefrontpathtracing_gb300 as wf
+        with wf.Renderer(8, 8, tlas_metric=metric) as q:
+            q.tlas_build(inst)                          # warm-up (module load, allocation)
+            t0 = time.perf_counter()
+            gt = q.tlas_build(inst)
+            out[f"gpu_tlas_{name}_ms"] = round(1e3 * (time.perf_counter() - t0), 3)
+        if metric == 0:
+            out["tlas_equal"] = bool(np.array_equal(gt, ct))
+    return out
+
+
 def flush_l2(torch, buf):
     if buf is not None:
         buf.add_(1)
@@ -448,6 +479,10 @@ def run_ours(args, rank, world, local):
         v, sdesc, _, _ = cpu_sample(sc, desc, args.cpu_seconds, threads, seed=1)
         cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                "sample": sdesc + "; reference TLAS metric"}
+    # --- builders: GPU vs the oracle's restatement of the reference's single-threaded C++ builders
+    builders = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        builders = builders_leg(r, desc)
     r.close()
     adjoint = None
     if rank == 0 and not args.no_adjoint:
@@ -478,6 +513,8 @@ def run_ours(args, rank, world, local):
                 "clocks": clk.summary()}
         if cpu:
             line["cpu_baseline"] = cpu
+        if builders:
+            line["builders"] = builders
         if adjoint:
             line["adjoint"] = adjoint
         if batched:
