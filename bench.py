@@ -417,6 +417,7 @@ def run_ours(args, rank, world, local):
             if torch is not None:
                 torch.cuda.synchronize()
             s = frame(frame_seed(i, rank), True)
+            last = s
             gpu_ms += s["ms_total"]
             rays += s["rays_extend"] + s["rays_connect"]
             launches += s["launches"]
@@ -503,6 +504,9 @@ def run_ours(args, rank, world, local):
                 "spp_per_s": round(spp_per_s, 3),
                 "rays_per_step": rays // args.steps,
                 "gpu_launches": launches,
+                "stages_ms": {k: round(last[f"ms_{k}"], 3) for k in ("generate", "extend", "shade", "connect", "post")},
+                "queue_sizes": {"extend": [int(x) for x in last["extend_rays_depth"][:DEPTH + 1]],
+                                "shadow": [int(x) for x in last["shadow_rays_depth"][:DEPTH]]},
                 "e2e": {"value": round(e2e_value, 3) if e2e_value else None, "unit": "Mrays/s",
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": round(achieved, 1),

@@ -128,6 +128,8 @@ typedef struct wf_stats {
     uint64_t shadow_tlas_node_loads, shadow_instance_loads, shadow_blas_node_loads, shadow_triangle_tests;
     /* host<->device bytes copied by this context since wf_create (cumulative) */
     uint64_t h2d_bytes, d2h_bytes;
+    /* queue sizes of the call (wavefront path): extension and shadow rays per depth */
+    uint64_t extend_rays_depth[16], shadow_rays_depth[16];
 } wf_stats;
 
 /* ---- lifetime (renderer::init / exit, renderer.h:23-24) ------------------ */
@@ -136,6 +138,11 @@ int wf_destroy(wf_ctx* ctx);
 const char* wf_status_string(int status);
 const char* wf_last_error(void);
 int wf_abi_version(void);
+/* Process-wide cap on the device memory the library allocates (all contexts
+ * and batches); an allocation past it fails with WF_ERR_OOM and leaves the
+ * caller's objects usable.  0 = no cap (the default). */
+int wf_set_device_memory_limit(uint64_t bytes);
+int wf_get_device_memory_usage(uint64_t* out_bytes);
 /* The context's cudaStream_t, for callers that time or order work around it. */
 int wf_get_stream(wf_ctx* ctx, void** out_stream);
 /* Waits for the context's stream; reports a device-side error flag if set. */
@@ -206,6 +213,16 @@ int wf_read_image(wf_ctx* ctx, float* out_rgba, uint64_t float_count);
 int wf_read_image_ldr(wf_ctx* ctx, uint8_t* out_rgba8, uint64_t byte_count);
 int wf_get_stats(wf_ctx* ctx, wf_stats* out);
 
+/* ---- checkpoint / resume of a progressive render (no counterpart in the reference,
+ * whose only accumulation state is accum_count, renderer.cpp:47-51, 593-596) --
+ * The state is the accumulator (per pixel radiance sum and sample count), the
+ * number of samples accumulated, the view and the last frame seed.  Resume:
+ * wf_create, the same meshes and scene (wf_scene_begin with the saved view),
+ * wf_load_accumulator, then wf_render with accumulate = 1 and the same
+ * frame_seed: the result equals one uninterrupted render bit for bit. */
+int wf_save_accumulator(wf_ctx* ctx, const char* path);
+int wf_load_accumulator(wf_ctx* ctx, const char* path, uint32_t* out_samples, uint32_t* out_frame_seed);
+
 /* ---- differentiable rendering (no counterpart in the reference) ---------- */
 /* Number of scene triangles: the instances' triangles in submission order,
  * each instance's in primitive order.  Valid after wf_scene_end. */
@@ -244,7 +261,10 @@ typedef struct wf_batch_config {
     uint32_t block;           /* threads per block of regeneration and shading: 128, 256 or 512; 0 = 256 */
     uint32_t use_graph;       /* 1 = one CUDA-graph launch with a device-side loop (default);
                                  0 = host-driven loop that polls for completion */
-    uint32_t reserved[4];
+    uint32_t max_iterations;  /* iteration budget of the device loop: 0 = a bound derived from the
+                                 batch (never reached by a correct run); a render that needs more
+                                 stops and returns WF_ERR_TIMEOUT, leaving the batch usable */
+    uint32_t reserved[3];
 } wf_batch_config;
 
 typedef struct wf_batch_stats {

@@ -168,3 +168,47 @@ def test_submit_many_equals_one_by_one(orc):
             imgs.append(r.read_image())
     assert insts[0].tobytes() == insts[1].tobytes()
     assert_images_equal(imgs[1], imgs[0])
+
+
+def test_per_depth_queue_sizes_match_the_oracle(orc):
+    desc = scenes.instanced_scene(width=48, height=32, instances=60, freqs=(5, 8), spp=2, max_bounces=5)
+    img, want, stats, ost, _, _ = render_both(orc, desc, spp=2, frame_seed=9, nee=1, rr=2)
+    assert_images_equal(img, want)
+    assert stats["extend_rays_depth"][:6] == ost["extend_rays"][:6]
+    assert stats["shadow_rays_depth"][:6] == ost["shadow_rays"][:6]
+    assert sum(stats["extend_rays_depth"]) == stats["rays_extend"]
+
+
+def test_checkpoint_resume_equals_uninterrupted_render(tmp_path):
+    """Accumulator checkpoint: 2 spp, save, a new context loads and adds 3
+    more spp with the same frame seed == 5 spp in one context, bit for bit."""
+    desc = scenes.box_scene(width=40, height=32, max_bounces=3)
+    path = str(tmp_path / "accum.bin")
+    with Renderer(40, 32) as r:
+        load_scene_into(r, desc)
+        r.render(max_bounces=3, spp=2, frame_seed=6, accumulate=True)
+        r.save_accumulator(path)
+    with Renderer(40, 32) as r:
+        load_scene_into(r, desc)
+        assert r.load_accumulator(path) == (2, 6)
+        r.render(max_bounces=3, spp=3, frame_seed=6, accumulate=True)
+        resumed = r.read_image()
+    with Renderer(40, 32) as r:
+        load_scene_into(r, desc)
+        r.render(max_bounces=3, spp=5, frame_seed=6, accumulate=True)
+        whole = r.read_image()
+    assert (resumed[..., 3] == 5).all()
+    assert_images_equal(resumed, whole)
+    # another view or image size is refused
+    other = scenes.box_scene(width=40, height=32, max_bounces=3)
+    other.view = scenes.make_view((0.5, 0.5, -1.0), (0.5, 0.5, 0.5), 40.0, 40, 32)
+    import wavefrontpathtracing_gb300 as wf
+    with Renderer(40, 32) as r:
+        load_scene_into(r, other)
+        with pytest.raises(wf.WFError):
+            r.load_accumulator(path)
+    with Renderer(20, 16) as r:
+        small = scenes.box_scene(width=20, height=16, max_bounces=3)
+        load_scene_into(r, small)
+        with pytest.raises(wf.WFError):
+            r.load_accumulator(path)

@@ -41,6 +41,8 @@ SIGNATURES = {
     "wf_status_string": [ctypes.c_int],
     "wf_last_error": [],
     "wf_abi_version": [],
+    "wf_set_device_memory_limit": [_u64],
+    "wf_get_device_memory_usage": [_pu64],
     "wf_get_stream": [_vp, ctypes.POINTER(_vp)],
     "wf_synchronize": [_vp],
     "wf_mesh_create": [_vp, _vp, _u32, _vp, _u32, _vp, _pu32],
@@ -67,6 +69,8 @@ SIGNATURES = {
     "wf_scene_set_emission": [_vp, _u32, ctypes.c_float],
     "wf_adjoint": [_vp, _vp, _vp, _u32, _vp, _vp, _vp],
     "wf_texture_create": [_vp, _u32, _u32, _u32, _vp, _pu32],
+    "wf_save_accumulator": [_vp, ctypes.c_char_p],
+    "wf_load_accumulator": [_vp, ctypes.c_char_p, _pu32, _pu32],
     "wf_batch_create": [_vp, ctypes.POINTER(_vp)],
     "wf_batch_destroy": [_vp],
     "wf_batch_scene_begin": [_vp, _u32, _u32, _u32, _vp, _vp, _pu32],
@@ -291,6 +295,15 @@ class Renderer:
         check(self.L.wf_adjoint(self.h, ctypes.byref(s), ctypes.byref(o), frame_seed, ptr(d), ptr(ga), ptr(ge)))
         return ga.reshape(-1, 3), ge
 
+    def save_accumulator(self, path):
+        check(self.L.wf_save_accumulator(self.h, os.fsencode(path)))
+
+    def load_accumulator(self, path):
+        """Returns (samples accumulated, frame seed of the last render)."""
+        n, seed = ctypes.c_uint32(), ctypes.c_uint32()
+        check(self.L.wf_load_accumulator(self.h, os.fsencode(path), ctypes.byref(n), ctypes.byref(seed)))
+        return n.value, seed.value
+
     def read_image(self):
         out = np.zeros((self.height, self.width, 4), dtype=np.float32)
         check(self.L.wf_read_image(self.h, ptr(out), out.size))
@@ -411,8 +424,8 @@ class Batch:
         check(self.L.wf_batch_get_config(self.h, ctypes.byref(c)))
         return c.as_dict()
 
-    def set_config(self, capacity=0, regen_threshold=0.0, block=0, use_graph=1):
-        c = BatchConfig(capacity, regen_threshold, block, use_graph)
+    def set_config(self, capacity=0, regen_threshold=0.0, block=0, use_graph=1, max_iterations=0):
+        c = BatchConfig(capacity, regen_threshold, block, use_graph, max_iterations)
         check(self.L.wf_batch_set_config(self.h, ctypes.byref(c)))
 
     @staticmethod

@@ -92,19 +92,23 @@ class Stats(ctypes.Structure):
                 ("blas_node_loads", ctypes.c_uint64), ("triangle_tests", ctypes.c_uint64),
                 ("shadow_tlas_node_loads", ctypes.c_uint64), ("shadow_instance_loads", ctypes.c_uint64),
                 ("shadow_blas_node_loads", ctypes.c_uint64), ("shadow_triangle_tests", ctypes.c_uint64),
-                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("extend_rays_depth", ctypes.c_uint64 * 16), ("shadow_rays_depth", ctypes.c_uint64 * 16)]
 
     def as_dict(self):
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        d = {name: getattr(self, name) for name, _ in self._fields_}
+        d["extend_rays_depth"] = list(self.extend_rays_depth)
+        d["shadow_rays_depth"] = list(self.shadow_rays_depth)
+        return d
 
 
 class BatchConfig(ctypes.Structure):
     _fields_ = [("capacity", ctypes.c_uint32), ("regen_threshold", ctypes.c_float), ("block", ctypes.c_uint32),
-                ("use_graph", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
+                ("use_graph", ctypes.c_uint32), ("max_iterations", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 3)]
 
     def as_dict(self):
         return {"capacity": self.capacity, "regen_threshold": round(self.regen_threshold, 6), "block": self.block,
-                "use_graph": self.use_graph}
+                "use_graph": self.use_graph, "max_iterations": self.max_iterations}
 
 
 class BatchStats(ctypes.Structure):

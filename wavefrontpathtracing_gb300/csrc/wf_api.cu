@@ -12,6 +12,11 @@
 #include <string>
 #include <vector>
 
+#include <mutex>
+#include <unordered_map>
+
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/wf.h"
 #include "wf_bvh.h"
 #include "wf_ctx.h"
@@ -41,7 +46,7 @@ template <typename T>
 int dev_alloc(T** p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    cudaError_t e = dmalloc(reinterpret_cast<void**>(p), count * sizeof(T));
     if (e != cudaSuccess) {
         *p = nullptr;
         cudaGetLastError();
@@ -52,7 +57,7 @@ int dev_alloc(T** p, size_t count) {
 
 template <typename T>
 void dev_free(T*& p) {
-    if (p) cudaFree(const_cast<void*>(reinterpret_cast<const void*>(p)));
+    if (p) dfree(const_cast<void*>(reinterpret_cast<const void*>(p)));
     p = nullptr;
 }
 
@@ -93,6 +98,10 @@ struct EventPair {
 };
 
 enum Stage { ST_GENERATE = 0, ST_EXTEND, ST_SHADE, ST_CONNECT, ST_POST, ST_TLAS, ST_COUNT };
+// NVTX range names: the reference's GPU profiler scope labels (gpu_profiler.h:59-66)
+// plus the added connect stage.
+const char* const kStageLabel[ST_COUNT] = {"Wavefront Generate", "Wavefront Extend", "Wavefront Shade",
+                                           "Wavefront Connect", "Post-Process", "TLAS Build"};
 
 }  // namespace
 
@@ -107,6 +116,7 @@ struct wf_ctx {
     float env[3] = {1.0f, 1.0f, 1.0f};
     uint32_t env_texture = 0;
     uint32_t last_view_mode = 0;
+    uint32_t last_frame_seed = 0;
     std::vector<Texture> textures;          // id k + 1
     DevBuf<TexRef> tex_table;               // entry 0 unused
 
@@ -132,7 +142,8 @@ struct wf_ctx {
     RenderBuffers B{};
     float4* accum = nullptr;
     uint32_t accum_samples = 0;
-    unsigned long long* totals = nullptr;   // [0] extension rays, [1] shadow rays
+    unsigned long long* totals = nullptr;   // [0] extension rays, [1] shadow rays, [2 + d] extension
+                                            // rays at depth d, [2 + kMaxDepth + d] shadow rays at depth d
     DevBuf<float4> image;
     DevBuf<uchar4> image_ldr;
     DevBuf<uint8_t> trace_io;
@@ -172,12 +183,14 @@ cudaError_t d2h(wf_ctx* c, void* dst, const void* src, size_t bytes) {
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
 }
 
-// Records an event pair around a stage when profiling.
+// An NVTX range around a stage's enqueue (seen by Nsight Systems), and a CUDA
+// event pair around its GPU work when profiling.
 struct StageTimer {
     wf_ctx* c;
     cudaStream_t st;
     EventPair* ev = nullptr;
     StageTimer(wf_ctx* ctx, bool on, int stage, cudaStream_t stream = nullptr) : c(ctx), st(stream ? stream : ctx->stream) {
+        nvtxRangePushA(kStageLabel[stage]);
         if (!on) return;
         if (c->events_used == c->events.size()) {
             EventPair p{};
@@ -191,6 +204,7 @@ struct StageTimer {
     }
     ~StageTimer() {
         if (ev) cudaEventRecord(ev->b, st);
+        nvtxRangePop();
     }
 };
 
@@ -415,11 +429,15 @@ int finish_timing(wf_ctx* c) {
     c->stats.ms_connect = st[ST_CONNECT];
     c->stats.ms_post = st[ST_POST];
     c->stats.ms_tlas_build = st[ST_TLAS];
-    unsigned long long tot[2] = {0, 0};
+    unsigned long long tot[2 + 2 * kMaxDepth] = {};
     WF_CUDA(d2h(c, tot, c->totals, sizeof(tot)));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     c->stats.rays_extend = tot[0];
     c->stats.rays_connect = tot[1];
+    for (uint32_t d = 0; d < kMaxDepth; ++d) {
+        c->stats.extend_rays_depth[d] = tot[2 + d];
+        c->stats.shadow_rays_depth[d] = tot[2 + kMaxDepth + d];
+    }
     if (c->count_traffic) {
         Counters k[2];
         WF_CUDA(d2h(c, k, c->counters, sizeof(k)));
@@ -444,7 +462,7 @@ int begin_call(wf_ctx* c, bool count_traffic) {
     c->events_used = 0;
     c->launches = c->launches_extend = c->launches_connect = 0;
     c->count_traffic = count_traffic;
-    WF_CUDA(cudaMemsetAsync(c->totals, 0, 2 * sizeof(unsigned long long), c->stream));
+    WF_CUDA(cudaMemsetAsync(c->totals, 0, (2 + 2 * kMaxDepth) * sizeof(unsigned long long), c->stream));
     WF_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(Counters), c->stream));
     WF_CUDA(cudaEventRecord(c->t0, c->stream));
     return WF_OK;
@@ -462,6 +480,40 @@ int end_call(wf_ctx* c) {
 }  // namespace
 
 namespace wf {
+
+namespace {
+std::mutex g_mem_mutex;
+std::unordered_map<void*, size_t> g_mem_blocks;
+uint64_t g_mem_used = 0, g_mem_limit = 0;   // limit 0: none
+}  // namespace
+
+cudaError_t dmalloc(void** p, size_t bytes) {
+    *p = nullptr;
+    std::lock_guard<std::mutex> lock(g_mem_mutex);
+    if (g_mem_limit && g_mem_used + bytes > g_mem_limit) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return e;
+    }
+    g_mem_blocks[*p] = bytes;
+    g_mem_used += bytes;
+    return cudaSuccess;
+}
+
+void dfree(void* p) {
+    if (!p) return;
+    {
+        std::lock_guard<std::mutex> lock(g_mem_mutex);
+        auto it = g_mem_blocks.find(p);
+        if (it != g_mem_blocks.end()) {
+            g_mem_used -= it->second;
+            g_mem_blocks.erase(it);
+        }
+    }
+    cudaFree(p);
+}
+
 // Lets entry points defined in other translation units set wf_last_error().
 int report_error(int code, const char* msg) { return fail(code, msg); }
 
@@ -615,6 +667,19 @@ const char* wf_last_error(void) { return g_error.c_str(); }
 
 int wf_abi_version(void) { return WF_ABI_VERSION; }
 
+int wf_set_device_memory_limit(uint64_t bytes) {
+    std::lock_guard<std::mutex> lock(g_mem_mutex);
+    g_mem_limit = bytes;
+    return WF_OK;
+}
+
+int wf_get_device_memory_usage(uint64_t* bytes) {
+    if (!bytes) return fail(WF_ERR_INVALID, "wf_get_device_memory_usage: null argument");
+    std::lock_guard<std::mutex> lock(g_mem_mutex);
+    *bytes = g_mem_used;
+    return WF_OK;
+}
+
 int wf_create(const wf_init_params* p, wf_ctx** out) {
     if (!p || !out) return fail(WF_ERR_INVALID, "wf_create: null argument");
     *out = nullptr;
@@ -655,11 +720,11 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
     if (rc == WF_OK) rc = dev_alloc(&c->status, 1);
     if (rc == WF_OK) rc = dev_alloc(&c->counters, 2);
     if (rc == WF_OK) rc = dev_alloc(&c->trace_fetch, 1);
-    if (rc == WF_OK) rc = dev_alloc(&c->totals, 2);
+    if (rc == WF_OK) rc = dev_alloc(&c->totals, 2 + 2 * kMaxDepth);
     if (rc == WF_OK) {
         cudaMemset(c->status, 0, 4);
         cudaMemset(c->counters, 0, 2 * sizeof(Counters));
-        cudaMemset(c->totals, 0, 2 * sizeof(unsigned long long));
+        cudaMemset(c->totals, 0, (2 + 2 * kMaxDepth) * sizeof(unsigned long long));
         if (cudaDeviceSynchronize() != cudaSuccess) rc = fail(WF_ERR_CUDA, "wf_create: device initialization failed");
     }
     if (rc != WF_OK) {
@@ -1142,6 +1207,8 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
         }
     }
     if (pending) WF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_conn[W.max_bounces - 1], 0));
+    WF_CUDA(launch_depth_counts(B.counts, c->totals + 2, c->stream));
+    c->launches++;
     if (resolve) {
         {
             StageTimer t(c, P.prof, ST_POST);
@@ -1177,6 +1244,7 @@ int wf_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o,
         if ((rc = run_wave(c, P, wv, c->accum_samples, none, true))) return rc;
     c->accum_samples += o->spp;
     c->last_view_mode = s->render_view_mode;
+    c->last_frame_seed = frame_seed;
     c->stats.paths = (uint64_t)npix * o->spp;
     uint64_t paths = c->stats.paths;
     rc = end_call(c);
@@ -1291,6 +1359,70 @@ int wf_scene_set_emission(wf_ctx* c, uint32_t instance, float strength) {
     // rebuild the scene's device tables (instance data, TLAS, emitter table)
     c->in_scene = true;
     return wf_scene_end(c);
+}
+
+// ---------------------------------------------------------------------------- checkpoint / resume
+
+namespace {
+struct AccumHeader {
+    char magic[8];              // "WFACCUM1"
+    uint32_t width, height, samples, frame_seed;
+    view_t view;
+};
+}  // namespace
+
+int wf_save_accumulator(wf_ctx* c, const char* path) {
+    if (!c || !path) return fail(WF_ERR_INVALID, "wf_save_accumulator: null argument");
+    if (!c->buffers_ready || !c->view_valid) return fail(WF_ERR_STATE, "wf_save_accumulator: nothing rendered");
+    int rc = use_device(c);
+    if (rc) return rc;
+    const size_t npix = (size_t)c->width * c->height;
+    std::vector<float4> acc(npix);
+    WF_CUDA(d2h(c, acc.data(), c->accum, npix * sizeof(float4)));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    if ((rc = take_status(c))) return rc;
+    AccumHeader h{};
+    std::memcpy(h.magic, "WFACCUM1", 8);
+    h.width = c->width;
+    h.height = c->height;
+    h.samples = c->accum_samples;
+    h.frame_seed = c->last_frame_seed;
+    h.view = c->view;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(WF_ERR_INVALID, std::string("wf_save_accumulator: cannot open ") + path);
+    const bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(acc.data(), sizeof(float4), npix, f) == npix;
+    const bool closed = std::fclose(f) == 0;
+    if (!ok || !closed) return fail(WF_ERR_INVALID, std::string("wf_save_accumulator: write failed: ") + path);
+    return WF_OK;
+}
+
+int wf_load_accumulator(wf_ctx* c, const char* path, uint32_t* out_samples, uint32_t* out_frame_seed) {
+    if (!c || !path) return fail(WF_ERR_INVALID, "wf_load_accumulator: null argument");
+    if (!c->view_valid) return fail(WF_ERR_STATE, "wf_load_accumulator: call wf_scene_begin with the saved view first");
+    int rc = use_device(c);
+    if (rc) return rc;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(WF_ERR_INVALID, std::string("wf_load_accumulator: cannot open ") + path);
+    AccumHeader h{};
+    const size_t npix = (size_t)c->width * c->height;
+    std::vector<float4> acc(npix);
+    bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, "WFACCUM1", 8) == 0 &&
+              h.width == c->width && h.height == c->height;
+    if (ok) ok = std::fread(acc.data(), sizeof(float4), npix, f) == npix;
+    std::fclose(f);
+    if (!ok) return fail(WF_ERR_INVALID, "wf_load_accumulator: not an accumulator of this image size");
+    if (std::memcmp(&h.view, &c->view, sizeof(view_t)) != 0)
+        return fail(WF_ERR_INVALID, "wf_load_accumulator: the checkpoint was rendered from another view");
+    if ((rc = ensure_buffers(c))) return rc;
+    WF_CUDA(h2d(c, c->accum, acc.data(), npix * sizeof(float4)));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    c->accum_samples = h.samples;
+    c->last_frame_seed = h.frame_seed;
+    c->view_changed = false;
+    c->last_view_mode = RENDER_VIEW_MODE_NONE;
+    if (out_samples) *out_samples = h.samples;
+    if (out_frame_seed) *out_frame_seed = h.frame_seed;
+    return WF_OK;
 }
 
 int wf_read_image(wf_ctx* c, float* out, uint64_t nfloat) {

@@ -360,7 +360,7 @@ struct DBuf {
         if (n == 0) n = 1;
         if (n <= cap && p) return WF_OK;
         release();
-        if (cudaMalloc(reinterpret_cast<void**>(&p), n * sizeof(T)) != cudaSuccess) {
+        if (dmalloc(reinterpret_cast<void**>(&p), n * sizeof(T)) != cudaSuccess) {
             cudaGetLastError();
             p = nullptr;
             return fail_code(WF_ERR_OOM, "wf_batch: device allocation of " + std::to_string(n * sizeof(T)) +
@@ -370,7 +370,7 @@ struct DBuf {
         return WF_OK;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) dfree(p);
         p = nullptr;
         cap = 0;
     }
@@ -569,7 +569,7 @@ int ensure_pool(wf_batch* b) {
     for (int k = 0; k < 2; ++k)
         if ((rc = b->s_o[k].reserve(C)) || (rc = b->s_d[k].reserve(C)) || (rc = b->s_c[k].reserve(C))) return rc;
     if (!b->ctl) {
-        if (cudaMalloc(&b->ctl, sizeof(BatchCtl)) != cudaSuccess) {
+        if (dmalloc(reinterpret_cast<void**>(&b->ctl), sizeof(BatchCtl)) != cudaSuccess) {
             cudaGetLastError();
             b->ctl = nullptr;
             return fail_code(WF_ERR_OOM, "wf_batch: control block allocation failed");
@@ -768,6 +768,7 @@ int render(wf_batch* b, const render_settings_t* s, const wf_render_options* o, 
     const double per_admit = std::max(1.0, (double)h.capacity - (double)h.threshold + 1.0);
     const double bound = (std::ceil((double)h.total / per_admit) + 2.0) * (s->max_bounces + 2.0) + 1024.0;
     h.max_iter = (uint32_t)std::min(bound, 2.0e9);
+    if (b->cfg.max_iterations) h.max_iter = std::min(h.max_iter, b->cfg.max_iterations);
     BCUDA(ctx_h2d(c, b->ctl, &h, sizeof(BatchCtl)));
     BCUDA(cudaEventRecord(b->t0, st));
     uint64_t graph_launches = 0;
@@ -871,7 +872,7 @@ int wf_batch_destroy(wf_batch* b) {
         if (b->ev_conn[k]) cudaEventDestroy(b->ev_conn[k]);
     }
     if (b->side) cudaStreamDestroy(b->side);
-    if (b->ctl) cudaFree(b->ctl);
+    if (b->ctl) dfree(b->ctl);
     if (b->ctl_host) cudaFreeHost(b->ctl_host);
     if (b->t0) cudaEventDestroy(b->t0);
     if (b->t1) cudaEventDestroy(b->t1);

@@ -714,13 +714,13 @@ struct Pool {
     T* get(size_t count) {
         void* p = nullptr;
         if (err != cudaSuccess) return nullptr;
-        err = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        err = dmalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
         if (err != cudaSuccess) return nullptr;
         blocks.push_back(p);
         return static_cast<T*>(p);
     }
     ~Pool() {
-        for (void* p : blocks) cudaFree(p);
+        for (void* p : blocks) dfree(p);
     }
 };
 
@@ -877,9 +877,9 @@ int gpu_bvh_build(const triangle_t* tris, uint32_t n, const wf_bvh_options& o, c
     const uint32_t nc = 2 + 2 * internal;
     float4* d_nodes = nullptr;
     float4* d_tris = nullptr;
-    BVH_CUDA(cudaMalloc(&d_nodes, 32ull * nc));
-    if (cudaMalloc(&d_tris, 48ull * n) != cudaSuccess) {
-        cudaFree(d_nodes);
+    BVH_CUDA(dmalloc(reinterpret_cast<void**>(&d_nodes), 32ull * nc));
+    if (dmalloc(reinterpret_cast<void**>(&d_tris), 48ull * n) != cudaSuccess) {
+        dfree(d_nodes);
         cudaGetLastError();
         g_err = "gpu_bvh_build: cudaMalloc failed";
         return WF_ERR_OOM;
@@ -897,8 +897,8 @@ int gpu_bvh_build(const triangle_t* tris, uint32_t n, const wf_bvh_options& o, c
         e = cudaMemcpyAsync(blob + 12 + nodes_bytes + tri_bytes, C.idx, idx_bytes, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
-        cudaFree(d_nodes);
-        cudaFree(d_tris);
+        dfree(d_nodes);
+        dfree(d_tris);
         g_err = std::string("gpu_bvh_build: ") + cudaGetErrorString(e);
         return WF_ERR_CUDA;
     }

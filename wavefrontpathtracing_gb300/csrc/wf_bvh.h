@@ -20,4 +20,8 @@ int gpu_bvh_build(const triangle_t* tris, uint32_t n, const wf_bvh_options& opts
                   BvhBuildOut* out);
 const char* bvh_last_error();
 
+// The library's accounted device allocator (wf_api.cu).
+cudaError_t dmalloc(void** p, size_t bytes);
+void dfree(void* p);
+
 }  // namespace wf

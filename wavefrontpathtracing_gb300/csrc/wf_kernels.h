@@ -98,6 +98,9 @@ cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t 
 // counter (zeroed here), totals[0..1] += extension / shadow rays.
 cudaError_t launch_megakernel(const SceneRefs& S, const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W,
                               uint32_t* fetch, unsigned long long* totals, cudaStream_t stream);
+// per_depth[d] += counts[d] for the wave's extension (d < kMaxDepth) and shadow
+// (kMaxDepth + d) ray counts.
+cudaError_t launch_depth_counts(const uint32_t* counts, unsigned long long* per_depth, cudaStream_t stream);
 // Adds each pixel's paths of the wave to the accumulator in sample order.
 cudaError_t launch_wave_resolve(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream);
 // post_process.hlsl:25-72 for a render view mode (tonemap only for mode 0,
@@ -114,6 +117,11 @@ cudaError_t launch_tlas_build(const float* aabbs /* 6 floats per instance */, ui
                               uint32_t* scratch, uint32_t metric, cudaStream_t stream);
 
 int sm_count();
+// Device allocations of the library go through these: they enforce the
+// process-wide limit set by wf_set_device_memory_limit (an allocation past it
+// fails with cudaErrorMemoryAllocation without reaching the driver).
+cudaError_t dmalloc(void** p, size_t bytes);
+void dfree(void* p);
 // Sets the calling thread's wf_last_error() message; returns code.
 int report_error(int code, const char* msg);
 

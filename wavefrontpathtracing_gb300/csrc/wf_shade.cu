@@ -174,6 +174,18 @@ cudaError_t launch_reduce_replicas(float4* g, uint32_t triangles, uint32_t repli
     return cudaGetLastError();
 }
 
+namespace {
+__global__ void k_depth_counts(const uint32_t* counts, unsigned long long* per_depth) {
+    const uint32_t d = threadIdx.x;
+    if (d < 2 * kMaxDepth) per_depth[d] += counts[d];
+}
+}  // namespace
+
+cudaError_t launch_depth_counts(const uint32_t* counts, unsigned long long* per_depth, cudaStream_t stream) {
+    k_depth_counts<<<1, 2 * kMaxDepth, 0, stream>>>(counts, per_depth);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_wave_resolve(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream) {
     k_wave_resolve<<<grid_for(W.np), kBlock, 0, stream>>>(B, W);
     return cudaGetLastError();
