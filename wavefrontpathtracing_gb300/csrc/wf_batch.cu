@@ -21,8 +21,9 @@
 // extend (shadow queues, counts and hand-out counters alternate by iteration
 // parity); the next shade waits for it.
 //
-// Camera paths are numbered scene by scene, sample-major inside a scene
-// (path = path_base + sample * pixels + pixel), and admitted in that order.  A
+// Camera paths are numbered scene by scene, pixel-major inside a scene
+// (path = path_base + pixel * spp + sample, so a pixel's identical camera rays
+// share a warp), and admitted in that order.  A
 // path's random numbers are keyed by (scene-local pixel, sample, depth) as in
 // wf_render, its radiance is summed in the same order, and each finished path
 // stores its radiance at its own index; the resolve adds a pixel's samples in
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(BLOCK) k_bregen(const BatchScene* sc, const ui
         const uint32_t s = scene_of(pbase, ns, g);
         const BatchScene& S = sc[s];
         const uint32_t local = g - S.path_base;
-        const uint32_t sample = local / S.np, pixel = local - sample * S.np;
+        const uint32_t pixel = local / S.spp, sample = local - pixel * S.spp;
         V3 o, d;
         primary_ray(S, pixel % S.width, pixel / S.width, o, d);
         const uint32_t slot = s0 + j;
@@ -263,7 +264,7 @@ __global__ void __launch_bounds__(BLOCK) k_bshade(ShadeRefs SH, const BatchScene
                 L4.z = L4.z + o.add.z;
             }
             if (!o.enqueue) {
-                gidx = S.path_base + in.sample * S.np + pixel;
+                gidx = S.path_base + pixel * S.spp + in.sample;
                 Q.out_L[gidx] = L4;
             }
         }
@@ -314,7 +315,7 @@ __global__ void k_bresolve(const BatchScene* sc, const uint32_t* pixbase, uint32
         const uint32_t p = q - S.pix_base;
         float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         for (uint32_t k = 0; k < S.spp; ++k) {
-            const float4 L = out_L[(size_t)S.path_base + (size_t)k * S.np + p];
+            const float4 L = out_L[(size_t)S.path_base + (size_t)p * S.spp + k];
             acc.x = acc.x + L.x;
             acc.y = acc.y + L.y;
             acc.z = acc.z + L.z;

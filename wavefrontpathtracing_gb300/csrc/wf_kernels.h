@@ -70,8 +70,10 @@ struct WaveParams {
     float4 view_to_world[4];
     uint32_t width, height;     // image size (pixel index -> x, y)
     float dim_x, dim_y;         // view_t.render_dim (uv of the primary ray)
-    // A wave holds samples [s0, s0 + nsamples) of pixels [pix0, pix0 + np):
-    // path p is sample s0 + p / np of pixel pix0 + p % np; npaths = nsamples * np.
+    // A wave holds samples [s0, s0 + nsamples) of pixels [pix0, pix0 + np),
+    // pixel-major: path p is sample s0 + p % nsamples of pixel pix0 + p / nsamples
+    // (npaths = nsamples * np), so the identical camera rays of a pixel's
+    // samples share a warp and traverse in lockstep.
     uint32_t pix0, np, s0, nsamples, npaths;
     uint32_t frame_seed;
     uint32_t max_bounces, nee, rr_start, cosine;

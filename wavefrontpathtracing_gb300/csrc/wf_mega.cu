@@ -36,8 +36,8 @@ __global__ void __launch_bounds__(kMegaBlock) k_mega(SceneRefs S, ShadeRefs SH, 
         if (base >= W.npaths) break;
         const uint32_t path = base + lane;
         if (path < W.npaths) {
-            const uint32_t pixel = W.pix0 + path % W.np;
-            const uint32_t sample = W.s0 + path / W.np;
+            const uint32_t pixel = W.pix0 + path / W.nsamples;
+            const uint32_t sample = W.s0 + path % W.nsamples;
             V3 ro, rd;
             primary_ray(W, pixel % W.width, pixel / W.width, ro, rd);
             V3 T = mk(1.0f, 1.0f, 1.0f);

@@ -22,7 +22,7 @@ unsigned grid_for(uint32_t n) {
 __global__ void __launch_bounds__(kBlock) k_generate(RenderBuffers B, WaveParams W) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W.npaths; p += stride) {
-        const uint32_t pixel = W.pix0 + p % W.np;
+        const uint32_t pixel = W.pix0 + p / W.nsamples;
         V3 o, d;
         primary_ray(W, pixel % W.width, pixel / W.width, o, d);
         B.q_o[0][p] = make_float4(o.x, o.y, o.z, __uint_as_float(0u));
@@ -64,8 +64,8 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
             in.T = xyz(T4);
             in.last_pdf = T4.w;
             in.flags = B.ps_flags[path];
-            in.pixel = W.pix0 + path % W.np;
-            in.sample = W.s0 + path / W.np;
+            in.pixel = W.pix0 + path / W.nsamples;
+            in.sample = W.s0 + path % W.nsamples;
             in.depth = depth;
             shade_one(SH, K, in, A, path, in.pixel, o);
             if (o.has_add) {
@@ -126,7 +126,7 @@ __global__ void k_wave_resolve(RenderBuffers B, WaveParams W) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W.np; p += stride) {
         float4 acc = B.accum[W.pix0 + p];
         for (uint32_t s = 0; s < W.nsamples; ++s) {
-            const float4 L = B.ps_L[(size_t)s * W.np + p];
+            const float4 L = B.ps_L[(size_t)p * W.nsamples + s];
             acc.x = acc.x + L.x;
             acc.y = acc.y + L.y;
             acc.z = acc.z + L.z;
