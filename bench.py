@@ -449,6 +449,7 @@ def run_ours(args, rank, world, local):
     ms_per_launch = ext_ms / max(1, ext_launches)
     achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
+    traffic = ncu_traffic()
     # --- end to end through the C ABI with host buffers
     img = np.zeros((H, W, 4), dtype=np.float32)
     inst_mesh = np.array([ids[m] for m, _, _ in desc.instances], dtype=np.uint32)
@@ -511,9 +512,12 @@ def run_ours(args, rank, world, local):
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": round(achieved, 1),
                              "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                             "frac": round(achieved / peak, 4), "traffic": ncu_traffic(),
+                             "frac": round(achieved / peak, 4), "traffic": traffic,
                              "alg_bytes_per_launch": int(bytes_per_launch),
-                             "ms_per_launch": round(ms_per_launch, 4)},
+                             "ms_per_launch": round(ms_per_launch, 4),
+                             # DRAM bytes actually moved (ncu, per launch) over the live launch time
+                             "dram_gbs": round(traffic / (ms_per_launch / 1e3) / 1e9, 1) if traffic else None,
+                             "dram_frac": round(traffic / (ms_per_launch / 1e3) / 1e9 / peak, 4) if traffic else None},
                 "clocks": clk.summary()}
         if cpu:
             line["cpu_baseline"] = cpu
