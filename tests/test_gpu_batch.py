@@ -111,7 +111,7 @@ def test_batch_autotune_picks_a_valid_config(batch_case):
     with Renderer(8, 8) as r:
         b = make_batch(r, meshes, descs)
         cfg = b.autotune(frame_seed=SEED, **RENDER)
-        assert cfg["capacity"] in (1 << 19, 1 << 20, 1 << 21, 1 << 22, 1 << 23)
+        assert cfg["capacity"] in (1 << 19, 1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24)
         assert round(cfg["regen_threshold"], 4) in (0.5, 0.75, 0.9, 1.0)
         assert cfg["block"] in (128, 256, 512)
         assert b.config() == cfg

@@ -972,7 +972,7 @@ int wf_batch_autotune(wf_batch* b, const render_settings_t* s, const wf_render_o
     }
     uint64_t tp = 0;
     for (const HostScene& H : b->scenes) tp += (uint64_t)H.width * H.height * H.spp;
-    const uint32_t caps[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22, 1u << 23};
+    const uint32_t caps[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
     wf_batch_config base = best;
     for (uint32_t cap : caps) {
         if (cap == base.capacity) continue;
