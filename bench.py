@@ -41,6 +41,7 @@ L2_BYTES = 256 << 20
 # algorithmic bytes per extend ray, reference layouts: ray 32 + hit 20, and per
 # fetch: TLAS node 32, bvh_instance_t 92, BLAS node 32, triangle 36 + index 4
 B_RAY, B_HIT, B_TNODE, B_INST, B_BNODE, B_TRI = 32, 20, 32, 92, 32, 40
+B_SRAY = 32   # a shadow ray's origin/tmax and direction/path (its contribution is read only when unoccluded)
 
 
 def dist_env():
@@ -402,7 +403,7 @@ def run_ours(args, rank, world, local):
 
     def frame(seed, profile):
         r.render(max_bounces=DEPTH, spp=SPP, frame_seed=seed, nee=1, rr_start_depth=RR, accumulate=False,
-                 profile=profile)
+                 profile=profile, fused_connect=args.fused_connect)
         return r.stats()
 
     for i in range(args.warmup):
@@ -445,7 +446,12 @@ def run_ours(args, rank, world, local):
     c = r.stats()
     alg_bytes = (c["rays_extend"] * (B_RAY + B_HIT) + c["tlas_node_loads"] * B_TNODE + c["instance_loads"] * B_INST
                  + c["blas_node_loads"] * B_BNODE + c["triangle_tests"] * B_TRI)
-    bytes_per_launch = alg_bytes / max(1, c["launches_extend"])
+    if args.fused_connect:
+        # the traversal launches also carry the previous depth's shadow rays
+        alg_bytes += (c["rays_connect"] * B_SRAY + c["shadow_tlas_node_loads"] * B_TNODE
+                      + c["shadow_instance_loads"] * B_INST + c["shadow_blas_node_loads"] * B_BNODE
+                      + c["shadow_triangle_tests"] * B_TRI)
+    bytes_per_launch = alg_bytes / max(1, ext_launches / args.steps)
     ms_per_launch = ext_ms / max(1, ext_launches)
     achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
@@ -464,7 +470,7 @@ def run_ours(args, rank, world, local):
         r.submit_render_meshes(inst_mesh, inst_xf, inst_mat)
         r.end_scene()
         r.render(max_bounces=DEPTH, spp=SPP, frame_seed=frame_seed(i, rank), nee=1, rr_start_depth=RR,
-                 accumulate=False)
+                 accumulate=False, fused_connect=args.fused_connect)
         wf.check(r.L.wf_read_image(r.h, wf.abi.ptr(img), img.size))
         s = r.stats()
         e2e_rays += s["rays_extend"] + s["rays_connect"]
@@ -510,7 +516,10 @@ def run_ours(args, rank, world, local):
                                 "shadow": [int(x) for x in last["shadow_rays_depth"][:DEPTH]]},
                 "e2e": {"value": round(e2e_value, 3) if e2e_value else None, "unit": "Mrays/s",
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-                "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": round(achieved, 1),
+                "roofline": {"bound": "hbm",
+                             "kernel": ("k_trace_pair (extend d + shadow rays d-1)" if args.fused_connect
+                                        else "k_trace (extend)"),
+                             "achieved": round(achieved, 1),
                              "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                              "frac": round(achieved / peak, 4), "traffic": traffic,
                              "alg_bytes_per_launch": int(bytes_per_launch),
@@ -622,6 +631,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes leg")
     ap.add_argument("--no-megakernel", action="store_true", help="skip the megakernel A/B leg")
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--fused-connect", action="store_true",
+                    help="shadow rays of depth d in one launch with the extension rays of depth d + 1")
     ap.add_argument("--workload", default="instanced", choices=["instanced", "traversal", "batched"])
     ap.add_argument("--soup-triangles", type=int, default=8_000_000)
     ap.add_argument("--soup-side", type=int, default=4096, help="rays per set = side^2")

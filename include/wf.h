@@ -105,8 +105,21 @@ typedef struct wf_render_options {
     uint32_t wave_paths;     /* paths per wave, <= context capacity; 0 = capacity */
     uint32_t profile;        /* 1 = time every stage with CUDA events (wf_get_stats) */
     uint32_t count_traffic;  /* 1 = count node/instance/triangle fetches (slower) */
-    uint32_t reserved[2];
+    /* how the shadow rays of depth d are traced (next-event estimation on):
+     * WF_SCHEDULE_SEPARATE (0) = their own launch on a second stream beside
+     * the extension rays of depth d + 1; WF_SCHEDULE_FUSED (1) = in one
+     * persistent launch with the extension rays of depth d + 1 (ms_extend then
+     * includes them, ms_connect is 0, and the launch counts in both
+     * launches_extend and launches_connect).  Images are identical.
+     * count_traffic uses the separate schedule. */
+    uint32_t trace_schedule;
+    uint32_t reserved[1];
 } wf_render_options;
+
+enum wf_trace_schedule {
+    WF_SCHEDULE_SEPARATE = 0,
+    WF_SCHEDULE_FUSED = 1
+};
 
 enum wf_trace_flags {
     WF_TRACE_ANY_HIT = 1u,       /* stop at the first accepted hit (shadow-ray query) */

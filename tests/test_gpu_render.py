@@ -6,9 +6,12 @@ same float operations, and every pixel receives its contributions in the same
 order, so the accumulated images are compared bit for bit, together with the
 number of rays traced per call.  The FP64 oracle bounds the error of the FP32
 arithmetic itself (image RMSE, tolerance written in the test)."""
+import ctypes
+
 import numpy as np
 import pytest
 
+import wavefrontpathtracing_gb300 as wf
 from wavefrontpathtracing_gb300 import Renderer, scenes
 from tests.helpers import load_scene_into, oracle_scene_from_renderer
 
@@ -146,6 +149,33 @@ def test_megakernel_equals_wavefront(orc, name):
     assert_images_equal(mega, wave)
     assert sm["rays_extend"] == sw["rays_extend"] and sm["rays_connect"] == sw["rays_connect"]
     assert sm["launches"] < sw["launches"]
+
+
+@pytest.mark.parametrize("wave_paths", [0, 1000])
+def test_fused_and_separate_connect_agree(orc, wave_paths):
+    """The shadow rays of depth d traced in their own launches on a second
+    stream (the default) or in one launch with the extension rays of depth
+    d + 1: the same rays, the same image bit for bit, fewer launches when
+    fused."""
+    desc = scenes.instanced_scene(width=64, height=36, instances=48, freqs=(6, 9), spp=2, max_bounces=6)
+    kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=3, wave_paths=wave_paths)
+    with Renderer(desc.width, desc.height) as r:
+        load_scene_into(r, desc)
+        r.render(frame_seed=33, accumulate=False, fused_connect=True, **kw)
+        fused = r.read_image()
+        sf = r.stats()
+        r.render(frame_seed=33, accumulate=False, **kw)
+        sep = r.read_image()
+        ss = r.stats()
+        with pytest.raises(wf.WFError):
+            o = wf.abi.RenderOptions(1, 1, 0xFFFFFFFF, 0, 0, 0, 2)
+            s = wf.abi.RenderSettings(1, 1, 0, 2, 1, 0, 1.0)
+            wf.check(r.L.wf_render(r.h, ctypes.byref(s), ctypes.byref(o), 1))
+    assert sf["rays_connect"] > 0
+    assert_images_equal(fused, sep)
+    for k in ("rays_extend", "rays_connect", "extend_rays_depth", "shadow_rays_depth"):
+        assert np.array_equal(np.asarray(sf[k]), np.asarray(ss[k])), k
+    assert sf["launches"] < ss["launches"]
 
 
 def test_submit_many_equals_one_by_one(orc):

@@ -73,12 +73,14 @@ class Env(ctypes.Structure):
 
 
 TEXTURE_RGBA8, TEXTURE_RGBA8_SRGB, TEXTURE_RG8, TEXTURE_RGBA32F = 0, 1, 2, 3
+SCHEDULE_SEPARATE, SCHEDULE_FUSED = 0, 1
 
 
 class RenderOptions(ctypes.Structure):
     _fields_ = [("spp", ctypes.c_uint32), ("nee", ctypes.c_uint32), ("rr_start_depth", ctypes.c_uint32),
                 ("wave_paths", ctypes.c_uint32), ("profile", ctypes.c_uint32),
-                ("count_traffic", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+                ("count_traffic", ctypes.c_uint32), ("trace_schedule", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 1)]
 
 
 class Stats(ctypes.Structure):

@@ -1085,7 +1085,7 @@ struct Pass {
     SceneRefs S;
     ShadeRefs SH;
     RenderBuffers B;
-    bool nee, prof, cnt, mega;
+    bool nee, prof, cnt, mega, fused;
 };
 
 int validate_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o, const char* who) {
@@ -1095,6 +1095,8 @@ int validate_render(wf_ctx* c, const render_settings_t* s, const wf_render_optio
     if (o->spp == 0) return fail(WF_ERR_INVALID, std::string(who) + ": spp must be >= 1");
     if (s->render_view_mode >= RENDER_VIEW_MODE_COUNT)
         return fail(WF_ERR_INVALID, std::string(who) + ": unknown render_view_mode");
+    if (o->trace_schedule > WF_SCHEDULE_FUSED)
+        return fail(WF_ERR_INVALID, std::string(who) + ": unknown trace_schedule");
     return WF_OK;
 }
 
@@ -1141,6 +1143,8 @@ Pass make_pass(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     P.prof = o->profile != 0;
     P.mega = s->use_wavefront_pathtracing == 0;
     P.cnt = o->count_traffic != 0;
+    // traffic counting keeps per-kind counters, so it traces the kinds apart
+    P.fused = P.nee && !P.cnt && o->trace_schedule == WF_SCHEDULE_FUSED;
     return P;
 }
 
@@ -1177,7 +1181,12 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
     c->launches++;
     bool pending = false;   // a connect on the side stream not yet joined
     for (uint32_t d = 0; d <= W.max_bounces; ++d) {
-        {
+        if (P.fused && d > 0) {
+            // the shadow rays of depth d - 1 with the extension rays of depth d
+            StageTimer t(c, P.prof, ST_EXTEND);
+            WF_CUDA(launch_trace_pair(P.S, B, d, c->totals, c->stream));
+            c->launches_connect++;
+        } else {
             StageTimer t(c, P.prof, ST_EXTEND);
             WF_CUDA(launch_extend(P.S, B, d, W.npaths, P.cnt, c->totals, c->stream));
         }
@@ -1192,7 +1201,7 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
         }
         c->launches += 2;
         c->launches_extend++;
-        if (P.nee && d < W.max_bounces) {
+        if (P.nee && !P.fused && d < W.max_bounces) {
             // the shadow rays of depth d overlap the extension rays of depth d + 1
             WF_CUDA(cudaEventRecord(c->ev_shade[d], c->stream));
             WF_CUDA(cudaStreamWaitEvent(c->side, c->ev_shade[d], 0));

@@ -95,6 +95,10 @@ cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const Wave
                          uint32_t max_rays, const AdjointRefs& A, cudaStream_t stream);
 cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
                            bool count, unsigned long long* total, cudaStream_t stream);
+// The shadow rays of depth - 1 and the extension rays of depth in one launch
+// (depth >= 1); totals[0] / totals[1] count the extension / shadow rays.
+cudaError_t launch_trace_pair(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, unsigned long long* totals,
+                              cudaStream_t stream);
 // The megakernel (use_wavefront_pathtracing = 0): whole paths per thread, each
 // path's radiance left in ps_L like the wavefront stages; fetch = a device
 // counter (zeroed here), totals[0..1] += extension / shadow rays.

@@ -53,6 +53,43 @@ struct ConnectIO {
     }
 };
 
+// The shadow rays of depth d and the extension rays of depth d + 1 in one
+// persistent launch: both queues are complete once shade(d) has run, and one
+// shared pool of rays keeps every warp busy until the last ray of either kind
+// instead of leaving two half-empty tails.  Rays [0, n_first) are shadow rays
+// (any hit), the rest extension rays (closest hit); each is loaded, traced
+// and stored exactly as in its own launch.
+struct PairIO {
+    ConnectIO c;
+    ExtendIO e;
+    uint32_t n_first;
+    __device__ __forceinline__ bool any(uint32_t i) const { return i < n_first; }
+    __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
+        if (i < n_first) c.load(i, o, d, tmax, nc);
+        else e.load(i - n_first, o, d, tmax, nc);
+    }
+    __device__ __forceinline__ uint32_t root(uint32_t, const SceneRefs& S) const { return S.inst_count ? 0u : kInvalid; }
+    __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool ok) const {
+        if (i < n_first) c.store(i, h, ok);
+        else e.store(i - n_first, h, ok);
+    }
+};
+
+__global__ void __launch_bounds__(kTraceBlock, WF_TRACE_MIN_BLOCKS)
+    k_trace_pair(SceneRefs S, PairIO io, const uint32_t* n_shadow, const uint32_t* n_extend, uint32_t* fetch,
+                 uint32_t* status, unsigned long long* totals) {
+    io.n_first = *n_shadow;
+    const uint32_t ne = *n_extend;
+    if (totals && blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(&totals[0], (unsigned long long)ne);
+        atomicAdd(&totals[1], (unsigned long long)io.n_first);
+    }
+    LocalCounters c = {0, 0, 0, 0};
+    bool overflow = false;
+    trace_persistent<false, false>(S, io, io.n_first + ne, fetch, c, overflow);
+    if (overflow) atomicOr(status, ERRF_STACK);
+}
+
 template <bool ANY, bool COUNT, class IO>
 cudaError_t launch(const SceneRefs& S, const IO& io, const uint32_t* count_ptr, uint32_t count, uint32_t* fetch,
                    uint32_t* status, Counters* counters, unsigned long long* total, cudaStream_t stream) {
@@ -107,6 +144,19 @@ cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t 
                                       stream)
                  : launch<true, false>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, B.counters + 1, total,
                                        stream);
+}
+
+cudaError_t launch_trace_pair(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, unsigned long long* totals,
+                              cudaStream_t stream) {
+    PairIO io;
+    const int par = (depth - 1) & 1, cur = depth & 1;
+    io.c.so = B.s_o[par]; io.c.sd = B.s_d[par]; io.c.sc = B.s_c[par]; io.c.L = B.ps_L;
+    io.e.qo = B.q_o[cur]; io.e.qd = B.q_d[cur]; io.e.tuvp = B.h_tuvp; io.e.inst = B.h_inst;
+    io.n_first = 0;
+    uint32_t* fetch = B.counts + 2 * kMaxDepth + depth;
+    k_trace_pair<<<persistent_grid(k_trace_pair), kTraceBlock, 0, stream>>>(
+        S, io, B.counts + kMaxDepth + depth - 1, B.counts + depth, fetch, B.status, totals);
+    return cudaGetLastError();
 }
 
 }  // namespace wf

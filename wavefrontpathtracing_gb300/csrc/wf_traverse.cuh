@@ -20,6 +20,7 @@
 // Lanes whose ray finished take new rays in groups through one atomic per warp
 // (kRefill idle lanes, or all of them) from a per-launch counter.
 #pragma once
+#include <type_traits>
 #include "wf_device.cuh"
 
 namespace wf {
@@ -57,7 +58,14 @@ constexpr int kRefill = WF_TRACE_REFILL;
 
 // Ray sources / sinks.  load(i, o, d, tmax, no_cull); root(i, S) = the TLAS
 // root node of the ray's scene, kInvalid for an empty scene; store(i, hit, ok)
-// where ok is false when a traversal stack overflowed.
+// where ok is false when a traversal stack overflowed.  A source that mixes
+// closest-hit and any-hit rays in one launch also has any(i) (true for an
+// any-hit ray); the others take the kernel's ANY for every ray.
+template <class IO, class = void>
+struct MixedIO : std::false_type {};
+template <class IO>
+struct MixedIO<IO, std::void_t<decltype(std::declval<const IO&>().any(0u))>> : std::true_type {};
+
 struct AosIO {
     const float4* rays;   // RayDesc2
     uint32_t* hits;       // hit_result_t
@@ -89,6 +97,7 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
     __shared__ float s_t[kTraceBlock], s_u[kTraceBlock], s_v[kTraceBlock];
     uint32_t ri = kNoRay;
     bool exhausted = false;
+    bool any_ray = ANY;   // this lane's ray stops at its first hit
     // current-space ray and 1/dir; ct = ray.t (the closest hit so far, shared
     // by world and object space because instance rays are not renormalised)
     V3 co = mk(0, 0, 0), cd = mk(0, 0, 0), ci = mk(0, 0, 0);
@@ -146,6 +155,7 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                     if (k < n) {
                         ri = k;
                         io.load(k, co, cd, ct, no_cull);
+                        if constexpr (MixedIO<IO>::value) any_ray = io.any(k);
                         s_wo[col] = make_float4(co.x, co.y, co.z, 0.0f);
                         s_wd[col] = make_float4(cd.x, cd.y, cd.z, 0.0f);
                         clear_hit();
@@ -203,7 +213,7 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                 s_prim[col] = __float_as_uint(a.w);
                 s_u[col] = bu; s_v[col] = bv;
                 hit_here = true;
-                if (ANY) { s_inst[col] = ii; s_t[col] = ct; finish = true; }
+                if (any_ray) { s_inst[col] = ii; s_t[col] = ct; finish = true; }
             }
             w0++;
             w1--;
