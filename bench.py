@@ -512,6 +512,14 @@ def run_ours(args, rank, world, local):
                 "rays_per_step": rays // args.steps,
                 "gpu_launches": launches,
                 "stages_ms": {k: round(last[f"ms_{k}"], 3) for k in ("generate", "extend", "shade", "connect", "post")},
+                "traversal_per_ray": {
+                    "extend": {"nodes": round((c["tlas_node_loads"] + c["blas_node_loads"]) / max(1, c["rays_extend"]), 1),
+                               "instances": round(c["instance_loads"] / max(1, c["rays_extend"]), 2),
+                               "triangles": round(c["triangle_tests"] / max(1, c["rays_extend"]), 2)},
+                    "shadow": {"nodes": round((c["shadow_tlas_node_loads"] + c["shadow_blas_node_loads"])
+                                              / max(1, c["rays_connect"]), 1),
+                               "instances": round(c["shadow_instance_loads"] / max(1, c["rays_connect"]), 2),
+                               "triangles": round(c["shadow_triangle_tests"] / max(1, c["rays_connect"]), 2)}},
                 "queue_sizes": {"extend": [int(x) for x in last["extend_rays_depth"][:DEPTH + 1]],
                                 "shadow": [int(x) for x in last["shadow_rays_depth"][:DEPTH]]},
                 "e2e": {"value": round(e2e_value, 3) if e2e_value else None, "unit": "Mrays/s",
@@ -547,8 +555,9 @@ def run_traversal(args, rank, world, local):
     """Traversal micro-benchmark: 8M soup triangles (centroids uniform in the
     unit cube, log-normal edges mu=-5 sigma=0.5, seed 7), one BLAS (16 bins,
     <= 4 triangles per leaf) under a 1-instance TLAS; 16.8M coherent pinhole
-    rays (4096^2) and 16.8M incoherent rays (origins in the cube, uniform
-    directions); closest hit and any hit (tmax U[0,1]).  Prints one JSON line
+    rays (4096^2, camera 0.5 in front of the cube, 90-degree field of view)
+    and 16.8M incoherent rays (origins in the cube, uniform directions);
+    closest hit and any hit (tmax U[0,1]).  Prints one JSON line
     per ray set / query kind (the headline line is the default workload)."""
     import torch
     import wavefrontpathtracing_gb300 as wf
@@ -564,7 +573,7 @@ def run_traversal(args, rank, world, local):
         t0 = time.perf_counter()
         mesh = r.create_mesh_from_triangles(tris, interval_count=16, max_leaf_prims=4)
         build_s = time.perf_counter() - t0
-        r.begin_scene(scenes.make_view((0.5, 0.5, -1.0), (0.5, 0.5, 0.5), 60.0, 16, 16))
+        r.begin_scene(scenes.make_view((0.5, 0.5, -0.5), (0.5, 0.5, 0.5), 90.0, 16, 16))
         r.submit_render_mesh(mesh, np.eye(4))
         r.end_scene()
         blas_bytes = len(r.mesh_blas(mesh))

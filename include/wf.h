@@ -130,6 +130,8 @@ enum wf_trace_flags {
 /* Counters and timings of the most recent wf_render / wf_trace call. */
 typedef struct wf_stats {
     double   ms_total;       /* GPU time of the whole call (CUDA events) */
+    /* per stage; the wavefront path makes its camera rays inside the depth-0
+     * extend launch, so ms_generate is 0 there */
     double   ms_generate, ms_extend, ms_shade, ms_connect, ms_post, ms_tlas_build;
     uint64_t launches;       /* kernels this library launched */
     uint64_t launches_extend, launches_connect;

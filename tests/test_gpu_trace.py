@@ -119,7 +119,7 @@ def test_triangle_soup_microbench_small(orc):
     with Renderer(16, 16) as r:
         blob = orc.bvh_build(tris, 16, False, 4)
         m = r.create_mesh_prebuilt(tris, blob)
-        r.begin_scene(scenes.make_view((0.5, 0.5, -1), (0.5, 0.5, 0.5), 60, 16, 16))
+        r.begin_scene(scenes.make_view((0.5, 0.5, -0.5), (0.5, 0.5, 0.5), 90, 16, 16))
         r.submit_render_mesh(m, np.eye(4))
         r.end_scene()
         for kind in ("coherent", "incoherent"):
@@ -128,7 +128,10 @@ def test_triangle_soup_microbench_small(orc):
             assert_hits_equal(r.trace(rays), want, kind)
             rays["tmax"] = np.random.default_rng(3).uniform(0, 1, len(rays)).astype(np.float32)
             want, _, _ = sc.trace(rays, flags=1, threads=8)
-            assert_hits_equal(r.trace(rays, any_hit=True), want, kind + " any-hit")
+            got = r.trace(rays, any_hit=True)
+            assert_hits_equal(got, want, kind + " any-hit")
+            hit = (got["instance"] != 0xFFFFFFFF).mean()
+            assert 0.05 < hit < 0.99, (kind, hit)   # tmax ends both before and after the first triangle
 
 
 def test_tlas_builder_goldens_and_large(orc):

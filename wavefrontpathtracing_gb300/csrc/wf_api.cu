@@ -1174,14 +1174,14 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
         }
         return WF_OK;
     }
-    {
-        StageTimer t(c, P.prof, ST_GENERATE);
-        WF_CUDA(launch_generate(B, W, c->stream));
-    }
-    c->launches++;
+    // generate.hlsl's camera rays are made inside the depth-0 traversal launch
+    // and shade takes the starting path state at depth 0, so no pass writes them
     bool pending = false;   // a connect on the side stream not yet joined
     for (uint32_t d = 0; d <= W.max_bounces; ++d) {
-        if (P.fused && d > 0) {
+        if (d == 0) {
+            StageTimer t(c, P.prof, ST_EXTEND);
+            WF_CUDA(launch_extend_camera(P.S, B, W, P.cnt, c->totals, c->stream));
+        } else if (P.fused) {
             // the shadow rays of depth d - 1 with the extension rays of depth d
             StageTimer t(c, P.prof, ST_EXTEND);
             WF_CUDA(launch_trace_pair(P.S, B, d, c->totals, c->stream));

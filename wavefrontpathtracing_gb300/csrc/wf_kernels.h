@@ -87,10 +87,12 @@ struct WaveParams {
 // fetch: a zeroed device counter the persistent kernel hands rays out from.
 cudaError_t launch_trace_aos(const SceneRefs& S, const void* rays, uint32_t n, void* hits, uint32_t flags,
                              bool count, uint32_t* fetch, uint32_t* status, Counters* counters, cudaStream_t stream);
-cudaError_t launch_generate(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream);
 // total (device) accumulates the number of rays each launch traced.
 cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
                           bool count, unsigned long long* total, cudaStream_t stream);
+// The camera rays of a wave (depth 0), made inside the traversal launch.
+cudaError_t launch_extend_camera(const SceneRefs& S, const RenderBuffers& B, const WaveParams& W, bool count,
+                                 unsigned long long* total, cudaStream_t stream);
 cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W, uint32_t depth,
                          uint32_t max_rays, const AdjointRefs& A, cudaStream_t stream);
 cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,

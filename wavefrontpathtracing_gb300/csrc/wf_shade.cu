@@ -1,6 +1,7 @@
-// wf_shade.cu — generate (clear_buffers.hlsl + generate.hlsl), shade
-// (shade.hlsl:42-174 plus the added metal / dielectric / next-event /
-// Russian-roulette steps) and post-process (post_process.hlsl:25-72).
+// wf_shade.cu — shade (shade.hlsl:42-174 plus the added metal / dielectric /
+// next-event / Russian-roulette steps; at depth 0 it also stands in for
+// clear_buffers.hlsl + generate.hlsl: the camera rays themselves are made in
+// the depth-0 traversal launch) and post-process (post_process.hlsl:25-72).
 //
 // The per-path arithmetic is the CPU oracle's (oracle/orc_impl.h) operation
 // for operation; both are compiled without fused multiply-add.
@@ -19,25 +20,13 @@ unsigned grid_for(uint32_t n) {
     return blocks ? blocks : 1u;
 }
 
-__global__ void __launch_bounds__(kBlock) k_generate(RenderBuffers B, WaveParams W) {
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W.npaths; p += stride) {
-        const uint32_t pixel = W.pix0 + p / W.nsamples;
-        V3 o, d;
-        primary_ray(W, pixel % W.width, pixel / W.width, o, d);
-        B.q_o[0][p] = make_float4(o.x, o.y, o.z, __uint_as_float(0u));
-        B.q_d[0][p] = make_float4(d.x, d.y, d.z, FLT_MAX);
-        B.q_path[0][p] = p;
-        B.ps_T[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-        B.ps_flags[p] = kFlagSpecular;
-        B.ps_L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) B.counts[0] = W.npaths;
-}
-
 __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B, WaveParams W, uint32_t depth,
                                                   AdjointRefs A) {
-    const uint32_t n = B.counts[depth];
+    // depth 0 shades the camera paths of the wave in path order, their state
+    // the one a path starts with (throughput 1, specular flag, no radiance),
+    // so nothing is read but the hit; it also records the depth-0 count
+    const uint32_t n = depth ? B.counts[depth] : W.npaths;
+    if (depth == 0 && blockIdx.x == 0 && threadIdx.x == 0) B.counts[0] = W.npaths;
     const int cur = depth & 1, nxt = cur ^ 1;
     ShadeCtl K;
     K.frame_seed = W.frame_seed; K.max_bounces = W.max_bounces; K.nee = W.nee; K.rr_start = W.rr_start;
@@ -55,24 +44,37 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
         o.enqueue = false; o.shadow = false; o.em_key = kInvalid; o.em_val = 0.0f;
         uint32_t path = 0;
         if (i < n) {
-            path = B.q_path[cur][i];
             ShadeIn in;
-            in.rd = xyz(B.q_d[cur][i]);
+            if (depth == 0) {
+                path = i;
+                in.pixel = W.pix0 + path / W.nsamples;
+                V3 ro;
+                primary_ray(W, in.pixel % W.width, in.pixel / W.width, ro, in.rd);
+                in.T = mk(1.0f, 1.0f, 1.0f);
+                in.last_pdf = 0.0f;
+                in.flags = kFlagSpecular;
+            } else {
+                path = B.q_path[cur][i];
+                in.pixel = W.pix0 + path / W.nsamples;
+                in.rd = xyz(B.q_d[cur][i]);
+                const float4 T4 = B.ps_T[path];
+                in.T = xyz(T4);
+                in.last_pdf = T4.w;
+                in.flags = B.ps_flags[path];
+            }
             in.tuvp = B.h_tuvp[i];
             in.inst = B.h_inst[i];
-            const float4 T4 = B.ps_T[path];
-            in.T = xyz(T4);
-            in.last_pdf = T4.w;
-            in.flags = B.ps_flags[path];
-            in.pixel = W.pix0 + path / W.nsamples;
             in.sample = W.s0 + path % W.nsamples;
             in.depth = depth;
             shade_one(SH, K, in, A, path, in.pixel, o);
-            if (o.has_add) {
-                float4 acc = B.ps_L[path];
-                acc.x = acc.x + o.add.x;
-                acc.y = acc.y + o.add.y;
-                acc.z = acc.z + o.add.z;
+            if (o.has_add || depth == 0) {
+                // the path's radiance starts at zero here
+                float4 acc = depth ? B.ps_L[path] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (o.has_add) {
+                    acc.x = acc.x + o.add.x;
+                    acc.y = acc.y + o.add.y;
+                    acc.z = acc.z + o.add.z;
+                }
                 B.ps_L[path] = acc;
             }
         }
@@ -157,11 +159,6 @@ __global__ void k_reduce_replicas(float4* g, uint32_t triangles, uint32_t replic
 }
 
 }  // namespace
-
-cudaError_t launch_generate(const RenderBuffers& B, const WaveParams& W, cudaStream_t stream) {
-    k_generate<<<grid_for(W.npaths), kBlock, 0, stream>>>(B, W);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W, uint32_t depth,
                          uint32_t max_rays, const AdjointRefs& A, cudaStream_t stream) {

@@ -1,7 +1,7 @@
 // wf_trace.cu — ray-query kernels: extend (closest hit, extend.hlsl:25-40),
 // connect (any-hit shadow rays; the reference's connect.hlsl is empty) and the
 // stand-alone query behind wf_trace.
-#include "wf_kernels.h"
+#include "wf_shade.cuh"
 #include "wf_traverse.cuh"
 
 namespace wf {
@@ -20,6 +20,27 @@ struct ExtendIO {
         const float4 a = qo[i], b = qd[i];
         o = xyz(a); d = xyz(b); tmax = b.w;
         nc = (__float_as_uint(a.w) & kFlagInside) != 0u;
+    }
+    __device__ __forceinline__ uint32_t root(uint32_t, const SceneRefs& S) const { return S.inst_count ? 0u : kInvalid; }
+    __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool) const {
+        tuvp[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
+        inst[i] = h.inst;
+    }
+};
+
+// Camera rays (depth 0), made where they are traced instead of read from a
+// queue that a separate generate pass wrote (generate.hlsl): path i is sample
+// s0 + i % nsamples of pixel pix0 + i / nsamples, its ray make_primary_ray's
+// (common.hlsl:182-195) with tmax = FLT_MAX and no ray flags.
+struct CameraIO {
+    WaveParams W;
+    float4* tuvp;
+    uint32_t* inst;
+    __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
+        const uint32_t pixel = W.pix0 + i / W.nsamples;
+        primary_ray(W, pixel % W.width, pixel / W.width, o, d);
+        tmax = FLT_MAX;
+        nc = false;
     }
     __device__ __forceinline__ uint32_t root(uint32_t, const SceneRefs& S) const { return S.inst_count ? 0u : kInvalid; }
     __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool) const {
@@ -132,6 +153,16 @@ cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t d
     uint32_t* fetch = B.counts + 2 * kMaxDepth + depth;
     return count ? launch<false, true>(S, io, B.counts + depth, 0, fetch, B.status, B.counters, total, stream)
                  : launch<false, false>(S, io, B.counts + depth, 0, fetch, B.status, B.counters, total, stream);
+}
+
+cudaError_t launch_extend_camera(const SceneRefs& S, const RenderBuffers& B, const WaveParams& W, bool count,
+                                 unsigned long long* total, cudaStream_t stream) {
+    if (W.npaths == 0) return cudaSuccess;
+    CameraIO io;
+    io.W = W; io.tuvp = B.h_tuvp; io.inst = B.h_inst;
+    uint32_t* fetch = B.counts + 2 * kMaxDepth;
+    return count ? launch<false, true>(S, io, nullptr, W.npaths, fetch, B.status, B.counters, total, stream)
+                 : launch<false, false>(S, io, nullptr, W.npaths, fetch, B.status, B.counters, total, stream);
 }
 
 cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t, bool count,

@@ -400,18 +400,21 @@ def triangle_soup(n, seed=7, mu=-5.0, sigma=0.5):
 
 def soup_rays(n_side, seed=7, kind="coherent"):
     """Rays for the traversal micro-benchmark.  coherent: pinhole camera at
-    (0.5, 0.5, -1.0) looking at the cube centre, n_side^2 rays; incoherent:
-    origins uniform in the cube, directions uniform on the sphere."""
+    (0.5, 0.5, -0.5) looking down +z with a 90-degree field of view, so the
+    n_side^2 rays enter the unit cube through its z = 0 face (at distance 0.5
+    .. 0.87) and an any-hit query with tmax U[0, 1] ends on either side of the
+    first triangle; incoherent: origins uniform in the cube, directions
+    uniform on the sphere."""
     n = n_side * n_side
     r = np.zeros(n, dtype=ray_dtype)
     if kind == "coherent":
         ys, xs = np.divmod(np.arange(n, dtype=np.int64), n_side)
         u = (xs + 0.5) / n_side * 2.0 - 1.0
         v = 1.0 - (ys + 0.5) / n_side * 2.0
-        half = math.tan(math.radians(30.0))
+        half = math.tan(math.radians(45.0))
         d = np.stack([u * half, v * half, np.ones_like(u)], axis=1)
         d /= np.linalg.norm(d, axis=1, keepdims=True)
-        r["origin"] = (0.5, 0.5, -1.0)
+        r["origin"] = (0.5, 0.5, -0.5)
         r["dir"] = d
     else:
         rng = np.random.default_rng(seed + 1)
