@@ -19,3 +19,11 @@ g++ -std=c++20 -O2 -ffp-contract=off -fPIC -shared -w \
   "$REF/source/renderer/bvh/bvh_builder.cpp" \
   "$REF/source/renderer/bvh/tlas_builder.cpp"
 echo "built $OUT/libref_bvh.so"
+# The reference's scene loaders' libraries (cgltf, ufbx, vendored under
+# extern/) behind oracle/ref_assets.c, a restatement of asset_loader.cpp's data
+# extraction: pins wavefrontpathtracing_gb300.gltf / .fbx.
+if [ -f "$REF/extern/ufbx/ufbx.c" ] && [ -f "$REF/extern/cgltf/cgltf.h" ]; then
+  gcc -std=gnu11 -O1 -fPIC -shared -w -I "$REF/extern" \
+    -o "$OUT/libref_assets.so" "$HERE/ref_assets.c" "$REF/extern/ufbx/ufbx.c" -lm
+  echo "built $OUT/libref_assets.so"
+fi

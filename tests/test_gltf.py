@@ -15,6 +15,7 @@ import zlib
 import numpy as np
 import pytest
 
+from tests import ref_assets
 from wavefrontpathtracing_gb300 import gltf
 
 
@@ -161,9 +162,7 @@ def test_png_decoder_all_filters():
     assert np.array_equal(gltf.decode_png(encode_png(img)), img)
 
 
-@pytest.mark.parametrize("form", ["glb", "gltf"])
-def test_load_scene(tmp_path, form):
-    img = image()
+def write_form(tmp_path, form, img):
     doc, blob = build_scene_doc(encode_png(img))
     if form == "glb":
         path = tmp_path / "scene.glb"
@@ -176,6 +175,13 @@ def test_load_scene(tmp_path, form):
         doc["images"] = [{"uri": "data:image/png;base64," + base64.b64encode(png).decode()}]
         path = tmp_path / "scene.gltf"
         path.write_text(json.dumps(doc))
+    return path
+
+
+@pytest.mark.parametrize("form", ["glb", "gltf"])
+def test_load_scene(tmp_path, form):
+    img = image()
+    path = write_form(tmp_path, form, img)
     sc = gltf.load(str(path))
     assert len(sc.meshes) == 3 and len(sc.images) == 1 and np.array_equal(sc.images[0], img)
     (v0, i0), (v1, i1), (v2, i2) = sc.meshes
@@ -190,9 +196,38 @@ def test_load_scene(tmp_path, form):
     np.testing.assert_allclose(sc.instances[2][1], child, atol=1e-6)
     m0, m1, m2 = sc.materials
     assert m0["base_color_factor"][:3] == [0.5, 0.25, 1.0] and m0["roughness_factor"] == 0.75
-    assert m0["metallic_factor"] == 0.0 and m0["base_color_image"] == 0 and m0["emissive_strength"] == 1.0
+    assert m0["metallic_factor"] == 0.0 and m0["base_color_image"] == 0 and m0["emissive_strength"] == 0.0
     assert m1["emissive_factor"] == [0.0, 0.0, 0.0] and m1["metallic_factor"] == 1.0   # defaults kept
     assert m2["emissive_strength"] == 8.0 and m2["emissive_image"] == 0 and m2["base_color_factor"] == [1, 1, 1, 1]
+
+
+@pytest.mark.skipif(not ref_assets.available(), reason="reference loaders not built (oracle/_ref)")
+@pytest.mark.parametrize("form", ["glb", "gltf"])
+def test_matches_the_reference_loader(tmp_path, form):
+    """The same file through cgltf as the reference reads it
+    (oracle/ref_assets.c over the reference's vendored cgltf): materials,
+    every primitive's vertices and indices bit for bit, every instance's
+    mesh, material and world transform."""
+    path = write_form(tmp_path, form, image())
+    got = gltf.load(str(path))
+    ref = ref_assets.load(str(path))
+    assert len(got.materials) == len(ref.materials)
+    for m, r in zip(got.materials, ref.materials):
+        for key in ("base_color_factor", "emissive_factor"):
+            assert np.allclose(m[key], r[key])
+        for key in ("metallic_factor", "roughness_factor", "emissive_strength"):
+            assert m[key] == pytest.approx(r[key])
+        assert [m[k] for k in ("base_color_image", "normal_image", "metallic_roughness_image",
+                               "emissive_image")] == r["images"]
+    assert len(got.meshes) == len(ref.meshes)
+    for (v, idx), (rv, ridx) in zip(got.meshes, ref.meshes):
+        assert np.array_equal(idx, ridx)
+        assert np.array_equal(v["position"], rv[:, 0:3]) and np.array_equal(v["normal"], rv[:, 3:6])
+        assert np.array_equal(v["uv"], rv[:, 6:8])
+    assert len(got.instances) == len(ref.instances)
+    for (g, w, mat), (rg, rmat, rw) in zip(got.instances, ref.instances):
+        assert g == rg and mat == rmat
+        assert np.allclose(np.asarray(w, np.float32), rw, rtol=1e-6, atol=1e-6)
 
 
 def test_missing_attributes_are_rejected(tmp_path):

@@ -14,7 +14,9 @@ Same rules as the reference: POSITION, NORMAL and TEXCOORD_0 are required
 (the reference asserts on them, asset_loader.cpp:529-533); a material without
 pbrMetallicRoughness keeps the defaults (white, metallic 1, roughness 1, no
 emission); with it, the factors, emissiveFactor and
-KHR_materials_emissive_strength (default 1) are taken.  Where the reference
+KHR_materials_emissive_strength are taken, the strength being 0 when the
+extension is absent (cgltf's value there, which the reference copies, so such
+materials do not emit) and 1 when it is present without a value.  Where the reference
 would read out of bounds or garbage, this loader is defined instead: 8-bit
 indices and primitives without indices are accepted, and each node's
 primitives map to the meshes of that node's own glTF mesh.  Only triangle
@@ -260,8 +262,10 @@ def load(path):
             mat["metallic_factor"] = pbr.get("metallicFactor", 1.0)
             mat["roughness_factor"] = pbr.get("roughnessFactor", 1.0)
             mat["emissive_factor"] = list(m.get("emissiveFactor", [0.0, 0.0, 0.0]))
-            mat["emissive_strength"] = m.get("extensions", {}).get("KHR_materials_emissive_strength", {}) \
-                .get("emissiveStrength", 1.0)
+            # cgltf leaves the strength at 0 unless the extension is present
+            # (1 when it is, without a value), and the reference copies it
+            ext = m.get("extensions", {}).get("KHR_materials_emissive_strength")
+            mat["emissive_strength"] = ext.get("emissiveStrength", 1.0) if ext is not None else 0.0
             mat["base_color_image"] = image_of(pbr.get("baseColorTexture"))
             mat["metallic_roughness_image"] = image_of(pbr.get("metallicRoughnessTexture"))
             mat["normal_image"] = image_of(m.get("normalTexture"))
