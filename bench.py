@@ -446,6 +446,7 @@ def run_ours(args, rank, world, local):
     c = r.stats()
     alg_bytes = (c["rays_extend"] * (B_RAY + B_HIT) + c["tlas_node_loads"] * B_TNODE + c["instance_loads"] * B_INST
                  + c["blas_node_loads"] * B_BNODE + c["triangle_tests"] * B_TRI)
+    alg_bytes -= c["paths"] * B_RAY   # camera rays are made in the depth-0 launch, not read
     if args.fused_connect:
         # the traversal launches also carry the previous depth's shadow rays
         alg_bytes += (c["rays_connect"] * B_SRAY + c["shadow_tlas_node_loads"] * B_TNODE
