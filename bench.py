@@ -403,7 +403,7 @@ def run_ours(args, rank, world, local):
 
     def frame(seed, profile):
         r.render(max_bounces=DEPTH, spp=SPP, frame_seed=seed, nee=1, rr_start_depth=RR, accumulate=False,
-                 profile=profile, fused_connect=args.fused_connect)
+                 profile=profile, fused_connect=args.fused_connect, tail_paths=args.tail_paths)
         return r.stats()
 
     for i in range(args.warmup):
@@ -452,6 +452,12 @@ def run_ours(args, rank, world, local):
         alg_bytes += (c["rays_connect"] * B_SRAY + c["shadow_tlas_node_loads"] * B_TNODE
                       + c["shadow_instance_loads"] * B_INST + c["shadow_blas_node_loads"] * B_BNODE
                       + c["shadow_triangle_tests"] * B_TRI)
+    # the launches measured are the staged extension launches: with a tail, the
+    # rays of its depths (under 1 % of them on this frame) leave the count
+    tail_d = int(last["tail_depth"])
+    if tail_d:
+        q = [int(x) for x in c["extend_rays_depth"][:DEPTH + 1]]
+        alg_bytes = alg_bytes * sum(q[:tail_d]) / max(1, sum(q))
     bytes_per_launch = alg_bytes / max(1, ext_launches / args.steps)
     ms_per_launch = ext_ms / max(1, ext_launches)
     achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9
@@ -471,7 +477,7 @@ def run_ours(args, rank, world, local):
         r.submit_render_meshes(inst_mesh, inst_xf, inst_mat)
         r.end_scene()
         r.render(max_bounces=DEPTH, spp=SPP, frame_seed=frame_seed(i, rank), nee=1, rr_start_depth=RR,
-                 accumulate=False, fused_connect=args.fused_connect)
+                 accumulate=False, fused_connect=args.fused_connect, tail_paths=args.tail_paths)
         wf.check(r.L.wf_read_image(r.h, wf.abi.ptr(img), img.size))
         s = r.stats()
         e2e_rays += s["rays_extend"] + s["rays_connect"]
@@ -512,7 +518,9 @@ def run_ours(args, rank, world, local):
                 "spp_per_s": round(spp_per_s, 3),
                 "rays_per_step": rays // args.steps,
                 "gpu_launches": launches,
-                "stages_ms": {k: round(last[f"ms_{k}"], 3) for k in ("generate", "extend", "shade", "connect", "post")},
+                "stages_ms": {k: round(last[f"ms_{k}"], 3) for k in ("generate", "extend", "shade", "connect", "post",
+                                                                        "tail")},
+                "tail_depth": int(last["tail_depth"]),
                 "traversal_per_ray": {
                     "extend": {"nodes": round((c["tlas_node_loads"] + c["blas_node_loads"]) / max(1, c["rays_extend"]), 1),
                                "instances": round(c["instance_loads"] / max(1, c["rays_extend"]), 2),
@@ -641,6 +649,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes leg")
     ap.add_argument("--no-megakernel", action="store_true", help="skip the megakernel A/B leg")
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--tail-paths", type=int, default=0,
+                    help="queue size below which a wave's remaining bounces run per path in one launch "
+                         "(0 = never)")
     ap.add_argument("--fused-connect", action="store_true",
                     help="shadow rays of depth d in one launch with the extension rays of depth d + 1")
     ap.add_argument("--workload", default="instanced", choices=["instanced", "traversal", "batched"])

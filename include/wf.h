@@ -113,7 +113,14 @@ typedef struct wf_render_options {
      * launches_extend and launches_connect).  Images are identical.
      * count_traffic uses the separate schedule. */
     uint32_t trace_schedule;
-    uint32_t reserved[1];
+    /* the tail: once a wave's extension queue is expected to hold fewer than
+     * tail_paths paths (from the previous wave's queue sizes, scaled to this
+     * wave), its remaining bounces run one path per thread in a single launch
+     * (the megakernel's loop, resumed from the wavefront's path state) instead
+     * of one launch per stage and depth.  0 = never (the default: on the
+     * 1080p instanced frame the tail from depth 4 took 2.0 ms against 1.5 ms
+     * for the staged depths).  Images are identical either way. */
+    uint32_t tail_paths;
 } wf_render_options;
 
 enum wf_trace_schedule {
@@ -145,6 +152,12 @@ typedef struct wf_stats {
     uint64_t h2d_bytes, d2h_bytes;
     /* queue sizes of the call (wavefront path): extension and shadow rays per depth */
     uint64_t extend_rays_depth[16], shadow_rays_depth[16];
+    /* the tail (wf_render_options.tail_paths): GPU time of its launches
+     * (profile = 1; not in ms_extend) and the depth at which the last wave
+     * handed its remaining bounces to it (0 = the wave ran every depth in
+     * stages; a tail launch counts in launches, not in launches_extend) */
+    double   ms_tail;
+    uint64_t tail_depth;
 } wf_stats;
 
 /* ---- lifetime (renderer::init / exit, renderer.h:23-24) ------------------ */

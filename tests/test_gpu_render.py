@@ -242,3 +242,28 @@ def test_checkpoint_resume_equals_uninterrupted_render(tmp_path):
         load_scene_into(r, small)
         with pytest.raises(wf.WFError):
             r.load_accumulator(path)
+
+
+@pytest.mark.parametrize("where", ["depth1", "middle"])
+def test_tail_kernel_equals_wavefront(orc, where):
+    """The tail: once a wave's queue (projected from the previous wave's
+    queue sizes) falls below tail_paths, its remaining bounces run one path per
+    thread in one launch.  Same rays, same per-depth queue sizes, the same image
+    bit for bit as the stage-per-depth loop, in fewer launches."""
+    desc = scenes.instanced_scene(width=64, height=36, instances=48, freqs=(6, 9), spp=2, max_bounces=6)
+    kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=3)
+    with Renderer(desc.width, desc.height) as r:
+        load_scene_into(r, desc)
+        r.render(frame_seed=41, accumulate=False, **kw)
+        want = r.read_image()
+        sw = r.stats()
+        q = [int(x) for x in sw["extend_rays_depth"][:7]]
+        limit = (1 << 31) if where == "depth1" else (q[2] + q[3]) // 2 + 1
+        assert where == "depth1" or q[3] < limit <= q[2]
+        r.render(frame_seed=41, accumulate=False, tail_paths=limit, **kw)   # the queue sizes are known now
+        got = r.read_image()
+        st = r.stats()
+    assert_images_equal(got, want)
+    for k in ("rays_extend", "rays_connect", "extend_rays_depth", "shadow_rays_depth"):
+        assert np.array_equal(np.asarray(st[k]), np.asarray(sw[k])), k
+    assert st["launches"] < sw["launches"]

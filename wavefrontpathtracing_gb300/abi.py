@@ -80,7 +80,7 @@ class RenderOptions(ctypes.Structure):
     _fields_ = [("spp", ctypes.c_uint32), ("nee", ctypes.c_uint32), ("rr_start_depth", ctypes.c_uint32),
                 ("wave_paths", ctypes.c_uint32), ("profile", ctypes.c_uint32),
                 ("count_traffic", ctypes.c_uint32), ("trace_schedule", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 1)]
+                ("tail_paths", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
@@ -95,7 +95,8 @@ class Stats(ctypes.Structure):
                 ("shadow_tlas_node_loads", ctypes.c_uint64), ("shadow_instance_loads", ctypes.c_uint64),
                 ("shadow_blas_node_loads", ctypes.c_uint64), ("shadow_triangle_tests", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                ("extend_rays_depth", ctypes.c_uint64 * 16), ("shadow_rays_depth", ctypes.c_uint64 * 16)]
+                ("extend_rays_depth", ctypes.c_uint64 * 16), ("shadow_rays_depth", ctypes.c_uint64 * 16),
+                ("ms_tail", ctypes.c_double), ("tail_depth", ctypes.c_uint64)]
 
     def as_dict(self):
         d = {name: getattr(self, name) for name, _ in self._fields_}

@@ -97,11 +97,11 @@ struct EventPair {
     int stage;
 };
 
-enum Stage { ST_GENERATE = 0, ST_EXTEND, ST_SHADE, ST_CONNECT, ST_POST, ST_TLAS, ST_COUNT };
+enum Stage { ST_GENERATE = 0, ST_EXTEND, ST_SHADE, ST_CONNECT, ST_POST, ST_TLAS, ST_TAIL, ST_COUNT };
 // NVTX range names: the reference's GPU profiler scope labels (gpu_profiler.h:59-66)
 // plus the added connect stage.
 const char* const kStageLabel[ST_COUNT] = {"Wavefront Generate", "Wavefront Extend", "Wavefront Shade",
-                                           "Wavefront Connect", "Post-Process", "TLAS Build"};
+                                           "Wavefront Connect", "Post-Process", "TLAS Build", "Wavefront Tail"};
 
 }  // namespace
 
@@ -160,8 +160,14 @@ struct wf_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_shade[kMaxDepth] = {}, ev_conn[kMaxDepth] = {};
     bool timing_pending = false;
+    // queue sizes of the last wave, copied to pinned host memory after it; they
+    // choose where the next wave hands its remaining bounces to the tail kernel
+    uint32_t* h_counts = nullptr;           // pinned, kMaxDepth extension counts
+    cudaEvent_t ev_counts = nullptr;
+    bool counts_pending = false, counts_known = false;
+    uint32_t last_counts[kMaxDepth] = {};
     wf_stats stats{};
-    uint64_t launches = 0, launches_extend = 0, launches_connect = 0;
+    uint64_t launches = 0, launches_extend = 0, launches_connect = 0, tail_depth = 0;
     bool count_traffic = false;
     uint64_t h2d_bytes = 0, d2h_bytes = 0;   // cumulative over the context's life
 };
@@ -417,7 +423,7 @@ int finish_timing(wf_ctx* c) {
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, c->t0, c->t1);
     c->stats.ms_total = ms;
-    double st[ST_COUNT] = {0, 0, 0, 0, 0, 0};
+    double st[ST_COUNT] = {0, 0, 0, 0, 0, 0, 0};
     for (size_t i = 0; i < c->events_used; ++i) {
         float e = 0.0f;
         cudaEventElapsedTime(&e, c->events[i].a, c->events[i].b);
@@ -429,6 +435,7 @@ int finish_timing(wf_ctx* c) {
     c->stats.ms_connect = st[ST_CONNECT];
     c->stats.ms_post = st[ST_POST];
     c->stats.ms_tlas_build = st[ST_TLAS];
+    c->stats.ms_tail = st[ST_TAIL];
     unsigned long long tot[2 + 2 * kMaxDepth] = {};
     WF_CUDA(d2h(c, tot, c->totals, sizeof(tot)));
     WF_CUDA(cudaStreamSynchronize(c->stream));
@@ -461,6 +468,7 @@ int begin_call(wf_ctx* c, bool count_traffic) {
     std::memset(&c->stats, 0, sizeof(c->stats));
     c->events_used = 0;
     c->launches = c->launches_extend = c->launches_connect = 0;
+    c->tail_depth = 0;
     c->count_traffic = count_traffic;
     WF_CUDA(cudaMemsetAsync(c->totals, 0, (2 + 2 * kMaxDepth) * sizeof(unsigned long long), c->stream));
     WF_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(Counters), c->stream));
@@ -474,6 +482,7 @@ int end_call(wf_ctx* c) {
     c->stats.launches = c->launches;
     c->stats.launches_extend = c->launches_extend;
     c->stats.launches_connect = c->launches_connect;
+    c->stats.tail_depth = c->tail_depth;
     return WF_OK;
 }
 
@@ -716,6 +725,9 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
             if (cudaEventCreateWithFlags(&c->ev_shade[d], cudaEventDisableTiming) != cudaSuccess ||
                 cudaEventCreateWithFlags(&c->ev_conn[d], cudaEventDisableTiming) != cudaSuccess)
                 rc = fail(WF_ERR_CUDA, "wf_create: event creation failed");
+        if (rc == WF_OK && (cudaEventCreateWithFlags(&c->ev_counts, cudaEventDisableTiming) != cudaSuccess ||
+                            cudaMallocHost(&c->h_counts, kMaxDepth * sizeof(uint32_t)) != cudaSuccess))
+            rc = fail(WF_ERR_CUDA, "wf_create: event / pinned buffer creation failed");
     }
     if (rc == WF_OK) rc = dev_alloc(&c->status, 1);
     if (rc == WF_OK) rc = dev_alloc(&c->counters, 2);
@@ -756,6 +768,8 @@ int wf_destroy(wf_ctx* c) {
         if (c->ev_shade[d]) cudaEventDestroy(c->ev_shade[d]);
         if (c->ev_conn[d]) cudaEventDestroy(c->ev_conn[d]);
     }
+    if (c->ev_counts) cudaEventDestroy(c->ev_counts);
+    if (c->h_counts) cudaFreeHost(c->h_counts);
     if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1086,6 +1100,7 @@ struct Pass {
     ShadeRefs SH;
     RenderBuffers B;
     bool nee, prof, cnt, mega, fused;
+    uint32_t tail_paths;
 };
 
 int validate_render(wf_ctx* c, const render_settings_t* s, const wf_render_options* o, const char* who) {
@@ -1145,6 +1160,7 @@ Pass make_pass(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     P.cnt = o->count_traffic != 0;
     // traffic counting keeps per-kind counters, so it traces the kinds apart
     P.fused = P.nee && !P.cnt && o->trace_schedule == WF_SCHEDULE_FUSED;
+    P.tail_paths = o->tail_paths;
     return P;
 }
 
@@ -1174,10 +1190,45 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
         }
         return WF_OK;
     }
+    // the depth from which the tail kernel finishes the wave: the first depth
+    // whose queue, projected from the last wave's sizes, is below tail_paths
+    uint32_t tail = kMaxDepth;
+    if (c->counts_pending) {
+        const cudaError_t q = cudaEventQuery(c->ev_counts);
+        if (q == cudaSuccess) {
+            std::memcpy(c->last_counts, c->h_counts, sizeof(c->last_counts));
+            c->counts_pending = false;
+            c->counts_known = c->last_counts[0] > 0;
+        } else if (q == cudaErrorNotReady) {
+            (void)cudaGetLastError();   // not an error: the copy is still in flight
+        } else {
+            WF_CUDA(q);
+        }
+    }
+    const bool tail_ok = !P.cnt && A.g_albedo == nullptr && P.tail_paths != 0u && c->counts_known;
+    if (tail_ok) {
+        const uint64_t limit = P.tail_paths;
+        for (uint32_t d = 1; d <= W.max_bounces; ++d) {
+            const uint64_t projected = (uint64_t)c->last_counts[d] * W.npaths / c->last_counts[0];
+            if (projected < limit) { tail = d; break; }
+        }
+    }
     // generate.hlsl's camera rays are made inside the depth-0 traversal launch
     // and shade takes the starting path state at depth 0, so no pass writes them
     bool pending = false;   // a connect on the side stream not yet joined
     for (uint32_t d = 0; d <= W.max_bounces; ++d) {
+        if (d == tail) {
+            // connect at depth d - 1 has added its contributions first
+            if (pending) {
+                WF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_conn[d - 1], 0));
+                pending = false;
+            }
+            StageTimer t(c, P.prof, ST_TAIL);
+            WF_CUDA(launch_megakernel_tail(P.S, P.SH, B, W, d, B.counts + 2 * kMaxDepth + d, c->totals, c->stream));
+            c->launches++;
+            c->tail_depth = d;
+            break;
+        }
         if (d == 0) {
             StageTimer t(c, P.prof, ST_EXTEND);
             WF_CUDA(launch_extend_camera(P.S, B, W, P.cnt, c->totals, c->stream));
@@ -1218,6 +1269,11 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
     if (pending) WF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_conn[W.max_bounces - 1], 0));
     WF_CUDA(launch_depth_counts(B.counts, c->totals + 2, c->stream));
     c->launches++;
+    if (!P.cnt) {
+        WF_CUDA(d2h(c, c->h_counts, B.counts, kMaxDepth * sizeof(uint32_t)));
+        WF_CUDA(cudaEventRecord(c->ev_counts, c->stream));
+        c->counts_pending = true;
+    }
     if (resolve) {
         {
             StageTimer t(c, P.prof, ST_POST);

@@ -106,6 +106,13 @@ cudaError_t launch_trace_pair(const SceneRefs& S, const RenderBuffers& B, uint32
 // counter (zeroed here), totals[0..1] += extension / shadow rays.
 cudaError_t launch_megakernel(const SceneRefs& S, const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W,
                               uint32_t* fetch, unsigned long long* totals, cudaStream_t stream);
+// The wave's remaining bounces from `depth` on, one path per thread: the paths
+// of queue `depth` resume from the state shade(depth - 1) left (the shadow
+// rays of depth - 1 must have been traced); fetch = a zeroed device counter;
+// the rays traced after the queue are added to the wave's per-depth counts.
+cudaError_t launch_megakernel_tail(const SceneRefs& S, const ShadeRefs& SH, const RenderBuffers& B,
+                                   const WaveParams& W, uint32_t depth, uint32_t* fetch,
+                                   unsigned long long* totals, cudaStream_t stream);
 // per_depth[d] += counts[d] for the wave's extension (d < kMaxDepth) and shadow
 // (kMaxDepth + d) ray counts.
 cudaError_t launch_depth_counts(const uint32_t* counts, unsigned long long* per_depth, cudaStream_t stream);
