@@ -586,7 +586,7 @@ def run_traversal(args, rank, world, local):
         r.submit_render_mesh(mesh, np.eye(4))
         r.end_scene()
         blas_bytes = len(r.mesh_blas(mesh))
-        for kind in ("coherent", "incoherent"):
+        for kind in args.ray_kinds.split(","):
             rays = scenes.soup_rays(side, seed=7, kind=kind)
             for any_hit in (False, True):
                 if any_hit:
@@ -657,6 +657,7 @@ def main():
     ap.add_argument("--workload", default="instanced", choices=["instanced", "traversal", "batched"])
     ap.add_argument("--soup-triangles", type=int, default=8_000_000)
     ap.add_argument("--soup-side", type=int, default=4096, help="rays per set = side^2")
+    ap.add_argument("--ray-kinds", default="coherent,incoherent", help="traversal ray sets to run")
     ap.add_argument("--res", default="1920x1080", help="image size WxH (the workload is 1920x1080; smaller sizes "
                                                        "are for profiling captures)")
     args = ap.parse_args()

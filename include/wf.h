@@ -35,7 +35,9 @@ enum wf_status {
     WF_ERR_TIMEOUT = -4,   /* a bounded device wait gave up */
     WF_ERR_STACK = -5,     /* a traversal stack overflowed (the ray was abandoned) */
     WF_ERR_CUDA = -6,      /* a CUDA runtime call failed */
-    WF_ERR_STATE = -7      /* call out of order (e.g. render before scene_end) */
+    WF_ERR_STATE = -7,     /* call out of order (e.g. render before scene_end) */
+    WF_ERR_BOUNDS = -8     /* checked builds (libwf_checked.so): a device index was out of
+                              bounds; the access was skipped */
 };
 
 typedef struct wf_ctx wf_ctx;
@@ -166,6 +168,10 @@ int wf_destroy(wf_ctx* ctx);
 const char* wf_status_string(int status);
 const char* wf_last_error(void);
 int wf_abi_version(void);
+/* 1 for the bounds-checked build (libwf_checked.so, compiled with WF_CHECKED:
+ * every index a kernel reads is checked before use, a bad one raises
+ * WF_ERR_BOUNDS), 0 for the normal build. */
+int wf_checked_build(void);
 /* Process-wide cap on the device memory the library allocates (all contexts
  * and batches); an allocation past it fails with WF_ERR_OOM and leaves the
  * caller's objects usable.  0 = no cap (the default). */

@@ -28,9 +28,12 @@ from .abi import (BatchConfig, BatchStats, BvhOptions, Env, InitParams, RenderOp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libwf.so")
+# WF_LIBRARY names another build of the library (the bounds-checked
+# _lib/libwf_checked.so); it must exist, nothing falls back to another build.
+LIB_ENV = "WF_LIBRARY"
 
 STATUS = {0: "WF_OK", -1: "WF_ERR_INVALID", -2: "WF_ERR_OOM", -3: "WF_ERR_CAPACITY", -4: "WF_ERR_TIMEOUT",
-          -5: "WF_ERR_STACK", -6: "WF_ERR_CUDA", -7: "WF_ERR_STATE"}
+          -5: "WF_ERR_STACK", -6: "WF_ERR_CUDA", -7: "WF_ERR_STATE", -8: "WF_ERR_BOUNDS"}
 
 # Every entry point declared in include/wf.h, with its ctypes signature.
 _vp, _u32, _u64, _i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32
@@ -41,6 +44,7 @@ SIGNATURES = {
     "wf_status_string": [ctypes.c_int],
     "wf_last_error": [],
     "wf_abi_version": [],
+    "wf_checked_build": [],
     "wf_set_device_memory_limit": [_u64],
     "wf_get_device_memory_usage": [_pu64],
     "wf_get_stream": [_vp, ctypes.POINTER(_vp)],
@@ -100,8 +104,10 @@ def load(path=None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get(LIB_ENV) or LIB_PATH
     if not os.path.exists(path):
+        if path != LIB_PATH:
+            raise FileNotFoundError(f"{LIB_ENV}={path}: no such library")
         from . import build as _build
         _build.build()
     L = ctypes.CDLL(path)

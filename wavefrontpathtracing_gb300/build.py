@@ -1,7 +1,10 @@
 """Builds the CUDA library libwf.so (sm_103a) in-tree.
 
 Each .cu translation unit is compiled in parallel, then linked with nvcc into
-wavefrontpathtracing_gb300/_lib/libwf.so.  Device code is compiled with
+wavefrontpathtracing_gb300/_lib/libwf.so.  build(checked=True) makes the
+bounds-checked variant _lib/libwf_checked.so (-DWF_CHECKED=1: every index a
+kernel reads is checked before use; see csrc/wf_device.cuh), which the tests
+run the GPU parity suite against a second time.  Device code is compiled with
 --fmad=false and IEEE division / square root: the kernels' float results are
 specified operation by operation (see csrc/wf_device.cuh), and the host side
 (-ffp-contract=off) computes instance boxes and the emitter table the same way.
@@ -16,6 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libwf.so")
+LIB_CHECKED = os.path.join(LIBDIR, "libwf_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["wf_api.cu", "wf_trace.cu", "wf_shade.cu", "wf_tlas.cu", "wf_bvh.cu", "wf_batch.cu", "wf_mega.cu"]
 
@@ -42,9 +46,13 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose=False, force=False):
-    """Compiles libwf.so if any source or header is newer than it; returns its path."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose=False, force=False, checked=False):
+    """Compiles libwf.so (or libwf_checked.so) if any source or header is newer
+    than it; returns its path."""
+    build_dir = BUILD + ("_checked" if checked else "")
+    lib = LIB_CHECKED if checked else LIB
+    defines = ["-DWF_CHECKED=1"] if checked else []
+    os.makedirs(build_dir, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers += [os.path.join(HERE, "..", "include", f) for f in ("wf.h", "wf_shared.h")]
@@ -53,10 +61,10 @@ def build(verbose=False, force=False):
     objs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(build_dir, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([cc] + _flags() + ["-c", s, "-o", o])
+            jobs.append([cc] + _flags() + defines + ["-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -68,9 +76,9 @@ def build(verbose=False, force=False):
         for out in ex.map(run, jobs):
             if verbose and out.strip():
                 print(out)
-    if force or jobs or _stale(LIB, objs):
-        run([cc] + ARCH + ["-shared", "-o", LIB] + objs)
-    return LIB
+    if force or jobs or _stale(lib, objs):
+        run([cc] + ARCH + ["-shared", "-o", lib] + objs)
+    return lib
 
 
 if __name__ == "__main__":

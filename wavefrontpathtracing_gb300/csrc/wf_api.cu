@@ -377,6 +377,7 @@ int ensure_buffers(wf_ctx* c) {
     B.accum = c->accum;
     B.status = c->status;
     B.counters = c->counters;
+    B.capacity = c->capacity;
     WF_CUDA(cudaMemsetAsync(c->accum, 0, npix * sizeof(float4), c->stream));
     c->accum_samples = 0;
     c->buffers_ready = true;
@@ -399,6 +400,9 @@ SceneRefs scene_refs(wf_ctx* c) {
     S.tinst = c->tinst.p;
     S.blas = c->blas.p;
     S.inst_count = (uint32_t)c->scene_bi.size();
+    S.tnode_count = 2u * S.inst_count;
+    S.mesh_count = (uint32_t)c->meshes.size();
+    S.status = c->status;
     return S;
 }
 
@@ -414,6 +418,7 @@ int take_status(wf_ctx* c) {
     if (s & ERRF_STACK) return fail(WF_ERR_STACK, "a traversal stack overflowed; affected rays report a miss");
     if (s & ERRF_TIMEOUT) return fail(WF_ERR_TIMEOUT, "a bounded device wait gave up");
     if (s & ERRF_CAPACITY) return fail(WF_ERR_CAPACITY, "a device queue overflowed");
+    if (s & ERRF_BOUNDS) return fail(WF_ERR_BOUNDS, "a device index was out of bounds (checked build); the access was skipped");
     return WF_OK;
 }
 
@@ -547,6 +552,7 @@ bool ctx_mesh(wf_ctx* c, uint32_t mesh, MeshView* out) {
     if (mesh >= c->meshes.size()) return false;
     const Mesh& m = c->meshes[mesh];
     out->tri_count = m.tri_count;
+    out->node_count = m.node_count;
     out->tris = m.tris.data();
     out->root_min = m.root_min;
     out->root_max = m.root_max;
@@ -675,6 +681,7 @@ const char* wf_status_string(int s) {
 const char* wf_last_error(void) { return g_error.c_str(); }
 
 int wf_abi_version(void) { return WF_ABI_VERSION; }
+int wf_checked_build(void) { return WF_CHECKED; }
 
 int wf_set_device_memory_limit(uint64_t bytes) {
     std::lock_guard<std::mutex> lock(g_mem_mutex);
@@ -988,6 +995,8 @@ int wf_scene_end(wf_ctx* c) {
         for (uint32_t i = 0; i < nm; ++i) {
             br[i].nodes = c->meshes[i].d_nodes;
             br[i].tris = c->meshes[i].d_tris;
+            br[i].node_count = c->meshes[i].node_count;
+            br[i].tri_count = c->meshes[i].tri_count;
             sp[i] = c->meshes[i].d_stri;
         }
         if ((rc = c->blas.reserve(br.size())) || (rc = c->stri.reserve(sp.size()))) return rc;
@@ -1151,6 +1160,12 @@ Pass make_pass(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     P.SH.tri_albedo = c->albedo_set ? c->tri_albedo.p : nullptr;
     P.SH.inst_tri_offset = c->albedo_set ? c->inst_tri_offset.p : nullptr;
     P.SH.textures = c->tex_table.p;
+    P.SH.blas = c->blas.p;
+    P.SH.inst_count = (uint32_t)c->scene_bi.size();
+    P.SH.mesh_count = (uint32_t)c->meshes.size();
+    P.SH.texture_count = (uint32_t)c->textures.size();
+    P.SH.albedo_count = (uint32_t)std::min<uint64_t>(c->scene_triangles, 0xFFFFFFFFull);
+    P.SH.status = c->status;
     P.B = c->B;
     P.B.status = c->status;
     P.B.counters = c->counters;

@@ -81,6 +81,9 @@ struct BatchQueues {
     float4* s_d[2];   // {direction, target}: pool slot of the continuing path, or kFinishedBit | camera path
     float4* s_c[2];   // {contribution, scene}
     float4* out_L;    // per camera path: its radiance
+    // checked builds: bounds of the pool, the camera paths and the scene ids
+    uint32_t capacity, total_paths, nscenes;
+    uint32_t* status;
 };
 
 struct BatchCtl {
@@ -137,6 +140,7 @@ __global__ void __launch_bounds__(BLOCK) k_bregen(const BatchScene* sc, const ui
     float4* const qL = cur ? Q.qL[1] : Q.qL[0];
     for (uint32_t j = blockIdx.x * BLOCK + threadIdx.x; j < m; j += gridDim.x * BLOCK) {
         const uint32_t g = g0 + j;
+        if (!in_bounds(s0 + j, Q.capacity, Q.status) || !in_bounds(g, Q.total_paths, Q.status)) continue;
         const uint32_t s = scene_of(pbase, ns, g);
         const BatchScene& S = sc[s];
         const uint32_t local = g - S.path_base;
@@ -157,13 +161,16 @@ struct BatchExtendIO {
     float4* tuvp;
     uint32_t* inst;
     const uint32_t* roots;
+    uint32_t nscenes;    // checked builds
+    uint32_t* status;
     __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
         const float4 a = qo[i], b = qd[i];
         o = xyz(a); d = xyz(b); tmax = FLT_MAX;
         nc = (__float_as_uint(a.w) & kFlagInside) != 0u;
     }
     __device__ __forceinline__ uint32_t root(uint32_t i, const SceneRefs&) const {
-        return roots[__float_as_uint(qo[i].w) >> kSceneShift];
+        const uint32_t scene = __float_as_uint(qo[i].w) >> kSceneShift;
+        return in_bounds(scene, nscenes, status) ? roots[scene] : kInvalid;
     }
     __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool) const {
         tuvp[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
@@ -176,6 +183,8 @@ struct BatchConnectIO {
     const float4* sd;
     const float4* sc;
     const uint32_t* roots;
+    uint32_t nscenes, capacity, total_paths;   // checked builds
+    uint32_t* status;
     float4* qL;       // radiance of the continuing paths (the next queue)
     float4* out_L;    // radiance of finished camera paths
     __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
@@ -183,12 +192,15 @@ struct BatchConnectIO {
         o = xyz(a); d = xyz(b); tmax = a.w; nc = false;
     }
     __device__ __forceinline__ uint32_t root(uint32_t i, const SceneRefs&) const {
-        return roots[__float_as_uint(sc[i].w)];
+        const uint32_t scene = __float_as_uint(sc[i].w);
+        return in_bounds(scene, nscenes, status) ? roots[scene] : kInvalid;
     }
     __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool ok) const {
         if (!ok || h.inst != kInvalid) return;
         const float4 k = sc[i];
         const uint32_t t = __float_as_uint(sd[i].w);
+        if ((t & kFinishedBit) ? !in_bounds(t & ~kFinishedBit, total_paths, status) : !in_bounds(t, capacity, status))
+            return;
         float4* dst = (t & kFinishedBit) ? out_L + (t & ~kFinishedBit) : qL + t;
         float4 acc = *dst;
         acc.x = acc.x + k.x;
@@ -238,6 +250,7 @@ __global__ void __launch_bounds__(BLOCK) k_bshade(ShadeRefs SH, const BatchScene
             L4 = qL[i];
             const uint32_t f = __float_as_uint(a.w);
             scene = f >> kSceneShift;
+            if (!in_bounds(scene, Q.nscenes, Q.status)) scene = 0u;   // checked builds: flagged, scene 0 stands in
             depth = (f >> kDepthShift) & 0xFFu;
             pixel = __float_as_uint(b.w);
             const BatchScene& S = sc[scene];
@@ -265,11 +278,11 @@ __global__ void __launch_bounds__(BLOCK) k_bshade(ShadeRefs SH, const BatchScene
             }
             if (!o.enqueue) {
                 gidx = S.path_base + pixel * S.spp + in.sample;
-                Q.out_L[gidx] = L4;
+                if (in_bounds(gidx, Q.total_paths, Q.status)) Q.out_L[gidx] = L4;
             }
         }
         const uint32_t slot = warp_append(ncount, o.enqueue);
-        if (o.enqueue) {
+        if (o.enqueue && in_bounds(slot, Q.capacity, Q.status)) {
             const uint32_t f = (o.flags & 0xFFu) | ((depth + 1u) << kDepthShift) | (scene << kSceneShift);
             no[slot] = make_float4(o.org.x, o.org.y, o.org.z, __uint_as_float(f));
             nd[slot] = make_float4(o.dir.x, o.dir.y, o.dir.z, __uint_as_float(pixel));
@@ -277,7 +290,7 @@ __global__ void __launch_bounds__(BLOCK) k_bshade(ShadeRefs SH, const BatchScene
             nL[slot] = L4;
         }
         const uint32_t sslot = warp_append(shadow_tail, o.shadow);
-        if (o.shadow) {
+        if (o.shadow && in_bounds(sslot, Q.capacity, Q.status)) {
             const uint32_t target = o.enqueue ? slot : (kFinishedBit | gidx);
             s_o[sslot] = make_float4(o.spos.x, o.spos.y, o.spos.z, o.stmax);
             s_d[sslot] = make_float4(o.sdir.x, o.sdir.y, o.sdir.z, __uint_as_float(target));
@@ -493,6 +506,8 @@ int build_tables(wf_batch* b) {
         ctx_mesh(c, i, &mv);
         br[i].nodes = mv.d_nodes;
         br[i].tris = mv.d_tris;
+        br[i].node_count = mv.node_count;
+        br[i].tri_count = mv.tri_count;
         sp[i] = mv.d_stri;
     }
     int rc;
@@ -601,6 +616,10 @@ BatchQueues queues(wf_batch* b) {
         Q.s_c[k] = b->s_c[k].p;
     }
     Q.out_L = b->out_L.p;
+    Q.capacity = b->cfg.capacity;
+    Q.total_paths = b->total_paths;
+    Q.nscenes = b->nscenes;
+    Q.status = ctx_status(b->ctx);
     return Q;
 }
 
@@ -639,6 +658,9 @@ int enqueue_iteration(wf_batch* b, int k, bool join_prev, bool join_self, cudaGr
     S.tinst = b->tinst.p;
     S.blas = b->blas.p;
     S.inst_count = b->total_inst;
+    S.tnode_count = 2u * b->total_inst;
+    S.mesh_count = ctx_mesh_count(b->ctx);
+    S.status = status;
     ShadeRefs SH;
     SH.sinst = b->sinst.p;
     SH.stri = b->stri.p;
@@ -648,11 +670,18 @@ int enqueue_iteration(wf_batch* b, int k, bool join_prev, bool join_self, cudaGr
     SH.tri_albedo = nullptr;
     SH.inst_tri_offset = nullptr;
     SH.textures = ctx_texture_table(b->ctx);
+    SH.blas = b->blas.p;
+    SH.inst_count = b->total_inst;
+    SH.mesh_count = ctx_mesh_count(b->ctx);
+    SH.texture_count = ctx_texture_count(b->ctx);
+    SH.albedo_count = 0;
+    SH.status = status;
     k_bbegin<<<1, 1, 0, st>>>(b->ctl, cur);
     BCUDA(cudaGetLastError());
     BCUDA(regen_or_shade(false, b, SH, Q, cur, st));
     BatchExtendIO ex;
     ex.qo = Q.qo[cur]; ex.qd = Q.qd[cur]; ex.tuvp = Q.h_tuvp; ex.inst = Q.h_inst; ex.roots = b->d_roots.p;
+    ex.nscenes = b->nscenes; ex.status = status;
     auto ke = k_btrace<false, BatchExtendIO>;
     ke<<<persistent_grid(ke), kTraceBlock, 0, st>>>(S, ex, &b->ctl->count[cur], &b->ctl->fetch[0], status);
     BCUDA(cudaGetLastError());
@@ -663,6 +692,7 @@ int enqueue_iteration(wf_batch* b, int k, bool join_prev, bool join_self, cudaGr
     BCUDA(cudaStreamWaitEvent(b->side, b->ev_shade[k], 0));
     BatchConnectIO cn;
     cn.so = Q.s_o[cur]; cn.sd = Q.s_d[cur]; cn.sc = Q.s_c[cur]; cn.roots = b->d_roots.p; cn.qL = Q.qL[cur ^ 1];
+    cn.nscenes = b->nscenes; cn.capacity = b->cfg.capacity; cn.total_paths = b->total_paths; cn.status = status;
     cn.out_L = Q.out_L;
     auto kc = k_btrace<true, BatchConnectIO>;
     kc<<<persistent_grid(kc), kTraceBlock, 0, b->side>>>(S, cn, &b->ctl->shadow[cur], &b->ctl->fetch[1 + cur], status);

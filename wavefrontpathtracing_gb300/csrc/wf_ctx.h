@@ -24,7 +24,7 @@ struct Instance {
 };
 
 struct MeshView {
-    uint32_t tri_count;
+    uint32_t tri_count, node_count;
     const triangle_t* tris;       // host copy, original order
     const float* root_min;
     const float* root_max;

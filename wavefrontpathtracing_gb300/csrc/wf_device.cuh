@@ -39,6 +39,7 @@ namespace wf {
 struct BlasRef {
     const float4* nodes;
     const float4* tris;
+    uint32_t node_count, tri_count;   // read by checked builds only
 };
 
 struct SceneRefs {
@@ -46,6 +47,8 @@ struct SceneRefs {
     const float4* tinst;       // TLAS instances
     const BlasRef* blas;       // indexed by mesh id
     uint32_t inst_count;
+    uint32_t tnode_count, mesh_count;   // checked builds: bounds of the indices above
+    uint32_t* status;                   // checked builds: where ERRF_BOUNDS is raised
 };
 
 constexpr int kInstRows = 7;   // float4 rows per instance in the shading table
@@ -70,7 +73,30 @@ struct Counters {
 };
 
 // Device error flags (bit set in the context's status word).
-enum : uint32_t { ERRF_STACK = 1u, ERRF_CAPACITY = 2u, ERRF_TIMEOUT = 4u };
+enum : uint32_t { ERRF_STACK = 1u, ERRF_CAPACITY = 2u, ERRF_TIMEOUT = 4u, ERRF_BOUNDS = 8u };
+
+// Checked builds (-DWF_CHECKED=1, libwf_checked.so): every index a kernel
+// takes from memory (a node's children, a leaf's triangles, an instance, a
+// mesh, a hit's primitive, a texture, a path, a queue slot) is compared with
+// the size of what it indexes before the access.  A bad index raises
+// ERRF_BOUNDS in the status word (WF_ERR_BOUNDS from the next synchronising
+// call) and the access is skipped: the ray reports a miss, the path ends,
+// the write is dropped.  Normal builds compile the checks away.  It takes the
+// place of compute-sanitizer, which this deployment cannot run: the GPU
+// parity suite runs a second time against the checked library.
+#ifndef WF_CHECKED
+#define WF_CHECKED 0
+#endif
+__device__ __forceinline__ bool in_bounds(uint64_t i, uint64_t n, uint32_t* status) {
+#if WF_CHECKED
+    if (i < n) return true;
+    if (status) atomicOr(status, ERRF_BOUNDS);
+    return false;
+#else
+    (void)i; (void)n; (void)status;
+    return true;
+#endif
+}
 
 constexpr int kStack = 64;                 // per level, as the reference (accelstruct.hlsl:64,160)
 constexpr float kEps = 1e-8f;              // SMALL_FLOAT (common.hlsl:8)

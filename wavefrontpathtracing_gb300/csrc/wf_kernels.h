@@ -19,6 +19,10 @@ struct ShadeRefs {
     const float4* tri_albedo;     // optional per scene triangle albedo (replaces the base colour)
     const uint32_t* inst_tri_offset;  // scene triangle of (instance i, primitive p) = offset[i] + p
     const TexRef* textures;       // indexed by texture id (entry 0 unused: id 0 = default texture)
+    // checked builds: bounds of the indices a hit record and the tables carry
+    const BlasRef* blas;          // per mesh (triangle counts)
+    uint32_t inst_count, mesh_count, texture_count, albedo_count;
+    uint32_t* status;
 };
 
 // Path-replay adjoint (null pointers in a forward pass).  The replay traces
@@ -59,6 +63,7 @@ struct RenderBuffers {
     float4* accum;        // per pixel {radiance sum rgb, samples}
     uint32_t* status;     // device error flags (ERRF_*)
     Counters* counters;   // [0] extension traffic, [1] shadow traffic
+    uint32_t capacity;    // paths per wave (queue and path-state entries)
 };
 
 constexpr uint32_t kMaxDepth = 16;

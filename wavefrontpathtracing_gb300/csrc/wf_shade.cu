@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
                 in.flags = kFlagSpecular;
             } else {
                 path = B.q_path[cur][i];
+                if (!in_bounds(path, W.npaths, B.status)) path = 0u;   // checked builds: flagged, path 0 stands in
                 in.pixel = W.pix0 + path / W.nsamples;
                 in.rd = xyz(B.q_d[cur][i]);
                 const float4 T4 = B.ps_T[path];
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
         }
         if (A.g_emission) warp_add_by_key(A.g_emission, o.em_key, o.em_val);
         const uint32_t slot = warp_append(&B.counts[depth + 1], o.enqueue);
-        if (o.enqueue) {
+        if (o.enqueue && in_bounds(slot, B.capacity, B.status)) {
             B.q_o[nxt][slot] = make_float4(o.org.x, o.org.y, o.org.z, __uint_as_float(o.flags & kFlagInside));
             B.q_d[nxt][slot] = make_float4(o.dir.x, o.dir.y, o.dir.z, FLT_MAX);
             B.q_path[nxt][slot] = path;
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
             B.ps_flags[path] = o.flags;
         }
         const uint32_t sslot = warp_append(&B.counts[kMaxDepth + depth], o.shadow);
-        if (o.shadow) {
+        if (o.shadow && in_bounds(sslot, B.capacity, B.status)) {
             s_o[sslot] = make_float4(o.spos.x, o.spos.y, o.spos.z, o.stmax);
             s_d[sslot] = make_float4(o.sdir.x, o.sdir.y, o.sdir.z, __uint_as_float(path));
             s_c[sslot] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, 0.0f);

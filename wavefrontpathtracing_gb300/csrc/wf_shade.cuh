@@ -101,7 +101,7 @@ __device__ __forceinline__ V3 abs3(V3 a) { return mk(fabsf(a.x), fabsf(a.y), fab
 
 // Material texture of a slot (id 0: the slot's default texture).
 __device__ __forceinline__ float4 mat_tex(const ShadeRefs& SH, uint32_t id, uint32_t slot, float u, float v) {
-    if (id == 0u) return tex_default(slot);
+    if (id == 0u || !in_bounds(id, SH.texture_count + 1ull, SH.status)) return tex_default(slot);
     return tex_bilinear(SH.textures[id], u, v);
 }
 
@@ -153,10 +153,12 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
         return;
     }
     const uint32_t inst = in.inst;
+    if (!in_bounds(inst, SH.inst_count, SH.status)) return;   // checked builds: the path ends
     const float4* ip = SH.sinst + (size_t)kInstRows * inst;
     const float4 c0 = ip[0], c1 = ip[1], c2 = ip[2], c3 = ip[3], mb = ip[4], me = ip[5], tx = ip[6];
     const uint32_t mesh = __float_as_uint(c0.w);
     const uint32_t prim = __float_as_uint(in.tuvp.w);
+    if (!in_bounds(mesh, SH.mesh_count, SH.status) || !in_bounds(prim, SH.blas[mesh].tri_count, SH.status)) return;
     const float4* tp = SH.stri[mesh] + 6ull * prim;
     const V3 p0 = xyz(tp[0]), p1 = xyz(tp[1]), p2 = xyz(tp[2]);
     const V3 n0 = xyz(tp[3]), n1 = xyz(tp[4]), n2 = xyz(tp[5]);
@@ -182,6 +184,7 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
     uint32_t stri = 0;
     if (SH.tri_albedo) {
         stri = SH.inst_tri_offset[inst] + prim;
+        if (!in_bounds(stri, SH.albedo_count, SH.status)) return;
         base_c = xyz(SH.tri_albedo[stri]);
     }
     const V3 le = mk(me.x * et.x, me.y * et.y, me.z * et.z);
@@ -369,7 +372,7 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
                 const float sc = (cos_x * w) / pdf_l;
                 V3 ltle = xyz(lt.le);
                 const uint32_t lt_tex = __float_as_uint(lt.le.w);
-                if (lt_tex != 0u) {
+                if (lt_tex != 0u && in_bounds(lt_tex, SH.texture_count + 1ull, SH.status)) {
                     // textured emitter: its emission texture at the sampled point
                     const float lu = (lt.uv01.x + b1 * (lt.uv01.z - lt.uv01.x)) + b2 * (lt.uv2.x - lt.uv01.x);
                     const float lv = (lt.uv01.y + b1 * (lt.uv01.w - lt.uv01.y)) + b2 * (lt.uv2.y - lt.uv01.y);

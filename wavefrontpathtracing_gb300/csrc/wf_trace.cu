@@ -16,13 +16,17 @@ struct ExtendIO {
     const float4* qd;
     float4* tuvp;
     uint32_t* inst;
+    uint32_t cap;        // checked builds: queue entries
+    uint32_t* status;
     __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
+        if (!in_bounds(i, cap, status)) i = 0u;   // checked builds: flagged, entry 0 stands in
         const float4 a = qo[i], b = qd[i];
         o = xyz(a); d = xyz(b); tmax = b.w;
         nc = (__float_as_uint(a.w) & kFlagInside) != 0u;
     }
     __device__ __forceinline__ uint32_t root(uint32_t, const SceneRefs& S) const { return S.inst_count ? 0u : kInvalid; }
     __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool) const {
+        if (!in_bounds(i, cap, status)) return;
         tuvp[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.prim));
         inst[i] = h.inst;
     }
@@ -57,15 +61,19 @@ struct ConnectIO {
     const float4* sd;
     const float4* sc;
     float4* L;
+    uint32_t cap;        // checked builds: queue and path entries
+    uint32_t* status;
     __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
+        if (!in_bounds(i, cap, status)) i = 0u;   // checked builds: flagged, entry 0 stands in
         const float4 a = so[i], b = sd[i];
         o = xyz(a); d = xyz(b); tmax = a.w; nc = false;
     }
     __device__ __forceinline__ uint32_t root(uint32_t, const SceneRefs& S) const { return S.inst_count ? 0u : kInvalid; }
     __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool ok) const {
-        if (!ok || h.inst != kInvalid) return;
+        if (!ok || h.inst != kInvalid || !in_bounds(i, cap, status)) return;
         const float4 k = sc[i];
         const uint32_t path = __float_as_uint(sd[i].w);
+        if (!in_bounds(path, cap, status)) return;
         float4 acc = L[path];
         acc.x = acc.x + k.x;
         acc.y = acc.y + k.y;
@@ -150,6 +158,7 @@ cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t d
     ExtendIO io;
     const int cur = depth & 1;
     io.qo = B.q_o[cur]; io.qd = B.q_d[cur]; io.tuvp = B.h_tuvp; io.inst = B.h_inst;
+    io.cap = B.capacity; io.status = B.status;
     uint32_t* fetch = B.counts + 2 * kMaxDepth + depth;
     return count ? launch<false, true>(S, io, B.counts + depth, 0, fetch, B.status, B.counters, total, stream)
                  : launch<false, false>(S, io, B.counts + depth, 0, fetch, B.status, B.counters, total, stream);
@@ -170,6 +179,7 @@ cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t 
     ConnectIO io;
     const int par = depth & 1;
     io.so = B.s_o[par]; io.sd = B.s_d[par]; io.sc = B.s_c[par]; io.L = B.ps_L;
+    io.cap = B.capacity; io.status = B.status;
     uint32_t* fetch = B.counts + 3 * kMaxDepth + depth;
     return count ? launch<true, true>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, B.counters + 1, total,
                                       stream)
@@ -183,6 +193,7 @@ cudaError_t launch_trace_pair(const SceneRefs& S, const RenderBuffers& B, uint32
     const int par = (depth - 1) & 1, cur = depth & 1;
     io.c.so = B.s_o[par]; io.c.sd = B.s_d[par]; io.c.sc = B.s_c[par]; io.c.L = B.ps_L;
     io.e.qo = B.q_o[cur]; io.e.qd = B.q_d[cur]; io.e.tuvp = B.h_tuvp; io.e.inst = B.h_inst;
+    io.c.cap = io.e.cap = B.capacity; io.c.status = io.e.status = B.status;
     io.n_first = 0;
     uint32_t* fetch = B.counts + 2 * kMaxDepth + depth;
     k_trace_pair<<<persistent_grid(k_trace_pair), kTraceBlock, 0, stream>>>(

@@ -162,6 +162,7 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                         ci = rcp(cd);
                         const uint32_t root = io.root(k, S);
                         bool miss = root == kInvalid;
+                        if (!miss && !in_bounds(root, S.tnode_count, S.status)) miss = true;
                         if (!miss) {
                             const float4 n0 = ldg4(S.tnodes + 2ull * root), n1 = ldg4(S.tnodes + 2ull * root + 1);
                             if (COUNT) cnt.tlas_nodes++;
@@ -190,17 +191,29 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
             // 0 the current ray is the world ray
             ii = w1;
             const float4* ip = S.tinst + 4ull * ii;
-            const float4 c0 = ldg4(ip), c1 = ldg4(ip + 1), c2 = ldg4(ip + 2), c3 = ldg4(ip + 3);
-            if (COUNT) cnt.instances++;
-            co = xform(co, 1.0f, c0, c1, c2, c3);
-            cd = xform(cd, 0.0f, c0, c1, c2, c3);
-            ci = rcp(cd);
-            B = S.blas[__float_as_uint(c0.w)];
-            const float4 r0 = ldg4(B.nodes), r1 = ldg4(B.nodes + 1);
-            if (COUNT) cnt.blas_nodes++;
-            w0 = __float_as_uint(r0.w);
-            w1 = __float_as_uint(r1.w);
-            level = 1; tb = sp; hit_here = false;
+            if (!in_bounds(ii, S.inst_count, S.status)) {
+                pop = true;
+            } else {
+                const float4 c0 = ldg4(ip), c1 = ldg4(ip + 1), c2 = ldg4(ip + 2), c3 = ldg4(ip + 3);
+                if (COUNT) cnt.instances++;
+                const uint32_t mesh = __float_as_uint(c0.w);
+                if (!in_bounds(mesh, S.mesh_count, S.status)) {
+                    pop = true;
+                } else {
+                    co = xform(co, 1.0f, c0, c1, c2, c3);
+                    cd = xform(cd, 0.0f, c0, c1, c2, c3);
+                    ci = rcp(cd);
+                    B = S.blas[mesh];
+                    const float4 r0 = ldg4(B.nodes), r1 = ldg4(B.nodes + 1);
+                    if (COUNT) cnt.blas_nodes++;
+                    w0 = __float_as_uint(r0.w);
+                    w1 = __float_as_uint(r1.w);
+                    level = 1; tb = sp; hit_here = false;
+                }
+            }
+        } else if (level == 1u && w1 > 0u && !in_bounds(w0, B.tri_count, S.status)) {
+            w1 = 0u;
+            pop = true;
         } else if (level == 1u && w1 > 0u) {
             // BLAS leaf: one triangle per step, in index-list order (w0 = the
             // next triangle, w1 = triangles left), so lanes on interior nodes
@@ -229,26 +242,32 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                 pa = B.nodes + 2ull * w0;
                 pb = pa + 2;
             }
-            const float4 a0 = ldg4(pa), a1 = ldg4(pa + 1), b0 = ldg4(pb), b1 = ldg4(pb + 1);
-            if (COUNT) { if (level == 0u) cnt.tlas_nodes += 2; else cnt.blas_nodes += 2; }
-            float dl = slab(xyz(a0), xyz(a1), co, ci, ct);
-            float dr = slab(xyz(b0), xyz(b1), co, ci, ct);
-            uint2 L = make_uint2(__float_as_uint(a0.w), __float_as_uint(a1.w));
-            uint2 R = make_uint2(__float_as_uint(b0.w), __float_as_uint(b1.w));
-            if (dl > dr) {
-                float td = dl; dl = dr; dr = td;
-                uint2 tn = L; L = R; R = tn;
-            }
-            if (dl == FLT_MAX) {
+            if (level == 0u ? !(in_bounds(w0 >> 16, S.tnode_count, S.status) &&
+                                in_bounds(w0 & 0xFFFFu, S.tnode_count, S.status))
+                            : !in_bounds(w0 + 1ull, B.node_count, S.status)) {
                 pop = true;
             } else {
-                w0 = L.x; w1 = L.y;
-                if (dr != FLT_MAX) {
-                    if ((level == 0u ? sp : sp - tb) == kStack) {
-                        clear_hit();
-                        finish = true; ok = false; overflow = true;
-                    } else {
-                        stack_push(R);
+                const float4 a0 = ldg4(pa), a1 = ldg4(pa + 1), b0 = ldg4(pb), b1 = ldg4(pb + 1);
+                if (COUNT) { if (level == 0u) cnt.tlas_nodes += 2; else cnt.blas_nodes += 2; }
+                float dl = slab(xyz(a0), xyz(a1), co, ci, ct);
+                float dr = slab(xyz(b0), xyz(b1), co, ci, ct);
+                uint2 L = make_uint2(__float_as_uint(a0.w), __float_as_uint(a1.w));
+                uint2 R = make_uint2(__float_as_uint(b0.w), __float_as_uint(b1.w));
+                if (dl > dr) {
+                    float td = dl; dl = dr; dr = td;
+                    uint2 tn = L; L = R; R = tn;
+                }
+                if (dl == FLT_MAX) {
+                    pop = true;
+                } else {
+                    w0 = L.x; w1 = L.y;
+                    if (dr != FLT_MAX) {
+                        if ((level == 0u ? sp : sp - tb) == kStack) {
+                            clear_hit();
+                            finish = true; ok = false; overflow = true;
+                        } else {
+                            stack_push(R);
+                        }
                     }
                 }
             }
@@ -290,7 +309,7 @@ template <bool ANY>
 __device__ __forceinline__ bool trace_single(const SceneRefs& S, uint32_t root, V3 wo, V3 wd, float tmax,
                                              bool no_cull, Hit& h) {
     h.inst = kInvalid; h.prim = kInvalid; h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f;
-    if (root == kInvalid) return true;
+    if (root == kInvalid || !in_bounds(root, S.tnode_count, S.status)) return true;
     const V3 wi = rcp(wd);
     float wt = tmax;
     float4 n0 = ldg4(S.tnodes + 2ull * root), n1 = ldg4(S.tnodes + 2ull * root + 1);
@@ -303,7 +322,14 @@ __device__ __forceinline__ bool trace_single(const SceneRefs& S, uint32_t root, 
             // trace_ray_bvh_instance: the ray in object space, t shared
             const uint32_t ii = t1;
             const float4* ip = S.tinst + 4ull * ii;
-            const float4 c0 = ldg4(ip), c1 = ldg4(ip + 1), c2 = ldg4(ip + 2), c3 = ldg4(ip + 3);
+            const float4 c0 = in_bounds(ii, S.inst_count, S.status) ? ldg4(ip) : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!in_bounds(ii, S.inst_count, nullptr) || !in_bounds(__float_as_uint(c0.w), S.mesh_count, S.status)) {
+                if (tsp == 0) break;
+                const uint2 e = tstack[--tsp];
+                t0 = e.x; t1 = e.y;
+                continue;
+            }
+            const float4 c1 = ldg4(ip + 1), c2 = ldg4(ip + 2), c3 = ldg4(ip + 3);
             const V3 co = xform(wo, 1.0f, c0, c1, c2, c3);
             const V3 cd = xform(wd, 0.0f, c0, c1, c2, c3);
             const V3 ci = rcp(cd);
@@ -316,7 +342,9 @@ __device__ __forceinline__ bool trace_single(const SceneRefs& S, uint32_t root, 
             bool hit_here = false;
             for (;;) {
                 bool pop = false;
-                if (b1 > 0u) {
+                if (b1 > 0u && !in_bounds((uint64_t)b0 + b1 - 1u, B.tri_count, S.status)) {
+                    pop = true;
+                } else if (b1 > 0u) {
                     for (uint32_t i = b0; i < b0 + b1; ++i) {
                         const float4* tp = B.tris + 3ull * i;
                         const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
@@ -328,6 +356,8 @@ __device__ __forceinline__ bool trace_single(const SceneRefs& S, uint32_t root, 
                             if (ANY) { h.inst = ii; h.t = ct; return true; }
                         }
                     }
+                    pop = true;
+                } else if (!in_bounds(b0 + 1ull, B.node_count, S.status)) {
                     pop = true;
                 } else {
                     const float4* pa = B.nodes + 2ull * b0;
@@ -358,6 +388,12 @@ __device__ __forceinline__ bool trace_single(const SceneRefs& S, uint32_t root, 
             }
             wt = ct;
             if (hit_here) { h.inst = ii; h.t = wt; }
+            if (tsp == 0) break;
+            const uint2 e = tstack[--tsp];
+            t0 = e.x; t1 = e.y;
+            continue;
+        }
+        if (!(in_bounds(t0 >> 16, S.tnode_count, S.status) && in_bounds(t0 & 0xFFFFu, S.tnode_count, S.status))) {
             if (tsp == 0) break;
             const uint2 e = tstack[--tsp];
             t0 = e.x; t1 = e.y;
