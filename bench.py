@@ -586,6 +586,7 @@ def run_traversal(args, rank, world, local):
         r.submit_render_mesh(mesh, np.eye(4))
         r.end_scene()
         blas_bytes = len(r.mesh_blas(mesh))
+        reorder = args.reorder == "on"
         for kind in args.ray_kinds.split(","):
             rays = scenes.soup_rays(side, seed=7, kind=kind)
             for any_hit in (False, True):
@@ -595,14 +596,14 @@ def run_traversal(args, rank, world, local):
                 d_hits = torch.zeros(len(rays) * 20, dtype=torch.uint8, device="cuda")
                 torch.cuda.synchronize()
                 for _ in range(args.warmup):
-                    r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit)
+                    r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit, reorder=reorder)
                 r.synchronize()
                 ms = []
                 l2 = torch.zeros(L2_BYTES // 4, dtype=torch.float32, device="cuda")
                 for _ in range(args.steps):
                     l2.add_(1)
                     torch.cuda.synchronize()
-                    r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit)
+                    r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit, reorder=reorder)
                     ms.append(r.stats()["ms_total"])
                 r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit, count_traffic=True)
                 c = r.stats()
@@ -612,7 +613,7 @@ def run_traversal(args, rank, world, local):
                 hits = d_hits.cpu().numpy().view(wf.abi.hit_dtype)
                 # e2e: host rays in, host hits out
                 t1 = time.perf_counter()
-                r.trace(rays, any_hit=any_hit)
+                r.trace(rays, any_hit=any_hit, reorder=reorder)
                 e2e_s = time.perf_counter() - t1
                 line = {"metric": "traversal Mrays/s", "value": round(len(rays) / (t / 1e3) / 1e6, 2),
                         "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -621,6 +622,8 @@ def run_traversal(args, rank, world, local):
                         "config": {"workload": f"traversal micro-benchmark, {n_tris} soup triangles, {len(rays)} "
                                                f"{kind} rays, {'any' if any_hit else 'closest'} hit",
                                    "blas_bytes": blas_bytes, "gpu_bvh_build_s": round(build_s, 3),
+                                   "ray_order": ("origins' Morton codes (stable radix sort inside the timed call)"
+                                                 if reorder else "as given"),
                                    "hit_fraction": round(float((hits['instance'] != 0xFFFFFFFF).mean()), 4)},
                         "e2e": {"value": round(len(rays) / e2e_s / 1e6, 2), "unit": "Mrays/s",
                                 "h2d_bytes_per_step": int(rays.nbytes), "d2h_bytes_per_step": int(len(rays) * 20)},
@@ -658,6 +661,8 @@ def main():
     ap.add_argument("--soup-triangles", type=int, default=8_000_000)
     ap.add_argument("--soup-side", type=int, default=4096, help="rays per set = side^2")
     ap.add_argument("--ray-kinds", default="coherent,incoherent", help="traversal ray sets to run")
+    ap.add_argument("--reorder", default="on", choices=["on", "off"],
+                    help="traversal workload: trace rays in their origins' Morton order (WF_TRACE_REORDER)")
     ap.add_argument("--res", default="1920x1080", help="image size WxH (the workload is 1920x1080; smaller sizes "
                                                        "are for profiling captures)")
     args = ap.parse_args()

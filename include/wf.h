@@ -133,7 +133,11 @@ enum wf_trace_schedule {
 enum wf_trace_flags {
     WF_TRACE_ANY_HIT = 1u,       /* stop at the first accepted hit (shadow-ray query) */
     WF_TRACE_NO_CULL = 2u,       /* accept back-facing triangles (|det| test) */
-    WF_TRACE_COUNT_TRAFFIC = 4u  /* count node/instance/triangle fetches into wf_stats (slower) */
+    WF_TRACE_COUNT_TRAFFIC = 4u, /* count node/instance/triangle fetches into wf_stats (slower) */
+    WF_TRACE_REORDER = 8u        /* trace the rays in the order of their origins' Morton codes in the
+                                    scene box (a stable radix sort inside the call, timed with it):
+                                    rays that start close together run together and share nodes in
+                                    L2; the hits, still at each ray's own index, do not change */
 };
 
 /* Counters and timings of the most recent wf_render / wf_trace call. */

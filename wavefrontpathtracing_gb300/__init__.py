@@ -339,16 +339,18 @@ class Renderer:
         return p.value
 
     # ---- queries and builders
-    def trace(self, rays, any_hit=False, no_cull=False):
+    def trace(self, rays, any_hit=False, no_cull=False, reorder=False):
+        """reorder: trace the rays in the order of their origins' Morton codes (WF_TRACE_REORDER)."""
         rays = np.ascontiguousarray(rays, dtype=ray_dtype)
         hits = np.zeros(len(rays), dtype=hit_dtype)
-        flags = (abi.TRACE_ANY_HIT if any_hit else 0) | (abi.TRACE_NO_CULL if no_cull else 0)
+        flags = (abi.TRACE_ANY_HIT if any_hit else 0) | (abi.TRACE_NO_CULL if no_cull else 0) | \
+            (abi.TRACE_REORDER if reorder else 0)
         check(self.L.wf_trace(self.h, ptr(rays), len(rays), ptr(hits), flags))
         return hits
 
-    def trace_device(self, d_rays, n, d_hits, any_hit=False, no_cull=False, count_traffic=False):
+    def trace_device(self, d_rays, n, d_hits, any_hit=False, no_cull=False, count_traffic=False, reorder=False):
         flags = (abi.TRACE_ANY_HIT if any_hit else 0) | (abi.TRACE_NO_CULL if no_cull else 0) | \
-            (abi.TRACE_COUNT_TRAFFIC if count_traffic else 0)
+            (abi.TRACE_COUNT_TRAFFIC if count_traffic else 0) | (abi.TRACE_REORDER if reorder else 0)
         check(self.L.wf_trace_device(self.h, ctypes.c_void_p(d_rays), n, ctypes.c_void_p(d_hits), flags))
 
     def bvh_build(self, tris, interval_count=8, subdivide_single_prim=False, max_leaf_prims=0):

@@ -37,7 +37,7 @@ BSDF_LAMBERT, BSDF_METAL, BSDF_DIELECTRIC = 0, 1, 2
  RENDER_VIEW_MODE_GEOMETRY_BARYCENTRICS, RENDER_VIEW_MODE_GEOMETRY_NORMAL, RENDER_VIEW_MODE_GEOMETRY_UV,
  RENDER_VIEW_MODE_MATERIAL_BASE_COLOR, RENDER_VIEW_MODE_MATERIAL_NORMAL, RENDER_VIEW_MODE_MATERIAL_METALLIC_ROUGHNESS,
  RENDER_VIEW_MODE_MATERIAL_EMISSIVE, RENDER_VIEW_MODE_WORLD_NORMAL, RENDER_VIEW_MODE_RENDER_TARGET_DEPTH) = range(12)
-TRACE_ANY_HIT, TRACE_NO_CULL, TRACE_COUNT_TRAFFIC = 1, 2, 4
+TRACE_ANY_HIT, TRACE_NO_CULL, TRACE_COUNT_TRAFFIC, TRACE_REORDER = 1, 2, 4, 8
 
 
 class RenderSettings(ctypes.Structure):

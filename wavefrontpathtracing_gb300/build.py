@@ -21,7 +21,8 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libwf.so")
 LIB_CHECKED = os.path.join(LIBDIR, "libwf_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["wf_api.cu", "wf_trace.cu", "wf_shade.cu", "wf_tlas.cu", "wf_bvh.cu", "wf_batch.cu", "wf_mega.cu"]
+SOURCES = ["wf_api.cu", "wf_trace.cu", "wf_shade.cu", "wf_tlas.cu", "wf_bvh.cu", "wf_batch.cu", "wf_mega.cu",
+           "wf_sort.cu"]
 
 
 def nvcc():

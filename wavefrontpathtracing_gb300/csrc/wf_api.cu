@@ -147,6 +147,7 @@ struct wf_ctx {
     DevBuf<float4> image;
     DevBuf<uchar4> image_ldr;
     DevBuf<uint8_t> trace_io;
+    DevBuf<uint32_t> sort_scratch;          // WF_TRACE_REORDER: keys, permutation, digit counts
     uint32_t* status = nullptr;
     uint32_t* trace_fetch = nullptr;        // fetch counter of wf_trace / wf_trace_device
     Counters* counters = nullptr;
@@ -766,7 +767,7 @@ int wf_destroy(wf_ctx* c) {
     c->lights.release(); c->aabbs.release(); c->tlas_scratch.release();
     c->tri_albedo.release(); c->inst_tri_offset.release(); c->L_final.release(); c->dimage.release();
     c->g_albedo.release(); c->g_emission.release();
-    c->image.release(); c->image_ldr.release(); c->trace_io.release();
+    c->image.release(); c->image_ldr.release(); c->trace_io.release(); c->sort_scratch.release();
     dev_free(c->status); dev_free(c->counters); dev_free(c->totals); dev_free(c->trace_fetch);
     for (EventPair& p : c->events) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     if (c->t0) cudaEventDestroy(c->t0);
@@ -1550,17 +1551,25 @@ int wf_trace_device(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* h
     if (!c || (n && (!rays || !hits))) return fail(WF_ERR_INVALID, "wf_trace_device: null argument");
     if ((reinterpret_cast<uintptr_t>(rays) & 15u) != 0 || (reinterpret_cast<uintptr_t>(hits) & 3u) != 0)
         return fail(WF_ERR_INVALID, "wf_trace_device: rays must be 16-byte and hits 4-byte aligned");
-    if (flags & ~7u) return fail(WF_ERR_INVALID, "wf_trace_device: unknown flags");
+    if (flags & ~15u) return fail(WF_ERR_INVALID, "wf_trace_device: unknown flags");
     if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_trace_device: call wf_scene_end first");
     int rc = use_device(c);
     if (rc) return rc;
     const bool count = (flags & WF_TRACE_COUNT_TRAFFIC) != 0;
     if ((rc = begin_call(c, count))) return rc;
     WF_CUDA(cudaMemsetAsync(c->trace_fetch, 0, 4, c->stream));
+    const uint32_t *perm = nullptr, *varied = nullptr;
+    if ((flags & WF_TRACE_REORDER) && n) {
+        if ((rc = c->sort_scratch.reserve(reorder_scratch_words(n)))) return rc;
+        StageTimer t(c, true, ST_EXTEND);
+        WF_CUDA(launch_reorder_rays(reinterpret_cast<const float4*>(rays), n, c->tnodes.p, !c->scene_bi.empty(),
+                                    c->sort_scratch.p, &perm, &varied, c->stream));
+        c->launches += 1 + 3 * 5;   // keys, then upsweep + 3 scan kernels + downsweep per pass
+    }
     {
         StageTimer t(c, true, ST_EXTEND);
         WF_CUDA(launch_trace_aos(scene_refs(c), rays, n, hits, flags & 3u, count, c->trace_fetch, c->status,
-                                 c->counters, c->stream));
+                                 c->counters, c->stream, perm, varied));
     }
     c->launches++;
     c->launches_extend++;
@@ -1571,7 +1580,7 @@ int wf_trace_device(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* h
 
 int wf_trace(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* hits, uint32_t flags) {
     if (!c || (n && (!rays || !hits))) return fail(WF_ERR_INVALID, "wf_trace: null argument");
-    if (flags & ~7u) return fail(WF_ERR_INVALID, "wf_trace: unknown flags");
+    if (flags & ~15u) return fail(WF_ERR_INVALID, "wf_trace: unknown flags");
     if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_trace: call wf_scene_end first");
     if (n == 0) return WF_OK;
     int rc = use_device(c);

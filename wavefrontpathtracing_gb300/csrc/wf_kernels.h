@@ -89,9 +89,22 @@ struct WaveParams {
     float far_plane;
 };
 
-// fetch: a zeroed device counter the persistent kernel hands rays out from.
+// fetch: a zeroed device counter the persistent kernel hands rays out from;
+// perm (optional): trace ray perm[k] as the k-th ray (hits at the rays' own
+// indices) when the device word *varied is non-zero, ray k otherwise.
 cudaError_t launch_trace_aos(const SceneRefs& S, const void* rays, uint32_t n, void* hits, uint32_t flags,
-                             bool count, uint32_t* fetch, uint32_t* status, Counters* counters, cudaStream_t stream);
+                             bool count, uint32_t* fetch, uint32_t* status, Counters* counters, cudaStream_t stream,
+                             const uint32_t* perm = nullptr, const uint32_t* varied = nullptr);
+// Ray order for WF_TRACE_REORDER (wf_sort.cu): a stable radix sort of the rays
+// by the Morton code of their origin in the scene box (root = the TLAS root
+// node, unused when has_scene is false); scratch holds
+// reorder_scratch_words(n) words; *perm points into it on return and *varied
+// to a device word that stays 0 when every origin fell in one cell (the sort
+// then did nothing and perm must not be used).
+size_t reorder_scratch_words(uint32_t n);
+cudaError_t launch_reorder_rays(const float4* rays, uint32_t n, const float4* root, bool has_scene,
+                                uint32_t* scratch, const uint32_t** perm, const uint32_t** varied,
+                                cudaStream_t stream);
 // total (device) accumulates the number of rays each launch traced.
 cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
                           bool count, unsigned long long* total, cudaStream_t stream);

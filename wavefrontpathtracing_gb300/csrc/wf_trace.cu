@@ -140,13 +140,24 @@ int sm_count() {
 }
 
 cudaError_t launch_trace_aos(const SceneRefs& S, const void* rays, uint32_t n, void* hits, uint32_t flags,
-                             bool count, uint32_t* fetch, uint32_t* status, Counters* counters, cudaStream_t stream) {
+                             bool count, uint32_t* fetch, uint32_t* status, Counters* counters, cudaStream_t stream,
+                             const uint32_t* perm, const uint32_t* varied) {
     if (n == 0) return cudaSuccess;
     AosIO io;
     io.rays = static_cast<const float4*>(rays);
     io.hits = static_cast<uint32_t*>(hits);
     io.no_cull = (flags & 2u) != 0;
     const bool any = (flags & 1u) != 0;
+    if (perm) {
+        PermutedAosIO pio;
+        pio.io = io;
+        pio.perm = perm;
+        pio.varied = varied;
+        if (any) return count ? launch<true, true>(S, pio, nullptr, n, fetch, status, counters, nullptr, stream)
+                              : launch<true, false>(S, pio, nullptr, n, fetch, status, counters, nullptr, stream);
+        return count ? launch<false, true>(S, pio, nullptr, n, fetch, status, counters, nullptr, stream)
+                     : launch<false, false>(S, pio, nullptr, n, fetch, status, counters, nullptr, stream);
+    }
     if (any) return count ? launch<true, true>(S, io, nullptr, n, fetch, status, counters, nullptr, stream)
                           : launch<true, false>(S, io, nullptr, n, fetch, status, counters, nullptr, stream);
     return count ? launch<false, true>(S, io, nullptr, n, fetch, status, counters, nullptr, stream)

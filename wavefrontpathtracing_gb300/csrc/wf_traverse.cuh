@@ -82,6 +82,20 @@ struct AosIO {
     }
 };
 
+// The same rays traced in the order of a permutation (the k-th ray handed
+// out is ray perm[k]); each hit still lands at its ray's own index.
+struct PermutedAosIO {
+    AosIO io;
+    const uint32_t* perm;
+    const uint32_t* varied;   // 0: the permutation was not built (identity)
+    __device__ __forceinline__ uint32_t ray(uint32_t k) const { return *varied ? perm[k] : k; }
+    __device__ __forceinline__ void load(uint32_t k, V3& o, V3& d, float& tmax, bool& nc) const {
+        io.load(ray(k), o, d, tmax, nc);
+    }
+    __device__ __forceinline__ uint32_t root(uint32_t, const SceneRefs& S) const { return S.inst_count ? 0u : kInvalid; }
+    __device__ __forceinline__ void store(uint32_t k, const Hit& h, bool ok) const { io.store(ray(k), h, ok); }
+};
+
 template <bool ANY, bool COUNT, class IO>
 __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& io, uint32_t n, uint32_t* fetch,
                                                  LocalCounters& cnt, bool& overflow) {
