@@ -355,7 +355,11 @@ int wf_trace_device(wf_ctx* ctx, const RayDesc2* device_rays, uint32_t count,
 /* ---- stand-alone builders (bvh_builder_t / tlas_builder_t) --------------- */
 /* Builds a BLAS on the GPU; writes [bvh_header_t | extract()] byte-identical to
  * the reference builder's output at equal options.  *inout_size: capacity in,
- * bytes written out (WF_ERR_CAPACITY with the needed size if too small). */
+ * bytes written out (WF_ERR_CAPACITY with the needed size if too small, after
+ * a whole build).  The blob never exceeds WF_BVH_BLOB_MAX(triangle_count)
+ * bytes (at most 2n nodes of 32 bytes, 36 + 4 bytes per triangle), so a
+ * buffer of that size needs a single call. */
+#define WF_BVH_BLOB_MAX(n) (12ull + 104ull * (unsigned long long)(n))
 int wf_bvh_build(wf_ctx* ctx, const triangle_t* triangles, uint32_t triangle_count,
                  const wf_bvh_options* opts, void* out_blob, uint64_t* inout_size);
 /* Builds a TLAS on the GPU with the context's tlas_metric; with metric 0 it

@@ -88,6 +88,13 @@ def test_degenerate_inputs(orc, r):
     same = np.repeat(one, 17)
     for single in (False, True):
         assert np.array_equal(r.bvh_build(same, 8, single), orc.bvh_build(same, 8, single))
+    # leaves larger than one warp's subtree: a root of 3000 equal triangles, and
+    # 2500 equal triangles beside 2500 random ones (a large leaf below the root)
+    many = np.repeat(one, 3000)
+    assert np.array_equal(r.bvh_build(many, 8, False), orc.bvh_build(many, 8, False))
+    mixed = np.concatenate([np.repeat(one, 2500), scenes.triangle_soup(2500, seed=4)])
+    for ic, ml in ((8, 0), (16, 4)):
+        assert np.array_equal(r.bvh_build(mixed, ic, False, ml), orc.bvh_build(mixed, ic, False, ml))
     flat = scenes.triangle_soup(3000, seed=9)
     for v in ("v0", "v1", "v2"):
         flat[v]["position"][:, 1] = 0.25   # coplanar: zero extent on y
@@ -109,3 +116,33 @@ def test_signed_zero_bounds_match_the_reference_fold(orc, r):
         want = orc.bvh_build(tris, ic, single, ml)
         got = r.bvh_build(tris, ic, single, ml)
         assert np.array_equal(got, want), first_difference(got, want)
+
+
+def test_blob_capacity_contract(orc, r):
+    """wf_bvh_build: a buffer of the exact size or of WF_BVH_BLOB_MAX(n) takes
+    one call; a smaller one gets WF_ERR_CAPACITY with the needed size and is
+    left untouched."""
+    import ctypes
+
+    from wavefrontpathtracing_gb300 import BvhOptions, ptr
+
+    WF_ERR_CAPACITY = -3
+
+    tris = scenes.triangle_soup(3000, seed=11, mu=-4.0)
+    want = orc.bvh_build(tris, 16, False, 4)
+    assert len(want) <= 12 + 104 * len(tris)
+    o = BvhOptions(16, 0, 4)
+    for cap in (len(want), 12 + 104 * len(tris)):
+        buf = np.full(cap, 0xAB, dtype=np.uint8)
+        n = ctypes.c_uint64(cap)
+        assert r.L.wf_bvh_build(r.h, ptr(tris), len(tris), ctypes.byref(o), ptr(buf), ctypes.byref(n)) == 0
+        assert n.value == len(want)
+        assert np.array_equal(buf[:n.value], want)
+    small = np.full(len(want) - 1, 0xAB, dtype=np.uint8)
+    n = ctypes.c_uint64(small.nbytes)
+    assert r.L.wf_bvh_build(r.h, ptr(tris), len(tris), ctypes.byref(o), ptr(small), ctypes.byref(n)) == WF_ERR_CAPACITY
+    assert n.value == len(want)
+    assert (small == 0xAB).all()
+    n = ctypes.c_uint64(0)
+    assert r.L.wf_bvh_build(r.h, ptr(tris), len(tris), ctypes.byref(o), None, ctypes.byref(n)) == WF_ERR_CAPACITY
+    assert n.value == len(want)

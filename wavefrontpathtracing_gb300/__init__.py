@@ -356,11 +356,11 @@ class Renderer:
     def bvh_build(self, tris, interval_count=8, subdivide_single_prim=False, max_leaf_prims=0):
         tris = np.ascontiguousarray(tris, dtype=triangle_dtype)
         o = BvhOptions(interval_count, int(subdivide_single_prim), max_leaf_prims)
-        n = ctypes.c_uint64(0)
-        self.L.wf_bvh_build(self.h, ptr(tris), len(tris), ctypes.byref(o), None, ctypes.byref(n))
-        out = np.zeros(n.value, dtype=np.uint8)
+        # WF_BVH_BLOB_MAX: 2n nodes of 32 bytes at most, 40 bytes per triangle
+        out = np.empty(12 + 104 * len(tris), dtype=np.uint8)
+        n = ctypes.c_uint64(out.nbytes)
         check(self.L.wf_bvh_build(self.h, ptr(tris), len(tris), ctypes.byref(o), ptr(out), ctypes.byref(n)))
-        return out
+        return out[:n.value]   # pages past the blob were never touched
 
     def tlas_build(self, instances):
         inst = np.ascontiguousarray(instances, dtype=bvh_instance_dtype)

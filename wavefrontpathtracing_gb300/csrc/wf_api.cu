@@ -1605,15 +1605,12 @@ int wf_bvh_build(wf_ctx* c, const triangle_t* tris, uint32_t n, const wf_bvh_opt
     if (rc) return rc;
     wf_bvh_options o = opts ? *opts : wf_bvh_options{8, 0, 0};
     BvhBuildOut bo;
+    bo.keep_device = false;
+    bo.dst = static_cast<uint8_t*>(out);
+    bo.dst_capacity = out ? *inout_size : 0;
     if ((rc = gpu_bvh_build(tris, n, o, c->stream, &bo))) return fail(rc, bvh_last_error());
-    dev_free(bo.d_nodes);
-    dev_free(bo.d_tris);
-    if (!out || *inout_size < bo.blob.size()) {
-        *inout_size = bo.blob.size();
-        return fail(WF_ERR_CAPACITY, "wf_bvh_build: output buffer too small");
-    }
-    std::memcpy(out, bo.blob.data(), bo.blob.size());
-    *inout_size = bo.blob.size();
+    *inout_size = bo.blob_size;
+    if (!bo.in_dst) return fail(WF_ERR_CAPACITY, "wf_bvh_build: output buffer too small");
     return WF_OK;
 }
 

@@ -4,9 +4,10 @@
 // Why the output matches:
 //  * every float is computed with the reference's operations: centroid
 //    ((p0 + p1) + p2) * 0.3333f, bin (int)((c - cmin) * (bins / (cmax - cmin)))
-//    clamped to bins-1, and the SAH sweep run sequentially per node by one
-//    thread (half area, count * area, strict "<" over axis 0..2, then plane
-//    0..bins-2);
+//    clamped to bins-1, and the SAH sweep's per-plane costs (half area,
+//    count * area) with the first minimum over axis 0..2, then plane
+//    0..bins-2, as the reference's strict "<" picks it (one thread per node in
+//    the large phase, a warp scan over the bins in the small phase);
 //  * bin and node bounds are min/max reductions, whose value does not depend
 //    on the order (a -0.0/+0.0 tie is the one case where the reference keeps
 //    the first operand it saw; a bound holding both zero signs may differ in
@@ -29,10 +30,15 @@
 //
 // Phases: nodes with more than kSmall triangles are processed level by level
 // by many CTAs (chunked binning into shared-memory bins, chunked scans for the
-// partition); subtrees of at most kSmall triangles are built by one warp each.
+// partition); subtrees of at most kSmall triangles are built by one warp each,
+// entirely in shared memory.  The host side makes one scratch allocation,
+// gathers the positions on several threads and writes the blob straight into
+// the caller's buffer when it fits.
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "wf_bvh.h"
@@ -45,8 +51,11 @@ namespace {
 constexpr uint32_t kMaxBins = 64;
 constexpr uint32_t kChunk = 4096;      // positions per CTA in the large-node phase
 constexpr uint32_t kChunkThreads = 256;
-constexpr uint32_t kSmall = 1024;      // subtrees at most this large are built by one warp
-constexpr uint32_t kSmallWarps = 4;    // warps per CTA in the small phase
+#ifndef WF_BVH_SMALL
+#define WF_BVH_SMALL 128
+#endif
+constexpr uint32_t kSmall = WF_BVH_SMALL;   // subtrees at most this large are built by one warp
+static_assert(kSmall >= 32 && kSmall <= 65536, "16-bit local positions");
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint32_t kBinWords = 7;      // count, min xyz, max xyz (order-preserving keys)
 constexpr uint32_t kBoxWords = 18;     // node min/max, centroid min/max keys, first-zero positions
@@ -78,12 +87,11 @@ struct Ctx {
     uint32_t* idx_tmp;       // partition target
     uint32_t* F;             // per-position scratch: front right-goers by rank
     uint32_t* G;             // per-position scratch: back left-goers by rank
-    uint32_t* stack;         // per-position scratch: warp subtree stacks
     float4* ta;              // temporary nodes {min xyz, first}
     float4* tb;              //                 {max xyz, count}
     uint32_t* tleft;         // left child (kNone for leaves); right child = left + 1
     uint32_t* tdepth;
-    uint32_t* tcount;        // [0] nodes allocated, [1] maximum depth, [2] small roots
+    uint32_t* tcount;        // [0] nodes allocated, [1] maximum depth, [2] small roots, [3] error
     uint32_t* small_list;
 };
 
@@ -93,11 +101,15 @@ struct Plan {
     float lo, scale;
 };
 
-__device__ __forceinline__ bool goes_left(const Ctx& C, const Plan& P, uint32_t t) {
+// c = the triangle's centroid component on P.axis.
+__device__ __forceinline__ bool goes_left_c(const Ctx& C, const Plan& P, float c) {
     if (P.pos == 0) return false;
-    int32_t bin = (int32_t)((comp(C.cen[t], P.axis) - P.lo) * P.scale);
+    int32_t bin = (int32_t)((c - P.lo) * P.scale);
     if ((int32_t)C.bins - 1 < bin) bin = (int32_t)C.bins - 1;
     return (uint32_t)bin < P.pos;
+}
+__device__ __forceinline__ bool goes_left(const Ctx& C, const Plan& P, uint32_t t) {
+    return goes_left_c(C, P, comp(C.cen[t], P.axis));
 }
 
 // find_best_split_plane's sweep (bvh_builder.cpp:196-249) over bins laid out
@@ -137,9 +149,10 @@ __device__ float sah_sweep(const uint32_t* bins, uint32_t B, const float* cmn, c
 }
 
 // subdivide_node's decision (bvh_builder.cpp:104-118, 139-143) plus the
-// max_leaf_prims extension.  Reads the element at nL to place the split p.
-__device__ Plan make_plan(const Ctx& C, const uint32_t* bins, uint32_t first, uint32_t count, const float* nmn,
-                          const float* nmx, const float* cmn, const float* cmx) {
+// max_leaf_prims extension, without the split position p (which needs the
+// element at position nL: the caller places it).
+__device__ Plan make_plan_bins(const Ctx& C, const uint32_t* bins, uint32_t count, const float* nmn,
+                               const float* nmx, const float* cmn, const float* cmx) {
     Plan P{};
     uint32_t axis = 0, pos = 0;
     float cost = sah_sweep(bins, C.bins, cmn, cmx, axis, pos);
@@ -163,8 +176,149 @@ __device__ Plan make_plan(const Ctx& C, const uint32_t* bins, uint32_t first, ui
         for (uint32_t b = 0; b < pos; ++b) nl += ab[b * kBinWords];
     }
     P.nl = nl;
-    P.p = nl < count ? nl + (goes_left(C, P, C.idx[first + nl]) ? 0u : 1u) : count;
+    P.p = count;
     P.children = (nl > 0 && nl < count) ? 1u : 0u;
+    return P;
+}
+
+// The same, reading the element at nL from the position list.
+__device__ Plan make_plan(const Ctx& C, const uint32_t* bins, uint32_t first, uint32_t count, const float* nmn,
+                          const float* nmx, const float* cmn, const float* cmx) {
+    Plan P = make_plan_bins(C, bins, count, nmn, nmx, cmn, cmx);
+    if (P.partition && P.nl < count) P.p = P.nl + (goes_left(C, P, C.idx[first + P.nl]) ? 0u : 1u);
+    return P;
+}
+
+// Warp-parallel form of sah_sweep for the small phase: every lane returns the
+// same (cheapest, axis, pos) and nl = the triangles in bins [0, pos).  Lane l
+// holds bins [q*l, q*l + q) (q = 1 for up to 32 bins, else 2); shuffle scans
+// give each plane its left prefix and right suffix.  Prefix and suffix boxes
+// are min/max folds and counts are integer sums, so every plane's box, area
+// and cost are the same floats the sequential sweep computes (a bound that
+// folds -0.0 with +0.0 may keep the other zero, which changes no area); the
+// first minimum in (axis, plane) order wins, as with the strict "<".
+__device__ float warp_sweep(const uint32_t* bins, uint32_t B, const float* cmn, const float* cmx, uint32_t lane,
+                            uint32_t& axis, uint32_t& pos, uint32_t& nl) {
+    float cheapest = FLT_MAX;
+    axis = 0;
+    pos = 0;
+    nl = 0;
+    const uint32_t q = (B + 31) >> 5;
+    for (uint32_t a = 0; a < 3; ++a) {
+        if (cmn[a] == cmx[a]) continue;
+        const uint32_t* ab = bins + a * B * kBinWords;
+        uint32_t cnt[2];
+        float bmn[2][3], bmx[2][3];
+        for (uint32_t k = 0; k < 2; ++k) {
+            const uint32_t j = lane * q + k;
+            const bool have = k < q && j < B;
+            const uint32_t* e = ab + j * kBinWords;
+            cnt[k] = have ? e[0] : 0u;
+            for (int c = 0; c < 3; ++c) {
+                bmn[k][c] = have ? fdec(e[1 + c]) : FLT_MAX;
+                bmx[k][c] = have ? fdec(e[4 + c]) : -FLT_MAX;
+            }
+        }
+        // lane totals, then inclusive scans up (prefix) and down (suffix)
+        uint32_t pc = cnt[0] + cnt[1], sc = pc;
+        float pmn[3], pmx[3], smn[3], smx[3];
+        for (int c = 0; c < 3; ++c) {
+            pmn[c] = smn[c] = gmin(bmn[0][c], bmn[1][c]);
+            pmx[c] = smx[c] = gmax(bmx[0][c], bmx[1][c]);
+        }
+        for (uint32_t off = 1; off < 32; off <<= 1) {
+            const uint32_t oc = __shfl_up_sync(0xffffffffu, pc, off), uc = __shfl_down_sync(0xffffffffu, sc, off);
+            float omn[3], omx[3], umn[3], umx[3];
+            for (int c = 0; c < 3; ++c) {
+                omn[c] = __shfl_up_sync(0xffffffffu, pmn[c], off);
+                omx[c] = __shfl_up_sync(0xffffffffu, pmx[c], off);
+                umn[c] = __shfl_down_sync(0xffffffffu, smn[c], off);
+                umx[c] = __shfl_down_sync(0xffffffffu, smx[c], off);
+            }
+            if (lane >= off) {
+                pc += oc;
+                for (int c = 0; c < 3; ++c) { pmn[c] = gmin(pmn[c], omn[c]); pmx[c] = gmax(pmx[c], omx[c]); }
+            }
+            if (lane + off < 32) {
+                sc += uc;
+                for (int c = 0; c < 3; ++c) { smn[c] = gmin(smn[c], umn[c]); smx[c] = gmax(smx[c], umx[c]); }
+            }
+        }
+        // exclusive: lanes below (prefix) and above (suffix)
+        uint32_t ec = __shfl_up_sync(0xffffffffu, pc, 1), xc = __shfl_down_sync(0xffffffffu, sc, 1);
+        float emn[3], emx[3], xmn[3], xmx[3];
+        for (int c = 0; c < 3; ++c) {
+            emn[c] = __shfl_up_sync(0xffffffffu, pmn[c], 1);
+            emx[c] = __shfl_up_sync(0xffffffffu, pmx[c], 1);
+            xmn[c] = __shfl_down_sync(0xffffffffu, smn[c], 1);
+            xmx[c] = __shfl_down_sync(0xffffffffu, smx[c], 1);
+        }
+        if (lane == 0) {
+            ec = 0;
+            for (int c = 0; c < 3; ++c) { emn[c] = FLT_MAX; emx[c] = -FLT_MAX; }
+        }
+        if (lane == 31) {
+            xc = 0;
+            for (int c = 0; c < 3; ++c) { xmn[c] = FLT_MAX; xmx[c] = -FLT_MAX; }
+        }
+        // planes j (between bin j and j + 1) held by this lane, first minimum
+        float bc = INFINITY;
+        uint32_t bi = 0xFFFFFFFFu, bl = 0;
+        for (uint32_t k = 0; k < 2; ++k) {
+            const uint32_t j = lane * q + k;
+            if (k >= q || j + 1 >= B) continue;
+            uint32_t lc = ec + cnt[0], rc = xc;
+            float lmn[3], lmx[3], rmn[3], rmx[3];
+            for (int c = 0; c < 3; ++c) {
+                lmn[c] = gmin(emn[c], bmn[0][c]);
+                lmx[c] = gmax(emx[c], bmx[0][c]);
+                rmn[c] = xmn[c];
+                rmx[c] = xmx[c];
+            }
+            if (k == 1) {
+                lc += cnt[1];
+                for (int c = 0; c < 3; ++c) { lmn[c] = gmin(lmn[c], bmn[1][c]); lmx[c] = gmax(lmx[c], bmx[1][c]); }
+            } else if (q == 2) {
+                rc += cnt[1];
+                for (int c = 0; c < 3; ++c) { rmn[c] = gmin(rmn[c], bmn[1][c]); rmx[c] = gmax(rmx[c], bmx[1][c]); }
+            }
+            const float cost = (float)lc * half_area(lmn, lmx) + (float)rc * half_area(rmn, rmx);
+            if (cost < FLT_MAX && cost < bc) { bc = cost; bi = j; bl = lc; }
+        }
+        for (uint32_t off = 16; off > 0; off >>= 1) {
+            const float oc = __shfl_xor_sync(0xffffffffu, bc, off);
+            const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, off), ol = __shfl_xor_sync(0xffffffffu, bl, off);
+            if (oc < bc || (oc == bc && oi < bi)) { bc = oc; bi = oi; bl = ol; }
+        }
+        if (bc < cheapest) { axis = a; pos = bi + 1; cheapest = bc; nl = bl; }
+    }
+    return cheapest;
+}
+
+// make_plan_bins for a whole warp over shared-memory bins (all lanes return
+// the same plan, p not yet placed).
+__device__ Plan make_plan_warp(const Ctx& C, const uint32_t* bins, uint32_t count, const float* nmn,
+                               const float* nmx, const float* cmn, const float* cmx, uint32_t lane) {
+    Plan P{};
+    uint32_t axis, pos, nl;
+    const float cost = warp_sweep(bins, C.bins, cmn, cmx, lane, axis, pos, nl);
+    bool leaf;
+    if (C.single) {
+        leaf = count == 1;
+    } else {
+        bool force = C.max_leaf > 0 && count > C.max_leaf;
+        float parent = (float)count * half_area(nmn, nmx);
+        leaf = !force && cost >= parent;
+    }
+    P.axis = axis;
+    P.pos = pos;
+    P.partition = leaf ? 0u : 1u;
+    if (leaf) return P;
+    P.lo = cmn[axis];
+    P.scale = pos > 0 ? (float)C.bins / (cmx[axis] - cmn[axis]) : 0.0f;
+    P.nl = pos > 0 ? nl : 0u;
+    P.p = count;
+    P.children = (P.nl > 0 && P.nl < count) ? 1u : 0u;
     return P;
 }
 
@@ -574,89 +728,184 @@ __global__ void __launch_bounds__(kChunkThreads) k_child_bounds(Ctx C, Level Lv)
 }
 
 // ---------------------------------------------------------------- small-subtree phase
-__global__ void __launch_bounds__(32 * kSmallWarps) k_small(Ctx C, uint32_t nsmall) {
-    __shared__ uint32_t sbins[kSmallWarps][3 * kMaxBins * kBinWords];
-    const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const uint32_t w = blockIdx.x * kSmallWarps + wl;
-    if (w >= nsmall) return;   // uniform per warp
-    uint32_t* sb = sbins[wl];
-    const uint32_t root = C.small_list[w];
-    uint32_t* stk = C.stack + __float_as_uint(C.ta[root].w);
-    uint32_t sp = 1;
-    if (lane == 0) stk[0] = root;
-    __syncwarp();
+// One warp (one CTA) builds a whole subtree of at most kSmall triangles with
+// the subtree held in shared memory: each triangle's centroid, min and max
+// corner (component k of local triangle j at d[k * kSmall + j]), its index,
+// and a 16-bit permutation of local triangles that the partitions reorder.
+// Only the node records and the final index list go to global memory.  Node
+// ids come from one reservation of 2 * (count - 1) per subtree (a subtree of
+// count triangles splits at most count - 1 times); ids a subtree does not use
+// keep tdepth = kNone and are skipped by the renumbering.  The warp descends
+// into the smaller child and keeps the larger on a lane-distributed stack, so
+// at most log2(kSmall) + 1 entries are pending.
+struct SmallSmem {
+    float* d;
+    uint32_t* oidx;
+    uint16_t *perm, *ptmp, *F, *G;
+    uint32_t* bins;
+};
+
+__host__ __device__ constexpr size_t small_smem_bytes(uint32_t bins) {
+    return (9ull + 1ull) * 4ull * kSmall + 4ull * 2ull * kSmall + 4ull * 3ull * bins * kBinWords;
+}
+
+__global__ void __launch_bounds__(32) k_small(Ctx C, uint32_t nsmall, uint32_t tcap) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    SmallSmem S;
+    S.d = reinterpret_cast<float*>(smem_raw);
+    S.oidx = reinterpret_cast<uint32_t*>(S.d + 9 * kSmall);
+    S.perm = reinterpret_cast<uint16_t*>(S.oidx + kSmall);
+    S.ptmp = S.perm + kSmall;
+    S.F = S.ptmp + kSmall;
+    S.G = S.F + kSmall;
+    S.bins = reinterpret_cast<uint32_t*>(S.G + kSmall);
+    const uint32_t lane = threadIdx.x;
     const uint32_t words = 3 * C.bins * kBinWords;
-    while (sp > 0) {
-        const uint32_t X = stk[--sp];
-        __syncwarp();
-        const uint32_t first = __float_as_uint(C.ta[X].w), count = __float_as_uint(C.tb[X].w);
-        float v[12];
-        uint32_t zp[6];
-        box_init(v);
-        zero_init(zp);
+    for (uint32_t w = blockIdx.x; w < nsmall; w += gridDim.x) {
+        const uint32_t R = C.small_list[w];
+        const uint32_t gfirst = __float_as_uint(C.ta[R].w), count = __float_as_uint(C.tb[R].w);
+        const uint32_t depth0 = C.tdepth[R];
         for (uint32_t i = lane; i < count; i += 32) {
-            const uint32_t t = C.idx[first + i];
-            box_add(v, C, t);
-            zero_add(zp, C, t, first + i);
+            const uint32_t t = C.idx[gfirst + i];
+            const float4 c = C.cen[t], mn = C.tmn[t], mx = C.tmx[t];
+            S.d[0 * kSmall + i] = c.x;  S.d[1 * kSmall + i] = c.y;  S.d[2 * kSmall + i] = c.z;
+            S.d[3 * kSmall + i] = mn.x; S.d[4 * kSmall + i] = mn.y; S.d[5 * kSmall + i] = mn.z;
+            S.d[6 * kSmall + i] = mx.x; S.d[7 * kSmall + i] = mx.y; S.d[8 * kSmall + i] = mx.z;
+            S.oidx[i] = t;
+            S.perm[i] = (uint16_t)i;
         }
-        box_warp_reduce(v);
-        zero_warp_reduce(zp);
-        zero_fix(C, v, zp);
-        if (lane == 0) {
-            C.ta[X] = make_float4(v[0], v[1], v[2], __uint_as_float(first));
-            C.tb[X] = make_float4(v[3], v[4], v[5], __uint_as_float(count));
+        uint32_t L0 = 0;
+        if (lane == 0) L0 = atomicAdd(&C.tcount[0], 2u * (count - 1));
+        L0 = __shfl_sync(0xffffffffu, L0, 0);
+        if ((uint64_t)L0 + 2ull * (count - 1) > tcap) {   // cannot happen for tcap = 2n + 2n / kSmall + 4
+            if (lane == 0) atomicOr(&C.tcount[3], 1u);
+            continue;
         }
-        bool deg[3];
-        float lo[3], scale[3];
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = v[6 + a];
-            deg[a] = v[6 + a] == v[9 + a];
-            scale[a] = deg[a] ? 0.0f : (float)C.bins / (v[9 + a] - v[6 + a]);
-        }
-        bins_reset(sb, words, lane, 32);
         __syncwarp();
-        for (uint32_t i = lane; i < count; i += 32) bin_element(C, sb, C.idx[first + i], deg, lo, scale);
-        __syncwarp();
-        Plan P{};
-        if (lane == 0) P = make_plan(C, sb, first, count, v, v + 3, v + 6, v + 9);
-        P.axis = __shfl_sync(0xffffffffu, P.axis, 0);
-        P.pos = __shfl_sync(0xffffffffu, P.pos, 0);
-        P.nl = __shfl_sync(0xffffffffu, P.nl, 0);
-        P.p = __shfl_sync(0xffffffffu, P.p, 0);
-        P.partition = __shfl_sync(0xffffffffu, P.partition, 0);
-        P.children = __shfl_sync(0xffffffffu, P.children, 0);
-        P.lo = __shfl_sync(0xffffffffu, P.lo, 0);
-        P.scale = __shfl_sync(0xffffffffu, P.scale, 0);
-        if (!P.partition) continue;
-        for (int pass = 0; pass < 2; ++pass) {
-            uint32_t run = 0;
-            for (uint32_t base = 0; base < count; base += 32) {
-                const uint32_t i = base + lane;
-                const bool valid = i < count;
-                const uint32_t t = valid ? C.idx[first + i] : 0u;
-                const bool left = valid && goes_left(C, P, t);
-                const unsigned m = __ballot_sync(0xffffffffu, left);
-                const uint32_t lpre = run + __popc(m & ((1u << lane) - 1u));
-                if (valid) {
-                    if (pass == 0) partition_rank(C, P, first, i, left, lpre);
-                    else C.idx_tmp[first + partition_dst(C, P, first, count, i, left, lpre)] = t;
-                }
-                run += __popc(m);
+        uint32_t splits = 0, maxd = depth0, sp = 0;
+        uint32_t sX = 0, sf = 0, sc = 0, sd = 0;   // stack entry `lane`
+        uint32_t X = R, f = 0, c = count, dep = depth0;
+        for (;;) {
+            // node bounds, centroid bounds and first zero positions
+            float v[12];
+            uint32_t zp[6];
+            box_init(v);
+            zero_init(zp);
+            for (uint32_t i = lane; i < c; i += 32) {
+                const uint32_t j = S.perm[f + i];
+                float e[9];
+                for (int k = 0; k < 9; ++k) e[k] = S.d[k * kSmall + j];
+                v[0] = gmin(v[0], e[3]); v[1] = gmin(v[1], e[4]); v[2] = gmin(v[2], e[5]);
+                v[3] = gmax(v[3], e[6]); v[4] = gmax(v[4], e[7]); v[5] = gmax(v[5], e[8]);
+                v[6] = gmin(v[6], e[0]); v[7] = gmin(v[7], e[1]); v[8] = gmin(v[8], e[2]);
+                v[9] = gmax(v[9], e[0]); v[10] = gmax(v[10], e[1]); v[11] = gmax(v[11], e[2]);
+                for (int k = 0; k < 6; ++k)
+                    if (e[3 + k] == 0.0f && zp[k] == kNone) zp[k] = i;
             }
-            __syncwarp();
-        }
-        for (uint32_t i = lane; i < count; i += 32) C.idx[first + i] = C.idx_tmp[first + i];
-        __syncwarp();
-        if (P.children) {
-            uint32_t L = 0;
+            box_warp_reduce(v);
+            zero_warp_reduce(zp);
+            for (int k = 0; k < 6; ++k)
+                if (v[k] == 0.0f && zp[k] != kNone) v[k] = S.d[(3 + k) * kSmall + S.perm[f + zp[k]]];
             if (lane == 0) {
-                new_children(C, X, first, count, P.nl, L);
-                stk[sp] = L + 1;
-                stk[sp + 1] = L;
+                C.ta[X] = make_float4(v[0], v[1], v[2], __uint_as_float(gfirst + f));
+                C.tb[X] = make_float4(v[3], v[4], v[5], __uint_as_float(c));
+                C.tleft[X] = kNone;
+                C.tdepth[X] = dep;
             }
-            sp += 2;
+            bool deg[3];
+            float lo[3], scale[3];
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = v[6 + a];
+                deg[a] = v[6 + a] == v[9 + a];
+                scale[a] = deg[a] ? 0.0f : (float)C.bins / (v[9 + a] - v[6 + a]);
+            }
+            bins_reset(S.bins, words, lane, 32);
             __syncwarp();
+            for (uint32_t i = lane; i < c; i += 32) {
+                const uint32_t j = S.perm[f + i];
+                for (uint32_t a = 0; a < 3; ++a) {
+                    if (deg[a]) continue;
+                    int32_t bin = (int32_t)((S.d[a * kSmall + j] - lo[a]) * scale[a]);
+                    if ((int32_t)C.bins - 1 < bin) bin = (int32_t)C.bins - 1;
+                    uint32_t* e = S.bins + (a * C.bins + (uint32_t)bin) * kBinWords;
+                    atomicAdd(&e[0], 1u);
+                    atomicMin(&e[1], fenc(S.d[3 * kSmall + j]));
+                    atomicMin(&e[2], fenc(S.d[4 * kSmall + j]));
+                    atomicMin(&e[3], fenc(S.d[5 * kSmall + j]));
+                    atomicMax(&e[4], fenc(S.d[6 * kSmall + j]));
+                    atomicMax(&e[5], fenc(S.d[7 * kSmall + j]));
+                    atomicMax(&e[6], fenc(S.d[8 * kSmall + j]));
+                }
+            }
+            __syncwarp();
+            Plan P = make_plan_warp(C, S.bins, c, v, v + 3, v + 6, v + 9, lane);
+            if (P.partition && P.nl < c)
+                P.p = P.nl + (goes_left_c(C, P, S.d[P.axis * kSmall + S.perm[f + P.nl]]) ? 0u : 1u);
+            __syncwarp();
+            if (P.partition) {
+                // the closed form of the two-pointer partition (see the file head),
+                // positions relative to the node's first position f
+                for (int pass = 0; pass < 2; ++pass) {
+                    uint32_t run = 0;
+                    for (uint32_t base = 0; base < c; base += 32) {
+                        const uint32_t i = base + lane;
+                        const bool valid = i < c;
+                        const uint32_t j = valid ? S.perm[f + i] : 0u;
+                        const bool left = valid && goes_left_c(C, P, S.d[P.axis * kSmall + j]);
+                        const unsigned m = __ballot_sync(0xffffffffu, left);
+                        const uint32_t lpre = run + __popc(m & ((1u << lane) - 1u));
+                        if (valid) {
+                            if (pass == 0) {
+                                if (i < P.p && !left) S.F[f + (i - lpre)] = (uint16_t)i;
+                                else if (i >= P.p && left) S.G[f + (P.nl - lpre) - 1] = (uint16_t)i;
+                            } else {
+                                uint32_t dst;
+                                if (i < P.p) {
+                                    const uint32_t mm = i - lpre + 1;
+                                    dst = left ? i : (mm == 1 ? c : (uint32_t)S.G[f + mm - 2]) - 1;
+                                } else {
+                                    dst = !left ? i - 1 : (uint32_t)S.F[f + (P.nl - lpre) - 1];
+                                }
+                                S.ptmp[f + dst] = (uint16_t)j;
+                            }
+                        }
+                        run += __popc(m);
+                    }
+                    __syncwarp();
+                }
+                for (uint32_t i = lane; i < c; i += 32) S.perm[f + i] = S.ptmp[f + i];
+                __syncwarp();
+            }
+            if (P.children) {
+                const uint32_t L = L0 + 2 * splits++;
+                if (lane == 0) C.tleft[X] = L;
+                const uint32_t nl = P.nl, nr = c - P.nl;
+                maxd = max(maxd, dep + 1);
+                // descend into the smaller child, push the larger
+                const bool go_left = nl <= nr;
+                if (lane == sp) {
+                    sX = go_left ? L + 1 : L;
+                    sf = go_left ? f + nl : f;
+                    sc = go_left ? nr : nl;
+                    sd = dep + 1;
+                }
+                ++sp;
+                X = go_left ? L : L + 1;
+                f = go_left ? f : f + nl;
+                c = go_left ? nl : nr;
+                dep = dep + 1;
+                continue;
+            }
+            if (sp == 0) break;
+            --sp;
+            X = __shfl_sync(0xffffffffu, sX, sp);
+            f = __shfl_sync(0xffffffffu, sf, sp);
+            c = __shfl_sync(0xffffffffu, sc, sp);
+            dep = __shfl_sync(0xffffffffu, sd, sp);
         }
+        for (uint32_t i = lane; i < count; i += 32) C.idx[gfirst + i] = S.oidx[S.perm[i]];
+        if (lane == 0) atomicMax(&C.tcount[1], maxd);
+        __syncwarp();
     }
 }
 
@@ -687,6 +936,7 @@ __global__ void k_rank(Ctx C, uint32_t T, uint32_t depth, const uint32_t* ic, ui
 __global__ void k_emit(Ctx C, uint32_t T, const uint32_t* rank, const uint32_t* fidx, float4* out) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t X = blockIdx.x * blockDim.x + threadIdx.x; X < T; X += stride) {
+        if (C.tdepth[X] == kNone) continue;   // id reserved by a small subtree but not used
         const float4 a = C.ta[X], b = C.tb[X];
         const bool internal = C.tleft[X] != kNone;
         const uint32_t f = fidx[X];
@@ -707,22 +957,43 @@ __global__ void k_leaf_tris(Ctx C, float4* out) {
 }
 
 // ---------------------------------------------------------------- host side
-struct Pool {
-    std::vector<void*> blocks;
-    cudaError_t err = cudaSuccess;
+// One device allocation for all of a build's scratch, carved into 256-byte
+// aligned parts (one cudaMalloc / cudaFree per build instead of one per array).
+struct Arena {
+    size_t bytes = 0;
     template <typename T>
-    T* get(size_t count) {
-        void* p = nullptr;
-        if (err != cudaSuccess) return nullptr;
-        err = dmalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
-        if (err != cudaSuccess) return nullptr;
-        blocks.push_back(p);
-        return static_cast<T*>(p);
-    }
-    ~Pool() {
-        for (void* p : blocks) dfree(p);
+    size_t part(size_t count) {
+        const size_t off = bytes;
+        bytes += (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~size_t(255);
+        return off;
     }
 };
+
+struct DeviceBlock {
+    void* p = nullptr;
+    ~DeviceBlock() { dfree(p); }
+};
+
+// f(lo, hi) over [0, n) on up to 16 host threads (inline if a thread cannot start).
+template <typename F>
+void host_parallel(uint64_t n, uint64_t grain, F f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const uint64_t parts = std::min<uint64_t>(std::min(hw, 16u), (n + grain - 1) / grain);
+    if (parts <= 1) { f(0, n); return; }
+    const uint64_t step = (n + parts - 1) / parts;
+    std::vector<std::thread> th;
+    for (uint64_t q = 1; q < parts; ++q) {
+        const uint64_t lo = q * step, hi = std::min(n, lo + step);
+        if (lo >= hi) continue;
+        try {
+            th.emplace_back(f, lo, hi);
+        } catch (...) {
+            f(lo, hi);
+        }
+    }
+    f(0, std::min(n, step));
+    for (auto& t : th) t.join();
+}
 
 unsigned blocks_for(uint64_t n, unsigned threads, unsigned cap = 152u * 16u) {
     uint64_t b = (n + threads - 1) / threads;
@@ -749,42 +1020,76 @@ int gpu_bvh_build(const triangle_t* tris, uint32_t n, const wf_bvh_options& o, c
         return WF_ERR_INVALID;
     }
     if (n > (1u << 30)) { g_err = "gpu_bvh_build: too many triangles"; return WF_ERR_CAPACITY; }
-    Pool pool;
-    std::vector<float> hpos(9ull * n);
-    for (uint32_t i = 0; i < n; ++i) {
-        std::memcpy(&hpos[9ull * i], tris[i].v0.position, 12);
-        std::memcpy(&hpos[9ull * i + 3], tris[i].v1.position, 12);
-        std::memcpy(&hpos[9ull * i + 6], tris[i].v2.position, 12);
-    }
     const uint32_t B = o.interval_count;
-    const uint64_t tcap = 2ull * n + 2;
+    // 2n + 2 ids hold any binary tree over n triangles; the small phase reserves
+    // 2 * (count - 1) per subtree, which can leave up to 2 * (large leaves) more
+    const uint64_t tcap = 2ull * n + 2ull * (n / kSmall) + 4;
     const uint32_t maxslots = n / kSmall + 2;
     const uint32_t maxchunks = n / kChunk + maxslots + 1;
+    const uint64_t max_nodes = 2ull * n;   // 2 + 2 * (internal nodes <= n - 1)
+
+    Arena A;
+    const size_t o_pos = A.part<float>(9ull * n), o_cen = A.part<float4>(n), o_tmn = A.part<float4>(n),
+                 o_tmx = A.part<float4>(n), o_idx = A.part<uint32_t>(n), o_idx_tmp = A.part<uint32_t>(n),
+                 o_F = A.part<uint32_t>(n), o_G = A.part<uint32_t>(n), o_ta = A.part<float4>(tcap),
+                 o_tb = A.part<float4>(tcap), o_tleft = A.part<uint32_t>(tcap), o_tdepth = A.part<uint32_t>(tcap),
+                 o_tcount = A.part<uint32_t>(4), o_small = A.part<uint32_t>(n);
+    const size_t o_st0 = A.part<uint32_t>(maxslots), o_st1 = A.part<uint32_t>(maxslots),
+                 o_sb0 = A.part<uint32_t>(kBoxWords * maxslots), o_sb1 = A.part<uint32_t>(kBoxWords * maxslots),
+                 o_bins = A.part<uint32_t>((size_t)maxslots * 3 * B * kBinWords),
+                 o_choff = A.part<uint32_t>(maxslots + 1), o_chl = A.part<uint32_t>(maxchunks),
+                 o_plan = A.part<Plan>(maxslots), o_child = A.part<uint32_t>(2ull * maxslots),
+                 o_next = A.part<uint32_t>(1), o_ic = A.part<uint32_t>(tcap), o_rank = A.part<uint32_t>(tcap),
+                 o_fidx = A.part<uint32_t>(tcap);
+    const size_t o_nodes = out->keep_device ? 0 : A.part<float4>(2 * max_nodes);
+    DeviceBlock scratch;
+    {
+        const cudaError_t e = dmalloc(&scratch.p, A.bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            g_err = std::string("gpu_bvh_build: cudaMalloc: ") + cudaGetErrorString(e);
+            return WF_ERR_OOM;
+        }
+    }
+    uint8_t* base = static_cast<uint8_t*>(scratch.p);
+    auto at = [base](size_t off) { return static_cast<void*>(base + off); };
+
+    // triangle positions, gathered on the host threads
+    std::unique_ptr<float[]> hpos(new (std::nothrow) float[9ull * n]);
+    if (!hpos) { g_err = "gpu_bvh_build: host allocation failed"; return WF_ERR_OOM; }
+    host_parallel(n, 1u << 16, [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            std::memcpy(&hpos[9 * i], tris[i].v0.position, 12);
+            std::memcpy(&hpos[9 * i + 3], tris[i].v1.position, 12);
+            std::memcpy(&hpos[9 * i + 6], tris[i].v2.position, 12);
+        }
+    });
+
     Ctx C{};
     C.n = n; C.bins = B; C.single = o.subdivide_single_prim ? 1u : 0u; C.max_leaf = o.max_leaf_prims;
-    float* d_pos = pool.get<float>(9ull * n);
+    float* d_pos = static_cast<float*>(at(o_pos));
     C.pos = d_pos;
-    C.cen = pool.get<float4>(n); C.tmn = pool.get<float4>(n); C.tmx = pool.get<float4>(n);
-    C.idx = pool.get<uint32_t>(n); C.idx_tmp = pool.get<uint32_t>(n);
-    C.F = pool.get<uint32_t>(n); C.G = pool.get<uint32_t>(n); C.stack = pool.get<uint32_t>(n);
-    C.ta = pool.get<float4>(tcap); C.tb = pool.get<float4>(tcap);
-    C.tleft = pool.get<uint32_t>(tcap); C.tdepth = pool.get<uint32_t>(tcap);
-    C.tcount = pool.get<uint32_t>(4);
-    C.small_list = pool.get<uint32_t>(n);
-    uint32_t* slot_tmp[2] = {pool.get<uint32_t>(maxslots), pool.get<uint32_t>(maxslots)};
-    uint32_t* slot_box[2] = {pool.get<uint32_t>(kBoxWords * maxslots), pool.get<uint32_t>(kBoxWords * maxslots)};
-    uint32_t* bins = pool.get<uint32_t>((size_t)maxslots * 3 * B * kBinWords);
-    uint32_t* chunk_off = pool.get<uint32_t>(maxslots + 1);
-    uint32_t* chunk_l = pool.get<uint32_t>(maxchunks);
-    Plan* plan = pool.get<Plan>(maxslots);
-    uint32_t* child_slot = pool.get<uint32_t>(2ull * maxslots);
-    uint32_t* next_count = pool.get<uint32_t>(1);
-    if (pool.err != cudaSuccess) {
-        g_err = std::string("gpu_bvh_build: cudaMalloc: ") + cudaGetErrorString(pool.err);
-        cudaGetLastError();
-        return WF_ERR_OOM;
-    }
-    BVH_CUDA(cudaMemcpyAsync(d_pos, hpos.data(), hpos.size() * 4, cudaMemcpyHostToDevice, st));
+    C.cen = static_cast<float4*>(at(o_cen)); C.tmn = static_cast<float4*>(at(o_tmn));
+    C.tmx = static_cast<float4*>(at(o_tmx));
+    C.idx = static_cast<uint32_t*>(at(o_idx)); C.idx_tmp = static_cast<uint32_t*>(at(o_idx_tmp));
+    C.F = static_cast<uint32_t*>(at(o_F)); C.G = static_cast<uint32_t*>(at(o_G));
+    C.ta = static_cast<float4*>(at(o_ta)); C.tb = static_cast<float4*>(at(o_tb));
+    C.tleft = static_cast<uint32_t*>(at(o_tleft)); C.tdepth = static_cast<uint32_t*>(at(o_tdepth));
+    C.tcount = static_cast<uint32_t*>(at(o_tcount));
+    C.small_list = static_cast<uint32_t*>(at(o_small));
+    uint32_t* slot_tmp[2] = {static_cast<uint32_t*>(at(o_st0)), static_cast<uint32_t*>(at(o_st1))};
+    uint32_t* slot_box[2] = {static_cast<uint32_t*>(at(o_sb0)), static_cast<uint32_t*>(at(o_sb1))};
+    uint32_t* bins = static_cast<uint32_t*>(at(o_bins));
+    uint32_t* chunk_off = static_cast<uint32_t*>(at(o_choff));
+    uint32_t* chunk_l = static_cast<uint32_t*>(at(o_chl));
+    Plan* plan = static_cast<Plan*>(at(o_plan));
+    uint32_t* child_slot = static_cast<uint32_t*>(at(o_child));
+    uint32_t* next_count = static_cast<uint32_t*>(at(o_next));
+    uint32_t* ic = static_cast<uint32_t*>(at(o_ic));
+    uint32_t* rank = static_cast<uint32_t*>(at(o_rank));
+    uint32_t* fidx = static_cast<uint32_t*>(at(o_fidx));
+
+    BVH_CUDA(cudaMemcpyAsync(d_pos, hpos.get(), 36ull * n, cudaMemcpyHostToDevice, st));
     k_prep<<<blocks_for(n, 256), 256, 0, st>>>(C);
     // root = temporary node 0
     {
@@ -848,24 +1153,24 @@ int gpu_bvh_build(const triangle_t* tris, uint32_t n, const wf_bvh_options& o, c
         BVH_CUDA(cudaStreamSynchronize(st));
         cur ^= 1;
     }
-    uint32_t counts[3];
+    uint32_t counts[4];
     BVH_CUDA(cudaMemcpyAsync(counts, C.tcount, 12, cudaMemcpyDeviceToHost, st));
     BVH_CUDA(cudaStreamSynchronize(st));
     if (counts[2] > 0) {
-        k_small<<<(counts[2] + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, 0, st>>>(C, counts[2]);
+        // ids from counts[0] on are reserved per small subtree; unused ones keep depth kNone
+        BVH_CUDA(cudaMemsetAsync(C.tdepth + counts[0], 0xFF, 4ull * (tcap - counts[0]), st));
+        const size_t smem = small_smem_bytes(B);
+        BVH_CUDA(cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_small<<<counts[2], 32, smem, st>>>(C, counts[2], (uint32_t)tcap);
         BVH_CUDA(cudaGetLastError());
     }
-    BVH_CUDA(cudaMemcpyAsync(counts, C.tcount, 12, cudaMemcpyDeviceToHost, st));
+    BVH_CUDA(cudaMemcpyAsync(counts, C.tcount, 16, cudaMemcpyDeviceToHost, st));
     BVH_CUDA(cudaStreamSynchronize(st));
-    const uint32_t T = counts[0], maxd = counts[1];
-    uint32_t* ic = pool.get<uint32_t>(T);
-    uint32_t* rank = pool.get<uint32_t>(T);
-    uint32_t* fidx = pool.get<uint32_t>(T);
-    if (pool.err != cudaSuccess) {
-        g_err = "gpu_bvh_build: cudaMalloc failed";
-        cudaGetLastError();
-        return WF_ERR_OOM;
+    if (counts[3] != 0) {
+        g_err = "gpu_bvh_build: small-subtree node ids exceeded the reserved range";
+        return WF_ERR_CAPACITY;
     }
+    const uint32_t T = counts[0], maxd = counts[1];
     const unsigned tgrid = blocks_for(T, 256);
     for (int d = (int)maxd; d >= 0; --d) k_internal_count<<<tgrid, 256, 0, st>>>(C, T, (uint32_t)d, ic);
     BVH_CUDA(cudaMemsetAsync(rank, 0, 4, st));
@@ -877,28 +1182,51 @@ int gpu_bvh_build(const triangle_t* tris, uint32_t n, const wf_bvh_options& o, c
     const uint32_t nc = 2 + 2 * internal;
     float4* d_nodes = nullptr;
     float4* d_tris = nullptr;
-    BVH_CUDA(dmalloc(reinterpret_cast<void**>(&d_nodes), 32ull * nc));
-    if (dmalloc(reinterpret_cast<void**>(&d_tris), 48ull * n) != cudaSuccess) {
-        dfree(d_nodes);
-        cudaGetLastError();
-        g_err = "gpu_bvh_build: cudaMalloc failed";
-        return WF_ERR_OOM;
+    if (out->keep_device) {
+        BVH_CUDA(dmalloc(reinterpret_cast<void**>(&d_nodes), 32ull * nc));
+        if (dmalloc(reinterpret_cast<void**>(&d_tris), 48ull * n) != cudaSuccess) {
+            dfree(d_nodes);
+            cudaGetLastError();
+            g_err = "gpu_bvh_build: cudaMalloc failed";
+            return WF_ERR_OOM;
+        }
+    } else {
+        d_nodes = static_cast<float4*>(at(o_nodes));
     }
+    auto drop = [&]() {
+        if (out->keep_device) {
+            dfree(d_nodes);
+            dfree(d_tris);
+        }
+    };
     cudaError_t e = cudaMemsetAsync(d_nodes, 0, 32ull * nc, st);
     k_emit<<<tgrid, 256, 0, st>>>(C, T, rank, fidx, d_nodes);
-    k_leaf_tris<<<blocks_for(n, 256), 256, 0, st>>>(C, d_tris);
+    if (d_tris) k_leaf_tris<<<blocks_for(n, 256), 256, 0, st>>>(C, d_tris);
     if (e == cudaSuccess) e = cudaGetLastError();
-    // blob: [header | nodes | bvh_triangle_t (original order) | index list]
+    // blob: [header | nodes | bvh_triangle_t (original order) | index list], written
+    // straight into the caller's buffer when it is large enough
     const uint64_t nodes_bytes = 32ull * nc, tri_bytes = 36ull * n, idx_bytes = 4ull * n;
-    out->blob.resize(12 + nodes_bytes + tri_bytes + idx_bytes);
-    uint8_t* blob = out->blob.data();
+    const uint64_t size = 12 + nodes_bytes + tri_bytes + idx_bytes;
+    uint8_t* blob;
+    if (out->dst && out->dst_capacity >= size) {
+        blob = out->dst;
+        out->in_dst = true;
+    } else {
+        out->blob.resize(size);
+        blob = out->blob.data();
+        out->in_dst = false;
+    }
+    out->blob_size = size;
     if (e == cudaSuccess) e = cudaMemcpyAsync(blob + 12, d_nodes, nodes_bytes, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(blob + 12 + nodes_bytes + tri_bytes, C.idx, idx_bytes, cudaMemcpyDeviceToHost, st);
+    uint8_t* tri_dst = blob + 12 + nodes_bytes;
+    host_parallel(tri_bytes, 1u << 22, [&](uint64_t lo, uint64_t hi) {
+        std::memcpy(tri_dst + lo, reinterpret_cast<const uint8_t*>(hpos.get()) + lo, hi - lo);
+    });
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
-        dfree(d_nodes);
-        dfree(d_tris);
+        drop();
         g_err = std::string("gpu_bvh_build: ") + cudaGetErrorString(e);
         return WF_ERR_CUDA;
     }
@@ -907,13 +1235,12 @@ int gpu_bvh_build(const triangle_t* tris, uint32_t n, const wf_bvh_options& o, c
     h.triangles_offset = (uint32_t)(12 + nodes_bytes);
     h.indices_offset = (uint32_t)(12 + nodes_bytes + tri_bytes);
     std::memcpy(blob, &h, 12);
-    std::memcpy(blob + h.triangles_offset, hpos.data(), tri_bytes);
     bvh_node_t root;
     std::memcpy(&root, blob + 12, 32);
     std::memcpy(out->root_min, root.aabb_min, 12);
     std::memcpy(out->root_max, root.aabb_max, 12);
     out->node_count = nc;
-    out->d_nodes = d_nodes;
+    out->d_nodes = out->keep_device ? d_nodes : nullptr;
     out->d_tris = d_tris;
     return WF_OK;
 }

@@ -8,10 +8,17 @@
 namespace wf {
 
 struct BvhBuildOut {
+    // in
+    bool keep_device = true;       // keep d_nodes / d_tris (a mesh's device BLAS)
+    uint8_t* dst = nullptr;        // optional caller buffer for the blob
+    uint64_t dst_capacity = 0;
+    // out
     uint32_t node_count = 0;
     float4* d_nodes = nullptr;     // 2 x float4 per node (reference bvh_node_t layout)
     float4* d_tris = nullptr;      // 3 x float4 per triangle in leaf order {v0, idx} {e1} {e2}
-    std::vector<uint8_t> blob;     // [bvh_header_t | nodes | bvh_triangle_t | uint32 index]
+    std::vector<uint8_t> blob;     // [bvh_header_t | nodes | bvh_triangle_t | uint32 index] unless in_dst
+    uint64_t blob_size = 0;
+    bool in_dst = false;           // the blob went to dst (capacity sufficed)
     float root_min[3], root_max[3];
 };
 
