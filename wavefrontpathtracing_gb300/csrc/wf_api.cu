@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include <atomic>
 #include <mutex>
 #include <unordered_map>
 
@@ -304,19 +305,21 @@ void free_mesh(Mesh& m) {
 
 int upload_shading_tris(wf_ctx* c, Mesh& m) {
     std::vector<float4> st(6ull * m.tri_count);
-    for (uint32_t i = 0; i < m.tri_count; ++i) {
-        const triangle_t& t = m.tris[i];
-        const vertex_t* v[3] = {&t.v0, &t.v1, &t.v2};
-        for (int k = 0; k < 3; ++k) {
-            st[6ull * i + k] = make_float4(v[k]->position[0], v[k]->position[1], v[k]->position[2], 0.0f);
-            st[6ull * i + 3 + k] = make_float4(v[k]->normal[0], v[k]->normal[1], v[k]->normal[2], 0.0f);
+    host_parallel(m.tri_count, 1u << 15, [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            const triangle_t& t = m.tris[i];
+            const vertex_t* v[3] = {&t.v0, &t.v1, &t.v2};
+            for (int k = 0; k < 3; ++k) {
+                st[6 * i + k] = make_float4(v[k]->position[0], v[k]->position[1], v[k]->position[2], 0.0f);
+                st[6 * i + 3 + k] = make_float4(v[k]->normal[0], v[k]->normal[1], v[k]->normal[2], 0.0f);
+            }
+            // vertex uv in the .w slots: {p0, u0} {p1, v0} {p2, u1} {n0, v1} {n1, u2} {n2, v2}
+            for (int k = 0; k < 3; ++k) {
+                st[6 * i + 2 * k].w = v[k]->uv[0];
+                st[6 * i + 2 * k + 1].w = v[k]->uv[1];
+            }
         }
-        // vertex uv in the .w slots: {p0, u0} {p1, v0} {p2, u1} {n0, v1} {n1, u2} {n2, v2}
-        for (int k = 0; k < 3; ++k) {
-            st[6ull * i + 2 * k].w = v[k]->uv[0];
-            st[6ull * i + 2 * k + 1].w = v[k]->uv[1];
-        }
-    }
+    });
     int rc = dev_alloc(&m.d_stri, st.size());
     if (rc) return rc;
     WF_CUDA(h2d(c, m.d_stri, st.data(), st.size() * sizeof(float4)));
@@ -830,13 +833,20 @@ int wf_mesh_create(wf_ctx* c, const vertex_t* vertices, uint32_t nv, const uint3
         return fail(WF_ERR_INVALID, "wf_mesh_create: bad argument");
     const uint32_t n = ni / 3;
     std::vector<triangle_t> tris(n);
-    for (uint32_t t = 0; t < n; ++t) {
-        uint32_t a = indices[3 * t], b = indices[3 * t + 1], d = indices[3 * t + 2];
-        if (a >= nv || b >= nv || d >= nv) return fail(WF_ERR_INVALID, "wf_mesh_create: index out of range");
-        tris[t].v0 = vertices[a];
-        tris[t].v1 = vertices[b];
-        tris[t].v2 = vertices[d];
-    }
+    std::atomic<bool> bad{false};
+    host_parallel(n, 1u << 15, [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t t = lo; t < hi; ++t) {
+            uint32_t a = indices[3 * t], b = indices[3 * t + 1], d = indices[3 * t + 2];
+            if (a >= nv || b >= nv || d >= nv) {
+                bad.store(true, std::memory_order_relaxed);
+                return;
+            }
+            tris[t].v0 = vertices[a];
+            tris[t].v1 = vertices[b];
+            tris[t].v2 = vertices[d];
+        }
+    });
+    if (bad.load()) return fail(WF_ERR_INVALID, "wf_mesh_create: index out of range");
     wf_bvh_options o = opts ? *opts : wf_bvh_options{8, 0, 0};
     int rc = use_device(c);
     if (rc) return rc;

@@ -38,7 +38,6 @@
 #include <cstring>
 #include <memory>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "wf_bvh.h"
@@ -973,27 +972,6 @@ struct DeviceBlock {
     void* p = nullptr;
     ~DeviceBlock() { dfree(p); }
 };
-
-// f(lo, hi) over [0, n) on up to 16 host threads (inline if a thread cannot start).
-template <typename F>
-void host_parallel(uint64_t n, uint64_t grain, F f) {
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const uint64_t parts = std::min<uint64_t>(std::min(hw, 16u), (n + grain - 1) / grain);
-    if (parts <= 1) { f(0, n); return; }
-    const uint64_t step = (n + parts - 1) / parts;
-    std::vector<std::thread> th;
-    for (uint64_t q = 1; q < parts; ++q) {
-        const uint64_t lo = q * step, hi = std::min(n, lo + step);
-        if (lo >= hi) continue;
-        try {
-            th.emplace_back(f, lo, hi);
-        } catch (...) {
-            f(lo, hi);
-        }
-    }
-    f(0, std::min(n, step));
-    for (auto& t : th) t.join();
-}
 
 unsigned blocks_for(uint64_t n, unsigned threads, unsigned cap = 152u * 16u) {
     uint64_t b = (n + threads - 1) / threads;

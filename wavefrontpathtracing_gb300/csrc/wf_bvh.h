@@ -1,6 +1,8 @@
 // wf_bvh.h — GPU binned-SAH BLAS builder (bvh_builder.cpp:6-264 semantics).
 #pragma once
+#include <algorithm>
 #include <cstdint>
+#include <thread>
 #include <vector>
 #include <cuda_runtime.h>
 #include "../../include/wf.h"
@@ -26,6 +28,28 @@ struct BvhBuildOut {
 int gpu_bvh_build(const triangle_t* tris, uint32_t n, const wf_bvh_options& opts, cudaStream_t stream,
                   BvhBuildOut* out);
 const char* bvh_last_error();
+
+// f(lo, hi) over [0, n) in parts of at least `grain`, on up to 16 host threads
+// (a part whose thread cannot start runs on the caller's thread).
+template <typename F>
+void host_parallel(uint64_t n, uint64_t grain, F f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const uint64_t parts = std::min<uint64_t>(std::min(hw, 16u), (n + grain - 1) / grain);
+    if (parts <= 1) { f(0, n); return; }
+    const uint64_t step = (n + parts - 1) / parts;
+    std::vector<std::thread> th;
+    for (uint64_t q = 1; q < parts; ++q) {
+        const uint64_t lo = q * step, hi = std::min(n, lo + step);
+        if (lo >= hi) continue;
+        try {
+            th.emplace_back(f, lo, hi);
+        } catch (...) {
+            f(lo, hi);
+        }
+    }
+    f(0, std::min(n, step));
+    for (auto& t : th) t.join();
+}
 
 // The library's accounted device allocator (wf_api.cu).
 cudaError_t dmalloc(void** p, size_t bytes);
