@@ -268,14 +268,17 @@ def adjoint_leg(device, tlas_metric):
                 "ratio": round(f_ms / a_ms, 3), "forward_ms": round(f_ms, 3), "adjoint_ms": round(a_ms, 3)}
 
 
-def batched_leg(device, tlas_metric, steps=3, count=64):
+def batched_leg(device, tlas_metric, steps=3, count=64, config=None):
     """Batched configuration: 64 scenes (displaced icosphere soups, triangles
     log-uniform in [1k, 2M]; square images of side 64..1024; spp 1, 4 or 16;
     depth 6, NEE, RR from 3) rendered as one batch (one CUDA-graph launch, pool
     parameters from the autotuner) against the same 64 scenes rendered one
     after another with wf_render (the plain single-scene wavefront loop).  Both
     sides are timed on the device with CUDA events; the plain side is the sum
-    of the 64 renders' GPU times.  Camera paths per second over all scenes."""
+    of the 64 renders' GPU times.  Camera paths per second over all scenes.
+    config: (capacity, regeneration threshold, block[, use_graph]) to use
+    instead of the autotuner's choice (profiling captures; use_graph 0 = the
+    host loop, the same kernels launched one by one)."""
     import wavefrontpathtracing_gb300 as wf
     from wavefrontpathtracing_gb300 import scenes
     depth, rr, seed = 6, 3, 11
@@ -298,7 +301,12 @@ def batched_leg(device, tlas_metric, steps=3, count=64):
                 b.submit(ids[mesh], l2w, mat)
             b.end_scene()
         t_tune = time.perf_counter()
-        cfg = b.autotune(frame_seed=seed, **kw)
+        if config is None:
+            cfg = b.autotune(frame_seed=seed, **kw)
+        else:
+            b.set_config(capacity=int(config[0]), regen_threshold=float(config[1]), block=int(config[2]),
+                         use_graph=int(config[3]) if len(config) > 3 else 1)
+            cfg = b.config()
         tune_s = time.perf_counter() - t_tune
         bms, bst = [], None
         for i in range(steps):
@@ -652,6 +660,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes leg")
     ap.add_argument("--no-megakernel", action="store_true", help="skip the megakernel A/B leg")
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-config", default=None,
+                    help="batched workload: CAPACITY,THRESHOLD,BLOCK[,USE_GRAPH] instead of the autotuner "
+                         "(profiling captures)")
     ap.add_argument("--tail-paths", type=int, default=0,
                     help="queue size below which a wave's remaining bounces run per path in one launch "
                          "(0 = never)")
@@ -675,7 +686,8 @@ def main():
         run_traversal(args, rank, world, local)
     elif args.workload == "batched":
         if rank == 0:
-            res = batched_leg(local, args.tlas_metric, steps=args.steps, count=args.batch_scenes)
+            cfg = args.batch_config.split(",") if args.batch_config else None
+            res = batched_leg(local, args.tlas_metric, steps=args.steps, count=args.batch_scenes, config=cfg)
             print(json.dumps({"metric": "batched camera paths/s vs plain wavefront", "value": res["batched_spp_per_s"],
                               "unit": "paths/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": res["batched_ms"], "higher_is_better": True, "dtype": "f32",

@@ -553,8 +553,14 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
             R nol = FMAX(K(0.0), FN(dot)(N, L));
             pdf = P->cosine_weighted_diffuse ? nol * ORC_INV_PI : ORC_INV_TWO_PI;
             R ip = K(1.0) / pdf;
-            wgt = FN(mk)((nol * (base.x * ORC_INV_PI)) * ip, (nol * (base.y * ORC_INV_PI)) * ip,
-                         (nol * (base.z * ORC_INV_PI)) * ip);
+            /* shade.hlsl:135 multiplies by 1 / pdf unguarded: a sample in the
+             * tangent plane (r1 == 1, or NoL rounding to 0) gives 0 * inf = NaN
+             * there.  Here the path ends (the GPU kernels do the same). */
+            if (ip <= MAXT)
+                wgt = FN(mk)((nol * (base.x * ORC_INV_PI)) * ip, (nol * (base.y * ORC_INV_PI)) * ip,
+                             (nol * (base.z * ORC_INV_PI)) * ip);
+            else
+                valid = 0;
         } else if (bsdf == 1) {
             R a2 = alpha * alpha;
             R cth = SQRT((K(1.0) - r1) / (K(1.0) + (a2 - K(1.0)) * r1));

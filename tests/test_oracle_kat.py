@@ -203,3 +203,26 @@ def test_equirect_environment_lookup(orc):
         want = env[int(w * 8), int(u * 16), :3]
         agree += np.array_equal(orc.env_texel(env, v), want)
     assert agree >= 495   # texel boundaries may round either way in float
+
+
+def test_tangent_plane_cosine_sample_ends_the_path(orc):
+    """Box scene at 512x512 (depth 6, per-triangle albedo 0.5, emitter strength
+    10, frame seed 5): sample 54 of pixel (494, 400) draws a cosine-weighted
+    direction in the tangent plane at its second hit.  The reference's
+    weight NoL * brdf * (1 / pdf) is 0 * inf = NaN there (shade.hlsl:123-135);
+    the oracle (and the GPU kernels) end the path instead, so the pixel stays
+    finite and FP32 agrees with FP64."""
+    from wavefrontpathtracing_gb300 import scenes
+    from tests.helpers import oracle_scene_from_desc
+    desc = scenes.box_scene(width=512, height=512, max_bounces=6)
+    sc = oracle_scene_from_desc(orc, desc)
+    sc.set_albedo(np.full((sc.triangle_count, 3), 0.5))
+    sc.set_emission(2, 10.0)
+    p = 400 * 512 + 494
+    kw = dict(max_bounces=6, spp=1, sample_offset=54, frame_seed=5, pixel_range=(p, p + 1))
+    a32, st = sc.render(desc.view, 512, 512, **kw)
+    a64, _ = sc.render(desc.view, 512, 512, f64=True, **kw)
+    v32, v64 = a32.reshape(-1, 4)[p], a64.reshape(-1, 4)[p]
+    assert st["extend_rays"][:2] == [1, 1] and sum(st["extend_rays"]) == 2   # no third segment
+    assert np.isfinite(v32).all() and v32[3] == 1
+    assert np.allclose(v32, v64, rtol=1e-5, atol=0)

@@ -271,8 +271,16 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
         const float nol = fmaxf(0.0f, dot(N, L));
         pdf = K.cosine ? nol * kInvPi : kInvTwoPi;
         const float ipdf = 1.0f / pdf;
-        wgt = mk((nol * (base_c.x * kInvPi)) * ipdf, (nol * (base_c.y * kInvPi)) * ipdf,
-                 (nol * (base_c.z * kInvPi)) * ipdf);
+        if (ipdf <= FLT_MAX) {
+            wgt = mk((nol * (base_c.x * kInvPi)) * ipdf, (nol * (base_c.y * kInvPi)) * ipdf,
+                     (nol * (base_c.z * kInvPi)) * ipdf);
+        } else {
+            // A cosine sample in the tangent plane (rand_float rounds to 1.0f, so
+            // sqrt(1 - r1) = 0, or the dot product rounds to 0): the reference's
+            // weight is 0 * inf = NaN (shade.hlsl:123-135) and its pixel turns
+            // NaN.  The path ends here instead.
+            valid = false;
+        }
     } else if (bsdf == 1u) {
         const float a2 = alpha * alpha;
         const float cth = sqrtf((1.0f - r1) / (1.0f + (a2 - 1.0f) * r1));
