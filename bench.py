@@ -390,6 +390,58 @@ def builders_leg(r, desc):
     return out
 
 
+def plain_small_leg(device, tlas_metric):
+    """The plain small configuration: box of 12 quads + icosphere (subdivision
+    5, radius 0.3) + emissive ceiling quad, 20,506 triangles; 256x256, 1 spp,
+    depth 4, Lambert only, no NEE.  GPU frame time (CUDA events, best of 5)
+    against the oracle's port of the reference's CPU path on all host cores
+    for the same frame (scene from the GPU's own blobs), the images compared
+    bit for bit; BLAS builds of its meshes on the GPU (through the C ABI) and
+    by the oracle's restatement of the reference's single-threaded builder."""
+    import wavefrontpathtracing_gb300 as wf
+    from wavefrontpathtracing_gb300 import scenes
+    from oracle import oracle as orc
+    from tests.helpers import oracle_scene_from_renderer
+    orc.build()
+    desc = scenes.box_scene(width=256, height=256, max_bounces=4)
+    o = desc.bvh_options
+    with wf.Renderer(256, 256, device=device, tlas_metric=tlas_metric) as r:
+        t0 = time.perf_counter()
+        ids = [r.create_mesh_from_triangles(t, interval_count=o["interval_count"], max_leaf_prims=o["max_leaf_prims"])
+               for t in desc.meshes]
+        gpu_build_ms = (time.perf_counter() - t0) * 1e3
+        r.begin_scene(desc.view, desc.settings["env"])
+        for mesh, l2w, mat in desc.instances:
+            r.submit_render_mesh(ids[mesh], l2w, mat)
+        r.end_scene()
+        ms = []
+        for i in range(6):
+            r.render(max_bounces=4, spp=1, frame_seed=1, accumulate=False)
+            ms.append(r.stats()["ms_total"])
+        st = r.stats()
+        img = r.read_image()
+        sc, _ = oracle_scene_from_renderer(orc, desc, r, ids)
+    t0 = time.perf_counter()
+    for t in desc.meshes:
+        orc.bvh_build(t, o["interval_count"], False, o["max_leaf_prims"])
+    cpu_build_ms = (time.perf_counter() - t0) * 1e3
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    acc, ost = sc.render(desc.view, 256, 256, max_bounces=4, spp=1, frame_seed=1, threads=threads)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    want = np.zeros_like(acc)
+    want[..., :3] = acc[..., :3] / acc[..., 3:]
+    want[..., 3] = acc[..., 3]
+    rays = st["rays_extend"] + st["rays_connect"]
+    gpu_ms = min(ms[1:])
+    return {"config": f"box scene 256x256, 1 spp, depth 4, {desc.triangle_count} triangles, Lambert, no NEE",
+            "gpu_ms": round(gpu_ms, 3), "gpu_mrays_per_s": round(rays / (gpu_ms / 1e3) / 1e6, 1),
+            "cpu_ms": round(cpu_ms, 1), "cpu_mrays_per_s": round(sum(ost["extend_rays"]) / (cpu_ms / 1e3) / 1e6, 2),
+            "cpu_cores": threads, "cpu_kind": "port",
+            "images_equal": bool(np.array_equal(img.view(np.uint32), want.view(np.uint32))),
+            "gpu_blas_build_ms": round(gpu_build_ms, 2), "cpu_blas_build_ms": round(cpu_build_ms, 2)}
+
+
 def flush_l2(torch, buf):
     if buf is not None:
         buf.add_(1)
@@ -507,6 +559,9 @@ def run_ours(args, rank, world, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         builders = builders_leg(r, desc)
     r.close()
+    small = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        small = plain_small_leg(local, args.tlas_metric)
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = adjoint_leg(local, args.tlas_metric)
@@ -557,6 +612,8 @@ def run_ours(args, rank, world, local):
             line["cpu_baseline"] = cpu
         if builders:
             line["builders"] = builders
+        if small:
+            line["plain_small"] = small
         if adjoint:
             line["adjoint"] = adjoint
         if batched:
@@ -566,6 +623,10 @@ def run_ours(args, rank, world, local):
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+CPU_TRACE_SAMPLE = 200_000   # first sample of rays per set traced by the oracle for the CPU baseline
+CPU_TRACE_SECONDS = 5.0      # the sample then grows to about this much CPU time
 
 
 def run_traversal(args, rank, world, local):
@@ -593,8 +654,20 @@ def run_traversal(args, rank, world, local):
         r.begin_scene(scenes.make_view((0.5, 0.5, -0.5), (0.5, 0.5, 0.5), 90.0, 16, 16))
         r.submit_render_mesh(mesh, np.eye(4))
         r.end_scene()
-        blas_bytes = len(r.mesh_blas(mesh))
+        blob = r.mesh_blas(mesh)
+        blas_bytes = len(blob)
         reorder = args.reorder == "on"
+        sc = None
+        if not args.no_cpu_baseline:
+            # the oracle's port of the reference's scalar traversal over the same BLAS / TLAS bytes
+            from oracle import oracle as orc
+            orc.build()
+            bi = r.scene_instances()
+            oi = np.zeros(1, dtype=orc.instance_dtype)
+            oi["local_to_world"] = np.eye(4, dtype=np.float32).reshape(16)
+            oi["world_to_local"] = bi[0]["world_to_local"]
+            sc = orc.Scene([(tris, blob)], r.scene_tlas(), oi)
+        del blob
         for kind in args.ray_kinds.split(","):
             rays = scenes.soup_rays(side, seed=7, kind=kind)
             for any_hit in (False, True):
@@ -641,6 +714,24 @@ def run_traversal(args, rank, world, local):
                                      "alg_bytes_per_launch": int(alg),
                                      "fetches_per_ray": round((c["blas_node_loads"] + c["tlas_node_loads"]) / len(rays), 2),
                                      "triangle_tests_per_ray": round(c["triangle_tests"] / len(rays), 2)}}
+                if sc is not None:
+                    # a random sample of the set, grown after a first pass to about CPU_TRACE_SECONDS
+                    threads = os.cpu_count() or 1
+                    n_cpu = CPU_TRACE_SAMPLE
+                    for _ in range(2):
+                        pick = np.sort(np.random.default_rng(5).choice(len(rays), n_cpu, replace=False))
+                        t1 = time.perf_counter()
+                        want, _, _ = sc.trace(rays[pick], flags=1 if any_hit else 0, threads=threads)
+                        cpu_s = time.perf_counter() - t1
+                        n_next = min(len(rays), int(n_cpu * CPU_TRACE_SECONDS / max(cpu_s, 1e-3)))
+                        if n_next <= 2 * n_cpu:
+                            break
+                        n_cpu = n_next
+                    line["cpu_baseline"] = {"value": round(len(pick) / cpu_s / 1e6, 3), "unit": "Mrays/s",
+                                            "cores": threads, "kind": "port",
+                                            "sample": f"{len(pick)} random rays of the set ({cpu_s:.2f} s)",
+                                            "sample_hits_equal": bool(np.array_equal(
+                                                hits[pick].view(np.uint32), want.view(np.uint32)))}
                 print(json.dumps(line), flush=True)
                 del d_rays, d_hits
 
