@@ -27,6 +27,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -108,8 +109,10 @@ class ClockSampler:
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-            self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+            # the raw samples go to $WF_CLOCKS_DIR (default: the system's temporary directory)
+            d = os.environ.get("WF_CLOCKS_DIR") or tempfile.gettempdir()
+            os.makedirs(d, exist_ok=True)
+            self.path = os.path.join(d, f"clocks_{os.getpid()}.csv")
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
