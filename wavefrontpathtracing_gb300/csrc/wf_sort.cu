@@ -39,6 +39,30 @@ __device__ __forceinline__ uint32_t cell8(float x, float lo, float inv) {
     return (uint32_t)(u * 256.0f) & 0xFFu;
 }
 
+// WF_SORT_DIR_BITS = k > 0: the key's top 24 - 3k bits are the origin's
+// Morton code at 8 - k bits per axis and its low 3k bits the Morton code of
+// the direction quantised to k bits per axis, so rays that start in one cell
+// are also ordered by where they go.
+#ifndef WF_SORT_DIR_BITS
+#define WF_SORT_DIR_BITS 0
+#endif
+static_assert(WF_SORT_DIR_BITS >= 0 && WF_SORT_DIR_BITS <= 4, "WF_SORT_DIR_BITS: 0..4");
+
+__device__ __forceinline__ uint32_t ray_key(const float4* __restrict__ rays, uint32_t i, float3 lo, float3 inv) {
+    const float4 o = __ldg(rays + 2ull * i);
+    constexpr int k = WF_SORT_DIR_BITS;
+    uint32_t key = (spread8(cell8(o.x, lo.x, inv.x) >> k) << 2) | (spread8(cell8(o.y, lo.y, inv.y) >> k) << 1) |
+                   spread8(cell8(o.z, lo.z, inv.z) >> k);
+    if constexpr (k > 0) {
+        const float4 d = __ldg(rays + 2ull * i + 1);
+        // direction components in [-1, 1] -> [0, 1] -> k bits (cell8 clamps and maps NaN to 0)
+        const uint32_t dx = cell8(d.x, -1.0f, 0.5f) >> (8 - k), dy = cell8(d.y, -1.0f, 0.5f) >> (8 - k),
+                       dz = cell8(d.z, -1.0f, 0.5f) >> (8 - k);
+        key = (key << (3 * k)) | (spread8(dx) << 2) | (spread8(dy) << 1) | spread8(dz);
+    }
+    return key;
+}
+
 // Key = 24-bit Morton code of the origin in the scene box (clamped), value =
 // the ray's index.  Without a scene every key is 0 (the input order stays).
 __global__ void k_origin_keys(const float4* __restrict__ rays, uint32_t n, const float4* __restrict__ root,
@@ -51,20 +75,10 @@ __global__ void k_origin_keys(const float4* __restrict__ rays, uint32_t n, const
         const float ex = b.x - a.x, ey = b.y - a.y, ez = b.z - a.z;
         inv = make_float3(ex > 0.f ? 1.0f / ex : 0.f, ey > 0.f ? 1.0f / ey : 0.f, ez > 0.f ? 1.0f / ez : 0.f);
     }
-    uint32_t key0 = 0;
-    if (has_scene) {
-        const float4 o = __ldg(rays);
-        key0 = (spread8(cell8(o.x, lo.x, inv.x)) << 2) | (spread8(cell8(o.y, lo.y, inv.y)) << 1) |
-               spread8(cell8(o.z, lo.z, inv.z));
-    }
+    const uint32_t key0 = has_scene ? ray_key(rays, 0u, lo, inv) : 0u;
     bool differs = false;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t key = 0;
-        if (has_scene) {
-            const float4 o = __ldg(rays + 2ull * i);
-            key = (spread8(cell8(o.x, lo.x, inv.x)) << 2) | (spread8(cell8(o.y, lo.y, inv.y)) << 1) |
-                  spread8(cell8(o.z, lo.z, inv.z));
-        }
+        const uint32_t key = has_scene ? ray_key(rays, i, lo, inv) : 0u;
         keys[i] = key;
         vals[i] = i;
         differs |= key != key0;
