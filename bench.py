@@ -660,7 +660,7 @@ def run_traversal(args, rank, world, local):
         blob = r.mesh_blas(mesh)
         blas_bytes = len(blob)
         reorder = args.reorder == "on"
-        sc = None
+        sc, cpu_build_s, blas_equal = None, None, None
         if not args.no_cpu_baseline:
             # the oracle's port of the reference's scalar traversal over the same BLAS / TLAS bytes
             from oracle import oracle as orc
@@ -670,6 +670,12 @@ def run_traversal(args, rank, world, local):
             oi["local_to_world"] = np.eye(4, dtype=np.float32).reshape(16)
             oi["world_to_local"] = bi[0]["world_to_local"]
             sc = orc.Scene([(tris, blob)], r.scene_tlas(), oi)
+            # the reference's single-threaded C++ BLAS build (the oracle's restatement) of the same soup
+            t0 = time.perf_counter()
+            ref_blob = orc.bvh_build(tris, 16, False, 4)
+            cpu_build_s = time.perf_counter() - t0
+            blas_equal = bool(np.array_equal(ref_blob, blob))
+            del ref_blob
         del blob
         for kind in args.ray_kinds.split(","):
             rays = scenes.soup_rays(side, seed=7, kind=kind)
@@ -706,6 +712,8 @@ def run_traversal(args, rank, world, local):
                         "config": {"workload": f"traversal micro-benchmark, {n_tris} soup triangles, {len(rays)} "
                                                f"{kind} rays, {'any' if any_hit else 'closest'} hit",
                                    "blas_bytes": blas_bytes, "gpu_bvh_build_s": round(build_s, 3),
+                                   "cpu_bvh_build_s": round(cpu_build_s, 2) if cpu_build_s else None,
+                                   "blas_equal_to_cpu_build": blas_equal,
                                    "ray_order": ("origins' Morton codes (stable radix sort inside the timed call)"
                                                  if reorder else "as given"),
                                    "hit_fraction": round(float((hits['instance'] != 0xFFFFFFFF).mean()), 4)},
