@@ -369,10 +369,10 @@ int wf_tlas_build(wf_ctx* ctx, const bvh_instance_t* instances, uint32_t instanc
                   void* out_blob, uint64_t* inout_size);
 
 /* ---- allocation-free TLAS build (no counterpart in the reference) --------
- * For callers that cannot allocate device memory: code running while a CUDA
- * stream is being captured into a graph (cudaMalloc / cudaFree are not allowed
- * during capture) and per-frame render threads that must not pay an
- * allocation's implicit device synchronisation.  The caller owns both device
+ * For callers that cannot allocate device memory: per-frame render threads
+ * that must not pay an allocation's implicit device synchronisation, and
+ * engines that hand out all of their device memory from a budget fixed up
+ * front (their own pool, a hard memory cap).  The caller owns both device
  * buffers: device_aabbs = instance_count x {min xyz, max xyz} floats,
  * device_nodes = 2 * instance_count tlas_node_t (one when instance_count is 0);
  * the result equals the nodes wf_tlas_build writes with the same tlas_metric (0 or 1;

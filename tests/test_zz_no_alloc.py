@@ -1,5 +1,5 @@
 """GPU: wf_tlas_build_noalloc, the entry point for callers that cannot allocate
-device memory (code inside CUDA graph capture, per-frame render threads).
+device memory (per-frame render threads, engines with a fixed device-memory budget).
 
 It is called through the C ABI on device buffers the test owns, twice in a
 row (different sizes and pairing metrics, so the shared static working list

@@ -365,10 +365,10 @@ cudaError_t launch_tlas_build(const float* aabbs, uint32_t n, float4* nodes, uin
 // ============================================================================
 // Allocation-free TLAS build (wf_tlas_build_noalloc).
 //
-// Some callers cannot allocate device memory: code that runs while a stream is
-// being captured into a CUDA graph (cudaMalloc/cudaFree are not permitted during
-// capture), or a per-frame render thread where an allocation's implicit
-// device-wide synchronisation would stall the frame.  They pass their own
+// Some callers cannot allocate device memory: a per-frame render thread where
+// an allocation's implicit device-wide synchronisation would stall the frame,
+// or an engine that hands out all of its device memory from a budget fixed up
+// front (its own pool, a hard memory cap).  They pass their own
 // device buffers for the instance boxes and the output nodes; the build's
 // working list (7 words per instance) lives in one fixed-size static device
 // array that every call on a device shares.
