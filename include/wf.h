@@ -381,8 +381,11 @@ int wf_tlas_build(wf_ctx* ctx, const bvh_instance_t* instances, uint32_t instanc
  *   - at most 8192 instances (larger counts return WF_ERR_CAPACITY);
  *   - every call on a device shares that array: calls that overlap on the GPU
  *     (other streams, other threads) race and must be serialised by the caller;
- *   - the first call on a device (with that device current) loads the module and
- *     looks up the array's device address; make it before any stream capture.
+ *   - the first call in a CUDA context (the device's primary context, or one the
+ *     caller created and made current) loads the module and looks up the
+ *     array's device address in that context; make it before any stream
+ *     capture.  Up to 64 contexts are remembered; in others the address is
+ *     looked up on every call.
  * Enqueued on `stream` (a cudaStream_t; NULL = default stream), not synchronised;
  * allocates nothing. */
 int wf_tlas_build_noalloc(const float* device_aabbs, uint32_t instance_count, void* device_nodes,

@@ -53,6 +53,37 @@ def test_noalloc_tlas_matches_allocating_build_on_two_calls():
         assert np.array_equal(got, want), f"call {call}: first differing byte {np.argmax(got != want)}"
 
 
+def test_noalloc_tlas_edge_sizes():
+    """No instance (exactly one zero node is written), one instance (the walk
+    has nothing to pair) and the full static capacity of 8192 instances."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    L = wf.load()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for n, metric, seed in [(0, 0, 0), (1, 0, 21), (8192, 0, 22), (1, 1, 23)]:
+        d_nodes = torch.full((16 * max(n, 1),), -1.0, dtype=torch.float32, device="cuda")
+        if n == 0:
+            rc = L.wf_tlas_build_noalloc(None, 0, ctypes.c_void_p(d_nodes.data_ptr()), metric, stream)
+            assert rc == 0, L.wf_last_error()
+            torch.cuda.synchronize()
+            got = d_nodes.cpu().numpy()
+            assert np.all(got[:8].view(np.uint32) == 0) and np.all(got[8:] == -1.0)
+            continue
+        inst = random_instances(n, seed)
+        with wf.Renderer(8, 8, tlas_metric=metric) as r:
+            want = r.tlas_build(inst)[8:8 + 64 * n]
+        boxes = np.concatenate([inst["aabb_min"], inst["aabb_max"]], axis=1).astype(np.float32)
+        d_boxes = torch.from_numpy(boxes.copy()).cuda()
+        torch.cuda.synchronize()
+        rc = L.wf_tlas_build_noalloc(ctypes.c_void_p(d_boxes.data_ptr()), n, ctypes.c_void_p(d_nodes.data_ptr()),
+                                     metric, stream)
+        assert rc == 0, L.wf_last_error()
+        torch.cuda.synchronize()
+        got = d_nodes.cpu().numpy().view(np.uint8)
+        assert np.array_equal(got, want), f"n={n}: first differing byte {np.argmax(got != want)}"
+
+
 def test_noalloc_rejects_more_than_its_static_capacity():
     L = wf.load()
     rc = L.wf_tlas_build_noalloc(ctypes.c_void_p(16), 8193, ctypes.c_void_p(16), 0, None)

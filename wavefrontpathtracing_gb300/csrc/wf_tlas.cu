@@ -66,11 +66,12 @@ __device__ __forceinline__ void store_node(float4* nodes, uint32_t k, const floa
     nodes[2 * k + 1] = make_float4(mx[0], mx[1], mx[2], __uint_as_float(inst));
 }
 
-// One warp.  aabbs: 6 floats per instance (min xyz, max xyz); nodes: 2n nodes.
-__global__ void __launch_bounds__(32) k_tlas_build(const float* __restrict__ aabbs, uint32_t n, float4* nodes,
-                                                   uint32_t* gscratch, uint32_t metric) {
-    extern __shared__ uint32_t smem[];
-    uint32_t* base = (n <= kSmemInstances) ? smem : gscratch;
+// The reference's A/B/C walk (tlas_builder.cpp:18-67) for one warp.  aabbs:
+// 6 floats per instance (min xyz, max xyz); nodes: 2n nodes; base: the
+// working list, 7 words per instance (node index, box min, box max), in
+// shared memory, a scratch buffer or the allocation-free build's static array.
+__device__ __forceinline__ void tlas_walk(const float* __restrict__ aabbs, uint32_t n, float4* nodes, uint32_t* base,
+                                          uint32_t metric) {
     List L;
     L.idx = base;
     L.bmn = reinterpret_cast<float*>(base + n);
@@ -120,6 +121,13 @@ __global__ void __launch_bounds__(32) k_tlas_build(const float* __restrict__ aab
         nodes[0] = a;
         nodes[1] = b;
     }
+}
+
+// One warp; the list in shared memory when it fits, else in gscratch.
+__global__ void __launch_bounds__(32) k_tlas_build(const float* __restrict__ aabbs, uint32_t n, float4* nodes,
+                                                   uint32_t* gscratch, uint32_t metric) {
+    extern __shared__ uint32_t smem[];
+    tlas_walk(aabbs, n, nodes, (n <= kSmemInstances) ? smem : gscratch, metric);
 }
 
 }  // namespace
@@ -376,66 +384,43 @@ cudaError_t launch_tlas_build(const float* aabbs, uint32_t n, float4* nodes, uin
 namespace {
 
 constexpr uint32_t kNoAllocMaxInstances = 8192;
-constexpr int kNoAllocMaxDevices = 64;
+constexpr int kNoAllocMaxContexts = 64;
 
 // 7 x 8192 words = 224 KiB, resident on every GPU that loads the library.
 static __device__ __align__(256) uint32_t g_tlas_noalloc_list[7u * kNoAllocMaxInstances];
 
+// The array's device address per CUDA context (a module global has its own
+// address in each context: the device's primary context, or one an engine
+// created and made current itself).
+struct NoAllocAddr {
+    void* ctx;
+    uint32_t* list;
+};
 std::mutex g_noalloc_mu;
-uint32_t* g_noalloc_list_addr[kNoAllocMaxDevices] = {};
+NoAllocAddr g_noalloc_addr[kNoAllocMaxContexts] = {};
+int g_noalloc_count = 0;
 
-// The walk of k_tlas_build with the list always in `list` (global memory).
+// cuCtxGetCurrent, looked up through the runtime (no link against the driver library).
+typedef int (*CtxGetCurrentFn)(void** ctx);
+CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<CtxGetCurrentFn>(f);
+    }();
+    return fn;
+}
+
+// The walk of k_tlas_build with the list in the static array (`list` is its
+// device address).
 __global__ void __launch_bounds__(32) k_tlas_build_noalloc(const float* __restrict__ aabbs, uint32_t n,
                                                            float4* nodes, uint32_t* list, uint32_t metric) {
-    List L;
-    L.idx = list;
-    L.bmn = reinterpret_cast<float*>(list + n);
-    L.bmx = reinterpret_cast<float*>(list + 4 * n);
-    const uint32_t lane = threadIdx.x;
-    for (uint32_t i = lane; i < n; i += 32u) {
-        float mn[3] = {aabbs[6 * i], aabbs[6 * i + 1], aabbs[6 * i + 2]};
-        float mx[3] = {aabbs[6 * i + 3], aabbs[6 * i + 4], aabbs[6 * i + 5]};
-        store_node(nodes, 1 + i, mn, 0u, mx, i);
-        L.idx[i] = 1 + i;
-        for (int a = 0; a < 3; ++a) { L.bmn[3 * i + a] = mn[a]; L.bmx[3 * i + a] = mx[a]; }
-    }
-    __syncwarp();
-    uint32_t remaining = n, at = n + 1;
-    uint32_t A = 0;
-    uint32_t B = best_match(L, A, remaining, metric);
-    while (remaining > 1) {
-        const uint32_t C = best_match(L, B, remaining, metric);
-        if (A == C) {
-            if (lane == 0) {
-                const uint32_t ia = L.idx[A], ib = L.idx[B];
-                float mn[3], mx[3];
-                for (int a = 0; a < 3; ++a) {
-                    mn[a] = gmin(L.bmn[3 * A + a], L.bmn[3 * B + a]);
-                    mx[a] = gmax(L.bmx[3 * A + a], L.bmx[3 * B + a]);
-                }
-                store_node(nodes, at, mn, ia + (ib << 16), mx, 0u);
-                L.idx[A] = at;
-                for (int a = 0; a < 3; ++a) { L.bmn[3 * A + a] = mn[a]; L.bmx[3 * A + a] = mx[a]; }
-                const uint32_t last = remaining - 1;
-                L.idx[B] = L.idx[last];
-                for (int a = 0; a < 3; ++a) { L.bmn[3 * B + a] = L.bmn[3 * last + a]; L.bmx[3 * B + a] = L.bmx[3 * last + a]; }
-            }
-            __syncwarp();
-            at++;
-            remaining--;
-            B = best_match(L, A, remaining, metric);
-        } else {
-            A = B;
-            B = C;
-        }
-    }
-    __syncwarp();
-    if (lane == 0) {
-        const uint32_t r = L.idx[A];
-        const float4 a = nodes[2 * r], b = nodes[2 * r + 1];
-        nodes[0] = a;
-        nodes[1] = b;
-    }
+    tlas_walk(aabbs, n, nodes, list, metric);
 }
 
 }  // namespace
@@ -453,26 +438,35 @@ extern "C" int wf_tlas_build_noalloc(const float* device_aabbs, uint32_t instanc
     if ((reinterpret_cast<uintptr_t>(device_aabbs) & 3u) || (reinterpret_cast<uintptr_t>(device_nodes) & 15u))
         return report_error(WF_ERR_INVALID, "wf_tlas_build_noalloc: boxes must be 4-byte, nodes 16-byte aligned");
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return report_error(WF_ERR_CUDA, "wf_tlas_build_noalloc: no usable current CUDA device");
     }
+    // The current context.  It is still null when no call has made the
+    // device's primary context current yet; cudaGetSymbolAddress below does,
+    // and the entry is keyed by the context current after it.
+    CtxGetCurrentFn get_ctx = ctx_get_current();
+    void* ctx = nullptr;
+    if (get_ctx) get_ctx(&ctx);
     uint32_t* list = nullptr;
     {
-        // Set-up, once per device, with that device current: the host-side name
-        // g_tlas_noalloc_list is only a stand-in, so the kernel gets the
+        // Set-up, once per context, with that context current: the host-side
+        // name g_tlas_noalloc_list is only a stand-in, so the kernel gets the
         // array's device address.
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_list_addr[dev]) {
+        for (int i = 0; ctx && i < g_noalloc_count; ++i)
+            if (g_noalloc_addr[i].ctx == ctx) list = g_noalloc_addr[i].list;
+        if (!list) {
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_tlas_noalloc_list);
             if (e != cudaSuccess || !p) {
                 cudaGetLastError();
                 return report_error(WF_ERR_CUDA, "wf_tlas_build_noalloc: cudaGetSymbolAddress failed");
             }
-            g_noalloc_list_addr[dev] = static_cast<uint32_t*>(p);
+            list = static_cast<uint32_t*>(p);
+            if (get_ctx && !ctx) get_ctx(&ctx);   // the lookup made the primary context current
+            if (ctx && g_noalloc_count < kNoAllocMaxContexts) g_noalloc_addr[g_noalloc_count++] = {ctx, list};
         }
-        list = g_noalloc_list_addr[dev];
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e;
