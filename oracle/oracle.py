@@ -101,6 +101,11 @@ def lib():
         L.orc_path_seed.argtypes = [u32, u32, u32, u32]
         L.orc_path_seed.restype = u32
         L.orc_sincos_2pi.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+        L.orc_sincos.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+        L.orc_hemisphere_sample.argtypes = [vp, ctypes.c_float, ctypes.c_float, i32, vp]
+        dbl = ctypes.c_double
+        L.orc_sample_bsdf_batch.argtypes = [i32, u32, vp, dbl, dbl, vp, vp, vp, u32, i32, vp, vp, vp, vp]
+        L.orc_eval_bsdf_batch.argtypes = [u32, vp, dbl, vp, vp, vp, u32, i32, vp, vp, vp]
         L.orc_intersect_triangle.argtypes = [vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_float), vp, i32]
         L.orc_intersect_aabb.argtypes = [vp, vp, vp, vp, ctypes.c_float]
         L.orc_intersect_aabb.restype = ctypes.c_float
@@ -299,6 +304,38 @@ def env_texel(texels, d):
     dd = np.asarray(d, dtype=np.float32)
     out = np.zeros(3, np.float32)
     lib().orc_env_texel(ctypes.byref(texture_struct(texels)), ptr(dd), ptr(out))
+    return out
+
+
+def sample_bsdf(bsdf, base, alpha, ior, n, rd, r, cosine=1, f64=True):
+    """The shade stage's scattering step for m random pairs r (m x 2) at one
+    surface: returns (L m x 3, weight m x 3, pdf m, flags m: 1 delta, 2 valid,
+    4 crosses the dielectric)."""
+    L_ = lib()
+    d = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    r = d(r).reshape(-1, 2)
+    m = len(r)
+    Lo, w, pdf, fl = np.zeros((m, 3)), np.zeros((m, 3)), np.zeros(m), np.zeros(m, np.int32)
+    L_.orc_sample_bsdf_batch(int(f64), bsdf, ptr(d(base)), float(alpha), float(ior), ptr(d(n)), ptr(d(rd)), ptr(r), m,
+                             int(cosine), ptr(Lo), ptr(w), ptr(pdf), ptr(fl))
+    return Lo, w, pdf, fl
+
+
+def eval_bsdf(bsdf, base, alpha, n, v, wl, cosine=1):
+    """BSDF value and sampling pdf toward directions wl (m x 3): (f m x 3, pdf m, ok m)."""
+    L_ = lib()
+    d = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    wl = d(wl).reshape(-1, 3)
+    m = len(wl)
+    f, pdf, ok = np.zeros((m, 3)), np.zeros(m), np.zeros(m, np.int32)
+    L_.orc_eval_bsdf_batch(bsdf, ptr(d(base)), float(alpha), ptr(d(n)), ptr(d(v)), ptr(wl), m, int(cosine), ptr(f),
+                           ptr(pdf), ptr(ok))
+    return f, pdf, ok
+
+
+def hemisphere_sample(n, r1, r2, cosine):
+    out = np.zeros(3, np.float32)
+    lib().orc_hemisphere_sample(ptr(np.asarray(n, np.float32)), r1, r2, int(cosine), ptr(out))
     return out
 
 

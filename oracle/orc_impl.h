@@ -277,6 +277,24 @@ static inline FN(v3) FN(to_world)(FN(v3) v, FN(v3) tg, FN(v3) n, FN(v3) bt) {
                   v.x * tg.z + v.y * n.z + v.z * bt.z);
 }
 
+/* cosine_weighted_hemisphere_sample / uniform_hemisphere_sample
+ * (sample.hlsl:29-54): phi = 2 pi r2 (SINCOS2PI), the local direction
+ * normalised, then mul(local, basis). */
+static inline FN(v3) FN(hemisphere)(FN(v3) n, FN(v3) tg, FN(v3) bt, R r1, R r2, int cosine) {
+    FN(v3) loc;
+    R sn, cs;
+    if (cosine) {
+        R st_ = SQRT(r1);
+        SINCOS2PI(r2, &sn, &cs);
+        loc = FN(mk)(st_ * cs, SQRT(K(1.0) - r1), st_ * sn);
+    } else {
+        R st_ = SQRT(K(1.0) - r1 * r1);
+        SINCOS2PI(r2, &sn, &cs);
+        loc = FN(mk)(st_ * cs, r1, st_ * sn);
+    }
+    return FN(to_world)(FN(normalize)(loc), tg, n, bt);
+}
+
 typedef struct {
     FN(v3) p0, e1, e2, n, le;
     R area;
@@ -373,6 +391,132 @@ static inline R FN(ggx_d)(R noh, R a2) { R q = (noh * noh) * (a2 - K(1.0)) + K(1
 
 static inline R FN(offset_eps)(FN(v3) p) {
     return K(1e-5) * (K(1.0) + FMAX(FABS(p.x), FMAX(FABS(p.y), FABS(p.z))));
+}
+
+typedef struct {
+    FN(v3) L, wgt, org;     /* next direction, throughput factor, next origin */
+    R pdf;                  /* solid-angle pdf of L (0 for delta lobes) */
+    int delta, valid, toggle_inside;
+} FN(scatter);
+
+/* The shade stage's scattering step at a surface point with shading normal N
+ * (basis tg, bt) for a ray arriving along rd: bsdf 0 = Lambert
+ * (shade.hlsl:107-135: cosine-weighted or uniform hemisphere, weight
+ * NoL * base/pi / pdf), 1 = GGX metal (alpha = roughness^2; half vector from
+ * the GGX normal distribution, weight F * G1(L) G1(V) * VoH / (NoV * NoH),
+ * Schlick F with F0 = base), 3 = mirror (metal with alpha < 1e-4: weight
+ * Schlick F at NoV), 2 = smooth dielectric (exact Fresnel reflectance chooses
+ * reflection or refraction, weight 1, origin offset along L). */
+static FN(scatter) FN(sample_bsdf)(uint32_t bsdf, FN(v3) base, R alpha, R ior, FN(v3) N, FN(v3) tg, FN(v3) bt,
+                                   FN(v3) rd, FN(v3) pos, R r1, R r2, int cosine) {
+    FN(scatter) o;
+    FN(v3) V = FN(neg)(rd);
+    FN(v3) L = FN(mk)(0, 0, 0), wgt = FN(mk)(0, 0, 0);
+    R pdf = K(0.0);
+    int delta = 0, valid = 1, toggle_inside = 0;
+    FN(v3) org = pos;
+    if (bsdf == 0) {
+        /* shade.hlsl:107-135 */
+        L = FN(hemisphere)(N, tg, bt, r1, r2, cosine);
+        R nol = FMAX(K(0.0), FN(dot)(N, L));
+        pdf = cosine ? nol * ORC_INV_PI : ORC_INV_TWO_PI;
+        R ip = K(1.0) / pdf;
+        /* shade.hlsl:135 multiplies by 1 / pdf unguarded: a sample in the
+         * tangent plane (r1 == 1, or NoL rounding to 0) gives 0 * inf = NaN
+         * there.  Here the path ends (the GPU kernels do the same). */
+        if (ip <= MAXT)
+            wgt = FN(mk)((nol * (base.x * ORC_INV_PI)) * ip, (nol * (base.y * ORC_INV_PI)) * ip,
+                         (nol * (base.z * ORC_INV_PI)) * ip);
+        else
+            valid = 0;
+    } else if (bsdf == 1) {
+        R a2 = alpha * alpha;
+        R cth = SQRT((K(1.0) - r1) / (K(1.0) + (a2 - K(1.0)) * r1));
+        R sth = SQRT(FMAX(K(0.0), K(1.0) - cth * cth));
+        R sn, cs;
+        SINCOS2PI(r2, &sn, &cs);
+        FN(v3) H = FN(to_world)(FN(mk)(sth * cs, cth, sth * sn), tg, N, bt);
+        R voh = FN(dot)(V, H);
+        L = FN(sub)(FN(scl)(H, K(2.0) * voh), V);
+        R nol = FN(dot)(N, L), nov = FN(dot)(N, V), noh = FN(dot)(N, H);
+        if (nol <= K(0.0) || nov <= K(0.0) || voh <= K(0.0) || noh <= K(0.0)) {
+            valid = 0;
+        } else {
+            FN(v3) F = FN(schlick)(base, voh);
+            R G = FN(g1)(nol, a2) * FN(g1)(nov, a2);
+            R gw = (G * voh) / (nov * noh);
+            wgt = FN(scl)(F, gw);
+            pdf = (FN(ggx_d)(noh, a2) * noh) / (K(4.0) * voh);
+        }
+    } else if (bsdf == 3) {
+        R nov = FN(dot)(N, V);
+        delta = 1;
+        if (nov <= K(0.0)) valid = 0;
+        else {
+            L = FN(sub)(FN(scl)(N, K(2.0) * nov), V);
+            wgt = FN(schlick)(base, nov);
+        }
+    } else {
+        /* smooth dielectric */
+        R ci = FN(dot)(V, N);
+        int entering = ci > K(0.0);
+        R n1 = entering ? K(1.0) : ior, n2 = entering ? ior : K(1.0);
+        FN(v3) nn = entering ? N : FN(neg)(N);
+        ci = FABS(ci);
+        R eta = n1 / n2;
+        R s2t = (eta * eta) * (K(1.0) - ci * ci);
+        R F = K(1.0), ct = K(0.0);
+        if (s2t < K(1.0)) {
+            ct = SQRT(K(1.0) - s2t);
+            R rs = (n1 * ci - n2 * ct) / (n1 * ci + n2 * ct);
+            R rp = (n1 * ct - n2 * ci) / (n1 * ct + n2 * ci);
+            F = K(0.5) * (rs * rs + rp * rp);
+        }
+        if (r1 < F) {
+            L = FN(add)(rd, FN(scl)(nn, K(2.0) * ci));
+        } else {
+            L = FN(normalize)(FN(add)(FN(scl)(rd, eta), FN(scl)(nn, eta * ci - ct)));
+            toggle_inside = 1;
+        }
+        wgt = FN(mk)(K(1.0), K(1.0), K(1.0));
+        delta = 1;
+        org = FN(add)(pos, FN(scl)(L, FN(offset_eps)(pos)));
+    }
+
+    o.L = L; o.wgt = wgt; o.org = org; o.pdf = pdf;
+    o.delta = delta; o.valid = valid; o.toggle_inside = toggle_inside;
+    return o;
+}
+
+/* The BSDF value f toward wl and the pdf with which sample_bsdf would have
+ * drawn wl (the connect stage's multiple importance sampling): Lambert
+ * base/pi, GGX metal F D G / (4 cos_x NoV) with pdf D NoH / (4 VoH).  Returns
+ * 0 where the metal's half vector faces away or D is not finite. */
+static int FN(eval_bsdf)(uint32_t bsdf, FN(v3) base, R alpha, FN(v3) N, FN(v3) V, FN(v3) wl, R cos_x, int cosine,
+                         FN(v3)* f_out, R* pdf_out) {
+    FN(v3) f = FN(mk)(0, 0, 0);
+    R pdf_b = K(0.0);
+    int ok = 1;
+    if (bsdf == 0) {
+        f = FN(scl)(base, ORC_INV_PI);
+        pdf_b = cosine ? cos_x * ORC_INV_PI : ORC_INV_TWO_PI;
+    } else {
+        FN(v3) H = FN(normalize)(FN(add)(V, wl));
+        R nov = FN(dot)(N, V), noh = FN(dot)(N, H), voh = FN(dot)(V, H);
+        if (nov <= K(0.0) || voh <= K(0.0)) ok = 0;
+        else {
+            R a2 = alpha * alpha;
+            R D = FN(ggx_d)(noh, a2);
+            R G = FN(g1)(cos_x, a2) * FN(g1)(nov, a2);
+            FN(v3) F = FN(schlick)(base, voh);
+            f = FN(scl)(F, (D * G) / ((K(4.0) * cos_x) * nov));
+            pdf_b = (D * noh) / (K(4.0) * voh);
+            if (!(D <= MAXT)) ok = 0;
+        }
+    }
+    *f_out = f;
+    *pdf_out = pdf_b;
+    return ok;
 }
 
 typedef struct {
@@ -535,86 +679,10 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
             rec->rho[rec->n][0] = base.x; rec->rho[rec->n][1] = base.y; rec->rho[rec->n][2] = base.z;
             rec->n++;
         }
-        if (bsdf == 0) {
-            /* shade.hlsl:107-135 */
-            FN(v3) loc;
-            if (P->cosine_weighted_diffuse) {
-                R sn, cs;
-                R st_ = SQRT(r1);
-                SINCOS2PI(r2, &sn, &cs);
-                loc = FN(mk)(st_ * cs, SQRT(K(1.0) - r1), st_ * sn);
-            } else {
-                R sn, cs;
-                R st_ = SQRT(K(1.0) - r1 * r1);
-                SINCOS2PI(r2, &sn, &cs);
-                loc = FN(mk)(st_ * cs, r1, st_ * sn);
-            }
-            L = FN(to_world)(FN(normalize)(loc), tg, N, bt);
-            R nol = FMAX(K(0.0), FN(dot)(N, L));
-            pdf = P->cosine_weighted_diffuse ? nol * ORC_INV_PI : ORC_INV_TWO_PI;
-            R ip = K(1.0) / pdf;
-            /* shade.hlsl:135 multiplies by 1 / pdf unguarded: a sample in the
-             * tangent plane (r1 == 1, or NoL rounding to 0) gives 0 * inf = NaN
-             * there.  Here the path ends (the GPU kernels do the same). */
-            if (ip <= MAXT)
-                wgt = FN(mk)((nol * (base.x * ORC_INV_PI)) * ip, (nol * (base.y * ORC_INV_PI)) * ip,
-                             (nol * (base.z * ORC_INV_PI)) * ip);
-            else
-                valid = 0;
-        } else if (bsdf == 1) {
-            R a2 = alpha * alpha;
-            R cth = SQRT((K(1.0) - r1) / (K(1.0) + (a2 - K(1.0)) * r1));
-            R sth = SQRT(FMAX(K(0.0), K(1.0) - cth * cth));
-            R sn, cs;
-            SINCOS2PI(r2, &sn, &cs);
-            FN(v3) H = FN(to_world)(FN(mk)(sth * cs, cth, sth * sn), tg, N, bt);
-            R voh = FN(dot)(V, H);
-            L = FN(sub)(FN(scl)(H, K(2.0) * voh), V);
-            R nol = FN(dot)(N, L), nov = FN(dot)(N, V), noh = FN(dot)(N, H);
-            if (nol <= K(0.0) || nov <= K(0.0) || voh <= K(0.0) || noh <= K(0.0)) {
-                valid = 0;
-            } else {
-                FN(v3) F = FN(schlick)(base, voh);
-                R G = FN(g1)(nol, a2) * FN(g1)(nov, a2);
-                R gw = (G * voh) / (nov * noh);
-                wgt = FN(scl)(F, gw);
-                pdf = (FN(ggx_d)(noh, a2) * noh) / (K(4.0) * voh);
-            }
-        } else if (bsdf == 3) {
-            R nov = FN(dot)(N, V);
-            delta = 1;
-            if (nov <= K(0.0)) valid = 0;
-            else {
-                L = FN(sub)(FN(scl)(N, K(2.0) * nov), V);
-                wgt = FN(schlick)(base, nov);
-            }
-        } else {
-            /* smooth dielectric */
-            R ci = FN(dot)(V, N);
-            int entering = ci > K(0.0);
-            R ior = (R)in->ior;
-            R n1 = entering ? K(1.0) : ior, n2 = entering ? ior : K(1.0);
-            FN(v3) nn = entering ? N : FN(neg)(N);
-            ci = FABS(ci);
-            R eta = n1 / n2;
-            R s2t = (eta * eta) * (K(1.0) - ci * ci);
-            R F = K(1.0), ct = K(0.0);
-            if (s2t < K(1.0)) {
-                ct = SQRT(K(1.0) - s2t);
-                R rs = (n1 * ci - n2 * ct) / (n1 * ci + n2 * ct);
-                R rp = (n1 * ct - n2 * ci) / (n1 * ct + n2 * ci);
-                F = K(0.5) * (rs * rs + rp * rp);
-            }
-            if (r1 < F) {
-                L = FN(add)(rd, FN(scl)(nn, K(2.0) * ci));
-            } else {
-                L = FN(normalize)(FN(add)(FN(scl)(rd, eta), FN(scl)(nn, eta * ci - ct)));
-                toggle_inside = 1;
-            }
-            wgt = FN(mk)(K(1.0), K(1.0), K(1.0));
-            delta = 1;
-            org = FN(add)(pos, FN(scl)(L, FN(offset_eps)(pos)));
-        }
+        FN(scatter) sc_ = FN(sample_bsdf)(bsdf, base, alpha, (R)in->ior, N, tg, bt, rd, pos, r1, r2,
+                                          (int)P->cosine_weighted_diffuse);
+        L = sc_.L; wgt = sc_.wgt; org = sc_.org; pdf = sc_.pdf;
+        delta = sc_.delta; valid = sc_.valid; toggle_inside = sc_.toggle_inside;
 
         /* connect: next-event estimation towards the emitter table */
         if (P->nee && !delta && d < P->max_bounces && J->lights.count > 0) {
@@ -633,26 +701,9 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
             R cos_x = FN(dot)(N, wl);
             if (cos_l > K(0.0) && cos_x > K(0.0)) {
                 R pdf_l = dd2 / (cos_l * J->lights.total);
-                FN(v3) f = FN(mk)(0, 0, 0);
-                R pdf_b = K(0.0);
-                int ok = 1;
-                if (bsdf == 0) {
-                    f = FN(scl)(base, ORC_INV_PI);
-                    pdf_b = P->cosine_weighted_diffuse ? cos_x * ORC_INV_PI : ORC_INV_TWO_PI;
-                } else {
-                    FN(v3) H = FN(normalize)(FN(add)(V, wl));
-                    R nov = FN(dot)(N, V), noh = FN(dot)(N, H), voh = FN(dot)(V, H);
-                    if (nov <= K(0.0) || voh <= K(0.0)) ok = 0;
-                    else {
-                        R a2 = alpha * alpha;
-                        R D = FN(ggx_d)(noh, a2);
-                        R G = FN(g1)(cos_x, a2) * FN(g1)(nov, a2);
-                        FN(v3) F = FN(schlick)(base, voh);
-                        f = FN(scl)(F, (D * G) / ((K(4.0) * cos_x) * nov));
-                        pdf_b = (D * noh) / (K(4.0) * voh);
-                        if (!(D <= MAXT)) ok = 0;
-                    }
-                }
+                FN(v3) f;
+                R pdf_b;
+                int ok = FN(eval_bsdf)(bsdf, base, alpha, N, V, wl, cos_x, (int)P->cosine_weighted_diffuse, &f, &pdf_b);
                 if (ok) {
                     R q = pdf_b / pdf_l;
                     R w = (q == q) ? K(1.0) / (K(1.0) + q * q) : K(0.0);

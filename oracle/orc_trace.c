@@ -38,17 +38,21 @@ uint32_t orc_path_seed(uint32_t frame_seed, uint32_t pixel, uint32_t sample, uin
     return s;
 }
 
-/* sin(2*pi*r), cos(2*pi*r) for r in [0, 1].  Range reduction is exact in r:
- * t = 4r, k = rint(t), f = t - k in [-1/2, 1/2], x = f * (pi/2) in
+/* sin(phi), cos(phi): Cody-Waite reduction by pi/2 with a three-part
+ * constant (1.5703125 + 4.838268e-4 + 2.563344e-12; the first two parts have
+ * 8 and 22 significant bits, so k times them is exact while |k| <= 4, i.e.
+ * for |phi| up to about 7), k = rint(phi * 2/pi), x = phi - k*pi/2 in about
  * [-pi/4, pi/4]; then truncated Taylor series (sin to x^9, cos to x^10,
  * truncation error below 2e-9) in Horner form, and a quarter-turn rotation by
- * k mod 4.  Written out operation by operation so the CUDA kernels can
- * evaluate the identical sequence. */
-void orc_sincos_2pi(float r, float* s_out, float* c_out) {
-    float t = r * 4.0f;
-    float k = rintf(t);
-    float f = t - k;
-    float x = f * 1.57079637f;
+ * k mod 4.  Absolute error against sin/cos of the same float phi < 1e-7 on
+ * [0, 2*pi].  Written out operation by operation so the CUDA kernels can
+ * evaluate the identical sequence.  This is this project's definition of the
+ * HLSL sin / cos intrinsics, whose precision nothing in the reference pins. */
+void orc_sincos(float phi, float* s_out, float* c_out) {
+    float k = rintf(phi * 0.636619747f);
+    float x = phi - k * 1.5703125f;
+    x = x - k * 4.83826792e-4f;
+    x = x - k * 2.56334415e-12f;
     float x2 = x * x;
     float sp = -1.98412698e-4f + x2 * 2.75573192e-6f;
     sp = 8.33333377e-3f + x2 * sp;
@@ -68,6 +72,11 @@ void orc_sincos_2pi(float r, float* s_out, float* c_out) {
     *s_out = s;
     *c_out = c;
 }
+
+/* The hemisphere samplers' angle (sample.hlsl:29-54): phi = 2.0 * PI * r.y
+ * with PI = 3.14159265, i.e. the float 6.28318548 times r, rounded to float,
+ * then sin(phi) and cos(phi). */
+void orc_sincos_2pi(float r, float* s_out, float* c_out) { orc_sincos(6.28318548f * r, s_out, c_out); }
 
 static void sincos_2pi_f64(double r, double* s, double* c) {
     double a = 6.283185307179586 * r;
@@ -157,6 +166,12 @@ void orc_env_texel(const orc_texture* t, const float dir[3], float out[3]) {
     v3_f32 c = env_texel_f32(t, mk_f32(dir[0], dir[1], dir[2]));
     out[0] = c.x; out[1] = c.y; out[2] = c.z;
 }
+void orc_hemisphere_sample(const float n[3], float r1, float r2, int cosine, float out[3]) {
+    v3_f32 N = mk_f32(n[0], n[1], n[2]), tg, bt;
+    basis_f32(N, &tg, &bt);
+    v3_f32 L = hemisphere_f32(N, tg, bt, r1, r2, cosine);
+    out[0] = L.x; out[1] = L.y; out[2] = L.z;
+}
 
 #undef ATAN2
 #undef ASIN
@@ -174,6 +189,63 @@ void orc_env_texel(const orc_texture* t, const float dir[3], float out[3]) {
 #define SINCOS2PI(r, s, c) sincos_2pi_f64((r), (s), (c))
 #define MAXT ((double)FLT_MAX)
 #include "orc_impl.h"
+
+/* ---- the scattering models on their own (physics tests) ------------------- */
+/* Draws one scattering direction at a surface with shading normal n for a ray
+ * arriving along rd, as the shade stage does (in = bsdf, base[3], alpha, ior,
+ * r1, r2, cosine; out = L[3], weight[3], pdf, flags bit 0 delta, bit 1 valid,
+ * bit 2 toggles inside).  f64 selects the double instance. */
+int orc_sample_bsdf(int f64, uint32_t bsdf, const double base[3], double alpha, double ior, const double n[3],
+                    const double rd[3], double r1, double r2, int cosine, double L[3], double wgt[3], double* pdf) {
+    scatter_f64 o;
+    if (f64) {
+        v3_f64 N = mk_f64(n[0], n[1], n[2]), tg, bt;
+        basis_f64(N, &tg, &bt);
+        o = sample_bsdf_f64(bsdf, mk_f64(base[0], base[1], base[2]), alpha, ior, N, tg, bt,
+                            mk_f64(rd[0], rd[1], rd[2]), mk_f64(0, 0, 0), r1, r2, cosine);
+    } else {
+        v3_f32 N = mk_f32((float)n[0], (float)n[1], (float)n[2]), tg, bt;
+        basis_f32(N, &tg, &bt);
+        scatter_f32 q = sample_bsdf_f32(bsdf, mk_f32((float)base[0], (float)base[1], (float)base[2]), (float)alpha,
+                                        (float)ior, N, tg, bt, mk_f32((float)rd[0], (float)rd[1], (float)rd[2]),
+                                        mk_f32(0, 0, 0), (float)r1, (float)r2, cosine);
+        o.L = mk_f64(q.L.x, q.L.y, q.L.z);
+        o.wgt = mk_f64(q.wgt.x, q.wgt.y, q.wgt.z);
+        o.pdf = q.pdf;
+        o.delta = q.delta; o.valid = q.valid; o.toggle_inside = q.toggle_inside;
+    }
+    L[0] = o.L.x; L[1] = o.L.y; L[2] = o.L.z;
+    wgt[0] = o.wgt.x; wgt[1] = o.wgt.y; wgt[2] = o.wgt.z;
+    *pdf = o.pdf;
+    return (o.delta ? 1 : 0) | (o.valid ? 2 : 0) | (o.toggle_inside ? 4 : 0);
+}
+
+/* orc_sample_bsdf for m random pairs r[2m] at one surface configuration. */
+void orc_sample_bsdf_batch(int f64, uint32_t bsdf, const double base[3], double alpha, double ior, const double n[3],
+                           const double rd[3], const double* r, uint32_t m, int cosine, double* L, double* wgt,
+                           double* pdf, int* flags) {
+    for (uint32_t i = 0; i < m; ++i)
+        flags[i] = orc_sample_bsdf(f64, bsdf, base, alpha, ior, n, rd, r[2 * i], r[2 * i + 1], cosine, L + 3 * i,
+                                   wgt + 3 * i, pdf + i);
+}
+
+/* The BSDF value toward wl and its sampling pdf, as the connect stage
+ * evaluates them (v = the direction back to the viewer).  Returns 1 if
+ * valid. */
+int orc_eval_bsdf(uint32_t bsdf, const double base[3], double alpha, const double n[3], const double v[3],
+                  const double wl[3], int cosine, double f[3], double* pdf) {
+    v3_f64 N = mk_f64(n[0], n[1], n[2]), W = mk_f64(wl[0], wl[1], wl[2]), fo;
+    int ok = eval_bsdf_f64(bsdf, mk_f64(base[0], base[1], base[2]), alpha, N, mk_f64(v[0], v[1], v[2]), W,
+                           dot_f64(N, W), cosine, &fo, pdf);
+    f[0] = fo.x; f[1] = fo.y; f[2] = fo.z;
+    return ok;
+}
+
+/* orc_eval_bsdf toward m directions wl[3m]. */
+void orc_eval_bsdf_batch(uint32_t bsdf, const double base[3], double alpha, const double n[3], const double v[3],
+                         const double* wl, uint32_t m, int cosine, double* f, double* pdf, int* ok) {
+    for (uint32_t i = 0; i < m; ++i) ok[i] = orc_eval_bsdf(bsdf, base, alpha, n, v, wl + 3 * i, cosine, f + 3 * i, pdf + i);
+}
 
 /* ---- exported known-answer helpers ---------------------------------------- */
 int orc_intersect_triangle(const float v0[3], const float v1[3], const float v2[3], const float org[3],

@@ -6,7 +6,8 @@
  * (extern/cgltf/cgltf.h and extern/ufbx/ufbx.c, compiled from the reference
  * checkout by oracle/build_ref.sh; nothing of them is copied here).  Instead of
  * calling the renderer it writes what the loader would hand it to a flat dump
- * that tests/test_assets_ref.py compares with wavefrontpathtracing_gb300.gltf
+ * that tests/test_gltf.py and tests/test_fbx.py (through tests/ref_assets.py)
+ * compare with wavefrontpathtracing_gb300.gltf
  * and wavefrontpathtracing_gb300.fbx.
  *
  * Where the reference is undefined this restatement takes the defined choice

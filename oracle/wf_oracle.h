@@ -16,10 +16,16 @@
  * Pinning: the builders are pinned byte-for-byte against the reference's own
  * bvh_builder.cpp / tlas_builder.cpp compiled from the reference sources
  * (oracle/build_ref.sh -> oracle/_ref/libref_bvh.so) and against golden blobs
- * in tests/golden/.  The reference has no test, golden image or known-answer
- * vector for traversal or shading, and its HLSL cannot run here (no D3D12), so
- * those parts follow the HLSL line by line with the operation order written
- * down in each function ("parity unpinned" by reference outputs for them).
+ * in tests/golden/.  Traversal, intersection, the RNG, primary rays, Lambert
+ * sampling, materials, the environment, the debug views and the shade stage
+ * are pinned bit for bit against the reference's own HLSL text compiled as
+ * C++ (oracle/ref_hlsl/ -> oracle/_ref/libref_hlsl.so, tests/test_ref_hlsl.py);
+ * what that comparison shares with this oracle (intrinsic implementations,
+ * the keyed seeds) is listed in oracle/ref_hlsl/hlsl_shim.h.  The scattering
+ * models the reference does not have (metal, dielectric, next-event
+ * estimation, Russian roulette) are checked against the physics instead:
+ * energy, normalisation, reciprocity and an independently written FP64
+ * estimator (tests/test_physics.py).
  */
 #ifndef WF_ORACLE_H
 #define WF_ORACLE_H
@@ -141,11 +147,31 @@ int orc_render_f64(const orc_scene* s, const view_t* view, const orc_render_para
 int orc_adjoint_f64(const orc_scene* s, const view_t* view, const orc_render_params* p, const double* dloss_dimage,
                     double* d_albedo, double* d_emission);
 
+/* --- the scattering models on their own (physics tests) -------------------- */
+/* One scattering direction at a surface (bsdf 0 Lambert, 1 GGX metal, 2
+ * smooth dielectric, 3 mirror) for a ray arriving along rd, normal n; f64
+ * selects the double instance.  Returns flags: bit 0 delta lobe, bit 1 valid,
+ * bit 2 the ray crosses into / out of the dielectric. */
+int orc_sample_bsdf(int f64, uint32_t bsdf, const double base[3], double alpha, double ior, const double n[3],
+                    const double rd[3], double r1, double r2, int cosine, double L[3], double wgt[3], double* pdf);
+/* The BSDF value toward wl and the pdf with which orc_sample_bsdf draws wl
+ * (v: direction back to the viewer), double instance.  Returns 1 if valid. */
+int orc_eval_bsdf(uint32_t bsdf, const double base[3], double alpha, const double n[3], const double v[3],
+                  const double wl[3], int cosine, double f[3], double* pdf);
+/* The same for m random pairs r[2m] / m directions wl[3m]. */
+void orc_sample_bsdf_batch(int f64, uint32_t bsdf, const double base[3], double alpha, double ior, const double n[3],
+                           const double rd[3], const double* r, uint32_t m, int cosine, double* L, double* wgt,
+                           double* pdf, int* flags);
+void orc_eval_bsdf_batch(uint32_t bsdf, const double base[3], double alpha, const double n[3], const double v[3],
+                         const double* wl, uint32_t m, int cosine, double* f, double* pdf, int* ok);
+
 /* --- small helpers exported for known-answer tests --------------------------- */
 uint32_t orc_wang_hash(uint32_t seed);
 float orc_rand_float(uint32_t* seed);
 uint32_t orc_path_seed(uint32_t frame_seed, uint32_t pixel, uint32_t sample, uint32_t depth);
 void orc_sincos_2pi(float r, float* s, float* c);
+/* sin / cos of an angle in radians (the definition of the HLSL intrinsics). */
+void orc_sincos(float phi, float* s, float* c);
 int orc_intersect_triangle(const float v0[3], const float v1[3], const float v2[3],
                            const float org[3], const float dir[3], float* t_inout,
                            float bary[2], int no_cull);
@@ -157,6 +183,9 @@ float orc_asin(float y);
 void orc_int_to_color(uint32_t v, float out[3]);
 void orc_tex_sample(const orc_texture* t, float u, float v, float out[4]);
 void orc_env_texel(const orc_texture* t, const float dir[3], float out[3]);
+/* Lambert direction about the normal n (cosine-weighted or uniform), as the
+ * path loop draws it from r1, r2. */
+void orc_hemisphere_sample(const float n[3], float r1, float r2, int cosine, float out[3]);
 
 #ifdef __cplusplus
 }

@@ -35,14 +35,22 @@ def test_rand_float_range_and_rounding(orc):
 
 
 def test_sincos_2pi_accuracy(orc):
+    # the samplers' angle is phi = float(2.0 * PI) * r rounded to float
+    # (sample.hlsl:31-32, 47-48); sin / cos of that phi to < 1.2e-7, and so
+    # within the rounding of phi of the exact sin(2 pi r)
     L = orc.lib()
     s, c = ctypes.c_float(), ctypes.c_float()
-    worst = 0.0
-    for r in np.linspace(0.0, 1.0, 4097, dtype=np.float32):
+    worst_phi = worst_exact = 0.0
+    rs = np.concatenate([np.linspace(0.0, 1.0, 4097, dtype=np.float32),
+                         np.random.default_rng(5).random(4096, dtype=np.float32)])
+    for r in rs:
         L.orc_sincos_2pi(float(r), ctypes.byref(s), ctypes.byref(c))
+        phi = float(np.float32(np.float32(6.28318548) * r))
+        worst_phi = max(worst_phi, abs(s.value - math.sin(phi)), abs(c.value - math.cos(phi)))
         a = 2.0 * math.pi * float(r)
-        worst = max(worst, abs(s.value - math.sin(a)), abs(c.value - math.cos(a)))
-    assert worst < 4e-7
+        worst_exact = max(worst_exact, abs(s.value - math.sin(a)), abs(c.value - math.cos(a)))
+    assert worst_phi < 1.2e-7
+    assert worst_exact < 6e-7
 
 
 def _tri(orc, v0, v1, v2, o, d, t=3.4e38, no_cull=0):

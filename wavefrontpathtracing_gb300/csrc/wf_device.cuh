@@ -155,15 +155,17 @@ __host__ __device__ __forceinline__ uint32_t path_seed(uint32_t frame_seed, uint
     return s;
 }
 
-// sin(2*pi*r), cos(2*pi*r): exact reduction in r (t = 4r, k = rint(t),
-// f = t - k), x = f*(pi/2), truncated Taylor series in Horner form (sin to
-// x^9, cos to x^10; truncation error < 2e-9 on [-pi/4, pi/4]), then a
-// quarter-turn rotation by k mod 4.
-__host__ __device__ __forceinline__ void sincos_2pi(float r, float& s_out, float& c_out) {
-    float t = r * 4.0f;
-    float k = rintf(t);
-    float f = t - k;
-    float x = f * 1.57079637f;
+// sin(phi), cos(phi): Cody-Waite reduction by pi/2 with a three-part
+// constant (1.5703125 + 4.838268e-4 + 2.563344e-12; k times the first two
+// parts is exact while |k| <= 4), k = rint(phi * 2/pi), x = phi - k*pi/2;
+// truncated Taylor series in Horner form (sin to x^9, cos to x^10; truncation
+// error < 2e-9 on [-pi/4, pi/4]), then a quarter-turn rotation by k mod 4.
+// Absolute error against sin/cos of the same float phi < 1e-7 on [0, 2*pi].
+__host__ __device__ __forceinline__ void sincos_rad(float phi, float& s_out, float& c_out) {
+    float k = rintf(phi * 0.636619747f);
+    float x = phi - k * 1.5703125f;
+    x = x - k * 4.83826792e-4f;
+    x = x - k * 2.56334415e-12f;
     float x2 = x * x;
     float sp = -1.98412698e-4f + x2 * 2.75573192e-6f;
     sp = 8.33333377e-3f + x2 * sp;
@@ -179,6 +181,13 @@ __host__ __device__ __forceinline__ void sincos_2pi(float r, float& s_out, float
     else if (q == 1) { s_out = cs; c_out = -sn; }
     else if (q == 2) { s_out = -sn; c_out = -cs; }
     else { s_out = -cs; c_out = sn; }
+}
+
+// The hemisphere samplers' angle (sample.hlsl:29-54): phi = 2.0 * PI * r.y
+// with PI = 3.14159265, i.e. the float 6.28318548 times r rounded to float,
+// then sin(phi) and cos(phi).
+__host__ __device__ __forceinline__ void sincos_2pi(float r, float& s_out, float& c_out) {
+    sincos_rad(6.28318548f * r, s_out, c_out);
 }
 
 // ---------------------------------------------------------------- intersection

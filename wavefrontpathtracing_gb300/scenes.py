@@ -8,6 +8,8 @@ seeds so that the GPU library and the CPU oracle see identical bytes:
                      (subdivision 5, radius 0.3, centre (0.5,0.3,0.5)) and an
                      emissive ceiling quad of radiance 15; Lambert albedo per
                      mesh uniform in [0.2,0.8]^3 from PCG32 seed 1.
+  mixed_box_scene()  the box scene's room with one sphere of each material
+                     (Lambert, GGX metal, mirror-smooth metal, dielectric).
   instanced_scene()  8 noise-displaced icospheres, 1,024 instances with random
                      rotation, scale in [0.5,2], translation in a 100^3 box,
                      60/25/15 % Lambert/metal/dielectric, one area light.
@@ -288,6 +290,37 @@ def box_scene(width=256, height=256, subdivision=5, max_bounces=4, spp=1):
     settings = dict(max_bounces=max_bounces, spp=spp, nee=0, rr_start_depth=0xFFFFFFFF, env=(0.0, 0.0, 0.0),
                     env_strength=1.0, cosine=1)
     return SceneDesc("box", [box, sphere, light], instances, view, width, height, settings,
+                     dict(interval_count=16, subdivide_single_prim=0, max_leaf_prims=4))
+
+
+def mixed_box_scene(width=80, height=60, subdivision=3, max_bounces=8, spp=1):
+    """The box scene's room (walls and block, Lambert) with one sphere of each
+    of the instanced configuration's materials standing on the floor —
+    Lambert, GGX metal at roughness 0.3 and 0.1, a metal smooth enough to be a
+    mirror (roughness 0.005, alpha below 1e-4) and a dielectric of IOR 1.5 —
+    under a 0.5 x 0.5 ceiling light of radiance 6; next-event estimation and
+    Russian roulette from depth 3, as the instanced configuration renders."""
+    box = box_scene(width, height, subdivision=1).meshes[0]
+    sphere = icosphere(2 ** subdivision)
+    light = quad((0.25, 0.998, 0.25), (0.5, 0, 0), (0, 0, 0.5))   # faces -y
+    rng = PCG32(4)
+    wall = tuple(rng.uniform(0.3, 0.8) for _ in range(3))
+    instances = [
+        (0, np.eye(4), material(base=wall)),
+        (2, np.eye(4), material(base=(0.8, 0.8, 0.8), emissive=(1.0, 0.95, 0.9), strength=6.0)),
+        (1, translate_scale((0.22, 0.13, 0.62), 0.13), material(base=(0.75, 0.3, 0.25))),
+        (1, translate_scale((0.50, 0.14, 0.68), 0.14),
+         material(base=(0.9, 0.7, 0.4), bsdf=BSDF_METAL, roughness=0.3, metallic=1.0)),
+        (1, translate_scale((0.72, 0.11, 0.48), 0.11),
+         material(base=(0.6, 0.8, 0.9), bsdf=BSDF_METAL, roughness=0.1, metallic=1.0)),
+        (1, translate_scale((0.35, 0.12, 0.30), 0.12),
+         material(base=(0.95, 0.95, 0.95), bsdf=BSDF_METAL, roughness=0.005, metallic=1.0)),
+        (1, translate_scale((0.60, 0.14, 0.20), 0.14), material(base=(1.0, 1.0, 1.0), bsdf=BSDF_DIELECTRIC, ior=1.5)),
+    ]
+    view = make_view((0.5, 0.38, -0.55), (0.48, 0.16, 0.45), 45.0, width, height)   # the spheres fill the frame
+    settings = dict(max_bounces=max_bounces, spp=spp, nee=1, rr_start_depth=3, env=(0.0, 0.0, 0.0),
+                    env_strength=1.0, cosine=1)
+    return SceneDesc("mixed_box", [box, sphere, light], instances, view, width, height, settings,
                      dict(interval_count=16, subdivide_single_prim=0, max_leaf_prims=4))
 
 
