@@ -13,6 +13,15 @@ frame the scene is re-submitted (1,025 instances, TLAS rebuilt on the GPU, as
 the reference rebuilds its TLAS every frame, renderer.cpp:637-669) and the
 1080p RGBA float image is read back to the host.
 
+Beside the headline: the roofline per depth (extension and shadow-ray
+launches, algorithmic bytes of an instrumented pass over the timed CUDA-event
+time of each depth's launch) and over the secondary depths alone; the same
+frame with the reference's TLAS (tlas_metric 0); the CPU baseline with the
+reference TLAS and with the clustering TLAS on the same pixels; the traversal
+micro-benchmark at 4.2M rays per set (closest / any hit, coherent /
+incoherent, as given / Morton-ordered, with its CPU baseline); the plain small,
+differentiable and batched configurations; the megakernel A/B.
+
 Reference arm (--impl reference): the reference's algorithm on the host CPU
 cores: the oracle's restatement of its builders, traversal and shading
 (reference TLAS metric), all threads, each step a bounded sample of pixels of
@@ -161,13 +170,48 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """Per-launch DRAM bytes of the extend kernel from the committed ncu summary."""
+def ncu_traffic(rays_per_launch):
+    """DRAM bytes per extension launch from the committed ncu summary
+    (profiles/extend_instanced_1080p.json: read + written bytes per ray of
+    the depth >= 1 extension launches of a reduced frame, and the git commit
+    it was captured at), scaled to this frame's rays per launch."""
     p = os.path.join(ROOT, "profiles", "extend_instanced_1080p.json")
-    if os.path.exists(p):
-        d = json.load(open(p))
-        return d.get("dram_bytes_per_launch")
-    return None
+    if not os.path.exists(p):
+        return None, None
+    d = json.load(open(p))
+    if "dram_bytes_per_ray" in d:
+        return int(d["dram_bytes_per_ray"] * rays_per_launch), {
+            "file": "profiles/extend_instanced_1080p.json", "commit": d.get("commit"),
+            "captured": d.get("workload"), "dram_bytes_per_ray": d["dram_bytes_per_ray"]}
+    return d.get("dram_bytes_per_launch"), {"file": "profiles/extend_instanced_1080p.json", "commit": d.get("commit")}
+
+
+def tlas_reference_leg(local, desc, steps, torch, l2buf):
+    """The benchmark frame on the GPU with the reference's TLAS (tlas_metric
+    0: its agglomerative walk and pairing metric, tlas_builder.cpp:6-110)
+    instead of the clustering build: rays/s and TLAS node loads per extension
+    ray, to separate the TLAS's share of the speed-up from the kernels'."""
+    import wavefrontpathtracing_gb300 as wf
+    kw = dict(max_bounces=DEPTH, spp=SPP, nee=1, rr_start_depth=RR, accumulate=False)
+    with wf.Renderer(W, H, device=local, tlas_metric=0) as r0:
+        build_scene(r0, desc)
+        for i in range(2):
+            r0.render(frame_seed=500 + i, profile=True, **kw)
+        ms, rays = 0.0, 0
+        for i in range(steps):
+            flush_l2(torch, l2buf)
+            if torch is not None:
+                torch.cuda.synchronize()
+            r0.render(frame_seed=frame_seed(i, 0), profile=True, **kw)
+            st = r0.stats()
+            ms += st["ms_total"]
+            rays += st["rays_extend"] + st["rays_connect"]
+        r0.render(frame_seed=1, count_traffic=True, **kw)
+        c0 = r0.stats()
+    return {"tlas_metric": "reference", "value": round(rays / (ms / 1e3) / 1e6, 3), "unit": "Mrays/s",
+            "ms_per_step": round(ms / steps, 3), "steps": steps,
+            "spp_per_s": round(SPP * steps / (ms / 1e3), 3),
+            "tlas_node_loads_per_ray": round(c0["tlas_node_loads"] / max(1, c0["rays_extend"]), 1)}
 
 
 def build_scene(r, desc):
@@ -181,31 +225,50 @@ def oracle_scene(desc, tlas_metric):
     from tests.helpers import oracle_scene_from_desc
     sc = oracle_scene_from_desc(orc, desc)
     if tlas_metric:
-        # rebuild the TLAS of the same instances with the merged-box metric
+        # rebuild the TLAS of the same instances with the merged-box walk (1)
+        # or the parallel clustering build (2)
         from wavefrontpathtracing_gb300.abi import bvh_instance_dtype
         h = sc._tlas[:8].view(np.uint32)
         inst = sc._tlas[h[1]:].view(bvh_instance_dtype).copy()
-        sc = orc.Scene(list(zip(sc._tris, sc._blas)), orc.tlas_build(inst, metric=1), sc._inst)
+        sc = orc.Scene(list(zip(sc._tris, sc._blas)), orc.tlas_build(inst, metric=tlas_metric), sc._inst)
     return sc
 
 
-def cpu_sample(sc, desc, seconds, threads, seed):
-    """Renders consecutive pixel rows of the frame on the host until ~seconds of
-    work, calibrated by a short first pass.  Returns (Mrays/s, description)."""
+CPU_BANDS = 8
+
+
+def cpu_sample(sc, desc, seconds, threads, seed, n=None):
+    """Renders CPU_BANDS bands of consecutive pixels spread evenly over the
+    frame (band k centred on pixel (k + 1/2) W H / CPU_BANDS) on the host, about
+    `seconds` of work in all, calibrated by a short first pass unless n (the
+    pixel count) is given.  Returns (Mrays/s, description, rays, seconds, n)."""
     npix = W * H
-    n = 2048
-    t0 = time.perf_counter()
-    _, st = sc.render(desc.view, W, H, max_bounces=DEPTH, spp=SPP, frame_seed=seed, nee=1, rr_start_depth=RR,
-                      threads=threads, pixel_range=(npix // 2, npix // 2 + n))
-    dt = time.perf_counter() - t0
-    n = int(min(npix, max(n, n * seconds / max(dt, 1e-3))))
-    p0 = max(0, npix // 2 - n // 2)
-    t0 = time.perf_counter()
-    _, st = sc.render(desc.view, W, H, max_bounces=DEPTH, spp=SPP, frame_seed=seed, nee=1, rr_start_depth=RR,
-                      threads=threads, pixel_range=(p0, p0 + n))
-    dt = time.perf_counter() - t0
-    rays = sum(st["extend_rays"]) + sum(st["shadow_rays"])
-    return rays / dt / 1e6, f"{n} pixels x {SPP} spp of the 1920x1080 frame ({rays} rays, {dt:.1f} s)", rays, dt
+
+    def run(n):
+        nb = max(1, n // CPU_BANDS)
+        rays, t = 0, 0.0
+        for k in range(CPU_BANDS):
+            p0 = min(npix - nb, max(0, int((k + 0.5) * npix / CPU_BANDS) - nb // 2))
+            t0 = time.perf_counter()
+            _, st = sc.render(desc.view, W, H, max_bounces=DEPTH, spp=SPP, frame_seed=seed, nee=1,
+                              rr_start_depth=RR, threads=threads, pixel_range=(p0, p0 + nb))
+            t += time.perf_counter() - t0
+            rays += sum(st["extend_rays"]) + sum(st["shadow_rays"])
+        return rays, t, nb * CPU_BANDS
+
+    if n is None:
+        # calibrate on a pass of at least a tenth of the target (each call has
+        # a fixed start-up cost that a tiny pass would overweight)
+        n = 2048
+        while True:
+            rays, dt, m = run(n)
+            if dt >= 0.1 * seconds or n >= npix:
+                break
+            n = min(npix, n * 4)
+        n = int(min(npix, max(n, n * seconds / max(dt, 1e-3))))
+    rays, dt, n = run(n)
+    return (rays / dt / 1e6, f"{n} pixels x {SPP} spp of the 1920x1080 frame in {CPU_BANDS} bands spread over it "
+            f"({rays} rays, {dt:.1f} s)", rays, dt, n)
 
 
 def run_reference(args, rank, world):
@@ -221,7 +284,7 @@ def run_reference(args, rank, world):
         cpu_sample(sc, desc, per_step, threads, seed=100 + i)
     rays_total, t_total, desc_s = 0, 0.0, ""
     for i in range(args.steps):
-        _, desc_s, rays, dt = cpu_sample(sc, desc, per_step, threads, seed=1 + i)
+        _, desc_s, rays, dt, _ = cpu_sample(sc, desc, per_step, threads, seed=1 + i)
         rays_total += rays
         t_total += dt
     v = rays_total / t_total / 1e6
@@ -475,6 +538,7 @@ def run_ours(args, rank, world, local):
     # --- device-resident timing
     barrier(dist)
     gpu_ms, rays, launches, ext_ms, ext_launches = 0.0, 0, 0, 0.0, 0
+    ext_depth_ms, con_depth_ms = np.zeros(16), np.zeros(16)
     with ClockSampler(local) as clk:
         for i in range(args.steps):
             flush_l2(torch, l2buf)
@@ -487,6 +551,8 @@ def run_ours(args, rank, world, local):
             launches += s["launches"]
             ext_ms += s["ms_extend"]
             ext_launches += s["launches_extend"]
+            ext_depth_ms += np.array(s["ms_extend_depth"])
+            con_depth_ms += np.array(s["ms_connect_depth"])
         r.synchronize()
     barrier(dist)
     t_max, rays_all, value = aggregate_weak(dist, gpu_ms, rays)
@@ -525,7 +591,36 @@ def run_ours(args, rank, world, local):
     ms_per_launch = ext_ms / max(1, ext_launches)
     achieved = bytes_per_launch / (ms_per_launch / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = ncu_traffic()
+    traffic, traffic_src = ncu_traffic(c["rays_extend"] / max(1, ext_launches / args.steps))
+    # per depth: the extension launches (depth 0 makes its camera rays) and the
+    # shadow-ray launches, algorithmic bytes of the counted pass over the
+    # timed frames' CUDA-event time of that depth's launch
+    per_depth, secondary, connect = None, None, None
+    if not args.fused_connect:
+        per_depth, connect = [], []
+        for d in range(DEPTH + 1):
+            n_d, f = int(c["extend_rays_depth"][d]), c["extend_fetch_depth"][d]
+            ms_d = ext_depth_ms[d] / args.steps
+            if n_d and ms_d > 0:
+                b = (n_d * (B_HIT + (0 if d == 0 else B_RAY)) + f[0] * B_TNODE + f[1] * B_INST + f[2] * B_BNODE
+                     + f[3] * B_TRI)
+                per_depth.append({"depth": d, "rays": n_d, "alg_bytes": int(b), "ms": round(ms_d, 4),
+                                  "achieved_gbs": round(b / (ms_d / 1e3) / 1e9, 1),
+                                  "frac": round(b / (ms_d / 1e3) / 1e9 / peak, 4),
+                                  "fetches_per_ray": round((f[0] + f[2]) / n_d, 1)})
+            n_s, f = int(c["shadow_rays_depth"][d]), c["shadow_fetch_depth"][d]
+            ms_s = con_depth_ms[d] / args.steps
+            if d < DEPTH and n_s and ms_s > 0:
+                b = n_s * B_SRAY + f[0] * B_TNODE + f[1] * B_INST + f[2] * B_BNODE + f[3] * B_TRI
+                connect.append({"depth": d, "rays": n_s, "alg_bytes": int(b), "ms": round(ms_s, 4),
+                                "frac": round(b / (ms_s / 1e3) / 1e9 / peak, 4)})
+
+        def total(rows):
+            b, t = sum(x["alg_bytes"] for x in rows), sum(x["ms"] for x in rows)
+            return {"alg_bytes": int(b), "ms": round(t, 4), "achieved_gbs": round(b / (t / 1e3) / 1e9, 1) if t else None,
+                    "frac": round(b / (t / 1e3) / 1e9 / peak, 4) if t else None}
+        secondary = total([x for x in per_depth if x["depth"] >= 1])
+        connect = {"launches": connect, **total(connect)}
     # --- end to end through the C ABI with host buffers
     img = np.zeros((H, W, 4), dtype=np.float32)
     inst_mesh = np.array([ids[m] for m, _, _ in desc.instances], dtype=np.uint32)
@@ -550,18 +645,36 @@ def run_ours(args, rank, world, local):
     h2d = (s1["h2d_bytes"] - s0["h2d_bytes"]) // args.steps
     d2h = (s1["d2h_bytes"] - s0["d2h_bytes"]) // args.steps
     # --- CPU baseline (rank 0 only, N = 1 only): the oracle on a bounded sample
-    cpu = None
+    # with the reference's TLAS (tlas_metric 0), and the same pixels with the
+    # clustering TLAS the GPU line uses (tlas_metric 2)
+    cpu, cpu_clustering = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sc = oracle_scene(desc, tlas_metric=0)
         threads = os.cpu_count() or 1
-        v, sdesc, _, _ = cpu_sample(sc, desc, args.cpu_seconds, threads, seed=1)
+        sc = oracle_scene(desc, tlas_metric=0)
+        v, sdesc, _, _, n_px = cpu_sample(sc, desc, args.cpu_seconds, threads, seed=1)
         cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                "sample": sdesc + "; reference TLAS metric"}
+        sc = oracle_scene(desc, tlas_metric=2)
+        v2, sdesc2, _, _, _ = cpu_sample(sc, desc, args.cpu_seconds, threads, seed=1, n=n_px)
+        cpu_clustering = {"value": round(v2, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                          "sample": sdesc2 + "; clustering TLAS (as the GPU line)"}
+        del sc
     # --- builders: GPU vs the oracle's restatement of the reference's single-threaded C++ builders
     builders = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         builders = builders_leg(r, desc)
     r.close()
+    # --- the same frame on the GPU with the reference's TLAS (tlas_metric 0)
+    tlas_ref = None
+    if rank == 0 and not args.no_tlas_reference and args.tlas_metric != 0:
+        tlas_ref = tlas_reference_leg(local, desc, max(3, min(args.steps, 5)), torch, l2buf)
+    # --- the traversal micro-benchmark at 4.2M rays per set
+    traversal = None
+    if rank == 0 and world == 1 and not args.no_traversal:
+        info, res = traversal_runs(local, args.soup_triangles, 2048, max(3, min(args.steps, 5)), 3,
+                                   orders=(False, True), cpu=not args.no_cpu_baseline, cpu_seconds=2.0)
+        traversal = {"config": TRAVERSAL_CONFIG.format(n=args.soup_triangles, rays=2048 * 2048, side=2048),
+                     **info, "results": res}
     small = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         small = plain_small_leg(local, args.tlas_metric)
@@ -604,7 +717,11 @@ def run_ours(args, rank, world, local):
                                         else "k_trace (extend)"),
                              "achieved": round(achieved, 1),
                              "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                             "frac": round(achieved / peak, 4), "traffic": traffic,
+                             "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_source": traffic_src,
+                             # depth 0 carries 82 % of the rays: 16 identical camera rays per pixel share a
+                             # warp, so one fetch serves 16 of them; the secondary depths are the real traversal
+                             "per_depth": per_depth, "frac_secondary": secondary["frac"] if secondary else None,
+                             "secondary": secondary, "connect": connect,
                              "alg_bytes_per_launch": int(bytes_per_launch),
                              "ms_per_launch": round(ms_per_launch, 4),
                              # DRAM bytes actually moved (ncu, per launch) over the live launch time
@@ -613,6 +730,12 @@ def run_ours(args, rank, world, local):
                 "clocks": clk.summary()}
         if cpu:
             line["cpu_baseline"] = cpu
+        if cpu_clustering:
+            line["cpu_baseline_clustering_tlas"] = cpu_clustering
+        if tlas_ref:
+            line["gpu_reference_tlas"] = tlas_ref
+        if traversal:
+            line["traversal"] = traversal
         if builders:
             line["builders"] = builders
         if small:
@@ -630,38 +753,44 @@ def run_ours(args, rank, world, local):
 
 CPU_TRACE_SAMPLE = 200_000   # first sample of rays per set traced by the oracle for the CPU baseline
 CPU_TRACE_SECONDS = 5.0      # the sample then grows to about this much CPU time
+TRAVERSAL_CONFIG = ("{n} soup triangles (centroids uniform in the unit cube, log-normal edges mu=-5 sigma=0.5, "
+                    "seed 7), one BLAS (16 bins, <= 4 triangles per leaf) under a 1-instance TLAS; {rays} rays per "
+                    "set: coherent pinhole rays ({side}^2, camera 0.5 in front of the cube, 90-degree field of "
+                    "view) and incoherent rays (origins in the cube, uniform directions); closest hit and any hit "
+                    "(tmax U[0,1])")
 
 
-def run_traversal(args, rank, world, local):
-    """Traversal micro-benchmark: 8M soup triangles (centroids uniform in the
-    unit cube, log-normal edges mu=-5 sigma=0.5, seed 7), one BLAS (16 bins,
-    <= 4 triangles per leaf) under a 1-instance TLAS; 16.8M coherent pinhole
-    rays (4096^2, camera 0.5 in front of the cube, 90-degree field of view)
-    and 16.8M incoherent rays (origins in the cube, uniform directions);
-    closest hit and any hit (tmax U[0,1]).  Prints one JSON line
-    per ray set / query kind (the headline line is the default workload)."""
+def traversal_runs(local, n_tris, side, steps, warmup, kinds=("coherent", "incoherent"), orders=(True,),
+                   cpu_seconds=CPU_TRACE_SECONDS, cpu=True, cpu_build=False):
+    """Traversal micro-benchmark: n_tris soup triangles in one BLAS under a
+    1-instance TLAS; side^2 rays per set.  For every ray set, query kind
+    (closest / any hit) and ray order (as given / origins' Morton order,
+    WF_TRACE_REORDER with the sort inside the timed call) one result: GPU time
+    per call (CUDA events, L2 flushed between calls), algorithmic bytes (the
+    reference layouts' fetches, counted by an instrumented pass), the
+    end-to-end rate with host rays and hits, and (cpu) the oracle's port of
+    the reference's scalar traversal on all host cores over a random sample of
+    the set, its hits compared with the GPU's.  Returns (info, results)."""
     import torch
     import wavefrontpathtracing_gb300 as wf
     from wavefrontpathtracing_gb300 import scenes
-    if rank != 0:
-        return
     torch.cuda.set_device(local)
-    n_tris = args.soup_triangles
-    side = args.soup_side
+    t0 = time.perf_counter()
     tris = scenes.triangle_soup(n_tris, seed=7)
+    info = {"soup_generation_s": round(time.perf_counter() - t0, 1)}
     peak, peak_kind = measured_peaks()
+    results = []
     with wf.Renderer(16, 16, device=local) as r:
         t0 = time.perf_counter()
         mesh = r.create_mesh_from_triangles(tris, interval_count=16, max_leaf_prims=4)
-        build_s = time.perf_counter() - t0
+        info["gpu_bvh_build_s"] = round(time.perf_counter() - t0, 3)
         r.begin_scene(scenes.make_view((0.5, 0.5, -0.5), (0.5, 0.5, 0.5), 90.0, 16, 16))
         r.submit_render_mesh(mesh, np.eye(4))
         r.end_scene()
         blob = r.mesh_blas(mesh)
-        blas_bytes = len(blob)
-        reorder = args.reorder == "on"
-        sc, cpu_build_s, blas_equal = None, None, None
-        if not args.no_cpu_baseline:
+        info["blas_bytes"] = len(blob)
+        sc = None
+        if cpu:
             # the oracle's port of the reference's scalar traversal over the same BLAS / TLAS bytes
             from oracle import oracle as orc
             orc.build()
@@ -670,81 +799,104 @@ def run_traversal(args, rank, world, local):
             oi["local_to_world"] = np.eye(4, dtype=np.float32).reshape(16)
             oi["world_to_local"] = bi[0]["world_to_local"]
             sc = orc.Scene([(tris, blob)], r.scene_tlas(), oi)
-            # the reference's single-threaded C++ BLAS build (the oracle's restatement) of the same soup
-            t0 = time.perf_counter()
-            ref_blob = orc.bvh_build(tris, 16, False, 4)
-            cpu_build_s = time.perf_counter() - t0
-            blas_equal = bool(np.array_equal(ref_blob, blob))
-            del ref_blob
+            if cpu_build:
+                # the reference's single-threaded C++ BLAS build (the oracle's restatement) of the same soup
+                t0 = time.perf_counter()
+                ref_blob = orc.bvh_build(tris, 16, False, 4)
+                info["cpu_bvh_build_s"] = round(time.perf_counter() - t0, 2)
+                info["blas_equal_to_cpu_build"] = bool(np.array_equal(ref_blob, blob))
+                del ref_blob
         del blob
-        for kind in args.ray_kinds.split(","):
+        for kind in kinds:
             rays = scenes.soup_rays(side, seed=7, kind=kind)
             for any_hit in (False, True):
                 if any_hit:
                     rays["tmax"] = np.random.default_rng(9).uniform(0, 1, len(rays)).astype(np.float32)
                 d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
                 d_hits = torch.zeros(len(rays) * 20, dtype=torch.uint8, device="cuda")
-                torch.cuda.synchronize()
-                for _ in range(args.warmup):
-                    r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit, reorder=reorder)
-                r.synchronize()
-                ms = []
                 l2 = torch.zeros(L2_BYTES // 4, dtype=torch.float32, device="cuda")
-                for _ in range(args.steps):
-                    l2.add_(1)
-                    torch.cuda.synchronize()
-                    r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit, reorder=reorder)
-                    ms.append(r.stats()["ms_total"])
                 r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit, count_traffic=True)
                 c = r.stats()
                 alg = (len(rays) * (B_RAY + B_HIT) + c["tlas_node_loads"] * B_TNODE + c["instance_loads"] * B_INST
                        + c["blas_node_loads"] * B_BNODE + c["triangle_tests"] * B_TRI)
-                t = float(np.mean(ms))
-                hits = d_hits.cpu().numpy().view(wf.abi.hit_dtype)
-                # e2e: host rays in, host hits out
-                t1 = time.perf_counter()
-                r.trace(rays, any_hit=any_hit, reorder=reorder)
-                e2e_s = time.perf_counter() - t1
-                line = {"metric": "traversal Mrays/s", "value": round(len(rays) / (t / 1e3) / 1e6, 2),
-                        "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-                        "ms_per_step": round(t, 3), "higher_is_better": True, "dtype": "f32",
-                        "data": "synthetic (seeded triangle soup)",
-                        "config": {"workload": f"traversal micro-benchmark, {n_tris} soup triangles, {len(rays)} "
-                                               f"{kind} rays, {'any' if any_hit else 'closest'} hit",
-                                   "blas_bytes": blas_bytes, "gpu_bvh_build_s": round(build_s, 3),
-                                   "cpu_bvh_build_s": round(cpu_build_s, 2) if cpu_build_s else None,
-                                   "blas_equal_to_cpu_build": blas_equal,
-                                   "ray_order": ("origins' Morton codes (stable radix sort inside the timed call)"
-                                                 if reorder else "as given"),
-                                   "hit_fraction": round(float((hits['instance'] != 0xFFFFFFFF).mean()), 4)},
-                        "e2e": {"value": round(len(rays) / e2e_s / 1e6, 2), "unit": "Mrays/s",
-                                "h2d_bytes_per_step": int(rays.nbytes), "d2h_bytes_per_step": int(len(rays) * 20)},
-                        "roofline": {"bound": "hbm", "kernel": "k_trace (AoS)",
-                                     "achieved": round(alg / (t / 1e3) / 1e9, 1), "peak": peak, "peak_kind": peak_kind,
-                                     "unit": "GB/s", "frac": round(alg / (t / 1e3) / 1e9 / peak, 4),
-                                     "alg_bytes_per_launch": int(alg),
-                                     "fetches_per_ray": round((c["blas_node_loads"] + c["tlas_node_loads"]) / len(rays), 2),
-                                     "triangle_tests_per_ray": round(c["triangle_tests"] / len(rays), 2)}}
-                if sc is not None:
-                    # a random sample of the set, grown after a first pass to about CPU_TRACE_SECONDS
-                    threads = os.cpu_count() or 1
-                    n_cpu = CPU_TRACE_SAMPLE
-                    for _ in range(2):
-                        pick = np.sort(np.random.default_rng(5).choice(len(rays), n_cpu, replace=False))
-                        t1 = time.perf_counter()
-                        want, _, _ = sc.trace(rays[pick], flags=1 if any_hit else 0, threads=threads)
-                        cpu_s = time.perf_counter() - t1
-                        n_next = min(len(rays), int(n_cpu * CPU_TRACE_SECONDS / max(cpu_s, 1e-3)))
-                        if n_next <= 2 * n_cpu:
-                            break
-                        n_cpu = n_next
-                    line["cpu_baseline"] = {"value": round(len(pick) / cpu_s / 1e6, 3), "unit": "Mrays/s",
-                                            "cores": threads, "kind": "port",
-                                            "sample": f"{len(pick)} random rays of the set ({cpu_s:.2f} s)",
-                                            "sample_hits_equal": bool(np.array_equal(
-                                                hits[pick].view(np.uint32), want.view(np.uint32)))}
-                print(json.dumps(line), flush=True)
-                del d_rays, d_hits
+                cpu_res = None
+                for reorder in orders:
+                    torch.cuda.synchronize()
+                    for _ in range(warmup):
+                        r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit,
+                                       reorder=reorder)
+                    r.synchronize()
+                    ms = []
+                    for _ in range(steps):
+                        l2.add_(1)
+                        torch.cuda.synchronize()
+                        r.trace_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), any_hit=any_hit,
+                                       reorder=reorder)
+                        ms.append(r.stats()["ms_total"])
+                    t = float(np.mean(ms))
+                    hits = d_hits.cpu().numpy().view(wf.abi.hit_dtype)
+                    t1 = time.perf_counter()
+                    r.trace(rays, any_hit=any_hit, reorder=reorder)
+                    e2e_s = time.perf_counter() - t1
+                    res = {"rays": kind, "query": "any" if any_hit else "closest",
+                           "order": "morton" if reorder else "as given", "n": len(rays), "ms": round(t, 3),
+                           "mrays_per_s": round(len(rays) / (t / 1e3) / 1e6, 2),
+                           "e2e_mrays_per_s": round(len(rays) / e2e_s / 1e6, 2),
+                           "alg_bytes": int(alg), "achieved_gbs": round(alg / (t / 1e3) / 1e9, 1),
+                           "peak": peak, "peak_kind": peak_kind, "frac": round(alg / (t / 1e3) / 1e9 / peak, 4),
+                           "fetches_per_ray": round((c["blas_node_loads"] + c["tlas_node_loads"]) / len(rays), 2),
+                           "triangle_tests_per_ray": round(c["triangle_tests"] / len(rays), 2),
+                           "hit_fraction": round(float((hits["instance"] != 0xFFFFFFFF).mean()), 4)}
+                    if sc is not None and cpu_res is None:
+                        # a random sample of the set, grown after a first pass to about cpu_seconds
+                        threads = os.cpu_count() or 1
+                        n_cpu = min(len(rays), CPU_TRACE_SAMPLE)
+                        for _ in range(2):
+                            pick = np.sort(np.random.default_rng(5).choice(len(rays), n_cpu, replace=False))
+                            t1 = time.perf_counter()
+                            want, _, _ = sc.trace(rays[pick], flags=1 if any_hit else 0, threads=threads)
+                            cpu_s = time.perf_counter() - t1
+                            n_next = min(len(rays), int(n_cpu * cpu_seconds / max(cpu_s, 1e-3)))
+                            if n_next <= 2 * n_cpu:
+                                break
+                            n_cpu = n_next
+                        cpu_res = {"value": round(len(pick) / cpu_s / 1e6, 3), "unit": "Mrays/s", "cores": threads,
+                                   "kind": "port", "sample": f"{len(pick)} random rays of the set ({cpu_s:.2f} s)",
+                                   "sample_hits_equal": bool(np.array_equal(hits[pick].view(np.uint32),
+                                                                            want.view(np.uint32)))}
+                    if cpu_res is not None:
+                        res["cpu_baseline"] = cpu_res
+                    results.append(res)
+                del d_rays, d_hits, l2
+    return info, results
+
+
+def run_traversal(args, rank, world, local):
+    """The traversal micro-benchmark on its own: one JSON line per ray set and
+    query kind (8M soup triangles, 16.8M rays per set by default)."""
+    if rank != 0:
+        return
+    info, results = traversal_runs(local, args.soup_triangles, args.soup_side, args.steps, args.warmup,
+                                   kinds=args.ray_kinds.split(","), orders=(args.reorder == "on",),
+                                   cpu=not args.no_cpu_baseline, cpu_build=not args.no_cpu_baseline)
+    for res in results:
+        line = {"metric": "traversal Mrays/s", "value": res["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
+                "dtype": "f32", "data": "synthetic (seeded triangle soup)",
+                "config": {"workload": f"traversal micro-benchmark, {args.soup_triangles} soup triangles, {res['n']} "
+                                       f"{res['rays']} rays, {res['query']} hit",
+                           "ray_order": ("origins' Morton codes (stable radix sort inside the timed call)"
+                                         if res["order"] == "morton" else "as given"),
+                           "hit_fraction": res["hit_fraction"], **info},
+                "e2e": {"value": res["e2e_mrays_per_s"], "unit": "Mrays/s", "h2d_bytes_per_step": res["n"] * 32,
+                        "d2h_bytes_per_step": res["n"] * 20},
+                "roofline": {"bound": "hbm", "kernel": "k_trace (AoS)", "achieved": res["achieved_gbs"],
+                             "peak": res["peak"], "peak_kind": res["peak_kind"], "unit": "GB/s", "frac": res["frac"],
+                             "alg_bytes_per_launch": res["alg_bytes"], "fetches_per_ray": res["fetches_per_ray"],
+                             "triangle_tests_per_ray": res["triangle_tests_per_ray"]}}
+        if "cpu_baseline" in res:
+            line["cpu_baseline"] = res["cpu_baseline"]
+        print(json.dumps(line), flush=True)
 
 
 def main():
@@ -761,6 +913,9 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rendering leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes leg")
     ap.add_argument("--no-megakernel", action="store_true", help="skip the megakernel A/B leg")
+    ap.add_argument("--no-traversal", action="store_true", help="skip the traversal micro-benchmark leg")
+    ap.add_argument("--no-tlas-reference", action="store_true",
+                    help="skip the frame rendered with the reference's TLAS (tlas_metric 0)")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-config", default=None,
                     help="batched workload: CAPACITY,THRESHOLD,BLOCK[,USE_GRAPH] instead of the autotuner "

@@ -164,6 +164,12 @@ typedef struct wf_stats {
      * stages; a tail launch counts in launches, not in launches_extend) */
     double   ms_tail;
     uint64_t tail_depth;
+    /* profile = 1: GPU time of the extension (incl. the depth-0 camera rays)
+     * and shadow-ray launches, per depth */
+    double   ms_extend_depth[16], ms_connect_depth[16];
+    /* count_traffic = 1: the fetches per depth, {TLAS nodes, instances, BLAS
+     * nodes, triangle tests}, of the extension and the shadow rays */
+    uint64_t extend_fetch_depth[16][4], shadow_fetch_depth[16][4];
 } wf_stats;
 
 /* ---- lifetime (renderer::init / exit, renderer.h:23-24) ------------------ */

@@ -23,7 +23,7 @@ instance_dtype = np.dtype([("local_to_world", "<f4", 16), ("world_to_local", "<f
                            ("material", material_dtype), ("mesh", "<u4"), ("bsdf", "<u4"), ("ior", "<f4")])
 assert instance_dtype.itemsize == 192
 
-ANY_HIT, NO_CULL = 1, 2
+ANY_HIT, NO_CULL, TIE_RULE = 1, 2, 4
 
 
 class _Mesh(ctypes.Structure):
@@ -54,7 +54,8 @@ class RenderParams(ctypes.Structure):
                 ("hdr_env_strength", ctypes.c_float), ("env_color", ctypes.c_float * 3),
                 ("spp", ctypes.c_uint32), ("sample_offset", ctypes.c_uint32), ("nee", ctypes.c_uint32),
                 ("rr_start_depth", ctypes.c_uint32), ("frame_seed", ctypes.c_uint32),
-                ("pixel_begin", ctypes.c_uint32), ("pixel_end", ctypes.c_uint32), ("view_mode", ctypes.c_uint32)]
+                ("pixel_begin", ctypes.c_uint32), ("pixel_end", ctypes.c_uint32), ("view_mode", ctypes.c_uint32),
+                ("tie_rule", ctypes.c_uint32)]
 
 
 class RenderStats(ctypes.Structure):
@@ -259,9 +260,10 @@ class Scene:
 
     def render(self, view, width, height, max_bounces=4, spp=1, frame_seed=1, nee=0, rr_start_depth=0xFFFFFFFF,
                env_color=(0.0, 0.0, 0.0), env_strength=1.0, cosine=1, sample_offset=0, threads=1, f64=False,
-               pixel_range=None, accum=None, view_mode=0):
+               pixel_range=None, accum=None, view_mode=0, tie_rule=False):
         p = RenderParams()
         p.view_mode = view_mode
+        p.tie_rule = int(tie_rule)
         p.max_bounces, p.cosine_weighted_diffuse, p.hdr_env_strength = max_bounces, cosine, env_strength
         p.env_color[:] = env_color
         p.spp, p.sample_offset, p.nee, p.rr_start_depth, p.frame_seed = spp, sample_offset, nee, rr_start_depth, \

@@ -40,7 +40,7 @@ static inline FN(v3) FN(xform)(FN(v3) v, R w, const float* m) {
 
 /* intersect_ray_aabb (intersect.hlsl:53-76); min/max are IEEE minNum/maxNum
  * like HLSL's. */
-static inline R FN(slab)(const float* bmn, const float* bmx, FN(v3) o, FN(v3) inv, R t) {
+static inline R FN(slab_cmp)(const float* bmn, const float* bmx, FN(v3) o, FN(v3) inv, R t, int tie) {
     R tx1 = ((R)bmn[0] - o.x) * inv.x, tx2 = ((R)bmx[0] - o.x) * inv.x;
     R tmin = FMIN(tx1, tx2), tmax = FMAX(tx1, tx2);
     R ty1 = ((R)bmn[1] - o.y) * inv.y, ty2 = ((R)bmx[1] - o.y) * inv.y;
@@ -49,14 +49,17 @@ static inline R FN(slab)(const float* bmn, const float* bmx, FN(v3) o, FN(v3) in
     R tz1 = ((R)bmn[2] - o.z) * inv.z, tz2 = ((R)bmx[2] - o.z) * inv.z;
     tmin = FMAX(tmin, FMIN(tz1, tz2));
     tmax = FMIN(tmax, FMAX(tz1, tz2));
-    if (tmax >= tmin && tmin < t && tmax > K(0.0)) return tmin;
+    if (tmax >= tmin && (tie ? tmin <= t : tmin < t) && tmax > K(0.0)) return tmin;
     return MAXT;
+}
+static inline R FN(slab)(const float* bmn, const float* bmx, FN(v3) o, FN(v3) inv, R t) {
+    return FN(slab_cmp)(bmn, bmx, o, inv, t, 0);
 }
 
 /* intersect_ray_triangle (intersect.hlsl:7-51), Moeller-Trumbore with the
  * back-face test det < 1e-8 (|det| < 1e-8 without culling). */
-static inline int FN(tri)(FN(v3) v0, FN(v3) v1, FN(v3) v2, FN(v3) o, FN(v3) d, R* t_io, R* bu, R* bv,
-                          int no_cull) {
+static inline int FN(tri_cmp)(FN(v3) v0, FN(v3) v1, FN(v3) v2, FN(v3) o, FN(v3) d, R* t_io, R* bu, R* bv,
+                              int no_cull, int tie_wins) {
     FN(v3) e1 = FN(sub)(v1, v0), e2 = FN(sub)(v2, v0);
     FN(v3) pvec = FN(cross)(d, e2);
     R det = FN(dot)(e1, pvec);
@@ -69,9 +72,13 @@ static inline int FN(tri)(FN(v3) v0, FN(v3) v1, FN(v3) v2, FN(v3) o, FN(v3) d, R
     R w = FN(dot)(d, qvec) * inv_det;
     if (w < K(0.0) || v + w > K(1.0)) return 0;
     R t = FN(dot)(e2, qvec) * inv_det;
-    if (t < K(0.0) || t >= *t_io) return 0;
+    if (t < K(0.0) || t > *t_io || (t == *t_io && !tie_wins)) return 0;
     *t_io = t; *bu = v; *bv = w;
     return 1;
+}
+static inline int FN(tri)(FN(v3) v0, FN(v3) v1, FN(v3) v2, FN(v3) o, FN(v3) d, R* t_io, R* bu, R* bv,
+                          int no_cull) {
+    return FN(tri_cmp)(v0, v1, v2, o, d, t_io, bu, bv, no_cull, 0);
 }
 
 typedef struct {
@@ -82,9 +89,15 @@ typedef struct {
 #define ORC_STACK 64
 
 /* trace_ray_bvh_local (accelstruct.hlsl:58-131).  Returns 1 on a hit, 0 on
- * none, -1 when the 64-entry stack overflowed. */
+ * none, -1 when the 64-entry stack overflowed.  With ORC_TIE_RULE (closest
+ * hit only) a triangle at exactly the current t wins when its (instance,
+ * primitive) is smaller than the current hit's, and boxes entered at exactly
+ * the current t are visited: the result is then the smallest (t, instance,
+ * primitive) whatever the visiting order (the order the reference's strict
+ * "t < ray.t" makes matter only on exact ties). */
 static int FN(trace_blas)(const uint8_t* blas, FN(v3) o, FN(v3) d, FN(v3) inv, R* t, FN(hit)* h,
-                          uint32_t flags, orc_counters* c) {
+                          uint32_t flags, orc_counters* c, uint32_t inst) {
+    const int tie = (flags & ORC_TIE_RULE) && !(flags & ORC_ANY_HIT);
     bvh_header_t hd;
     memcpy(&hd, blas, sizeof(hd));
     const uint8_t* nodes = blas + hd.nodes_offset;
@@ -103,8 +116,14 @@ static int FN(trace_blas)(const uint8_t* blas, FN(v3) o, FN(v3) d, FN(v3) inv, R
                 memcpy(&tr, tris + 36ull * ti, 36);
                 c->triangle_tests++;
                 R bu, bv;
-                if (FN(tri)(FN(ld)(tr.p0), FN(ld)(tr.p1), FN(ld)(tr.p2), o, d, t, &bu, &bv,
-                            (flags & ORC_NO_CULL) != 0)) {
+                int wins = 0;
+                if (tie) {
+                    /* the current hit: this instance once it has one here, else the outer one */
+                    const uint32_t bi = has_hit ? inst : h->inst;
+                    wins = inst < bi || (inst == bi && ti < h->prim);
+                }
+                if (FN(tri_cmp)(FN(ld)(tr.p0), FN(ld)(tr.p1), FN(ld)(tr.p2), o, d, t, &bu, &bv,
+                                (flags & ORC_NO_CULL) != 0, wins)) {
                     h->prim = ti; h->u = bu; h->v = bv;
                     has_hit = 1;
                     if (flags & ORC_ANY_HIT) return 1;
@@ -118,8 +137,8 @@ static int FN(trace_blas)(const uint8_t* blas, FN(v3) o, FN(v3) d, FN(v3) inv, R
         memcpy(&l, nodes + 32ull * node.left_first, 32);
         memcpy(&r, nodes + 32ull * (node.left_first + 1), 32);
         c->blas_node_loads += 2;
-        R dl = FN(slab)(l.aabb_min, l.aabb_max, o, inv, *t);
-        R dr = FN(slab)(r.aabb_min, r.aabb_max, o, inv, *t);
+        R dl = FN(slab_cmp)(l.aabb_min, l.aabb_max, o, inv, *t, tie);
+        R dr = FN(slab_cmp)(r.aabb_min, r.aabb_max, o, inv, *t, tie);
         if (dl > dr) { R td = dl; dl = dr; dr = td; bvh_node_t tn = l; l = r; r = tn; }
         if (dl == MAXT) {
             if (sp == 0) break;
@@ -151,8 +170,9 @@ static int FN(trace_one)(const orc_scene* s, FN(v3) o, FN(v3) d, R tmax, uint32_
     int sp = 0;
     memcpy(&node, nodes, 32);
     c->tlas_node_loads++;
+    const int tie = (flags & ORC_TIE_RULE) && !(flags & ORC_ANY_HIT);
     if (s->inst_count == 0) return 0;
-    if (FN(slab)(node.aabb_min, node.aabb_max, o, inv, t) == MAXT) return 0;
+    if (FN(slab_cmp)(node.aabb_min, node.aabb_max, o, inv, t, tie) == MAXT) return 0;
     for (;;) {
         if (node.left_right == 0) {
             bvh_instance_t in;
@@ -162,7 +182,7 @@ static int FN(trace_one)(const orc_scene* s, FN(v3) o, FN(v3) d, R tmax, uint32_
             FN(v3) ld = FN(xform)(d, K(0.0), in.world_to_local);
             FN(v3) linv = FN(mk)(K(1.0) / ld.x, K(1.0) / ld.y, K(1.0) / ld.z);
             R lt = t;
-            int r = FN(trace_blas)(s->meshes[in.bvh_index].blas, lo, ld, linv, &lt, h, flags, c);
+            int r = FN(trace_blas)(s->meshes[in.bvh_index].blas, lo, ld, linv, &lt, h, flags, c, node.instance_idx);
             if (r < 0) {
                 h->inst = WF_INVALID_INDEX; h->prim = WF_INVALID_INDEX; h->t = MAXT; h->u = 0; h->v = 0;
                 return -1;
@@ -181,8 +201,8 @@ static int FN(trace_one)(const orc_scene* s, FN(v3) o, FN(v3) d, R tmax, uint32_
         memcpy(&l, nodes + 32ull * (node.left_right >> 16), 32);
         memcpy(&r, nodes + 32ull * (node.left_right & 0xFFFFu), 32);
         c->tlas_node_loads += 2;
-        R dl = FN(slab)(l.aabb_min, l.aabb_max, o, inv, t);
-        R dr = FN(slab)(r.aabb_min, r.aabb_max, o, inv, t);
+        R dl = FN(slab_cmp)(l.aabb_min, l.aabb_max, o, inv, t, tie);
+        R dr = FN(slab_cmp)(r.aabb_min, r.aabb_max, o, inv, t, tie);
         if (dl > dr) { R td = dl; dl = dr; dr = td; tlas_node_t tn = l; l = r; r = tn; }
         if (dl == MAXT) {
             if (sp == 0) break;
@@ -564,7 +584,8 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
     for (uint32_t d = 0; d <= P->max_bounces; ++d) {
         st->extend_rays[d < 16 ? d : 15]++;
         FN(hit) h;
-        int tr = FN(trace_one)(s, ro, rd, MAXT, (flags & ORC_F_INSIDE) ? ORC_NO_CULL : 0, &h,
+        int tr = FN(trace_one)(s, ro, rd, MAXT,
+                               ((flags & ORC_F_INSIDE) ? ORC_NO_CULL : 0) | (P->tie_rule ? ORC_TIE_RULE : 0), &h,
                                &st->extend_traffic);
         if (tr < 0) { st->stack_overflows++; }
         if (h.inst == WF_INVALID_INDEX) {

@@ -94,7 +94,10 @@ typedef struct orc_counters {
     uint64_t tlas_node_loads, instance_loads, blas_node_loads, triangle_tests;
 } orc_counters;
 
-enum { ORC_ANY_HIT = 1, ORC_NO_CULL = 2 };
+/* ORC_TIE_RULE: closest hit = smallest (t, instance, primitive), whatever
+ * the visiting order (the reference keeps the first of equal-t hits it
+ * visits); the GPU library's quantized 4-wide BLAS layout uses it. */
+enum { ORC_ANY_HIT = 1, ORC_NO_CULL = 2, ORC_TIE_RULE = 4 };
 
 /* Software closest-hit / any-hit query (accelstruct.hlsl:58-218,
  * intersect.hlsl:7-76).  Returns the number of rays whose 64-entry stack
@@ -118,6 +121,7 @@ typedef struct orc_render_params {
     uint32_t frame_seed;
     uint32_t pixel_begin, pixel_end;   /* render only this pixel range (end 0 = all) */
     uint32_t view_mode;       /* RENDER_VIEW_MODE_* (shade.hlsl:140-153); 0 = path tracing */
+    uint32_t tie_rule;        /* 1: closest-hit rays use ORC_TIE_RULE */
 } orc_render_params;
 
 typedef struct orc_render_stats {

@@ -96,12 +96,16 @@ class Stats(ctypes.Structure):
                 ("shadow_blas_node_loads", ctypes.c_uint64), ("shadow_triangle_tests", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("extend_rays_depth", ctypes.c_uint64 * 16), ("shadow_rays_depth", ctypes.c_uint64 * 16),
-                ("ms_tail", ctypes.c_double), ("tail_depth", ctypes.c_uint64)]
+                ("ms_tail", ctypes.c_double), ("tail_depth", ctypes.c_uint64),
+                ("ms_extend_depth", ctypes.c_double * 16), ("ms_connect_depth", ctypes.c_double * 16),
+                ("extend_fetch_depth", (ctypes.c_uint64 * 4) * 16), ("shadow_fetch_depth", (ctypes.c_uint64 * 4) * 16)]
 
     def as_dict(self):
         d = {name: getattr(self, name) for name, _ in self._fields_}
-        d["extend_rays_depth"] = list(self.extend_rays_depth)
-        d["shadow_rays_depth"] = list(self.shadow_rays_depth)
+        for k in ("extend_rays_depth", "shadow_rays_depth", "ms_extend_depth", "ms_connect_depth"):
+            d[k] = list(getattr(self, k))
+        for k in ("extend_fetch_depth", "shadow_fetch_depth"):
+            d[k] = [list(row) for row in getattr(self, k)]
         return d
 
 
@@ -126,6 +130,7 @@ class BatchStats(ctypes.Structure):
 
 assert ctypes.sizeof(RenderSettings) == 28 and ctypes.sizeof(View) == 272
 assert ctypes.sizeof(BatchConfig) == 32 and ctypes.sizeof(BatchStats) == 64
+assert ctypes.sizeof(Stats) == 1736   # wf_stats
 
 
 def ptr(a):

@@ -96,6 +96,7 @@ struct Mesh {
 struct EventPair {
     cudaEvent_t a, b;
     int stage;
+    int depth;   // the bounce depth of an extend / connect launch, else -1
 };
 
 enum Stage { ST_GENERATE = 0, ST_EXTEND, ST_SHADE, ST_CONNECT, ST_POST, ST_TLAS, ST_TAIL, ST_COUNT };
@@ -197,7 +198,8 @@ struct StageTimer {
     wf_ctx* c;
     cudaStream_t st;
     EventPair* ev = nullptr;
-    StageTimer(wf_ctx* ctx, bool on, int stage, cudaStream_t stream = nullptr) : c(ctx), st(stream ? stream : ctx->stream) {
+    StageTimer(wf_ctx* ctx, bool on, int stage, cudaStream_t stream = nullptr, int depth = -1)
+        : c(ctx), st(stream ? stream : ctx->stream) {
         nvtxRangePushA(kStageLabel[stage]);
         if (!on) return;
         if (c->events_used == c->events.size()) {
@@ -208,6 +210,7 @@ struct StageTimer {
         }
         ev = &c->events[c->events_used++];
         ev->stage = stage;
+        ev->depth = depth;
         cudaEventRecord(ev->a, st);
     }
     ~StageTimer() {
@@ -436,7 +439,12 @@ int finish_timing(wf_ctx* c) {
     for (size_t i = 0; i < c->events_used; ++i) {
         float e = 0.0f;
         cudaEventElapsedTime(&e, c->events[i].a, c->events[i].b);
-        st[c->events[i].stage] += e;
+        const EventPair& ev = c->events[i];
+        st[ev.stage] += e;
+        if (ev.depth >= 0 && ev.depth < (int)kMaxDepth) {
+            if (ev.stage == ST_EXTEND) c->stats.ms_extend_depth[ev.depth] += e;
+            if (ev.stage == ST_CONNECT) c->stats.ms_connect_depth[ev.depth] += e;
+        }
     }
     c->stats.ms_generate = st[ST_GENERATE];
     c->stats.ms_extend = st[ST_EXTEND];
@@ -455,17 +463,28 @@ int finish_timing(wf_ctx* c) {
         c->stats.shadow_rays_depth[d] = tot[2 + kMaxDepth + d];
     }
     if (c->count_traffic) {
-        Counters k[2];
+        // one counter slot per depth: [d] extension rays, [kMaxDepth + d] shadow rays
+        Counters k[2 * kMaxDepth];
         WF_CUDA(d2h(c, k, c->counters, sizeof(k)));
         WF_CUDA(cudaStreamSynchronize(c->stream));
-        c->stats.tlas_node_loads = k[0].tlas_node_loads;
-        c->stats.instance_loads = k[0].instance_loads;
-        c->stats.blas_node_loads = k[0].blas_node_loads;
-        c->stats.triangle_tests = k[0].triangle_tests;
-        c->stats.shadow_tlas_node_loads = k[1].tlas_node_loads;
-        c->stats.shadow_instance_loads = k[1].instance_loads;
-        c->stats.shadow_blas_node_loads = k[1].blas_node_loads;
-        c->stats.shadow_triangle_tests = k[1].triangle_tests;
+        for (uint32_t d = 0; d < kMaxDepth; ++d) {
+            const Counters& e = k[d];
+            const Counters& h = k[kMaxDepth + d];
+            c->stats.tlas_node_loads += e.tlas_node_loads;
+            c->stats.instance_loads += e.instance_loads;
+            c->stats.blas_node_loads += e.blas_node_loads;
+            c->stats.triangle_tests += e.triangle_tests;
+            c->stats.shadow_tlas_node_loads += h.tlas_node_loads;
+            c->stats.shadow_instance_loads += h.instance_loads;
+            c->stats.shadow_blas_node_loads += h.blas_node_loads;
+            c->stats.shadow_triangle_tests += h.triangle_tests;
+            const uint64_t ef[4] = {e.tlas_node_loads, e.instance_loads, e.blas_node_loads, e.triangle_tests};
+            const uint64_t hf[4] = {h.tlas_node_loads, h.instance_loads, h.blas_node_loads, h.triangle_tests};
+            for (int j = 0; j < 4; ++j) {
+                c->stats.extend_fetch_depth[d][j] = ef[j];
+                c->stats.shadow_fetch_depth[d][j] = hf[j];
+            }
+        }
     }
     c->timing_pending = false;
     return WF_OK;
@@ -480,7 +499,7 @@ int begin_call(wf_ctx* c, bool count_traffic) {
     c->tail_depth = 0;
     c->count_traffic = count_traffic;
     WF_CUDA(cudaMemsetAsync(c->totals, 0, (2 + 2 * kMaxDepth) * sizeof(unsigned long long), c->stream));
-    WF_CUDA(cudaMemsetAsync(c->counters, 0, 2 * sizeof(Counters), c->stream));
+    WF_CUDA(cudaMemsetAsync(c->counters, 0, 2 * kMaxDepth * sizeof(Counters), c->stream));
     WF_CUDA(cudaEventRecord(c->t0, c->stream));
     return WF_OK;
 }
@@ -741,12 +760,12 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
             rc = fail(WF_ERR_CUDA, "wf_create: event / pinned buffer creation failed");
     }
     if (rc == WF_OK) rc = dev_alloc(&c->status, 1);
-    if (rc == WF_OK) rc = dev_alloc(&c->counters, 2);
+    if (rc == WF_OK) rc = dev_alloc(&c->counters, 2 * kMaxDepth);
     if (rc == WF_OK) rc = dev_alloc(&c->trace_fetch, 1);
     if (rc == WF_OK) rc = dev_alloc(&c->totals, 2 + 2 * kMaxDepth);
     if (rc == WF_OK) {
         cudaMemset(c->status, 0, 4);
-        cudaMemset(c->counters, 0, 2 * sizeof(Counters));
+        cudaMemset(c->counters, 0, 2 * kMaxDepth * sizeof(Counters));
         cudaMemset(c->totals, 0, (2 + 2 * kMaxDepth) * sizeof(unsigned long long));
         if (cudaDeviceSynchronize() != cudaSuccess) rc = fail(WF_ERR_CUDA, "wf_create: device initialization failed");
     }
@@ -1256,15 +1275,15 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
             break;
         }
         if (d == 0) {
-            StageTimer t(c, P.prof, ST_EXTEND);
+            StageTimer t(c, P.prof, ST_EXTEND, nullptr, (int)d);
             WF_CUDA(launch_extend_camera(P.S, B, W, P.cnt, c->totals, c->stream));
         } else if (P.fused) {
             // the shadow rays of depth d - 1 with the extension rays of depth d
-            StageTimer t(c, P.prof, ST_EXTEND);
+            StageTimer t(c, P.prof, ST_EXTEND, nullptr, (int)d);
             WF_CUDA(launch_trace_pair(P.S, B, d, c->totals, c->stream));
             c->launches_connect++;
         } else {
-            StageTimer t(c, P.prof, ST_EXTEND);
+            StageTimer t(c, P.prof, ST_EXTEND, nullptr, (int)d);
             WF_CUDA(launch_extend(P.S, B, d, W.npaths, P.cnt, c->totals, c->stream));
         }
         // connect at depth d - 1 has added its contributions before shade adds more
@@ -1283,7 +1302,7 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
             WF_CUDA(cudaEventRecord(c->ev_shade[d], c->stream));
             WF_CUDA(cudaStreamWaitEvent(c->side, c->ev_shade[d], 0));
             {
-                StageTimer t(c, P.prof, ST_CONNECT, c->side);
+                StageTimer t(c, P.prof, ST_CONNECT, c->side, (int)d);
                 WF_CUDA(launch_connect(P.S, B, d, W.npaths, P.cnt, c->totals + 1, c->side));
             }
             WF_CUDA(cudaEventRecord(c->ev_conn[d], c->side));

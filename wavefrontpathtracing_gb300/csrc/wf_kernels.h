@@ -62,7 +62,7 @@ struct RenderBuffers {
                           // [2 kMaxDepth + d], [3 kMaxDepth + d] the traversal kernels' fetch counters
     float4* accum;        // per pixel {radiance sum rgb, samples}
     uint32_t* status;     // device error flags (ERRF_*)
-    Counters* counters;   // [0] extension traffic, [1] shadow traffic
+    Counters* counters;   // fetch counts per depth: [d] extension rays, [kMaxDepth + d] shadow rays
     uint32_t capacity;    // paths per wave (queue and path-state entries)
 };
 

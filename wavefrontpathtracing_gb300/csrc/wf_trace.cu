@@ -171,8 +171,9 @@ cudaError_t launch_extend(const SceneRefs& S, const RenderBuffers& B, uint32_t d
     io.qo = B.q_o[cur]; io.qd = B.q_d[cur]; io.tuvp = B.h_tuvp; io.inst = B.h_inst;
     io.cap = B.capacity; io.status = B.status;
     uint32_t* fetch = B.counts + 2 * kMaxDepth + depth;
-    return count ? launch<false, true>(S, io, B.counts + depth, 0, fetch, B.status, B.counters, total, stream)
-                 : launch<false, false>(S, io, B.counts + depth, 0, fetch, B.status, B.counters, total, stream);
+    Counters* ctr = B.counters + depth;
+    return count ? launch<false, true>(S, io, B.counts + depth, 0, fetch, B.status, ctr, total, stream)
+                 : launch<false, false>(S, io, B.counts + depth, 0, fetch, B.status, ctr, total, stream);
 }
 
 cudaError_t launch_extend_camera(const SceneRefs& S, const RenderBuffers& B, const WaveParams& W, bool count,
@@ -192,10 +193,9 @@ cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t 
     io.so = B.s_o[par]; io.sd = B.s_d[par]; io.sc = B.s_c[par]; io.L = B.ps_L;
     io.cap = B.capacity; io.status = B.status;
     uint32_t* fetch = B.counts + 3 * kMaxDepth + depth;
-    return count ? launch<true, true>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, B.counters + 1, total,
-                                      stream)
-                 : launch<true, false>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, B.counters + 1, total,
-                                       stream);
+    Counters* ctr = B.counters + kMaxDepth + depth;
+    return count ? launch<true, true>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, ctr, total, stream)
+                 : launch<true, false>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, ctr, total, stream);
 }
 
 cudaError_t launch_trace_pair(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, unsigned long long* totals,

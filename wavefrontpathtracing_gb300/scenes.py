@@ -420,15 +420,29 @@ def batch_scenes(count=64, seed=5, tri_range=(1_000, 2_000_000), resolutions=(64
 
 def triangle_soup(n, seed=7, mu=-5.0, sigma=0.5):
     """n triangles: centroid uniform in [0,1]^3, three vertices at centroid +
-    L * (random unit vector), L log-normal(mu, sigma)."""
+    L * (random unit vector), L log-normal(mu, sigma).  The random draws are
+    made in one stream; the per-triangle arithmetic runs on row blocks in
+    threads (the same operations on every row, so the result does not depend
+    on the split)."""
+    import concurrent.futures
+    import os
     rng = np.random.default_rng(seed)
     c = rng.random((n, 3), dtype=np.float64)
     L = rng.lognormal(mu, sigma, size=(n, 1))
     dirs = rng.normal(size=(n, 3, 3))
-    dirs /= np.linalg.norm(dirs, axis=2, keepdims=True)
-    p = c[:, None, :] + L[:, None, :] * dirs
-    p -= p.mean(axis=1, keepdims=True) - c[:, None, :]
-    return _tris_from_arrays(p[:, 0], p[:, 1], p[:, 2])
+    out = np.zeros(n, dtype=triangle_dtype)
+
+    def block(lo, hi):
+        d = dirs[lo:hi]
+        d /= np.linalg.norm(d, axis=2, keepdims=True)
+        p = c[lo:hi, None, :] + L[lo:hi, None, :] * d
+        p -= p.mean(axis=1, keepdims=True) - c[lo:hi, None, :]
+        out[lo:hi] = _tris_from_arrays(p[:, 0], p[:, 1], p[:, 2])
+
+    step = 1 << 18
+    with concurrent.futures.ThreadPoolExecutor(min(16, os.cpu_count() or 1)) as ex:
+        list(ex.map(lambda lo: block(lo, min(n, lo + step)), range(0, n, step)))
+    return out
 
 
 def soup_rays(n_side, seed=7, kind="coherent"):
