@@ -172,9 +172,9 @@ def measured_peaks():
 
 def ncu_traffic(rays_per_launch):
     """DRAM bytes per extension launch from the committed ncu summary
-    (profiles/extend_instanced_1080p.json: read + written bytes per ray of
-    the depth >= 1 extension launches of a reduced frame, and the git commit
-    it was captured at), scaled to this frame's rays per launch."""
+    (profiles/extend_instanced_1080p.json: read + written bytes per ray over
+    the nine extension launches of a reduced frame, and the git commit it was
+    captured at), scaled to this frame's rays per launch."""
     p = os.path.join(ROOT, "profiles", "extend_instanced_1080p.json")
     if not os.path.exists(p):
         return None, None
@@ -524,7 +524,7 @@ def run_ours(args, rank, world, local):
     except Exception:
         torch, l2buf = None, None
     desc = scenes.instanced_scene(width=W, height=H, spp=SPP, max_bounces=DEPTH)
-    r = wf.Renderer(W, H, device=local, tlas_metric=args.tlas_metric)
+    r = wf.Renderer(W, H, device=local, tlas_metric=args.tlas_metric, blas_layout=args.blas_layout)
     ids = build_scene(r, desc)
 
     def frame(seed, profile):
@@ -672,7 +672,8 @@ def run_ours(args, rank, world, local):
     traversal = None
     if rank == 0 and world == 1 and not args.no_traversal:
         info, res = traversal_runs(local, args.soup_triangles, 2048, max(3, min(args.steps, 5)), 3,
-                                   orders=(False, True), cpu=not args.no_cpu_baseline, cpu_seconds=2.0)
+                                   orders=(False, True), cpu=not args.no_cpu_baseline, cpu_seconds=2.0,
+                                   blas_layout=args.blas_layout)
         traversal = {"config": TRAVERSAL_CONFIG.format(n=args.soup_triangles, rays=2048 * 2048, side=2048),
                      **info, "results": res}
     small = None
@@ -693,6 +694,7 @@ def run_ours(args, rank, world, local):
                            "triangles": desc.triangle_count,
                            "instanced_triangles": desc.instanced_triangle_count, "instances": len(desc.instances),
                            "tlas_metric": ["reference", "merged-box walk", "parallel clustering"][args.tlas_metric],
+                           "blas_layout": ["binary child pairs", "quantized 4-wide"][args.blas_layout],
                            "l2": "256 MiB buffer written between timed frames; working set > L2"},
                 "spp_per_s": round(spp_per_s, 3),
                 "rays_per_step": rays // args.steps,
@@ -761,7 +763,7 @@ TRAVERSAL_CONFIG = ("{n} soup triangles (centroids uniform in the unit cube, log
 
 
 def traversal_runs(local, n_tris, side, steps, warmup, kinds=("coherent", "incoherent"), orders=(True,),
-                   cpu_seconds=CPU_TRACE_SECONDS, cpu=True, cpu_build=False):
+                   cpu_seconds=CPU_TRACE_SECONDS, cpu=True, cpu_build=False, blas_layout=0):
     """Traversal micro-benchmark: n_tris soup triangles in one BLAS under a
     1-instance TLAS; side^2 rays per set.  For every ray set, query kind
     (closest / any hit) and ray order (as given / origins' Morton order,
@@ -780,7 +782,7 @@ def traversal_runs(local, n_tris, side, steps, warmup, kinds=("coherent", "incoh
     info = {"soup_generation_s": round(time.perf_counter() - t0, 1)}
     peak, peak_kind = measured_peaks()
     results = []
-    with wf.Renderer(16, 16, device=local) as r:
+    with wf.Renderer(16, 16, device=local, blas_layout=blas_layout) as r:
         t0 = time.perf_counter()
         mesh = r.create_mesh_from_triangles(tris, interval_count=16, max_leaf_prims=4)
         info["gpu_bvh_build_s"] = round(time.perf_counter() - t0, 3)
@@ -878,7 +880,8 @@ def run_traversal(args, rank, world, local):
         return
     info, results = traversal_runs(local, args.soup_triangles, args.soup_side, args.steps, args.warmup,
                                    kinds=args.ray_kinds.split(","), orders=(args.reorder == "on",),
-                                   cpu=not args.no_cpu_baseline, cpu_build=not args.no_cpu_baseline)
+                                   cpu=not args.no_cpu_baseline, cpu_build=not args.no_cpu_baseline,
+                                   blas_layout=args.blas_layout)
     for res in results:
         line = {"metric": "traversal Mrays/s", "value": res["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
@@ -908,6 +911,9 @@ def main():
     ap.add_argument("--tlas-metric", type=int, default=2,
                     help="TLAS build: 0 = reference walk and metric, 1 = merged-box walk, 2 = parallel clustering")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--blas-layout", type=int, default=0, choices=[0, 1],
+                    help="BLAS layout the traversal reads: 0 = the reference's binary child pairs, 1 = quantized "
+                         "4-wide nodes (order-independent tie rule for closest hits)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rendering leg")

@@ -54,7 +54,17 @@ typedef struct wf_init_params {
                                    (tlas_builder.cpp:96-97, bit-exact), 1 = the same walk pairing by the
                                    half area of the merged box (better trees), 2 = parallel
                                    locally-ordered clustering on the merged-box area (fast rebuilds) */
-    uint32_t reserved[1];
+    /* BLAS layout the traversal reads: 0 = the reference's binary tree, child
+     * pairs of 32-byte nodes (bvh_node_t) walked in the reference's order;
+     * 1 = the same tree collapsed to 4-wide 64-byte nodes with child boxes
+     * quantized to 8 bits per plane (conservatively: each contains its exact
+     * box), half the dependent steps per ray.  With 1, closest hits follow an
+     * order-independent tie rule (smallest t, then smallest (instance,
+     * primitive)) instead of "the first of equal-t hits visited": hits differ
+     * from layout 0 only on exact-t ties.  The megakernel, the fused trace
+     * schedule's shadow rays and the batched pipeline read the binary nodes
+     * (kept in both layouts). */
+    uint32_t blas_layout;
 } wf_init_params;
 
 /* bvh_builder_t::build_options_t (bvh_builder.h:13-17) plus max_leaf_prims:
@@ -96,7 +106,20 @@ enum wf_texture_format {
     WF_TEXTURE_RGBA8 = 0,
     WF_TEXTURE_RGBA8_SRGB = 1,
     WF_TEXTURE_RG8 = 2,
-    WF_TEXTURE_RGBA32F = 3
+    WF_TEXTURE_RGBA32F = 3,
+    /* block-compressed (the reference's TEXTURE_FORMAT_BC*, dds.h:125-147):
+     * data = the 4x4 blocks as a DDS file stores them, decoded on the GPU;
+     * BC7 is recognised (wf_image_decode) but not decoded (WF_ERR_INVALID) */
+    WF_TEXTURE_BC1 = 4,
+    WF_TEXTURE_BC1_SRGB = 5,
+    WF_TEXTURE_BC2 = 6,
+    WF_TEXTURE_BC2_SRGB = 7,
+    WF_TEXTURE_BC3 = 8,
+    WF_TEXTURE_BC3_SRGB = 9,
+    WF_TEXTURE_BC4 = 10,
+    WF_TEXTURE_BC5 = 11,
+    WF_TEXTURE_BC7 = 12,
+    WF_TEXTURE_BC7_SRGB = 13
 };
 
 /* Options of one wf_render call beyond render_settings_t. */
@@ -373,6 +396,28 @@ int wf_bvh_build(wf_ctx* ctx, const triangle_t* triangles, uint32_t triangle_cou
  * 32768 instances (16-bit child indices). */
 int wf_tlas_build(wf_ctx* ctx, const bvh_instance_t* instances, uint32_t instance_count,
                   void* out_blob, uint64_t* inout_size);
+/* The quantized 4-wide nodes (blas_layout 1) of a BLAS blob, built on the
+ * host: 64 bytes per node (4 x float4: {origin xyz, biased exponents and child
+ * count}, {lo planes x/y/z, leaf counts low bytes}, {hi planes, leaf counts
+ * high bytes}, {child: node index, or first triangle of a leaf}) into
+ * out_nodes (NULL = size query through *inout_size); *out_root_count = the
+ * triangles of a BLAS that is a single leaf (then no nodes), else 0.  No
+ * counterpart in the reference (its BLAS is binary). */
+int wf_bvh_quantize(const void* blob, uint64_t blob_size, void* out_nodes, uint64_t* inout_size,
+                    uint32_t* out_root_count);
+
+/* ---- image files (asset_loader.cpp:56-206) -----------------------------
+ * Decodes a .jpg / .jpeg (baseline or progressive; the reference calls
+ * stbi_load with 4 channels, asset_loader.cpp:109), a Radiance .hdr (stbi_loadf
+ * with 4 channels, :150) or a .dds (its top mip level, :179-206) held in
+ * memory: *out_format = WF_TEXTURE_RGBA8 (JPEG), WF_TEXTURE_RGBA32F (HDR) or
+ * the DDS file's format (RGBA8 / RGBA8_SRGB / RG8 / RGBA32F texels, BC1-BC5 /
+ * BC7 blocks as stored); out receives what wf_texture_create takes with that
+ * format (NULL = size query through *inout_size).  Host only. */
+int wf_image_decode(const void* file, uint64_t file_size, uint32_t* out_width, uint32_t* out_height,
+                    uint32_t* out_format, void* out, uint64_t* inout_size);
+/* Reads a texture's RGBA float texels back (width * height * 4 floats). */
+int wf_texture_read(wf_ctx* ctx, uint32_t texture, float* out, uint64_t float_count);
 
 /* ---- allocation-free TLAS build (no counterpart in the reference) --------
  * For callers that cannot allocate device memory: per-frame render threads

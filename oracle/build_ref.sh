@@ -5,6 +5,7 @@
 #   libref_bvh.so    the reference's BLAS / TLAS builders (bvh_builder.cpp,
 #                    tlas_builder.cpp) with a malloc-backed arena header
 #   libref_assets.so oracle/ref_assets.c on the reference's vendored cgltf / ufbx
+#   libref_stb.so    oracle/ref_stb.c on the reference's vendored stb_image
 #   libref_hlsl.so   the reference's traversal, intersection, sampling and
 #                    shade-stage HLSL, rewritten by ref_hlsl/hlsl_to_cpp.py into
 #                    oracle/_ref/hlsl/ and compiled with ref_hlsl/hlsl_shim.h
@@ -34,6 +35,13 @@ if [ -f "$REF/extern/ufbx/ufbx.c" ] && [ -f "$REF/extern/cgltf/cgltf.h" ]; then
   gcc -std=gnu11 -O1 -fPIC -shared -w -I "$REF/extern" \
     -o "$OUT/libref_assets.so" "$HERE/ref_assets.c" "$REF/extern/ufbx/ufbx.c" -lm
   echo "built $OUT/libref_assets.so"
+fi
+# The reference's image decoder (extern/stb/stb_image.h, vendored): pins the
+# library's JPEG and Radiance HDR decoders.
+if [ -f "$REF/extern/stb/stb_image.h" ]; then
+  gcc -std=gnu11 -O2 -fPIC -shared -w -I "$REF/extern" \
+    -o "$OUT/libref_stb.so" "$HERE/ref_stb.c" -lm
+  echo "built $OUT/libref_stb.so"
 fi
 # The reference's compute shaders as C++: pins oracle/orc_impl.h (traversal and
 # shading).  -ffp-contract=off keeps every float operation rounding as written

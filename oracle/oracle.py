@@ -118,6 +118,7 @@ def lib():
         L.orc_int_to_color.argtypes = [u32, vp]
         L.orc_tex_sample.argtypes = [ctypes.POINTER(_Texture), ctypes.c_float, ctypes.c_float, vp]
         L.orc_env_texel.argtypes = [ctypes.POINTER(_Texture), vp, vp]
+        L.orc_decode_bc.argtypes = [u32, vp, u32, u32, vp]
         _lib = L
     return _lib
 
@@ -333,6 +334,15 @@ def eval_bsdf(bsdf, base, alpha, n, v, wl, cosine=1):
     L_.orc_eval_bsdf_batch(bsdf, ptr(d(base)), float(alpha), ptr(d(n)), ptr(d(v)), ptr(wl), m, int(cosine), ptr(f),
                            ptr(pdf), ptr(ok))
     return f, pdf, ok
+
+
+def decode_bc(fmt, blocks, w, h):
+    """BC1-BC5 blocks -> h x w x 4 uint8 (the checker of the GPU block decoder)."""
+    out = np.zeros((h, w, 4), np.uint8)
+    blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+    if lib().orc_decode_bc(fmt, ptr(blocks), w, h, ptr(out)) != 0:
+        raise ValueError("oracle: unknown block format")
+    return out
 
 
 def hemisphere_sample(n, r1, r2, cosine):

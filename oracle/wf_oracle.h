@@ -169,6 +169,11 @@ void orc_sample_bsdf_batch(int f64, uint32_t bsdf, const double base[3], double 
 void orc_eval_bsdf_batch(uint32_t bsdf, const double base[3], double alpha, const double n[3], const double v[3],
                          const double* wl, uint32_t m, int cosine, double* f, double* pdf, int* ok);
 
+/* --- block-compressed textures (orc_bc.c) ----------------------------------- */
+/* BC1-BC5 blocks (format = the library's WF_TEXTURE_BC* value) -> RGBA8;
+ * returns 0, or -1 for another format. */
+int orc_decode_bc(uint32_t format, const uint8_t* blocks, uint32_t w, uint32_t h, uint8_t* rgba);
+
 /* --- small helpers exported for known-answer tests --------------------------- */
 uint32_t orc_wang_hash(uint32_t seed);
 float orc_rand_float(uint32_t* seed);

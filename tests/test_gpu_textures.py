@@ -190,3 +190,61 @@ def test_batch_with_textures_equals_single_render(orc):
         b.render(max_bounces=st["max_bounces"], frame_seed=3, nee=1, rr_start_depth=2)
         assert_same(b.read_image(0), single, "batch")
         b.close()
+
+
+# ------------------------------------------------- block-compressed textures
+
+def srgb_lut():
+    k = np.arange(256) / 255.0
+    return np.where(k <= 0.04045, k / 12.92, ((k + 0.055) / 1.055) ** 2.4).astype(np.float32)
+
+
+def to_float(rgba8, srgb):
+    """wf_texture_create's 8-bit conversion: c / 255 (or the sRGB curve) for
+    colour, c / 255 for alpha."""
+    lin = np.arange(256, dtype=np.float32) / np.float32(255.0)
+    col = (srgb_lut() if srgb else lin)[rgba8[..., :3]]
+    return np.concatenate([col, lin[rgba8[..., 3:]]], axis=-1)
+
+
+@pytest.mark.parametrize("fmt", [abi.TEXTURE_BC1, abi.TEXTURE_BC1_SRGB, abi.TEXTURE_BC2, abi.TEXTURE_BC2_SRGB,
+                                 abi.TEXTURE_BC3, abi.TEXTURE_BC3_SRGB, abi.TEXTURE_BC4, abi.TEXTURE_BC5])
+def test_block_compressed_textures_decode_like_the_oracle(orc, fmt):
+    """Random BC blocks of a 13 x 9 image (partial edge blocks), expanded on
+    the GPU by wf_texture_create, read back: the oracle's decode, converted
+    to float as the library converts 8-bit texels, bit for bit."""
+    w, h = 13, 9
+    small = fmt in (abi.TEXTURE_BC1, abi.TEXTURE_BC1_SRGB, abi.TEXTURE_BC4)
+    rng = np.random.default_rng(fmt)
+    blocks = rng.integers(0, 256, ((w + 3) // 4) * ((h + 3) // 4) * (8 if small else 16), dtype=np.uint8)
+    with Renderer(8, 8) as r:
+        tid = r.create_texture_raw(blocks, w, h, fmt)
+        got = r.read_texture(tid)
+    srgb = fmt in (abi.TEXTURE_BC1_SRGB, abi.TEXTURE_BC2_SRGB, abi.TEXTURE_BC3_SRGB)
+    want = to_float(orc.decode_bc(fmt, blocks, w, h), srgb)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_bc7_is_refused():
+    from wavefrontpathtracing_gb300 import WFError
+    with Renderer(8, 8) as r:
+        with pytest.raises(WFError):
+            r.create_texture_raw(np.zeros(16, np.uint8), 4, 4, abi.TEXTURE_BC7)
+
+
+def test_texture_files_load_as_the_reference_loads_them(orc, tmp_path):
+    """load_texture_file: a DDS of BC1 blocks (sRGB, as base colours load) and a
+    Radiance HDR file (float texels as stored) written here."""
+    from tests.test_image_decode import dds_header, random_rgbe, write_hdr
+    w, h = 10, 6
+    blocks = np.random.default_rng(8).integers(0, 256, 3 * 2 * 8, dtype=np.uint8)
+    (tmp_path / "t.dds").write_bytes(dds_header(w, h, fourcc=b"DXT1") + blocks.tobytes())
+    px = random_rgbe(5, 12, 9)
+    (tmp_path / "t.hdr").write_bytes(write_hdr(px))
+    with Renderer(8, 8) as r:
+        a = r.read_texture(r.load_texture_file(str(tmp_path / "t.dds"), srgb=True))
+        b = r.read_texture(r.load_texture_file(str(tmp_path / "t.hdr")))
+    assert np.array_equal(a.view(np.uint32), to_float(orc.decode_bc(abi.TEXTURE_BC1, blocks, w, h), True).view(np.uint32))
+    import wavefrontpathtracing_gb300 as wf
+    want, _, _, _ = wf.decode_image(write_hdr(px))
+    assert np.array_equal(b.view(np.uint32), want.view(np.uint32))

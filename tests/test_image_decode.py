@@ -1,0 +1,238 @@
+"""CPU: the library's image decoders (wf_image_decode, csrc/wf_image.cu) for the
+files the reference's asset loader reads (asset_loader.cpp:56-206).
+
+  Radiance .hdr   bit for bit against the reference's stb_image (stbi_loadf,
+                  oracle/_ref/libref_stb.so) on files written here, flat and
+                  run-length scanlines;
+  JPEG            against stb_image (stbi_load) on the reference's own
+                  textures (baseline 4:4:4 and 4:2:0, progressive) where the
+                  checkout is present: within 3 of 255 per sample (both are
+                  exact decoders up to their IDCT and colour-conversion
+                  rounding: stb's are fixed point, ours double);
+  DDS             the headers of the reference's own .dds files (all BC1) and
+                  of files written here, the blocks returned as stored;
+  BC1-BC5         the oracle's block decoder (the GPU decoder's checker) on
+                  the formats' known answers.
+"""
+import ctypes
+import glob
+import os
+import struct
+
+import numpy as np
+import pytest
+
+import wavefrontpathtracing_gb300 as wf
+from wavefrontpathtracing_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+STB = os.path.join(ROOT, "oracle", "_ref", "libref_stb.so")
+REF = os.environ.get("WF_REFERENCE_ROOT") or os.path.join(os.path.dirname(ROOT), "reference")
+need_stb = pytest.mark.skipif(not os.path.exists(STB), reason="oracle/_ref/libref_stb.so not built")
+
+
+def stb():
+    S = ctypes.CDLL(STB)
+    for fn, rt in (("ref_stb_load_rgba8", ctypes.c_void_p), ("ref_stb_load_rgbaf", ctypes.c_void_p)):
+        getattr(S, fn).restype = rt
+        getattr(S, fn).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                   ctypes.POINTER(ctypes.c_int)]
+    S.ref_stb_free.argtypes = [ctypes.c_void_p]
+    return S
+
+
+def stb_decode(data, floats):
+    S = stb()
+    buf = np.frombuffer(data, np.uint8)
+    w, h = ctypes.c_int(), ctypes.c_int()
+    fn = S.ref_stb_load_rgbaf if floats else S.ref_stb_load_rgba8
+    p = fn(buf.ctypes.data, len(data), ctypes.byref(w), ctypes.byref(h))
+    assert p, "stb_image failed"
+    n = w.value * h.value * 4
+    out = np.frombuffer(ctypes.string_at(p, n * (4 if floats else 1)), np.float32 if floats else np.uint8).copy()
+    S.ref_stb_free(p)
+    return out.reshape(h.value, w.value, 4)
+
+
+# ------------------------------------------------------------------- HDR
+
+def write_hdr(rgbe, rle=True):
+    """A Radiance file of RGBE pixels (h x w x 4 uint8); scanlines in the
+    2-2-width run-length form (runs where bytes repeat) or flat."""
+    h, w, _ = rgbe.shape
+    out = bytearray(b"#?RADIANCE\n# test\nFORMAT=32-bit_rle_rgbe\nEXPOSURE=1.0\n\n" + f"-Y {h} +X {w}\n".encode())
+    for y in range(h):
+        row = rgbe[y]
+        if not rle:
+            out += row.tobytes()
+            continue
+        out += bytes([2, 2, w >> 8, w & 255])
+        for c in range(4):
+            v = row[:, c]
+            x = 0
+            while x < w:
+                run = 1
+                while x + run < w and run < 127 and v[x + run] == v[x]:
+                    run += 1
+                if run >= 3:
+                    out += bytes([128 + run, v[x]])
+                    x += run
+                else:
+                    lit = []
+                    while x < w and len(lit) < 128:
+                        if x + 2 < w and v[x] == v[x + 1] == v[x + 2]:
+                            break
+                        lit.append(v[x])
+                        x += 1
+                    out += bytes([len(lit)]) + bytes(lit)
+    return bytes(out)
+
+
+def random_rgbe(h, w, seed):
+    rng = np.random.default_rng(seed)
+    px = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+    px[..., 3] = rng.integers(100, 160, (h, w), dtype=np.uint8)
+    px[:, ::5] = px[:, :1]                       # runs
+    px[2, 3, 3] = 0                               # a zero exponent
+    return px
+
+
+@need_stb
+@pytest.mark.parametrize("rle", [True, False])
+def test_hdr_equals_stb_bit_for_bit(rle):
+    px = random_rgbe(37, 61 if rle else 5, 3)
+    data = write_hdr(px, rle)
+    ours, w, h, fmt = wf.decode_image(data)
+    assert fmt == abi.TEXTURE_RGBA32F and (w, h) == (px.shape[1], px.shape[0])
+    want = stb_decode(data, True)
+    assert np.array_equal(ours.view(np.uint32), want.view(np.uint32))
+
+
+def test_hdr_known_answers():
+    px = np.array([[[128, 64, 32, 129], [255, 0, 1, 136], [9, 9, 9, 0]]], np.uint8)
+    ours, w, h, fmt = wf.decode_image(write_hdr(px, rle=False))
+    # mantissa * 2^(e - 136), alpha 1; exponent 0 reads as black
+    want = np.array([[[1.0, 0.5, 0.25, 1.0], [255.0, 0.0, 1.0, 1.0], [0.0, 0.0, 0.0, 1.0]]], np.float32)
+    assert np.array_equal(ours, want)
+
+
+def test_rejects_unknown_and_truncated_files():
+    for data in (b"GIF89a....", b"#?RADIANCE\nFORMAT=32-bit_rle_xyze\n\n-Y 1 +X 1\n\0\0\0\0",
+                 write_hdr(random_rgbe(4, 16, 1))[:-10], b"\xff\xd8\xff\xc0\x00\x11\x08", b"DDS \x7c\x00\x00\x00"):
+        with pytest.raises(wf.WFError):
+            wf.decode_image(data)
+
+
+# ------------------------------------------------------------------- JPEG
+
+def reference_jpegs():
+    files = sorted(glob.glob(os.path.join(REF, "assets", "**", "*.jpg"), recursive=True))
+    kinds = {}
+    for f in files:
+        b = open(f, "rb").read(4096)
+        i = 2
+        while i + 4 < len(b) and b[i] == 0xFF:
+            m, L = b[i + 1], struct.unpack(">H", b[i + 2:i + 4])[0]
+            if m in (0xC0, 0xC1, 0xC2):
+                kinds.setdefault((m, b[i + 11]), []).append(f)
+                break
+            i += 2 + L
+    # every coding / sampling kind the reference's textures use, two files of each
+    return [f for group in kinds.values() for f in group[:2]]
+
+
+@need_stb
+@pytest.mark.skipif(not reference_jpegs(), reason="the reference checkout's textures are not present")
+def test_jpeg_matches_stb_on_the_reference_textures():
+    files = reference_jpegs()
+    assert len(files) >= 4
+    for f in files:
+        data = open(f, "rb").read()
+        ours, w, h, fmt = wf.decode_image(data)
+        want = stb_decode(data, False)
+        assert fmt == abi.TEXTURE_RGBA8 and ours.shape == want.shape
+        d = np.abs(ours.astype(np.int16) - want.astype(np.int16))
+        assert d.max() <= 3 and d.mean() < 0.1 and (d > 2).mean() < 1e-3, (f, d.max(), d.mean())
+        assert np.all(ours[..., 3] == 255)
+
+
+# ------------------------------------------------------------------- DDS
+
+def dds_header(w, h, fourcc=None, dxgi=None, rgba8=False):
+    pf = bytearray(32)
+    struct.pack_into("<I", pf, 0, 32)
+    if fourcc or dxgi is not None:
+        struct.pack_into("<I4s", pf, 4, 4, b"DX10" if dxgi is not None else fourcc)
+    elif rgba8:
+        struct.pack_into("<IIIIIII", pf, 4, 0x41, 0, 32, 0xFF, 0xFF00, 0xFF0000, 0xFF000000)
+    hdr = bytearray(124)
+    struct.pack_into("<IIIII", hdr, 0, 124, 0x1007, h, w, 0)
+    hdr[72:104] = pf
+    out = b"DDS " + bytes(hdr)
+    if dxgi is not None:
+        out += struct.pack("<IIIII", dxgi, 3, 0, 1, 0)
+    return out
+
+
+@pytest.mark.parametrize("kind,fmt,bpb", [("DXT1", abi.TEXTURE_BC1, 8), ("DXT5", abi.TEXTURE_BC3, 16),
+                                          (77, abi.TEXTURE_BC3, 16), (83, abi.TEXTURE_BC5, 16),
+                                          (98, abi.TEXTURE_BC7, 16), ("ATI1", abi.TEXTURE_BC4, 8)])
+def test_dds_blocks_returned_as_stored(kind, fmt, bpb):
+    w, h = 13, 9
+    blocks = np.random.default_rng(2).integers(0, 256, ((w + 3) // 4) * ((h + 3) // 4) * bpb, dtype=np.uint8)
+    head = dds_header(w, h, dxgi=kind) if isinstance(kind, int) else dds_header(w, h, fourcc=kind.encode())
+    out, ow, oh, of = wf.decode_image(head + blocks.tobytes() + b"mips")
+    assert (ow, oh, of) == (w, h, fmt) and np.array_equal(out, blocks)
+
+
+def test_dds_uncompressed_rgba8():
+    px = np.random.default_rng(3).integers(0, 256, (5, 7, 4), dtype=np.uint8)
+    out, w, h, f = wf.decode_image(dds_header(7, 5, rgba8=True) + px.tobytes())
+    assert (w, h, f) == (7, 5, abi.TEXTURE_RGBA8) and np.array_equal(out, px)
+
+
+@pytest.mark.skipif(not glob.glob(os.path.join(REF, "assets", "**", "*.dds"), recursive=True),
+                    reason="the reference checkout's textures are not present")
+def test_reference_dds_files_parse():
+    files = sorted(glob.glob(os.path.join(REF, "assets", "**", "*.dds"), recursive=True))
+    for f in files[:40]:
+        data = open(f, "rb").read()
+        out, w, h, fmt = wf.decode_image(data)
+        hh, ww = struct.unpack("<II", data[12:20])
+        assert (w, h) == (ww, hh) and fmt == abi.TEXTURE_BC1
+        assert out.nbytes == ((w + 3) // 4) * ((h + 3) // 4) * 8
+        assert out.tobytes() == data[128:128 + out.nbytes]
+
+
+# ------------------------------------------------------- BC known answers
+
+def bc1_block(c0, c1, idx):
+    return np.frombuffer(struct.pack("<HHI", c0, c1, idx), np.uint8)
+
+
+def test_bc1_known_answers(orc):
+    red, blue = 0xF800, 0x001F
+    # four-colour mode (c0 > c1): endpoints and the thirds, indices 0,1,2,3 repeating
+    idx = sum(((t & 3) << (2 * t)) for t in range(16))
+    px = orc.decode_bc(abi.TEXTURE_BC1, bc1_block(red, blue, idx), 4, 4).reshape(16, 4)
+    assert px[0].tolist() == [255, 0, 0, 255] and px[1].tolist() == [0, 0, 255, 255]
+    assert px[2].tolist() == [170, 0, 85, 255] and px[3].tolist() == [85, 0, 170, 255]
+    # three-colour mode (c0 <= c1): the midpoint and transparent black
+    px = orc.decode_bc(abi.TEXTURE_BC1, bc1_block(blue, red, idx), 4, 4).reshape(16, 4)
+    assert px[2].tolist() == [128, 0, 128, 255] and px[3].tolist() == [0, 0, 0, 0]
+    # inside BC2 / BC3 the colour block always has four colours
+    b2 = np.concatenate([np.full(8, 0x9F, np.uint8), bc1_block(blue, red, idx)])
+    px = orc.decode_bc(abi.TEXTURE_BC2, b2, 4, 4).reshape(16, 4)
+    assert px[3][:3].tolist() == [170, 0, 85] and px[0][3] == 0xF * 17 and px[1][3] == 9 * 17
+
+
+def test_bc4_known_answers(orc):
+    idx = sum((t & 7) << (3 * t) for t in range(16))
+    blk = np.frombuffer(bytes([200, 60]) + idx.to_bytes(6, "little"), np.uint8)
+    px = orc.decode_bc(abi.TEXTURE_BC4, blk, 4, 4).reshape(16, 4)
+    eight = [200, 60] + [((8 - i) * 200 + (i - 1) * 60 + 3) // 7 for i in range(2, 8)]
+    assert [int(p[0]) for p in px[:8]] == eight and np.all(px[:, 3] == 255) and np.all(px[:, 1:3] == 0)
+    blk = np.frombuffer(bytes([60, 200]) + idx.to_bytes(6, "little"), np.uint8)
+    px = orc.decode_bc(abi.TEXTURE_BC4, blk, 4, 4).reshape(16, 4)
+    six = [60, 200] + [((6 - i) * 60 + (i - 1) * 200 + 2) // 5 for i in range(2, 6)] + [0, 255]
+    assert [int(p[0]) for p in px[:8]] == six

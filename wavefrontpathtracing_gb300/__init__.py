@@ -68,6 +68,9 @@ SIGNATURES = {
     "wf_bvh_build": [_vp, _vp, _u32, _vp, _vp, _pu64],
     "wf_tlas_build": [_vp, _vp, _u32, _vp, _pu64],
     "wf_tlas_build_noalloc": [_vp, _u32, _vp, _u32, _vp],
+    "wf_bvh_quantize": [_vp, _u64, _vp, _pu64, _pu32],
+    "wf_image_decode": [_vp, _u64, _pu32, _pu32, _pu32, _vp, _pu64],
+    "wf_texture_read": [_vp, _u32, _vp, _u64],
     "wf_scene_triangle_count": [_vp, _pu64],
     "wf_scene_set_albedo": [_vp, _vp, _u64],
     "wf_scene_set_emission": [_vp, _u32, ctypes.c_float],
@@ -134,16 +137,55 @@ def _f16(m):
     return a
 
 
+def decode_image(data):
+    """A .jpg / .hdr / .dds file's contents decoded by wf_image_decode (host
+    only): (texels or BC blocks as a uint8 / float32 array, width, height,
+    wf_texture_format)."""
+    L = load()
+    buf = np.frombuffer(bytes(data), dtype=np.uint8)
+    w, h, f = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+    n = ctypes.c_uint64(0)
+    check(L.wf_image_decode(ptr(buf), buf.nbytes, ctypes.byref(w), ctypes.byref(h), ctypes.byref(f), None,
+                            ctypes.byref(n)))
+    out = np.zeros(max(1, n.value), np.uint8)
+    check(L.wf_image_decode(ptr(buf), buf.nbytes, ctypes.byref(w), ctypes.byref(h), ctypes.byref(f), ptr(out),
+                            ctypes.byref(n)))
+    out = out[:n.value]
+    if f.value == abi.TEXTURE_RGBA32F:
+        out = out.view(np.float32).reshape(h.value, w.value, 4)
+    elif f.value in (abi.TEXTURE_RGBA8, abi.TEXTURE_RGBA8_SRGB):
+        out = out.reshape(h.value, w.value, 4)
+    elif f.value == abi.TEXTURE_RG8:
+        out = out.reshape(h.value, w.value, 2)
+    return out, w.value, h.value, f.value
+
+
+def bvh_quantize(blob):
+    """The quantized 4-wide nodes of a BLAS blob (wf_bvh_quantize; host only):
+    (uint32 array of 16 words per node, root leaf triangle count)."""
+    L = load()
+    blob = np.ascontiguousarray(blob, dtype=np.uint8)
+    n = ctypes.c_uint64(0)
+    rc_root = ctypes.c_uint32(0)
+    check(L.wf_bvh_quantize(ptr(blob), blob.nbytes, None, ctypes.byref(n), ctypes.byref(rc_root)))
+    out = np.zeros(max(1, n.value // 4), dtype=np.uint32)
+    check(L.wf_bvh_quantize(ptr(blob), blob.nbytes, ptr(out), ctypes.byref(n), ctypes.byref(rc_root)))
+    return out[:n.value // 4], rc_root.value
+
+
 class Renderer:
     """One wf_ctx: a CUDA device, its stream and all device memory."""
 
-    def __init__(self, width, height, device=0, wave_capacity=0, tlas_metric=0):
+    def __init__(self, width, height, device=0, wave_capacity=0, tlas_metric=0, blas_layout=0):
+        """blas_layout 1: the traversal reads the quantized 4-wide BLAS nodes
+        (with the order-independent tie rule for closest hits)."""
         L = load()
-        p = InitParams(width, height, 1, 0, device, wave_capacity, tlas_metric)
+        p = InitParams(width, height, 1, 0, device, wave_capacity, tlas_metric, blas_layout)
         h = ctypes.c_void_p()
         check(L.wf_create(ctypes.byref(p), ctypes.byref(h)))
         self.h, self.L, self.width, self.height = h, L, width, height
         self._batches = weakref.WeakSet()
+        self._tex_sizes = {}
 
     def close(self):
         if getattr(self, "h", None):
@@ -210,7 +252,48 @@ class Renderer:
                 fmt = abi.TEXTURE_RGBA8
         out = ctypes.c_uint32()
         check(self.L.wf_texture_create(self.h, w, h, fmt, ptr(texels), ctypes.byref(out)))
+        self._tex_sizes[out.value] = (w, h)
         return out.value
+
+    def read_texture(self, texture):
+        """A texture's RGBA float texels (h x w x 4) as the sampler reads them."""
+        w, h = self._texture_size(texture)
+        out = np.zeros((h, w, 4), np.float32)
+        check(self.L.wf_texture_read(self.h, texture, ptr(out), out.size))
+        return out
+
+    def _texture_size(self, texture):
+        return self._tex_sizes[texture]
+
+    def create_texture_raw(self, data, width, height, fmt):
+        """Texels or BC blocks in a wf_texture_format (as wf_image_decode
+        returns them).  Returns the texture id."""
+        data = np.ascontiguousarray(data)
+        out = ctypes.c_uint32()
+        check(self.L.wf_texture_create(self.h, width, height, fmt, ptr(data), ctypes.byref(out)))
+        self._tex_sizes[out.value] = (width, height)
+        return out.value
+
+    def load_texture_file(self, path, srgb=False):
+        """A texture from an image file, as the reference's asset loader takes
+        it (asset_loader.cpp:56-206): .png (gltf.decode_png) / .jpg / .jpeg
+        (RGBA8, or RGBA8_SRGB when srgb), .hdr (RGBA32F), .dds (its format,
+        the sRGB variant of RGBA8 / BC1-BC3 when srgb, dds.h:125-147)."""
+        ext = os.path.splitext(path)[1].lower()
+        data = open(path, "rb").read()
+        if ext == ".png":
+            from .gltf import decode_png
+            img = decode_png(data)
+            return self.create_texture_raw(img, img.shape[1], img.shape[0],
+                                           abi.TEXTURE_RGBA8_SRGB if srgb else abi.TEXTURE_RGBA8)
+        if ext not in (".jpg", ".jpeg", ".hdr", ".dds"):
+            raise ValueError(f"unsupported texture file type: {path}")
+        raw, w, h, fmt = decode_image(data)
+        if srgb:
+            fmt = {abi.TEXTURE_RGBA8: abi.TEXTURE_RGBA8_SRGB, abi.TEXTURE_BC1: abi.TEXTURE_BC1_SRGB,
+                   abi.TEXTURE_BC2: abi.TEXTURE_BC2_SRGB, abi.TEXTURE_BC3: abi.TEXTURE_BC3_SRGB,
+                   abi.TEXTURE_BC7: abi.TEXTURE_BC7_SRGB}.get(fmt, fmt)
+        return self.create_texture_raw(raw, w, h, fmt)
 
     # ---- scene
     def begin_scene(self, view, env=None, env_texture=0):

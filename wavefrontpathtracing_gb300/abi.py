@@ -60,7 +60,7 @@ class InitParams(ctypes.Structure):
     _fields_ = [("render_width", ctypes.c_uint32), ("render_height", ctypes.c_uint32),
                 ("backbuffer_count", ctypes.c_uint32), ("vsync", ctypes.c_uint32),
                 ("device", ctypes.c_int32), ("wave_capacity", ctypes.c_uint32),
-                ("tlas_metric", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 1)]
+                ("tlas_metric", ctypes.c_uint32), ("blas_layout", ctypes.c_uint32)]
 
 
 class BvhOptions(ctypes.Structure):
@@ -73,6 +73,8 @@ class Env(ctypes.Structure):
 
 
 TEXTURE_RGBA8, TEXTURE_RGBA8_SRGB, TEXTURE_RG8, TEXTURE_RGBA32F = 0, 1, 2, 3
+(TEXTURE_BC1, TEXTURE_BC1_SRGB, TEXTURE_BC2, TEXTURE_BC2_SRGB, TEXTURE_BC3, TEXTURE_BC3_SRGB, TEXTURE_BC4,
+ TEXTURE_BC5, TEXTURE_BC7, TEXTURE_BC7_SRGB) = range(4, 14)
 SCHEDULE_SEPARATE, SCHEDULE_FUSED = 0, 1
 
 

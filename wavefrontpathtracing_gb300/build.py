@@ -22,7 +22,7 @@ LIB = os.path.join(LIBDIR, "libwf.so")
 LIB_CHECKED = os.path.join(LIBDIR, "libwf_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["wf_api.cu", "wf_trace.cu", "wf_shade.cu", "wf_tlas.cu", "wf_bvh.cu", "wf_batch.cu", "wf_mega.cu",
-           "wf_sort.cu"]
+           "wf_sort.cu", "wf_qbvh.cu", "wf_texture.cu", "wf_image.cu"]
 
 
 def nvcc():

@@ -91,6 +91,8 @@ struct Mesh {
     float4* d_nodes = nullptr;
     float4* d_tris = nullptr;         // traversal triangles, leaf order
     float4* d_stri = nullptr;         // shading triangles, original order
+    float4* d_qnodes = nullptr;       // quantized 4-wide nodes (blas_layout 1)
+    uint32_t qnode_count = 0, root_count = 0;
 };
 
 struct EventPair {
@@ -110,7 +112,7 @@ const char* const kStageLabel[ST_COUNT] = {"Wavefront Generate", "Wavefront Exte
 struct wf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
-    uint32_t width = 0, height = 0, capacity = 0, tlas_metric = 0;
+    uint32_t width = 0, height = 0, capacity = 0, tlas_metric = 0, blas_layout = 0;
     std::vector<Mesh> meshes;
     std::vector<Instance> instances;
     view_t view{};
@@ -304,6 +306,22 @@ void free_mesh(Mesh& m) {
     dev_free(m.d_nodes);
     dev_free(m.d_tris);
     dev_free(m.d_stri);
+    dev_free(m.d_qnodes);
+}
+
+// The quantized 4-wide nodes of the mesh's BLAS (blas_layout 1), from its blob.
+int upload_qnodes(wf_ctx* c, Mesh& m) {
+    if (c->blas_layout != 1) return WF_OK;
+    std::vector<uint32_t> words;
+    const char* err = nullptr;
+    int rc = qbvh_convert(m.blob.data(), m.blob.size(), words, &m.root_count, &err);
+    if (rc) return fail(rc, err);
+    m.qnode_count = (uint32_t)(words.size() / 16);
+    if (m.qnode_count == 0) return WF_OK;
+    if ((rc = dev_alloc(&m.d_qnodes, 4ull * m.qnode_count))) return rc;
+    WF_CUDA(h2d(c, m.d_qnodes, words.data(), words.size() * 4));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    return WF_OK;
 }
 
 int upload_shading_tris(wf_ctx* c, Mesh& m) {
@@ -410,6 +428,7 @@ SceneRefs scene_refs(wf_ctx* c) {
     S.tnode_count = 2u * S.inst_count;
     S.mesh_count = (uint32_t)c->meshes.size();
     S.status = c->status;
+    S.qbvh = c->blas_layout == 1 ? 1u : 0u;
     return S;
 }
 
@@ -740,6 +759,11 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
         return fail(WF_ERR_INVALID, "wf_create: tlas_metric must be 0, 1 or 2");
     }
     c->tlas_metric = p->tlas_metric;
+    if (p->blas_layout > 1) {
+        delete c;
+        return fail(WF_ERR_INVALID, "wf_create: blas_layout must be 0 or 1");
+    }
+    c->blas_layout = p->blas_layout;
     const uint64_t npix = (uint64_t)c->width * c->height;
     // default: up to 16 samples of every pixel in flight, at most 2^25 paths
     const uint64_t cap = p->wave_capacity ? p->wave_capacity : std::min<uint64_t>(npix * 16, 1ull << 25);
@@ -839,7 +863,7 @@ int wf_mesh_create_prebuilt(wf_ctx* c, const triangle_t* tris, uint32_t n, const
     m.tri_count = n;
     m.tris.assign(tris, tris + n);
     m.blob.assign(static_cast<const uint8_t*>(blob), static_cast<const uint8_t*>(blob) + size);
-    if ((rc = upload_blob(c, m)) || (rc = upload_shading_tris(c, m))) {
+    if ((rc = upload_blob(c, m)) || (rc = upload_shading_tris(c, m)) || (rc = upload_qnodes(c, m))) {
         free_mesh(m);
         return rc;
     }
@@ -880,7 +904,7 @@ int wf_mesh_create(wf_ctx* c, const vertex_t* vertices, uint32_t nv, const uint3
     m.blob = std::move(bo.blob);
     std::memcpy(m.root_min, bo.root_min, 12);
     std::memcpy(m.root_max, bo.root_max, 12);
-    if ((rc = upload_shading_tris(c, m))) {
+    if ((rc = upload_shading_tris(c, m)) || (rc = upload_qnodes(c, m))) {
         free_mesh(m);
         return rc;
     }
@@ -905,36 +929,59 @@ int wf_texture_create(wf_ctx* c, uint32_t w, uint32_t h, uint32_t format, const 
     if (!c || !data || !out) return fail(WF_ERR_INVALID, "wf_texture_create: null argument");
     if (w == 0 || h == 0 || w > 16384 || h > 16384)
         return fail(WF_ERR_INVALID, "wf_texture_create: width and height must be in [1, 16384]");
-    if (format > WF_TEXTURE_RGBA32F) return fail(WF_ERR_INVALID, "wf_texture_create: unknown format");
+    if (format > WF_TEXTURE_BC7_SRGB) return fail(WF_ERR_INVALID, "wf_texture_create: unknown format");
+    if (format == WF_TEXTURE_BC7 || format == WF_TEXTURE_BC7_SRGB)
+        return fail(WF_ERR_INVALID, "wf_texture_create: BC7 blocks are not decoded by this library");
     int rc = use_device(c);
     if (rc) return rc;
     const size_t n = (size_t)w * h;
-    std::vector<float4> tx(n);
-    const uint8_t* b = static_cast<const uint8_t*>(data);
-    if (format == WF_TEXTURE_RGBA32F) {
-        std::memcpy(tx.data(), data, n * sizeof(float4));
-    } else if (format == WF_TEXTURE_RG8) {
-        for (size_t i = 0; i < n; ++i) tx[i] = make_float4(b[2 * i] / 255.0f, b[2 * i + 1] / 255.0f, 0.0f, 1.0f);
-    } else {
-        float lut[256];
-        for (int k = 0; k < 256; ++k) {
-            if (format == WF_TEXTURE_RGBA8_SRGB) {
-                // sRGB transfer function inverse (IEC 61966-2-1), evaluated in double
-                const double v = k / 255.0;
-                lut[k] = (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
-            } else {
-                lut[k] = k / 255.0f;
-            }
+    const bool srgb = format == WF_TEXTURE_RGBA8_SRGB || format == WF_TEXTURE_BC1_SRGB ||
+                      format == WF_TEXTURE_BC2_SRGB || format == WF_TEXTURE_BC3_SRGB;
+    float lut[256];
+    for (int k = 0; k < 256; ++k) {
+        if (srgb) {
+            // sRGB transfer function inverse (IEC 61966-2-1), evaluated in double
+            const double v = k / 255.0;
+            lut[k] = (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
+        } else {
+            lut[k] = k / 255.0f;
         }
-        for (size_t i = 0; i < n; ++i)
-            tx[i] = make_float4(lut[b[4 * i]], lut[b[4 * i + 1]], lut[b[4 * i + 2]], b[4 * i + 3] / 255.0f);
     }
     Texture t;
     t.w = w;
     t.h = h;
     if ((rc = dev_alloc(&t.d, n))) return rc;
-    cudaError_t e = h2d(c, t.d, tx.data(), n * sizeof(float4));
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaError_t e = cudaSuccess;
+    if (format >= WF_TEXTURE_BC1) {
+        // blocks to the device, expanded there (one thread per 4x4 block)
+        const uint64_t bytes = bc_bytes(format, w, h);
+        uint8_t* d_blocks = nullptr;
+        float* d_lut = nullptr;
+        if ((rc = dev_alloc(&d_blocks, bytes)) || (rc = dev_alloc(&d_lut, 256))) {
+            dev_free(d_blocks);
+            dev_free(t.d);
+            return rc;
+        }
+        e = h2d(c, d_blocks, data, bytes);
+        if (e == cudaSuccess) e = h2d(c, d_lut, lut, sizeof(lut));
+        if (e == cudaSuccess) e = launch_decode_bc(d_blocks, format, w, h, d_lut, t.d, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        dev_free(d_blocks);
+        dev_free(d_lut);
+    } else {
+        std::vector<float4> tx(n);
+        const uint8_t* b = static_cast<const uint8_t*>(data);
+        if (format == WF_TEXTURE_RGBA32F) {
+            std::memcpy(tx.data(), data, n * sizeof(float4));
+        } else if (format == WF_TEXTURE_RG8) {
+            for (size_t i = 0; i < n; ++i) tx[i] = make_float4(b[2 * i] / 255.0f, b[2 * i + 1] / 255.0f, 0.0f, 1.0f);
+        } else {
+            for (size_t i = 0; i < n; ++i)
+                tx[i] = make_float4(lut[b[4 * i]], lut[b[4 * i + 1]], lut[b[4 * i + 2]], b[4 * i + 3] / 255.0f);
+        }
+        e = h2d(c, t.d, tx.data(), n * sizeof(float4));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    }
     if (e != cudaSuccess) {
         dev_free(t.d);
         return fail(WF_ERR_CUDA, std::string("wf_texture_create: ") + cudaGetErrorString(e));
@@ -948,6 +995,18 @@ int wf_texture_create(wf_ctx* c, uint32_t w, uint32_t h, uint32_t format, const 
     WF_CUDA(h2d(c, c->tex_table.p, table.data(), table.size() * sizeof(TexRef)));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     *out = (uint32_t)c->textures.size();
+    return WF_OK;
+}
+
+int wf_texture_read(wf_ctx* c, uint32_t id, float* out, uint64_t count) {
+    if (!c || !out || id == 0 || id > c->textures.size()) return fail(WF_ERR_INVALID, "wf_texture_read: bad argument");
+    const Texture& t = c->textures[id - 1];
+    const uint64_t need = 4ull * t.w * t.h;
+    if (count < need) return fail(WF_ERR_CAPACITY, "wf_texture_read: output buffer too small");
+    int rc = use_device(c);
+    if (rc) return rc;
+    WF_CUDA(d2h(c, out, t.d, need * sizeof(float)));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
     return WF_OK;
 }
 
@@ -1027,6 +1086,9 @@ int wf_scene_end(wf_ctx* c) {
             br[i].tris = c->meshes[i].d_tris;
             br[i].node_count = c->meshes[i].node_count;
             br[i].tri_count = c->meshes[i].tri_count;
+            br[i].qnodes = c->meshes[i].d_qnodes;
+            br[i].qnode_count = c->meshes[i].qnode_count;
+            br[i].root_count = c->meshes[i].root_count;
             sp[i] = c->meshes[i].d_stri;
         }
         if ((rc = c->blas.reserve(br.size())) || (rc = c->stri.reserve(sp.size()))) return rc;

@@ -40,6 +40,10 @@ struct BlasRef {
     const float4* nodes;
     const float4* tris;
     uint32_t node_count, tri_count;   // read by checked builds only
+    // the quantized 4-wide layout (wf_init_params.blas_layout = 1; csrc/wf_qbvh.cu):
+    // 4 float4 per node; root_count = the triangles of a BLAS that is one leaf
+    const float4* qnodes = nullptr;
+    uint32_t qnode_count = 0, root_count = 0;
 };
 
 struct SceneRefs {
@@ -49,6 +53,7 @@ struct SceneRefs {
     uint32_t inst_count;
     uint32_t tnode_count, mesh_count;   // checked builds: bounds of the indices above
     uint32_t* status;                   // checked builds: where ERRF_BOUNDS is raised
+    uint32_t qbvh = 0;                  // 1: BLAS traversal over the quantized 4-wide nodes, tie rule
 };
 
 constexpr int kInstRows = 7;   // float4 rows per instance in the shading table
@@ -205,6 +210,21 @@ __device__ __forceinline__ float slab(V3 bmn, V3 bmx, V3 o, V3 inv, float t) {
     return (tmax >= tmin && tmin < t && tmax > 0.0f) ? tmin : FLT_MAX;
 }
 
+// The slab test of the order-independent tie rule (closest-hit rays over the
+// quantized layout): a box entered at exactly the current t is still visited,
+// since it may hold an equal-t hit with a smaller (instance, primitive).
+__device__ __forceinline__ float slab_le(V3 bmn, V3 bmx, V3 o, V3 inv, float t) {
+    float tx1 = (bmn.x - o.x) * inv.x, tx2 = (bmx.x - o.x) * inv.x;
+    float tmin = fminf(tx1, tx2), tmax = fmaxf(tx1, tx2);
+    float ty1 = (bmn.y - o.y) * inv.y, ty2 = (bmx.y - o.y) * inv.y;
+    tmin = fmaxf(tmin, fminf(ty1, ty2));
+    tmax = fminf(tmax, fmaxf(ty1, ty2));
+    float tz1 = (bmn.z - o.z) * inv.z, tz2 = (bmx.z - o.z) * inv.z;
+    tmin = fmaxf(tmin, fminf(tz1, tz2));
+    tmax = fminf(tmax, fmaxf(tz1, tz2));
+    return (tmax >= tmin && tmin <= t && tmax > 0.0f) ? tmin : FLT_MAX;
+}
+
 // intersect_ray_triangle (intersect.hlsl:7-51) on a pre-differenced triangle.
 __device__ __forceinline__ bool tri_hit(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& t_io, float& bu, float& bv,
                                         bool no_cull) {
@@ -220,6 +240,26 @@ __device__ __forceinline__ bool tri_hit(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& 
     if (w < 0.0f || v + w > 1.0f) return false;
     float t = dot(e2, qvec) * inv_det;
     if (t < 0.0f || t >= t_io) return false;
+    t_io = t; bu = v; bv = w;
+    return true;
+}
+
+// The same test under the tie rule: a hit at exactly t_io is taken when
+// tie_wins (its (instance, primitive) is smaller than the current hit's).
+__device__ __forceinline__ bool tri_hit_tie(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float& t_io, float& bu, float& bv,
+                                            bool no_cull, bool tie_wins) {
+    V3 pvec = cross(d, e2);
+    float det = dot(e1, pvec);
+    if (no_cull ? (fabsf(det) < kEps) : (det < kEps)) return false;
+    float inv_det = 1.0f / det;
+    V3 tvec = sub(o, v0);
+    float v = dot(tvec, pvec) * inv_det;
+    if (v < 0.0f || v > 1.0f) return false;
+    V3 qvec = cross(tvec, e1);
+    float w = dot(d, qvec) * inv_det;
+    if (w < 0.0f || v + w > 1.0f) return false;
+    float t = dot(e2, qvec) * inv_det;
+    if (t < 0.0f || t > t_io || (t == t_io && !tie_wins)) return false;
     t_io = t; bu = v; bv = w;
     return true;
 }

@@ -2,6 +2,7 @@
 // and the kernel translation units.  Every wrapper enqueues on `stream` and
 // returns the launch error (cudaGetLastError) without synchronizing.
 #pragma once
+#include <vector>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "wf_device.cuh"
@@ -157,5 +158,15 @@ cudaError_t dmalloc(void** p, size_t bytes);
 void dfree(void* p);
 // Sets the calling thread's wf_last_error() message; returns code.
 int report_error(int code, const char* msg);
+// Block-compressed textures (csrc/wf_texture.cu): bytes of a w x h BC image,
+// and the GPU decode of its blocks into RGBA float texels (lut: the 8-bit to
+// float table of the colour channels).
+uint64_t bc_bytes(uint32_t format, uint32_t w, uint32_t h);
+cudaError_t launch_decode_bc(const uint8_t* d_blocks, uint32_t format, uint32_t w, uint32_t h, const float* d_lut,
+                             float4* d_out, cudaStream_t stream);
+// The quantized 4-wide nodes of a BLAS blob (csrc/wf_qbvh.cu): 16 words per
+// node; *root_count = the triangles of a single-leaf BLAS (no nodes), else 0.
+int qbvh_convert(const uint8_t* blob, uint64_t size, std::vector<uint32_t>& out, uint32_t* root_count,
+                 const char** error);
 
 }  // namespace wf

@@ -104,7 +104,8 @@ struct PairIO {
     }
 };
 
-__global__ void __launch_bounds__(kTraceBlock, WF_TRACE_MIN_BLOCKS)
+template <bool QB>
+__global__ void __launch_bounds__(kTraceBlock, QB ? WF_TRACE_QB_MIN_BLOCKS : WF_TRACE_MIN_BLOCKS)
     k_trace_pair(SceneRefs S, PairIO io, const uint32_t* n_shadow, const uint32_t* n_extend, uint32_t* fetch,
                  uint32_t* status, unsigned long long* totals) {
     io.n_first = *n_shadow;
@@ -115,15 +116,22 @@ __global__ void __launch_bounds__(kTraceBlock, WF_TRACE_MIN_BLOCKS)
     }
     LocalCounters c = {0, 0, 0, 0};
     bool overflow = false;
-    trace_persistent<false, false>(S, io, io.n_first + ne, fetch, c, overflow);
+    trace_persistent<false, false, QB>(S, io, io.n_first + ne, fetch, c, overflow);
     if (overflow) atomicOr(status, ERRF_STACK);
 }
 
+// The traversal kernel for the scene's BLAS layout (binary child pairs, or
+// the quantized 4-wide nodes with the tie rule).
 template <bool ANY, bool COUNT, class IO>
 cudaError_t launch(const SceneRefs& S, const IO& io, const uint32_t* count_ptr, uint32_t count, uint32_t* fetch,
                    uint32_t* status, Counters* counters, unsigned long long* total, cudaStream_t stream) {
-    auto k = k_trace<ANY, COUNT, IO>;
-    k<<<persistent_grid(k), kTraceBlock, 0, stream>>>(S, io, count_ptr, count, fetch, status, counters, total);
+    if (S.qbvh) {
+        auto k = k_trace<ANY, COUNT, true, IO>;
+        k<<<persistent_grid(k), kTraceBlock, 0, stream>>>(S, io, count_ptr, count, fetch, status, counters, total);
+    } else {
+        auto k = k_trace<ANY, COUNT, false, IO>;
+        k<<<persistent_grid(k), kTraceBlock, 0, stream>>>(S, io, count_ptr, count, fetch, status, counters, total);
+    }
     return cudaGetLastError();
 }
 
@@ -207,8 +215,12 @@ cudaError_t launch_trace_pair(const SceneRefs& S, const RenderBuffers& B, uint32
     io.c.cap = io.e.cap = B.capacity; io.c.status = io.e.status = B.status;
     io.n_first = 0;
     uint32_t* fetch = B.counts + 2 * kMaxDepth + depth;
-    k_trace_pair<<<persistent_grid(k_trace_pair), kTraceBlock, 0, stream>>>(
-        S, io, B.counts + kMaxDepth + depth - 1, B.counts + depth, fetch, B.status, totals);
+    if (S.qbvh)
+        k_trace_pair<true><<<persistent_grid(k_trace_pair<true>), kTraceBlock, 0, stream>>>(
+            S, io, B.counts + kMaxDepth + depth - 1, B.counts + depth, fetch, B.status, totals);
+    else
+        k_trace_pair<false><<<persistent_grid(k_trace_pair<false>), kTraceBlock, 0, stream>>>(
+            S, io, B.counts + kMaxDepth + depth - 1, B.counts + depth, fetch, B.status, totals);
     return cudaGetLastError();
 }
 

@@ -96,7 +96,12 @@ struct PermutedAosIO {
     __device__ __forceinline__ void store(uint32_t k, const Hit& h, bool ok) const { io.store(ray(k), h, ok); }
 };
 
-template <bool ANY, bool COUNT, class IO>
+// QB: BLAS levels over the quantized 4-wide nodes (csrc/wf_qbvh.cu); its
+// closest-hit rays use the order-independent tie rule (smallest t, then
+// smallest (instance, primitive); boxes entered at exactly t still visited),
+// so their hits equal the binary traversal's whatever order the wider nodes
+// visit leaves in.  Any-hit rays keep "t < tmax": only whether they hit matters.
+template <bool ANY, bool COUNT, bool QB, class IO>
 __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& io, uint32_t n, uint32_t* fetch,
                                                  LocalCounters& cnt, bool& overflow) {
     const unsigned FULL = 0xffffffffu;
@@ -180,7 +185,8 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                         if (!miss) {
                             const float4 n0 = ldg4(S.tnodes + 2ull * root), n1 = ldg4(S.tnodes + 2ull * root + 1);
                             if (COUNT) cnt.tlas_nodes++;
-                            miss = slab(xyz(n0), xyz(n1), co, ci, ct) == FLT_MAX;
+                            miss = ((QB && !any_ray) ? slab_le(xyz(n0), xyz(n1), co, ci, ct)
+                                                     : slab(xyz(n0), xyz(n1), co, ci, ct)) == FLT_MAX;
                             level = 0; w0 = __float_as_uint(n0.w); w1 = __float_as_uint(n1.w); sp = 0; lo = 0;
                         }
                         if (miss) { io.store(k, hit_record(), true); ri = kNoRay; }
@@ -218,10 +224,16 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
                     cd = xform(cd, 0.0f, c0, c1, c2, c3);
                     ci = rcp(cd);
                     B = S.blas[mesh];
-                    const float4 r0 = ldg4(B.nodes), r1 = ldg4(B.nodes + 1);
-                    if (COUNT) cnt.blas_nodes++;
-                    w0 = __float_as_uint(r0.w);
-                    w1 = __float_as_uint(r1.w);
+                    if (QB) {
+                        // node 0, or the one leaf of a single-leaf BLAS
+                        w0 = 0u;
+                        w1 = B.root_count;
+                    } else {
+                        const float4 r0 = ldg4(B.nodes), r1 = ldg4(B.nodes + 1);
+                        if (COUNT) cnt.blas_nodes++;
+                        w0 = __float_as_uint(r0.w);
+                        w1 = __float_as_uint(r1.w);
+                    }
                     level = 1; tb = sp; hit_here = false;
                 }
             }
@@ -236,7 +248,17 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
             const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
             if (COUNT) cnt.tris++;
             float bu, bv;
-            if (tri_hit(xyz(a), xyz(b), xyz(c), co, cd, ct, bu, bv, no_cull)) {
+            bool accepted;
+            if (QB && !any_ray) {
+                // the current hit: this instance once it has one here, else the outer one
+                const uint32_t bi = hit_here ? ii : s_inst[col];
+                const uint32_t pr = __float_as_uint(a.w);
+                const bool wins = ii < bi || (ii == bi && pr < s_prim[col]);
+                accepted = tri_hit_tie(xyz(a), xyz(b), xyz(c), co, cd, ct, bu, bv, no_cull, wins);
+            } else {
+                accepted = tri_hit(xyz(a), xyz(b), xyz(c), co, cd, ct, bu, bv, no_cull);
+            }
+            if (accepted) {
                 s_prim[col] = __float_as_uint(a.w);
                 s_u[col] = bu; s_v[col] = bv;
                 hit_here = true;
@@ -245,6 +267,64 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
             w0++;
             w1--;
             pop = !finish && w1 == 0u;
+        } else if (QB && level == 1u) {
+            // quantized 4-wide BLAS node: up to four child boxes (origin + q *
+            // 2^e per plane), visited nearest first, the others pushed
+            if (!in_bounds(w0, B.qnode_count, S.status)) {
+                pop = true;
+            } else {
+                const float4* qp = B.qnodes + 4ull * w0;
+                const float4 q0 = ldg4(qp), q1 = ldg4(qp + 1), q2 = ldg4(qp + 2), q3 = ldg4(qp + 3);
+                if (COUNT) cnt.blas_nodes += 2;   // 64 bytes, as a binary child pair
+                const uint32_t meta = __float_as_uint(q0.w);
+                const float sx = __uint_as_float((meta & 0xFFu) << 23);
+                const float sy = __uint_as_float(((meta >> 8) & 0xFFu) << 23);
+                const float sz = __uint_as_float(((meta >> 16) & 0xFFu) << 23);
+                const uint32_t nch = meta >> 24;
+                const uint32_t lx = __float_as_uint(q1.x), ly = __float_as_uint(q1.y), lz = __float_as_uint(q1.z);
+                const uint32_t hx = __float_as_uint(q2.x), hy = __float_as_uint(q2.y), hz = __float_as_uint(q2.z);
+                const uint32_t cl = __float_as_uint(q1.w), chi = __float_as_uint(q2.w);
+                const uint32_t kid[4] = {__float_as_uint(q3.x), __float_as_uint(q3.y), __float_as_uint(q3.z),
+                                         __float_as_uint(q3.w)};
+                const bool tie = !any_ray;
+                float d[4];
+                uint2 e[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const uint32_t sh = 8u * (uint32_t)i;
+                    const V3 bmn = mk(q0.x + (float)((lx >> sh) & 0xFFu) * sx, q0.y + (float)((ly >> sh) & 0xFFu) * sy,
+                                      q0.z + (float)((lz >> sh) & 0xFFu) * sz);
+                    const V3 bmx = mk(q0.x + (float)((hx >> sh) & 0xFFu) * sx, q0.y + (float)((hy >> sh) & 0xFFu) * sy,
+                                      q0.z + (float)((hz >> sh) & 0xFFu) * sz);
+                    const float di = tie ? slab_le(bmn, bmx, co, ci, ct) : slab(bmn, bmx, co, ci, ct);
+                    d[i] = (uint32_t)i < nch ? di : FLT_MAX;
+                    e[i] = make_uint2(kid[i], ((cl >> sh) & 0xFFu) | (((chi >> sh) & 0xFFu) << 8));
+                }
+                // order the four by entry distance (a five-comparator network)
+                auto cswap = [&](int a, int b) {
+                    if (d[a] > d[b]) {
+                        const float td = d[a]; d[a] = d[b]; d[b] = td;
+                        const uint2 te = e[a]; e[a] = e[b]; e[b] = te;
+                    }
+                };
+                cswap(0, 1); cswap(2, 3); cswap(0, 2); cswap(1, 3); cswap(1, 2);
+                if (d[0] == FLT_MAX) {
+                    pop = true;
+                } else {
+                    w0 = e[0].x; w1 = e[0].y;
+#pragma unroll
+                    for (int i = 3; i >= 1; --i) {
+                        if (d[i] != FLT_MAX && !finish) {
+                            if (sp - tb == kStack) {
+                                clear_hit();
+                                finish = true; ok = false; overflow = true;
+                            } else {
+                                stack_push(e[i]);
+                            }
+                        }
+                    }
+                }
+            }
         } else {
             // interior node, TLAS or BLAS: the two children, nearer first
             const float4* pa;
@@ -263,8 +343,9 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
             } else {
                 const float4 a0 = ldg4(pa), a1 = ldg4(pa + 1), b0 = ldg4(pb), b1 = ldg4(pb + 1);
                 if (COUNT) { if (level == 0u) cnt.tlas_nodes += 2; else cnt.blas_nodes += 2; }
-                float dl = slab(xyz(a0), xyz(a1), co, ci, ct);
-                float dr = slab(xyz(b0), xyz(b1), co, ci, ct);
+                const bool tie = QB && !any_ray;
+                float dl = tie ? slab_le(xyz(a0), xyz(a1), co, ci, ct) : slab(xyz(a0), xyz(a1), co, ci, ct);
+                float dr = tie ? slab_le(xyz(b0), xyz(b1), co, ci, ct) : slab(xyz(b0), xyz(b1), co, ci, ct);
                 uint2 L = make_uint2(__float_as_uint(a0.w), __float_as_uint(a1.w));
                 uint2 R = make_uint2(__float_as_uint(b0.w), __float_as_uint(b1.w));
                 if (dl > dr) {
@@ -464,20 +545,25 @@ __device__ __forceinline__ void flush_counters(const LocalCounters& c, Counters*
 #ifndef WF_TRACE_MIN_BLOCKS
 #define WF_TRACE_MIN_BLOCKS 9
 #endif
+// The same for the quantized 4-wide BLAS layout, whose node step holds four
+// child boxes and their sort keys at once.
+#ifndef WF_TRACE_QB_MIN_BLOCKS
+#define WF_TRACE_QB_MIN_BLOCKS 9
+#endif
 int sm_count();
 
 // The traversal kernel: a persistent grid over count rays (read from
 // count_ptr on the device when it is non-null), rays handed out from *fetch.
 // total (optional) accumulates the number of rays of each launch.
-template <bool ANY, bool COUNT, class IO>
-__global__ void __launch_bounds__(kTraceBlock, WF_TRACE_MIN_BLOCKS) k_trace(SceneRefs S, IO io, const uint32_t* count_ptr, uint32_t count,
+template <bool ANY, bool COUNT, bool QB, class IO>
+__global__ void __launch_bounds__(kTraceBlock, QB ? WF_TRACE_QB_MIN_BLOCKS : WF_TRACE_MIN_BLOCKS) k_trace(SceneRefs S, IO io, const uint32_t* count_ptr, uint32_t count,
                                                   uint32_t* fetch, uint32_t* status, Counters* counters,
                                                   unsigned long long* total) {
     const uint32_t n = count_ptr ? *count_ptr : count;
     if (total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(total, (unsigned long long)n);
     LocalCounters c = {0, 0, 0, 0};
     bool overflow = false;
-    trace_persistent<ANY, COUNT>(S, io, n, fetch, c, overflow);
+    trace_persistent<ANY, COUNT, QB>(S, io, n, fetch, c, overflow);
     if (overflow) atomicOr(status, ERRF_STACK);
     if (COUNT) flush_counters(c, counters);
 }
