@@ -186,6 +186,10 @@ def ncu_traffic(rays_per_launch):
     return d.get("dram_bytes_per_launch"), {"file": "profiles/extend_instanced_1080p.json", "commit": d.get("commit")}
 
 
+# Instance world boxes of the main frame (wf_init_params.instance_bounds).
+DEFAULT_INSTANCE_BOUNDS = 1
+
+
 def tlas_reference_leg(local, desc, steps, torch, l2buf):
     """The benchmark frame on the GPU with the reference's TLAS (tlas_metric
     0: its agglomerative walk and pairing metric, tlas_builder.cpp:6-110)
@@ -219,19 +223,12 @@ def build_scene(r, desc):
     return load_scene_into(r, desc)
 
 
-def oracle_scene(desc, tlas_metric):
-    """Oracle scene for the CPU legs, from the oracle's own builders (untimed)."""
+def oracle_scene(desc):
+    """Oracle scene for the CPU legs, from the oracle's own builders with the
+    reference's TLAS metric (untimed)."""
     from oracle import oracle as orc
     from tests.helpers import oracle_scene_from_desc
-    sc = oracle_scene_from_desc(orc, desc)
-    if tlas_metric:
-        # rebuild the TLAS of the same instances with the merged-box walk (1)
-        # or the parallel clustering build (2)
-        from wavefrontpathtracing_gb300.abi import bvh_instance_dtype
-        h = sc._tlas[:8].view(np.uint32)
-        inst = sc._tlas[h[1]:].view(bvh_instance_dtype).copy()
-        sc = orc.Scene(list(zip(sc._tris, sc._blas)), orc.tlas_build(inst, metric=tlas_metric), sc._inst)
-    return sc
+    return oracle_scene_from_desc(orc, desc)
 
 
 CPU_BANDS = 8
@@ -277,7 +274,7 @@ def run_reference(args, rank, world):
         return
     from wavefrontpathtracing_gb300 import scenes
     desc = scenes.instanced_scene(width=W, height=H, spp=SPP, max_bounces=DEPTH)
-    sc = oracle_scene(desc, tlas_metric=0)
+    sc = oracle_scene(desc)
     threads = os.cpu_count() or 1
     per_step = max(3.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
     for i in range(args.warmup):
@@ -524,7 +521,8 @@ def run_ours(args, rank, world, local):
     except Exception:
         torch, l2buf = None, None
     desc = scenes.instanced_scene(width=W, height=H, spp=SPP, max_bounces=DEPTH)
-    r = wf.Renderer(W, H, device=local, tlas_metric=args.tlas_metric, blas_layout=args.blas_layout)
+    r = wf.Renderer(W, H, device=local, tlas_metric=args.tlas_metric, blas_layout=args.blas_layout,
+                    instance_bounds=args.instance_bounds)
     ids = build_scene(r, desc)
 
     def frame(seed, profile):
@@ -646,18 +644,20 @@ def run_ours(args, rank, world, local):
     d2h = (s1["d2h_bytes"] - s0["d2h_bytes"]) // args.steps
     # --- CPU baseline (rank 0 only, N = 1 only): the oracle on a bounded sample
     # with the reference's TLAS (tlas_metric 0), and the same pixels with the
-    # clustering TLAS the GPU line uses (tlas_metric 2)
+    # acceleration structures the GPU line traced (read back from the device)
     cpu, cpu_clustering = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sc = oracle_scene(desc, tlas_metric=0)
+        sc = oracle_scene(desc)
         v, sdesc, _, _, n_px = cpu_sample(sc, desc, args.cpu_seconds, threads, seed=1)
         cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                "sample": sdesc + "; reference TLAS metric"}
-        sc = oracle_scene(desc, tlas_metric=2)
+        from oracle import oracle as orc
+        from tests.helpers import oracle_scene_from_renderer
+        sc, _ = oracle_scene_from_renderer(orc, desc, r, ids)
         v2, sdesc2, _, _, _ = cpu_sample(sc, desc, args.cpu_seconds, threads, seed=1, n=n_px)
         cpu_clustering = {"value": round(v2, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                          "sample": sdesc2 + "; clustering TLAS (as the GPU line)"}
+                          "sample": sdesc2 + "; the GPU line's own TLAS and instance boxes"}
         del sc
     # --- builders: GPU vs the oracle's restatement of the reference's single-threaded C++ builders
     builders = None
@@ -695,6 +695,8 @@ def run_ours(args, rank, world, local):
                            "instanced_triangles": desc.instanced_triangle_count, "instances": len(desc.instances),
                            "tlas_metric": ["reference", "merged-box walk", "parallel clustering"][args.tlas_metric],
                            "blas_layout": ["binary child pairs", "quantized 4-wide"][args.blas_layout],
+                           "instance_bounds": ["transformed BLAS root box",
+                                               "BLAS frontier boxes (tight)"][args.instance_bounds],
                            "l2": "256 MiB buffer written between timed frames; working set > L2"},
                 "spp_per_s": round(spp_per_s, 3),
                 "rays_per_step": rays // args.steps,
@@ -704,10 +706,12 @@ def run_ours(args, rank, world, local):
                 "tail_depth": int(last["tail_depth"]),
                 "traversal_per_ray": {
                     "extend": {"nodes": round((c["tlas_node_loads"] + c["blas_node_loads"]) / max(1, c["rays_extend"]), 1),
+                               "tlas_nodes": round(c["tlas_node_loads"] / max(1, c["rays_extend"]), 1),
                                "instances": round(c["instance_loads"] / max(1, c["rays_extend"]), 2),
                                "triangles": round(c["triangle_tests"] / max(1, c["rays_extend"]), 2)},
                     "shadow": {"nodes": round((c["shadow_tlas_node_loads"] + c["shadow_blas_node_loads"])
                                               / max(1, c["rays_connect"]), 1),
+                               "tlas_nodes": round(c["shadow_tlas_node_loads"] / max(1, c["rays_connect"]), 1),
                                "instances": round(c["shadow_instance_loads"] / max(1, c["rays_connect"]), 2),
                                "triangles": round(c["shadow_triangle_tests"] / max(1, c["rays_connect"]), 2)}},
                 "queue_sizes": {"extend": [int(x) for x in last["extend_rays_depth"][:DEPTH + 1]],
@@ -908,6 +912,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--instance-bounds", type=int, default=DEFAULT_INSTANCE_BOUNDS, choices=[0, 1],
+                    help="instance world boxes: 0 = the transformed BLAS root box (the reference's), "
+                         "1 = from the BLAS frontier boxes (tight)")
     ap.add_argument("--tlas-metric", type=int, default=2,
                     help="TLAS build: 0 = reference walk and metric, 1 = merged-box walk, 2 = parallel clustering")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

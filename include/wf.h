@@ -65,6 +65,16 @@ typedef struct wf_init_params {
      * schedule's shadow rays and the batched pipeline read the binary nodes
      * (kept in both layouts). */
     uint32_t blas_layout;
+    /* world box of each instance, the TLAS's leaf box: 0 = the world box of
+     * the 8 transformed corners of the BLAS root box (renderer.cpp:1324-1336);
+     * 1 = the union of the world boxes of up to 4096 BLAS frontier boxes (the
+     * interior nodes of largest area opened first), computed on the GPU at
+     * wf_scene_end: nearly the transformed geometry's own box (about half the
+     * area of 0's for rotated rounded meshes), so rays enter fewer TLAS
+     * subtrees and instances that they miss.  The TLAS differs, so hits can
+     * differ only in which of exactly equal-t hits is found first.  The
+     * batched pipeline keeps 0's boxes. */
+    uint32_t instance_bounds;
 } wf_init_params;
 
 /* bvh_builder_t::build_options_t (bvh_builder.h:13-17) plus max_leaf_prims:

@@ -80,3 +80,38 @@ def test_product_does_not_import_the_oracle():
         for f in files:
             if f.endswith((".py", ".cu", ".h", ".cuh")):
                 assert not bad.search(open(os.path.join(root, f)).read()), f
+
+
+def test_ctypes_mirrors_match_the_c_header(tmp_path):
+    """Every ctypes structure of the binding has the size and field offsets
+    that a C compiler gives the include/wf.h declaration it mirrors."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = {"RenderSettings": "render_settings_t", "View": "view_t", "InitParams": "wf_init_params",
+             "BvhOptions": "wf_bvh_options", "Env": "wf_env", "RenderOptions": "wf_render_options",
+             "Stats": "wf_stats", "BatchConfig": "wf_batch_config", "BatchStats": "wf_batch_stats"}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "wf.h"', "int main(void) {"]
+    for py, c in pairs.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (py, c))
+        for name, _ in getattr(abi, py)._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (py, name, c, name))
+    lines.append("return 0; }")
+    src = tmp_path / "sizes.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "sizes"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            k, v = line.rsplit(" ", 1)
+            got[k] = int(v)
+    for py in pairs:
+        cls = getattr(abi, py)
+        assert got[py + " size"] == ctypes.sizeof(cls), py
+        for name, _ in cls._fields_:
+            assert got["%s %s" % (py, name)] == getattr(cls, name).offset, (py, name)

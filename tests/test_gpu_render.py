@@ -18,7 +18,7 @@ from tests.helpers import load_scene_into, oracle_scene_from_renderer
 pytestmark = pytest.mark.gpu
 
 
-def render_both(orc, desc, spp, frame_seed=5, nee=None, rr=None, wave=0, prebuilt=True, threads=8):
+def render_both(orc, desc, spp, frame_seed=5, nee=None, rr=None, wave=0, prebuilt=True, threads=8, **renderer_kw):
     o = desc.bvh_options
     st = desc.settings
     nee = st["nee"] if nee is None else nee
@@ -26,7 +26,7 @@ def render_both(orc, desc, spp, frame_seed=5, nee=None, rr=None, wave=0, prebuil
     w, h = desc.width, desc.height
     blobs = [orc.bvh_build(t, o["interval_count"], False, o["max_leaf_prims"]) for t in desc.meshes] \
         if prebuilt else None
-    with Renderer(w, h, wave_capacity=wave) as r:
+    with Renderer(w, h, wave_capacity=wave, **renderer_kw) as r:
         ids = load_scene_into(r, desc, prebuilt_blobs=blobs)
         sc, _ = oracle_scene_from_renderer(orc, desc, r, ids)
         r.render(max_bounces=st["max_bounces"], spp=spp, frame_seed=frame_seed, nee=nee, rr_start_depth=rr)
@@ -63,11 +63,13 @@ def test_box_scene_waves_smaller_than_the_image(orc):
     assert stats["rays_extend"] == sum(ost["extend_rays"])
 
 
-def test_mixed_materials_nee_rr_bit_exact(orc):
+@pytest.mark.parametrize("renderer_kw", [{}, {"instance_bounds": 1, "tlas_metric": 2}])
+def test_mixed_materials_nee_rr_bit_exact(orc, renderer_kw):
     """Lambert / GGX metal / dielectric, next-event estimation through the
-    connect stage, Russian roulette from depth 3."""
+    connect stage, Russian roulette from depth 3; also with the TLAS built
+    over tight instance boxes (the oracle traverses the same TLAS)."""
     desc = scenes.instanced_scene(width=80, height=60, instances=60, freqs=(8, 12), spp=4, max_bounces=8)
-    img, want, stats, ost, _, _ = render_both(orc, desc, spp=4)
+    img, want, stats, ost, _, _ = render_both(orc, desc, spp=4, **renderer_kw)
     assert img[..., :3].max() > 0.0
     assert_images_equal(img, want)
     assert stats["rays_extend"] == sum(ost["extend_rays"])

@@ -176,11 +176,13 @@ def bvh_quantize(blob):
 class Renderer:
     """One wf_ctx: a CUDA device, its stream and all device memory."""
 
-    def __init__(self, width, height, device=0, wave_capacity=0, tlas_metric=0, blas_layout=0):
+    def __init__(self, width, height, device=0, wave_capacity=0, tlas_metric=0, blas_layout=0, instance_bounds=0):
         """blas_layout 1: the traversal reads the quantized 4-wide BLAS nodes
-        (with the order-independent tie rule for closest hits)."""
+        (with the order-independent tie rule for closest hits).
+        instance_bounds 1: instance world boxes from the BLAS frontier boxes
+        (tighter TLAS leaves) instead of the transformed root box."""
         L = load()
-        p = InitParams(width, height, 1, 0, device, wave_capacity, tlas_metric, blas_layout)
+        p = InitParams(width, height, 1, 0, device, wave_capacity, tlas_metric, blas_layout, instance_bounds)
         h = ctypes.c_void_p()
         check(L.wf_create(ctypes.byref(p), ctypes.byref(h)))
         self.h, self.L, self.width, self.height = h, L, width, height

@@ -60,7 +60,8 @@ class InitParams(ctypes.Structure):
     _fields_ = [("render_width", ctypes.c_uint32), ("render_height", ctypes.c_uint32),
                 ("backbuffer_count", ctypes.c_uint32), ("vsync", ctypes.c_uint32),
                 ("device", ctypes.c_int32), ("wave_capacity", ctypes.c_uint32),
-                ("tlas_metric", ctypes.c_uint32), ("blas_layout", ctypes.c_uint32)]
+                ("tlas_metric", ctypes.c_uint32), ("blas_layout", ctypes.c_uint32),
+                ("instance_bounds", ctypes.c_uint32)]
 
 
 class BvhOptions(ctypes.Structure):

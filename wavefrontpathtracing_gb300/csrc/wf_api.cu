@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <unordered_map>
@@ -83,6 +84,8 @@ struct Texture {
     uint32_t w = 0, h = 0;
 };
 
+constexpr uint32_t kHullBoxes = 4096;   // instance_bounds 1: frontier boxes per BLAS
+
 struct Mesh {
     uint32_t tri_count = 0, node_count = 0;
     std::vector<triangle_t> tris;     // original order (create_render_mesh keeps them too)
@@ -93,6 +96,8 @@ struct Mesh {
     float4* d_stri = nullptr;         // shading triangles, original order
     float4* d_qnodes = nullptr;       // quantized 4-wide nodes (blas_layout 1)
     uint32_t qnode_count = 0, root_count = 0;
+    float4* d_hull = nullptr;         // instance_bounds 1: the BLAS frontier boxes {min, max}
+    uint32_t hull_count = 0;
 };
 
 struct EventPair {
@@ -112,7 +117,7 @@ const char* const kStageLabel[ST_COUNT] = {"Wavefront Generate", "Wavefront Exte
 struct wf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
-    uint32_t width = 0, height = 0, capacity = 0, tlas_metric = 0, blas_layout = 0;
+    uint32_t width = 0, height = 0, capacity = 0, tlas_metric = 0, blas_layout = 0, instance_bounds = 0;
     std::vector<Mesh> meshes;
     std::vector<Instance> instances;
     view_t view{};
@@ -130,6 +135,7 @@ struct wf_ctx {
     DevBuf<const float4*> stri;
     DevBuf<LightTri> lights;
     DevBuf<float> aabbs;
+    DevBuf<HullRef> hulls;                  // instance_bounds 1: per mesh
     DevBuf<uint32_t> tlas_scratch;
     uint32_t light_count = 0;
     float light_total = 0.0f;
@@ -307,6 +313,68 @@ void free_mesh(Mesh& m) {
     dev_free(m.d_tris);
     dev_free(m.d_stri);
     dev_free(m.d_qnodes);
+    dev_free(m.d_hull);
+}
+
+// instance_bounds 1: up to kHullBoxes boxes of the mesh's BLAS that together
+// hold every triangle, the frontier reached from the root by repeatedly
+// opening the interior node of largest surface area (ties: lower node index).
+// An instance's world box is then the union of these boxes' world boxes,
+// much closer to the transformed geometry's own box than the world box of the
+// transformed root box (for a randomly rotated sphere, about half its area).
+int upload_hull(wf_ctx* c, Mesh& m) {
+    if (c->instance_bounds != 1 || m.node_count == 0) return WF_OK;
+    bvh_header_t h;
+    std::memcpy(&h, m.blob.data(), 12);
+    auto node = [&](uint32_t i) {
+        bvh_node_t n;
+        std::memcpy(&n, m.blob.data() + h.nodes_offset + 32ull * i, 32);
+        return n;
+    };
+    auto area = [](const bvh_node_t& n) {
+        const float ex = n.aabb_max[0] - n.aabb_min[0], ey = n.aabb_max[1] - n.aabb_min[1],
+                    ez = n.aabb_max[2] - n.aabb_min[2];
+        return ex * ey + ey * ez + ez * ex;
+    };
+    // max-heap on (area, then lower index): interior nodes still to open
+    auto cmp = [](const std::pair<float, uint32_t>& a, const std::pair<float, uint32_t>& b) {
+        return a.first < b.first || (a.first == b.first && a.second > b.second);
+    };
+    std::vector<std::pair<float, uint32_t>> open;
+    std::vector<uint32_t> done;   // leaves: cannot be opened
+    const bvh_node_t root = node(0);
+    if (root.prim_count > 0) done.push_back(0);
+    else open.push_back({area(root), 0});
+    while (!open.empty() && open.size() + done.size() < kHullBoxes) {
+        std::pop_heap(open.begin(), open.end(), cmp);
+        const uint32_t i = open.back().second;
+        open.pop_back();
+        const uint32_t l = node(i).left_first;
+        if (l + 1 >= m.node_count) return fail(WF_ERR_INVALID, "BLAS child index out of range");
+        for (uint32_t ch = l; ch <= l + 1; ++ch) {
+            const bvh_node_t n = node(ch);
+            if (n.prim_count > 0) {
+                done.push_back(ch);
+            } else {
+                open.push_back({area(n), ch});
+                std::push_heap(open.begin(), open.end(), cmp);
+            }
+        }
+    }
+    for (const auto& e : open) done.push_back(e.second);
+    std::sort(done.begin(), done.end());
+    std::vector<float4> boxes(2 * done.size());
+    for (size_t k = 0; k < done.size(); ++k) {
+        const bvh_node_t n = node(done[k]);
+        boxes[2 * k] = make_float4(n.aabb_min[0], n.aabb_min[1], n.aabb_min[2], 0.0f);
+        boxes[2 * k + 1] = make_float4(n.aabb_max[0], n.aabb_max[1], n.aabb_max[2], 0.0f);
+    }
+    m.hull_count = (uint32_t)done.size();
+    int rc = dev_alloc(&m.d_hull, boxes.size());
+    if (rc) return rc;
+    WF_CUDA(h2d(c, m.d_hull, boxes.data(), boxes.size() * sizeof(float4)));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    return WF_OK;
 }
 
 // The quantized 4-wide nodes of the mesh's BLAS (blas_layout 1), from its blob.
@@ -763,7 +831,12 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
         delete c;
         return fail(WF_ERR_INVALID, "wf_create: blas_layout must be 0 or 1");
     }
+    if (p->instance_bounds > 1) {
+        delete c;
+        return fail(WF_ERR_INVALID, "wf_create: instance_bounds must be 0 or 1");
+    }
     c->blas_layout = p->blas_layout;
+    c->instance_bounds = p->instance_bounds;
     const uint64_t npix = (uint64_t)c->width * c->height;
     // default: up to 16 samples of every pixel in flight, at most 2^25 paths
     const uint64_t cap = p->wave_capacity ? p->wave_capacity : std::min<uint64_t>(npix * 16, 1ull << 25);
@@ -863,7 +936,8 @@ int wf_mesh_create_prebuilt(wf_ctx* c, const triangle_t* tris, uint32_t n, const
     m.tri_count = n;
     m.tris.assign(tris, tris + n);
     m.blob.assign(static_cast<const uint8_t*>(blob), static_cast<const uint8_t*>(blob) + size);
-    if ((rc = upload_blob(c, m)) || (rc = upload_shading_tris(c, m)) || (rc = upload_qnodes(c, m))) {
+    if ((rc = upload_blob(c, m)) || (rc = upload_shading_tris(c, m)) || (rc = upload_qnodes(c, m)) ||
+        (rc = upload_hull(c, m))) {
         free_mesh(m);
         return rc;
     }
@@ -904,7 +978,7 @@ int wf_mesh_create(wf_ctx* c, const vertex_t* vertices, uint32_t nv, const uint3
     m.blob = std::move(bo.blob);
     std::memcpy(m.root_min, bo.root_min, 12);
     std::memcpy(m.root_max, bo.root_max, 12);
-    if ((rc = upload_shading_tris(c, m)) || (rc = upload_qnodes(c, m))) {
+    if ((rc = upload_shading_tris(c, m)) || (rc = upload_qnodes(c, m)) || (rc = upload_hull(c, m))) {
         free_mesh(m);
         return rc;
     }
@@ -1111,13 +1185,27 @@ int wf_scene_end(wf_ctx* c) {
         (rc = c->tlas_scratch.reserve(tlas_scratch_words(n, c->tlas_metric))))
         return rc;
     WF_CUDA(cudaMemsetAsync(c->tnodes.p, 0, 32, c->stream));
+    const bool tight = c->instance_bounds == 1 && n > 0;
+    if (tight) {
+        std::vector<HullRef> hr(nm ? nm : 1);
+        for (uint32_t i = 0; i < nm; ++i) hr[i] = HullRef{c->meshes[i].d_hull, c->meshes[i].hull_count, 0u};
+        if ((rc = c->hulls.reserve(hr.size()))) return rc;
+        WF_CUDA(h2d(c, c->hulls.p, hr.data(), hr.size() * sizeof(HullRef)));
+    }
     if (n) {
-        WF_CUDA(h2d(c, c->aabbs.p, aabbs.data(), aabbs.size() * 4));
         WF_CUDA(h2d(c, c->tinst.p, ti.data(), ti.size() * 16));
         WF_CUDA(h2d(c, c->sinst.p, si.data(), si.size() * 16));
         StageTimer st(c, true, ST_TLAS);
+        if (tight) {
+            // the instance boxes from the meshes' frontier boxes, on the device
+            WF_CUDA(launch_instance_bounds(c->sinst.p, kInstRows, n, c->hulls.p, nm, c->aabbs.p, c->stream));
+            c->launches++;
+        } else {
+            WF_CUDA(h2d(c, c->aabbs.p, aabbs.data(), aabbs.size() * 4));
+        }
         WF_CUDA(launch_tlas_build(c->aabbs.p, n, c->tnodes.p, c->tlas_scratch.p, c->tlas_metric, c->stream));
         c->launches++;
+        if (tight) WF_CUDA(d2h(c, aabbs.data(), c->aabbs.p, aabbs.size() * 4));
     }
     // emitter table (every triangle of every emissive instance, world space)
     std::vector<LightTri> lt;
@@ -1133,6 +1221,11 @@ int wf_scene_end(wf_ctx* c) {
     if (!lt.empty())
         WF_CUDA(h2d(c, c->lights.p, lt.data(), lt.size() * sizeof(LightTri)));
     WF_CUDA(cudaStreamSynchronize(c->stream));
+    if (tight)   // the instance records report the boxes the TLAS was built from
+        for (uint32_t i = 0; i < n; ++i) {
+            std::memcpy(c->scene_bi[i].aabb_min, &aabbs[6ull * i], 12);
+            std::memcpy(c->scene_bi[i].aabb_max, &aabbs[6ull * i + 3], 12);
+        }
     c->in_scene = false;
     c->scene_ready = true;
     return WF_OK;

@@ -147,6 +147,17 @@ cudaError_t launch_resolve(const float4* accum, uint32_t npix, float4* out, cuda
 // reference's agglomerative walk), 2 = parallel locally-ordered clustering.
 // scratch: tlas_scratch_words(n, metric) words.
 size_t tlas_scratch_words(uint32_t n, uint32_t metric);
+// instance_bounds 1: a mesh's BLAS frontier boxes ({min, max} float4 pairs).
+struct HullRef {
+    const float4* boxes;
+    uint32_t count;
+    uint32_t pad;
+};
+// World AABBs (6 floats per instance) of n instances from their shading rows
+// (rows float4 per instance; rows 0-3 = the local-to-world columns, the mesh
+// index in row 0's w) and their meshes' frontier boxes.
+cudaError_t launch_instance_bounds(const float4* sinst, uint32_t rows, uint32_t n, const HullRef* hulls,
+                                   uint32_t mesh_count, float* aabbs, cudaStream_t stream);
 cudaError_t launch_tlas_build(const float* aabbs /* 6 floats per instance */, uint32_t n, float4* nodes,
                               uint32_t* scratch, uint32_t metric, cudaStream_t stream);
 

@@ -333,6 +333,58 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restr
     }
 }
 
+// instance_bounds 1: one block per instance.  Each frontier box's world box
+// is its transformed centre +/- its half extents through |M| (the exact box of
+// the transformed box), widened by 2^-19 of the magnitudes of the terms summed
+// so that float rounding cannot shrink it; the instance box is their union.
+// sinst rows 0-3 of an instance hold the columns of its local-to-world matrix
+// (the mesh index in row 0's w).
+constexpr int kBoundsThreads = 256;
+__global__ void __launch_bounds__(kBoundsThreads) k_instance_bounds(const float4* __restrict__ sinst, uint32_t rows,
+                                                                   const HullRef* __restrict__ hulls,
+                                                                   uint32_t mesh_count, float* __restrict__ aabbs) {
+    const uint32_t i = blockIdx.x;
+    const float4* r = sinst + (size_t)rows * i;
+    const float4 m0 = r[0], m1 = r[1], m2 = r[2], m3 = r[3];
+    const uint32_t mesh = __float_as_uint(m0.w);
+    const HullRef H = mesh < mesh_count ? hulls[mesh] : HullRef{nullptr, 0u, 0u};
+    const float col[4][3] = {{m0.x, m0.y, m0.z}, {m1.x, m1.y, m1.z}, {m2.x, m2.y, m2.z}, {m3.x, m3.y, m3.z}};
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t j = threadIdx.x; j < H.count; j += kBoundsThreads) {
+        const float4 mn = H.boxes[2ull * j], mx = H.boxes[2ull * j + 1];
+        const float c[3] = {0.5f * (mn.x + mx.x), 0.5f * (mn.y + mx.y), 0.5f * (mn.z + mx.z)};
+        const float h[3] = {0.5f * (mx.x - mn.x), 0.5f * (mx.y - mn.y), 0.5f * (mx.z - mn.z)};
+        for (int a = 0; a < 3; ++a) {
+            float wc = col[3][a], wh = 0.0f, mag = fabsf(col[3][a]);
+            for (int k = 0; k < 3; ++k) {
+                wc = wc + col[k][a] * c[k];
+                wh = wh + fabsf(col[k][a]) * h[k];
+                mag = mag + fabsf(col[k][a]) * (fabsf(c[k]) + h[k]);
+            }
+            const float pad = mag * 0x1p-19f;
+            lo[a] = fminf(lo[a], wc - wh - pad);
+            hi[a] = fmaxf(hi[a], wc + wh + pad);
+        }
+    }
+    __shared__ float s[kBoundsThreads / 32][6];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (int a = 0; a < 3; ++a) {
+        for (int off = 16; off > 0; off >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], off));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], off));
+        }
+    }
+    if (lane == 0)
+        for (int a = 0; a < 3; ++a) { s[warp][a] = lo[a]; s[warp][3 + a] = hi[a]; }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const bool is_lo = threadIdx.x < 3;
+        float v = s[0][threadIdx.x];
+        for (int w = 1; w < kBoundsThreads / 32; ++w) v = is_lo ? fminf(v, s[w][threadIdx.x]) : fmaxf(v, s[w][threadIdx.x]);
+        aabbs[6ull * i + threadIdx.x] = v;
+    }
+}
+
 uint32_t pow2_at_least(uint32_t n) {
     uint32_t p = 1;
     while (p < n) p <<= 1;
@@ -340,6 +392,13 @@ uint32_t pow2_at_least(uint32_t n) {
 }
 
 }  // namespace
+
+cudaError_t launch_instance_bounds(const float4* sinst, uint32_t rows, uint32_t n, const HullRef* hulls,
+                                   uint32_t mesh_count, float* aabbs, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    k_instance_bounds<<<n, kBoundsThreads, 0, stream>>>(sinst, rows, hulls, mesh_count, aabbs);
+    return cudaGetLastError();
+}
 
 size_t tlas_scratch_words(uint32_t n, uint32_t metric) {
     if (metric == 2) return 2ull * pow2_at_least(n ? n : 1) + 5ull * n + 8;
