@@ -841,9 +841,12 @@ def traversal_runs(local, n_tris, side, steps, warmup, kinds=("coherent", "incoh
                         ms.append(r.stats()["ms_total"])
                     t = float(np.mean(ms))
                     hits = d_hits.cpu().numpy().view(wf.abi.hit_dtype)
-                    t1 = time.perf_counter()
+                    # end to end through wf_trace (host arrays in and out): the mean of 3 calls
                     r.trace(rays, any_hit=any_hit, reorder=reorder)
-                    e2e_s = time.perf_counter() - t1
+                    t1 = time.perf_counter()
+                    for _ in range(3):
+                        r.trace(rays, any_hit=any_hit, reorder=reorder)
+                    e2e_s = (time.perf_counter() - t1) / 3
                     res = {"rays": kind, "query": "any" if any_hit else "closest",
                            "order": "morton" if reorder else "as given", "n": len(rays), "ms": round(t, 3),
                            "mrays_per_s": round(len(rays) / (t / 1e3) / 1e6, 2),
