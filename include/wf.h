@@ -314,9 +314,17 @@ int wf_scene_set_emission(wf_ctx* ctx, uint32_t instance, float strength);
  * 3 floats per pixel (row-major); writes d(loss)/d(albedo) (3 floats per scene
  * triangle) and d(loss)/d(emissive_strength) (1 per instance).  Each wave is
  * traced once forward (path radiance L) and replayed from the same per-path
- * seeds, adding w*L/albedo at every Lambert vertex and w.L/strength at the
- * emitter (w = dloss_dimage / spp) with atomics — memory O(paths), no tape.
- * Requires wf_scene_set_albedo, nee = 0 and Russian roulette off. */
+ * seeds (w = dloss_dimage / spp, atomics, memory O(paths), no tape): a Lambert
+ * vertex adds w*(L - L_before)/albedo, L_before being what the path gathered
+ * before it (everything after it, its next-event shadow ray included, is
+ * linear in its albedo); each emitted contribution c (an emission hit, or an
+ * unoccluded shadow ray with next-event estimation) adds w.c/strength to its
+ * emitter.  Russian roulette's survival probabilities are held constant (the
+ * replay takes the forward pass's decisions): the gradient of the expected
+ * image stays unbiased.  Metal and dielectric base colours are not
+ * differentiated, nor an albedo of exactly 0 (its path carries nothing
+ * further).  Requires wf_scene_set_albedo; the shadow rays are traced in
+ * their own launches whatever trace_schedule says. */
 int wf_adjoint(wf_ctx* ctx, const render_settings_t* settings, const wf_render_options* opts, uint32_t frame_seed,
                const float* dloss_dimage, float* d_albedo, float* d_emission);
 

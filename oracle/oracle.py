@@ -95,6 +95,7 @@ def lib():
                                      vp, i32]
         L.orc_adjoint_f64.argtypes = [ctypes.POINTER(_Scene), ctypes.POINTER(View), ctypes.POINTER(RenderParams), vp,
                                       vp, vp]
+        L.orc_adjoint_f32.argtypes = L.orc_adjoint_f64.argtypes
         L.orc_wang_hash.argtypes = [u32]
         L.orc_wang_hash.restype = u32
         L.orc_rand_float.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
@@ -234,16 +235,20 @@ class Scene:
         self._inst[instance]["material"]["emissive_strength"] = strength
 
     def adjoint(self, view, width, height, dloss_dimage, max_bounces=6, spp=1, frame_seed=1, cosine=1,
-                env_color=(0.0, 0.0, 0.0), env_strength=1.0):
+                env_color=(0.0, 0.0, 0.0), env_strength=1.0, nee=0, rr_start_depth=0xFFFFFFFF, f64=True):
+        """d(loss)/d(albedo) per scene triangle and d(loss)/d(strength) per
+        instance; f64=False traces the paths in single precision (the GPU's
+        paths), the gradient still summed in double."""
         p = RenderParams()
         p.max_bounces, p.cosine_weighted_diffuse, p.hdr_env_strength = max_bounces, cosine, env_strength
         p.env_color[:] = env_color
-        p.spp, p.sample_offset, p.nee, p.rr_start_depth, p.frame_seed = spp, 0, 0, 0xFFFFFFFF, frame_seed
+        p.spp, p.sample_offset, p.nee, p.rr_start_depth, p.frame_seed = spp, 0, nee, rr_start_depth, frame_seed
         d = np.ascontiguousarray(dloss_dimage, dtype=np.float64).reshape(-1)
         assert len(d) == 3 * width * height
         ga = np.zeros(3 * self.triangle_count, dtype=np.float64)
         ge = np.zeros(len(self._inst), dtype=np.float64)
-        rc = lib().orc_adjoint_f64(ctypes.byref(self.c), ctypes.byref(view), ctypes.byref(p), ptr(d), ptr(ga), ptr(ge))
+        fn = lib().orc_adjoint_f64 if f64 else lib().orc_adjoint_f32
+        rc = fn(ctypes.byref(self.c), ctypes.byref(view), ctypes.byref(p), ptr(d), ptr(ga), ptr(ge))
         if rc != 0:
             raise ValueError("oracle adjoint failed")
         return ga.reshape(-1, 3), ge

@@ -320,6 +320,8 @@ typedef struct {
     R area;
     R uv[6];                  /* vertex uv (u0, v0, u1, v1, u2, v2) */
     uint32_t tex;             /* emissive texture id (0 = none) */
+    uint32_t inst;            /* the instance it belongs to (the adjoint's emitter key) */
+    R strength;               /* that instance's emissive strength */
 } FN(light);
 
 typedef struct {
@@ -373,6 +375,8 @@ static void FN(build_lights)(const orc_scene* s, FN(lights)* L) {
             lt->uv[2] = (R)me->tris[t].v1.uv[0]; lt->uv[3] = (R)me->tris[t].v1.uv[1];
             lt->uv[4] = (R)me->tris[t].v2.uv[0]; lt->uv[5] = (R)me->tris[t].v2.uv[1];
             lt->tex = m->emissive_index;
+            lt->inst = i;
+            lt->strength = (R)m->emissive_strength;
             run = run + lt->area;
             L->cdf[k] = run;
             k++;
@@ -553,12 +557,19 @@ typedef struct {
     orc_render_stats st;
 } FN(tstate);
 
+/* What the adjoint needs of one path: every Lambert vertex (its scene
+ * triangle, albedo, and the path radiance gathered before it: the part that
+ * does not depend on that albedo), and every emitted contribution (an
+ * emission hit or an unoccluded shadow ray) with its emitter and strength. */
 typedef struct {
     uint32_t n;
     uint32_t tri[32];       /* scene triangle of each Lambert vertex */
     R rho[32][3];           /* its albedo */
-    uint32_t emitter;       /* instance whose emission ended the path, or WF_INVALID_INDEX */
-    R strength;
+    R before[32][3];        /* path radiance before the vertex */
+    uint32_t ne;
+    uint32_t em_inst[32];   /* emitter instance of each emitted contribution */
+    R em_strength[32];
+    R em_c[32][3];          /* the contribution */
 } FN(record);
 
 /* One camera path of the wavefront loop (generate.hlsl, extend.hlsl,
@@ -567,7 +578,7 @@ typedef struct {
  * them (shade at depth d, then connect at depth d, then depth d+1). */
 static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_render_stats* st,
                      FN(record)* rec) {
-    if (rec) { rec->n = 0; rec->emitter = WF_INVALID_INDEX; rec->strength = K(0.0); }
+    if (rec) { rec->n = 0; rec->ne = 0; }
     const orc_scene* s = J->s;
     const orc_render_params* P = J->p;
     uint32_t px = pixel % J->width, py = pixel / J->width;
@@ -675,7 +686,14 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
             acc[0] = acc[0] + (T.x * le.x) * w;
             acc[1] = acc[1] + (T.y * le.y) * w;
             acc[2] = acc[2] + (T.z * le.z) * w;
-            if (rec) { rec->emitter = h.inst; rec->strength = (R)m->emissive_strength; }
+            if (rec && rec->ne < 32) {
+                rec->em_inst[rec->ne] = h.inst;
+                rec->em_strength[rec->ne] = (R)m->emissive_strength;
+                rec->em_c[rec->ne][0] = (T.x * le.x) * w;
+                rec->em_c[rec->ne][1] = (T.y * le.y) * w;
+                rec->em_c[rec->ne][2] = (T.z * le.z) * w;
+                rec->ne++;
+            }
             return;
         }
         uint32_t seed = orc_path_seed(P->frame_seed, pixel, sample, d);
@@ -698,6 +716,7 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
         if (bsdf == 0 && rec && s->tri_albedo && rec->n < 32) {
             rec->tri[rec->n] = stri;
             rec->rho[rec->n][0] = base.x; rec->rho[rec->n][1] = base.y; rec->rho[rec->n][2] = base.z;
+            rec->before[rec->n][0] = acc[0]; rec->before[rec->n][1] = acc[1]; rec->before[rec->n][2] = acc[2];
             rec->n++;
         }
         FN(scatter) sc_ = FN(sample_bsdf)(bsdf, base, alpha, (R)in->ior, N, tg, bt, rd, pos, r1, r2,
@@ -749,6 +768,14 @@ static void FN(path)(FN(job)* J, uint32_t pixel, uint32_t sample, R acc[3], orc_
                         acc[0] = acc[0] + contrib.x;
                         acc[1] = acc[1] + contrib.y;
                         acc[2] = acc[2] + contrib.z;
+                        if (rec && rec->ne < 32) {
+                            rec->em_inst[rec->ne] = lt->inst;
+                            rec->em_strength[rec->ne] = lt->strength;
+                            rec->em_c[rec->ne][0] = contrib.x;
+                            rec->em_c[rec->ne][1] = contrib.y;
+                            rec->em_c[rec->ne][2] = contrib.z;
+                            rec->ne++;
+                        }
                     }
                 }
             }

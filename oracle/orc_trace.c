@@ -470,33 +470,53 @@ int orc_render_f64(const orc_scene* s, const view_t* view, const orc_render_para
     return run_render(s, view, p, NULL, accum, NULL, threads);
 }
 
+/* The adjoint of one precision: each path traced as path_<R> traces it, the
+ * gradient accumulated in double. */
+#define ORC_ADJOINT_BODY(SUF)                                                                                 \
+    job_##SUF J;                                                                                              \
+    memset(&J, 0, sizeof(J));                                                                                 \
+    J.s = s; J.view = view; J.p = p; J.width = (uint32_t)view->render_dim[0];                                 \
+    build_lights_##SUF(s, &J.lights);                                                                         \
+    const uint32_t npix = J.width * (uint32_t)view->render_dim[1];                                            \
+    const double inv_spp = 1.0 / (double)p->spp;                                                              \
+    orc_render_stats st;                                                                                      \
+    memset(&st, 0, sizeof(st));                                                                               \
+    record_##SUF rec;                                                                                         \
+    for (uint32_t px = 0; px < npix; ++px) {                                                                  \
+        for (uint32_t si = 0; si < p->spp; ++si) {                                                            \
+            R_##SUF L[3] = {0, 0, 0};                                                                         \
+            path_##SUF(&J, px, p->sample_offset + si, L, &st, &rec);                                          \
+            const double w[3] = {dimg[3ull * px] * inv_spp, dimg[3ull * px + 1] * inv_spp,                   \
+                                 dimg[3ull * px + 2] * inv_spp};                                              \
+            /* a Lambert vertex scales everything gathered after it */                                        \
+            for (uint32_t v = 0; v < rec.n; ++v)                                                              \
+                for (int c = 0; c < 3; ++c)                                                                   \
+                    if (rec.rho[v][c] != 0)                                                                   \
+                        g_albedo[3ull * rec.tri[v] + c] +=                                                    \
+                            w[c] * ((double)L[c] - (double)rec.before[v][c]) / (double)rec.rho[v][c];         \
+            /* an emitted contribution is linear in its emitter's strength */                                 \
+            for (uint32_t e = 0; e < rec.ne; ++e)                                                             \
+                if (rec.em_strength[e] != 0)                                                                  \
+                    g_emission[rec.em_inst[e]] += (w[0] * rec.em_c[e][0] + w[1] * rec.em_c[e][1] +            \
+                                                   w[2] * rec.em_c[e][2]) / (double)rec.em_strength[e];       \
+        }                                                                                                     \
+    }                                                                                                         \
+    free(J.lights.tri);                                                                                       \
+    free(J.lights.cdf);
+
+typedef float R_f32;
+typedef double R_f64;
+
 int orc_adjoint_f64(const orc_scene* s, const view_t* view, const orc_render_params* p, const double* dimg,
                     double* g_albedo, double* g_emission) {
-    if (!s || !view || !p || !dimg || !g_albedo || !g_emission || !s->tri_albedo || p->nee ||
-        p->rr_start_depth <= p->max_bounces || p->max_bounces > 15)
-        return -1;
-    job_f64 J;
-    memset(&J, 0, sizeof(J));
-    J.s = s; J.view = view; J.p = p; J.width = (uint32_t)view->render_dim[0];
-    build_lights_f64(s, &J.lights);
-    const uint32_t npix = J.width * (uint32_t)view->render_dim[1];
-    const double inv_spp = 1.0 / (double)p->spp;
-    orc_render_stats st;
-    memset(&st, 0, sizeof(st));
-    record_f64 rec;
-    for (uint32_t px = 0; px < npix; ++px) {
-        for (uint32_t si = 0; si < p->spp; ++si) {
-            double L[3] = {0.0, 0.0, 0.0};
-            path_f64(&J, px, p->sample_offset + si, L, &st, &rec);
-            const double w[3] = {dimg[3ull * px] * inv_spp, dimg[3ull * px + 1] * inv_spp, dimg[3ull * px + 2] * inv_spp};
-            for (uint32_t v = 0; v < rec.n; ++v)
-                for (int c = 0; c < 3; ++c)
-                    if (rec.rho[v][c] != 0.0) g_albedo[3ull * rec.tri[v] + c] += w[c] * L[c] / rec.rho[v][c];
-            if (rec.emitter != WF_INVALID_INDEX && rec.strength != 0.0)
-                g_emission[rec.emitter] += (w[0] * L[0] + w[1] * L[1] + w[2] * L[2]) / rec.strength;
-        }
-    }
-    free(J.lights.tri);
-    free(J.lights.cdf);
+    if (!s || !view || !p || !dimg || !g_albedo || !g_emission || !s->tri_albedo || p->max_bounces > 15) return -1;
+    ORC_ADJOINT_BODY(f64)
+    return 0;
+}
+
+int orc_adjoint_f32(const orc_scene* s, const view_t* view, const orc_render_params* p, const double* dimg,
+                    double* g_albedo, double* g_emission) {
+    if (!s || !view || !p || !dimg || !g_albedo || !g_emission || !s->tri_albedo || p->max_bounces > 15) return -1;
+    ORC_ADJOINT_BODY(f32)
     return 0;
 }

@@ -144,11 +144,20 @@ int orc_render_f64(const orc_scene* s, const view_t* view, const orc_render_para
 /* Path-replay adjoint reference (double precision, single thread): for the
  * paths orc_render_f64 would trace, accumulates d(loss)/d(albedo) per scene
  * triangle (3 per triangle) and d(loss)/d(emissive_strength) per instance,
- * given dloss_dimage = d(loss)/d(average radiance), 3 per pixel.  Every path
- * contribution is a product of Lambert albedos along the path times the
- * emitter's strength, so each contributes L/albedo per vertex and L/strength
- * for its emitter.  Requires nee = 0 and Russian roulette off. */
+ * given dloss_dimage = d(loss)/d(average radiance), 3 per pixel.  Everything a
+ * path gathers after a Lambert vertex (its next-event contribution and the
+ * rest of the path) is linear in that vertex's albedo, so the vertex adds
+ * (L - L_before) / albedo; every emitted contribution (an emission hit or an
+ * unoccluded shadow ray) is linear in its emitter's strength and adds
+ * contribution / strength.  Russian roulette's survival probabilities are
+ * held constant (the replay takes the same decisions), which keeps the
+ * gradient of the expected image unbiased.  Only Lambert albedos are
+ * differentiated (a metal's base colour enters through Fresnel). */
 int orc_adjoint_f64(const orc_scene* s, const view_t* view, const orc_render_params* p, const double* dloss_dimage,
+                    double* d_albedo, double* d_emission);
+/* The same with every path traced in single precision, as orc_render traces
+ * it (the GPU's paths; gradients still summed in double). */
+int orc_adjoint_f32(const orc_scene* s, const view_t* view, const orc_render_params* p, const double* dloss_dimage,
                     double* d_albedo, double* d_emission);
 
 /* --- the scattering models on their own (physics tests) -------------------- */

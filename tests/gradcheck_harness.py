@@ -15,6 +15,7 @@ class RenderImage(torch.autograd.Function):
         r.set_albedo(albedo.detach().cpu().numpy())
         r.set_emission(light_instance, float(strength.detach().cpu().item()))
         r.render(max_bounces=settings["max_bounces"], spp=settings["spp"], frame_seed=settings["frame_seed"],
+                 nee=settings.get("nee", 0), rr_start_depth=settings.get("rr_start_depth", 0xFFFFFFFF),
                  accumulate=False)
         img = r.read_image()[..., :3].astype(np.float64)
         ctx.renderer, ctx.light, ctx.settings = r, light_instance, settings
@@ -24,6 +25,7 @@ class RenderImage(torch.autograd.Function):
     def backward(ctx, grad_image):
         s = ctx.settings
         ga, ge = ctx.renderer.adjoint(grad_image.detach().cpu().numpy().astype(np.float32),
-                                      max_bounces=s["max_bounces"], spp=s["spp"], frame_seed=s["frame_seed"])
+                                      max_bounces=s["max_bounces"], spp=s["spp"], frame_seed=s["frame_seed"],
+                                      nee=s.get("nee", 0), rr_start_depth=s.get("rr_start_depth", 0xFFFFFFFF))
         return (torch.from_numpy(ga.astype(np.float64)), torch.tensor(float(ge[ctx.light]), dtype=torch.float64),
                 None, None, None)

@@ -380,10 +380,10 @@ class Renderer:
         check(self.L.wf_scene_set_emission(self.h, instance, strength))
 
     def adjoint(self, dloss_dimage, max_bounces=6, spp=1, frame_seed=1, cosine=1, env_strength=1.0, wave_paths=0,
-                profile=False):
+                profile=False, nee=0, rr_start_depth=0xFFFFFFFF):
         """Returns (d_albedo (triangles x 3), d_emission (instances,))."""
         s = RenderSettings(1, 1, 0, max_bounces, cosine, 0, env_strength)
-        o = RenderOptions(spp, 0, 0xFFFFFFFF, wave_paths, int(profile), 0)
+        o = RenderOptions(spp, nee, rr_start_depth, wave_paths, int(profile), 0)
         d = np.ascontiguousarray(dloss_dimage, dtype=np.float32).reshape(-1)
         assert len(d) == 3 * self.width * self.height
         ga = np.zeros(3 * self.scene_triangle_count(), dtype=np.float32)

@@ -146,6 +146,8 @@ struct wf_ctx {
     DevBuf<uint32_t> inst_tri_offset;
     DevBuf<float4> L_final, dimage, g_albedo;   // adjoint buffers
     DevBuf<float> g_emission;
+    DevBuf<float> g_em_rep;                 // adjoint: shadow rays' emitter gradients, 32 replicas
+    DevBuf<float4> L_comp, L_final_lo;      // adjoint: rounding errors of the path radiance sums
 
     // wavefront buffers
     bool buffers_ready = false;
@@ -455,6 +457,7 @@ int ensure_buffers(wf_ctx* c) {
     if (c->buffers_ready) return WF_OK;
     const size_t C = c->capacity, npix = (size_t)c->width * c->height;
     RenderBuffers& B = c->B;
+    B.ps_Lc = nullptr;   // only wf_adjoint's passes keep rounding errors
     int rc = 0;
     for (int k = 0; k < 2; ++k) {
         if ((rc = dev_alloc(&B.q_o[k], C)) || (rc = dev_alloc(&B.q_d[k], C)) || (rc = dev_alloc(&B.q_path[k], C)))
@@ -738,7 +741,7 @@ void instance_rows(const Instance& in, float4 ti[4], float4 si[kInstRows], float
     si[6] = make_float4(tb, tn, tm, te);
 }
 
-void append_emitters(const Instance& in, const MeshView& m, std::vector<LightTri>& out, float& run) {
+void append_emitters(const Instance& in, uint32_t inst, const MeshView& m, std::vector<LightTri>& out, float& run) {
     float le[3] = {in.mat.emissive_strength * in.mat.emissive_factor[0],
                    in.mat.emissive_strength * in.mat.emissive_factor[1],
                    in.mat.emissive_strength * in.mat.emissive_factor[2]};
@@ -759,7 +762,9 @@ void append_emitters(const Instance& in, const MeshView& m, std::vector<LightTri
         L.p0 = make_float4(p0[0], p0[1], p0[2], area);
         L.e1 = make_float4(e1[0], e1[1], e1[2], run);
         L.e2 = make_float4(e2[0], e2[1], e2[2], 0.0f);
-        L.n = make_float4(cr[0] * il, cr[1] * il, cr[2] * il, 0.0f);
+        float key;
+        std::memcpy(&key, &inst, 4);
+        L.n = make_float4(cr[0] * il, cr[1] * il, cr[2] * il, key);
         float tex;
         std::memcpy(&tex, &in.mat.emissive_index, 4);
         L.le = make_float4(le[0], le[1], le[2], tex);
@@ -1213,7 +1218,7 @@ int wf_scene_end(wf_ctx* c) {
     for (uint32_t i = 0; i < n; ++i) {
         MeshView mv;
         ctx_mesh(c, c->instances[i].mesh, &mv);
-        append_emitters(c->instances[i], mv, lt, run);
+        append_emitters(c->instances[i], i, mv, lt, run);
     }
     c->light_count = (uint32_t)lt.size();
     c->light_total = run;
@@ -1458,7 +1463,13 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
             WF_CUDA(cudaStreamWaitEvent(c->side, c->ev_shade[d], 0));
             {
                 StageTimer t(c, P.prof, ST_CONNECT, c->side, (int)d);
-                WF_CUDA(launch_connect(P.S, B, d, W.npaths, P.cnt, c->totals + 1, c->side));
+                if (A.g_em_rep) {
+                    const AdjConnect adj{A.dimage, P.SH.sinst, A.g_em_rep, A.instances, W.pix0, W.nsamples,
+                                         A.inv_spp};
+                    WF_CUDA(launch_connect(P.S, B, d, W.npaths, false, c->totals + 1, c->side, &adj));
+                } else {
+                    WF_CUDA(launch_connect(P.S, B, d, W.npaths, P.cnt, c->totals + 1, c->side));
+                }
             }
             WF_CUDA(cudaEventRecord(c->ev_conn[d], c->side));
             pending = true;
@@ -1527,8 +1538,6 @@ int wf_adjoint(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     if (!s->use_wavefront_pathtracing)
         return fail(WF_ERR_INVALID, "wf_adjoint: replays the wavefront stages (use_wavefront_pathtracing = 1)");
     if (!c->albedo_set) return fail(WF_ERR_STATE, "wf_adjoint: set the per-triangle albedo first (wf_scene_set_albedo)");
-    if (o->nee || o->rr_start_depth <= s->max_bounces)
-        return fail(WF_ERR_INVALID, "wf_adjoint: path replay needs nee = 0 and Russian roulette off");
     if ((rc = use_device(c))) return rc;
     if ((rc = ensure_buffers(c))) return rc;
     const uint32_t npix = c->width * c->height;
@@ -1537,7 +1546,9 @@ int wf_adjoint(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     uint32_t replicas = 32;
     while (replicas > 1 && (uint64_t)replicas * ntri * sizeof(float4) > (256ull << 20)) replicas >>= 1;
     if ((rc = c->L_final.reserve(c->capacity)) || (rc = c->dimage.reserve(npix)) ||
-        (rc = c->g_albedo.reserve((uint64_t)replicas * ntri)) || (rc = c->g_emission.reserve(ninst)))
+        (rc = c->g_albedo.reserve((uint64_t)replicas * ntri)) || (rc = c->g_emission.reserve(ninst)) ||
+        (rc = c->g_em_rep.reserve(32ull * std::max<uint64_t>(ninst, 1))) ||
+        (rc = c->L_comp.reserve(c->capacity)) || (rc = c->L_final_lo.reserve(c->capacity)))
         return rc;
     std::vector<float4> dimg(npix);
     for (uint32_t p = 0; p < npix; ++p)
@@ -1546,9 +1557,17 @@ int wf_adjoint(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     WF_CUDA(h2d(c, c->dimage.p, dimg.data(), dimg.size() * sizeof(float4)));
     WF_CUDA(cudaMemsetAsync(c->g_albedo.p, 0, (uint64_t)replicas * ntri * sizeof(float4), c->stream));
     WF_CUDA(cudaMemsetAsync(c->g_emission.p, 0, std::max<uint64_t>(ninst, 1) * sizeof(float), c->stream));
+    WF_CUDA(cudaMemsetAsync(c->g_em_rep.p, 0, 32ull * std::max<uint64_t>(ninst, 1) * sizeof(float), c->stream));
     const uint32_t wave = o->wave_paths ? std::min(o->wave_paths, c->capacity) : c->capacity;
     Pass P = make_pass(c, s, o, frame_seed);
+    P.fused = false;   // the replay's shadow rays need their own launches (AdjConnectIO)
+    P.cnt = false;
+    P.tail_paths = 0;
+    P.B.ps_Lc = c->L_comp.p;   // both passes keep the radiance sums' rounding errors
     AdjointRefs A{};
+    A.g_em_rep = c->g_em_rep.p;
+    A.L_final_lo = c->L_final_lo.p;
+    A.instances = (uint32_t)ninst;
     A.L_final = c->L_final.p;
     A.dimage = c->dimage.p;
     A.g_albedo = c->g_albedo.p;
@@ -1562,15 +1581,20 @@ int wf_adjoint(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
         if ((rc = run_wave(c, P, wv, 0, none, false))) return rc;
         WF_CUDA(cudaMemcpyAsync(c->L_final.p, c->B.ps_L, (size_t)wv.k * wv.np * sizeof(float4),
                                 cudaMemcpyDeviceToDevice, c->stream));
+        WF_CUDA(cudaMemcpyAsync(c->L_final_lo.p, c->L_comp.p, (size_t)wv.k * wv.np * sizeof(float4),
+                                cudaMemcpyDeviceToDevice, c->stream));
         // replay: the same paths from the same seeds, accumulating gradients
         if ((rc = run_wave(c, P, wv, 0, A, false))) return rc;
     }
     WF_CUDA(launch_reduce_replicas(c->g_albedo.p, (uint32_t)ntri, replicas, c->stream));
     c->launches++;
     std::vector<float4> ga(ntri);
-    std::vector<float> ge(ninst);
+    std::vector<float> ge(ninst), gr(32ull * ninst);
     WF_CUDA(d2h(c, ga.data(), c->g_albedo.p, ntri * sizeof(float4)));
-    if (ninst) WF_CUDA(d2h(c, ge.data(), c->g_emission.p, ninst * sizeof(float)));
+    if (ninst) {
+        WF_CUDA(d2h(c, ge.data(), c->g_emission.p, ninst * sizeof(float)));
+        WF_CUDA(d2h(c, gr.data(), c->g_em_rep.p, gr.size() * sizeof(float)));
+    }
     if ((rc = end_call(c))) return rc;
     WF_CUDA(cudaStreamSynchronize(c->stream));
     for (uint64_t t = 0; t < ntri; ++t) {
@@ -1578,7 +1602,11 @@ int wf_adjoint(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
         d_albedo[3 * t + 1] = ga[t].y;
         d_albedo[3 * t + 2] = ga[t].z;
     }
-    for (uint64_t i = 0; i < ninst; ++i) d_emission[i] = ge[i];
+    for (uint64_t i = 0; i < ninst; ++i) {
+        float e = ge[i];
+        for (uint32_t r = 0; r < 32; ++r) e = e + gr[(size_t)r * ninst + i];
+        d_emission[i] = e;
+    }
     c->stats.paths = (uint64_t)npix * o->spp;
     return take_status(c);
 }

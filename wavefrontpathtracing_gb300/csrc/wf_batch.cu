@@ -534,7 +534,7 @@ int build_tables(wf_batch* b) {
             instance_rows(in, &ti[4ull * k], &si[(size_t)kInstRows * k], &ab[6ull * k]);
             MeshView mv;
             ctx_mesh(c, in.mesh, &mv);
-            append_emitters(in, mv, lt, run);
+            append_emitters(in, k, mv, lt, run);
             ++k;
         }
         b->light_cnt[s] = (uint32_t)lt.size() - b->light_off[s];

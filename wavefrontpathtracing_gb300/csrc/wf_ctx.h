@@ -57,7 +57,9 @@ int make_instance(wf_ctx* c, uint32_t mesh, const float* l2w, const material_t* 
 void instance_rows(const Instance& in, float4 ti[4], float4 si[kInstRows], float aabb[6]);
 // Appends the world-space emitter triangles of an emissive instance, with the
 // running area sum the light sampler searches.
-void append_emitters(const Instance& in, const MeshView& m, std::vector<LightTri>& out, float& running_area);
+// inst: the instance's index, kept in each triangle's n.w (the adjoint's emitter key).
+void append_emitters(const Instance& in, uint32_t inst, const MeshView& m, std::vector<LightTri>& out,
+                     float& running_area);
 
 int fail_code(int code, const std::string& msg);
 

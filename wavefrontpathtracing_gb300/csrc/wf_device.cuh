@@ -58,11 +58,20 @@ struct SceneRefs {
 
 constexpr int kInstRows = 7;   // float4 rows per instance in the shading table
 
+// Knuth's TwoSum: s = fl(a + b) and e with a + b = s + e exactly (IEEE
+// arithmetic without contraction, as this library is compiled).
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+    const float s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+    return s;
+}
+
 struct LightTri {
     float4 p0;   // .w = area
     float4 e1;   // .w = running area sum (cdf)
     float4 e2;
-    float4 n;    // unit geometric normal
+    float4 n;    // unit geometric normal, .w = instance index (bits)
     float4 le;   // emitted radiance (strength * factor), .w = emissive texture id (bits)
     float4 uv01; // vertex uv {u0, v0, u1, v1}
     float4 uv2;  // {u2, v2, -, -}

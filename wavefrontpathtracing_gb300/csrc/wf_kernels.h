@@ -39,6 +39,9 @@ struct AdjointRefs {
     float inv_spp;
     uint32_t replicas;            // power of two; a warp adds into replica (block ^ warp) % replicas
     uint32_t triangles;
+    const float4* L_final_lo;     // per path: the forward pass's ps_Lc (L_final + L_final_lo = the exact sum)
+    float* g_em_rep;              // shadow rays' emitter gradients: 32 replicas x instances
+    uint32_t instances;
 };
 
 // Sums the gradient replicas into replica 0.
@@ -56,6 +59,7 @@ struct RenderBuffers {
     float4* ps_T;         // {throughput rgb, pdf of the last BSDF sample}
     uint32_t* ps_flags;   // path flags
     float4* ps_L;         // path radiance (rgb), summed from zero
+    float4* ps_Lc;        // wf_adjoint's passes only (else null): the rounding errors of ps_L's additions
     float4* s_o[2];       // shadow {origin, tmax}, by depth parity (connect at depth d
     float4* s_d[2];       // shadow {direction, path id}   runs while shade at d + 1
     float4* s_c[2];       // shadow {contribution rgb, -}  fills the other buffer)
@@ -114,8 +118,18 @@ cudaError_t launch_extend_camera(const SceneRefs& S, const RenderBuffers& B, con
                                  unsigned long long* total, cudaStream_t stream);
 cudaError_t launch_shade(const ShadeRefs& SH, const RenderBuffers& B, const WaveParams& W, uint32_t depth,
                          uint32_t max_rays, const AdjointRefs& A, cudaStream_t stream);
+// The adjoint replay's shadow rays (wf_adjoint with next-event estimation):
+// each unoccluded ray's contribution is linear in its emitter's strength.
+struct AdjConnect {
+    const float4* dimage;   // per pixel: dloss/d(average radiance)
+    const float4* sinst;    // shading rows (row 5 .w = emissive strength)
+    float* g_rep;           // 32 replicas x ninst emitter gradients (replica = queue slot % 32)
+    uint32_t ninst, pix0, nsamples;
+    float inv_spp;
+};
 cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t max_rays,
-                           bool count, unsigned long long* total, cudaStream_t stream);
+                           bool count, unsigned long long* total, cudaStream_t stream,
+                           const AdjConnect* adj = nullptr);
 // The shadow rays of depth - 1 and the extension rays of depth in one launch
 // (depth >= 1); totals[0] / totals[1] count the extension / shadow rays.
 cudaError_t launch_trace_pair(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, unsigned long long* totals,

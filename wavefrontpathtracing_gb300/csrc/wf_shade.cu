@@ -67,11 +67,27 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
             in.inst = B.h_inst[i];
             in.sample = W.s0 + path % W.nsamples;
             in.depth = depth;
+            in.Lb = mk(0.0f, 0.0f, 0.0f);
+            in.Lb_lo = in.Lb;
+            if (A.g_albedo && depth) {
+                in.Lb = xyz(B.ps_L[path]);
+                in.Lb_lo = xyz(B.ps_Lc[path]);
+            }
             shade_one(SH, K, in, A, path, in.pixel, o);
             if (o.has_add || depth == 0) {
                 // the path's radiance starts at zero here
                 float4 acc = depth ? B.ps_L[path] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                if (o.has_add) {
+                if (B.ps_Lc) {
+                    // the adjoint's passes also keep the additions' rounding errors
+                    float4 lc = depth ? B.ps_Lc[path] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (o.has_add) {
+                        float e;
+                        acc.x = two_sum(acc.x, o.add.x, e); lc.x = lc.x + e;
+                        acc.y = two_sum(acc.y, o.add.y, e); lc.y = lc.y + e;
+                        acc.z = two_sum(acc.z, o.add.z, e); lc.z = lc.z + e;
+                    }
+                    B.ps_Lc[path] = lc;
+                } else if (o.has_add) {
                     acc.x = acc.x + o.add.x;
                     acc.y = acc.y + o.add.y;
                     acc.z = acc.z + o.add.z;
@@ -92,7 +108,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(ShadeRefs SH, RenderBuffers B,
         if (o.shadow && in_bounds(sslot, B.capacity, B.status)) {
             s_o[sslot] = make_float4(o.spos.x, o.spos.y, o.spos.z, o.stmax);
             s_d[sslot] = make_float4(o.sdir.x, o.sdir.y, o.sdir.z, __uint_as_float(path));
-            s_c[sslot] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, 0.0f);
+            s_c[sslot] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, __uint_as_float(o.light_inst));
         }
     }
 }

@@ -83,6 +83,7 @@ struct ShadeIn {
     float last_pdf;    // pdf of the BSDF sample that produced the ray
     uint32_t flags;    // path flags
     uint32_t pixel, sample, depth;   // keys of the path's random numbers
+    V3 Lb, Lb_lo;      // adjoint replay only: the path's radiance before this event (and its rounding errors)
 };
 
 // Per-wave (or per-scene) constants of shading.
@@ -115,6 +116,7 @@ struct ShadeOut {
     bool shadow;       // a next-event shadow ray (spos, sdir, stmax) carrying contrib
     V3 spos, sdir, contrib;
     float stmax;
+    uint32_t light_inst;   // the shadow ray's emitter instance (the adjoint's key)
     uint32_t em_key;   // adjoint: emitter reached (kInvalid if none) and its gradient
     float em_val;
 };
@@ -223,8 +225,9 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
         o.add = mk((T.x * le.x) * w, (T.y * le.y) * w, (T.z * le.z) * w);
         o.has_add = true;
         if (A.g_emission && me.w != 0.0f) {
-            const float4 L = A.L_final[adj_path], g = A.dimage[adj_pixel];
-            const float gl = (g.x * A.inv_spp) * L.x + (g.y * A.inv_spp) * L.y + (g.z * A.inv_spp) * L.z;
+            // the contribution is linear in this emitter's strength
+            const float4 g = A.dimage[adj_pixel];
+            const float gl = (g.x * A.inv_spp) * o.add.x + (g.y * A.inv_spp) * o.add.y + (g.z * A.inv_spp) * o.add.z;
             o.em_key = inst;
             o.em_val = gl / me.w;
         }
@@ -248,12 +251,19 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
     V3 tg, bt;
     basis(N, tg, bt);
     if (bsdf == 0u && A.g_albedo && SH.tri_albedo) {
-        const float4 Lf = A.L_final[adj_path], g = A.dimage[adj_pixel];
+        // everything the path gathers from here on (this vertex's shadow ray
+        // and the rest of the path) is linear in this albedo: the final
+        // radiance less what was gathered before (both sums carry their
+        // rounding errors, so the difference keeps its precision when the
+        // rest of the path adds little)
+        const float4 Lf = A.L_final[adj_path], Lo = A.L_final_lo[adj_path], g = A.dimage[adj_pixel];
+        const V3 Ld = mk((Lf.x - in.Lb.x) + (Lo.x - in.Lb_lo.x), (Lf.y - in.Lb.y) + (Lo.y - in.Lb_lo.y),
+                         (Lf.z - in.Lb.z) + (Lo.z - in.Lb_lo.z));
         const uint32_t rep = (blockIdx.x ^ (threadIdx.x >> 5)) & (A.replicas - 1u);
         float* ga = reinterpret_cast<float*>(A.g_albedo + (size_t)rep * A.triangles + stri);
-        if (base_c.x != 0.0f) atomicAdd(ga, ((g.x * A.inv_spp) * Lf.x) / base_c.x);
-        if (base_c.y != 0.0f) atomicAdd(ga + 1, ((g.y * A.inv_spp) * Lf.y) / base_c.y);
-        if (base_c.z != 0.0f) atomicAdd(ga + 2, ((g.z * A.inv_spp) * Lf.z) / base_c.z);
+        if (base_c.x != 0.0f) atomicAdd(ga, ((g.x * A.inv_spp) * Ld.x) / base_c.x);
+        if (base_c.y != 0.0f) atomicAdd(ga + 1, ((g.y * A.inv_spp) * Ld.y) / base_c.y);
+        if (base_c.z != 0.0f) atomicAdd(ga + 2, ((g.z * A.inv_spp) * Ld.z) / base_c.z);
     }
     if (bsdf == 0u) {
         V3 loc;
@@ -391,6 +401,7 @@ __device__ __forceinline__ void shade_one(const ShadeRefs& SH, const ShadeCtl& K
                 o.spos = pos;
                 o.sdir = wl;
                 o.stmax = dist * kShadowTmaxScale;
+                o.light_inst = __float_as_uint(lt.n.w);
                 o.shadow = true;
             }
         }

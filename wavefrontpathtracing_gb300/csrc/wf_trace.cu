@@ -61,6 +61,7 @@ struct ConnectIO {
     const float4* sd;
     const float4* sc;
     float4* L;
+    float4* Lc;          // wf_adjoint's passes: the additions' rounding errors (else null)
     uint32_t cap;        // checked builds: queue and path entries
     uint32_t* status;
     __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d, float& tmax, bool& nc) const {
@@ -75,10 +76,38 @@ struct ConnectIO {
         const uint32_t path = __float_as_uint(sd[i].w);
         if (!in_bounds(path, cap, status)) return;
         float4 acc = L[path];
-        acc.x = acc.x + k.x;
-        acc.y = acc.y + k.y;
-        acc.z = acc.z + k.z;
+        if (Lc) {
+            float4 lc = Lc[path];
+            float e;
+            acc.x = two_sum(acc.x, k.x, e); lc.x = lc.x + e;
+            acc.y = two_sum(acc.y, k.y, e); lc.y = lc.y + e;
+            acc.z = two_sum(acc.z, k.z, e); lc.z = lc.z + e;
+            Lc[path] = lc;
+        } else {
+            acc.x = acc.x + k.x;
+            acc.y = acc.y + k.y;
+            acc.z = acc.z + k.z;
+        }
         L[path] = acc;
+    }
+};
+
+// The adjoint replay's shadow rays: ConnectIO's store, and an unoccluded
+// ray's contribution (linear in its emitter's strength) adds
+// dloss/dimage . contribution / strength to that emitter's gradient.
+struct AdjConnectIO : ConnectIO {
+    AdjConnect A;
+    __device__ __forceinline__ void store(uint32_t i, const Hit& h, bool ok) const {
+        if (!ok || h.inst != kInvalid || !in_bounds(i, cap, status)) return;
+        ConnectIO::store(i, h, ok);
+        const float4 k = sc[i];
+        const uint32_t path = __float_as_uint(sd[i].w), inst = __float_as_uint(k.w);
+        if (!in_bounds(path, cap, status) || !in_bounds(inst, A.ninst, status)) return;
+        const float strength = A.sinst[(size_t)kInstRows * inst + 5].w;
+        if (strength == 0.0f) return;
+        const float4 g = A.dimage[A.pix0 + path / A.nsamples];
+        const float v = (g.x * A.inv_spp) * k.x + (g.y * A.inv_spp) * k.y + (g.z * A.inv_spp) * k.z;
+        atomicAdd(&A.g_rep[(size_t)(i & 31u) * A.ninst + inst], v / strength);
     }
 };
 
@@ -195,13 +224,19 @@ cudaError_t launch_extend_camera(const SceneRefs& S, const RenderBuffers& B, con
 }
 
 cudaError_t launch_connect(const SceneRefs& S, const RenderBuffers& B, uint32_t depth, uint32_t, bool count,
-                           unsigned long long* total, cudaStream_t stream) {
+                           unsigned long long* total, cudaStream_t stream, const AdjConnect* adj) {
     ConnectIO io;
     const int par = depth & 1;
-    io.so = B.s_o[par]; io.sd = B.s_d[par]; io.sc = B.s_c[par]; io.L = B.ps_L;
+    io.so = B.s_o[par]; io.sd = B.s_d[par]; io.sc = B.s_c[par]; io.L = B.ps_L; io.Lc = B.ps_Lc;
     io.cap = B.capacity; io.status = B.status;
     uint32_t* fetch = B.counts + 3 * kMaxDepth + depth;
     Counters* ctr = B.counters + kMaxDepth + depth;
+    if (adj) {
+        AdjConnectIO aio;
+        static_cast<ConnectIO&>(aio) = io;
+        aio.A = *adj;
+        return launch<true, false>(S, aio, B.counts + kMaxDepth + depth, 0, fetch, B.status, ctr, total, stream);
+    }
     return count ? launch<true, true>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, ctr, total, stream)
                  : launch<true, false>(S, io, B.counts + kMaxDepth + depth, 0, fetch, B.status, ctr, total, stream);
 }
@@ -210,7 +245,7 @@ cudaError_t launch_trace_pair(const SceneRefs& S, const RenderBuffers& B, uint32
                               cudaStream_t stream) {
     PairIO io;
     const int par = (depth - 1) & 1, cur = depth & 1;
-    io.c.so = B.s_o[par]; io.c.sd = B.s_d[par]; io.c.sc = B.s_c[par]; io.c.L = B.ps_L;
+    io.c.so = B.s_o[par]; io.c.sd = B.s_d[par]; io.c.sc = B.s_c[par]; io.c.L = B.ps_L; io.c.Lc = B.ps_Lc;
     io.e.qo = B.q_o[cur]; io.e.qd = B.q_d[cur]; io.e.tuvp = B.h_tuvp; io.e.inst = B.h_inst;
     io.c.cap = io.e.cap = B.capacity; io.c.status = io.e.status = B.status;
     io.n_first = 0;
