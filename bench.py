@@ -555,6 +555,19 @@ def run_ours(args, rank, world, local):
     barrier(dist)
     t_max, rays_all, value = aggregate_weak(dist, gpu_ms, rays)
     spp_per_s = world * SPP * args.steps / (t_max / 1e3)
+    # --- solo launch times (untimed): frames with the shadow rays on the main
+    # stream, so that no extension and shadow-ray launches overlap and each
+    # launch's CUDA-event time is its own
+    SOLO = 3
+    solo_ext, solo_con = np.zeros(16), np.zeros(16)
+    if not args.fused_connect:
+        for i in range(SOLO):
+            flush_l2(torch, l2buf)
+            r.render(max_bounces=DEPTH, spp=SPP, frame_seed=frame_seed(i, rank), nee=1, rr_start_depth=RR,
+                     accumulate=False, profile=True, serial_connect=True, tail_paths=args.tail_paths)
+            so = r.stats()
+            solo_ext += np.array(so["ms_extend_depth"])
+            solo_con += np.array(so["ms_connect_depth"])
     # --- megakernel A/B (use_wavefront_pathtracing = 0): the same frame, whole paths per thread
     mega = None
     if not args.no_megakernel:
@@ -593,32 +606,47 @@ def run_ours(args, rank, world, local):
     # per depth: the extension launches (depth 0 makes its camera rays) and the
     # shadow-ray launches, algorithmic bytes of the counted pass over the
     # timed frames' CUDA-event time of that depth's launch
-    per_depth, secondary, connect = None, None, None
-    if not args.fused_connect:
-        per_depth, connect = [], []
+    def depth_rows(ext_ms_d, con_ms_d, frames):
+        """Per depth: rays, algorithmic bytes (the counted pass) and the
+        CUDA-event time of the extension / shadow-ray launch of that depth."""
+        ext_rows, con_rows = [], []
         for d in range(DEPTH + 1):
             n_d, f = int(c["extend_rays_depth"][d]), c["extend_fetch_depth"][d]
-            ms_d = ext_depth_ms[d] / args.steps
+            ms_d = ext_ms_d[d] / frames
             if n_d and ms_d > 0:
                 b = (n_d * (B_HIT + (0 if d == 0 else B_RAY)) + f[0] * B_TNODE + f[1] * B_INST + f[2] * B_BNODE
                      + f[3] * B_TRI)
-                per_depth.append({"depth": d, "rays": n_d, "alg_bytes": int(b), "ms": round(ms_d, 4),
-                                  "achieved_gbs": round(b / (ms_d / 1e3) / 1e9, 1),
-                                  "frac": round(b / (ms_d / 1e3) / 1e9 / peak, 4),
-                                  "fetches_per_ray": round((f[0] + f[2]) / n_d, 1)})
+                ext_rows.append({"depth": d, "rays": n_d, "alg_bytes": int(b), "ms": round(ms_d, 4),
+                                 "achieved_gbs": round(b / (ms_d / 1e3) / 1e9, 1),
+                                 "frac": round(b / (ms_d / 1e3) / 1e9 / peak, 4),
+                                 "fetches_per_ray": round((f[0] + f[2]) / n_d, 1)})
             n_s, f = int(c["shadow_rays_depth"][d]), c["shadow_fetch_depth"][d]
-            ms_s = con_depth_ms[d] / args.steps
+            ms_s = con_ms_d[d] / frames
             if d < DEPTH and n_s and ms_s > 0:
                 b = n_s * B_SRAY + f[0] * B_TNODE + f[1] * B_INST + f[2] * B_BNODE + f[3] * B_TRI
-                connect.append({"depth": d, "rays": n_s, "alg_bytes": int(b), "ms": round(ms_s, 4),
-                                "frac": round(b / (ms_s / 1e3) / 1e9 / peak, 4)})
+                con_rows.append({"depth": d, "rays": n_s, "alg_bytes": int(b), "ms": round(ms_s, 4),
+                                 "frac": round(b / (ms_s / 1e3) / 1e9 / peak, 4)})
+        return ext_rows, con_rows
 
-        def total(rows):
-            b, t = sum(x["alg_bytes"] for x in rows), sum(x["ms"] for x in rows)
-            return {"alg_bytes": int(b), "ms": round(t, 4), "achieved_gbs": round(b / (t / 1e3) / 1e9, 1) if t else None,
-                    "frac": round(b / (t / 1e3) / 1e9 / peak, 4) if t else None}
+    def total(rows):
+        b, t = sum(x["alg_bytes"] for x in rows), sum(x["ms"] for x in rows)
+        return {"alg_bytes": int(b), "ms": round(t, 4), "achieved_gbs": round(b / (t / 1e3) / 1e9, 1) if t else None,
+                "frac": round(b / (t / 1e3) / 1e9 / peak, 4) if t else None}
+
+    per_depth, secondary, connect, solo = None, None, None, None
+    if not args.fused_connect:
+        # the timed frames (shadow rays overlapping the next depth's extension
+        # rays on a second stream, so each launch's time includes the other's
+        # competition) ...
+        per_depth, con = depth_rows(ext_depth_ms, con_depth_ms, args.steps)
         secondary = total([x for x in per_depth if x["depth"] >= 1])
-        connect = {"launches": connect, **total(connect)}
+        connect = {"launches": con, **total(con)}
+        # ... and the solo frames (every launch alone)
+        s_ext, s_con = depth_rows(solo_ext, solo_con, SOLO)
+        solo = {"frames": SOLO, "schedule": "shadow rays on the main stream after shade (no overlap)",
+                "extend_per_depth": s_ext, "extend": total(s_ext),
+                "extend_secondary": total([x for x in s_ext if x["depth"] >= 1]),
+                "connect_per_depth": s_con, "connect": total(s_con)}
     # --- end to end through the C ABI with host buffers
     img = np.zeros((H, W, 4), dtype=np.float32)
     inst_mesh = np.array([ids[m] for m, _, _ in desc.instances], dtype=np.uint32)
@@ -676,6 +704,13 @@ def run_ours(args, rank, world, local):
                                    blas_layout=args.blas_layout)
         traversal = {"config": TRAVERSAL_CONFIG.format(n=args.soup_triangles, rays=2048 * 2048, side=2048),
                      **info, "results": res}
+        if args.blas_layout == 0:
+            # the DRAM-latency-bound sets again over the quantized 4-wide BLAS
+            # (wf_init_params.blas_layout = 1; its algorithmic bytes are its own
+            # 64-byte node fetches)
+            qinfo, qres = traversal_runs(local, args.soup_triangles, 2048, max(3, min(args.steps, 5)), 3,
+                                         kinds=("incoherent",), orders=(False, True), cpu=False, blas_layout=1)
+            traversal["quantized_4wide"] = {"gpu_bvh_build_s": qinfo["gpu_bvh_build_s"], "results": qres}
     small = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         small = plain_small_leg(local, args.tlas_metric)
@@ -727,7 +762,7 @@ def run_ours(args, rank, world, local):
                              # depth 0 carries 82 % of the rays: 16 identical camera rays per pixel share a
                              # warp, so one fetch serves 16 of them; the secondary depths are the real traversal
                              "per_depth": per_depth, "frac_secondary": secondary["frac"] if secondary else None,
-                             "secondary": secondary, "connect": connect,
+                             "secondary": secondary, "connect": connect, "solo": solo,
                              "alg_bytes_per_launch": int(bytes_per_launch),
                              "ms_per_launch": round(ms_per_launch, 4),
                              # DRAM bytes actually moved (ncu, per launch) over the live launch time

@@ -145,8 +145,10 @@ typedef struct wf_render_options {
      * the extension rays of depth d + 1; WF_SCHEDULE_FUSED (1) = in one
      * persistent launch with the extension rays of depth d + 1 (ms_extend then
      * includes them, ms_connect is 0, and the launch counts in both
-     * launches_extend and launches_connect).  Images are identical.
-     * count_traffic uses the separate schedule. */
+     * launches_extend and launches_connect); WF_SCHEDULE_SERIAL (2) = their
+     * own launch on the main stream after shade (nothing overlaps: each
+     * launch's profile time is its own, for per-kernel measurements).
+     * Images are identical.  count_traffic uses the separate schedule. */
     uint32_t trace_schedule;
     /* the tail: once a wave's extension queue is expected to hold fewer than
      * tail_paths paths (from the previous wave's queue sizes, scaled to this
@@ -160,7 +162,8 @@ typedef struct wf_render_options {
 
 enum wf_trace_schedule {
     WF_SCHEDULE_SEPARATE = 0,
-    WF_SCHEDULE_FUSED = 1
+    WF_SCHEDULE_FUSED = 1,
+    WF_SCHEDULE_SERIAL = 2
 };
 
 enum wf_trace_flags {

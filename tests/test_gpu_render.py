@@ -156,9 +156,10 @@ def test_megakernel_equals_wavefront(orc, name):
 @pytest.mark.parametrize("wave_paths", [0, 1000])
 def test_fused_and_separate_connect_agree(orc, wave_paths):
     """The shadow rays of depth d traced in their own launches on a second
-    stream (the default) or in one launch with the extension rays of depth
-    d + 1: the same rays, the same image bit for bit, fewer launches when
-    fused."""
+    stream (the default), in one launch with the extension rays of depth
+    d + 1, or in their own launches on the main stream: the same rays, the
+    same image bit for bit, fewer launches when fused; an unknown schedule is
+    refused."""
     desc = scenes.instanced_scene(width=64, height=36, instances=48, freqs=(6, 9), spp=2, max_bounces=6)
     kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=3, wave_paths=wave_paths)
     with Renderer(desc.width, desc.height) as r:
@@ -169,14 +170,19 @@ def test_fused_and_separate_connect_agree(orc, wave_paths):
         r.render(frame_seed=33, accumulate=False, **kw)
         sep = r.read_image()
         ss = r.stats()
+        r.render(frame_seed=33, accumulate=False, serial_connect=True, **kw)
+        ser = r.read_image()
+        sr = r.stats()
         with pytest.raises(wf.WFError):
-            o = wf.abi.RenderOptions(1, 1, 0xFFFFFFFF, 0, 0, 0, 2)
+            o = wf.abi.RenderOptions(1, 1, 0xFFFFFFFF, 0, 0, 0, 3)
             s = wf.abi.RenderSettings(1, 1, 0, 2, 1, 0, 1.0)
             wf.check(r.L.wf_render(r.h, ctypes.byref(s), ctypes.byref(o), 1))
     assert sf["rays_connect"] > 0
     assert_images_equal(fused, sep)
+    assert_images_equal(ser, sep)
     for k in ("rays_extend", "rays_connect", "extend_rays_depth", "shadow_rays_depth"):
         assert np.array_equal(np.asarray(sf[k]), np.asarray(ss[k])), k
+        assert np.array_equal(np.asarray(sr[k]), np.asarray(ss[k])), k
     assert sf["launches"] < ss["launches"]
 
 

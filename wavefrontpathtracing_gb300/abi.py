@@ -76,7 +76,7 @@ class Env(ctypes.Structure):
 TEXTURE_RGBA8, TEXTURE_RGBA8_SRGB, TEXTURE_RG8, TEXTURE_RGBA32F = 0, 1, 2, 3
 (TEXTURE_BC1, TEXTURE_BC1_SRGB, TEXTURE_BC2, TEXTURE_BC2_SRGB, TEXTURE_BC3, TEXTURE_BC3_SRGB, TEXTURE_BC4,
  TEXTURE_BC5, TEXTURE_BC7, TEXTURE_BC7_SRGB) = range(4, 14)
-SCHEDULE_SEPARATE, SCHEDULE_FUSED = 0, 1
+SCHEDULE_SEPARATE, SCHEDULE_FUSED, SCHEDULE_SERIAL = 0, 1, 2
 
 
 class RenderOptions(ctypes.Structure):

@@ -1298,7 +1298,7 @@ struct Pass {
     SceneRefs S;
     ShadeRefs SH;
     RenderBuffers B;
-    bool nee, prof, cnt, mega, fused;
+    bool nee, prof, cnt, mega, fused, serial;
     uint32_t tail_paths;
 };
 
@@ -1309,7 +1309,7 @@ int validate_render(wf_ctx* c, const render_settings_t* s, const wf_render_optio
     if (o->spp == 0) return fail(WF_ERR_INVALID, std::string(who) + ": spp must be >= 1");
     if (s->render_view_mode >= RENDER_VIEW_MODE_COUNT)
         return fail(WF_ERR_INVALID, std::string(who) + ": unknown render_view_mode");
-    if (o->trace_schedule > WF_SCHEDULE_FUSED)
+    if (o->trace_schedule > WF_SCHEDULE_SERIAL)
         return fail(WF_ERR_INVALID, std::string(who) + ": unknown trace_schedule");
     return WF_OK;
 }
@@ -1365,6 +1365,7 @@ Pass make_pass(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     P.cnt = o->count_traffic != 0;
     // traffic counting keeps per-kind counters, so it traces the kinds apart
     P.fused = P.nee && !P.cnt && o->trace_schedule == WF_SCHEDULE_FUSED;
+    P.serial = o->trace_schedule == WF_SCHEDULE_SERIAL;
     P.tail_paths = o->tail_paths;
     return P;
 }
@@ -1459,20 +1460,26 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
         c->launches_extend++;
         if (P.nee && !P.fused && d < W.max_bounces) {
             // the shadow rays of depth d overlap the extension rays of depth d + 1
-            WF_CUDA(cudaEventRecord(c->ev_shade[d], c->stream));
-            WF_CUDA(cudaStreamWaitEvent(c->side, c->ev_shade[d], 0));
+            // (the serial schedule keeps them on the main stream)
+            cudaStream_t cs = P.serial ? c->stream : c->side;
+            if (!P.serial) {
+                WF_CUDA(cudaEventRecord(c->ev_shade[d], c->stream));
+                WF_CUDA(cudaStreamWaitEvent(c->side, c->ev_shade[d], 0));
+            }
             {
-                StageTimer t(c, P.prof, ST_CONNECT, c->side, (int)d);
+                StageTimer t(c, P.prof, ST_CONNECT, cs, (int)d);
                 if (A.g_em_rep) {
                     const AdjConnect adj{A.dimage, P.SH.sinst, A.g_em_rep, A.instances, W.pix0, W.nsamples,
                                          A.inv_spp};
-                    WF_CUDA(launch_connect(P.S, B, d, W.npaths, false, c->totals + 1, c->side, &adj));
+                    WF_CUDA(launch_connect(P.S, B, d, W.npaths, false, c->totals + 1, cs, &adj));
                 } else {
-                    WF_CUDA(launch_connect(P.S, B, d, W.npaths, P.cnt, c->totals + 1, c->side));
+                    WF_CUDA(launch_connect(P.S, B, d, W.npaths, P.cnt, c->totals + 1, cs));
                 }
             }
-            WF_CUDA(cudaEventRecord(c->ev_conn[d], c->side));
-            pending = true;
+            if (!P.serial) {
+                WF_CUDA(cudaEventRecord(c->ev_conn[d], c->side));
+                pending = true;
+            }
             c->launches++;
             c->launches_connect++;
         }
