@@ -428,10 +428,12 @@ int wf_bvh_quantize(const void* blob, uint64_t blob_size, void* out_nodes, uint6
                     uint32_t* out_root_count);
 
 /* ---- image files (asset_loader.cpp:56-206) -----------------------------
- * Decodes a .jpg / .jpeg (baseline or progressive; the reference calls
- * stbi_load with 4 channels, asset_loader.cpp:109), a Radiance .hdr (stbi_loadf
- * with 4 channels, :150) or a .dds (its top mip level, :179-206) held in
- * memory: *out_format = WF_TEXTURE_RGBA8 (JPEG), WF_TEXTURE_RGBA32F (HDR) or
+ * Decodes a .jpg / .jpeg (baseline or progressive) or a .png (every colour
+ * type and bit depth, interlaced or not; 16-bit samples keep their high
+ * byte) — the reference calls stbi_load with 4 channels for both,
+ * asset_loader.cpp:109 — a Radiance .hdr (stbi_loadf with 4 channels, :150)
+ * or a .dds (its top mip level, :179-206) held in memory: *out_format =
+ * WF_TEXTURE_RGBA8 (JPEG, PNG), WF_TEXTURE_RGBA32F (HDR) or
  * the DDS file's format (RGBA8 / RGBA8_SRGB / RG8 / RGBA32F texels, BC1-BC5 /
  * BC7 blocks as stored); out receives what wf_texture_create takes with that
  * format (NULL = size query through *inout_size).  Host only. */

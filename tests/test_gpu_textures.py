@@ -233,17 +233,21 @@ def test_bc7_is_refused():
 
 
 def test_texture_files_load_as_the_reference_loads_them(orc, tmp_path):
-    """load_texture_file: a DDS of BC1 blocks (sRGB, as base colours load) and a
-    Radiance HDR file (float texels as stored) written here."""
-    from tests.test_image_decode import dds_header, random_rgbe, write_hdr
+    """load_texture_file: a DDS of BC1 blocks (sRGB, as base colours load), a
+    Radiance HDR file (float texels as stored) and a PNG written here."""
+    from tests.test_image_decode import dds_header, random_rgbe, write_hdr, write_png
     w, h = 10, 6
     blocks = np.random.default_rng(8).integers(0, 256, 3 * 2 * 8, dtype=np.uint8)
     (tmp_path / "t.dds").write_bytes(dds_header(w, h, fourcc=b"DXT1") + blocks.tobytes())
     px = random_rgbe(5, 12, 9)
     (tmp_path / "t.hdr").write_bytes(write_hdr(px))
+    rgba = np.random.default_rng(4).integers(0, 256, (7, 9, 4))
+    (tmp_path / "t.png").write_bytes(write_png(rgba, 6, 8))
     with Renderer(8, 8) as r:
         a = r.read_texture(r.load_texture_file(str(tmp_path / "t.dds"), srgb=True))
         b = r.read_texture(r.load_texture_file(str(tmp_path / "t.hdr")))
+        c = r.read_texture(r.load_texture_file(str(tmp_path / "t.png")))
+    assert np.array_equal(c.reshape(7, 9, 4), to_float(rgba.astype(np.uint8), False))
     assert np.array_equal(a.view(np.uint32), to_float(orc.decode_bc(abi.TEXTURE_BC1, blocks, w, h), True).view(np.uint32))
     import wavefrontpathtracing_gb300 as wf
     want, _, _, _ = wf.decode_image(write_hdr(px))

@@ -9,6 +9,11 @@ files the reference's asset loader reads (asset_loader.cpp:56-206).
                   checkout is present: within 3 of 255 per sample (both are
                   exact decoders up to their IDCT and colour-conversion
                   rounding: stb's are fixed point, ours double);
+  PNG             bit for bit against stb_image (stbi_load) on files written
+                  here (every colour type and bit depth, the five filters,
+                  Adam7, tRNS, stored / fixed / dynamic DEFLATE blocks) and on
+                  the reference's own PNG textures where the checkout is
+                  present;
   DDS             the headers of the reference's own .dds files (all BC1) and
                   of files written here, the blocks returned as stored;
   BC1-BC5         the oracle's block decoder (the GPU decoder's checker) on
@@ -154,6 +159,144 @@ def test_jpeg_matches_stb_on_the_reference_textures():
         d = np.abs(ours.astype(np.int16) - want.astype(np.int16))
         assert d.max() <= 3 and d.mean() < 0.1 and (d > 2).mean() < 1e-3, (f, d.max(), d.mean())
         assert np.all(ours[..., 3] == 255)
+
+
+# ------------------------------------------------------------------- PNG
+
+def png_chunk(t, data):
+    import zlib
+    return struct.pack(">I", len(data)) + t + data + struct.pack(">I", zlib.crc32(t + data) & 0xFFFFFFFF)
+
+
+def pack_row(samples, depth):
+    """One scanline's samples (ints) at the given bit depth, big-endian / MSB first."""
+    if depth == 16:
+        return b"".join(struct.pack(">H", int(v)) for v in samples)
+    if depth == 8:
+        return bytes(int(v) for v in samples)
+    out, acc, nb = bytearray(), 0, 0
+    for v in samples:
+        acc = (acc << depth) | int(v)
+        nb += depth
+        if nb == 8:
+            out.append(acc)
+            acc, nb = 0, 0
+    if nb:
+        out.append(acc << (8 - nb))
+    return bytes(out)
+
+
+def filter_row(raw, prev, bpp, f):
+    out = bytearray()
+    for i, x in enumerate(raw):
+        a = raw[i - bpp] if i >= bpp else 0
+        b = prev[i] if prev else 0
+        c = prev[i - bpp] if prev and i >= bpp else 0
+        if f == 0:
+            pred = 0
+        elif f == 1:
+            pred = a
+        elif f == 2:
+            pred = b
+        elif f == 3:
+            pred = (a + b) >> 1
+        else:
+            p_ = a + b - c
+            pa, pb, pc = abs(p_ - a), abs(p_ - b), abs(p_ - c)
+            pred = a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+        out.append((x - pred) & 255)
+    return bytes([f]) + bytes(out)
+
+
+ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
+
+
+def write_png(samples, ctype, depth, interlace=0, level=6, palette=None, trns=None, seed=0):
+    """A PNG of samples (h x w x channels ints); every scanline gets a filter
+    drawn from 0..4; zlib level 0 gives stored blocks, 1 mostly fixed Huffman
+    codes, 9 dynamic ones."""
+    import zlib
+    rng = np.random.default_rng(seed)
+    h, w, ch = samples.shape
+    bpp = max(1, ch * depth // 8)
+    raw = bytearray()
+    passes = ADAM7 if interlace else [(0, 0, 1, 1)]
+    for x0, y0, dx, dy in passes:
+        sub = samples[y0::dy, x0::dx]
+        if sub.shape[0] == 0 or sub.shape[1] == 0:
+            continue
+        prev = None
+        for y in range(sub.shape[0]):
+            row = pack_row(sub[y].reshape(-1), depth)
+            raw += filter_row(row, prev, bpp, int(rng.integers(0, 5)))
+            prev = row
+    out = b"\x89PNG\r\n\x1a\n" + png_chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, interlace))
+    if palette is not None:
+        out += png_chunk(b"PLTE", bytes(palette))
+    if trns is not None:
+        out += png_chunk(b"tRNS", bytes(trns))
+    z = zlib.compress(bytes(raw), level)
+    out += png_chunk(b"IDAT", z[: len(z) // 2]) + png_chunk(b"IDAT", z[len(z) // 2:])   # split across two chunks
+    return out + png_chunk(b"IEND", b"")
+
+
+PNG_CASES = [
+    # ctype, depth, interlace, level, trns
+    (6, 8, 0, 9, None), (6, 8, 1, 1, None), (6, 16, 0, 6, None), (2, 8, 0, 0, None), (2, 8, 1, 9, "key"),
+    (2, 16, 1, 9, "key"), (0, 8, 0, 9, "key"), (0, 1, 0, 9, None), (0, 2, 1, 6, None), (0, 4, 0, 1, "key"),
+    (0, 16, 0, 9, "key"), (4, 8, 1, 9, None), (4, 16, 0, 9, None), (3, 8, 0, 9, "alpha"), (3, 4, 1, 9, "alpha"),
+    (3, 2, 0, 1, None), (3, 1, 1, 0, None),
+]
+
+
+@need_stb
+@pytest.mark.parametrize("ctype,depth,interlace,level,trns", PNG_CASES)
+def test_png_equals_stb_bit_for_bit(ctype, depth, interlace, level, trns):
+    rng = np.random.default_rng(ctype * 100 + depth * 10 + interlace)
+    h, w = 23, 37
+    ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    top = (1 << depth) - 1
+    smp = rng.integers(0, top + 1, (h, w, ch))
+    smp[:, 5:12] = smp[:, 5:6]                    # runs, for the DEFLATE matches
+    palette, tr = None, None
+    if ctype == 3:
+        ncol = min(1 << depth, 200)
+        smp = rng.integers(0, ncol, (h, w, 1))
+        palette = rng.integers(0, 256, 3 * ncol).astype(np.uint8)
+        if trns == "alpha":
+            tr = rng.integers(0, 256, ncol // 2 + 1).astype(np.uint8)
+    elif trns == "key":
+        key = smp[3, 4]
+        smp[10:12, 2:9] = key                     # some pixels equal the key
+        tr = b"".join(struct.pack(">H", int(v)) for v in key)
+    data = write_png(smp, ctype, depth, interlace, level, palette, tr, seed=depth)
+    ours, ow, oh, fmt = wf.decode_image(data)
+    assert fmt == abi.TEXTURE_RGBA8 and (ow, oh) == (w, h)
+    want = stb_decode(data, False)
+    assert np.array_equal(ours, want)
+
+
+def test_png_rejects_corrupt_data():
+    smp = np.zeros((4, 4, 3), int)
+    data = bytearray(write_png(smp, 2, 8))
+    with pytest.raises(wf.WFError):
+        wf.decode_image(bytes(data[:40]))          # IDAT cut short
+    data[16 + 8 + 9] = 7                           # colour type 7
+    with pytest.raises(wf.WFError):
+        wf.decode_image(bytes(data))
+
+
+def reference_pngs():
+    return sorted(glob.glob(os.path.join(REF, "assets", "**", "*.png"), recursive=True))
+
+
+@need_stb
+@pytest.mark.skipif(not reference_pngs(), reason="the reference checkout's textures are not present")
+def test_png_matches_stb_on_the_reference_textures():
+    for f in reference_pngs():
+        data = open(f, "rb").read()
+        ours, w, h, fmt = wf.decode_image(data)
+        assert np.array_equal(ours, stb_decode(data, False)), f
 
 
 # ------------------------------------------------------------------- DDS

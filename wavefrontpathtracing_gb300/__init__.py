@@ -278,17 +278,12 @@ class Renderer:
 
     def load_texture_file(self, path, srgb=False):
         """A texture from an image file, as the reference's asset loader takes
-        it (asset_loader.cpp:56-206): .png (gltf.decode_png) / .jpg / .jpeg
-        (RGBA8, or RGBA8_SRGB when srgb), .hdr (RGBA32F), .dds (its format,
-        the sRGB variant of RGBA8 / BC1-BC3 when srgb, dds.h:125-147)."""
+        it (asset_loader.cpp:56-206), decoded by wf_image_decode: .png / .jpg /
+        .jpeg (RGBA8, or RGBA8_SRGB when srgb), .hdr (RGBA32F), .dds (its
+        format, the sRGB variant of RGBA8 / BC1-BC3 when srgb, dds.h:125-147)."""
         ext = os.path.splitext(path)[1].lower()
         data = open(path, "rb").read()
-        if ext == ".png":
-            from .gltf import decode_png
-            img = decode_png(data)
-            return self.create_texture_raw(img, img.shape[1], img.shape[0],
-                                           abi.TEXTURE_RGBA8_SRGB if srgb else abi.TEXTURE_RGBA8)
-        if ext not in (".jpg", ".jpeg", ".hdr", ".dds"):
+        if ext not in (".png", ".jpg", ".jpeg", ".hdr", ".dds"):
             raise ValueError(f"unsupported texture file type: {path}")
         raw, w, h, fmt = decode_image(data)
         if srgb:

@@ -12,11 +12,19 @@
 //   HDR   Greg Ward's Radiance RGBE: header, "-Y h +X w" resolution, scanlines
 //         flat or with the 2-2-width run-length encoding; RGBE -> float as
 //         mantissa * 2^(e - 136).  Output RGBA32F (alpha 1).
+//   PNG   PNG (ISO/IEC 15948): zlib / DEFLATE (RFC 1950 / 1951: stored,
+//         fixed and dynamic Huffman blocks), the five scanline filters,
+//         Adam7 interlacing, colour types 0 / 2 / 3 / 4 / 6 at every bit
+//         depth the format allows, tRNS transparency; 16-bit samples keep
+//         their high byte (as the reference's stbi_load with 4 channels,
+//         asset_loader.cpp:109).  Output RGBA8.
 //   DDS   the DirectDraw Surface header (with or without the DX10 extension):
 //         RGBA8, RG8, RGBA32F texels or BC1-BC5 / BC7 blocks of the top mip
 //         level as stored (BC blocks are decoded on the GPU by
 //         wf_texture_create).
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -318,14 +326,16 @@ struct Jpeg {
 
     // dequantize + inverse DCT (A.3.3) of every block, samples of each component
     void reconstruct(std::vector<std::vector<uint8_t>>& planes) {
-        static double cosv[8][8];
-        static bool init = false;
-        if (!init) {
-            for (int x = 0; x < 8; ++x)
-                for (int u = 0; u < 8; ++u)
-                    cosv[x][u] = (u == 0 ? std::sqrt(0.5) : 1.0) * std::cos((2 * x + 1) * u * M_PI / 16.0);
-            init = true;
-        }
+        struct CosTable {
+            double v[8][8];
+            CosTable() {
+                for (int x = 0; x < 8; ++x)
+                    for (int u = 0; u < 8; ++u)
+                        v[x][u] = (u == 0 ? std::sqrt(0.5) : 1.0) * std::cos((2 * x + 1) * u * M_PI / 16.0);
+            }
+        };
+        static const CosTable table;   // initialised once, thread-safe
+        const auto& cosv = table.v;
         planes.resize(comp.size());
         for (size_t ci = 0; ci < comp.size(); ++ci) {
             Comp& c = comp[ci];
@@ -592,6 +602,315 @@ int decode_dds(const uint8_t* d, size_t n, uint32_t* w, uint32_t* h, uint32_t* f
     return WF_OK;
 }
 
+// ------------------------------------------------------------------ PNG
+// DEFLATE decoder (RFC 1951), reading bits LSB first; Huffman codes decoded
+// canonically one bit at a time.
+struct Inflate {
+    const uint8_t* d;
+    size_t n, pos = 0;
+    uint64_t buf = 0;
+    int cnt = 0;
+    bool bad = false;
+    std::vector<uint8_t> out;
+
+    uint32_t bits(int k) {
+        while (cnt < k) {
+            if (pos >= n) { bad = true; return 0; }
+            buf |= (uint64_t)d[pos++] << cnt;
+            cnt += 8;
+        }
+        const uint32_t v = (uint32_t)(buf & ((1ull << k) - 1));
+        buf >>= k;
+        cnt -= k;
+        return v;
+    }
+    struct Huffman {
+        uint16_t count[16] = {};
+        uint16_t symbol[320] = {};
+    };
+    // counts per length and symbols in (length, value) order; false for an
+    // over-subscribed set of lengths
+    static bool build(Huffman& hf, const uint8_t* len, int nsym) {
+        for (int i = 0; i < 16; ++i) hf.count[i] = 0;
+        for (int i = 0; i < nsym; ++i) hf.count[len[i]]++;
+        hf.count[0] = 0;
+        int left = 1;
+        for (int l = 1; l < 16; ++l) {
+            left <<= 1;
+            left -= hf.count[l];
+            if (left < 0) return false;
+        }
+        uint16_t off[16];
+        off[1] = 0;
+        for (int l = 1; l < 15; ++l) off[l + 1] = off[l] + hf.count[l];
+        for (int i = 0; i < nsym; ++i)
+            if (len[i]) hf.symbol[off[len[i]]++] = (uint16_t)i;
+        return true;
+    }
+    int decode(const Huffman& hf) {
+        int code = 0, first = 0, index = 0;
+        for (int l = 1; l < 16; ++l) {
+            code |= (int)bits(1);
+            if (bad) return -1;
+            const int c = hf.count[l];
+            if (code - first < c) return hf.symbol[index + (code - first)];
+            index += c;
+            first += c;
+            first <<= 1;
+            code <<= 1;
+        }
+        bad = true;   // no code of 15 bits or fewer matched
+        return -1;
+    }
+    bool codes(const Huffman& lit, const Huffman& dist) {
+        static const uint16_t lbase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                                           31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+        static const uint8_t lext[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                                         2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+        static const uint16_t dbase[30] = {1,   2,   3,   4,   5,   7,    9,    13,   17,   25,   33,   49,   65,    97,    129,
+                                           193, 257, 385, 513, 769, 1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
+        static const uint8_t dext[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
+                                         6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+        for (;;) {
+            const int sym = decode(lit);
+            if (sym < 0) return false;
+            if (sym < 256) {
+                out.push_back((uint8_t)sym);
+            } else if (sym == 256) {
+                return true;
+            } else {
+                const int li = sym - 257;
+                if (li >= 29) return false;
+                const size_t len = lbase[li] + bits(lext[li]);
+                const int ds = decode(dist);
+                if (ds < 0 || ds >= 30) return false;
+                const size_t dd = dbase[ds] + bits(dext[ds]);
+                if (bad || dd > out.size()) return false;
+                const size_t from = out.size() - dd;
+                for (size_t k = 0; k < len; ++k) out.push_back(out[from + k]);
+            }
+        }
+    }
+    bool run() {
+        int last;
+        do {
+            last = (int)bits(1);
+            const uint32_t type = bits(2);
+            if (bad) return false;
+            if (type == 0) {
+                buf = 0;   // stored block: the rest of the current byte is dropped
+                cnt = 0;
+                if (pos + 4 > n) return false;
+                const uint32_t len = d[pos] | (d[pos + 1] << 8), nlen = d[pos + 2] | (d[pos + 3] << 8);
+                pos += 4;
+                if ((len ^ 0xFFFFu) != nlen || pos + len > n) return false;
+                out.insert(out.end(), d + pos, d + pos + len);
+                pos += len;
+            } else if (type == 1) {
+                static const struct Fixed {
+                    Huffman lit, dist;
+                    Fixed() {
+                        uint8_t l[288];
+                        for (int i = 0; i < 288; ++i) l[i] = i < 144 ? 8 : i < 256 ? 9 : i < 280 ? 7 : 8;
+                        build(lit, l, 288);
+                        uint8_t dl[30];
+                        for (int i = 0; i < 30; ++i) dl[i] = 5;
+                        build(dist, dl, 30);
+                    }
+                } fixed;
+                if (!codes(fixed.lit, fixed.dist)) return false;
+            } else if (type == 2) {
+                const int hlit = (int)bits(5) + 257, hdist = (int)bits(5) + 1, hclen = (int)bits(4) + 4;
+                static const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+                uint8_t cl[19] = {};
+                for (int i = 0; i < hclen; ++i) cl[order[i]] = (uint8_t)bits(3);
+                Huffman clh;
+                if (bad || hlit > 286 || hdist > 30 || !build(clh, cl, 19)) return false;
+                uint8_t lens[320] = {};
+                int i = 0;
+                while (i < hlit + hdist) {
+                    const int sym = decode(clh);
+                    if (sym < 0) return false;
+                    if (sym < 16) {
+                        lens[i++] = (uint8_t)sym;
+                    } else {
+                        int rep, val = 0;
+                        if (sym == 16) {
+                            if (i == 0) return false;
+                            val = lens[i - 1];
+                            rep = 3 + (int)bits(2);
+                        } else if (sym == 17) {
+                            rep = 3 + (int)bits(3);
+                        } else {
+                            rep = 11 + (int)bits(7);
+                        }
+                        if (i + rep > hlit + hdist) return false;
+                        while (rep--) lens[i++] = (uint8_t)val;
+                    }
+                }
+                Huffman lit, dist;
+                if (bad || lens[256] == 0 || !build(lit, lens, hlit) || !build(dist, lens + hlit, hdist)) return false;
+                if (!codes(lit, dist)) return false;
+            } else {
+                return false;
+            }
+        } while (!last);
+        return !bad;
+    }
+};
+
+uint32_t be32(const uint8_t* p) {
+    return ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3];
+}
+
+int decode_png(const uint8_t* d, size_t n, uint32_t* w, uint32_t* h, std::vector<uint8_t>& rgba, std::string& err) {
+    static const uint8_t sig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
+    if (n < 8 || std::memcmp(d, sig, 8) != 0) { err = "not a PNG file"; return WF_ERR_INVALID; }
+    size_t pos = 8;
+    uint32_t width = 0, height = 0;
+    int depth = 0, ctype = -1, interlace = 0;
+    std::vector<uint8_t> idat, plte, trns;
+    bool ihdr = false, iend = false;
+    while (pos + 12 <= n && !iend) {
+        const uint32_t len = be32(d + pos);
+        const uint8_t* type = d + pos + 4;
+        if (len > n - pos - 12) { err = "truncated chunk"; return WF_ERR_INVALID; }
+        const uint8_t* data = d + pos + 8;
+        if (!std::memcmp(type, "IHDR", 4)) {
+            if (len != 13) { err = "bad IHDR"; return WF_ERR_INVALID; }
+            width = be32(data);
+            height = be32(data + 4);
+            depth = data[8];
+            ctype = data[9];
+            interlace = data[12];
+            if (data[10] != 0 || data[11] != 0 || interlace > 1) { err = "unknown compression, filter or interlace method"; return WF_ERR_INVALID; }
+            ihdr = true;
+        } else if (!std::memcmp(type, "PLTE", 4)) {
+            plte.assign(data, data + len);
+        } else if (!std::memcmp(type, "tRNS", 4)) {
+            trns.assign(data, data + len);
+        } else if (!std::memcmp(type, "IDAT", 4)) {
+            idat.insert(idat.end(), data, data + len);
+        } else if (!std::memcmp(type, "IEND", 4)) {
+            iend = true;
+        } else if (!(type[0] & 0x20)) {
+            err = "unknown critical chunk";
+            return WF_ERR_INVALID;
+        }
+        pos += 12ull + len;
+    }
+    if (!ihdr || idat.size() < 2) { err = "missing IHDR or IDAT"; return WF_ERR_INVALID; }
+    if (width == 0 || height == 0 || width > 16384 || height > 16384) { err = "unsupported image size"; return WF_ERR_INVALID; }
+    int channels;
+    switch (ctype) {
+        case 0: channels = 1; break;
+        case 2: channels = 3; break;
+        case 3: channels = 1; break;
+        case 4: channels = 2; break;
+        case 6: channels = 4; break;
+        default: err = "unknown colour type"; return WF_ERR_INVALID;
+    }
+    const bool depth_ok = (ctype == 0 && (depth == 1 || depth == 2 || depth == 4 || depth == 8 || depth == 16)) ||
+                          (ctype == 3 && (depth == 1 || depth == 2 || depth == 4 || depth == 8)) ||
+                          ((ctype == 2 || ctype == 4 || ctype == 6) && (depth == 8 || depth == 16));
+    if (!depth_ok) { err = "invalid bit depth for the colour type"; return WF_ERR_INVALID; }
+    if (ctype == 3 && (plte.empty() || plte.size() % 3 != 0)) { err = "missing or bad PLTE"; return WF_ERR_INVALID; }
+    // zlib header (RFC 1950): deflate, no preset dictionary
+    if ((idat[0] & 15) != 8 || ((idat[0] << 8) | idat[1]) % 31 != 0 || (idat[1] & 0x20)) {
+        err = "bad zlib header";
+        return WF_ERR_INVALID;
+    }
+    Inflate inf;
+    inf.d = idat.data() + 2;
+    inf.n = idat.size() - 2;
+    if (!inf.run()) { err = "corrupt DEFLATE data"; return WF_ERR_INVALID; }
+    const std::vector<uint8_t>& raw = inf.out;
+    const int bpp = std::max(1, channels * depth / 8);   // filter byte distance
+    // samples of the whole image, 16 bits each, in row-major pixel order
+    std::vector<uint16_t> smp((size_t)width * height * channels);
+    static const int ax0[7] = {0, 4, 0, 2, 0, 1, 0}, ay0[7] = {0, 0, 4, 0, 2, 0, 1};
+    static const int adx[7] = {8, 8, 4, 4, 2, 2, 1}, ady[7] = {8, 8, 8, 4, 4, 2, 2};
+    size_t rp = 0;
+    for (int pass = 0; pass < (interlace ? 7 : 1); ++pass) {
+        const uint32_t x0 = interlace ? ax0[pass] : 0, y0 = interlace ? ay0[pass] : 0;
+        const uint32_t dx = interlace ? adx[pass] : 1, dy = interlace ? ady[pass] : 1;
+        if (x0 >= width || y0 >= height) continue;
+        const uint32_t pw = (width - x0 + dx - 1) / dx, ph = (height - y0 + dy - 1) / dy;
+        const size_t stride = ((size_t)pw * channels * depth + 7) / 8;
+        std::vector<uint8_t> prev(stride, 0), cur(stride);
+        for (uint32_t y = 0; y < ph; ++y) {
+            if (rp + 1 + stride > raw.size()) { err = "image data too short"; return WF_ERR_INVALID; }
+            const uint8_t f = raw[rp];
+            const uint8_t* src = raw.data() + rp + 1;
+            rp += 1 + stride;
+            for (size_t i = 0; i < stride; ++i) {
+                const int a = i >= (size_t)bpp ? cur[i - bpp] : 0, b = prev[i], c = i >= (size_t)bpp ? prev[i - bpp] : 0;
+                int v = src[i];
+                switch (f) {
+                    case 0: break;
+                    case 1: v += a; break;
+                    case 2: v += b; break;
+                    case 3: v += (a + b) >> 1; break;
+                    case 4: {
+                        const int p = a + b - c, pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+                        v += (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+                        break;
+                    }
+                    default: err = "unknown scanline filter"; return WF_ERR_INVALID;
+                }
+                cur[i] = (uint8_t)v;
+            }
+            for (uint32_t x = 0; x < pw; ++x) {
+                const size_t o = (((size_t)(y0 + y * dy)) * width + (x0 + x * dx)) * channels;
+                for (int ch = 0; ch < channels; ++ch) {
+                    const size_t k = (size_t)x * channels + ch;
+                    uint16_t v;
+                    if (depth == 16) v = (uint16_t)((cur[2 * k] << 8) | cur[2 * k + 1]);
+                    else if (depth == 8) v = cur[k];
+                    else v = (uint16_t)((cur[(k * depth) >> 3] >> (8 - depth - (int)((k * depth) & 7))) & ((1 << depth) - 1));
+                    smp[o + ch] = v;
+                }
+            }
+            std::swap(prev, cur);
+        }
+    }
+    // to RGBA8: 16-bit samples keep their high byte; grey below 8 bits is
+    // scaled to 0..255; tRNS keys compare with the samples at their own depth
+    const int scale = depth == 1 ? 255 : depth == 2 ? 85 : depth == 4 ? 17 : 1;
+    rgba.resize((size_t)width * height * 4);
+    const size_t npx = (size_t)width * height;
+    for (size_t i = 0; i < npx; ++i) {
+        const uint16_t* s = smp.data() + i * channels;
+        uint8_t* o = rgba.data() + i * 4;
+        auto to8 = [&](uint16_t v) { return (uint8_t)(depth == 16 ? (v >> 8) : v * scale); };
+        if (ctype == 3) {
+            const size_t idx = s[0];
+            if (3 * idx + 2 >= plte.size()) { err = "palette index out of range"; return WF_ERR_INVALID; }
+            o[0] = plte[3 * idx];
+            o[1] = plte[3 * idx + 1];
+            o[2] = plte[3 * idx + 2];
+            o[3] = idx < trns.size() ? trns[idx] : 255;
+        } else if (ctype == 0 || ctype == 4) {
+            o[0] = o[1] = o[2] = to8(s[0]);
+            if (ctype == 4) o[3] = to8(s[1]);
+            else o[3] = (trns.size() >= 2 && s[0] == (((uint16_t)trns[0] << 8) | trns[1])) ? 0 : 255;
+        } else {
+            for (int ch = 0; ch < 3; ++ch) o[ch] = to8(s[ch]);
+            if (ctype == 6) {
+                o[3] = to8(s[3]);
+            } else {
+                const bool key = trns.size() >= 6 && s[0] == (((uint16_t)trns[0] << 8) | trns[1]) &&
+                                 s[1] == (((uint16_t)trns[2] << 8) | trns[3]) &&
+                                 s[2] == (((uint16_t)trns[4] << 8) | trns[5]);
+                o[3] = key ? 0 : 255;
+            }
+        }
+    }
+    *w = width;
+    *h = height;
+    return WF_OK;
+}
+
 }  // namespace
 }  // namespace wf
 
@@ -621,8 +940,14 @@ extern "C" int wf_image_decode(const void* file, uint64_t file_size, uint32_t* o
         bytes = rgbaf.size() * 4ull;
     } else if (n >= 4 && d[0] == 'D' && d[1] == 'D' && d[2] == 'S' && d[3] == ' ') {
         rc = decode_dds(d, n, &w, &h, &f, &src, &bytes, err);
+    } else if (n >= 8 && d[0] == 137 && d[1] == 'P' && d[2] == 'N' && d[3] == 'G') {
+        rc = decode_png(d, n, &w, &h, rgba8, err);
+        f = WF_TEXTURE_RGBA8;
+        src = rgba8.data();
+        bytes = rgba8.size();
     } else {
-        return report_error(WF_ERR_INVALID, "wf_image_decode: unrecognised file (JPEG, Radiance HDR or DDS expected)");
+        return report_error(WF_ERR_INVALID,
+                            "wf_image_decode: unrecognised file (JPEG, PNG, Radiance HDR or DDS expected)");
     }
     if (rc) return report_error(rc, ("wf_image_decode: " + err).c_str());
     *out_width = w;
