@@ -611,6 +611,7 @@ struct Inflate {
     uint64_t buf = 0;
     int cnt = 0;
     bool bad = false;
+    size_t limit = 0;   // the output the image needs: more is an error, not an allocation
     std::vector<uint8_t> out;
 
     uint32_t bits(int k) {
@@ -675,6 +676,7 @@ struct Inflate {
             const int sym = decode(lit);
             if (sym < 0) return false;
             if (sym < 256) {
+                if (out.size() >= limit) return false;
                 out.push_back((uint8_t)sym);
             } else if (sym == 256) {
                 return true;
@@ -685,7 +687,7 @@ struct Inflate {
                 const int ds = decode(dist);
                 if (ds < 0 || ds >= 30) return false;
                 const size_t dd = dbase[ds] + bits(dext[ds]);
-                if (bad || dd > out.size()) return false;
+                if (bad || dd > out.size() || len > limit - out.size()) return false;
                 const size_t from = out.size() - dd;
                 for (size_t k = 0; k < len; ++k) out.push_back(out[from + k]);
             }
@@ -703,7 +705,7 @@ struct Inflate {
                 if (pos + 4 > n) return false;
                 const uint32_t len = d[pos] | (d[pos + 1] << 8), nlen = d[pos + 2] | (d[pos + 3] << 8);
                 pos += 4;
-                if ((len ^ 0xFFFFu) != nlen || pos + len > n) return false;
+                if ((len ^ 0xFFFFu) != nlen || pos + len > n || len > limit - out.size()) return false;
                 out.insert(out.end(), d + pos, d + pos + len);
                 pos += len;
             } else if (type == 1) {
@@ -823,6 +825,17 @@ int decode_png(const uint8_t* d, size_t n, uint32_t* w, uint32_t* h, std::vector
     Inflate inf;
     inf.d = idat.data() + 2;
     inf.n = idat.size() - 2;
+    // filtered scanlines of every pass: a filter byte and the packed samples per row
+    for (int pass = 0; pass < (interlace ? 7 : 1); ++pass) {
+        static const int px0[7] = {0, 4, 0, 2, 0, 1, 0}, py0[7] = {0, 0, 4, 0, 2, 0, 1};
+        static const int pdx[7] = {8, 8, 4, 4, 2, 2, 1}, pdy[7] = {8, 8, 8, 4, 4, 2, 2};
+        const uint32_t x0 = interlace ? px0[pass] : 0, y0 = interlace ? py0[pass] : 0;
+        const uint32_t dx = interlace ? pdx[pass] : 1, dy = interlace ? pdy[pass] : 1;
+        if (x0 >= width || y0 >= height) continue;
+        const uint64_t pw = (width - x0 + dx - 1) / dx, ph = (height - y0 + dy - 1) / dy;
+        inf.limit += (size_t)(ph * (1 + (pw * channels * depth + 7) / 8));
+    }
+    inf.out.reserve(inf.limit);
     if (!inf.run()) { err = "corrupt DEFLATE data"; return WF_ERR_INVALID; }
     const std::vector<uint8_t>& raw = inf.out;
     const int bpp = std::max(1, channels * depth / 8);   // filter byte distance
