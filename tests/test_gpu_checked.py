@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SUITE = ["tests/test_gpu_render.py", "tests/test_gpu_trace.py", "tests/test_gpu_batch.py", "tests/test_gpu_qbvh.py",
-         "tests/test_gpu_textures.py", "tests/test_gltf.py", "tests/test_fbx.py"]
+         "tests/test_gpu_instance_bounds.py", "tests/test_gpu_textures.py", "tests/test_gltf.py", "tests/test_fbx.py"]
 
 
 def test_checked_build_reports_itself():
