@@ -648,7 +648,13 @@ def run_ours(args, rank, world, local):
                 "extend_secondary": total([x for x in s_ext if x["depth"] >= 1]),
                 "connect_per_depth": s_con, "connect": total(s_con)}
     # --- end to end through the C ABI with host buffers
-    img = np.zeros((H, W, 4), dtype=np.float32)
+    # the image is read into page-locked host memory (a pageable buffer's copy
+    # speed depends on the host's page state: 1-60 GB/s on the same box)
+    if torch is not None:
+        img_t = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True)
+        img = img_t.numpy()
+    else:
+        img = np.zeros((H, W, 4), dtype=np.float32)
     inst_mesh = np.array([ids[m] for m, _, _ in desc.instances], dtype=np.uint32)
     inst_xf = np.stack([np.asarray(t, dtype=np.float32) for _, t, _ in desc.instances])
     inst_mat = np.array([m for _, _, m in desc.instances], dtype=wf.abi.material_ext_dtype)
