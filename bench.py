@@ -31,6 +31,7 @@ Prints one JSON line (rank 0).  Multi-GPU (torchrun): each rank renders its
 own frame (different seeds), weak scaling, max time over ranks.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -882,12 +883,22 @@ def traversal_runs(local, n_tris, side, steps, warmup, kinds=("coherent", "incoh
                         ms.append(r.stats()["ms_total"])
                     t = float(np.mean(ms))
                     hits = d_hits.cpu().numpy().view(wf.abi.hit_dtype)
-                    # end to end through wf_trace (host arrays in and out): the mean of 3 calls
-                    r.trace(rays, any_hit=any_hit, reorder=reorder)
+                    # end to end through wf_trace (rays in and hits out in page-locked host
+                    # memory, copied by the call): the mean of 3 calls
+                    h_rays = torch.empty(len(rays) * 32, dtype=torch.uint8, pin_memory=True)
+                    h_rays.numpy()[:] = np.frombuffer(rays.tobytes(), np.uint8)
+                    h_hits = torch.empty(len(rays) * 20, dtype=torch.uint8, pin_memory=True)
+                    flags = (wf.abi.TRACE_ANY_HIT if any_hit else 0) | (wf.abi.TRACE_REORDER if reorder else 0)
+
+                    def call():
+                        wf.check(r.L.wf_trace(r.h, ctypes.c_void_p(h_rays.data_ptr()), len(rays),
+                                              ctypes.c_void_p(h_hits.data_ptr()), flags))
+                    call()
                     t1 = time.perf_counter()
                     for _ in range(3):
-                        r.trace(rays, any_hit=any_hit, reorder=reorder)
+                        call()
                     e2e_s = (time.perf_counter() - t1) / 3
+                    assert np.array_equal(h_hits.numpy().view(wf.abi.hit_dtype), hits)
                     res = {"rays": kind, "query": "any" if any_hit else "closest",
                            "order": "morton" if reorder else "as given", "n": len(rays), "ms": round(t, 3),
                            "mrays_per_s": round(len(rays) / (t / 1e3) / 1e6, 2),
