@@ -286,3 +286,45 @@ def test_loaded_scene_renders_like_the_oracle(tmp_path, orc):
     want[..., 3] = acc[..., 3]
     assert got[..., :3].mean() > 0.0
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def reference_helmet():
+    import os as _os
+    root = _os.environ.get("WF_REFERENCE_ROOT") or _os.path.join(
+        _os.path.dirname(_os.path.dirname(_os.path.abspath(__file__))), "..", "reference")
+    p = _os.path.join(root, "assets", "meshes", "damaged_helmet", "DamagedHelmet.gltf")
+    return p if _os.path.exists(p) else None
+
+
+@pytest.mark.skipif(not ref_assets.available() or reference_helmet() is None,
+                    reason="the reference checkout's DamagedHelmet or the reference loaders are not present")
+def test_reference_damaged_helmet_loads_like_the_reference():
+    """The reference's own asset (assets/meshes/damaged_helmet: glTF + .bin +
+    five JPEG textures) through gltf.load against cgltf as the reference reads
+    it: materials with their texture slots, the mesh's vertices and indices
+    bit for bit, the instance; its JPEG textures decode (wf_image_decode)
+    within 3/255 of the reference's stb_image."""
+    from tests.test_image_decode import stb_decode, STB
+    import os as _os
+    path = reference_helmet()
+    got = gltf.load(path)
+    ref = ref_assets.load(path)
+    assert len(got.materials) == len(ref.materials) == 1 and len(got.meshes) == len(ref.meshes) == 1
+    m, r = got.materials[0], ref.materials[0]
+    for key in ("base_color_factor", "emissive_factor"):
+        assert np.allclose(m[key], r[key])
+    assert [m[k] for k in ("base_color_image", "normal_image", "metallic_roughness_image",
+                           "emissive_image")] == r["images"]
+    (v, idx), (rv, ridx) = got.meshes[0], ref.meshes[0]
+    assert len(idx) > 10000 and np.array_equal(idx, ridx)
+    assert np.array_equal(v["position"], rv[:, 0:3]) and np.array_equal(v["normal"], rv[:, 3:6])
+    assert np.array_equal(v["uv"], rv[:, 6:8])
+    assert [(g, mat) for g, _, mat in got.instances] == [(rg, rmat) for rg, rmat, _ in ref.instances]
+    assert len(got.images) == 5
+    if _os.path.exists(STB):
+        import json
+        doc = json.load(open(path))
+        for k, im in enumerate(doc["images"]):
+            data = open(_os.path.join(_os.path.dirname(path), im["uri"]), "rb").read()
+            d = np.abs(got.images[k].astype(np.int16) - stb_decode(data, False).astype(np.int16))
+            assert d.max() <= 3 and d.mean() < 0.1, (im["uri"], d.max(), d.mean())

@@ -138,9 +138,9 @@ def _f16(m):
 
 
 def decode_image(data):
-    """A .jpg / .hdr / .dds file's contents decoded by wf_image_decode (host
-    only): (texels or BC blocks as a uint8 / float32 array, width, height,
-    wf_texture_format)."""
+    """A .jpg / .png / .hdr / .dds file's contents decoded by wf_image_decode
+    (host only): (texels or BC blocks as a uint8 / float32 array, width,
+    height, wf_texture_format)."""
     L = load()
     buf = np.frombuffer(bytes(data), dtype=np.uint8)
     w, h, f = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()

@@ -60,7 +60,7 @@ import zlib
 import numpy as np
 
 from .abi import vertex_dtype
-from .gltf import GltfScene, decode_png, submit  # noqa: F401  (submit is this module's too)
+from .gltf import GltfScene, decode_image_file, decode_png, submit  # noqa: F401  (submit is this module's too)
 
 _MAGIC = b"Kaydara FBX Binary  \x00"
 _ARRAY = {"f": np.float32, "d": np.float64, "l": np.int64, "i": np.int32, "b": np.uint8}
@@ -523,9 +523,9 @@ def load(path):
         if name not in images:
             images[name] = None
             full = os.path.join(base, name.replace("\\", os.sep))
-            if name.lower().endswith(".png") and os.path.exists(full):
+            if name.lower().endswith((".png", ".jpg", ".jpeg", ".dds")) and os.path.exists(full):
                 with open(full, "rb") as f:
-                    scene.images.append(decode_png(f.read()))
+                    scene.images.append(decode_image_file(f.read()))
                 images[name] = len(scene.images) - 1
         return images[name]
 

@@ -220,6 +220,26 @@ def _world_matrices(doc):
 
 # --------------------------------------------------------------------------- loading
 
+class BlockImage:
+    """An image kept as the file stores it for wf_texture_create (a DDS's BC
+    blocks or float texels): raw bytes / floats, size and format."""
+
+    def __init__(self, raw, width, height, fmt):
+        self.raw, self.width, self.height, self.format = raw, width, height, fmt
+
+
+def decode_image_file(data):
+    """A texture file's image as the reference's asset loader takes it
+    (asset_loader.cpp:56-206), decoded by the library (wf_image_decode): 8-bit
+    RGBA (PNG, JPEG, an RGBA8 DDS) as an h x w x 4 uint8 array, anything else
+    (BC blocks, float texels) as a BlockImage."""
+    from . import decode_image
+    raw, w, h, fmt = decode_image(bytes(data))
+    if fmt == TEXTURE_RGBA8:
+        return raw
+    return BlockImage(raw, w, h, fmt)
+
+
 class GltfScene:
     """meshes: one (vertices[vertex_dtype], uint32 indices) per primitive;
     images: h x w x 4 uint8 arrays; materials: dicts of factors and image
@@ -242,7 +262,7 @@ def load(path):
         else:
             with open(os.path.join(base, im["uri"]), "rb") as f:
                 data = f.read()
-        scene.images.append(decode_png(bytes(data)))
+        scene.images.append(decode_image_file(data))
     textures = doc.get("textures", [])
 
     def image_of(info):
@@ -317,6 +337,17 @@ class Submitted:
         self.instance_materials, self.transforms = instance_materials, transforms
 
 
+# the sRGB variant of a file's format, as colour textures load (dds.h:125-147)
+def _srgb_table():
+    from . import abi
+    return {abi.TEXTURE_RGBA8: abi.TEXTURE_RGBA8_SRGB, abi.TEXTURE_BC1: abi.TEXTURE_BC1_SRGB,
+            abi.TEXTURE_BC2: abi.TEXTURE_BC2_SRGB, abi.TEXTURE_BC3: abi.TEXTURE_BC3_SRGB,
+            abi.TEXTURE_BC7: abi.TEXTURE_BC7_SRGB}
+
+
+_SRGB = _srgb_table()
+
+
 def submit(renderer, scene, object_transform=None, bvh=None):
     """Creates the scene's textures and meshes in `renderer` and submits its
     instances (call between begin_scene and end_scene); returns a Submitted."""
@@ -328,7 +359,12 @@ def submit(renderer, scene, object_transform=None, bvh=None):
             return 0
         key = (image, srgb)
         if key not in tex_ids:
-            tex_ids[key] = renderer.create_texture(scene.images[image], TEXTURE_RGBA8_SRGB if srgb else TEXTURE_RGBA8)
+            im = scene.images[image]
+            if isinstance(im, BlockImage):
+                fmt = _SRGB.get(im.format, im.format) if srgb else im.format
+                tex_ids[key] = renderer.create_texture_raw(im.raw, im.width, im.height, fmt)
+            else:
+                tex_ids[key] = renderer.create_texture(im, TEXTURE_RGBA8_SRGB if srgb else TEXTURE_RGBA8)
         return tex_ids[key]
 
     mats = np.zeros(len(scene.materials) + 1, dtype=material_ext_dtype)
