@@ -53,7 +53,8 @@ def ngon_geometry(gid):
     return fw.geometry(gid, "ngon", pts, [list(range(8))], normals=[(0, 0, 1)] * 8, uvs=[(0, 0)] * 8)
 
 
-def write_scene(path, settings=None, version=7400, compress=False, with_normals=True):
+def write_scene(path, settings=None, version=7400, compress=False, with_normals=True,
+                textures=("tex.png", "spec.png")):
     objs = [cube_geometry(10, compress, with_normals), strip_geometry(11, compress), ngon_geometry(12),
             fw.model(20, "root", translation=(10, 20, 30), rotation=(10, 20, 30), scaling=(2, 2, 2)),
             fw.model(21, "child", translation=(5, 0, 0), rotation=(30, -45, 60), rotation_order=4,
@@ -65,7 +66,7 @@ def write_scene(path, settings=None, version=7400, compress=False, with_normals=
             fw.model(25, "ngon", rotation=(0, 0, 0), rotation_order=1, scaling=(3, 3, 3)),
             fw.material(30, "red", "phong", (1, 0, 0)), fw.material(31, "matte", "lambert", (0, 1, 0)),
             fw.material(32, "blue", "Phong", (0, 0, 1)),
-            fw.texture(40, "tex", "tex.png"), fw.texture(41, "spec", "spec.png")]
+            fw.texture(40, "tex", textures[0]), fw.texture(41, "spec", textures[1])]
     conns = [(20, 0), (21, 20), (22, 0), (23, 0), (24, 0), (25, 20),
              (10, 21), (30, 21), (31, 21),
              (11, 22), (11, 23), (11, 24), (32, 22), (32, 23),
@@ -119,6 +120,27 @@ def test_records_and_scene(files):
                      for k, a in enumerate(np.linspace(0, 2 * np.pi, 9)[:-1])]) * 0.01
     shoelace = 0.5 * abs(np.dot(ring[:, 0], np.roll(ring[:, 1], -1)) - np.dot(ring[:, 1], np.roll(ring[:, 0], -1)))
     assert area == pytest.approx(shoelace, rel=1e-5)
+
+
+def test_dds_and_png_textures(tmp_path, files):
+    """A phong material whose diffuse texture is a DDS of BC1 blocks (as the
+    reference's Sun Temple materials are) and whose specular texture is a
+    PNG: the DDS is kept as its blocks for wf_texture_create, the PNG
+    decoded."""
+    from tests.test_image_decode import dds_header
+    from wavefrontpathtracing_gb300 import abi
+    from wavefrontpathtracing_gb300.gltf import BlockImage
+    _, img = files
+    blocks = np.random.default_rng(3).integers(0, 256, 2 * 2 * 8, dtype=np.uint8)
+    (tmp_path / "diffuse.dds").write_bytes(dds_header(8, 8, fourcc=b"DXT1") + blocks.tobytes())
+    path = tmp_path / "dds.fbx"
+    write_scene(path, textures=("diffuse.dds", "spec.png"))
+    sc = fbx.load(path)
+    red = sc.materials[0]
+    im = sc.images[red["base_color_image"]]
+    assert isinstance(im, BlockImage) and im.format == abi.TEXTURE_BC1 and (im.width, im.height) == (8, 8)
+    assert np.array_equal(np.asarray(im.raw).reshape(-1), blocks)
+    assert np.array_equal(sc.images[red["metallic_roughness_image"]], img[::-1])
 
 
 def test_forms_agree(files):
@@ -197,16 +219,28 @@ def _linear_texels(rgba8):
 
 
 @pytest.mark.gpu
-def test_loaded_scene_renders_like_the_oracle(files, orc):
+@pytest.mark.parametrize("dds", [False, True])
+def test_loaded_scene_renders_like_the_oracle(files, orc, tmp_path, dds):
     """The loaded FBX scene through wf_texture_create / wf_mesh_create /
     wf_instance_submit_many, rendered against the oracle given the same
-    triangles, instances and texels, bit for bit."""
+    triangles, instances and texels, bit for bit; also with the diffuse
+    texture a DDS of BC1 blocks, expanded on the GPU (the oracle takes the
+    texels of its own block decoder)."""
     from wavefrontpathtracing_gb300 import Renderer, scenes
     from wavefrontpathtracing_gb300.abi import triangle_dtype
+    from wavefrontpathtracing_gb300.gltf import BlockImage
     from tests.helpers import oracle_scene_from_renderer
     from tests.test_gltf import srgb_texels
     paths, _ = files
-    sc = fbx.load(paths["zup_m"])
+    path = paths["zup_m"]
+    if dds:
+        from tests.test_image_decode import dds_header
+        blocks = np.random.default_rng(5).integers(0, 256, 2 * 2 * 8, dtype=np.uint8)
+        (tmp_path / "diffuse.dds").write_bytes(dds_header(8, 8, fourcc=b"DXT1") + blocks.tobytes())
+        path = tmp_path / "dds_scene.fbx"
+        write_scene(path, fw.global_settings(up=(2, 1), front=(1, -1), coord=(0, 1), unit=100.0),
+                    textures=("diffuse.dds", "spec.png"))
+    sc = fbx.load(path)
     pts = np.concatenate([(np.c_[sc.meshes[g][0]["position"], np.ones(len(sc.meshes[g][0]))] @ np.asarray(w).T)[:, :3]
                           for g, w, _ in sc.instances])
     lo, hi = pts.min(axis=0), pts.max(axis=0)
@@ -230,7 +264,10 @@ def test_loaded_scene_renders_like_the_oracle(files, orc):
         got = r.read_image()
     texels = [None] * len(done.texture_ids)
     for (image, srgb), tid in done.texture_ids.items():
-        texels[tid - 1] = srgb_texels(sc.images[image]) if srgb else _linear_texels(sc.images[image])
+        im = sc.images[image]
+        if isinstance(im, BlockImage):
+            im = orc.decode_bc(im.format, np.asarray(im.raw), im.width, im.height)
+        texels[tid - 1] = srgb_texels(im) if srgb else _linear_texels(im)
     osc.set_textures(texels)
     acc, _ = osc.render(view, 48, 40, max_bounces=3, spp=2, frame_seed=6, nee=1, rr_start_depth=2,
                         env_color=(0.3, 0.3, 0.3), threads=4)
