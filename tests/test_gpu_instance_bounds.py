@@ -70,3 +70,9 @@ def test_tight_instance_boxes(tlas_metric):
         assert np.array_equal(h0[f], h1[f]), f
     assert np.array_equal(h0["t"].view(np.uint32), h1["t"].view(np.uint32))
     assert np.array_equal(h0["bary"].view(np.uint32), h1["bary"].view(np.uint32))
+
+
+def test_unknown_instance_bounds_are_refused():
+    from wavefrontpathtracing_gb300 import WFError
+    with pytest.raises(WFError):
+        Renderer(8, 8, instance_bounds=2)
