@@ -173,7 +173,9 @@ enum wf_trace_flags {
     WF_TRACE_REORDER = 8u        /* trace the rays in the order of their origins' Morton codes in the
                                     scene box (a stable radix sort inside the call, timed with it):
                                     rays that start close together run together and share nodes in
-                                    L2; the hits, still at each ray's own index, do not change */
+                                    L2; the hits, still at each ray's own index, do not change.  The
+                                    sort is skipped when the input is already coherent (three in four
+                                    neighbouring rays start in one cell of a 16^3 grid) */
 };
 
 /* Counters and timings of the most recent wf_render / wf_trace call. */

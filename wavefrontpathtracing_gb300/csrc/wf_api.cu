@@ -1783,7 +1783,7 @@ int wf_trace_device(wf_ctx* c, const RayDesc2* rays, uint32_t n, hit_result_t* h
         StageTimer t(c, true, ST_EXTEND);
         WF_CUDA(launch_reorder_rays(reinterpret_cast<const float4*>(rays), n, c->tnodes.p, !c->scene_bi.empty(),
                                     c->sort_scratch.p, &perm, &varied, c->stream));
-        c->launches += 1 + 3 * 5;   // keys, then upsweep + 3 scan kernels + downsweep per pass
+        c->launches += 2 + 3 * 5;   // keys, the decision, then upsweep + 3 scan kernels + downsweep per pass
     }
     {
         StageTimer t(c, true, ST_EXTEND);

@@ -65,9 +65,11 @@ __device__ __forceinline__ uint32_t ray_key(const float4* __restrict__ rays, uin
 
 // Key = 24-bit Morton code of the origin in the scene box (clamped), value =
 // the ray's index.  Without a scene every key is 0 (the input order stays).
+// scattered counts the neighbouring rays (i, i + 1, within a warp's 32) whose
+// origins lie in different cells of a 16^3 grid over the scene box.
 __global__ void k_origin_keys(const float4* __restrict__ rays, uint32_t n, const float4* __restrict__ root,
                               bool has_scene, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                              uint32_t* __restrict__ varied) {
+                              uint32_t* __restrict__ varied, unsigned long long* __restrict__ scattered) {
     float3 lo = make_float3(0.f, 0.f, 0.f), inv = make_float3(0.f, 0.f, 0.f);
     if (has_scene) {
         const float4 a = root[0], b = root[1];
@@ -76,14 +78,34 @@ __global__ void k_origin_keys(const float4* __restrict__ rays, uint32_t n, const
         inv = make_float3(ex > 0.f ? 1.0f / ex : 0.f, ey > 0.f ? 1.0f / ey : 0.f, ez > 0.f ? 1.0f / ez : 0.f);
     }
     const uint32_t key0 = has_scene ? ray_key(rays, 0u, lo, inv) : 0u;
+    const uint32_t lane = threadIdx.x & 31u;
     bool differs = false;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t key = has_scene ? ray_key(rays, i, lo, inv) : 0u;
-        keys[i] = key;
-        vals[i] = i;
-        differs |= key != key0;
+    uint32_t far = 0;
+    // block-uniform loop, so that every lane takes part in the shuffles
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t key = valid && has_scene ? ray_key(rays, i, lo, inv) : 0u;
+        if (valid) {
+            keys[i] = key;
+            vals[i] = i;
+            differs |= key != key0;
+        }
+        const uint32_t next = __shfl_down_sync(0xffffffffu, key, 1);
+        const bool apart = valid && lane < 31u && i + 1u < n && ((key ^ next) >> 12) != 0u;
+        far += (uint32_t)__popc(__ballot_sync(0xffffffffu, apart));
     }
-    if (__any_sync(0xffffffffu, differs) && (threadIdx.x & 31u) == 0) atomicOr(varied, 1u);
+    if (__any_sync(0xffffffffu, differs) && lane == 0) atomicOr(varied, 1u);
+    if (lane == 0 && far) atomicAdd(scattered, (unsigned long long)far);
+}
+
+// The rays are sorted only when their origins are scattered: when fewer than
+// three in four neighbouring rays share a 16^3 cell, else the input order
+// stands (the sort would cost more than the locality it adds).
+__global__ void k_sort_decision(uint32_t* __restrict__ varied, const unsigned long long* __restrict__ scattered,
+                                uint32_t n) {
+    const unsigned long long pairs = (unsigned long long)n - (n + 31u) / 32u;
+    if (*varied && 4ull * *scattered < pairs) *varied = 0u;
 }
 
 // Digit counts of each tile: hist[digit * tiles + tile].
@@ -239,7 +261,7 @@ size_t reorder_scratch_words(uint32_t n) {
     const uint64_t tiles = (n + kTile - 1) / kTile;
     const uint64_t hist = (uint64_t)kRadix * tiles;
     const uint64_t sums = (hist + (uint64_t)kScanThreads * kScanItems - 1) / ((uint64_t)kScanThreads * kScanItems);
-    return 4ull * n + hist + sums + 1;
+    return 4ull * n + hist + sums + 4;   // + the flag, the scattered count (8-byte aligned)
 }
 
 cudaError_t launch_reorder_rays(const float4* rays, uint32_t n, const float4* root, bool has_scene,
@@ -252,10 +274,13 @@ cudaError_t launch_reorder_rays(const float4* rays, uint32_t n, const float4* ro
     uint32_t* v1 = k1 + n;
     uint32_t* hist = v1 + n;
     uint32_t* sums = hist + (size_t)kRadix * tiles;
-    uint32_t* varied = scratch + reorder_scratch_words(n) - 1;
-    cudaError_t e = cudaMemsetAsync(varied, 0, sizeof(uint32_t), stream);
+    const size_t words = reorder_scratch_words(n);
+    uint32_t* varied = scratch + words - 4;
+    unsigned long long* scattered = reinterpret_cast<unsigned long long*>(scratch + ((words - 2) & ~size_t(1)));
+    cudaError_t e = cudaMemsetAsync(varied, 0, 4 * sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
-    k_origin_keys<<<grid_for(n, 256), 256, 0, stream>>>(rays, n, root, has_scene, k0, v0, varied);
+    k_origin_keys<<<grid_for(n, 256), 256, 0, stream>>>(rays, n, root, has_scene, k0, v0, varied, scattered);
+    k_sort_decision<<<1, 1, 0, stream>>>(varied, scattered, n);
     e = cudaGetLastError();
     for (int pass = 0; pass < 3 && e == cudaSuccess; ++pass) {
         const int shift = 8 * pass;
