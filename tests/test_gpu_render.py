@@ -252,14 +252,18 @@ def test_checkpoint_resume_equals_uninterrupted_render(tmp_path):
             r.load_accumulator(path)
 
 
-@pytest.mark.parametrize("where,wave_paths", [("depth1", 0), ("middle", 0), ("middle", 1500)])
-def test_tail_kernel_equals_wavefront(orc, where, wave_paths):
+@pytest.mark.parametrize("where,wave_paths,fused", [("depth1", 0, False), ("middle", 0, False),
+                                                   ("middle", 1500, False), ("depth1", 0, True),
+                                                   ("middle", 0, True)])
+def test_tail_kernel_equals_wavefront(orc, where, wave_paths, fused):
     """The tail: once a wave's queue (projected from the previous wave's
     queue sizes) falls below tail_paths, its remaining bounces run one path per
     thread in one launch.  Same rays, same per-depth queue sizes, the same image
-    bit for bit as the stage-per-depth loop, in fewer launches."""
+    bit for bit as the stage-per-depth loop, in fewer launches; also under the
+    fused schedule, whose previous depth's shadow rays the tail would
+    otherwise never see traced."""
     desc = scenes.instanced_scene(width=64, height=36, instances=48, freqs=(6, 9), spp=2, max_bounces=6)
-    kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=3, wave_paths=wave_paths)
+    kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=3, wave_paths=wave_paths, fused_connect=fused)
     with Renderer(desc.width, desc.height) as r:
         load_scene_into(r, desc)
         r.render(frame_seed=41, accumulate=False, **kw)

@@ -1424,10 +1424,18 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
     bool pending = false;   // a connect on the side stream not yet joined
     for (uint32_t d = 0; d <= W.max_bounces; ++d) {
         if (d == tail) {
-            // connect at depth d - 1 has added its contributions first
+            // connect at depth d - 1 has added its contributions first (the
+            // fused schedule would have traced them with this depth's
+            // extension rays: trace them here)
             if (pending) {
                 WF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_conn[d - 1], 0));
                 pending = false;
+            }
+            if (P.fused && d >= 1) {
+                StageTimer t(c, P.prof, ST_CONNECT, nullptr, (int)(d - 1));
+                WF_CUDA(launch_connect(P.S, B, d - 1, W.npaths, false, c->totals + 1, c->stream));
+                c->launches++;
+                c->launches_connect++;
             }
             StageTimer t(c, P.prof, ST_TAIL);
             WF_CUDA(launch_megakernel_tail(P.S, P.SH, B, W, d, B.counts + 2 * kMaxDepth + d, c->totals, c->stream));
