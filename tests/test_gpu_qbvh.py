@@ -74,7 +74,9 @@ def test_quantized_layout_soup_hits_equal_oracle(orc):
 @pytest.mark.parametrize("name", ["instanced", "mixed_box"])
 def test_quantized_layout_render_equals_oracle_and_binary_layout(orc, name):
     """Every material, NEE and Russian roulette: the image equals the oracle's
-    (tie rule) bit for bit and the binary layout's image."""
+    (tie rule) bit for bit and the binary layout's image, with the shadow rays
+    in their own launches (both streams or the main one) or fused with the
+    next depth's extension rays."""
     if name == "instanced":
         desc, lit = scenes.instanced_scene(width=96, height=54, instances=96, freqs=(6, 9, 12, 15), spp=4), 0.01
     else:
@@ -88,6 +90,10 @@ def test_quantized_layout_render_equals_oracle_and_binary_layout(orc, name):
             r.render(**kw)
             imgs.append(r.read_image())
             if layout == 1:
+                # the fused and serial schedules trace the same rays over the quantized nodes
+                for sched in (dict(fused_connect=True), dict(serial_connect=True)):
+                    r.render(**kw, **sched)
+                    assert np.array_equal(r.read_image().view(np.uint32), imgs[0].view(np.uint32)), sched
                 acc, _ = sc.render(desc.view, w, h, max_bounces=8, spp=4, frame_seed=9, nee=1, rr_start_depth=3,
                                    threads=8, tie_rule=True)
                 want = np.zeros_like(acc)
