@@ -189,6 +189,9 @@ def ncu_traffic(rays_per_launch):
 
 # Instance world boxes of the main frame (wf_init_params.instance_bounds).
 DEFAULT_INSTANCE_BOUNDS = 1
+# Shadow rays traced with the next depth's extension rays from this depth on
+# (wf_render_options.fused_from_depth): 2 measured 1 % faster than 0 on the frame.
+DEFAULT_FUSED_FROM_DEPTH = 2
 
 
 def tlas_reference_leg(local, desc, steps, torch, l2buf):
@@ -528,7 +531,8 @@ def run_ours(args, rank, world, local):
 
     def frame(seed, profile):
         r.render(max_bounces=DEPTH, spp=SPP, frame_seed=seed, nee=1, rr_start_depth=RR, accumulate=False,
-                 profile=profile, fused_connect=args.fused_connect, tail_paths=args.tail_paths)
+                 profile=profile, fused_connect=args.fused_connect, tail_paths=args.tail_paths,
+                 fused_from_depth=args.fused_from_depth)
         return r.stats()
 
     for i in range(args.warmup):
@@ -588,11 +592,16 @@ def run_ours(args, rank, world, local):
     alg_bytes = (c["rays_extend"] * (B_RAY + B_HIT) + c["tlas_node_loads"] * B_TNODE + c["instance_loads"] * B_INST
                  + c["blas_node_loads"] * B_BNODE + c["triangle_tests"] * B_TRI)
     alg_bytes -= c["paths"] * B_RAY   # camera rays are made in the depth-0 launch, not read
-    if args.fused_connect:
-        # the traversal launches also carry the previous depth's shadow rays
-        alg_bytes += (c["rays_connect"] * B_SRAY + c["shadow_tlas_node_loads"] * B_TNODE
-                      + c["shadow_instance_loads"] * B_INST + c["shadow_blas_node_loads"] * B_BNODE
-                      + c["shadow_triangle_tests"] * B_TRI)
+    def shadow_bytes(d):
+        """Algorithmic bytes of the shadow rays of depth d (the counted pass)."""
+        f = c["shadow_fetch_depth"][d]
+        return (int(c["shadow_rays_depth"][d]) * B_SRAY + f[0] * B_TNODE + f[1] * B_INST + f[2] * B_BNODE
+                + f[3] * B_TRI)
+
+    # from this depth on, an extension launch also traces the previous depth's shadow rays
+    fuse_from = 1 if args.fused_connect else args.fused_from_depth
+    if fuse_from:
+        alg_bytes += sum(shadow_bytes(d - 1) for d in range(max(1, fuse_from), DEPTH + 1))
     # the launches measured are the staged extension launches: with a tail, the
     # rays of its depths (under 1 % of them on this frame) leave the count
     tail_d = int(last["tail_depth"])
@@ -607,9 +616,10 @@ def run_ours(args, rank, world, local):
     # per depth: the extension launches (depth 0 makes its camera rays) and the
     # shadow-ray launches, algorithmic bytes of the counted pass over the
     # timed frames' CUDA-event time of that depth's launch
-    def depth_rows(ext_ms_d, con_ms_d, frames):
+    def depth_rows(ext_ms_d, con_ms_d, frames, fuse_live):
         """Per depth: rays, algorithmic bytes (the counted pass) and the
-        CUDA-event time of the extension / shadow-ray launch of that depth."""
+        CUDA-event time of the extension / shadow-ray launch of that depth
+        (fuse_live: the frames fused shadow rays into the extension launches)."""
         ext_rows, con_rows = [], []
         for d in range(DEPTH + 1):
             n_d, f = int(c["extend_rays_depth"][d]), c["extend_fetch_depth"][d]
@@ -617,7 +627,11 @@ def run_ours(args, rank, world, local):
             if n_d and ms_d > 0:
                 b = (n_d * (B_HIT + (0 if d == 0 else B_RAY)) + f[0] * B_TNODE + f[1] * B_INST + f[2] * B_BNODE
                      + f[3] * B_TRI)
+                fused = fuse_live and fuse_from and d >= max(1, fuse_from)
+                if fused:
+                    b += shadow_bytes(d - 1)   # the launch also traced the shadow rays of depth d - 1
                 ext_rows.append({"depth": d, "rays": n_d, "alg_bytes": int(b), "ms": round(ms_d, 4),
+                                 **({"with_shadow_rays_of_depth": d - 1} if fused else {}),
                                  "achieved_gbs": round(b / (ms_d / 1e3) / 1e9, 1),
                                  "frac": round(b / (ms_d / 1e3) / 1e9 / peak, 4),
                                  "fetches_per_ray": round((f[0] + f[2]) / n_d, 1)})
@@ -639,11 +653,11 @@ def run_ours(args, rank, world, local):
         # the timed frames (shadow rays overlapping the next depth's extension
         # rays on a second stream, so each launch's time includes the other's
         # competition) ...
-        per_depth, con = depth_rows(ext_depth_ms, con_depth_ms, args.steps)
+        per_depth, con = depth_rows(ext_depth_ms, con_depth_ms, args.steps, True)
         secondary = total([x for x in per_depth if x["depth"] >= 1])
         connect = {"launches": con, **total(con)}
         # ... and the solo frames (every launch alone)
-        s_ext, s_con = depth_rows(solo_ext, solo_con, SOLO)
+        s_ext, s_con = depth_rows(solo_ext, solo_con, SOLO, False)
         solo = {"frames": SOLO, "schedule": "shadow rays on the main stream after shade (no overlap)",
                 "extend_per_depth": s_ext, "extend": total(s_ext),
                 "extend_secondary": total([x for x in s_ext if x["depth"] >= 1]),
@@ -668,7 +682,8 @@ def run_ours(args, rank, world, local):
         r.submit_render_meshes(inst_mesh, inst_xf, inst_mat)
         r.end_scene()
         r.render(max_bounces=DEPTH, spp=SPP, frame_seed=frame_seed(i, rank), nee=1, rr_start_depth=RR,
-                 accumulate=False, fused_connect=args.fused_connect, tail_paths=args.tail_paths)
+                 accumulate=False, fused_connect=args.fused_connect, tail_paths=args.tail_paths,
+                 fused_from_depth=args.fused_from_depth)
         wf.check(r.L.wf_read_image(r.h, wf.abi.ptr(img), img.size))
         s = r.stats()
         e2e_rays += s["rays_extend"] + s["rays_connect"]
@@ -739,6 +754,9 @@ def run_ours(args, rank, world, local):
                            "blas_layout": ["binary child pairs", "quantized 4-wide"][args.blas_layout],
                            "instance_bounds": ["transformed BLAS root box",
                                                "BLAS frontier boxes (tight)"][args.instance_bounds],
+                           "trace_schedule": ("fused" if args.fused_connect else
+                                              f"separate, shadow rays fused from depth {args.fused_from_depth}"
+                                              if args.fused_from_depth else "separate"),
                            "l2": "256 MiB buffer written between timed frames; working set > L2"},
                 "spp_per_s": round(spp_per_s, 3),
                 "rays_per_step": rays // args.steps,
@@ -762,6 +780,8 @@ def run_ours(args, rank, world, local):
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "roofline": {"bound": "hbm",
                              "kernel": ("k_trace_pair (extend d + shadow rays d-1)" if args.fused_connect
+                                        else f"k_trace (extend; from depth {args.fused_from_depth} with the "
+                                             f"shadow rays of the previous depth)" if args.fused_from_depth
                                         else "k_trace (extend)"),
                              "achieved": round(achieved, 1),
                              "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
@@ -993,6 +1013,9 @@ def main():
                          "(0 = never)")
     ap.add_argument("--fused-connect", action="store_true",
                     help="shadow rays of depth d in one launch with the extension rays of depth d + 1")
+    ap.add_argument("--fused-from-depth", type=int, default=DEFAULT_FUSED_FROM_DEPTH,
+                    help="separate schedule: from this depth on, each extension launch also traces the previous "
+                         "depth's shadow rays (0 = never)")
     ap.add_argument("--workload", default="instanced", choices=["instanced", "traversal", "batched"])
     ap.add_argument("--soup-triangles", type=int, default=8_000_000)
     ap.add_argument("--soup-side", type=int, default=4096, help="rays per set = side^2")

@@ -158,6 +158,12 @@ typedef struct wf_render_options {
      * 1080p instanced frame the tail from depth 4 took 2.0 ms against 1.5 ms
      * for the staged depths).  Images are identical either way. */
     uint32_t tail_paths;
+    /* WF_SCHEDULE_SEPARATE only: from this depth (>= 1) on, the extension
+     * launch of depth d also traces the shadow rays of depth d - 1, as the
+     * fused schedule does, while the earlier, larger queues keep their
+     * overlapped launches (one launch fewer per fused depth; the bench frame
+     * uses 2).  0 = never.  Images are identical. */
+    uint32_t fused_from_depth;
 } wf_render_options;
 
 enum wf_trace_schedule {

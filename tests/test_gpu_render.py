@@ -157,9 +157,9 @@ def test_megakernel_equals_wavefront(orc, name):
 def test_fused_and_separate_connect_agree(orc, wave_paths):
     """The shadow rays of depth d traced in their own launches on a second
     stream (the default), in one launch with the extension rays of depth
-    d + 1, or in their own launches on the main stream: the same rays, the
-    same image bit for bit, fewer launches when fused; an unknown schedule is
-    refused."""
+    d + 1, in their own launches on the main stream, or fused from depth 2
+    on: the same rays, the same image bit for bit, fewer launches when fused;
+    an unknown schedule is refused."""
     desc = scenes.instanced_scene(width=64, height=36, instances=48, freqs=(6, 9), spp=2, max_bounces=6)
     kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=3, wave_paths=wave_paths)
     with Renderer(desc.width, desc.height) as r:
@@ -173,6 +173,9 @@ def test_fused_and_separate_connect_agree(orc, wave_paths):
         r.render(frame_seed=33, accumulate=False, serial_connect=True, **kw)
         ser = r.read_image()
         sr = r.stats()
+        r.render(frame_seed=33, accumulate=False, fused_from_depth=2, **kw)
+        hyb = r.read_image()
+        sh = r.stats()
         with pytest.raises(wf.WFError):
             o = wf.abi.RenderOptions(1, 1, 0xFFFFFFFF, 0, 0, 0, 3)
             s = wf.abi.RenderSettings(1, 1, 0, 2, 1, 0, 1.0)
@@ -180,9 +183,12 @@ def test_fused_and_separate_connect_agree(orc, wave_paths):
     assert sf["rays_connect"] > 0
     assert_images_equal(fused, sep)
     assert_images_equal(ser, sep)
+    assert_images_equal(hyb, sep)
     for k in ("rays_extend", "rays_connect", "extend_rays_depth", "shadow_rays_depth"):
         assert np.array_equal(np.asarray(sf[k]), np.asarray(ss[k])), k
         assert np.array_equal(np.asarray(sr[k]), np.asarray(ss[k])), k
+        assert np.array_equal(np.asarray(sh[k]), np.asarray(ss[k])), k
+    assert sf["launches"] < sh["launches"] < ss["launches"]
     assert sf["launches"] < ss["launches"]
 
 
@@ -254,7 +260,7 @@ def test_checkpoint_resume_equals_uninterrupted_render(tmp_path):
 
 @pytest.mark.parametrize("where,wave_paths,fused", [("depth1", 0, False), ("middle", 0, False),
                                                    ("middle", 1500, False), ("depth1", 0, True),
-                                                   ("middle", 0, True)])
+                                                   ("middle", 0, True), ("middle", 1500, "from2")])
 def test_tail_kernel_equals_wavefront(orc, where, wave_paths, fused):
     """The tail: once a wave's queue (projected from the previous wave's
     queue sizes) falls below tail_paths, its remaining bounces run one path per
@@ -263,7 +269,8 @@ def test_tail_kernel_equals_wavefront(orc, where, wave_paths, fused):
     fused schedule, whose previous depth's shadow rays the tail would
     otherwise never see traced."""
     desc = scenes.instanced_scene(width=64, height=36, instances=48, freqs=(6, 9), spp=2, max_bounces=6)
-    kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=3, wave_paths=wave_paths, fused_connect=fused)
+    kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=3, wave_paths=wave_paths, fused_connect=fused is True,
+              fused_from_depth=2 if fused == "from2" else 0)
     with Renderer(desc.width, desc.height) as r:
         load_scene_into(r, desc)
         r.render(frame_seed=41, accumulate=False, **kw)

@@ -346,18 +346,21 @@ class Renderer:
     # ---- rendering
     def render(self, max_bounces=3, spp=1, frame_seed=1, nee=0, rr_start_depth=0xFFFFFFFF, accumulate=True,
                cosine=1, env_strength=1.0, wave_paths=0, profile=False, count_traffic=False, view_mode=0,
-               megakernel=False, fused_connect=False, tail_paths=0, serial_connect=False):
+               megakernel=False, fused_connect=False, tail_paths=0, serial_connect=False, fused_from_depth=0):
         """megakernel: whole paths per thread (use_wavefront_pathtracing = 0), the A/B comparator.
         fused_connect: the shadow rays of depth d in one launch with the extension rays of depth d + 1
         (instead of their own launch on a second stream).
         serial_connect: the shadow rays' launches on the main stream after shade (no
         overlap; per-kernel timings).
+        fused_from_depth: with the separate schedule, from this depth on each extension
+        launch also traces the previous depth's shadow rays (0 = never).
         tail_paths: queue size below which a wave's remaining bounces run per path in one launch
         (0 = never)."""
         s = RenderSettings(0 if megakernel else 1, 1, view_mode, max_bounces, cosine, int(accumulate), env_strength)
         o = RenderOptions(spp, nee, rr_start_depth, wave_paths, int(profile), int(count_traffic),
                           abi.SCHEDULE_FUSED if fused_connect else
-                          abi.SCHEDULE_SERIAL if serial_connect else abi.SCHEDULE_SEPARATE, tail_paths)
+                          abi.SCHEDULE_SERIAL if serial_connect else abi.SCHEDULE_SEPARATE, tail_paths,
+                          fused_from_depth)
         check(self.L.wf_render(self.h, ctypes.byref(s), ctypes.byref(o), frame_seed))
 
     # ---- differentiable rendering

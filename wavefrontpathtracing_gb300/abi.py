@@ -83,7 +83,7 @@ class RenderOptions(ctypes.Structure):
     _fields_ = [("spp", ctypes.c_uint32), ("nee", ctypes.c_uint32), ("rr_start_depth", ctypes.c_uint32),
                 ("wave_paths", ctypes.c_uint32), ("profile", ctypes.c_uint32),
                 ("count_traffic", ctypes.c_uint32), ("trace_schedule", ctypes.c_uint32),
-                ("tail_paths", ctypes.c_uint32)]
+                ("tail_paths", ctypes.c_uint32), ("fused_from_depth", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):

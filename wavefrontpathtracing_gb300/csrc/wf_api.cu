@@ -1299,6 +1299,7 @@ struct Pass {
     ShadeRefs SH;
     RenderBuffers B;
     bool nee, prof, cnt, mega, fused, serial;
+    uint32_t fuse_from;   // separate schedule: from this depth (>= 1) on, as fused; 0 = never
     uint32_t tail_paths;
 };
 
@@ -1366,6 +1367,7 @@ Pass make_pass(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     // traffic counting keeps per-kind counters, so it traces the kinds apart
     P.fused = P.nee && !P.cnt && o->trace_schedule == WF_SCHEDULE_FUSED;
     P.serial = o->trace_schedule == WF_SCHEDULE_SERIAL;
+    P.fuse_from = (P.nee && !P.cnt && o->trace_schedule == WF_SCHEDULE_SEPARATE) ? o->fused_from_depth : 0u;
     P.tail_paths = o->tail_paths;
     return P;
 }
@@ -1399,6 +1401,8 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
     // the depth from which the tail kernel finishes the wave: the first depth
     // whose queue, projected from the last wave's sizes, is below tail_paths
     uint32_t tail = kMaxDepth;
+    // whether the extension launch of depth d also traces the shadow rays of d - 1
+    auto fused_at = [&](uint32_t d) { return P.fused || (P.fuse_from != 0 && d >= P.fuse_from && !A.g_em_rep); };
     if (c->counts_pending) {
         const cudaError_t q = cudaEventQuery(c->ev_counts);
         if (q == cudaSuccess) {
@@ -1424,18 +1428,12 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
     bool pending = false;   // a connect on the side stream not yet joined
     for (uint32_t d = 0; d <= W.max_bounces; ++d) {
         if (d == tail) {
-            // connect at depth d - 1 has added its contributions first (the
-            // fused schedule would have traced them with this depth's
-            // extension rays: trace them here)
+            // connect at depth d - 1 has added its contributions first (also
+            // under the fused schedule: no extension launch of this depth
+            // takes them, so they had their own launch)
             if (pending) {
                 WF_CUDA(cudaStreamWaitEvent(c->stream, c->ev_conn[d - 1], 0));
                 pending = false;
-            }
-            if (P.fused && d >= 1) {
-                StageTimer t(c, P.prof, ST_CONNECT, nullptr, (int)(d - 1));
-                WF_CUDA(launch_connect(P.S, B, d - 1, W.npaths, false, c->totals + 1, c->stream));
-                c->launches++;
-                c->launches_connect++;
             }
             StageTimer t(c, P.prof, ST_TAIL);
             WF_CUDA(launch_megakernel_tail(P.S, P.SH, B, W, d, B.counts + 2 * kMaxDepth + d, c->totals, c->stream));
@@ -1446,7 +1444,7 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
         if (d == 0) {
             StageTimer t(c, P.prof, ST_EXTEND, nullptr, (int)d);
             WF_CUDA(launch_extend_camera(P.S, B, W, P.cnt, c->totals, c->stream));
-        } else if (P.fused) {
+        } else if (fused_at(d)) {
             // the shadow rays of depth d - 1 with the extension rays of depth d
             StageTimer t(c, P.prof, ST_EXTEND, nullptr, (int)d);
             WF_CUDA(launch_trace_pair(P.S, B, d, c->totals, c->stream));
@@ -1466,7 +1464,10 @@ int run_wave(wf_ctx* c, Pass& P, const Wave& wv, uint32_t sample_base, const Adj
         }
         c->launches += 2;
         c->launches_extend++;
-        if (P.nee && !P.fused && d < W.max_bounces) {
+        // the shadow rays of depth d: their own launch unless the extension
+        // launch of depth d + 1 takes them (the fused schedule, when depth
+        // d + 1 is not the tail's)
+        if (P.nee && !(fused_at(d + 1) && d + 1 < tail) && d < W.max_bounces) {
             // the shadow rays of depth d overlap the extension rays of depth d + 1
             // (the serial schedule keeps them on the main stream)
             cudaStream_t cs = P.serial ? c->stream : c->side;
@@ -1576,6 +1577,7 @@ int wf_adjoint(wf_ctx* c, const render_settings_t* s, const wf_render_options* o
     const uint32_t wave = o->wave_paths ? std::min(o->wave_paths, c->capacity) : c->capacity;
     Pass P = make_pass(c, s, o, frame_seed);
     P.fused = false;   // the replay's shadow rays need their own launches (AdjConnectIO)
+    P.fuse_from = 0;
     P.cnt = false;
     P.tail_paths = 0;
     P.B.ps_Lc = c->L_comp.p;   // both passes keep the radiance sums' rounding errors
