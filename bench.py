@@ -751,7 +751,7 @@ def run_ours(args, rank, world, local):
                            "triangles": desc.triangle_count,
                            "instanced_triangles": desc.instanced_triangle_count, "instances": len(desc.instances),
                            "tlas_metric": ["reference", "merged-box walk", "parallel clustering"][args.tlas_metric],
-                           "blas_layout": ["binary child pairs", "quantized 4-wide"][args.blas_layout],
+                           "blas_layout": ["binary child pairs", "quantized 4-wide", "exact 4-wide"][args.blas_layout],
                            "instance_bounds": ["transformed BLAS root box",
                                                "BLAS frontier boxes (tight)"][args.instance_bounds],
                            "trace_schedule": ("fused" if args.fused_connect else
@@ -993,9 +993,10 @@ def main():
     ap.add_argument("--tlas-metric", type=int, default=2,
                     help="TLAS build: 0 = reference walk and metric, 1 = merged-box walk, 2 = parallel clustering")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--blas-layout", type=int, default=0, choices=[0, 1],
+    ap.add_argument("--blas-layout", type=int, default=0, choices=[0, 1, 2],
                     help="BLAS layout the traversal reads: 0 = the reference's binary child pairs, 1 = quantized "
-                         "4-wide nodes (order-independent tie rule for closest hits)")
+                         "4-wide nodes, 2 = exact 4-wide nodes (both 4-wide: order-independent tie rule for "
+                         "closest hits)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rendering leg")

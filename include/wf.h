@@ -58,12 +58,13 @@ typedef struct wf_init_params {
      * pairs of 32-byte nodes (bvh_node_t) walked in the reference's order;
      * 1 = the same tree collapsed to 4-wide 64-byte nodes with child boxes
      * quantized to 8 bits per plane (conservatively: each contains its exact
-     * box), half the dependent steps per ray.  With 1, closest hits follow an
-     * order-independent tie rule (smallest t, then smallest (instance,
-     * primitive)) instead of "the first of equal-t hits visited": hits differ
-     * from layout 0 only on exact-t ties.  The megakernel, the fused trace
-     * schedule's shadow rays and the batched pipeline read the binary nodes
-     * (kept in both layouts). */
+     * box), half the dependent steps per ray; 2 = the same 4-wide nodes with
+     * exact float boxes, 128 bytes each (no decoding, two 64-byte lines per
+     * step).  With 1 and 2, closest hits follow an order-independent tie rule
+     * (smallest t, then smallest (instance, primitive)) instead of "the first
+     * of equal-t hits visited": hits differ from layout 0 only on exact-t
+     * ties.  The megakernel and the batched pipeline read the binary nodes
+     * (kept in every layout). */
     uint32_t blas_layout;
     /* world box of each instance, the TLAS's leaf box: 0 = the world box of
      * the 8 transformed corners of the BLAS root box (renderer.cpp:1324-1336);
@@ -434,6 +435,15 @@ int wf_tlas_build(wf_ctx* ctx, const bvh_instance_t* instances, uint32_t instanc
  * counterpart in the reference (its BLAS is binary). */
 int wf_bvh_quantize(const void* blob, uint64_t blob_size, void* out_nodes, uint64_t* inout_size,
                     uint32_t* out_root_count);
+/* The exact 4-wide nodes (wf_init_params.blas_layout = 2) of a BLAS blob, on
+ * the host: 128 bytes per node (8 x float4: the four children's lo x / hi x /
+ * lo y / hi y / lo z / hi z planes as float4 lanes, child[4] = node index or
+ * a leaf's first triangle in leaf order, count[4] = leaf triangle counts with
+ * the child count in count[0]'s top byte) into out_nodes (NULL = size query
+ * through *inout_size); *out_root_count as wf_bvh_quantize.  No counterpart
+ * in the reference (its BLAS is binary). */
+int wf_bvh_widen(const void* blob, uint64_t blob_size, void* out_nodes, uint64_t* inout_size,
+                 uint32_t* out_root_count);
 
 /* ---- image files (asset_loader.cpp:56-206) -----------------------------
  * Decodes a .jpg / .jpeg (baseline or progressive) or a .png (every colour

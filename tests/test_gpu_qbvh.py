@@ -1,4 +1,5 @@
-"""GPU parity of the quantized 4-wide BLAS layout (wf_init_params.blas_layout = 1).
+"""GPU parity of the 4-wide BLAS layouts (wf_init_params.blas_layout = 1:
+quantized, 2: exact).
 
 The traversal reads 64-byte nodes of up to four children with 8-bit planes
 (csrc/wf_qbvh.cu) and takes closest hits by the order-independent tie rule
@@ -33,10 +34,11 @@ CASES = {
 
 
 @pytest.mark.parametrize("name", list(CASES))
-def test_quantized_layout_hits_equal_oracle(orc, name):
+@pytest.mark.parametrize("layout", [1, 2])
+def test_quantized_layout_hits_equal_oracle(orc, name, layout):
     make, lo, hi = CASES[name]
     desc = make()
-    r, sc = scene_pair(orc, desc, 1)
+    r, sc = scene_pair(orc, desc, layout)
     try:
         rays = np.concatenate([orc.primary_rays(desc.view, desc.width, desc.height), random_rays(30000, lo, hi, 4)])
         want, _, ovf = sc.trace(rays, flags=orc.TIE_RULE, threads=8)
@@ -55,12 +57,13 @@ def test_quantized_layout_hits_equal_oracle(orc, name):
         r.close()
 
 
-def test_quantized_layout_soup_hits_equal_oracle(orc):
+@pytest.mark.parametrize("layout", [1, 2])
+def test_quantized_layout_soup_hits_equal_oracle(orc, layout):
     soup = scenes.triangle_soup(300_000, seed=11)
     desc = scenes.SceneDesc("soup", [soup], [(0, np.eye(4), scenes.material())],
                             scenes.make_view((0.5, 0.5, -0.5), (0.5, 0.5, 0.5), 90.0, 16, 16), 16, 16,
                             dict(env=(0, 0, 0)), dict(interval_count=16, subdivide_single_prim=0, max_leaf_prims=4))
-    r, sc = scene_pair(orc, desc, 1)
+    r, sc = scene_pair(orc, desc, layout)
     try:
         for kind in ("coherent", "incoherent"):
             rays = scenes.soup_rays(160, seed=7, kind=kind)
@@ -71,8 +74,9 @@ def test_quantized_layout_soup_hits_equal_oracle(orc):
         r.close()
 
 
+@pytest.mark.parametrize("layout", [1, 2])
 @pytest.mark.parametrize("name", ["instanced", "mixed_box"])
-def test_quantized_layout_render_equals_oracle_and_binary_layout(orc, name):
+def test_quantized_layout_render_equals_oracle_and_binary_layout(orc, name, layout):
     """Every material, NEE and Russian roulette: the image equals the oracle's
     (tie rule) bit for bit and the binary layout's image, with the shadow rays
     in their own launches (both streams or the main one) or fused with the
@@ -84,12 +88,12 @@ def test_quantized_layout_render_equals_oracle_and_binary_layout(orc, name):
     w, h = desc.width, desc.height
     kw = dict(max_bounces=8, spp=4, frame_seed=9, nee=1, rr_start_depth=3, accumulate=False)
     imgs = []
-    for layout in (1, 0):
-        r, sc = scene_pair(orc, desc, layout)
+    for lay in (layout, 0):
+        r, sc = scene_pair(orc, desc, lay)
         try:
             r.render(**kw)
             imgs.append(r.read_image())
-            if layout == 1:
+            if lay != 0:
                 # the fused and serial schedules trace the same rays over the quantized nodes
                 for sched in (dict(fused_connect=True), dict(serial_connect=True)):
                     r.render(**kw, **sched)

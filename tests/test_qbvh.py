@@ -43,8 +43,22 @@ def decode(words, k):
     return kids
 
 
-def check_blob(blob):
-    words, root_count = wf.bvh_quantize(blob)
+def decode_exact(words, k):
+    w = words[32 * k:32 * k + 32]
+    planes = w[0:24].view(np.float32).reshape(3, 2, 4)   # axis, lo / hi, child
+    nch = int(w[28]) >> 24
+    kids = []
+    for i in range(nch):
+        lo = np.array([planes[a, 0, i] for a in range(3)], np.float32)
+        hi = np.array([planes[a, 1, i] for a in range(3)], np.float32)
+        count = int(w[28 + i]) & (0x00FFFFFF if i == 0 else 0xFFFFFFFF)
+        kids.append((lo, hi, int(w[24 + i]), count))
+    return kids
+
+
+def check_blob(blob, exact=False):
+    words, root_count = (wf.bvh_widen if exact else wf.bvh_quantize)(blob)
+    stride = 32 if exact else 16
     mn, mx, lf, pc = binary_nodes(blob)
     if pc[0] > 0:
         assert root_count == pc[0] and len(words) == 0
@@ -60,10 +74,14 @@ def check_blob(blob):
                 kids_b.append(c)
             else:
                 kids_b += [lf[c], lf[c] + 1]
-        kids_q = decode(words, qk)
+        kids_q = (decode_exact if exact else decode)(words, qk)
         assert len(kids_q) == len(kids_b)
         for (lo, hi, child, count), b in zip(kids_q, kids_b):
-            assert np.all(lo <= mn[b]) and np.all(hi >= mx[b]), (lo, mn[b], hi, mx[b])
+            if exact:   # the binary boxes, bit for bit
+                assert np.array_equal(lo.view(np.uint32), mn[b].view(np.uint32))
+                assert np.array_equal(hi.view(np.uint32), mx[b].view(np.uint32))
+            else:       # quantized outward
+                assert np.all(lo <= mn[b]) and np.all(hi >= mx[b]), (lo, mn[b], hi, mx[b])
             assert count == pc[b]
             if pc[b] > 0:
                 assert child == lf[b]
@@ -74,15 +92,19 @@ def check_blob(blob):
                 walk(b, child)
 
     walk(0, 0)
-    assert len(words) == 16 * len(order)
+    assert len(words) == stride * len(order)
     leaves = np.nonzero(pc > 0)[0]
     # node 1 is the reference's unused slot; every other leaf once
     assert sorted(seen_leaves) == sorted(x for x in leaves if x != 1)
     return len(order)
 
 
+@pytest.mark.parametrize("exact", [False, True])
 @pytest.mark.parametrize("name", ["box", "instanced", "soup"])
-def test_quantized_boxes_contain_the_exact_boxes(orc, name):
+def test_quantized_boxes_contain_the_exact_boxes(orc, name, exact):
+    """Both 4-wide layouts reference every binary leaf once with its triangle
+    range; the quantized boxes contain the exact ones, the exact layout's
+    boxes are the binary ones bit for bit."""
     if name == "box":
         meshes = scenes.box_scene(width=8, height=8).meshes
     elif name == "instanced":
@@ -92,7 +114,7 @@ def test_quantized_boxes_contain_the_exact_boxes(orc, name):
     for t in meshes:
         for bins, leaf in ((16, 4), (8, 0)):
             blob = orc.bvh_build(t, bins, False, leaf)
-            n = check_blob(blob)
+            n = check_blob(blob, exact)
             if len(t) > 8:
                 assert n > 0
 
@@ -100,14 +122,17 @@ def test_quantized_boxes_contain_the_exact_boxes(orc, name):
 def test_single_leaf_blas_has_no_nodes(orc):
     t = scenes.quad((0, 0, 0), (1, 0, 0), (0, 1, 0))
     blob = orc.bvh_build(t, 8, False, 0)
-    words, root_count = wf.bvh_quantize(blob)
-    assert len(words) == 0 and root_count == 2
+    for fn in (wf.bvh_quantize, wf.bvh_widen):
+        words, root_count = fn(blob)
+        assert len(words) == 0 and root_count == 2
 
 
 def test_rejects_a_truncated_blob(orc):
     blob = orc.bvh_build(scenes.icosphere(4), 16, False, 4)
     with pytest.raises(wf.WFError):
         wf.bvh_quantize(blob[:20])
+    with pytest.raises(wf.WFError):
+        wf.bvh_widen(blob[:20])
 
 
 def test_tie_rule_changes_no_hit_on_the_configurations(orc):

@@ -69,6 +69,7 @@ SIGNATURES = {
     "wf_tlas_build": [_vp, _vp, _u32, _vp, _pu64],
     "wf_tlas_build_noalloc": [_vp, _u32, _vp, _u32, _vp],
     "wf_bvh_quantize": [_vp, _u64, _vp, _pu64, _pu32],
+    "wf_bvh_widen": [_vp, _u64, _vp, _pu64, _pu32],
     "wf_image_decode": [_vp, _u64, _pu32, _pu32, _pu32, _vp, _pu64],
     "wf_texture_read": [_vp, _u32, _vp, _u64],
     "wf_scene_triangle_count": [_vp, _pu64],
@@ -173,12 +174,25 @@ def bvh_quantize(blob):
     return out[:n.value // 4], rc_root.value
 
 
+def bvh_widen(blob):
+    """The exact 4-wide nodes of a BLAS blob (wf_bvh_widen; host only):
+    (uint32 array of 32 words per node, root leaf triangle count)."""
+    L = load()
+    blob = np.ascontiguousarray(blob, dtype=np.uint8)
+    n = ctypes.c_uint64(0)
+    rc_root = ctypes.c_uint32(0)
+    check(L.wf_bvh_widen(ptr(blob), blob.nbytes, None, ctypes.byref(n), ctypes.byref(rc_root)))
+    out = np.zeros(max(1, n.value // 4), dtype=np.uint32)
+    check(L.wf_bvh_widen(ptr(blob), blob.nbytes, ptr(out), ctypes.byref(n), ctypes.byref(rc_root)))
+    return out[:n.value // 4], rc_root.value
+
+
 class Renderer:
     """One wf_ctx: a CUDA device, its stream and all device memory."""
 
     def __init__(self, width, height, device=0, wave_capacity=0, tlas_metric=0, blas_layout=0, instance_bounds=0):
-        """blas_layout 1: the traversal reads the quantized 4-wide BLAS nodes
-        (with the order-independent tie rule for closest hits).
+        """blas_layout 1 / 2: the traversal reads the quantized / exact 4-wide
+        BLAS nodes (with the order-independent tie rule for closest hits).
         instance_bounds 1: instance world boxes from the BLAS frontier boxes
         (tighter TLAS leaves) instead of the transformed root box."""
         L = load()

@@ -379,16 +379,18 @@ int upload_hull(wf_ctx* c, Mesh& m) {
     return WF_OK;
 }
 
-// The quantized 4-wide nodes of the mesh's BLAS (blas_layout 1), from its blob.
+// The 4-wide nodes of the mesh's BLAS (blas_layout 1: quantized, 64 bytes;
+// 2: exact, 128 bytes), from its blob.
 int upload_qnodes(wf_ctx* c, Mesh& m) {
-    if (c->blas_layout != 1) return WF_OK;
+    if (c->blas_layout == 0) return WF_OK;
     std::vector<uint32_t> words;
     const char* err = nullptr;
-    int rc = qbvh_convert(m.blob.data(), m.blob.size(), words, &m.root_count, &err);
+    const bool exact = c->blas_layout == 2;
+    int rc = qbvh_convert(m.blob.data(), m.blob.size(), words, &m.root_count, &err, exact);
     if (rc) return fail(rc, err);
-    m.qnode_count = (uint32_t)(words.size() / 16);
+    m.qnode_count = (uint32_t)(words.size() / (exact ? 32 : 16));
     if (m.qnode_count == 0) return WF_OK;
-    if ((rc = dev_alloc(&m.d_qnodes, 4ull * m.qnode_count))) return rc;
+    if ((rc = dev_alloc(&m.d_qnodes, words.size() / 4))) return rc;
     WF_CUDA(h2d(c, m.d_qnodes, words.data(), words.size() * 4));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     return WF_OK;
@@ -499,7 +501,7 @@ SceneRefs scene_refs(wf_ctx* c) {
     S.tnode_count = 2u * S.inst_count;
     S.mesh_count = (uint32_t)c->meshes.size();
     S.status = c->status;
-    S.qbvh = c->blas_layout == 1 ? 1u : 0u;
+    S.qbvh = c->blas_layout;
     return S;
 }
 
@@ -832,9 +834,9 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
         return fail(WF_ERR_INVALID, "wf_create: tlas_metric must be 0, 1 or 2");
     }
     c->tlas_metric = p->tlas_metric;
-    if (p->blas_layout > 1) {
+    if (p->blas_layout > 2) {
         delete c;
-        return fail(WF_ERR_INVALID, "wf_create: blas_layout must be 0 or 1");
+        return fail(WF_ERR_INVALID, "wf_create: blas_layout must be 0, 1 or 2");
     }
     if (p->instance_bounds > 1) {
         delete c;

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kTraceBlock, WF_TRACE_MIN_BLOCKS) k_btrace(Sce
     if (n == 0) return;
     LocalCounters lc = {0, 0, 0, 0};
     bool overflow = false;
-    trace_persistent<ANY, false, false>(S, io, n, fetch, lc, overflow);   // the binary BLAS layout
+    trace_persistent<ANY, false, 0>(S, io, n, fetch, lc, overflow);   // the binary BLAS layout
     if (overflow) atomicOr(status, ERRF_STACK);
 }
 

@@ -40,8 +40,9 @@ struct BlasRef {
     const float4* nodes;
     const float4* tris;
     uint32_t node_count, tri_count;   // read by checked builds only
-    // the quantized 4-wide layout (wf_init_params.blas_layout = 1; csrc/wf_qbvh.cu):
-    // 4 float4 per node; root_count = the triangles of a BLAS that is one leaf
+    // the 4-wide layouts (wf_init_params.blas_layout = 1 / 2; csrc/wf_qbvh.cu):
+    // 4 (quantized) or 8 (exact) float4 per node; root_count = the triangles of
+    // a BLAS that is one leaf
     const float4* qnodes = nullptr;
     uint32_t qnode_count = 0, root_count = 0;
 };
@@ -53,7 +54,7 @@ struct SceneRefs {
     uint32_t inst_count;
     uint32_t tnode_count, mesh_count;   // checked builds: bounds of the indices above
     uint32_t* status;                   // checked builds: where ERRF_BOUNDS is raised
-    uint32_t qbvh = 0;                  // 1: BLAS traversal over the quantized 4-wide nodes, tie rule
+    uint32_t qbvh = 0;                  // BLAS layout: 1 / 2 = the quantized / exact 4-wide nodes, tie rule
 };
 
 constexpr int kInstRows = 7;   // float4 rows per instance in the shading table

@@ -192,6 +192,6 @@ cudaError_t launch_decode_bc(const uint8_t* d_blocks, uint32_t format, uint32_t 
 // The quantized 4-wide nodes of a BLAS blob (csrc/wf_qbvh.cu): 16 words per
 // node; *root_count = the triangles of a single-leaf BLAS (no nodes), else 0.
 int qbvh_convert(const uint8_t* blob, uint64_t size, std::vector<uint32_t>& out, uint32_t* root_count,
-                 const char** error);
+                 const char** error, bool exact = false);
 
 }  // namespace wf

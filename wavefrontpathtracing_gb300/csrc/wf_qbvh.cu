@@ -24,6 +24,15 @@
 // these boxes therefore visits every leaf the exact boxes would, and with the
 // order-independent tie rule (closest hit = smallest t, then smallest
 // (instance, primitive)) its hits equal those of the exact binary traversal.
+//
+// The exact 4-wide layout (blas_layout = 2) collapses the same levels without
+// quantizing: 128 bytes per node (8 x float4: the four children's lo_x, hi_x,
+// lo_y, hi_y, lo_z, hi_z planes as float4 lanes, then child[4], then
+// count[4] with the child count in count[0]'s top byte), so a step tests four
+// exact boxes for two 64-byte lines and no decoding.  A grandchild's box lies
+// inside its parent's in float as well (the same coordinates, and rounding is
+// monotone), so skipping the parent's test only adds visits, and with the tie
+// rule the hits equal the binary traversal's.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -89,8 +98,10 @@ bool quantize_axis(float origin, float pmax, const float* cmin, const float* cma
 struct Converter {
     const uint8_t* nodes;
     uint64_t node_count;
-    std::vector<uint32_t> words;   // 16 words per node
+    bool exact = false;            // the exact layout (32 words per node) instead of the quantized one
+    std::vector<uint32_t> words;   // 16 (quantized) or 32 (exact) words per node
     const char* error = nullptr;
+    uint32_t stride() const { return exact ? 32u : 16u; }
 
     BNode get(uint32_t i) const {
         BNode b;
@@ -101,8 +112,8 @@ struct Converter {
     // Emits the node for binary interior node bi; returns its index.
     uint32_t emit(uint32_t bi, int depth) {
         if (depth > 64) { error = "BLAS deeper than the traversal stack"; return 0; }
-        const uint32_t me = (uint32_t)(words.size() / 16);
-        words.resize(words.size() + 16, 0u);
+        const uint32_t me = (uint32_t)(words.size() / stride());
+        words.resize(words.size() + stride(), 0u);
         const BNode p = get(bi);
         uint32_t kid[4];
         int n = 0;
@@ -126,6 +137,23 @@ struct Converter {
             if (b.prim_count > 0xFFFFu) { error = "a BLAS leaf holds more than 65535 triangles"; return 0; }
             // a leaf's first triangle; an interior child's own binary index (emitted below)
             entry[i] = b.prim_count > 0 ? b.left_first : kid[i];
+        }
+        if (exact) {
+            for (int i = 0; i < n; ++i)
+                if (count[i] == 0) entry[i] = emit(entry[i], depth + 1);
+            if (error) return 0;
+            uint32_t* w = words.data() + 32ull * me;
+            for (int i = 0; i < 4; ++i) {
+                for (int a = 0; a < 3; ++a) {
+                    const float lo_v = i < n ? cmin[a][i] : 0.0f, hi_v = i < n ? cmax[a][i] : 0.0f;
+                    std::memcpy(&w[8 * a + i], &lo_v, 4);
+                    std::memcpy(&w[8 * a + 4 + i], &hi_v, 4);
+                }
+                w[24 + i] = i < n ? entry[i] : 0xFFFFFFFFu;
+                w[28 + i] = i < n ? count[i] : 0u;
+            }
+            w[28] |= (uint32_t)n << 24;
+            return me;
         }
         // the node's box: the union of its children (the binary node's box)
         uint8_t lo[3][4] = {}, hi[3][4] = {};
@@ -169,7 +197,7 @@ struct Converter {
 // Builds the quantized nodes of a BLAS blob; *root_count = the root's
 // triangle count when the whole BLAS is one leaf (no nodes then), else 0.
 int qbvh_convert(const uint8_t* blob, uint64_t size, std::vector<uint32_t>& out, uint32_t* root_count,
-                 const char** error) {
+                 const char** error, bool exact) {
     bvh_header_t h;
     if (size < 12 + 32) { *error = "BLAS blob too small"; return WF_ERR_INVALID; }
     std::memcpy(&h, blob, 12);
@@ -178,6 +206,7 @@ int qbvh_convert(const uint8_t* blob, uint64_t size, std::vector<uint32_t>& out,
         return WF_ERR_INVALID;
     }
     Converter cv;
+    cv.exact = exact;
     cv.nodes = blob + 12;
     cv.node_count = (h.triangles_offset - 12) / 32;
     const BNode root = cv.get(0);
@@ -203,12 +232,31 @@ extern "C" int wf_bvh_quantize(const void* blob, uint64_t blob_size, void* out_n
     if (!blob || !inout_size || !out_root_count) return wf::report_error(WF_ERR_INVALID, "wf_bvh_quantize: null argument");
     std::vector<uint32_t> words;
     const char* err = nullptr;
-    int rc = wf::qbvh_convert(static_cast<const uint8_t*>(blob), blob_size, words, out_root_count, &err);
+    int rc = wf::qbvh_convert(static_cast<const uint8_t*>(blob), blob_size, words, out_root_count, &err, false);
     if (rc) return wf::report_error(rc, err);
     const uint64_t bytes = words.size() * 4ull;
     if (!out_nodes || *inout_size < bytes) {
         *inout_size = bytes;
         return out_nodes ? wf::report_error(WF_ERR_CAPACITY, "wf_bvh_quantize: output buffer too small") : WF_OK;
+    }
+    std::memcpy(out_nodes, words.data(), bytes);
+    *inout_size = bytes;
+    return WF_OK;
+}
+
+// The exact 4-wide nodes of a BLAS blob (blas_layout 2), on the host: 128
+// bytes per node into out_nodes (NULL = size query).
+extern "C" int wf_bvh_widen(const void* blob, uint64_t blob_size, void* out_nodes, uint64_t* inout_size,
+                            uint32_t* out_root_count) {
+    if (!blob || !inout_size || !out_root_count) return wf::report_error(WF_ERR_INVALID, "wf_bvh_widen: null argument");
+    std::vector<uint32_t> words;
+    const char* err = nullptr;
+    int rc = wf::qbvh_convert(static_cast<const uint8_t*>(blob), blob_size, words, out_root_count, &err, true);
+    if (rc) return wf::report_error(rc, err);
+    const uint64_t bytes = words.size() * 4ull;
+    if (!out_nodes || *inout_size < bytes) {
+        *inout_size = bytes;
+        return out_nodes ? wf::report_error(WF_ERR_CAPACITY, "wf_bvh_widen: output buffer too small") : WF_OK;
     }
     std::memcpy(out_nodes, words.data(), bytes);
     *inout_size = bytes;

@@ -133,8 +133,8 @@ struct PairIO {
     }
 };
 
-template <bool QB>
-__global__ void __launch_bounds__(kTraceBlock, QB ? WF_TRACE_QB_MIN_BLOCKS : WF_TRACE_MIN_BLOCKS)
+template <int LAY>
+__global__ void __launch_bounds__(kTraceBlock, LAY ? WF_TRACE_QB_MIN_BLOCKS : WF_TRACE_MIN_BLOCKS)
     k_trace_pair(SceneRefs S, PairIO io, const uint32_t* n_shadow, const uint32_t* n_extend, uint32_t* fetch,
                  uint32_t* status, unsigned long long* totals) {
     io.n_first = *n_shadow;
@@ -145,22 +145,27 @@ __global__ void __launch_bounds__(kTraceBlock, QB ? WF_TRACE_QB_MIN_BLOCKS : WF_
     }
     LocalCounters c = {0, 0, 0, 0};
     bool overflow = false;
-    trace_persistent<false, false, QB>(S, io, io.n_first + ne, fetch, c, overflow);
+    trace_persistent<false, false, LAY>(S, io, io.n_first + ne, fetch, c, overflow);
     if (overflow) atomicOr(status, ERRF_STACK);
 }
 
 // The traversal kernel for the scene's BLAS layout (binary child pairs, or
-// the quantized 4-wide nodes with the tie rule).
+// the quantized / exact 4-wide nodes with the tie rule).
+template <bool ANY, bool COUNT, int LAY, class IO>
+void launch_layout(const SceneRefs& S, const IO& io, const uint32_t* count_ptr, uint32_t count, uint32_t* fetch,
+                   uint32_t* status, Counters* counters, unsigned long long* total, cudaStream_t stream) {
+    auto k = k_trace<ANY, COUNT, LAY, IO>;
+    k<<<persistent_grid(k), kTraceBlock, 0, stream>>>(S, io, count_ptr, count, fetch, status, counters, total);
+}
 template <bool ANY, bool COUNT, class IO>
 cudaError_t launch(const SceneRefs& S, const IO& io, const uint32_t* count_ptr, uint32_t count, uint32_t* fetch,
                    uint32_t* status, Counters* counters, unsigned long long* total, cudaStream_t stream) {
-    if (S.qbvh) {
-        auto k = k_trace<ANY, COUNT, true, IO>;
-        k<<<persistent_grid(k), kTraceBlock, 0, stream>>>(S, io, count_ptr, count, fetch, status, counters, total);
-    } else {
-        auto k = k_trace<ANY, COUNT, false, IO>;
-        k<<<persistent_grid(k), kTraceBlock, 0, stream>>>(S, io, count_ptr, count, fetch, status, counters, total);
-    }
+    if (S.qbvh == 2u)
+        launch_layout<ANY, COUNT, 2>(S, io, count_ptr, count, fetch, status, counters, total, stream);
+    else if (S.qbvh == 1u)
+        launch_layout<ANY, COUNT, 1>(S, io, count_ptr, count, fetch, status, counters, total, stream);
+    else
+        launch_layout<ANY, COUNT, 0>(S, io, count_ptr, count, fetch, status, counters, total, stream);
     return cudaGetLastError();
 }
 
@@ -250,12 +255,17 @@ cudaError_t launch_trace_pair(const SceneRefs& S, const RenderBuffers& B, uint32
     io.c.cap = io.e.cap = B.capacity; io.c.status = io.e.status = B.status;
     io.n_first = 0;
     uint32_t* fetch = B.counts + 2 * kMaxDepth + depth;
-    if (S.qbvh)
-        k_trace_pair<true><<<persistent_grid(k_trace_pair<true>), kTraceBlock, 0, stream>>>(
-            S, io, B.counts + kMaxDepth + depth - 1, B.counts + depth, fetch, B.status, totals);
+    const uint32_t* ns = B.counts + kMaxDepth + depth - 1;
+    const uint32_t* ne = B.counts + depth;
+    if (S.qbvh == 2u)
+        k_trace_pair<2><<<persistent_grid(k_trace_pair<2>), kTraceBlock, 0, stream>>>(S, io, ns, ne, fetch, B.status,
+                                                                                       totals);
+    else if (S.qbvh == 1u)
+        k_trace_pair<1><<<persistent_grid(k_trace_pair<1>), kTraceBlock, 0, stream>>>(S, io, ns, ne, fetch, B.status,
+                                                                                       totals);
     else
-        k_trace_pair<false><<<persistent_grid(k_trace_pair<false>), kTraceBlock, 0, stream>>>(
-            S, io, B.counts + kMaxDepth + depth - 1, B.counts + depth, fetch, B.status, totals);
+        k_trace_pair<0><<<persistent_grid(k_trace_pair<0>), kTraceBlock, 0, stream>>>(S, io, ns, ne, fetch, B.status,
+                                                                                       totals);
     return cudaGetLastError();
 }
 

@@ -96,14 +96,16 @@ struct PermutedAosIO {
     __device__ __forceinline__ void store(uint32_t k, const Hit& h, bool ok) const { io.store(ray(k), h, ok); }
 };
 
-// QB: BLAS levels over the quantized 4-wide nodes (csrc/wf_qbvh.cu); its
-// closest-hit rays use the order-independent tie rule (smallest t, then
-// smallest (instance, primitive); boxes entered at exactly t still visited),
-// so their hits equal the binary traversal's whatever order the wider nodes
-// visit leaves in.  Any-hit rays keep "t < tmax": only whether they hit matters.
-template <bool ANY, bool COUNT, bool QB, class IO>
+// LAY: the BLAS layout (0 = binary child pairs; 1 = quantized and 2 = exact
+// 4-wide nodes, csrc/wf_qbvh.cu).  Over the 4-wide nodes closest-hit rays use
+// the order-independent tie rule (smallest t, then smallest (instance,
+// primitive); boxes entered at exactly t still visited), so their hits equal
+// the binary traversal's whatever order the wider nodes visit leaves in.
+// Any-hit rays keep "t < tmax": only whether they hit matters.
+template <bool ANY, bool COUNT, int LAY, class IO>
 __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& io, uint32_t n, uint32_t* fetch,
                                                  LocalCounters& cnt, bool& overflow) {
+    constexpr bool QB = LAY != 0;   // a 4-wide layout, with the tie rule
     const unsigned FULL = 0xffffffffu;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t col = threadIdx.x;
@@ -268,37 +270,56 @@ __device__ __forceinline__ void trace_persistent(const SceneRefs& S, const IO& i
             w1--;
             pop = !finish && w1 == 0u;
         } else if (QB && level == 1u) {
-            // quantized 4-wide BLAS node: up to four child boxes (origin + q *
-            // 2^e per plane), visited nearest first, the others pushed
+            // 4-wide BLAS node: up to four child boxes (quantized: origin + q *
+            // 2^e per plane; exact: the planes as stored), visited nearest
+            // first, the others pushed
             if (!in_bounds(w0, B.qnode_count, S.status)) {
                 pop = true;
             } else {
-                const float4* qp = B.qnodes + 4ull * w0;
-                const float4 q0 = ldg4(qp), q1 = ldg4(qp + 1), q2 = ldg4(qp + 2), q3 = ldg4(qp + 3);
-                if (COUNT) cnt.blas_nodes += 2;   // 64 bytes, as a binary child pair
-                const uint32_t meta = __float_as_uint(q0.w);
-                const float sx = __uint_as_float((meta & 0xFFu) << 23);
-                const float sy = __uint_as_float(((meta >> 8) & 0xFFu) << 23);
-                const float sz = __uint_as_float(((meta >> 16) & 0xFFu) << 23);
-                const uint32_t nch = meta >> 24;
-                const uint32_t lx = __float_as_uint(q1.x), ly = __float_as_uint(q1.y), lz = __float_as_uint(q1.z);
-                const uint32_t hx = __float_as_uint(q2.x), hy = __float_as_uint(q2.y), hz = __float_as_uint(q2.z);
-                const uint32_t cl = __float_as_uint(q1.w), chi = __float_as_uint(q2.w);
-                const uint32_t kid[4] = {__float_as_uint(q3.x), __float_as_uint(q3.y), __float_as_uint(q3.z),
-                                         __float_as_uint(q3.w)};
                 const bool tie = !any_ray;
                 float d[4];
                 uint2 e[4];
+                if constexpr (LAY == 1) {
+                    const float4* qp = B.qnodes + 4ull * w0;
+                    const float4 q0 = ldg4(qp), q1 = ldg4(qp + 1), q2 = ldg4(qp + 2), q3 = ldg4(qp + 3);
+                    if (COUNT) cnt.blas_nodes += 2;   // 64 bytes, as a binary child pair
+                    const uint32_t meta = __float_as_uint(q0.w);
+                    const float sx = __uint_as_float((meta & 0xFFu) << 23);
+                    const float sy = __uint_as_float(((meta >> 8) & 0xFFu) << 23);
+                    const float sz = __uint_as_float(((meta >> 16) & 0xFFu) << 23);
+                    const uint32_t nch = meta >> 24;
+                    const uint32_t lx = __float_as_uint(q1.x), ly = __float_as_uint(q1.y), lz = __float_as_uint(q1.z);
+                    const uint32_t hx = __float_as_uint(q2.x), hy = __float_as_uint(q2.y), hz = __float_as_uint(q2.z);
+                    const uint32_t cl = __float_as_uint(q1.w), chi = __float_as_uint(q2.w);
+                    const uint32_t kid[4] = {__float_as_uint(q3.x), __float_as_uint(q3.y), __float_as_uint(q3.z),
+                                             __float_as_uint(q3.w)};
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const uint32_t sh = 8u * (uint32_t)i;
-                    const V3 bmn = mk(q0.x + (float)((lx >> sh) & 0xFFu) * sx, q0.y + (float)((ly >> sh) & 0xFFu) * sy,
-                                      q0.z + (float)((lz >> sh) & 0xFFu) * sz);
-                    const V3 bmx = mk(q0.x + (float)((hx >> sh) & 0xFFu) * sx, q0.y + (float)((hy >> sh) & 0xFFu) * sy,
-                                      q0.z + (float)((hz >> sh) & 0xFFu) * sz);
-                    const float di = tie ? slab_le(bmn, bmx, co, ci, ct) : slab(bmn, bmx, co, ci, ct);
-                    d[i] = (uint32_t)i < nch ? di : FLT_MAX;
-                    e[i] = make_uint2(kid[i], ((cl >> sh) & 0xFFu) | (((chi >> sh) & 0xFFu) << 8));
+                    for (int i = 0; i < 4; ++i) {
+                        const uint32_t sh = 8u * (uint32_t)i;
+                        const V3 bmn = mk(q0.x + (float)((lx >> sh) & 0xFFu) * sx, q0.y + (float)((ly >> sh) & 0xFFu) * sy,
+                                          q0.z + (float)((lz >> sh) & 0xFFu) * sz);
+                        const V3 bmx = mk(q0.x + (float)((hx >> sh) & 0xFFu) * sx, q0.y + (float)((hy >> sh) & 0xFFu) * sy,
+                                          q0.z + (float)((hz >> sh) & 0xFFu) * sz);
+                        const float di = tie ? slab_le(bmn, bmx, co, ci, ct) : slab(bmn, bmx, co, ci, ct);
+                        d[i] = (uint32_t)i < nch ? di : FLT_MAX;
+                        e[i] = make_uint2(kid[i], ((cl >> sh) & 0xFFu) | (((chi >> sh) & 0xFFu) << 8));
+                    }
+                } else {
+                    const float4* wp = B.qnodes + 8ull * w0;
+                    const float4 xl = ldg4(wp), xh = ldg4(wp + 1), yl = ldg4(wp + 2), yh = ldg4(wp + 3);
+                    const float4 zl = ldg4(wp + 4), zh = ldg4(wp + 5), en = ldg4(wp + 6), cn = ldg4(wp + 7);
+                    if (COUNT) cnt.blas_nodes += 4;   // 128 bytes, as two binary child pairs
+                    const uint32_t nch = __float_as_uint(cn.x) >> 24;
+                    auto lane4 = [](const float4& v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; };
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const V3 bmn = mk(lane4(xl, i), lane4(yl, i), lane4(zl, i));
+                        const V3 bmx = mk(lane4(xh, i), lane4(yh, i), lane4(zh, i));
+                        const float di = tie ? slab_le(bmn, bmx, co, ci, ct) : slab(bmn, bmx, co, ci, ct);
+                        d[i] = (uint32_t)i < nch ? di : FLT_MAX;
+                        const uint32_t c = __float_as_uint(lane4(cn, i));
+                        e[i] = make_uint2(__float_as_uint(lane4(en, i)), i == 0 ? (c & 0x00FFFFFFu) : c);
+                    }
                 }
                 // order the four by entry distance (a five-comparator network)
                 auto cswap = [&](int a, int b) {
@@ -545,25 +566,26 @@ __device__ __forceinline__ void flush_counters(const LocalCounters& c, Counters*
 #ifndef WF_TRACE_MIN_BLOCKS
 #define WF_TRACE_MIN_BLOCKS 9
 #endif
-// The same for the quantized 4-wide BLAS layout, whose node step holds four
-// child boxes and their sort keys at once.
+// The same for the 4-wide BLAS layouts, whose node step holds four child
+// boxes and their sort keys at once: 8 blocks (64 registers) measured 1-3 %
+// faster than 9 (56 registers, 40-72 bytes of spills) on both layouts.
 #ifndef WF_TRACE_QB_MIN_BLOCKS
-#define WF_TRACE_QB_MIN_BLOCKS 9
+#define WF_TRACE_QB_MIN_BLOCKS 8
 #endif
 int sm_count();
 
 // The traversal kernel: a persistent grid over count rays (read from
 // count_ptr on the device when it is non-null), rays handed out from *fetch.
 // total (optional) accumulates the number of rays of each launch.
-template <bool ANY, bool COUNT, bool QB, class IO>
-__global__ void __launch_bounds__(kTraceBlock, QB ? WF_TRACE_QB_MIN_BLOCKS : WF_TRACE_MIN_BLOCKS) k_trace(SceneRefs S, IO io, const uint32_t* count_ptr, uint32_t count,
+template <bool ANY, bool COUNT, int LAY, class IO>
+__global__ void __launch_bounds__(kTraceBlock, LAY ? WF_TRACE_QB_MIN_BLOCKS : WF_TRACE_MIN_BLOCKS) k_trace(SceneRefs S, IO io, const uint32_t* count_ptr, uint32_t count,
                                                   uint32_t* fetch, uint32_t* status, Counters* counters,
                                                   unsigned long long* total) {
     const uint32_t n = count_ptr ? *count_ptr : count;
     if (total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(total, (unsigned long long)n);
     LocalCounters c = {0, 0, 0, 0};
     bool overflow = false;
-    trace_persistent<ANY, COUNT, QB>(S, io, n, fetch, c, overflow);
+    trace_persistent<ANY, COUNT, LAY>(S, io, n, fetch, c, overflow);
     if (overflow) atomicOr(status, ERRF_STACK);
     if (COUNT) flush_counters(c, counters);
 }
