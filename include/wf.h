@@ -119,8 +119,9 @@ enum wf_texture_format {
     WF_TEXTURE_RG8 = 2,
     WF_TEXTURE_RGBA32F = 3,
     /* block-compressed (the reference's TEXTURE_FORMAT_BC*, dds.h:125-147):
-     * data = the 4x4 blocks as a DDS file stores them, decoded on the GPU;
-     * BC7 is recognised (wf_image_decode) but not decoded (WF_ERR_INVALID) */
+     * data = the 4x4 blocks as a DDS file stores them, decoded on the GPU
+     * (BC7 texel for texel as the GPU's texture sampler decodes it; BC1-BC5
+     * with the palette interpolations rounded to nearest 8-bit integers) */
     WF_TEXTURE_BC1 = 4,
     WF_TEXTURE_BC1_SRGB = 5,
     WF_TEXTURE_BC2 = 6,

@@ -342,7 +342,7 @@ def eval_bsdf(bsdf, base, alpha, n, v, wl, cosine=1):
 
 
 def decode_bc(fmt, blocks, w, h):
-    """BC1-BC5 blocks -> h x w x 4 uint8 (the checker of the GPU block decoder)."""
+    """BC1-BC5 / BC7 blocks -> h x w x 4 uint8 (the checker of the GPU block decoder)."""
     out = np.zeros((h, w, 4), np.uint8)
     blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
     if lib().orc_decode_bc(fmt, ptr(blocks), w, h, ptr(out)) != 0:

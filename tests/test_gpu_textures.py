@@ -207,29 +207,64 @@ def to_float(rgba8, srgb):
     return np.concatenate([col, lin[rgba8[..., 3:]]], axis=-1)
 
 
-@pytest.mark.parametrize("fmt", [abi.TEXTURE_BC1, abi.TEXTURE_BC1_SRGB, abi.TEXTURE_BC2, abi.TEXTURE_BC2_SRGB,
-                                 abi.TEXTURE_BC3, abi.TEXTURE_BC3_SRGB, abi.TEXTURE_BC4, abi.TEXTURE_BC5])
-def test_block_compressed_textures_decode_like_the_oracle(orc, fmt):
-    """Random BC blocks of a 13 x 9 image (partial edge blocks), expanded on
-    the GPU by wf_texture_create, read back: the oracle's decode, converted
-    to float as the library converts 8-bit texels, bit for bit."""
-    w, h = 13, 9
+def random_blocks(fmt, n, seed):
+    """n seeded blocks; BC7 blocks spread over its eight modes and the
+    reserved one (random bytes would be half mode 0)."""
+    rng = np.random.default_rng(seed)
+    if fmt in (abi.TEXTURE_BC7, abi.TEXTURE_BC7_SRGB):
+        from tests.golden.make_bc_hw import bc7_blocks
+        b = bc7_blocks(rng)
+        return b[rng.permutation(len(b))[:n]] if n <= len(b) else b
     small = fmt in (abi.TEXTURE_BC1, abi.TEXTURE_BC1_SRGB, abi.TEXTURE_BC4)
-    rng = np.random.default_rng(fmt)
-    blocks = rng.integers(0, 256, ((w + 3) // 4) * ((h + 3) // 4) * (8 if small else 16), dtype=np.uint8)
+    return rng.integers(0, 256, (n, 8 if small else 16), dtype=np.uint8)
+
+
+SRGB_BC = (abi.TEXTURE_BC1_SRGB, abi.TEXTURE_BC2_SRGB, abi.TEXTURE_BC3_SRGB, abi.TEXTURE_BC7_SRGB)
+
+
+@pytest.mark.parametrize("fmt", [abi.TEXTURE_BC1, abi.TEXTURE_BC1_SRGB, abi.TEXTURE_BC2, abi.TEXTURE_BC2_SRGB,
+                                 abi.TEXTURE_BC3, abi.TEXTURE_BC3_SRGB, abi.TEXTURE_BC4, abi.TEXTURE_BC5,
+                                 abi.TEXTURE_BC7, abi.TEXTURE_BC7_SRGB])
+def test_block_compressed_textures_decode_like_the_oracle(orc, fmt):
+    """Random BC blocks of a ragged image (partial edge blocks: 13 x 9, or
+    63 x 514 for BC7's 2,064 blocks of every mode), expanded on the GPU by
+    wf_texture_create, read back: the oracle's decode, converted to float as
+    the library converts 8-bit texels, bit for bit."""
+    w, h = (63, 514) if fmt in (abi.TEXTURE_BC7, abi.TEXTURE_BC7_SRGB) else (13, 9)
+    blocks = random_blocks(fmt, ((w + 3) // 4) * ((h + 3) // 4), fmt).reshape(-1)
     with Renderer(8, 8) as r:
         tid = r.create_texture_raw(blocks, w, h, fmt)
         got = r.read_texture(tid)
-    srgb = fmt in (abi.TEXTURE_BC1_SRGB, abi.TEXTURE_BC2_SRGB, abi.TEXTURE_BC3_SRGB)
-    want = to_float(orc.decode_bc(fmt, blocks, w, h), srgb)
+    want = to_float(orc.decode_bc(fmt, blocks, w, h), fmt in SRGB_BC)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
-def test_bc7_is_refused():
-    from wavefrontpathtracing_gb300 import WFError
+from tests.test_image_decode import BC_SAMPLER_TOLERANCE  # noqa: E402
+
+
+@pytest.mark.parametrize("fmt", [abi.TEXTURE_BC1, abi.TEXTURE_BC2, abi.TEXTURE_BC3, abi.TEXTURE_BC4,
+                                 abi.TEXTURE_BC5, abi.TEXTURE_BC7])
+def test_block_decoder_equals_the_texture_sampler(fmt):
+    """wf_texture_create's decode against this GPU's texture sampler reading
+    the same blocks through a block-compressed CUDA texture (tests/
+    hw_sampler.cu; the reference's D3D12 path decodes them in the sampler
+    too): BC7 bit for bit (its texels are exact 8-bit values by definition),
+    BC1-BC5 within the interpolation the formats leave open (per channel,
+    BC_SAMPLER_TOLERANCE).  BC4 / BC5 compare their one / two channels."""
+    from tests import hw_sampler
+    bw, bh = 16, 129 if fmt == abi.TEXTURE_BC7 else 8
+    blocks = random_blocks(fmt, bw * bh, 100 + fmt).reshape(-1)
+    hw = hw_sampler.decode(fmt, blocks, bw, bh)
     with Renderer(8, 8) as r:
-        with pytest.raises(WFError):
-            r.create_texture_raw(np.zeros(16, np.uint8), 4, 4, abi.TEXTURE_BC7)
+        got = r.read_texture(r.create_texture_raw(blocks, 4 * bw, 4 * bh, fmt))
+    ch = {abi.TEXTURE_BC4: 1, abi.TEXTURE_BC5: 2}.get(fmt, 4)
+    if fmt == abi.TEXTURE_BC7:
+        assert np.abs(hw * 255.0 - np.rint(hw * 255.0)).max() < 1e-3
+        assert np.array_equal(np.rint(got * 255.0), np.rint(hw * 255.0))
+    else:
+        diff = np.abs(got[..., :ch].astype(np.float64) - hw[..., :ch]) * 255.0
+        tol = np.asarray(BC_SAMPLER_TOLERANCE[fmt])
+        assert np.all(diff.reshape(-1, ch).max(0) <= tol), (diff.reshape(-1, ch).max(0), tol)
 
 
 def test_texture_files_load_as_the_reference_loads_them(orc, tmp_path):

@@ -1011,13 +1011,11 @@ int wf_texture_create(wf_ctx* c, uint32_t w, uint32_t h, uint32_t format, const 
     if (w == 0 || h == 0 || w > 16384 || h > 16384)
         return fail(WF_ERR_INVALID, "wf_texture_create: width and height must be in [1, 16384]");
     if (format > WF_TEXTURE_BC7_SRGB) return fail(WF_ERR_INVALID, "wf_texture_create: unknown format");
-    if (format == WF_TEXTURE_BC7 || format == WF_TEXTURE_BC7_SRGB)
-        return fail(WF_ERR_INVALID, "wf_texture_create: BC7 blocks are not decoded by this library");
     int rc = use_device(c);
     if (rc) return rc;
     const size_t n = (size_t)w * h;
     const bool srgb = format == WF_TEXTURE_RGBA8_SRGB || format == WF_TEXTURE_BC1_SRGB ||
-                      format == WF_TEXTURE_BC2_SRGB || format == WF_TEXTURE_BC3_SRGB;
+                      format == WF_TEXTURE_BC2_SRGB || format == WF_TEXTURE_BC3_SRGB || format == WF_TEXTURE_BC7_SRGB;
     float lut[256];
     for (int k = 0; k < 256; ++k) {
         if (srgb) {
