@@ -11,7 +11,9 @@ timed frames (CUDA events recorded by the library on its own stream around
 each frame); e2e = the same metric through the C ABI with host buffers — per
 frame the scene is re-submitted (1,025 instances, TLAS rebuilt on the GPU, as
 the reference rebuilds its TLAS every frame, renderer.cpp:637-669) and the
-1080p RGBA float image is read back to the host.
+1080p RGBA float image is read back to the host, frames pipelined as a
+real-time caller keeps them in flight (the next scene submitted during a
+render, each image copied during the next render, the last copy waited for).
 
 Beside the headline: the roofline per depth (extension and shadow-ray
 launches, algorithmic bytes of an instrumented pass over the timed CUDA-event
@@ -662,14 +664,18 @@ def run_ours(args, rank, world, local):
                 "extend_per_depth": s_ext, "extend": total(s_ext),
                 "extend_secondary": total([x for x in s_ext if x["depth"] >= 1]),
                 "connect_per_depth": s_con, "connect": total(s_con)}
-    # --- end to end through the C ABI with host buffers
-    # the image is read into page-locked host memory (a pageable buffer's copy
-    # speed depends on the host's page state: 1-60 GB/s on the same box)
+    # --- end to end through the C ABI with host buffers: every frame submits
+    # its instances (host arrays), rebuilds the TLAS, renders and copies the
+    # image to the host.  Frames are pipelined as a real-time caller runs
+    # them: frame i's scene is submitted while frame i - 1 renders, its image
+    # is copied on the copy stream while frame i + 1 renders (into one of two
+    # page-locked host images: a pageable buffer's copy speed depends on the
+    # host's page state, 1-60 GB/s on the same box), and the last copy is
+    # waited for inside the timed region.
     if torch is not None:
-        img_t = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True)
-        img = img_t.numpy()
+        imgs = [torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
     else:
-        img = np.zeros((H, W, 4), dtype=np.float32)
+        imgs = [np.zeros((H, W, 4), dtype=np.float32) for _ in range(2)]
     inst_mesh = np.array([ids[m] for m, _, _ in desc.instances], dtype=np.uint32)
     inst_xf = np.stack([np.asarray(t, dtype=np.float32) for _, t, _ in desc.instances])
     inst_mat = np.array([m for _, _, m in desc.instances], dtype=wf.abi.material_ext_dtype)
@@ -677,14 +683,20 @@ def run_ours(args, rank, world, local):
     barrier(dist)
     t0 = time.perf_counter()
     e2e_rays = 0
-    for i in range(0 if args.no_e2e else args.steps):
+    e2e_steps = 0 if args.no_e2e else args.steps
+    for i in range(e2e_steps):
         r.begin_scene(desc.view, desc.settings["env"])
         r.submit_render_meshes(inst_mesh, inst_xf, inst_mat)
         r.end_scene()
+        if i > 0:   # the previous frame's counters, read before this frame's render resets them
+            s = r.stats()
+            e2e_rays += s["rays_extend"] + s["rays_connect"]
         r.render(max_bounces=DEPTH, spp=SPP, frame_seed=frame_seed(i, rank), nee=1, rr_start_depth=RR,
                  accumulate=False, fused_connect=args.fused_connect, tail_paths=args.tail_paths,
                  fused_from_depth=args.fused_from_depth)
-        wf.check(r.L.wf_read_image(r.h, wf.abi.ptr(img), img.size))
+        r.read_image_async(imgs[i % 2])
+    if e2e_steps:
+        r.synchronize()
         s = r.stats()
         e2e_rays += s["rays_extend"] + s["rays_connect"]
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)

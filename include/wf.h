@@ -278,7 +278,9 @@ int wf_instance_submit_ex(wf_ctx* ctx, uint32_t mesh, const float local_to_world
 int wf_instance_submit_many(wf_ctx* ctx, uint32_t count, const uint32_t* meshes, const float* local_to_world,
                             const wf_material_ext* materials);
 /* Uploads instances, builds the TLAS on the GPU (renderer.cpp:637-669 builds
- * it on the CPU every frame) and the emitter table used by next-event estimation. */
+ * it on the CPU every frame) and the emitter table used by next-event
+ * estimation.  Returns once the work is queued on the context's stream (the
+ * host arrays are consumed by then); wf_render and the readbacks run after it. */
 int wf_scene_end(wf_ctx* ctx);
 /* The scene's bvh_instance_t array (world_to_local, world AABB, mesh id). */
 int wf_scene_get_instances(wf_ctx* ctx, bvh_instance_t* out, uint32_t capacity, uint32_t* out_count);
@@ -299,6 +301,12 @@ int wf_render(wf_ctx* ctx, const render_settings_t* settings,
               const wf_render_options* opts, uint32_t frame_seed);
 /* Average radiance per pixel, RGBA float32 (alpha = samples), row-major, row 0 = top. */
 int wf_read_image(wf_ctx* ctx, float* out_rgba, uint64_t float_count);
+/* The same image, copied on a stream of its own while the caller goes on
+ * (the next wf_scene_begin .. wf_render overlap the copy): out_rgba is
+ * complete once wf_synchronize returns (immediately for pageable memory,
+ * which the copy finishes before returning; page-locked memory is copied
+ * asynchronously).  A later resolve waits for the copy on the device. */
+int wf_read_image_async(wf_ctx* ctx, float* out_rgba, uint64_t float_count);
 /* post_process.hlsl:25-72: NaN/Inf flag, Reinhard, linear->sRGB, RGBA8. */
 int wf_read_image_ldr(wf_ctx* ctx, uint8_t* out_rgba8, uint64_t byte_count);
 int wf_get_stats(wf_ctx* ctx, wf_stats* out);

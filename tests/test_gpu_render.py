@@ -214,6 +214,51 @@ def test_submit_many_equals_one_by_one(orc):
     assert_images_equal(imgs[1], imgs[0])
 
 
+def test_pipelined_frames_with_async_readback_equal_blocking_ones():
+    """The e2e loop's pattern: frame i + 1's scene submitted (wf_scene_end
+    returns before its TLAS is built) while frame i's image is still being
+    copied by wf_read_image_async (page-locked and pageable buffers), a
+    resize of nothing in between: every image equals the same frame rendered
+    and read back blocking, and the instance records carry the tight boxes."""
+    torch = pytest.importorskip("torch")
+    desc = scenes.instanced_scene(width=64, height=40, instances=48, freqs=(5, 7), spp=2, max_bounces=5)
+    mesh_ids = None
+
+    def scene(r):
+        r.begin_scene(desc.view, desc.settings["env"])
+        r.submit_render_meshes([mesh_ids[m] for m, _, _ in desc.instances],
+                               np.stack([np.asarray(t, np.float32) for _, t, _ in desc.instances]),
+                               np.array([m for _, _, m in desc.instances]))
+        r.end_scene()
+
+    kw = dict(max_bounces=5, spp=2, nee=1, rr_start_depth=2, accumulate=False)
+    with Renderer(desc.width, desc.height, tlas_metric=2, instance_bounds=1) as r:
+        mesh_ids = [r.create_mesh_from_triangles(t, interval_count=16, max_leaf_prims=4) for t in desc.meshes]
+        outs = [torch.empty((desc.height, desc.width, 4), dtype=torch.float32, pin_memory=True).numpy(),
+                np.zeros((desc.height, desc.width, 4), np.float32),
+                torch.empty((desc.height, desc.width, 4), dtype=torch.float32, pin_memory=True).numpy()]
+        for i, out in enumerate(outs):
+            scene(r)
+            r.render(frame_seed=11 + i, **kw)
+            r.read_image_async(out)
+        r.synchronize()
+        got = [o.copy() for o in outs]
+        boxes = r.scene_instances()
+        want = []
+        for i in range(len(outs)):
+            scene(r)
+            r.render(frame_seed=11 + i, **kw)
+            want.append(r.read_image())
+    with Renderer(desc.width, desc.height, tlas_metric=2, instance_bounds=1) as r2:
+        mesh_ids = [r2.create_mesh_from_triangles(t, interval_count=16, max_leaf_prims=4) for t in desc.meshes]
+        scene(r2)
+        r2.synchronize()
+        assert boxes.tobytes() == r2.scene_instances().tobytes()
+    for g, w in zip(got, want):
+        assert_images_equal(g, w)
+    assert not np.array_equal(got[0], got[1])
+
+
 def test_per_depth_queue_sizes_match_the_oracle(orc):
     desc = scenes.instanced_scene(width=48, height=32, instances=60, freqs=(5, 8), spp=2, max_bounces=5)
     img, want, stats, ost, _, _ = render_both(orc, desc, spp=2, frame_seed=9, nee=1, rr=2)

@@ -61,6 +61,7 @@ SIGNATURES = {
     "wf_scene_get_tlas": [_vp, _vp, _pu64],
     "wf_render": [_vp, _vp, _vp, _u32],
     "wf_read_image": [_vp, _vp, _u64],
+    "wf_read_image_async": [_vp, _vp, _u64],
     "wf_read_image_ldr": [_vp, _vp, _u64],
     "wf_get_stats": [_vp, _vp],
     "wf_trace": [_vp, _vp, _u32, _vp, _u32],
@@ -419,6 +420,12 @@ class Renderer:
         out = np.zeros((self.height, self.width, 4), dtype=np.float32)
         check(self.L.wf_read_image(self.h, ptr(out), out.size))
         return out
+
+    def read_image_async(self, out):
+        """Starts copying the image into out ((height, width, 4) float32, best
+        page-locked) and returns; out is complete after synchronize()."""
+        assert out.dtype == np.float32 and out.flags["C_CONTIGUOUS"] and out.size >= self.width * self.height * 4
+        check(self.L.wf_read_image_async(self.h, ptr(out), out.size))
 
     def read_image_ldr(self):
         out = np.zeros((self.height, self.width, 4), dtype=np.uint8)

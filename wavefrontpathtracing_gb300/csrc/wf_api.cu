@@ -140,6 +140,7 @@ struct wf_ctx {
     uint32_t light_count = 0;
     float light_total = 0.0f;
     std::vector<bvh_instance_t> scene_bi;
+    bool bounds_pending = false;            // scene_bi's boxes still on the device (aabbs)
     uint64_t scene_triangles = 0;           // sum of the instances' triangle counts
     bool albedo_set = false;
     DevBuf<float4> tri_albedo;              // per scene triangle (wf_scene_set_albedo)
@@ -177,6 +178,12 @@ struct wf_ctx {
     // choose where the next wave hands its remaining bounces to the tail kernel
     uint32_t* h_counts = nullptr;           // pinned, kMaxDepth extension counts
     cudaEvent_t ev_counts = nullptr;
+    // wf_read_image_async: the resolved image is copied to the host on `copy`
+    // (after img_ready on `stream`) while the next frame renders; the next
+    // resolve into `image` waits for img_copied
+    cudaStream_t copy = nullptr;
+    cudaEvent_t img_ready = nullptr, img_copied = nullptr;
+    bool img_copy_pending = false;
     bool counts_pending = false, counts_known = false;
     uint32_t last_counts[kMaxDepth] = {};
     wf_stats stats{};
@@ -679,19 +686,18 @@ bool ctx_mesh(wf_ctx* c, uint32_t mesh, MeshView* out) {
 
 int make_instance(wf_ctx* c, uint32_t mesh, const float* l2w, const material_t* mat, uint32_t bsdf, float ior,
                   const char* who, Instance* out) {
-    const std::string w(who);
-    if (!l2w || !mat) return fail(WF_ERR_INVALID, w + ": null argument");
-    if (mesh >= c->meshes.size()) return fail(WF_ERR_INVALID, w + ": unknown mesh");
-    if (bsdf > WF_BSDF_DIELECTRIC) return fail(WF_ERR_INVALID, w + ": unknown BSDF");
+    if (!l2w || !mat) return fail(WF_ERR_INVALID, std::string(who) + ": null argument");
+    if (mesh >= c->meshes.size()) return fail(WF_ERR_INVALID, std::string(who) + ": unknown mesh");
+    if (bsdf > WF_BSDF_DIELECTRIC) return fail(WF_ERR_INVALID, std::string(who) + ": unknown BSDF");
     const uint32_t ids[4] = {mat->base_color_index, mat->normal_index, mat->metallic_roughness_index,
                              mat->emissive_index};
     for (uint32_t id : ids)
-        if (id > c->textures.size()) return fail(WF_ERR_INVALID, w + ": material names an unknown texture");
+        if (id > c->textures.size()) return fail(WF_ERR_INVALID, std::string(who) + ": material names an unknown texture");
     Instance& in = *out;
     in = Instance{};
     in.mesh = mesh;
     std::memcpy(in.l2w, l2w, 64);
-    if (!invert4(l2w, in.w2l)) return fail(WF_ERR_INVALID, w + ": transform is not invertible");
+    if (!invert4(l2w, in.w2l)) return fail(WF_ERR_INVALID, std::string(who) + ": transform is not invertible");
     in.mat = *mat;
     in.bsdf = bsdf;
     in.ior = ior;
@@ -862,6 +868,10 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
         if (rc == WF_OK && (cudaEventCreateWithFlags(&c->ev_counts, cudaEventDisableTiming) != cudaSuccess ||
                             cudaMallocHost(&c->h_counts, kMaxDepth * sizeof(uint32_t)) != cudaSuccess))
             rc = fail(WF_ERR_CUDA, "wf_create: event / pinned buffer creation failed");
+        if (rc == WF_OK && (cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking) != cudaSuccess ||
+                            cudaEventCreateWithFlags(&c->img_ready, cudaEventDisableTiming) != cudaSuccess ||
+                            cudaEventCreateWithFlags(&c->img_copied, cudaEventDisableTiming) != cudaSuccess))
+            rc = fail(WF_ERR_CUDA, "wf_create: copy stream / event creation failed");
     }
     if (rc == WF_OK) rc = dev_alloc(&c->status, 1);
     if (rc == WF_OK) rc = dev_alloc(&c->counters, 2 * kMaxDepth);
@@ -885,6 +895,7 @@ int wf_destroy(wf_ctx* c) {
     if (!c) return WF_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copy) cudaStreamSynchronize(c->copy);
     for (Mesh& m : c->meshes) free_mesh(m);
     for (Texture& t : c->textures) dev_free(t.d);
     c->tex_table.release();
@@ -905,6 +916,9 @@ int wf_destroy(wf_ctx* c) {
     if (c->ev_counts) cudaEventDestroy(c->ev_counts);
     if (c->h_counts) cudaFreeHost(c->h_counts);
     if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
+    if (c->copy) { cudaStreamSynchronize(c->copy); cudaStreamDestroy(c->copy); }
+    if (c->img_ready) cudaEventDestroy(c->img_ready);
+    if (c->img_copied) cudaEventDestroy(c->img_copied);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return WF_OK;
@@ -921,6 +935,10 @@ int wf_synchronize(wf_ctx* c) {
     int rc = use_device(c);
     if (rc) return rc;
     WF_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->img_copy_pending) {
+        WF_CUDA(cudaStreamSynchronize(c->copy));
+        c->img_copy_pending = false;
+    }
     return take_status(c);
 }
 
@@ -1210,7 +1228,6 @@ int wf_scene_end(wf_ctx* c) {
         }
         WF_CUDA(launch_tlas_build(c->aabbs.p, n, c->tnodes.p, c->tlas_scratch.p, c->tlas_metric, c->stream));
         c->launches++;
-        if (tight) WF_CUDA(d2h(c, aabbs.data(), c->aabbs.p, aabbs.size() * 4));
     }
     // emitter table (every triangle of every emissive instance, world space)
     std::vector<LightTri> lt;
@@ -1225,20 +1242,36 @@ int wf_scene_end(wf_ctx* c) {
     if ((rc = c->lights.reserve(lt.size()))) return rc;
     if (!lt.empty())
         WF_CUDA(h2d(c, c->lights.p, lt.data(), lt.size() * sizeof(LightTri)));
-    WF_CUDA(cudaStreamSynchronize(c->stream));
-    if (tight)   // the instance records report the boxes the TLAS was built from
-        for (uint32_t i = 0; i < n; ++i) {
-            std::memcpy(c->scene_bi[i].aabb_min, &aabbs[6ull * i], 12);
-            std::memcpy(c->scene_bi[i].aabb_max, &aabbs[6ull * i + 3], 12);
-        }
+    // No wait: the uploads above are staged by the time their calls return and
+    // the builds stay queued on the stream ahead of the render.  Device-built
+    // boxes reach the host instance records when they are asked for.
+    c->bounds_pending = tight;
     c->in_scene = false;
     c->scene_ready = true;
+    return WF_OK;
+}
+
+// The instance records report the boxes the TLAS was built from: with
+// instance_bounds 1 those were computed on the device by wf_scene_end.
+static int fetch_bounds(wf_ctx* c) {
+    if (!c->bounds_pending) return WF_OK;
+    const size_t n = c->scene_bi.size();
+    std::vector<float> aabbs(6 * n);
+    WF_CUDA(d2h(c, aabbs.data(), c->aabbs.p, aabbs.size() * 4));
+    WF_CUDA(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; ++i) {
+        std::memcpy(c->scene_bi[i].aabb_min, &aabbs[6 * i], 12);
+        std::memcpy(c->scene_bi[i].aabb_max, &aabbs[6 * i + 3], 12);
+    }
+    c->bounds_pending = false;
     return WF_OK;
 }
 
 int wf_scene_get_instances(wf_ctx* c, bvh_instance_t* out, uint32_t cap, uint32_t* count) {
     if (!c || !count) return fail(WF_ERR_INVALID, "wf_scene_get_instances: null argument");
     if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_scene_get_instances: no finished scene");
+    int rc = use_device(c);
+    if (rc || (rc = fetch_bounds(c))) return rc;
     *count = (uint32_t)c->scene_bi.size();
     if (!out || cap < *count) return fail(WF_ERR_CAPACITY, "wf_scene_get_instances: output too small");
     std::memcpy(out, c->scene_bi.data(), c->scene_bi.size() * sizeof(bvh_instance_t));
@@ -1249,7 +1282,7 @@ int wf_scene_get_tlas(wf_ctx* c, void* out, uint64_t* inout_size) {
     if (!c || !inout_size) return fail(WF_ERR_INVALID, "wf_scene_get_tlas: null argument");
     if (!c->scene_ready) return fail(WF_ERR_STATE, "wf_scene_get_tlas: no finished scene");
     int rc = use_device(c);
-    if (rc) return rc;
+    if (rc || (rc = fetch_bounds(c))) return rc;
     const uint32_t n = (uint32_t)c->scene_bi.size();
     const uint64_t nodes = n ? 2ull * n : 1ull;
     const uint64_t size = 8 + 32 * nodes + 92ull * n;
@@ -1735,18 +1768,50 @@ int wf_load_accumulator(wf_ctx* c, const char* path, uint32_t* out_samples, uint
     return WF_OK;
 }
 
+// The resolved image in c->image, once an asynchronous copy out of it has
+// finished (the stream waits for it on the device; a new buffer waits on the host).
+static int resolve_image(wf_ctx* c, uint64_t npix) {
+    if (c->img_copy_pending) {
+        if (c->image.cap < npix) {
+            WF_CUDA(cudaStreamSynchronize(c->copy));
+            c->img_copy_pending = false;
+        } else {
+            WF_CUDA(cudaStreamWaitEvent(c->stream, c->img_copied, 0));
+        }
+    }
+    int rc = c->image.reserve(npix);
+    if (rc) return rc;
+    WF_CUDA(launch_resolve(c->accum, (uint32_t)npix, c->image.p, c->stream));
+    return WF_OK;
+}
+
 int wf_read_image(wf_ctx* c, float* out, uint64_t nfloat) {
     if (!c || !out) return fail(WF_ERR_INVALID, "wf_read_image: null argument");
     const uint64_t npix = (uint64_t)c->width * c->height;
     if (nfloat < 4 * npix) return fail(WF_ERR_CAPACITY, "wf_read_image: output smaller than width*height*4 floats");
     if (!c->buffers_ready) return fail(WF_ERR_STATE, "wf_read_image: nothing rendered");
     int rc = use_device(c);
-    if (rc) return rc;
-    if ((rc = c->image.reserve(npix))) return rc;
-    WF_CUDA(launch_resolve(c->accum, (uint32_t)npix, c->image.p, c->stream));
+    if (rc || (rc = resolve_image(c, npix))) return rc;
     WF_CUDA(d2h(c, out, c->image.p, npix * sizeof(float4)));
     WF_CUDA(cudaStreamSynchronize(c->stream));
     return take_status(c);
+}
+
+int wf_read_image_async(wf_ctx* c, float* out, uint64_t nfloat) {
+    if (!c || !out) return fail(WF_ERR_INVALID, "wf_read_image_async: null argument");
+    const uint64_t npix = (uint64_t)c->width * c->height;
+    if (nfloat < 4 * npix)
+        return fail(WF_ERR_CAPACITY, "wf_read_image_async: output smaller than width*height*4 floats");
+    if (!c->buffers_ready) return fail(WF_ERR_STATE, "wf_read_image_async: nothing rendered");
+    int rc = use_device(c);
+    if (rc || (rc = resolve_image(c, npix))) return rc;
+    WF_CUDA(cudaEventRecord(c->img_ready, c->stream));
+    WF_CUDA(cudaStreamWaitEvent(c->copy, c->img_ready, 0));
+    c->d2h_bytes += npix * sizeof(float4);
+    WF_CUDA(cudaMemcpyAsync(out, c->image.p, npix * sizeof(float4), cudaMemcpyDeviceToHost, c->copy));
+    WF_CUDA(cudaEventRecord(c->img_copied, c->copy));
+    c->img_copy_pending = true;
+    return WF_OK;
 }
 
 int wf_read_image_ldr(wf_ctx* c, uint8_t* out, uint64_t nbytes) {
