@@ -134,7 +134,8 @@ __global__ void __launch_bounds__(32) k_tlas_build(const float* __restrict__ aab
 
 // ---------------------------------------------------------------------------
 // metric 2: parallel locally-ordered clustering (Meister and Bittner 2018).
-// One block of 1024 threads: Morton order of the box centres by a bitonic sort,
+// One block of 1024 threads, its working set in shared memory up to 2048
+// instances: Morton order of the box centres by a bitonic sort,
 // then rounds of nearest-neighbour search within kPlocRadius list positions
 // (smallest merged half area, ties to the lower position), merging of mutual
 // pairs (new nodes numbered in list order by a block scan) and in-order
@@ -160,13 +161,36 @@ __device__ __forceinline__ uint32_t quantize10(float c, float lo, float ext) {
     return (uint32_t)(q * 1023.0f);
 }
 
+// The build's working arrays: in dynamic shared memory when they fit
+// (n <= kPlocSmemMax), else in the caller's global scratch, same layout.
 struct PlocScratch {
     unsigned long long* key;   // P (power of two >= n)
     uint32_t* cl[2];           // node id per list position
     uint32_t* nn;              // nearest neighbour per position
     uint32_t* flag;            // per position: 1 = creates a node
     uint32_t* keep;            // per position: 1 = stays in the list
+    float* box[2];             // per position: the cluster's box (min xyz, max xyz)
 };
+
+constexpr uint32_t kPlocSmemMax = 2048;
+
+__host__ __device__ inline size_t ploc_bytes(uint32_t n, uint32_t P) {
+    return 8ull * P + 4ull * 5 * n + 4ull * 12 * n;
+}
+
+__device__ inline PlocScratch ploc_carve(void* base, uint32_t n, uint32_t P) {
+    PlocScratch S;
+    S.key = static_cast<unsigned long long*>(base);
+    uint32_t* w = reinterpret_cast<uint32_t*>(S.key + P);
+    S.cl[0] = w;
+    S.cl[1] = w + n;
+    S.nn = w + 2 * n;
+    S.flag = w + 3 * n;
+    S.keep = w + 4 * n;
+    S.box[0] = reinterpret_cast<float*>(w + 5 * n);
+    S.box[1] = S.box[0] + 6 * n;
+    return S;
+}
 
 __device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t x) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -203,9 +227,12 @@ __device__ uint32_t block_scan(uint32_t* v, uint32_t count, uint32_t* s_wt) {
 }
 
 __global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restrict__ aabbs, uint32_t n,
-                                                            float4* nodes, PlocScratch S, uint32_t P) {
+                                                            float4* nodes, uint32_t* scratch, uint32_t P,
+                                                            bool smem) {
+    extern __shared__ unsigned long long s_dyn[];
     __shared__ uint32_t s_part[33];
     __shared__ float s_red[6][32];
+    const PlocScratch S = ploc_carve(smem ? static_cast<void*>(s_dyn) : static_cast<void*>(scratch), n, P);
     const uint32_t t = threadIdx.x;
     // leaves and the centre bounds
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
@@ -260,24 +287,31 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restr
             }
             __syncthreads();
         }
-    for (uint32_t k = t; k < n; k += kPlocThreads) S.cl[0][k] = 1u + (uint32_t)(S.key[k] & 0xFFFFFFFFull);
+    for (uint32_t k = t; k < n; k += kPlocThreads) {
+        const uint32_t leaf = (uint32_t)(S.key[k] & 0xFFFFFFFFull);
+        S.cl[0][k] = 1u + leaf;
+        for (int a = 0; a < 6; ++a) S.box[0][6 * k + a] = aabbs[6ull * leaf + a];
+    }
     __syncthreads();
     uint32_t count = n, next = n + 1, cur = 0;
     while (count > 1) {
         const uint32_t* cl = S.cl[cur];
         uint32_t* ncl = S.cl[cur ^ 1];
+        const float* bx = S.box[cur];
+        float* nbx = S.box[cur ^ 1];
         for (uint32_t k = t; k < count; k += kPlocThreads) {
-            const float4 an = nodes[2 * cl[k]], ax = nodes[2 * cl[k] + 1];
+            const float* A = bx + 6 * k;
+            const float anx = A[0], any_ = A[1], anz = A[2], axx = A[3], axy = A[4], axz = A[5];
             const uint32_t j0 = k > kPlocRadius ? k - kPlocRadius : 0u;
             const uint32_t j1 = k + kPlocRadius < count - 1 ? k + kPlocRadius : count - 1;
             float best = FLT_MAX;
             uint32_t bj = (k == 0) ? 1u : k - 1;
             for (uint32_t j = j0; j <= j1; ++j) {
                 if (j == k) continue;
-                const float4 bn = nodes[2 * cl[j]], bx = nodes[2 * cl[j] + 1];
-                const float ex = gmax(ax.x, bx.x) - gmin(an.x, bn.x);
-                const float ey = gmax(ax.y, bx.y) - gmin(an.y, bn.y);
-                const float ez = gmax(ax.z, bx.z) - gmin(an.z, bn.z);
+                const float* Bj = bx + 6 * j;
+                const float ex = gmax(axx, Bj[3]) - gmin(anx, Bj[0]);
+                const float ey = gmax(axy, Bj[4]) - gmin(any_, Bj[1]);
+                const float ez = gmax(axz, Bj[5]) - gmin(anz, Bj[2]);
                 const float d = ex * ey + ey * ez + ez * ex;
                 if (d < best) { best = d; bj = j; }
             }
@@ -308,17 +342,20 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restr
             const bool mutual = S.nn[m] == k;
             if (mutual && k > m) continue;
             const uint32_t pos = S.keep[k];
+            const float* A = bx + 6 * k;
+            float* O = nbx + 6 * pos;
             if (mutual) {
                 const uint32_t id = next + S.flag[k];
-                const float4 an = nodes[2 * cl[k]], ax = nodes[2 * cl[k] + 1];
-                const float4 bn = nodes[2 * cl[m]], bx = nodes[2 * cl[m] + 1];
-                nodes[2 * id] = make_float4(gmin(an.x, bn.x), gmin(an.y, bn.y), gmin(an.z, bn.z),
-                                            __uint_as_float((cl[k] << 16) | cl[m]));
-                nodes[2 * id + 1] = make_float4(gmax(ax.x, bx.x), gmax(ax.y, bx.y), gmax(ax.z, bx.z),
-                                                __uint_as_float(0u));
+                const float* Bm = bx + 6 * m;
+                const float mn[3] = {gmin(A[0], Bm[0]), gmin(A[1], Bm[1]), gmin(A[2], Bm[2])};
+                const float mx[3] = {gmax(A[3], Bm[3]), gmax(A[4], Bm[4]), gmax(A[5], Bm[5])};
+                nodes[2 * id] = make_float4(mn[0], mn[1], mn[2], __uint_as_float((cl[k] << 16) | cl[m]));
+                nodes[2 * id + 1] = make_float4(mx[0], mx[1], mx[2], __uint_as_float(0u));
                 ncl[pos] = id;
+                for (int a = 0; a < 3; ++a) { O[a] = mn[a]; O[3 + a] = mx[a]; }
             } else {
                 ncl[pos] = cl[k];
+                for (int a = 0; a < 6; ++a) O[a] = A[a];
             }
         }
         __syncthreads();
@@ -401,7 +438,7 @@ cudaError_t launch_instance_bounds(const float4* sinst, uint32_t rows, uint32_t 
 }
 
 size_t tlas_scratch_words(uint32_t n, uint32_t metric) {
-    if (metric == 2) return 2ull * pow2_at_least(n ? n : 1) + 5ull * n + 8;
+    if (metric == 2) return (n <= kPlocSmemMax) ? 8 : ploc_bytes(n, pow2_at_least(n ? n : 1)) / 4 + 8;
     return 7ull * n + 1;
 }
 
@@ -409,15 +446,16 @@ cudaError_t launch_tlas_build(const float* aabbs, uint32_t n, float4* nodes, uin
                               cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
     if (metric == 2) {
+        // the working set in shared memory up to kPlocSmemMax instances
+        // (152 KiB at 2048), else in the scratch (8-byte aligned: cudaMalloc)
         const uint32_t P = pow2_at_least(n);
-        PlocScratch S;
-        S.key = reinterpret_cast<unsigned long long*>(scratch);   // 8-byte aligned: scratch comes from cudaMalloc
-        S.cl[0] = scratch + 2ull * P;
-        S.cl[1] = S.cl[0] + n;
-        S.nn = S.cl[1] + n;
-        S.flag = S.nn + n;
-        S.keep = S.flag + n;
-        k_tlas_ploc<<<1, kPlocThreads, 0, stream>>>(aabbs, n, nodes, S, P);
+        const bool smem = n <= kPlocSmemMax;
+        const size_t bytes = smem ? ploc_bytes(n, P) : 0;
+        if (bytes > 48u * 1024u) {
+            cudaError_t e = cudaFuncSetAttribute(k_tlas_ploc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e != cudaSuccess) return e;
+        }
+        k_tlas_ploc<<<1, kPlocThreads, bytes, stream>>>(aabbs, n, nodes, scratch, P, smem);
         return cudaGetLastError();
     }
     size_t smem = (n <= kSmemInstances) ? (size_t)n * 7u * 4u : 0u;
