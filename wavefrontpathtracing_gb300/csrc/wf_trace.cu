@@ -8,8 +8,6 @@ namespace wf {
 
 namespace {
 
-int g_sms = 0;
-
 // Extension rays: queue[depth & 1] -> hits.  Ray flags in origin.w select culling.
 struct ExtendIO {
     const float4* qo;
@@ -172,13 +170,17 @@ cudaError_t launch(const SceneRefs& S, const IO& io, const uint32_t* count_ptr, 
 }  // namespace
 
 int sm_count() {
-    if (g_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = 1;
-    }
-    return g_sms;
+    // per device (a process may drive different GPUs), queried once each
+    static int s_sms[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int* slot = (dev >= 0 && dev < 64) ? &s_sms[dev] : nullptr;
+    if (slot && *slot > 0) return *slot;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+    if (slot) *slot = sms;
+    return sms;
 }
 
 cudaError_t launch_trace_aos(const SceneRefs& S, const void* rays, uint32_t n, void* hits, uint32_t flags,
