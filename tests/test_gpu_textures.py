@@ -287,3 +287,19 @@ def test_texture_files_load_as_the_reference_loads_them(orc, tmp_path):
     import wavefrontpathtracing_gb300 as wf
     want, _, _, _ = wf.decode_image(write_hdr(px))
     assert np.array_equal(b.view(np.uint32), want.view(np.uint32))
+
+
+def test_bc7_dds_loads_as_the_sampler_decodes_it(orc, tmp_path):
+    """A DX10 DDS of BC7 blocks (DXGI_FORMAT_BC7_UNORM, every mode), loaded
+    as a base colour (sRGB) and as linear data: the oracle's decode, which
+    equals the GPU texture sampler's for BC7, converted as 8-bit texels."""
+    from tests.test_image_decode import dds_header
+    w, h = 30, 21
+    blocks = random_blocks(abi.TEXTURE_BC7, ((w + 3) // 4) * ((h + 3) // 4), 77).reshape(-1)
+    (tmp_path / "t.dds").write_bytes(dds_header(w, h, dxgi=98) + blocks.tobytes())
+    want8 = orc.decode_bc(abi.TEXTURE_BC7, blocks, w, h)
+    with Renderer(8, 8) as r:
+        srgb = r.read_texture(r.load_texture_file(str(tmp_path / "t.dds"), srgb=True))
+        lin = r.read_texture(r.load_texture_file(str(tmp_path / "t.dds"), srgb=False))
+    assert np.array_equal(srgb.view(np.uint32), to_float(want8, True).view(np.uint32))
+    assert np.array_equal(lin.view(np.uint32), to_float(want8, False).view(np.uint32))

@@ -295,7 +295,7 @@ class Renderer:
         """A texture from an image file, as the reference's asset loader takes
         it (asset_loader.cpp:56-206), decoded by wf_image_decode: .png / .jpg /
         .jpeg (RGBA8, or RGBA8_SRGB when srgb), .hdr (RGBA32F), .dds (its
-        format, the sRGB variant of RGBA8 / BC1-BC3 when srgb, dds.h:125-147)."""
+        format, the sRGB variant of RGBA8 / BC1-BC3 / BC7 when srgb, dds.h:125-147)."""
         ext = os.path.splitext(path)[1].lower()
         data = open(path, "rb").read()
         if ext not in (".png", ".jpg", ".jpeg", ".hdr", ".dds"):
