@@ -668,42 +668,69 @@ def run_ours(args, rank, world, local):
     # its instances (host arrays), rebuilds the TLAS, renders and copies the
     # image to the host.  Frames are pipelined as a real-time caller runs
     # them: frame i's scene is submitted while frame i - 1 renders, its image
-    # is copied on the copy stream while frame i + 1 renders (into one of two
-    # page-locked host images: a pageable buffer's copy speed depends on the
-    # host's page state, 1-60 GB/s on the same box), and the last copy is
-    # waited for inside the timed region.
-    if torch is not None:
-        imgs = [torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
-    else:
-        imgs = [np.zeros((H, W, 4), dtype=np.float32) for _ in range(2)]
-    inst_mesh = np.array([ids[m] for m, _, _ in desc.instances], dtype=np.uint32)
-    inst_xf = np.stack([np.asarray(t, dtype=np.float32) for _, t, _ in desc.instances])
-    inst_mat = np.array([m for _, _, m in desc.instances], dtype=wf.abi.material_ext_dtype)
-    s0 = r.stats()
-    barrier(dist)
-    t0 = time.perf_counter()
-    e2e_rays = 0
-    e2e_steps = 0 if args.no_e2e else args.steps
-    for i in range(e2e_steps):
-        r.begin_scene(desc.view, desc.settings["env"])
-        r.submit_render_meshes(inst_mesh, inst_xf, inst_mat)
-        r.end_scene()
-        if i > 0:   # the previous frame's counters, read before this frame's render resets them
-            s = r.stats()
-            e2e_rays += s["rays_extend"] + s["rays_connect"]
-        r.render(max_bounces=DEPTH, spp=SPP, frame_seed=frame_seed(i, rank), nee=1, rr_start_depth=RR,
-                 accumulate=False, fused_connect=args.fused_connect, tail_paths=args.tail_paths,
-                 fused_from_depth=args.fused_from_depth)
-        r.read_image_async(imgs[i % 2])
-    if e2e_steps:
-        r.synchronize()
-        s = r.stats()
-        e2e_rays += s["rays_extend"] + s["rays_connect"]
-    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
-    s1 = r.stats()
-    e2e_value = sum_over_ranks(dist, e2e_rays) / e2e_s / 1e6 if not args.no_e2e else None
-    h2d = (s1["h2d_bytes"] - s0["h2d_bytes"]) // args.steps
-    d2h = (s1["d2h_bytes"] - s0["d2h_bytes"]) // args.steps
+    # is copied on the copy stream while frame i + 1 renders (into page-locked
+    # host images: a pageable buffer's copy speed depends on the host's page
+    # state, 1-60 GB/s on the same box), and the last copies are waited for
+    # inside the timed region.  With F frames in flight (--frames-in-flight,
+    # default 2) consecutive frames go to F contexts of the same scene in
+    # turn, one per frame in flight (each context has its own streams and
+    # buffers), so one frame's nearly idle deep depths overlap the next
+    # frame's first depths; F = 1 is also timed and reported.
+    def e2e_loop(ctxs, insts, imgs, steps):
+        rays, pending = 0, [False] * len(ctxs)
+        b0 = [c.stats() for c in ctxs]
+        barrier(dist)
+        t0 = time.perf_counter()
+        for i in range(steps):
+            k = i % len(ctxs)
+            c = ctxs[k]
+            c.begin_scene(desc.view, desc.settings["env"])
+            c.submit_render_meshes(*insts[k])
+            c.end_scene()
+            if pending[k]:   # this context's previous frame, read before its render resets the counters
+                s = c.stats()
+                rays += s["rays_extend"] + s["rays_connect"]
+            c.render(max_bounces=DEPTH, spp=SPP, frame_seed=frame_seed(i, rank), nee=1, rr_start_depth=RR,
+                     accumulate=False, fused_connect=args.fused_connect, tail_paths=args.tail_paths,
+                     fused_from_depth=args.fused_from_depth)
+            c.read_image_async(imgs[k])
+            pending[k] = True
+        for k, c in enumerate(ctxs):
+            c.synchronize()
+            if pending[k]:
+                s = c.stats()
+                rays += s["rays_extend"] + s["rays_connect"]
+        dt = max_over_ranks(dist, time.perf_counter() - t0)
+        b1 = [c.stats() for c in ctxs]
+        h2d = sum(b["h2d_bytes"] - a["h2d_bytes"] for a, b in zip(b0, b1)) // max(1, steps)
+        d2h = sum(b["d2h_bytes"] - a["d2h_bytes"] for a, b in zip(b0, b1)) // max(1, steps)
+        return sum_over_ranks(dist, rays) / dt / 1e6, h2d, d2h
+
+    def scene_arrays(ids_):
+        return (np.array([ids_[m] for m, _, _ in desc.instances], dtype=np.uint32),
+                np.stack([np.asarray(t, dtype=np.float32) for _, t, _ in desc.instances]),
+                np.array([m for _, _, m in desc.instances], dtype=wf.abi.material_ext_dtype))
+
+    e2e_value = e2e_single = None
+    h2d = d2h = 0
+    fif = max(1, args.frames_in_flight)
+    if not args.no_e2e:
+        imgs = [torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True).numpy() if torch is not None
+                else np.zeros((H, W, 4), dtype=np.float32) for _ in range(fif)]
+        e2e_single, h2d, d2h = e2e_loop([r], [scene_arrays(ids)], imgs[:1], args.steps)
+        e2e_value = e2e_single
+        if fif > 1:
+            extra = []
+            for _ in range(fif - 1):
+                rx = wf.Renderer(W, H, device=local, tlas_metric=args.tlas_metric, blas_layout=args.blas_layout,
+                                 instance_bounds=args.instance_bounds)
+                extra.append((rx, build_scene(rx, desc)))
+            ctxs = [r] + [x for x, _ in extra]
+            insts = [scene_arrays(ids)] + [scene_arrays(i_) for _, i_ in extra]
+            e2e_loop(ctxs, insts, imgs, fif)   # each context's buffers allocated, untimed
+            e2e_value, h2d, d2h = e2e_loop(ctxs, insts, imgs, args.steps)
+            for x, _ in extra:
+                x.close()
     # --- CPU baseline (rank 0 only, N = 1 only): the oracle on a bounded sample
     # with the reference's TLAS (tlas_metric 0), and the same pixels with the
     # acceleration structures the GPU line traced (read back from the device)
@@ -789,7 +816,9 @@ def run_ours(args, rank, world, local):
                 "queue_sizes": {"extend": [int(x) for x in last["extend_rays_depth"][:DEPTH + 1]],
                                 "shadow": [int(x) for x in last["shadow_rays_depth"][:DEPTH]]},
                 "e2e": {"value": round(e2e_value, 3) if e2e_value else None, "unit": "Mrays/s",
-                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                        "frames_in_flight": fif,
+                        "single_context": round(e2e_single, 3) if e2e_single else None},
                 "roofline": {"bound": "hbm",
                              "kernel": ("k_trace_pair (extend d + shadow rays d-1)" if args.fused_connect
                                         else f"k_trace (extend; from depth {args.fused_from_depth} with the "
@@ -1011,6 +1040,9 @@ def main():
                          "closest hits)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--frames-in-flight", type=int, default=2,
+                    help="end-to-end leg: frames in flight, one context each (1 = one context, each frame "
+                         "after the previous)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rendering leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-scenes leg")
     ap.add_argument("--no-megakernel", action="store_true", help="skip the megakernel A/B leg")
