@@ -259,6 +259,49 @@ def test_pipelined_frames_with_async_readback_equal_blocking_ones():
     assert not np.array_equal(got[0], got[1])
 
 
+def test_frames_in_flight_on_two_contexts_equal_one_context():
+    """The end-to-end bench's pattern: consecutive frames alternate between
+    two contexts of the same scene (each its own streams and buffers, their
+    launches overlapping on the GPU), scenes resubmitted and images read
+    back asynchronously; every image equals the same frame rendered alone."""
+    torch = pytest.importorskip("torch")
+    desc = scenes.instanced_scene(width=56, height=40, instances=40, freqs=(5, 7), spp=2, max_bounces=6)
+    kw = dict(max_bounces=6, spp=2, nee=1, rr_start_depth=2, accumulate=False, fused_from_depth=2)
+
+    def make():
+        r = Renderer(desc.width, desc.height, tlas_metric=2, instance_bounds=1)
+        ids = [r.create_mesh_from_triangles(t, interval_count=16, max_leaf_prims=4) for t in desc.meshes]
+        arrays = ([ids[m] for m, _, _ in desc.instances],
+                  np.stack([np.asarray(t, np.float32) for _, t, _ in desc.instances]),
+                  np.array([m for _, _, m in desc.instances]))
+        return r, arrays
+
+    ctxs = [make(), make()]
+    try:
+        outs = [torch.empty((desc.height, desc.width, 4), dtype=torch.float32, pin_memory=True).numpy()
+                for _ in range(4)]
+        for i in range(4):
+            r, arrays = ctxs[i % 2]
+            r.begin_scene(desc.view, desc.settings["env"])
+            r.submit_render_meshes(*arrays)
+            r.end_scene()
+            r.render(frame_seed=40 + i, **kw)
+            r.read_image_async(outs[i])
+        for r, _ in ctxs:
+            r.synchronize()
+        got = [o.copy() for o in outs]
+        r, arrays = ctxs[0]
+        for i in range(4):
+            r.begin_scene(desc.view, desc.settings["env"])
+            r.submit_render_meshes(*arrays)
+            r.end_scene()
+            r.render(frame_seed=40 + i, **kw)
+            assert_images_equal(got[i], r.read_image())
+    finally:
+        for r, _ in ctxs:
+            r.close()
+
+
 def test_per_depth_queue_sizes_match_the_oracle(orc):
     desc = scenes.instanced_scene(width=48, height=32, instances=60, freqs=(5, 8), spp=2, max_bounces=5)
     img, want, stats, ost, _, _ = render_both(orc, desc, spp=2, frame_seed=9, nee=1, rr=2)
