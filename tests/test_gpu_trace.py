@@ -163,11 +163,12 @@ def test_trace_device_pointers(orc, box):
     assert_hits_equal(got, want, "device pointers")
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 17, 1025, 9000, 32768])
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 1025, 2048, 2049, 9000, 32768])
 def test_tlas_ploc_matches_oracle(orc, n):
     """tlas_metric 2: the single-block GPU clustering build equals the
     oracle's restatement node for node (same Morton order, neighbour windows,
-    tie rules and node numbering)."""
+    tie rules and node numbering), with its working set in shared memory (up
+    to 2,048 instances) and in global scratch (2,049 on)."""
     rng = np.random.default_rng(100 + n)
     inst = np.zeros(n, dtype=bvh_instance_dtype)
     c = rng.random((n, 3)) * 100
