@@ -263,7 +263,7 @@ static uint32_t best_match(const tlas_node_t* nodes, uint32_t A, const uint32_t*
  * (ties to the lower position); mutual pairs merge into a new node (numbered
  * in list order, left child = the lower position), and the list is compacted
  * in order.  Leaves are nodes 1..n (instance order), the root is copied to 0. */
-#define PLOC_RADIUS 16
+#define PLOC_RADIUS 2
 
 static uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
     uint32_t code = 0;
