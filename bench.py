@@ -19,7 +19,7 @@ Beside the headline: the roofline per depth (extension and shadow-ray
 launches, algorithmic bytes of an instrumented pass over the timed CUDA-event
 time of each depth's launch) and over the secondary depths alone; the same
 frame with the reference's TLAS (tlas_metric 0); the CPU baseline with the
-reference TLAS and with the clustering TLAS on the same pixels; the traversal
+reference TLAS and with the GPU line's own TLAS on the same pixels; the traversal
 micro-benchmark at 4.2M rays per set (closest / any hit, coherent /
 incoherent, as given / Morton-ordered, with its CPU baseline); the plain small,
 differentiable and batched configurations; the megakernel A/B.
@@ -789,7 +789,8 @@ def run_ours(args, rank, world, local):
                 "config": {"workload": WORKLOAD if (W, H) == (1920, 1080) else f"{WORKLOAD} at {W}x{H}",
                            "triangles": desc.triangle_count,
                            "instanced_triangles": desc.instanced_triangle_count, "instances": len(desc.instances),
-                           "tlas_metric": ["reference", "merged-box walk", "parallel clustering"][args.tlas_metric],
+                           "tlas_metric": ["reference", "merged-box walk", "parallel clustering",
+                                           "top-down SAH sweep"][args.tlas_metric],
                            "blas_layout": ["binary child pairs", "quantized 4-wide", "exact 4-wide"][args.blas_layout],
                            "instance_bounds": ["transformed BLAS root box",
                                                "BLAS frontier boxes (tight)"][args.instance_bounds],
@@ -1031,8 +1032,9 @@ def main():
     ap.add_argument("--instance-bounds", type=int, default=DEFAULT_INSTANCE_BOUNDS, choices=[0, 1],
                     help="instance world boxes: 0 = the transformed BLAS root box (the reference's), "
                          "1 = from the BLAS frontier boxes (tight)")
-    ap.add_argument("--tlas-metric", type=int, default=2,
-                    help="TLAS build: 0 = reference walk and metric, 1 = merged-box walk, 2 = parallel clustering")
+    ap.add_argument("--tlas-metric", type=int, default=3,
+                    help="TLAS build: 0 = reference walk and metric, 1 = merged-box walk, 2 = parallel clustering, "
+                         "3 = top-down SAH sweep")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--blas-layout", type=int, default=0, choices=[0, 1, 2],
                     help="BLAS layout the traversal reads: 0 = the reference's binary child pairs, 1 = quantized "

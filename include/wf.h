@@ -53,7 +53,9 @@ typedef struct wf_init_params {
     uint32_t tlas_metric;       /* TLAS build: 0 = the reference's agglomerative walk and pairing metric
                                    (tlas_builder.cpp:96-97, bit-exact), 1 = the same walk pairing by the
                                    half area of the merged box (better trees), 2 = parallel
-                                   locally-ordered clustering on the merged-box area (fast rebuilds) */
+                                   locally-ordered clustering on the merged-box area (fast rebuilds),
+                                   3 = top-down surface-area-heuristic sweep over every boundary of
+                                   the box centres' x / y / z orders (the cheapest trees to traverse) */
     /* BLAS layout the traversal reads: 0 = the reference's binary tree, child
      * pairs of 32-byte nodes (bvh_node_t) walked in the reference's order;
      * 1 = the same tree collapsed to 4-wide 64-byte nodes with child boxes

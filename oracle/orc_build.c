@@ -263,7 +263,9 @@ static uint32_t best_match(const tlas_node_t* nodes, uint32_t A, const uint32_t*
  * (ties to the lower position); mutual pairs merge into a new node (numbered
  * in list order, left child = the lower position), and the list is compacted
  * in order.  Leaves are nodes 1..n (instance order), the root is copied to 0. */
+#ifndef PLOC_RADIUS
 #define PLOC_RADIUS 2
+#endif
 
 static uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
     uint32_t code = 0;
@@ -372,13 +374,157 @@ static void tlas_ploc(const bvh_instance_t* inst, uint32_t n, tlas_node_t* nodes
     free(nn);
 }
 
+/* ---- TLAS metric 3: top-down full-sweep SAH ---------------------------------
+ * The GPU library's highest-quality TLAS build (MacDonald and Booth's surface
+ * area heuristic, evaluated at every boundary).  Three lists hold the
+ * instances ordered by box centre along x, y and z (centre = (min + max) *
+ * 0.5, its bits mapped so that unsigned order is float order with -0 below
+ * +0; ties by instance index).  A list range [s, e) of two or more instances
+ * splits after the position k (s <= k < e - 1) of smallest cost
+ * A(s..k) * (k - s + 1) + A(k+1..e-1) * (e - k - 1), A the half area of the
+ * range part's union box in float (unions by smin / smax), over the three axes' lists (ties to the
+ * lower axis, then the lower k); the other two lists are partitioned stably
+ * by side, so a range holds the same instances in all three lists.  Every
+ * boundary between list positions is split exactly once, so the interior
+ * node of a range split after position k is node n + 1 + k; leaves are nodes
+ * 1..n (instance order); the root is copied to node 0. */
+static uint32_t sortable_bits(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+/* min / max in the order of sortable_bits (-0 below +0): associative and
+ * commutative, so a union box's bits do not depend on the order it is
+ * accumulated in (the GPU build scans ranges in warp-sized pieces) */
+static inline float smin(float x, float y) { return sortable_bits(y) < sortable_bits(x) ? y : x; }
+static inline float smax(float x, float y) { return sortable_bits(x) < sortable_bits(y) ? y : x; }
+
+typedef struct {
+    const bvh_instance_t* inst;
+    tlas_node_t* nodes;
+    uint32_t n;
+    uint32_t* list[3];
+    uint32_t* tmp;
+    uint8_t* left;
+    float* pre;    /* 6 floats per position: prefix union box */
+    float* cost;   /* per position k: the cost of splitting after k */
+} Sweep;
+
+/* Splits list range [s, e) (two or more instances): returns the position k
+ * the range splits after, the range's box in mn / mx, and leaves the three
+ * lists partitioned. */
+static uint32_t sweep_split(Sweep* w, uint32_t s, uint32_t e, float* rmn, float* rmx) {
+    float best = FLT_MAX;
+    int bax = -1;
+    uint32_t bk = s;
+    for (int ax = 0; ax < 3; ++ax) {
+        const uint32_t* L = w->list[ax];
+        float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (uint32_t i = s; i < e; ++i) {
+            const bvh_instance_t* b = &w->inst[L[i]];
+            for (int a = 0; a < 3; ++a) { mn[a] = smin(mn[a], b->aabb_min[a]); mx[a] = smax(mx[a], b->aabb_max[a]); }
+            memcpy(&w->pre[6ull * i], mn, 12);
+            memcpy(&w->pre[6ull * i + 3], mx, 12);
+        }
+        if (ax == 0) { memcpy(rmn, mn, 12); memcpy(rmx, mx, 12); }
+        /* suffix sweep from the end: the candidate after k pairs prefix k with suffix k + 1 */
+        float smn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, smx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (uint32_t i = e - 1; i > s; --i) {
+            const bvh_instance_t* b = &w->inst[L[i]];
+            for (int a = 0; a < 3; ++a) { smn[a] = smin(smn[a], b->aabb_min[a]); smx[a] = smax(smx[a], b->aabb_max[a]); }
+            w->cost[i - 1] = half_area(&w->pre[6ull * (i - 1)], &w->pre[6ull * (i - 1) + 3]) * (float)(i - s) +
+                             half_area(smn, smx) * (float)(e - i);
+        }
+        for (uint32_t k = s; k + 1 < e; ++k)
+            if (w->cost[k] < best) { best = w->cost[k]; bax = ax; bk = k; }
+    }
+    if (bax < 0) { bax = 0; bk = s; }   /* no cost below FLT_MAX (not for finite boxes) */
+    for (uint32_t i = s; i < e; ++i) w->left[w->list[bax][i]] = (uint8_t)(i <= bk);
+    for (int ax = 0; ax < 3; ++ax) {
+        if (ax == bax) continue;
+        uint32_t* L = w->list[ax];
+        uint32_t p = s;
+        for (uint32_t i = s; i < e; ++i) if (w->left[L[i]]) w->tmp[p++] = L[i];
+        for (uint32_t i = s; i < e; ++i) if (!w->left[L[i]]) w->tmp[p++] = L[i];
+        memcpy(&L[s], &w->tmp[s], sizeof(uint32_t) * (e - s));
+    }
+    return bk;
+}
+
+static void tlas_sweep(const bvh_instance_t* inst, uint32_t n, tlas_node_t* nodes) {
+    for (uint32_t i = 0; i < n; ++i) {
+        memcpy(nodes[1 + i].aabb_min, inst[i].aabb_min, 12);
+        memcpy(nodes[1 + i].aabb_max, inst[i].aabb_max, 12);
+        nodes[1 + i].instance_idx = i;
+        nodes[1 + i].left_right = 0;
+    }
+    if (n == 0) return;
+    Sweep w;
+    w.inst = inst;
+    w.nodes = nodes;
+    w.n = n;
+    uint64_t* key = (uint64_t*)malloc(sizeof(uint64_t) * n);
+    for (int ax = 0; ax < 3; ++ax) {
+        for (uint32_t i = 0; i < n; ++i) {
+            const float c = (inst[i].aabb_min[ax] + inst[i].aabb_max[ax]) * 0.5f;
+            key[i] = ((uint64_t)sortable_bits(c) << 32) | i;
+        }
+        qsort(key, n, sizeof(uint64_t), cmp_u64);
+        w.list[ax] = (uint32_t*)malloc(sizeof(uint32_t) * n);
+        for (uint32_t i = 0; i < n; ++i) w.list[ax][i] = (uint32_t)(key[i] & 0xFFFFFFFFu);
+    }
+    w.tmp = (uint32_t*)malloc(sizeof(uint32_t) * n);
+    w.left = (uint8_t*)malloc(n);
+    w.pre = (float*)malloc(sizeof(float) * 6 * n);
+    w.cost = (float*)malloc(sizeof(float) * n);
+    /* ranges to split: (s, e, parent node, 0 = left / 1 = right child); an
+     * explicit stack, since a range can be as deep as it is long */
+    uint32_t* task = (uint32_t*)malloc(sizeof(uint32_t) * 4 * n);
+    uint32_t top = 0, root = 1;
+    task[0] = 0; task[1] = n; task[2] = 0; task[3] = 2;
+    top = 1;
+    while (top) {
+        --top;
+        const uint32_t s = task[4 * top], e = task[4 * top + 1], parent = task[4 * top + 2], slot = task[4 * top + 3];
+        uint32_t id;
+        if (e - s == 1) {
+            id = 1 + w.list[0][s];
+        } else {
+            float mn[3], mx[3];
+            const uint32_t k = sweep_split(&w, s, e, mn, mx);
+            id = n + 1 + k;
+            tlas_node_t* t = &nodes[id];
+            memcpy(t->aabb_min, mn, 12);
+            memcpy(t->aabb_max, mx, 12);
+            t->left_right = 0;
+            t->instance_idx = 0;
+            /* right range below the left one: the left is taken first */
+            task[4 * top] = k + 1; task[4 * top + 1] = e; task[4 * top + 2] = id; task[4 * top + 3] = 1;
+            ++top;
+            task[4 * top] = s; task[4 * top + 1] = k + 1; task[4 * top + 2] = id; task[4 * top + 3] = 0;
+            ++top;
+        }
+        if (slot == 2) root = id;
+        else nodes[parent].left_right |= (slot == 0) ? (id << 16) : id;
+    }
+    nodes[0] = nodes[root];
+    for (int ax = 0; ax < 3; ++ax) free(w.list[ax]);
+    free(w.tmp);
+    free(w.left);
+    free(w.pre);
+    free(w.cost);
+    free(task);
+    free(key);
+}
+
 /* tlas_builder_t::build + extract (tlas_builder.cpp:6-84).  The reference's
  * working list is a 256-entry stack array (:14); this one is sized to n.
  * metric 0 is the reference's pairing metric; metric 1 replaces it by the
  * half area of the merged box (same walk, same tie rule). */
 int orc_tlas_build_metric(const bvh_instance_t* inst, uint32_t n, uint32_t metric, uint8_t** out_blob,
                           uint64_t* out_size) {
-    if (!out_blob || !out_size || (n > 0 && !inst) || n > 32768 || metric > 2) return -1;
+    if (!out_blob || !out_size || (n > 0 && !inst) || n > 32768 || metric > 3) return -1;
     uint32_t ncount = n * 2;
     tlas_node_t* nodes = (tlas_node_t*)calloc(ncount ? ncount : 1, sizeof(tlas_node_t));
     uint32_t* idx = (uint32_t*)calloc(n ? n : 1, sizeof(uint32_t));
@@ -391,8 +537,9 @@ int orc_tlas_build_metric(const bvh_instance_t* inst, uint32_t n, uint32_t metri
         nodes[at].left_right = 0;
         at++;
     }
-    if (metric == 2) {
-        tlas_ploc(inst, n, nodes);
+    if (metric == 2 || metric == 3) {
+        if (metric == 2) tlas_ploc(inst, n, nodes);
+        else tlas_sweep(inst, n, nodes);
         at = n ? 2 * n : 1;
     } else if (n > 0) {
         uint32_t A = 0;

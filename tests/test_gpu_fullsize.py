@@ -79,7 +79,7 @@ def test_soup_8m_blas_and_16m_ray_sets(orc):
 
 
 def test_instanced_1080p_frame(orc):
-    """The benchmark frame (clustering TLAS over tight instance boxes, as the
+    """The benchmark frame (SAH-sweep TLAS over tight instance boxes, as the
     bench runs it): the oracle renders six bands of 2,048 pixels of
     the same frame from the GPU's own BLAS, instances and TLAS, and those
     pixels must equal the GPU image bit for bit; over the whole frame the
@@ -91,7 +91,7 @@ def test_instanced_1080p_frame(orc):
     st = desc.settings
     kw = dict(max_bounces=8, spp=16, frame_seed=5, nee=1, rr_start_depth=3, accumulate=False)
     assert (st["spp"], st["max_bounces"], st["rr_start_depth"], st["nee"]) == (16, 8, 3, 1)
-    with Renderer(w, h, tlas_metric=2, instance_bounds=1) as r:
+    with Renderer(w, h, tlas_metric=3, instance_bounds=1) as r:
         ids = load_scene_into(r, desc)
         sc, _ = oracle_scene_from_renderer(orc, desc, r, ids)
         r.render(**kw)

@@ -163,12 +163,14 @@ def test_trace_device_pointers(orc, box):
     assert_hits_equal(got, want, "device pointers")
 
 
+@pytest.mark.parametrize("metric", [2, 3])
 @pytest.mark.parametrize("n", [1, 2, 3, 17, 1025, 2048, 2049, 9000, 32768])
-def test_tlas_ploc_matches_oracle(orc, n):
-    """tlas_metric 2: the single-block GPU clustering build equals the
-    oracle's restatement node for node (same Morton order, neighbour windows,
-    tie rules and node numbering), with its working set in shared memory (up
-    to 2,048 instances) and in global scratch (2,049 on)."""
+def test_tlas_ploc_matches_oracle(orc, n, metric):
+    """tlas_metric 2 / 3: the single-block GPU clustering build and the
+    top-down SAH sweep equal the oracle's restatements node for node (same
+    orders, neighbour windows or sweeps, tie rules and node numbering), with
+    their working sets in shared memory (up to 2,048 instances) and in global
+    scratch (2,049 on)."""
     rng = np.random.default_rng(100 + n)
     inst = np.zeros(n, dtype=bvh_instance_dtype)
     c = rng.random((n, 3)) * 100
@@ -177,16 +179,28 @@ def test_tlas_ploc_matches_oracle(orc, n):
     if n > 5:
         inst[4] = inst[3]
         inst["aabb_min"][5] = inst["aabb_max"][5] = inst["aabb_min"][2]   # a degenerate box
-    with Renderer(8, 8, tlas_metric=2) as r:
-        assert np.array_equal(r.tlas_build(inst), orc.tlas_build(inst, metric=2)), n
+    with Renderer(8, 8, tlas_metric=metric) as r:
+        assert np.array_equal(r.tlas_build(inst), orc.tlas_build(inst, metric=metric)), n
 
 
-def test_render_with_ploc_tlas_bit_exact(orc):
+def test_tlas_sweep_all_centres_equal(orc):
+    """The sweep over 300 identical boxes: every split ties, the tree is a
+    300-deep chain (300 levels of the build), equal to the oracle's."""
+    n = 300
+    inst = np.zeros(n, dtype=bvh_instance_dtype)
+    inst["aabb_min"] = -1.0
+    inst["aabb_max"] = 1.0
+    with Renderer(8, 8, tlas_metric=3) as r:
+        assert np.array_equal(r.tlas_build(inst), orc.tlas_build(inst, metric=3))
+
+
+@pytest.mark.parametrize("metric", [2, 3])
+def test_render_with_ploc_tlas_bit_exact(orc, metric):
     desc = scenes.instanced_scene(width=64, height=36, instances=200, freqs=(6, 9), spp=1, max_bounces=5)
-    with Renderer(desc.width, desc.height, tlas_metric=2) as r:
+    with Renderer(desc.width, desc.height, tlas_metric=metric) as r:
         ids = load_scene_into(r, desc)
         sc, bi = oracle_scene_from_renderer(orc, desc, r, ids)
-        assert np.array_equal(r.scene_tlas(), orc.tlas_build(bi, metric=2))
+        assert np.array_equal(r.scene_tlas(), orc.tlas_build(bi, metric=metric))
         r.render(max_bounces=5, spp=2, frame_seed=8, nee=1, rr_start_depth=3, accumulate=False)
         got = r.read_image()
     acc, _ = sc.render(desc.view, desc.width, desc.height, max_bounces=5, spp=2, frame_seed=8, nee=1,

@@ -118,11 +118,12 @@ def _tlas_nodes(blob):
     return f[:, 0:3], f[:, 4:7], u[:, 3], u[:, 7]
 
 
+@pytest.mark.parametrize("metric", [2, 3])
 @pytest.mark.parametrize("n", [1, 2, 3, 17, 1000, 5000])
-def test_tlas_ploc_is_a_valid_tree(orc, n):
-    """tlas_metric 2 (parallel locally-ordered clustering): leaves 1..n in
-    instance order, every instance reached exactly once from the root, every
-    box the union of its children's."""
+def test_tlas_ploc_is_a_valid_tree(orc, n, metric):
+    """tlas_metric 2 (parallel locally-ordered clustering) and 3 (top-down
+    SAH sweep): leaves 1..n in instance order, every instance reached exactly
+    once from the root, every box the union of its children's."""
     rng = np.random.default_rng(n)
     inst = np.zeros(n, dtype=bvh_instance_dtype)
     c = rng.random((n, 3)) * 100
@@ -130,7 +131,7 @@ def test_tlas_ploc_is_a_valid_tree(orc, n):
     inst["aabb_max"] = (c + rng.random((n, 3))).astype(np.float32)
     if n > 3:
         inst[3] = inst[2]                      # a duplicate box
-    blob = orc.tlas_build(inst, metric=2)
+    blob = orc.tlas_build(inst, metric=metric)
     mn, mx, lr, ii = _tlas_nodes(blob)
     assert len(mn) == 2 * n
     for i in range(n):
@@ -148,10 +149,31 @@ def test_tlas_ploc_is_a_valid_tree(orc, n):
     assert sorted(seen) == list(range(n))
 
 
-def test_tlas_ploc_all_centres_equal(orc):
+@pytest.mark.parametrize("metric", [2, 3])
+def test_tlas_ploc_all_centres_equal(orc, metric):
     n = 300
     inst = np.zeros(n, dtype=bvh_instance_dtype)
     inst["aabb_min"] = -1.0
     inst["aabb_max"] = 1.0
-    mn, mx, lr, ii = _tlas_nodes(orc.tlas_build(inst, metric=2))
+    mn, mx, lr, ii = _tlas_nodes(orc.tlas_build(inst, metric=metric))
     assert len(mn) == 2 * n and lr[0] != 0
+
+
+def test_tlas_sweep_beats_clustering_on_sah(orc):
+    """The sweep's tree has the smaller surface-area cost (sum of interior
+    box areas over the root's) on random instance boxes."""
+    n = 1000
+    rng = np.random.default_rng(12)
+    inst = np.zeros(n, dtype=bvh_instance_dtype)
+    c = rng.random((n, 3)) * 100
+    r = rng.uniform(0.5, 2.0, (n, 1))
+    inst["aabb_min"] = (c - r).astype(np.float32)
+    inst["aabb_max"] = (c + r).astype(np.float32)
+
+    def sah(blob):
+        mn, mx, lr, _ = _tlas_nodes(blob)
+        e = np.maximum(mx - mn, 0.0).astype(np.float64)
+        a = e[:, 0] * e[:, 1] + e[:, 1] * e[:, 2] + e[:, 2] * e[:, 0]
+        return a[1:][lr[1:] != 0].sum() / a[0]
+
+    assert sah(orc.tlas_build(inst, metric=3)) < sah(orc.tlas_build(inst, metric=2))

@@ -835,9 +835,9 @@ int wf_create(const wf_init_params* p, wf_ctx** out) {
     c->device = p->device;
     c->width = p->render_width;
     c->height = p->render_height;
-    if (p->tlas_metric > 2) {
+    if (p->tlas_metric > 3) {
         delete c;
-        return fail(WF_ERR_INVALID, "wf_create: tlas_metric must be 0, 1 or 2");
+        return fail(WF_ERR_INVALID, "wf_create: tlas_metric must be 0, 1, 2 or 3");
     }
     c->tlas_metric = p->tlas_metric;
     if (p->blas_layout > 2) {

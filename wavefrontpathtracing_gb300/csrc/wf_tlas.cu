@@ -377,6 +377,390 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restr
     }
 }
 
+// ---------------------------------------------------------------------------
+// metric 3: top-down full-sweep SAH, one block of 1024 threads.  Three lists
+// of the instances by box centre along x, y, z (one bitonic network over the
+// three axes' (sortable centre bits, index) keys); then level by level: a
+// range [s, e) of more than 8 instances goes to a team of three warps, one
+// per axis (warp scans of the prefix union boxes, their half areas kept per
+// position, then of the suffix boxes, each boundary's cost A(left) * |left|
+// + A(right) * |right| in float), which takes the cheapest boundary (ties to
+// the lower axis, then the lower position), partitions the other two lists
+// stably and queues the two halves for the next level; a range of up to 8
+// goes to one thread, which builds its whole subtree the same way.  The interior node of a range split after position k is node
+// n + 1 + k (every boundary is split once), so node numbers do not depend on
+// which warp takes which range; a child sets its half of the parent's
+// left_right word.  Identical, node for node, to the oracle's tlas_sweep.
+__device__ __forceinline__ uint32_t sortable_bits(float x) {
+    const uint32_t u = __float_as_uint(x);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+// min / max in sortable-bits order (-0 below +0): associative, so a union
+// box's bits do not depend on how a scan groups it
+__device__ __forceinline__ float smin(float x, float y) { return sortable_bits(y) < sortable_bits(x) ? y : x; }
+__device__ __forceinline__ float smax(float x, float y) { return sortable_bits(x) < sortable_bits(y) ? y : x; }
+__device__ __forceinline__ float half_area3(const float* mn, const float* mx) {
+    const float ex = mx[0] - mn[0], ey = mx[1] - mn[1], ez = mx[2] - mn[2];
+    return ex * ey + ey * ez + ez * ex;
+}
+
+constexpr uint32_t kSweepSmemMax = 2048;
+
+// Boxes live as sortable bits (an unsigned order equal to float order, -0
+// below +0), so a union is an integer min / max: order-independent, and one
+// instruction.  A box: min x, y, z then max x, y, z.
+__device__ __forceinline__ float from_sortable(uint32_t s) {
+    return __uint_as_float((s & 0x80000000u) ? (s & 0x7FFFFFFFu) : ~s);
+}
+__device__ __forceinline__ float half_area_sb(const uint32_t* b) {
+    const float ex = from_sortable(b[3]) - from_sortable(b[0]);
+    const float ey = from_sortable(b[4]) - from_sortable(b[1]);
+    const float ez = from_sortable(b[5]) - from_sortable(b[2]);
+    return ex * ey + ey * ez + ez * ex;
+}
+
+struct SweepScratch {
+    uint32_t* list[3];    // n each
+    uint32_t* tmp;        // n
+    uint32_t* left;       // n: 1 = the instance is in its range's left part
+    float* area[3];       // per axis and position: the half area of the prefix union box
+    unsigned long long* key;   // 3 P sort keys (the same words as area, before the sweep)
+    uint32_t* box;        // 6 per instance
+    uint32_t* task[2];    // per level: (s | e << 16, parent | slot << 16), n / 2 + 1 each
+};
+
+__host__ __device__ inline size_t sweep_words(uint32_t n, uint32_t P) {
+    return 6ull * P + 3ull * n + n + n + 6ull * n + 2ull * 2 * (n / 2 + 1);
+}
+
+__device__ inline SweepScratch sweep_carve(uint32_t* base, uint32_t n, uint32_t P) {
+    SweepScratch S;
+    S.key = reinterpret_cast<unsigned long long*>(base);   // first: 8-byte aligned
+    for (int a = 0; a < 3; ++a) S.area[a] = reinterpret_cast<float*>(base) + (size_t)a * n;
+    uint32_t* w = base + 6ull * P;
+    S.list[0] = w; S.list[1] = w + n; S.list[2] = w + 2 * n;
+    S.tmp = w + 3 * n;
+    S.left = w + 4 * n;
+    S.box = w + 5 * n;
+    S.task[0] = w + 11 * n;
+    S.task[1] = S.task[0] + 2 * (n / 2 + 1);
+    return S;
+}
+
+struct Split {
+    float cost;
+    uint32_t ax, k;
+};
+__device__ __forceinline__ bool better(const Split& a, const Split& b) {
+    return a.cost < b.cost || (a.cost == b.cost && (a.ax < b.ax || (a.ax == b.ax && a.k < b.k)));
+}
+
+// the identity of a box union: min fields at the top of the order, max at the bottom
+constexpr uint32_t kSbEmptyMin = 0xFFFFFFFFu, kSbEmptyMax = 0u;
+
+// Stable partition of list ax over [s, e) by S.left (nleft left instances), by one thread.
+__device__ void partition_serial(const SweepScratch& S, uint32_t s, uint32_t e, uint32_t ax) {
+    uint32_t* L = S.list[ax];
+    uint32_t p = s;
+    for (uint32_t i = s; i < e; ++i) if (S.left[L[i]]) S.tmp[p++] = L[i];
+    for (uint32_t i = s; i < e; ++i) if (!S.left[L[i]]) S.tmp[p++] = L[i];
+    for (uint32_t i = s; i < e; ++i) L[i] = S.tmp[i];
+}
+
+// One thread: the split of range [s, e) (e - s >= 2) by a sequential sweep,
+// the same candidates as the warps' sweeps; the lists left partitioned, the
+// range's box in rb.
+__device__ uint32_t sweep_serial(const SweepScratch& S, uint32_t s, uint32_t e, uint32_t* rb) {
+    Split best{FLT_MAX, 3u, 0u};
+    for (uint32_t ax = 0; ax < 3; ++ax) {
+        const uint32_t* L = S.list[ax];
+        float* A = S.area[ax];
+        uint32_t c[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+        for (uint32_t i = s; i < e; ++i) {
+            const uint32_t* b = S.box + 6ull * L[i];
+            for (int a = 0; a < 3; ++a) { c[a] = min(c[a], b[a]); c[3 + a] = max(c[3 + a], b[3 + a]); }
+            A[i] = half_area_sb(c);
+        }
+        if (ax == 0)
+            for (int a = 0; a < 6; ++a) rb[a] = c[a];
+        uint32_t q[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+        for (uint32_t i = e - 1; i > s; --i) {
+            const uint32_t* b = S.box + 6ull * L[i];
+            for (int a = 0; a < 3; ++a) { q[a] = min(q[a], b[a]); q[3 + a] = max(q[3 + a], b[3 + a]); }
+            const uint32_t k = i - 1;
+            const float cost = A[k] * (float)(k - s + 1) + half_area_sb(q) * (float)(e - 1 - k);
+            const Split cand{cost, ax, k};
+            if (cost < FLT_MAX && better(cand, best)) best = cand;
+        }
+    }
+    uint32_t bax = best.ax, bk = best.k;
+    if (bax == 3u) { bax = 0u; bk = s; }   // no cost below FLT_MAX (not for finite boxes)
+    for (uint32_t i = s; i < e; ++i) S.left[S.list[bax][i]] = i <= bk ? 1u : 0u;
+    for (uint32_t ax = 0; ax < 3; ++ax)
+        if (ax != bax) partition_serial(S, s, e, ax);
+    return bk;
+}
+
+__device__ __forceinline__ void store_sweep_node(float4* nodes, uint32_t id, const uint32_t* rb) {
+    nodes[2 * id] = make_float4(from_sortable(rb[0]), from_sortable(rb[1]), from_sortable(rb[2]), __uint_as_float(0u));
+    nodes[2 * id + 1] = make_float4(from_sortable(rb[3]), from_sortable(rb[4]), from_sortable(rb[5]), __uint_as_float(0u));
+}
+__device__ __forceinline__ void link_child(float4* nodes, uint32_t parent, uint32_t slot, uint32_t id) {
+    atomicOr(reinterpret_cast<uint32_t*>(nodes + 2 * parent) + 3, slot == 0u ? (id << 16) : id);
+}
+
+// One thread builds the whole subtree of a small range [s, e) (2 <= e - s
+// <= kSweepSerial) below parent / slot, depth-first.
+#ifndef WF_SWEEP_SERIAL
+#define WF_SWEEP_SERIAL 4
+#endif
+constexpr uint32_t kSweepSerial = WF_SWEEP_SERIAL;
+__device__ void sweep_subtree(const SweepScratch& S, float4* nodes, uint32_t n, uint32_t s0, uint32_t e0,
+                              uint32_t parent0, uint32_t slot0, uint32_t* root) {
+    uint32_t st[3 * kSweepSerial];
+    uint32_t top = 0;
+    st[0] = s0 | (e0 << 16); st[1] = parent0; st[2] = slot0;
+    top = 1;
+    while (top) {
+        --top;
+        const uint32_t s = st[3 * top] & 0xFFFFu, e = st[3 * top] >> 16, parent = st[3 * top + 1], slot = st[3 * top + 2];
+        uint32_t id;
+        if (e - s == 1) {
+            id = 1 + S.list[0][s];
+        } else {
+            uint32_t rb[6];
+            const uint32_t k = sweep_serial(S, s, e, rb);
+            id = n + 1 + k;
+            store_sweep_node(nodes, id, rb);
+            st[3 * top] = (k + 1) | (e << 16); st[3 * top + 1] = id; st[3 * top + 2] = 1u;
+            ++top;
+            st[3 * top] = s | ((k + 1) << 16); st[3 * top + 1] = id; st[3 * top + 2] = 0u;
+            ++top;
+        }
+        if (slot == 2u) *root = id;
+        else link_child(nodes, parent, slot, id);
+    }
+}
+
+// Inclusive warp scan of a sortable box (min fields by min, max fields by max).
+__device__ __forceinline__ void warp_scan_box(uint32_t* v, uint32_t lane) {
+    for (int off = 1; off < 32; off <<= 1)
+        for (int a = 0; a < 6; ++a) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, v[a], off);
+            if ((int)lane >= off) v[a] = a < 3 ? min(o, v[a]) : max(o, v[a]);
+        }
+}
+
+// One warp, one axis of range [s, e) (e - s >= 2): the prefix areas, then
+// the cheapest boundary along the axis (ties to the lower position); the
+// range's box in rb (every lane).
+__device__ Split sweep_axis(const SweepScratch& S, uint32_t ax, uint32_t s, uint32_t e, uint32_t* rb) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned FULL = 0xffffffffu;
+    const uint32_t* L = S.list[ax];
+    float* A = S.area[ax];
+    Split best{FLT_MAX, 3u, 0u};
+    uint32_t cb[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+    for (uint32_t c = s; c < e; c += 32) {
+        const uint32_t i = c + lane;
+        uint32_t v[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+        if (i < e) {
+            const uint32_t* b = S.box + 6ull * L[i];
+            for (int a = 0; a < 6; ++a) v[a] = b[a];
+        }
+        warp_scan_box(v, lane);
+        for (int a = 0; a < 6; ++a) v[a] = a < 3 ? min(cb[a], v[a]) : max(cb[a], v[a]);
+        if (i < e) A[i] = half_area_sb(v);
+        const uint32_t last = min(31u, e - 1 - c);
+        for (int a = 0; a < 6; ++a) cb[a] = __shfl_sync(FULL, v[a], last);
+    }
+    for (int a = 0; a < 6; ++a) rb[a] = cb[a];
+    __syncwarp();
+    // suffix boxes from the end; position i's suffix pairs with the prefix at i - 1
+    for (int a = 0; a < 6; ++a) cb[a] = a < 3 ? kSbEmptyMin : kSbEmptyMax;
+    for (uint32_t c = 0; c < e - s; c += 32) {
+        const uint32_t j = c + lane;   // j-th position from the end
+        const bool valid = j < e - s;
+        const uint32_t i = e - 1 - j;
+        uint32_t v[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+        if (valid) {
+            const uint32_t* b = S.box + 6ull * L[i];
+            for (int a = 0; a < 6; ++a) v[a] = b[a];
+        }
+        warp_scan_box(v, lane);
+        for (int a = 0; a < 6; ++a) v[a] = a < 3 ? min(cb[a], v[a]) : max(cb[a], v[a]);
+        if (valid && i > s) {
+            const uint32_t k = i - 1;
+            const float cost = A[k] * (float)(k - s + 1) + half_area_sb(v) * (float)(e - 1 - k);
+            const Split cand{cost, ax, k};
+            if (cost < FLT_MAX && better(cand, best)) best = cand;
+        }
+        const uint32_t last = min(31u, e - s - 1 - c);
+        for (int a = 0; a < 6; ++a) cb[a] = __shfl_sync(FULL, v[a], last);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const Split o{__shfl_xor_sync(FULL, best.cost, off), __shfl_xor_sync(FULL, best.ax, off),
+                      __shfl_xor_sync(FULL, best.k, off)};
+        if (better(o, best)) best = o;
+    }
+    return best;
+}
+
+// One warp: stable partition of list ax over [s, e) by S.left (nleft left
+// instances), through the axis's own prefix-area words (free once the split
+// is chosen; the two lists of a range are partitioned at the same time).
+__device__ void partition_warp(const SweepScratch& S, uint32_t ax, uint32_t s, uint32_t e, uint32_t nleft) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned FULL = 0xffffffffu;
+    uint32_t* L = S.list[ax];
+    uint32_t* T = reinterpret_cast<uint32_t*>(S.area[ax]);
+    uint32_t nl = 0, nr = 0;
+    for (uint32_t c = s; c < e; c += 32) {
+        const uint32_t i = c + lane;
+        const bool valid = i < e;
+        const uint32_t id = valid ? L[i] : 0u;
+        const bool isl = valid && S.left[id] != 0u;
+        const unsigned ml = __ballot_sync(FULL, isl), mr = __ballot_sync(FULL, valid && !isl);
+        const unsigned below = (1u << lane) - 1u;
+        if (isl) T[s + nl + __popc(ml & below)] = id;
+        else if (valid) T[s + nleft + nr + __popc(mr & below)] = id;
+        nl += __popc(ml);
+        nr += __popc(mr);
+    }
+    __syncwarp();
+    for (uint32_t i = s + lane; i < e; i += 32) L[i] = T[i];
+    __syncwarp();
+}
+
+__device__ __forceinline__ void team_sync(uint32_t team) {
+    asm volatile("bar.sync %0, %1;" ::"r"(team + 1u), "r"(96) : "memory");
+}
+
+__global__ void __launch_bounds__(kPlocThreads) k_tlas_sweep(const float* __restrict__ aabbs, uint32_t n,
+                                                             float4* nodes, uint32_t* scratch, uint32_t P,
+                                                             bool smem) {
+    extern __shared__ unsigned long long s_dyn[];
+    constexpr uint32_t kTeams = kPlocThreads / 96;   // three warps each
+    __shared__ uint32_t s_count[2], s_root;
+    __shared__ Split s_split[kTeams][3];
+    __shared__ uint32_t s_box[kTeams][6];
+    const SweepScratch S = sweep_carve(smem ? reinterpret_cast<uint32_t*>(s_dyn) : scratch, n, P);
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    const uint32_t team = warp / 3u, axw = warp % 3u;
+    for (uint32_t i = t; i < n; i += kPlocThreads) {
+        const float* b = aabbs + 6ull * i;
+        nodes[2 * (1 + i)] = make_float4(b[0], b[1], b[2], __uint_as_float(0u));
+        nodes[2 * (1 + i) + 1] = make_float4(b[3], b[4], b[5], __uint_as_float(i));
+        for (int a = 0; a < 6; ++a) S.box[6ull * i + a] = sortable_bits(b[a]);
+    }
+    // the three sorted lists, sorted together: keys of axis a at [a P, (a + 1) P)
+    unsigned long long* key = S.key;
+    const uint32_t lgP = 31u - __clz(P);
+    for (uint32_t q = t; q < 3 * P; q += kPlocThreads) {
+        const uint32_t ax = q >> lgP, i = q & (P - 1);
+        if (i < n) {
+            const float c = (aabbs[6ull * i + ax] + aabbs[6ull * i + 3 + ax]) * 0.5f;
+            key[q] = ((unsigned long long)sortable_bits(c) << 32) | i;
+        } else {
+            key[q] = ~0ull;
+        }
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= P; size <<= 1)
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t q = t; q < 3 * P; q += kPlocThreads) {
+                const uint32_t i = q & (P - 1), j = i ^ stride;
+                if (j > i) {
+                    const uint32_t o = q - i;
+                    const unsigned long long x = key[o + i], y = key[o + j];
+                    const bool up = (i & size) == 0;
+                    if (up ? (x > y) : (x < y)) { key[o + i] = y; key[o + j] = x; }
+                }
+            }
+            __syncthreads();
+        }
+    // (the keys' words become the prefix areas after the next barrier)
+    for (uint32_t q = t; q < 3 * P; q += kPlocThreads) {
+        const uint32_t ax = q >> lgP, i = q & (P - 1);
+        if (i < n) S.list[ax][i] = (uint32_t)(key[q] & 0xFFFFFFFFull);
+    }
+    if (t == 0) {
+        s_root = 1u;   // a single instance is its own root
+        s_count[0] = n >= 2 ? 1u : 0u;
+        s_count[1] = 0u;
+        S.task[0][0] = 0u | (n << 16);
+        S.task[0][1] = 0u | (2u << 16);   // slot 2: the root
+    }
+    __syncthreads();
+    uint32_t cur = 0;
+    while (s_count[cur] > 0) {
+        const uint32_t ntask = s_count[cur];
+        // small ranges: one thread builds each one's whole subtree
+        for (uint32_t q = t; q < ntask; q += kPlocThreads) {
+            const uint32_t r0 = S.task[cur][2 * q], r1 = S.task[cur][2 * q + 1];
+            const uint32_t s = r0 & 0xFFFFu, e = r0 >> 16;
+            if (e - s <= kSweepSerial) sweep_subtree(S, nodes, n, s, e, r1 & 0xFFFFu, r1 >> 16, &s_root);
+        }
+        // larger ranges: a team of three warps each, one axis per warp; the
+        // halves queued for the next level
+        if (team < kTeams) {
+            for (uint32_t q = team; q < ntask; q += kTeams) {
+                const uint32_t r0 = S.task[cur][2 * q], r1 = S.task[cur][2 * q + 1];
+                const uint32_t s = r0 & 0xFFFFu, e = r0 >> 16, parent = r1 & 0xFFFFu, slot = r1 >> 16;
+                if (e - s <= kSweepSerial) continue;
+                uint32_t rb[6];
+                const Split mine = sweep_axis(S, axw, s, e, rb);
+                if (lane == 0) {
+                    s_split[team][axw] = mine;
+                    if (axw == 0)
+                        for (int a = 0; a < 6; ++a) s_box[team][a] = rb[a];
+                }
+                team_sync(team);
+                Split best = s_split[team][0];
+                for (int a = 1; a < 3; ++a)
+                    if (better(s_split[team][a], best)) best = s_split[team][a];
+                uint32_t bax = best.ax, k = best.k;
+                if (bax == 3u) { bax = 0u; k = s; }   // no cost below FLT_MAX (not for finite boxes)
+                if (axw == bax)
+                    for (uint32_t i = s + lane; i < e; i += 32) S.left[S.list[bax][i]] = i <= k ? 1u : 0u;
+                team_sync(team);
+                if (axw != bax) partition_warp(S, axw, s, e, k + 1 - s);
+                team_sync(team);
+                const uint32_t id = n + 1 + k;
+                if (axw == 0 && lane == 0) {
+                    uint32_t box[6];
+                    for (int a = 0; a < 6; ++a) box[a] = s_box[team][a];
+                    store_sweep_node(nodes, id, box);
+                    // a half of one instance is a leaf: its id goes in now
+                    if (k == s) link_child(nodes, id, 0u, 1u + S.list[0][s]);
+                    if (k + 2 == e) link_child(nodes, id, 1u, 1u + S.list[0][e - 1]);
+                    if (slot == 2u) s_root = id;
+                    else link_child(nodes, parent, slot, id);
+                    if (k > s) {
+                        const uint32_t p = atomicAdd(&s_count[cur ^ 1], 1u);
+                        S.task[cur ^ 1][2 * p] = s | ((k + 1) << 16);
+                        S.task[cur ^ 1][2 * p + 1] = id | (0u << 16);
+                    }
+                    if (k + 2 < e) {
+                        const uint32_t p = atomicAdd(&s_count[cur ^ 1], 1u);
+                        S.task[cur ^ 1][2 * p] = (k + 1) | (e << 16);
+                        S.task[cur ^ 1][2 * p + 1] = id | (1u << 16);
+                    }
+                }
+                team_sync(team);   // the team's shared slots free for its next range
+            }
+        }
+        __syncthreads();
+        if (t == 0) s_count[cur] = 0u;
+        cur ^= 1;
+        __syncthreads();
+    }
+    if (t == 0 && n > 0) {
+        nodes[0] = nodes[2 * s_root];
+        nodes[1] = nodes[2 * s_root + 1];
+    }
+}
+
 // instance_bounds 1: one block per instance.  Each frontier box's world box
 // is its transformed centre +/- its half extents through |M| (the exact box of
 // the transformed box), widened by 2^-19 of the magnitudes of the terms summed
@@ -446,6 +830,7 @@ cudaError_t launch_instance_bounds(const float4* sinst, uint32_t rows, uint32_t 
 
 size_t tlas_scratch_words(uint32_t n, uint32_t metric) {
     if (metric == 2) return (n <= kPlocSmemMax) ? 8 : ploc_bytes(n, pow2_at_least(n ? n : 1)) / 4 + 8;
+    if (metric == 3) return (n <= kSweepSmemMax) ? 8 : sweep_words(n, pow2_at_least(n ? n : 1)) + 8;
     return 7ull * n + 1;
 }
 
@@ -463,6 +848,19 @@ cudaError_t launch_tlas_build(const float* aabbs, uint32_t n, float4* nodes, uin
             if (e != cudaSuccess) return e;
         }
         k_tlas_ploc<<<1, kPlocThreads, bytes, stream>>>(aabbs, n, nodes, scratch, P, smem);
+        return cudaGetLastError();
+    }
+    if (metric == 3) {
+        // the working set in shared memory up to kSweepSmemMax instances
+        // (152 KiB at 2048), else in the scratch
+        const uint32_t P = pow2_at_least(n);
+        const bool smem = n <= kSweepSmemMax;
+        const size_t bytes = smem ? 4 * sweep_words(n, P) : 0;
+        if (bytes > 48u * 1024u) {
+            cudaError_t e = cudaFuncSetAttribute(k_tlas_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e != cudaSuccess) return e;
+        }
+        k_tlas_sweep<<<1, kPlocThreads, bytes, stream>>>(aabbs, n, nodes, scratch, P, smem);
         return cudaGetLastError();
     }
     size_t smem = (n <= kSmemInstances) ? (size_t)n * 7u * 4u : 0u;
