@@ -447,7 +447,7 @@ def builders_leg(r, desc):
     t0 = time.perf_counter()
     ct = orc.tlas_build(inst, metric=0)
     out["cpu_tlas_reference_ms"] = round(1e3 * (time.perf_counter() - t0), 2)
-    for metric, name in ((0, "reference"), (2, "clustering")):
+    for metric, name in ((0, "reference"), (2, "clustering"), (3, "sah_sweep")):
         import wavefrontpathtracing_gb300 as wf
         with wf.Renderer(8, 8, tlas_metric=metric) as q:
             q.tlas_build(inst)                          # warm-up (module load, allocation)
