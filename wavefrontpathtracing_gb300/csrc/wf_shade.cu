@@ -34,9 +34,10 @@ unsigned grid_for(uint32_t n) {
 constexpr int kShadeBlock = WF_SHADE_BLOCK;
 
 // PLAIN: path tracing without the adjoint's buffers or a debug view, the
-// render loop's usual case; the other variant serves every case.
+// render loop's usual case; the other variant serves every case, at 2
+// resident blocks (128 registers at most; left free it took 137, one block).
 template <bool PLAIN>
-__global__ void __launch_bounds__(kShadeBlock, PLAIN ? WF_SHADE_MIN_BLOCKS : 1)
+__global__ void __launch_bounds__(kShadeBlock, PLAIN ? WF_SHADE_MIN_BLOCKS : 2)
     k_shade(ShadeRefs SH, RenderBuffers B, WaveParams W, uint32_t depth, AdjointRefs A_in) {
     const AdjointRefs A = PLAIN ? AdjointRefs{} : A_in;
     if (PLAIN) B.ps_Lc = nullptr;
