@@ -183,6 +183,28 @@ def test_tlas_ploc_matches_oracle(orc, n, metric):
         assert np.array_equal(r.tlas_build(inst), orc.tlas_build(inst, metric=metric)), n
 
 
+@pytest.mark.parametrize("metric", [2, 3])
+def test_tlas_builds_with_signed_zeros_and_flat_boxes(orc, metric):
+    """Boxes touching the origin with -0 and +0 bounds, flat (zero-extent)
+    boxes and repeated centres: the GPU builds equal the oracle's bit for bit
+    (the sweep's unions order -0 below +0, so their bits cannot depend on how
+    a warp groups them)."""
+    rng = np.random.default_rng(31)
+    n = 96
+    inst = np.zeros(n, dtype=bvh_instance_dtype)
+    lo = rng.uniform(-2.0, 2.0, (n, 3)).astype(np.float32)
+    hi = (lo + rng.uniform(0.0, 1.0, (n, 3))).astype(np.float32)
+    lo[:24] = np.float32(-0.0)
+    hi[:12] = np.abs(hi[:12]) + np.float32(0.5)   # from -0 to a positive corner
+    hi[12:24] = np.float32(0.0)            # flat at the origin, min -0, max +0
+    hi[24:36] = lo[24:36]                  # flat boxes
+    lo[36:48] = lo[48:60]                  # repeated boxes
+    hi[36:48] = hi[48:60]
+    inst["aabb_min"], inst["aabb_max"] = lo, hi
+    with Renderer(8, 8, tlas_metric=metric) as r:
+        assert np.array_equal(r.tlas_build(inst), orc.tlas_build(inst, metric=metric))
+
+
 def test_tlas_sweep_all_centres_equal(orc):
     """The sweep over 300 identical boxes: every split ties, the tree is a
     300-deep chain (300 levels of the build), equal to the oracle's."""
