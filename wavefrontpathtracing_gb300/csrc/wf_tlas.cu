@@ -380,13 +380,15 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restr
 // ---------------------------------------------------------------------------
 // metric 3: top-down full-sweep SAH, one block of 1024 threads.  Three lists
 // of the instances by box centre along x, y, z (one bitonic network over the
-// three axes' (sortable centre bits, index) keys); then level by level: a
-// range [s, e) of more than 8 instances goes to a team of three warps, one
+// three axes' (sortable centre bits, index) keys, its strides below 32 in
+// warp shuffles); then level by level: on a level of at most two ranges the
+// whole block sweeps each range in turn (sweep_block), else a range [s, e)
+// of more than 4 instances goes to a team of three warps, one
 // per axis (warp scans of the prefix union boxes, their half areas kept per
 // position, then of the suffix boxes, each boundary's cost A(left) * |left|
 // + A(right) * |right| in float), which takes the cheapest boundary (ties to
 // the lower axis, then the lower position), partitions the other two lists
-// stably and queues the two halves for the next level; a range of up to 8
+// stably and queues the two halves for the next level; a range of up to 4
 // goes to one thread, which builds its whole subtree the same way.  The interior node of a range split after position k is node
 // n + 1 + k (every boundary is split once), so node numbers do not depend on
 // which warp takes which range; a child sets its half of the parent's
@@ -424,7 +426,8 @@ struct SweepScratch {
     uint32_t* tmp;        // n
     uint32_t* left;       // n: 1 = the instance is in its range's left part
     float* area[3];       // per axis and position: the half area of the prefix union box
-    unsigned long long* key;   // 3 P sort keys (the same words as area, before the sweep)
+    float* sarea[3];      // per axis and position: the half area of the suffix union box (block mode)
+    unsigned long long* key;   // 3 P sort keys (the same words as area and sarea, before the sweep)
     uint32_t* box;        // 6 per instance
     uint32_t* task[2];    // per level: (s | e << 16, parent | slot << 16), n / 2 + 1 each
 };
@@ -436,7 +439,10 @@ __host__ __device__ inline size_t sweep_words(uint32_t n, uint32_t P) {
 __device__ inline SweepScratch sweep_carve(uint32_t* base, uint32_t n, uint32_t P) {
     SweepScratch S;
     S.key = reinterpret_cast<unsigned long long*>(base);   // first: 8-byte aligned
-    for (int a = 0; a < 3; ++a) S.area[a] = reinterpret_cast<float*>(base) + (size_t)a * n;
+    for (int a = 0; a < 3; ++a) {
+        S.area[a] = reinterpret_cast<float*>(base) + (size_t)a * n;
+        S.sarea[a] = reinterpret_cast<float*>(base) + (size_t)(3 + a) * n;   // 6 n <= 6 P words
+    }
     uint32_t* w = base + 6ull * P;
     S.list[0] = w; S.list[1] = w + n; S.list[2] = w + 2 * n;
     S.tmp = w + 3 * n;
@@ -636,6 +642,215 @@ __device__ __forceinline__ void team_sync(uint32_t team) {
     asm volatile("bar.sync %0, %1;" ::"r"(team + 1u), "r"(96) : "memory");
 }
 
+// Block mode, for the top levels where a few large ranges would leave most
+// teams idle: the whole block on one range [s, e) (e - s > kSweepSerial), ten
+// warps per axis, each on a contiguous chunk of the range.  Chunk union boxes
+// first; then each warp scans its chunk starting from the union of the chunks
+// before it (prefix areas) and after it (suffix areas); then every boundary's
+// cost, the cheapest over the block, and a stable partition of the other two
+// lists from per-chunk left counts.  Unions of sortable bits do not depend on
+// grouping, so the areas, the costs (the same float expression) and the split
+// equal the team's.  Called by every thread; returns k, the range's box in rb.
+constexpr uint32_t kAxisWarps = kPlocThreads / 96;   // 10: warps 30 and 31 only keep the barriers
+#ifndef WF_SWEEP_BLOCK_TASKS
+#define WF_SWEEP_BLOCK_TASKS 2
+#endif
+constexpr uint32_t kSweepBlockTasks = WF_SWEEP_BLOCK_TASKS;   // block mode on levels of at most this many ranges
+
+struct SweepBlockShared {
+    uint32_t tot[3][kAxisWarps][6];   // per axis and chunk: the chunk's union box
+    Split best[3 * kAxisWarps];       // per warp: its chunk's cheapest boundary
+    uint32_t cnt[3][kAxisWarps];      // per axis and chunk: instances in the left part
+};
+
+__device__ __forceinline__ void box_union(uint32_t* d, const uint32_t* b) {
+    for (int a = 0; a < 3; ++a) { d[a] = min(d[a], b[a]); d[3 + a] = max(d[3 + a], b[3 + a]); }
+}
+
+__device__ uint32_t sweep_block(const SweepScratch& S, SweepBlockShared& B, uint32_t s, uint32_t e, uint32_t* rb) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const unsigned FULL = 0xffffffffu;
+    const bool active = warp < 3 * kAxisWarps;
+    const uint32_t ax = active ? warp / kAxisWarps : 0u, ch = warp % kAxisWarps;
+    const uint32_t clen = (e - s + kAxisWarps - 1) / kAxisWarps;
+    const uint32_t c0 = min(e, s + ch * clen), c1 = min(e, c0 + clen);   // this warp's chunk [c0, c1)
+    const uint32_t* L = S.list[ax];
+    if (active) {
+        uint32_t v[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+        for (uint32_t i = c0 + lane; i < c1; i += 32) box_union(v, S.box + 6ull * L[i]);
+        for (int off = 16; off > 0; off >>= 1)
+            for (int a = 0; a < 6; ++a) {
+                const uint32_t o = __shfl_xor_sync(FULL, v[a], off);
+                v[a] = a < 3 ? min(o, v[a]) : max(o, v[a]);
+            }
+        if (lane == 0)
+            for (int a = 0; a < 6; ++a) B.tot[ax][ch][a] = v[a];
+    }
+    __syncthreads();
+    if (active) {
+        uint32_t pre[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+        uint32_t post[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+        for (uint32_t c = 0; c < kAxisWarps; ++c) {
+            if (c < ch) box_union(pre, B.tot[ax][c]);
+            if (c > ch) box_union(post, B.tot[ax][c]);
+        }
+        uint32_t cb[6];
+        for (int a = 0; a < 6; ++a) cb[a] = pre[a];
+        for (uint32_t c = c0; c < c1; c += 32) {
+            const uint32_t i = c + lane;
+            uint32_t v[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+            if (i < c1) {
+                const uint32_t* b = S.box + 6ull * L[i];
+                for (int a = 0; a < 6; ++a) v[a] = b[a];
+            }
+            warp_scan_box(v, lane);
+            box_union(v, cb);
+            if (i < c1) S.area[ax][i] = half_area_sb(v);
+            const uint32_t last = min(31u, c1 - 1 - c);
+            for (int a = 0; a < 6; ++a) cb[a] = __shfl_sync(FULL, v[a], last);
+        }
+        for (int a = 0; a < 6; ++a) cb[a] = post[a];
+        for (uint32_t c = 0; c < c1 - c0; c += 32) {
+            const uint32_t j = c + lane;   // j-th position from the chunk's end
+            const bool valid = j < c1 - c0;
+            const uint32_t i = c1 - 1 - j;
+            uint32_t v[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+            if (valid) {
+                const uint32_t* b = S.box + 6ull * L[i];
+                for (int a = 0; a < 6; ++a) v[a] = b[a];
+            }
+            warp_scan_box(v, lane);
+            box_union(v, cb);
+            if (valid) S.sarea[ax][i] = half_area_sb(v);
+            const uint32_t last = min(31u, c1 - c0 - 1 - c);
+            for (int a = 0; a < 6; ++a) cb[a] = __shfl_sync(FULL, v[a], last);
+        }
+    }
+    __syncthreads();
+    if (active) {
+        // boundary k (after position k) pairs the prefix at k with the suffix at k + 1
+        Split best{FLT_MAX, 3u, 0u};
+        for (uint32_t k = c0 + lane; k < c1; k += 32) {
+            if (k + 1 >= e) continue;
+            const float cost = S.area[ax][k] * (float)(k - s + 1) + S.sarea[ax][k + 1] * (float)(e - 1 - k);
+            const Split cand{cost, ax, k};
+            if (cost < FLT_MAX && better(cand, best)) best = cand;
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            const Split o{__shfl_xor_sync(FULL, best.cost, off), __shfl_xor_sync(FULL, best.ax, off),
+                          __shfl_xor_sync(FULL, best.k, off)};
+            if (better(o, best)) best = o;
+        }
+        if (lane == 0) B.best[warp] = best;
+    }
+    __syncthreads();
+    // every candidate's cost is below FLT_MAX, so better() orders them totally
+    // and the reduction's order does not matter
+    Split best = B.best[0];
+    for (uint32_t w = 1; w < 3 * kAxisWarps; ++w)
+        if (better(B.best[w], best)) best = B.best[w];
+    uint32_t bax = best.ax, k = best.k;
+    if (bax == 3u) { bax = 0u; k = s; }   // no cost below FLT_MAX (not for finite boxes)
+    for (int a = 0; a < 6; ++a) rb[a] = a < 3 ? kSbEmptyMin : kSbEmptyMax;
+    for (uint32_t c = 0; c < kAxisWarps; ++c) box_union(rb, B.tot[0][c]);
+    if (active && ax == bax)
+        for (uint32_t i = c0 + lane; i < c1; i += 32) S.left[L[i]] = i <= k ? 1u : 0u;
+    __syncthreads();
+    const bool part = active && ax != bax;
+    if (part) {
+        uint32_t nl = 0;
+        for (uint32_t c = c0; c < c1; c += 32) {
+            const uint32_t i = c + lane;
+            nl += __popc(__ballot_sync(FULL, i < c1 && S.left[L[i]] != 0u));
+        }
+        if (lane == 0) B.cnt[ax][ch] = nl;
+    }
+    __syncthreads();
+    // the stable partition goes through the axis's prefix-area words (free now)
+    uint32_t* T = reinterpret_cast<uint32_t*>(S.area[ax]);
+    if (part) {
+        uint32_t nl = 0;
+        for (uint32_t c = 0; c < ch; ++c) nl += B.cnt[ax][c];
+        uint32_t nr = (c0 - s) - nl;
+        const uint32_t nleft = k + 1 - s;
+        for (uint32_t c = c0; c < c1; c += 32) {
+            const uint32_t i = c + lane;
+            const bool valid = i < c1;
+            const uint32_t id = valid ? L[i] : 0u;
+            const bool isl = valid && S.left[id] != 0u;
+            const unsigned ml = __ballot_sync(FULL, isl), mr = __ballot_sync(FULL, valid && !isl);
+            const unsigned below = (1u << lane) - 1u;
+            if (isl) T[s + nl + __popc(ml & below)] = id;
+            else if (valid) T[s + nleft + nr + __popc(mr & below)] = id;
+            nl += __popc(ml);
+            nr += __popc(mr);
+        }
+    }
+    __syncthreads();
+    if (part)
+        for (uint32_t i = c0 + lane; i < c1; i += 32) S.list[ax][i] = T[i];
+    __syncthreads();
+    return k;
+}
+
+// A compare-exchange of the bitonic network between lanes lane and lane ^ st
+// of a warp holding keys i (this lane's position in its axis) for stage
+// (size, st): an ascending pair (bit `size` of i clear) leaves the smaller key
+// at the lower position.
+__device__ __forceinline__ unsigned long long cx_lanes(unsigned long long x, uint32_t i, uint32_t size, uint32_t st,
+                                                       uint32_t lane) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, st);
+    const bool up = (i & size) == 0, low = (lane & st) == 0;
+    return (low == up) ? min(x, y) : max(x, y);
+}
+
+// Every window of 32 consecutive keys (P >= 32, so a window lies within one
+// axis's keys), one warp each: ALL = the stages of sizes 2-32, else the
+// strides 16-1 of stage `size`.
+template <bool ALL>
+__device__ void sort_windows(unsigned long long* key, uint32_t P, uint32_t size) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (uint32_t w = warp; w < 3 * (P >> 5); w += kPlocThreads / 32) {
+        const uint32_t q = 32 * w + lane, i = q & (P - 1);
+        unsigned long long x = key[q];
+        if (ALL) {
+#pragma unroll
+            for (uint32_t sz = 2; sz <= 32; sz <<= 1)
+#pragma unroll
+                for (uint32_t st = sz >> 1; st > 0; st >>= 1) x = cx_lanes(x, i, sz, st, lane);
+        } else {
+#pragma unroll
+            for (uint32_t st = 16; st > 0; st >>= 1) x = cx_lanes(x, i, size, st, lane);
+        }
+        key[q] = x;
+    }
+}
+
+// One thread, once range [s, e) is split after k and its lists partitioned:
+// the interior node n + 1 + k with the range's box, its single-instance
+// halves linked as leaves, the node linked into its parent (slot 2: the
+// root), and the larger halves queued for the next level.
+__device__ void emit_split(const SweepScratch& S, float4* nodes, uint32_t n, uint32_t s, uint32_t e, uint32_t k,
+                           uint32_t parent, uint32_t slot, const uint32_t* rb, uint32_t* next_count,
+                           uint32_t* next_task, uint32_t* root) {
+    const uint32_t id = n + 1 + k;
+    store_sweep_node(nodes, id, rb);
+    if (k == s) link_child(nodes, id, 0u, 1u + S.list[0][s]);
+    if (k + 2 == e) link_child(nodes, id, 1u, 1u + S.list[0][e - 1]);
+    if (slot == 2u) *root = id;
+    else link_child(nodes, parent, slot, id);
+    if (k > s) {
+        const uint32_t p = atomicAdd(next_count, 1u);
+        next_task[2 * p] = s | ((k + 1) << 16);
+        next_task[2 * p + 1] = id | (0u << 16);
+    }
+    if (k + 2 < e) {
+        const uint32_t p = atomicAdd(next_count, 1u);
+        next_task[2 * p] = (k + 1) | (e << 16);
+        next_task[2 * p + 1] = id | (1u << 16);
+    }
+}
+
 __global__ void __launch_bounds__(kPlocThreads) k_tlas_sweep(const float* __restrict__ aabbs, uint32_t n,
                                                              float4* nodes, uint32_t* scratch, uint32_t P,
                                                              bool smem) {
@@ -644,6 +859,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_sweep(const float* __rest
     __shared__ uint32_t s_count[2], s_root;
     __shared__ Split s_split[kTeams][3];
     __shared__ uint32_t s_box[kTeams][6];
+    __shared__ SweepBlockShared s_blk;
     const SweepScratch S = sweep_carve(smem ? reinterpret_cast<uint32_t*>(s_dyn) : scratch, n, P);
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const uint32_t team = warp / 3u, axw = warp % 3u;
@@ -666,19 +882,33 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_sweep(const float* __rest
         }
     }
     __syncthreads();
-    for (uint32_t size = 2; size <= P; size <<= 1)
-        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-            for (uint32_t q = t; q < 3 * P; q += kPlocThreads) {
-                const uint32_t i = q & (P - 1), j = i ^ stride;
-                if (j > i) {
-                    const uint32_t o = q - i;
-                    const unsigned long long x = key[o + i], y = key[o + j];
-                    const bool up = (i & size) == 0;
-                    if (up ? (x > y) : (x < y)) { key[o + i] = y; key[o + j] = x; }
-                }
+    // a bitonic network: strides of 32 and more as pairs in shared memory
+    // between barriers; the strides below 32 (and sizes 2-32 whole) in warp
+    // windows of 32 consecutive keys, through shuffles (P >= 32; a smaller P
+    // takes every stride as pairs)
+    const uint32_t G = P >= 32u ? 32u : 1u;
+    if (G == 32u) {
+        sort_windows<true>(key, P, 0u);
+        __syncthreads();
+    }
+    for (uint32_t size = 2 * G; size <= P; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride >= G; stride >>= 1) {
+            const uint32_t lgs = 31u - __clz(stride);
+            for (uint32_t p = t; p < 3 * (P >> 1); p += kPlocThreads) {
+                const uint32_t ax = p >> (lgP - 1), pi = p & ((P >> 1) - 1);
+                const uint32_t i = ((pi >> lgs) << (lgs + 1)) | (pi & (stride - 1)), j = i | stride;
+                const uint32_t o = ax << lgP;
+                const unsigned long long x = key[o + i], y = key[o + j];
+                const bool up = (i & size) == 0;
+                if (up ? (x > y) : (x < y)) { key[o + i] = y; key[o + j] = x; }
             }
             __syncthreads();
         }
+        if (G == 32u) {
+            sort_windows<false>(key, P, size);
+            __syncthreads();
+        }
+    }
     // (the keys' words become the prefix areas after the next barrier)
     for (uint32_t q = t; q < 3 * P; q += kPlocThreads) {
         const uint32_t ax = q >> lgP, i = q & (P - 1);
@@ -701,9 +931,21 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_sweep(const float* __rest
             const uint32_t s = r0 & 0xFFFFu, e = r0 >> 16;
             if (e - s <= kSweepSerial) sweep_subtree(S, nodes, n, s, e, r1 & 0xFFFFu, r1 >> 16, &s_root);
         }
-        // larger ranges: a team of three warps each, one axis per warp; the
-        // halves queued for the next level
-        if (team < kTeams) {
+        if (ntask <= kSweepBlockTasks) {
+            // a level of few ranges: the whole block on each larger range in turn
+            for (uint32_t q = 0; q < ntask; ++q) {
+                const uint32_t r0 = S.task[cur][2 * q], r1 = S.task[cur][2 * q + 1];
+                const uint32_t s = r0 & 0xFFFFu, e = r0 >> 16;
+                if (e - s <= kSweepSerial) continue;
+                uint32_t rb[6];
+                const uint32_t k = sweep_block(S, s_blk, s, e, rb);
+                if (t == 0)
+                    emit_split(S, nodes, n, s, e, k, r1 & 0xFFFFu, r1 >> 16, rb, &s_count[cur ^ 1], S.task[cur ^ 1],
+                               &s_root);
+            }
+        } else if (team < kTeams) {
+            // larger ranges: a team of three warps each, one axis per warp; the
+            // halves queued for the next level
             for (uint32_t q = team; q < ntask; q += kTeams) {
                 const uint32_t r0 = S.task[cur][2 * q], r1 = S.task[cur][2 * q + 1];
                 const uint32_t s = r0 & 0xFFFFu, e = r0 >> 16, parent = r1 & 0xFFFFu, slot = r1 >> 16;
@@ -726,26 +968,10 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_sweep(const float* __rest
                 team_sync(team);
                 if (axw != bax) partition_warp(S, axw, s, e, k + 1 - s);
                 team_sync(team);
-                const uint32_t id = n + 1 + k;
                 if (axw == 0 && lane == 0) {
                     uint32_t box[6];
                     for (int a = 0; a < 6; ++a) box[a] = s_box[team][a];
-                    store_sweep_node(nodes, id, box);
-                    // a half of one instance is a leaf: its id goes in now
-                    if (k == s) link_child(nodes, id, 0u, 1u + S.list[0][s]);
-                    if (k + 2 == e) link_child(nodes, id, 1u, 1u + S.list[0][e - 1]);
-                    if (slot == 2u) s_root = id;
-                    else link_child(nodes, parent, slot, id);
-                    if (k > s) {
-                        const uint32_t p = atomicAdd(&s_count[cur ^ 1], 1u);
-                        S.task[cur ^ 1][2 * p] = s | ((k + 1) << 16);
-                        S.task[cur ^ 1][2 * p + 1] = id | (0u << 16);
-                    }
-                    if (k + 2 < e) {
-                        const uint32_t p = atomicAdd(&s_count[cur ^ 1], 1u);
-                        S.task[cur ^ 1][2 * p] = (k + 1) | (e << 16);
-                        S.task[cur ^ 1][2 * p + 1] = id | (1u << 16);
-                    }
+                    emit_split(S, nodes, n, s, e, k, parent, slot, box, &s_count[cur ^ 1], S.task[cur ^ 1], &s_root);
                 }
                 team_sync(team);   // the team's shared slots free for its next range
             }
