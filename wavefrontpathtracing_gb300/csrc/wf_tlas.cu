@@ -383,7 +383,8 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restr
 // three axes' (sortable centre bits, index) keys, its strides below 32 in
 // warp shuffles); then level by level: on a level of at most two ranges the
 // whole block sweeps each range in turn (sweep_block), else a range [s, e)
-// of more than 4 instances goes to a team of three warps, one
+// of 5 to 10 instances goes to one warp (sweep_warp_small) and a larger one
+// to a team of three warps, one
 // per axis (warp scans of the prefix union boxes, their half areas kept per
 // position, then of the suffix boxes, each boundary's cost A(left) * |left|
 // + A(right) * |right| in float), which takes the cheapest boundary (ties to
@@ -396,14 +397,6 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restr
 __device__ __forceinline__ uint32_t sortable_bits(float x) {
     const uint32_t u = __float_as_uint(x);
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-// min / max in sortable-bits order (-0 below +0): associative, so a union
-// box's bits do not depend on how a scan groups it
-__device__ __forceinline__ float smin(float x, float y) { return sortable_bits(y) < sortable_bits(x) ? y : x; }
-__device__ __forceinline__ float smax(float x, float y) { return sortable_bits(x) < sortable_bits(y) ? y : x; }
-__device__ __forceinline__ float half_area3(const float* mn, const float* mx) {
-    const float ex = mx[0] - mn[0], ey = mx[1] - mn[1], ez = mx[2] - mn[2];
-    return ex * ey + ey * ez + ez * ex;
 }
 
 constexpr uint32_t kSweepSmemMax = 2048;
@@ -793,6 +786,86 @@ __device__ uint32_t sweep_block(const SweepScratch& S, SweepBlockShared& B, uint
     return k;
 }
 
+// Warp mode, for ranges of kSweepSerial + 1 to kSweepWarpMax instances: one
+// warp, the three axes side by side in segments of kSeg lanes (lane a kSeg + j
+// holds list a's position s + j in the prefix scan and e - 1 - j in the
+// suffix scan); each boundary's cost from its own prefix area and a shuffled
+// suffix area, the cheapest over the warp, a stable partition of the other
+// two lists by ballots within their segments, and the node emitted.  The
+// same areas, costs and split as the team's.
+constexpr uint32_t kSeg = 10;
+#ifndef WF_SWEEP_WARP_MAX
+#define WF_SWEEP_WARP_MAX 10
+#endif
+constexpr uint32_t kSweepWarpMax = WF_SWEEP_WARP_MAX;
+static_assert(kSweepWarpMax <= kSeg, "a warp-mode range fits one segment");
+
+__device__ __forceinline__ void seg_scan_box(uint32_t* v, uint32_t j) {
+    for (uint32_t off = 1; off < kSeg; off <<= 1)
+        for (int a = 0; a < 6; ++a) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, v[a], off);
+            if (j >= off) v[a] = a < 3 ? min(o, v[a]) : max(o, v[a]);
+        }
+}
+
+__device__ void emit_split(const SweepScratch& S, float4* nodes, uint32_t n, uint32_t s, uint32_t e, uint32_t k,
+                           uint32_t parent, uint32_t slot, const uint32_t* rb, uint32_t* next_count,
+                           uint32_t* next_task, uint32_t* root);
+
+__device__ void sweep_warp_small(const SweepScratch& S, float4* nodes, uint32_t n, uint32_t s, uint32_t e,
+                                 uint32_t parent, uint32_t slot, uint32_t* next_count, uint32_t* next_task,
+                                 uint32_t* root) {
+    const unsigned FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t a = lane / kSeg, j = lane - a * kSeg, m = e - s;
+    const bool in = a < 3u && j < m;
+    const uint32_t id = in ? S.list[a][s + j] : 0u;
+    uint32_t v[6] = {kSbEmptyMin, kSbEmptyMin, kSbEmptyMin, kSbEmptyMax, kSbEmptyMax, kSbEmptyMax};
+    if (in)
+        for (int c = 0; c < 6; ++c) v[c] = S.box[6ull * id + c];
+    seg_scan_box(v, j);
+    const float pa = half_area_sb(v);          // prefix area at s + j
+    uint32_t rb[6];                            // the range's box: list 0's last prefix
+    for (int c = 0; c < 6; ++c) rb[c] = __shfl_sync(FULL, v[c], m - 1);
+    for (int c = 0; c < 6; ++c) v[c] = c < 3 ? kSbEmptyMin : kSbEmptyMax;
+    if (in) {
+        const uint32_t* b = S.box + 6ull * S.list[a][e - 1 - j];
+        for (int c = 0; c < 6; ++c) v[c] = b[c];
+    }
+    seg_scan_box(v, j);
+    const float sa = half_area_sb(v);          // suffix area at e - 1 - j
+    // boundary k = s + j pairs the prefix at k with the suffix at k + 1,
+    // held by lane a kSeg + (m - 2 - j)
+    const bool cand_ok = in && j + 1 < m;
+    const float sa1 = __shfl_sync(FULL, sa, cand_ok ? a * kSeg + (m - 2 - j) : lane);
+    Split best{FLT_MAX, 3u, 0u};
+    if (cand_ok) {
+        const uint32_t k = s + j;
+        const float cost = pa * (float)(k - s + 1) + sa1 * (float)(e - 1 - k);
+        const Split cand{cost, a, k};
+        if (cost < FLT_MAX && better(cand, best)) best = cand;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const Split o{__shfl_xor_sync(FULL, best.cost, off), __shfl_xor_sync(FULL, best.ax, off),
+                      __shfl_xor_sync(FULL, best.k, off)};
+        if (better(o, best)) best = o;
+    }
+    uint32_t bax = best.ax, k = best.k;
+    if (bax == 3u) { bax = 0u; k = s; }   // no cost below FLT_MAX (not for finite boxes)
+    if (in && a == bax) S.left[id] = (s + j <= k) ? 1u : 0u;
+    __syncwarp();
+    const bool part = in && a != bax;
+    const bool isl = part && S.left[id] != 0u;
+    const unsigned seg = a < 3u ? (((1u << m) - 1u) << (a * kSeg)) : 0u;
+    const unsigned ml = __ballot_sync(FULL, isl) & seg, mr = __ballot_sync(FULL, part && !isl) & seg;
+    const unsigned below = (1u << lane) - 1u;
+    __syncwarp();
+    if (part) S.list[a][isl ? s + __popc(ml & below) : s + (k + 1 - s) + __popc(mr & below)] = id;
+    __syncwarp();
+    if (lane == 0) emit_split(S, nodes, n, s, e, k, parent, slot, rb, next_count, next_task, root);
+    __syncwarp();
+}
+
 // A compare-exchange of the bitonic network between lanes lane and lane ^ st
 // of a warp holding keys i (this lane's position in its axis) for stage
 // (size, st): an ascending pair (bit `size` of i clear) leaves the smaller key
@@ -856,7 +929,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_sweep(const float* __rest
                                                              bool smem) {
     extern __shared__ unsigned long long s_dyn[];
     constexpr uint32_t kTeams = kPlocThreads / 96;   // three warps each
-    __shared__ uint32_t s_count[2], s_root;
+    __shared__ uint32_t s_count[2], s_root, s_next;
     __shared__ Split s_split[kTeams][3];
     __shared__ uint32_t s_box[kTeams][6];
     __shared__ SweepBlockShared s_blk;
@@ -917,6 +990,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_sweep(const float* __rest
     if (t == 0) {
         s_root = 1u;   // a single instance is its own root
         s_count[0] = n >= 2 ? 1u : 0u;
+        s_next = 0u;
         s_count[1] = 0u;
         S.task[0][0] = 0u | (n << 16);
         S.task[0][1] = 0u | (2u << 16);   // slot 2: the root
@@ -943,41 +1017,56 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_sweep(const float* __rest
                     emit_split(S, nodes, n, s, e, k, r1 & 0xFFFFu, r1 >> 16, rb, &s_count[cur ^ 1], S.task[cur ^ 1],
                                &s_root);
             }
-        } else if (team < kTeams) {
-            // larger ranges: a team of three warps each, one axis per warp; the
-            // halves queued for the next level
-            for (uint32_t q = team; q < ntask; q += kTeams) {
+        } else {
+            if (team < kTeams) {
+                // larger ranges: a team of three warps each, one axis per warp; the
+                // halves queued for the next level
+                for (uint32_t q = team; q < ntask; q += kTeams) {
+                    const uint32_t r0 = S.task[cur][2 * q], r1 = S.task[cur][2 * q + 1];
+                    const uint32_t s = r0 & 0xFFFFu, e = r0 >> 16, parent = r1 & 0xFFFFu, slot = r1 >> 16;
+                    if (e - s <= kSweepWarpMax) continue;
+                    uint32_t rb[6];
+                    const Split mine = sweep_axis(S, axw, s, e, rb);
+                    if (lane == 0) {
+                        s_split[team][axw] = mine;
+                        if (axw == 0)
+                            for (int a = 0; a < 6; ++a) s_box[team][a] = rb[a];
+                    }
+                    team_sync(team);
+                    Split best = s_split[team][0];
+                    for (int a = 1; a < 3; ++a)
+                        if (better(s_split[team][a], best)) best = s_split[team][a];
+                    uint32_t bax = best.ax, k = best.k;
+                    if (bax == 3u) { bax = 0u; k = s; }   // no cost below FLT_MAX (not for finite boxes)
+                    if (axw == bax)
+                        for (uint32_t i = s + lane; i < e; i += 32) S.left[S.list[bax][i]] = i <= k ? 1u : 0u;
+                    team_sync(team);
+                    if (axw != bax) partition_warp(S, axw, s, e, k + 1 - s);
+                    team_sync(team);
+                    if (axw == 0 && lane == 0) {
+                        uint32_t box[6];
+                        for (int a = 0; a < 6; ++a) box[a] = s_box[team][a];
+                        emit_split(S, nodes, n, s, e, k, parent, slot, box, &s_count[cur ^ 1], S.task[cur ^ 1], &s_root);
+                    }
+                    team_sync(team);   // the team's shared slots free for its next range
+                }
+            }
+            // ranges of kSweepSerial + 1 to kSweepWarpMax: one warp each, taken
+            // in turn by whichever warp is free
+            for (;;) {
+                uint32_t q = 0;
+                if (lane == 0) q = atomicAdd(&s_next, 1u);
+                q = __shfl_sync(0xffffffffu, q, 0);
+                if (q >= ntask) break;
                 const uint32_t r0 = S.task[cur][2 * q], r1 = S.task[cur][2 * q + 1];
-                const uint32_t s = r0 & 0xFFFFu, e = r0 >> 16, parent = r1 & 0xFFFFu, slot = r1 >> 16;
-                if (e - s <= kSweepSerial) continue;
-                uint32_t rb[6];
-                const Split mine = sweep_axis(S, axw, s, e, rb);
-                if (lane == 0) {
-                    s_split[team][axw] = mine;
-                    if (axw == 0)
-                        for (int a = 0; a < 6; ++a) s_box[team][a] = rb[a];
-                }
-                team_sync(team);
-                Split best = s_split[team][0];
-                for (int a = 1; a < 3; ++a)
-                    if (better(s_split[team][a], best)) best = s_split[team][a];
-                uint32_t bax = best.ax, k = best.k;
-                if (bax == 3u) { bax = 0u; k = s; }   // no cost below FLT_MAX (not for finite boxes)
-                if (axw == bax)
-                    for (uint32_t i = s + lane; i < e; i += 32) S.left[S.list[bax][i]] = i <= k ? 1u : 0u;
-                team_sync(team);
-                if (axw != bax) partition_warp(S, axw, s, e, k + 1 - s);
-                team_sync(team);
-                if (axw == 0 && lane == 0) {
-                    uint32_t box[6];
-                    for (int a = 0; a < 6; ++a) box[a] = s_box[team][a];
-                    emit_split(S, nodes, n, s, e, k, parent, slot, box, &s_count[cur ^ 1], S.task[cur ^ 1], &s_root);
-                }
-                team_sync(team);   // the team's shared slots free for its next range
+                const uint32_t s = r0 & 0xFFFFu, e = r0 >> 16;
+                if (e - s <= kSweepSerial || e - s > kSweepWarpMax) continue;
+                sweep_warp_small(S, nodes, n, s, e, r1 & 0xFFFFu, r1 >> 16, &s_count[cur ^ 1], S.task[cur ^ 1],
+                                 &s_root);
             }
         }
         __syncthreads();
-        if (t == 0) s_count[cur] = 0u;
+        if (t == 0) { s_count[cur] = 0u; s_next = 0u; }
         cur ^= 1;
         __syncthreads();
     }
