@@ -383,14 +383,14 @@ __global__ void __launch_bounds__(kPlocThreads) k_tlas_ploc(const float* __restr
 // three axes' (sortable centre bits, index) keys, its strides below 32 in
 // warp shuffles); then level by level: on a level of at most two ranges the
 // whole block sweeps each range in turn (sweep_block), else a range [s, e)
-// of 5 to 10 instances goes to one warp (sweep_warp_small) and a larger one
+// of 3 to 10 instances goes to one warp (sweep_warp_small) and a larger one
 // to a team of three warps, one
 // per axis (warp scans of the prefix union boxes, their half areas kept per
 // position, then of the suffix boxes, each boundary's cost A(left) * |left|
 // + A(right) * |right| in float), which takes the cheapest boundary (ties to
 // the lower axis, then the lower position), partitions the other two lists
-// stably and queues the two halves for the next level; a range of up to 4
-// goes to one thread, which builds its whole subtree the same way.  The interior node of a range split after position k is node
+// stably and queues the two halves for the next level; a range of 2 goes to
+// one thread, which builds its whole subtree the same way.  The interior node of a range split after position k is node
 // n + 1 + k (every boundary is split once), so node numbers do not depend on
 // which warp takes which range; a child sets its half of the parent's
 // left_right word.  Identical, node for node, to the oracle's tlas_sweep.
@@ -511,7 +511,7 @@ __device__ __forceinline__ void link_child(float4* nodes, uint32_t parent, uint3
 // One thread builds the whole subtree of a small range [s, e) (2 <= e - s
 // <= kSweepSerial) below parent / slot, depth-first.
 #ifndef WF_SWEEP_SERIAL
-#define WF_SWEEP_SERIAL 4
+#define WF_SWEEP_SERIAL 2
 #endif
 constexpr uint32_t kSweepSerial = WF_SWEEP_SERIAL;
 __device__ void sweep_subtree(const SweepScratch& S, float4* nodes, uint32_t n, uint32_t s0, uint32_t e0,
